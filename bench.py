@@ -1,0 +1,309 @@
+#!/usr/bin/env python3
+"""Benchmark of the steady LU-SGS iteration of RocketCombustor on GB300.
+
+One step = one lu_sgs_stage (TimeStep, reconstruction, flux_sourceterm,
+LU_SGS_steady with the Newton update) over the whole mesh, launched as one
+captured CUDA graph.  Default workload: the reacting viscous nozzle of about
+120k triangles (4 species, T-dependent cp, global H2/O2 reaction), plain FP64.
+
+  value   cell-iters/s = NE * K / (sum of device-timed steps), state resident in
+          HBM, L2 flushed (256 MB write) between timed steps;
+  e2e     the same metric through the C ABI with the state in pinned host
+          memory: each step copies PA, WA host->device, runs the stage, reads the
+          residual norms and copies PA, WA device->host;
+  roofline  the dominant subroutine timed live with CUDA events;
+  cpu_baseline  the FP64 CPU oracle on all host threads, bounded sample.
+
+--impl reference times the CPU restatement of the reference (the oracle) on
+the host cores on the same workload; the Fortran reference itself cannot be
+built (no Fortran compiler, MPI or LAPACK).
+Multi-GPU: replicas only (each rank runs its own copy of the case).
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import shutil
+import subprocess
+import sys
+import tempfile
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+import numpy as np  # noqa: E402
+
+# Algorithmic bytes per cell-iteration of each reference subroutine, FP64,
+# triangles (NF/NE ~ 1.5), V = NVar: the per-kernel table of the design notes.
+def algo_bytes_per_cell(V: int, nf_ne: float, viscous: bool, combustion: bool) -> dict:
+    b = {
+        "timestep": 8 * V + 16 + nf_ne * 32,
+        "reconstruction": (24 * V + 84) + (40 * V + 56 + nf_ne * 16),
+        "flux_sourceterm": (32 * V + 32 + nf_ne * 40) + ((40 * V + 32 + nf_ne * 40) if viscous else 0)
+        + ((24 * V + 8) if combustion else 0),
+        "lu_sgs_steady": 2 * (24 * V + 28 + nf_ne * 32) + (32 * V + 8),
+    }
+    b["stage"] = sum(b.values())
+    return b
+
+
+def read_peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        with open(p) as f:
+            d = json.load(f)
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+class ClockSampler:
+    """nvidia-smi clocks/throttle sampling during the timed region."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+         "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+         "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu: int):
+        self.gpu = gpu
+        self.proc = None
+        self.out = None
+
+    def __enter__(self):
+        if shutil.which("nvidia-smi"):
+            self.out = tempfile.NamedTemporaryFile("w+", suffix=".csv", delete=False)
+            self.proc = subprocess.Popen(["nvidia-smi", f"--id={self.gpu}", f"--query-gpu={self.Q}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=self.out, stderr=subprocess.DEVNULL)
+        return self
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self):
+        if not self.out:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.out.flush()
+        rows = []
+        with open(self.out.name) as f:
+            for line in f:
+                p = [x.strip() for x in line.split(",")]
+                if len(p) >= 9:
+                    rows.append(p)
+        os.unlink(self.out.name)
+        if not rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["no samples"]}
+        sm = [float(r[1]) for r in rows if r[1].replace(".", "").isdigit()]
+        mx = [float(r[2]) for r in rows if r[2].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[k] for r in rows for k in range(4) if r[5 + k].lower().startswith("active")})
+        return {"sm_mhz": float(np.median(sm)) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": reasons, "samples": len(rows)}
+
+
+def make_workload(name: str, tmp: str, **over):
+    from rocketcombustor_gb300 import cases
+    d = os.path.join(tmp, name)
+    cfg = cases.make_case(d, name, **over)
+    return d, cfg
+
+
+def cpu_baseline(case_dir: str, budget_s: float = 15.0, threads: int = 0):
+    """Oracle on the host cores, parallel mode, as many whole iterations as fit
+    in about `budget_s` seconds (at least 2)."""
+    import oracle
+    threads = threads or oracle.Oracle.max_threads()
+    o = oracle.Oracle(case_dir, threads=threads)
+    t0 = time.perf_counter()
+    o.run(1)
+    one = time.perf_counter() - t0
+    n = max(2, int(budget_s / max(one, 1e-6)))
+    t0 = time.perf_counter()
+    o.run(n)
+    dt = time.perf_counter() - t0
+    ne = o.NE
+    o.close()
+    return {"value": ne * n / dt, "unit": "cell-iters/s", "cores": threads, "kind": "port",
+            "sample": f"{n} whole LU-SGS iterations of the same case after 1 warm-up iteration ({dt:.1f} s)"}
+
+
+def run_reference(args, rank, world):
+    import oracle
+    if rank != 0:
+        return 0
+    with tempfile.TemporaryDirectory() as tmp:
+        d, cfg = make_workload(args.case, tmp, **({"order": args.order} if args.order else {}))
+        threads = oracle.Oracle.max_threads()
+        o = oracle.Oracle(d, threads=threads)
+        o.run(args.warmup)
+        t0 = time.perf_counter()
+        o.run(args.steps)
+        dt = time.perf_counter() - t0
+        v = o.NE * args.steps / dt
+        line = {"impl": "reference", "metric": "cell-iters/s", "value": v, "unit": "cell-iters/s",
+                "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+                "ms_per_step": 1e3 * dt / args.steps, "higher_is_better": True, "scaling": "weak",
+                "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+                "config": workload_config(cfg, o.NE, o.NF, "replicas" if world > 1 else "single"),
+                "cpu_baseline": {"value": v, "unit": "cell-iters/s", "cores": threads, "kind": "port",
+                                 "sample": f"{args.steps} whole iterations after {args.warmup} warm-up"},
+                "e2e": {"value": v, "unit": "cell-iters/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+        print(json.dumps(line), flush=True)
+    return 0
+
+
+def workload_config(cfg, ne, nf, par):
+    return {"workload": f"{cfg.name}: steady LU-SGS, nozzle {ne} triangles / {nf} faces, "
+                        f"{cfg.nsp} species, {'viscous' if cfg.viscous else 'inviscid'}, "
+                        f"{'reacting' if cfg.combustion else 'frozen'}, cell order {cfg.order}",
+            "cells": ne, "faces": nf, "species": cfg.nsp, "viscous": cfg.viscous, "combustion": cfg.combustion,
+            "cfl": cfg.cfl, "cell_order": cfg.order, "l2": "flushed between timed steps (256 MB write)",
+            "parallelism": par}
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=50)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--case", default="c2")
+    ap.add_argument("--order", default=None)
+    ap.add_argument("--precision", default="fp64", choices=["fp64", "mixed"])
+    ap.add_argument("--e2e-steps", type=int, default=10)
+    ap.add_argument("--cpu-budget", type=float, default=15.0)
+    ap.add_argument("--no-cpu", action="store_true")
+    args = ap.parse_args()
+    args.warmup = max(args.warmup, 3)
+
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("gloo")
+    if args.impl == "reference":
+        rc_ = run_reference(args, rank, world)
+        if dist:
+            dist.barrier()
+            dist.destroy_process_group()
+        return rc_
+
+    import torch
+    import rocketcombustor_gb300 as rc
+
+    torch.cuda.set_device(local)
+    stream = torch.cuda.Stream(device=local)
+    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=f"cuda:{local}")
+    prec = rc.RC_PREC_MIXED if args.precision == "mixed" else rc.RC_PREC_FP64
+    with tempfile.TemporaryDirectory() as tmp:
+        d, cfg = make_workload(args.case, tmp, **({"order": args.order} if args.order else {}))
+        case = rc.Case(d)
+        s = rc.Solver(case, precision=prec, device=local, stream=stream.cuda_stream)
+        NE, NF, V = case.NE, case.NF, case.NVar
+        with torch.cuda.stream(stream):
+            for it in range(args.warmup):
+                s.lu_sgs_stage(it + 1)
+            s.sync()
+            ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
+                  for _ in range(args.steps)]
+            if dist:
+                dist.barrier()
+            torch.cuda.synchronize()
+            l0 = s.stats()["kernel_launches"]
+            with ClockSampler(local) as clk:
+                for it in range(args.steps):
+                    flush.zero_()
+                    ev[it][0].record(stream)
+                    s.lu_sgs_stage(args.warmup + it + 1)
+                    ev[it][1].record(stream)
+                s.sync()
+                torch.cuda.synchronize()
+            launches = s.stats()["kernel_launches"] - l0
+            ms = [a.elapsed_time(b) for a, b in ev]
+            t_local = sum(ms) / 1e3
+            res, romax = s.residual()
+            # per-subroutine timing (same stream, events), L2 flushed before each
+            sub = {}
+            for name, fn in (("timestep", s.timestep), ("reconstruction", s.reconstruction),
+                             ("flux_sourceterm", s.flux_sourceterm), ("lu_sgs_steady", s.lu_sgs_steady)):
+                sub[name] = []
+            nrep = max(3, min(args.steps, 20))
+            for _ in range(nrep):
+                for name, fn in (("timestep", s.timestep), ("reconstruction", s.reconstruction),
+                                 ("flux_sourceterm", s.flux_sourceterm), ("lu_sgs_steady", s.lu_sgs_steady)):
+                    flush.zero_()
+                    a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+                    a.record(stream)
+                    fn()
+                    b.record(stream)
+                    sub[name].append((a, b))
+            s.sync()
+            torch.cuda.synchronize()
+            sub_ms = {k: float(np.mean([a.elapsed_time(b) for a, b in v])) for k, v in sub.items()}
+        # end-to-end through the C ABI with pinned host buffers
+        PA_h = torch.empty((NE, V), dtype=torch.float64, pin_memory=True).numpy()
+        WA_h = torch.empty((NE, V), dtype=torch.float64, pin_memory=True).numpy()
+        PA_h[:], WA_h[:] = s.get_state()
+        s.sync()
+        t0 = time.perf_counter()
+        for it in range(args.e2e_steps):
+            s.set_state(PA_h, WA_h)
+            s.lu_sgs_stage(it + 1)
+            s.residual()
+            s.get_state(PA_h, WA_h)
+        e2e_dt = time.perf_counter() - t0
+        stats = s.stats()
+        s.close()
+
+        t_max = t_local
+        if dist:
+            tt = torch.tensor([t_local], dtype=torch.float64)
+            dist.all_reduce(tt, op=dist.ReduceOp.MAX)
+            t_max = float(tt[0])
+        if rank != 0:
+            dist.barrier()
+            dist.destroy_process_group()
+            return 0
+        value = world * NE * args.steps / t_max
+        peak, peak_kind = read_peaks()
+        ab = algo_bytes_per_cell(V, NF / NE, cfg.viscous, cfg.combustion)
+        dom = max(sub_ms, key=sub_ms.get)
+        achieved = ab[dom] * NE / (sub_ms[dom] * 1e-3) / 1e9
+        line = {
+            "metric": "cell-iters/s", "value": value, "unit": "cell-iters/s", "n_gpus": world,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * t_max / args.steps,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "f64" if prec == rc.RC_PREC_FP64 else "f32+f64", "data": "synthetic",
+            "config": workload_config(cfg, NE, NF, f"replicas x{world}" if world > 1 else "single GPU"),
+            "e2e": {"value": NE * args.e2e_steps / e2e_dt, "unit": "cell-iters/s",
+                    "h2d_bytes_per_step": 2 * NE * V * 8, "d2h_bytes_per_step": 2 * NE * V * 8 + (V + 1) * 8},
+            "gpu_launches": int(launches),
+            "roofline": {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": peak, "unit": "GB/s",
+                         "frac": achieved / peak, "peak_source": peak_kind,
+                         "algorithmic_bytes_per_cell": ab[dom], "traffic": None},
+            "subroutine_ms": sub_ms,
+            "stage_algorithmic_gbs": ab["stage"] * NE / (1e-3 * 1e3 * t_max / args.steps) / 1e9,
+            "levels": {"fwd": stats["fwd_levels"], "bwd": stats["bwd_levels"]},
+            "residual": [float(x) for x in res], "romax": romax,
+        }
+        line["clocks"] = clk.summary()
+        if not args.no_cpu:
+            line["cpu_baseline"] = cpu_baseline(d, args.cpu_budget)
+        print(json.dumps(line), flush=True)
+    if dist:
+        dist.barrier()
+        dist.destroy_process_group()
+    return 0
+
+
+if __name__ == "__main__":
+    sys.exit(main())

@@ -1,0 +1,159 @@
+/*
+ * rc_gpu.h -- drop-in C ABI for the steady implicit iteration of RocketCombustor
+ * (harryzhou2000/RocketCombustor) on one GB300 GPU.
+ *
+ * The reference runs its hot path as argument-less Fortran subroutines acting
+ * on module globals (module mainvar, src/module.f90:2-107).  This ABI keeps
+ * those boundaries: the host owns the same arrays in the same Fortran layout
+ * (column-major, 1-based indices stored as int32), hands them over once in
+ * rc_init, and then calls one entry point per reference subroutine.  The state
+ * stays resident on the device between calls; rc_set_state/rc_get_state are the
+ * only host<->device copies of the solution.
+ *
+ * Every entry point returns 0 (RC_OK) or a bit mask of RC_ERR_* codes.  The
+ * reference stops the program on these conditions (calls `stop`/MPI_STOP);
+ * device-detected conditions are latched in a device error word and reported
+ * by the next call that synchronises with the device (rc_residual,
+ * rc_get_state, rc_get_array, rc_sync).  rc_last_error() gives a message.
+ *
+ * Threading: one host thread per context; each context owns one CUDA stream.
+ */
+#ifndef RC_GPU_H
+#define RC_GPU_H
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define RC_OK 0
+#define RC_ERR_THERMO_T 1      /* ComputeGasParameter/compute_enthalpy T out of range (thermo_property.f90:174-177,214-217) */
+#define RC_ERR_TRANSPORT_T 2   /* compute_transport_property T out of range (transport_property.f90:101-105) */
+#define RC_ERR_NEG_TIMESTEP 4  /* rho, p or T < 0 in TimeStep (TimeStep.f90:66-70) */
+#define RC_ERR_NEG_FACE 8      /* rho or p < 0 at a face in flux_lax (flux_lax.f90:239-242) */
+#define RC_ERR_NAN 16          /* NaN in WA(1,1) after a stage (Time_LUSGS_steady.f90:94-97) */
+#define RC_ERR_BCTYPE 32       /* unknown boundary code (flux_lax.f90:232-235, update_flow_variables.f90:364-367) */
+#define RC_ERR_ARG 1024        /* invalid argument or unsupported configuration */
+#define RC_ERR_CUDA 2048       /* CUDA runtime failure */
+
+#define RC_PREC_FP64 0         /* plain FP64 path, operation order of the reference */
+#define RC_PREC_MIXED 1        /* FP32 reconstruction/limiter/flux with compensated accumulation;
+                                  FP64 diagonal, chemistry, Newton and norms */
+
+typedef struct rc_ctx rc_ctx;
+
+/*
+ * Mesh, geometry and stencils after ReadMesh + compute_reconstruction_matrix,
+ * exactly the module arrays of mainvar for one partition (NE_Vir == NE,
+ * NF_vir == NF).  Shapes are Fortran shapes; index arrays hold 1-based ids.
+ */
+typedef struct rc_mesh {
+  int NE, NF, NNT, MaxNei, Nghostcell;
+  const int* KFace;            /* KFace(NE)                     module.f90:31 */
+  const int* Neighbor;         /* Neighbor(2,NF), <0 = -BC code module.f90:28 */
+  const int* FNode;            /* FNode(2,NF)                   module.f90:28 */
+  const int* FProperty;        /* FProperty(NF)                 module.f90:28 */
+  const int* NeighF;           /* NeighF(4,NE), ascending face  module.f90:31 */
+  const int* Neigh;            /* Neigh(NE)                     module.f90:31 */
+  const int* NeighC;           /* NeighC(0:MaxNei,NE)           module.f90:31 */
+  const int* Ghostcell;        /* Ghostcell(MaxNei,NE)          module.f90:46 */
+  const int* Num_ghostcell;    /* Num_ghostcell(NE)             module.f90:46 */
+  const int* Hostcell;         /* Hostcell(Nghostcell)          module.f90:46 */
+  const int* BCtype_Ghostcell; /* BCtype_Ghostcell(Nghostcell)  module.f90:46 */
+  const double* COOR;          /* COOR(2,NNT)                   module.f90:38 */
+  const double* VECX;          /* VECX(2,NF)                    module.f90:40 */
+  const double* SideOfs;       /* SideOfs(2,NF)                 module.f90:40 */
+  const double* VOL;           /* VOL(NE)                       module.f90:42 */
+  const double* CELLXY;        /* CELLXY(2,NE)                  module.f90:42 */
+  const double* reflen;        /* reflen(2,NE)                  module.f90:42 */
+  const double* wdis;          /* wdis(MaxNei,NE)               module.f90:51 */
+  const double* AMLS;          /* AMLS(2,MaxNei,NE)             module.f90:67 */
+  const double* Coor_Ghostnode;/* Coor_Ghostnode(2,4,Nghostcell) module.f90:47 */
+  double total_volume;         /* total_volume                  module.f90:36 */
+} rc_mesh;
+
+/*
+ * Species, thermo, transport, diffusion, kinetics and inlet data as held by the
+ * modules of src/combustion_modeling after start-up and initialization (the
+ * inlet mass flows already divided by the inlet widths, initialization.f90:19-23).
+ */
+typedef struct rc_thermo {
+  int Nsp;                              /* species.f90:7 */
+  double Rconstant;                     /* species.f90:8 */
+  const double* mole_weight;            /* (Nsp) */
+  const double* R_species;              /* (Nsp) */
+  int order_of_cp_polynomial;           /* thermo_property.f90:86, must be 7 */
+  double thermo_lowest_tem, thermo_critical_tem, thermo_highest_tem;
+  const double* low_coef_Cp_species;    /* (order,Nsp) */
+  const double* high_coef_Cp_species;   /* (order,Nsp) */
+  const double* low_enthalpy_b1;        /* (Nsp) */
+  const double* high_enthalpy_b1;       /* (Nsp) */
+  double transport_lowest_tem, transport_critical_tem, transport_highest_tem;
+  const double* mu_K[16];               /* low_mu_A..D, high_mu_A..D, low_K_A..D, high_K_A..D, each (Nsp) */
+  const double* collision_diameter;     /* (Nsp) diffusion_velocity.f90:132 */
+  const double* LJ_energy;              /* (Nsp) */
+  int code_chemical_model;              /* chemical_kinetics.f90:6 */
+  const double* coef_f_react;           /* (Nsp) of reaction 1 */
+  const double* coef_r_react;           /* (Nsp) of reaction 1 */
+  double Af_react, E_react;             /* reaction 1 */
+  const double* oxidizer_mass_fraction; /* (Nsp) oxidizer.f90:323 */
+  double oxidizer_temp_in, oxidizer_mass_flow;
+  const double* fuel_mass_fraction;     /* (Nsp) fuel.f90:392 */
+  double fuel_temp_in, fuel_mass_flow;
+} rc_thermo;
+
+/* Solver flags read by startup (startup.f90:55-128) that select the path. */
+typedef struct rc_config {
+  int IfViscous;
+  int If_turn_on_combustion;
+  int limit_ID;
+  double cfl;
+  double p_out;      /* exit pressure, initialization.f90:32-33 */
+  int precision;     /* RC_PREC_* */
+  int device;        /* CUDA device ordinal */
+} rc_config;
+
+/* Upload geometry, stencils and tables; build the device layout and the
+ * LU-SGS level schedule from the reference cell order.
+ * Replaces the state left by ReadMesh/compute_reconstruction_matrix
+ * (src/mesh.f90:2, src/reconstruction_initialization.f90:1). */
+int rc_init(const rc_mesh* mesh, const rc_thermo* thermo, const rc_config* cfg, rc_ctx** out);
+int rc_finalize(rc_ctx* ctx);
+
+/* PA(NVar,NE), WA(NVar,NE) in the Fortran layout (module.f90:54). */
+int rc_set_state(rc_ctx* ctx, const double* PA, const double* WA);
+int rc_get_state(rc_ctx* ctx, double* PA, double* WA);
+
+/* One entry point per reference subroutine, acting on device-resident state. */
+int rc_timestep(rc_ctx* ctx);          /* TimeStep            TimeStep.f90:4 */
+int rc_reconstruction(rc_ctx* ctx);    /* reconstruction      fvm2d.f90:183 (gradient + Limiter_Barth) */
+int rc_flux_sourceterm(rc_ctx* ctx);   /* flux_sourceterm     fvm2d.f90:196 (flux_lax + flux_viscous + sourceterm) */
+int rc_lusgs_steady(rc_ctx* ctx);      /* LU_SGS_steady       Time_LUSGS_steady.f90:102 (incl. update_primitve_variables) */
+int rc_lusgs_stage(rc_ctx* ctx, int istep); /* lu_sgs_stage   Time_LUSGS_steady.f90:74, one captured graph */
+
+/* Residual + step_residual norms (residual.f90:4-21, 61-79): res(k) =
+ * sum(vol*|hWA(k,:)|)/total_volume, romax = max(WA(1,:)).  Synchronises. */
+int rc_residual(rc_ctx* ctx, double* res, double* romax);
+
+/* Wait for queued work; returns the latched device error bits. */
+int rc_sync(rc_ctx* ctx);
+
+/* Intermediate arrays in the Fortran layout, for per-subroutine checks:
+ * "PA","WA","hWA" (NVar,NE); "GradC" (2,NVar,NE); "alpaF" (NF); "step" (NE);
+ * "GPA" (NVar,Nghostcell).  rc_set_array accepts the same names. */
+int rc_get_array(rc_ctx* ctx, const char* name, double* out);
+int rc_set_array(rc_ctx* ctx, const char* name, const double* in);
+
+/* Run all work of this context on a caller-provided cudaStream_t. */
+int rc_set_stream(rc_ctx* ctx, void* cuda_stream);
+void* rc_get_stream(rc_ctx* ctx);
+
+/* Kernel launches issued by this context so far (graph replays counted per
+ * captured kernel node) and the number of LU-SGS levels of each sweep. */
+int rc_stats(rc_ctx* ctx, long long* kernel_launches, int* fwd_levels, int* bwd_levels);
+
+const char* rc_last_error(rc_ctx* ctx);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* RC_GPU_H */

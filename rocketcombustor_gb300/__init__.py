@@ -1,0 +1,295 @@
+"""GB300-native steady LU-SGS hot path of RocketCombustor (harryzhou2000/RocketCombustor).
+
+The compute path is librc_gpu.so (hand-written CUDA for sm_103a behind the C ABI
+of include/rc_gpu.h).  This module is a thin ctypes host mirroring the reference
+driver: `Case` performs start-up and set-up from a case directory in the
+reference's input formats (include/rc_host.h) and `Solver` exposes one method per
+reference subroutine of the steady iteration:
+
+    Solver.timestep()          TimeStep            src/TimeStep.f90:4
+    Solver.reconstruction()    reconstruction      src/fvm2d.f90:183
+    Solver.flux_sourceterm()   flux_sourceterm     src/fvm2d.f90:196
+    Solver.lu_sgs_steady()     LU_SGS_steady       src/Time_LUSGS_steady.f90:102
+    Solver.lu_sgs_stage(i)     lu_sgs_stage        src/Time_LUSGS_steady.f90:74
+    Solver.residual()          Residual/step_residual  src/residual.f90:4,61
+
+There is no CPU fallback: if the library is missing or no GPU is present the
+calls raise.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+from typing import Optional, Tuple
+
+import numpy as np
+
+from . import build as _build
+
+RC_OK = 0
+RC_ERR = {1: "thermo T out of range", 2: "transport T out of range", 4: "negative rho/p/T in TimeStep",
+          8: "negative rho/p at a face", 16: "NaN in WA(1,1)", 32: "unknown boundary code",
+          1024: "invalid argument", 2048: "CUDA error"}
+RC_PREC_FP64, RC_PREC_MIXED = 0, 1
+
+_i, _d, _l, _vp, _cp = ctypes.c_int, ctypes.c_double, ctypes.c_long, ctypes.c_void_p, ctypes.c_char_p
+_IP, _DP = ctypes.POINTER(ctypes.c_int), ctypes.POINTER(ctypes.c_double)
+
+
+class RcMesh(ctypes.Structure):
+    _fields_ = [("NE", _i), ("NF", _i), ("NNT", _i), ("MaxNei", _i), ("Nghostcell", _i),
+                ("KFace", _IP), ("Neighbor", _IP), ("FNode", _IP), ("FProperty", _IP), ("NeighF", _IP),
+                ("Neigh", _IP), ("NeighC", _IP), ("Ghostcell", _IP), ("Num_ghostcell", _IP), ("Hostcell", _IP),
+                ("BCtype_Ghostcell", _IP), ("COOR", _DP), ("VECX", _DP), ("SideOfs", _DP), ("VOL", _DP),
+                ("CELLXY", _DP), ("reflen", _DP), ("wdis", _DP), ("AMLS", _DP), ("Coor_Ghostnode", _DP),
+                ("total_volume", _d)]
+
+
+class RcThermo(ctypes.Structure):
+    _fields_ = [("Nsp", _i), ("Rconstant", _d), ("mole_weight", _DP), ("R_species", _DP),
+                ("order_of_cp_polynomial", _i), ("thermo_lowest_tem", _d), ("thermo_critical_tem", _d),
+                ("thermo_highest_tem", _d), ("low_coef_Cp_species", _DP), ("high_coef_Cp_species", _DP),
+                ("low_enthalpy_b1", _DP), ("high_enthalpy_b1", _DP), ("transport_lowest_tem", _d),
+                ("transport_critical_tem", _d), ("transport_highest_tem", _d), ("mu_K", _DP * 16),
+                ("collision_diameter", _DP), ("LJ_energy", _DP), ("code_chemical_model", _i),
+                ("coef_f_react", _DP), ("coef_r_react", _DP), ("Af_react", _d), ("E_react", _d),
+                ("oxidizer_mass_fraction", _DP), ("oxidizer_temp_in", _d), ("oxidizer_mass_flow", _d),
+                ("fuel_mass_fraction", _DP), ("fuel_temp_in", _d), ("fuel_mass_flow", _d)]
+
+
+class RcConfig(ctypes.Structure):
+    _fields_ = [("IfViscous", _i), ("If_turn_on_combustion", _i), ("limit_ID", _i), ("cfl", _d), ("p_out", _d),
+                ("precision", _i), ("device", _i)]
+
+
+# C-ABI symbol -> (restype, argtypes); the declarations of include/rc_gpu.h and rc_host.h
+SIGNATURES = {
+    "rc_init": (_i, [ctypes.POINTER(RcMesh), ctypes.POINTER(RcThermo), ctypes.POINTER(RcConfig),
+                     ctypes.POINTER(_vp)]),
+    "rc_finalize": (_i, [_vp]),
+    "rc_set_state": (_i, [_vp, _DP, _DP]),
+    "rc_get_state": (_i, [_vp, _DP, _DP]),
+    "rc_timestep": (_i, [_vp]),
+    "rc_reconstruction": (_i, [_vp]),
+    "rc_flux_sourceterm": (_i, [_vp]),
+    "rc_lusgs_steady": (_i, [_vp]),
+    "rc_lusgs_stage": (_i, [_vp, _i]),
+    "rc_residual": (_i, [_vp, _DP, _DP]),
+    "rc_sync": (_i, [_vp]),
+    "rc_get_array": (_i, [_vp, _cp, _DP]),
+    "rc_set_array": (_i, [_vp, _cp, _DP]),
+    "rc_set_stream": (_i, [_vp, _vp]),
+    "rc_get_stream": (_vp, [_vp]),
+    "rc_stats": (_i, [_vp, ctypes.POINTER(ctypes.c_longlong), _IP, _IP]),
+    "rc_last_error": (_cp, [_vp]),
+    "rc_case_open": (_i, [_cp, ctypes.POINTER(_vp)]),
+    "rc_case_error": (_cp, [_vp]),
+    "rc_case_close": (None, [_vp]),
+    "rc_case_views": (_i, [_vp, _i, _i, ctypes.POINTER(RcMesh), ctypes.POINTER(RcThermo),
+                           ctypes.POINTER(RcConfig)]),
+    "rc_case_dims": (None, [_vp, ctypes.POINTER(_l)]),
+    "rc_case_PA": (_DP, [_vp]),
+    "rc_case_WA": (_DP, [_vp]),
+    "rc_case_array": (_vp, [_vp, _cp, ctypes.POINTER(_l)]),
+    "rc_run_steady": (_i, [_vp, _i, _i, _l, _l, _DP]),
+}
+
+_lib: Optional[ctypes.CDLL] = None
+
+
+def library_path() -> str:
+    return _build.LIB
+
+
+def load(build_if_missing: bool = True) -> ctypes.CDLL:
+    """Load librc_gpu.so (building it first if asked); raises if unavailable."""
+    global _lib
+    if _lib is None:
+        if not os.path.exists(_build.LIB) or (build_if_missing and not _build.up_to_date()):
+            if not build_if_missing:
+                raise RuntimeError(f"{_build.LIB} is missing: run rocketcombustor_gb300.build.build()")
+            _build.build()
+        L = ctypes.CDLL(_build.LIB)
+        for name, (res, args) in SIGNATURES.items():
+            fn = getattr(L, name)
+            fn.restype = res
+            fn.argtypes = args
+        _lib = L
+    return _lib
+
+
+class RcError(RuntimeError):
+    def __init__(self, code: int, msg: str = ""):
+        bits = [v for k, v in RC_ERR.items() if code & k]
+        super().__init__(f"RC status {code} ({', '.join(bits)}) {msg}".strip())
+        self.code = code
+
+
+def _dp(a: np.ndarray):
+    return a.ctypes.data_as(_DP)
+
+
+_CASE_ARRAYS = {  # name -> (dtype, shape from dims NE,NF,NNT,NVar,Nsp,MaxNei,Ng)
+    "KFace": (np.int32, lambda d: (d[0],)), "N": (np.int32, lambda d: (d[0], 4)),
+    "Neighbor": (np.int32, lambda d: (d[1], 2)), "FNode": (np.int32, lambda d: (d[1], 2)),
+    "FProperty": (np.int32, lambda d: (d[1],)), "NeighF": (np.int32, lambda d: (d[0], 4)),
+    "Neigh": (np.int32, lambda d: (d[0],)), "NeighC": (np.int32, lambda d: (d[0], d[5] + 1)),
+    "Ghostcell": (np.int32, lambda d: (d[0], d[5])), "Num_ghostcell": (np.int32, lambda d: (d[0],)),
+    "Hostcell": (np.int32, lambda d: (d[6],)), "Hostface": (np.int32, lambda d: (d[6],)),
+    "BCtype_Ghostcell": (np.int32, lambda d: (d[6],)), "COOR": (np.float64, lambda d: (d[2], 2)),
+    "VECX": (np.float64, lambda d: (d[1], 2)), "SideOfs": (np.float64, lambda d: (d[1], 2)),
+    "VOL": (np.float64, lambda d: (d[0],)), "CELLXY": (np.float64, lambda d: (d[0], 2)),
+    "reflen": (np.float64, lambda d: (d[0], 2)), "wdis": (np.float64, lambda d: (d[0], d[5])),
+    "AMLS": (np.float64, lambda d: (d[0], d[5], 2)), "Coor_Ghostnode": (np.float64, lambda d: (d[6], 4, 2)),
+    "CellXY_Ghostcell": (np.float64, lambda d: (d[6], 2)), "vol_Ghostcell": (np.float64, lambda d: (d[6],)),
+    "XYH": (np.float64, lambda d: (d[0], 2)), "PA": (np.float64, lambda d: (d[0], d[3])),
+    "WA": (np.float64, lambda d: (d[0], d[3])),
+}
+
+
+class Case:
+    """A case directory after the reference's start-up and set-up (host side)."""
+
+    def __init__(self, case_dir: str):
+        L = load()
+        h = _vp()
+        st = L.rc_case_open(case_dir.encode(), ctypes.byref(h))
+        if st:
+            raise RcError(st, L.rc_case_error(None).decode())
+        self._h = h
+        d = (_l * 9)()
+        L.rc_case_dims(h, d)
+        self.NE, self.NF, self.NNT, self.NVar, self.Nsp, self.MaxNei, self.Nghost, self.nstep_max, self.nscreen = list(d)
+        self.dir = case_dir
+
+    def array(self, name: str) -> np.ndarray:
+        n = _l()
+        p = load().rc_case_array(self._h, name.encode(), ctypes.byref(n))
+        if not p:
+            raise KeyError(name)
+        dt, shp = _CASE_ARRAYS[name]
+        dims = (self.NE, self.NF, self.NNT, self.NVar, self.Nsp, self.MaxNei, self.Nghost)
+        buf = (ctypes.c_byte * (n.value * np.dtype(dt).itemsize)).from_address(p)
+        return np.frombuffer(buf, dtype=dt).reshape(shp(dims))
+
+    def views(self, precision: int = RC_PREC_FP64, device: int = 0):
+        m, t, g = RcMesh(), RcThermo(), RcConfig()
+        st = load().rc_case_views(self._h, precision, device, ctypes.byref(m), ctypes.byref(t), ctypes.byref(g))
+        if st:
+            raise RcError(st)
+        return m, t, g
+
+    def close(self):
+        if getattr(self, "_h", None):
+            load().rc_case_close(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+class Solver:
+    """Device-resident steady solver for one case (one CUDA stream)."""
+
+    def __init__(self, case: Case, precision: int = RC_PREC_FP64, device: int = 0, stream: Optional[int] = None):
+        L = load()
+        self.case = case
+        m, t, g = case.views(precision, device)
+        self._keep = (m, t, g)
+        h = _vp()
+        st = L.rc_init(ctypes.byref(m), ctypes.byref(t), ctypes.byref(g), ctypes.byref(h))
+        if st:
+            raise RcError(st, "rc_init")
+        self._h = h
+        self.NE, self.NF, self.NVar, self.Nghost = case.NE, case.NF, case.NVar, case.Nghost
+        if stream is not None:
+            self._check(L.rc_set_stream(h, _vp(stream)))
+        self.set_state(case.array("PA"), case.array("WA"))
+
+    # -- status
+    def _check(self, st: int):
+        if st:
+            raise RcError(st, load().rc_last_error(self._h).decode())
+        return st
+
+    # -- reference subroutines
+    def timestep(self):
+        return self._check(load().rc_timestep(self._h))
+
+    def reconstruction(self):
+        return self._check(load().rc_reconstruction(self._h))
+
+    def flux_sourceterm(self):
+        return self._check(load().rc_flux_sourceterm(self._h))
+
+    def lu_sgs_steady(self):
+        return self._check(load().rc_lusgs_steady(self._h))
+
+    def lu_sgs_stage(self, istep: int = 1):
+        return self._check(load().rc_lusgs_stage(self._h, int(istep)))
+
+    def run(self, nsteps: int):
+        for it in range(1, nsteps + 1):
+            self.lu_sgs_stage(it)
+        return self.sync()
+
+    def residual(self) -> Tuple[np.ndarray, float]:
+        r = np.zeros(self.NVar)
+        m = np.zeros(1)
+        self._check(load().rc_residual(self._h, _dp(r), _dp(m)))
+        return r, float(m[0])
+
+    def sync(self):
+        return self._check(load().rc_sync(self._h))
+
+    # -- state / arrays in the reference layout (numpy shape = reversed Fortran shape)
+    def set_state(self, PA: np.ndarray, WA: np.ndarray):
+        PA = np.ascontiguousarray(PA, dtype=np.float64)
+        WA = np.ascontiguousarray(WA, dtype=np.float64)
+        self._check(load().rc_set_state(self._h, _dp(PA), _dp(WA)))
+
+    def get_state(self, PA: Optional[np.ndarray] = None, WA: Optional[np.ndarray] = None):
+        """PA, WA (NE, NVar); writes into the given C-contiguous float64 buffers if any."""
+        PA = np.zeros((self.NE, self.NVar)) if PA is None else PA
+        WA = np.zeros((self.NE, self.NVar)) if WA is None else WA
+        for a in (PA, WA):
+            if a.dtype != np.float64 or not a.flags.c_contiguous or a.shape != (self.NE, self.NVar):
+                raise ValueError("state buffers must be C-contiguous float64 (NE, NVar)")
+        self._check(load().rc_get_state(self._h, _dp(PA), _dp(WA)))
+        return PA, WA
+
+    _SHAPES = {"PA": lambda s: (s.NE, s.NVar), "WA": lambda s: (s.NE, s.NVar), "hWA": lambda s: (s.NE, s.NVar),
+               "GradC": lambda s: (s.NE, s.NVar, 2), "GPA": lambda s: (s.Nghost, s.NVar),
+               "alpaF": lambda s: (s.NF,), "step": lambda s: (s.NE,)}
+
+    def get_array(self, name: str) -> np.ndarray:
+        out = np.zeros(self._SHAPES[name](self))
+        self._check(load().rc_get_array(self._h, name.encode(), _dp(out)))
+        return out
+
+    def set_array(self, name: str, a: np.ndarray):
+        a = np.ascontiguousarray(a, dtype=np.float64).reshape(self._SHAPES[name](self))
+        self._check(load().rc_set_array(self._h, name.encode(), _dp(a)))
+
+    def stream(self) -> int:
+        return load().rc_get_stream(self._h) or 0
+
+    def stats(self):
+        n = ctypes.c_longlong()
+        f, b = _i(), _i()
+        load().rc_stats(self._h, ctypes.byref(n), ctypes.byref(f), ctypes.byref(b))
+        return {"kernel_launches": n.value, "fwd_levels": f.value, "bwd_levels": b.value}
+
+    def close(self):
+        if getattr(self, "_h", None):
+            load().rc_finalize(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

@@ -1,0 +1,465 @@
+"""Synthetic nozzle cases written in the reference solver's own input formats.
+
+A case directory holds exactly the files the reference reads:
+
+* ``grid1.in`` — cell-based mesh (src/mesh.f90:10-65): header ``NE NE_Vir NNT
+  NNT_Vir NF NF_Vir``, one record per cell ``kface n1 n2 n3``, node records ``x y
+  0 0``, ``NConE=0``, boundary groups ``itype ibound`` + node pairs, ``NCon=0``;
+* ``combustion/{species,thermo,transport,diffusion,chemical_kinetics,oxidizer,
+  fuel}.in`` — read by the ``setup_*`` routines of src/combustion_modeling;
+* ``flow/flow_solver_info.in`` — solver flags (src/startup.f90:55-128);
+* ``fvp1.sav`` — the restart file read by ``Read_Backup`` (src/output.f90:276-338),
+  used here to carry the initial field.
+
+Geometry (planar convergent-divergent nozzle, upper half with a symmetry axis):
+chamber x in [0, 0.10] with half-height 0.04, cosine contraction to a throat of
+half-height 0.01 at x = 0.15, cosine expansion to 0.03 at x = 0.25.  A mapped
+nx-by-ny quad grid is split into triangles with alternating diagonals and the
+interior nodes are jittered by a seeded uniform +-10 % of the local spacing.
+
+Boundary codes follow src/update_flow_variables.f90:240-368: 2 symmetry (axis),
+3 mass-flux inlet (x = 0), 5 outlet (x = 0.25), 6 slip wall or 1 no-slip wall.
+
+Cell order — the order in ``grid1.in`` fixes the Gauss-Seidel recurrence of the
+LU-SGS sweeps, for the reference and for this project alike:
+
+* ``"natural"``: columns marching downstream, bottom to top inside a column;
+* ``"colored"``: a greedy colouring of the cell adjacency graph (natural order
+  inside each colour class), which gives a handful of sweep levels;
+* ``"random"``: a seeded permutation.
+"""
+from __future__ import annotations
+
+import math
+import os
+from dataclasses import dataclass, field, asdict
+from typing import Dict, List, Optional, Sequence
+
+import numpy as np
+
+R_UNIVERSAL = 8.31446261815324  # src/combustion/species.in:9
+
+X_CHAMBER, X_THROAT, X_EXIT = 0.10, 0.15, 0.25
+H_CHAMBER, H_THROAT, H_EXIT = 0.04, 0.01, 0.03
+
+
+def half_height(x: np.ndarray) -> np.ndarray:
+    """Nozzle wall y = h(x): flat chamber, cosine contraction and expansion."""
+    x = np.asarray(x, dtype=np.float64)
+    h = np.full_like(x, H_CHAMBER)
+    c = (x > X_CHAMBER) & (x <= X_THROAT)
+    t = (x[c] - X_CHAMBER) / (X_THROAT - X_CHAMBER)
+    h[c] = H_THROAT + 0.5 * (H_CHAMBER - H_THROAT) * (1.0 + np.cos(np.pi * t))
+    e = x > X_THROAT
+    t = (x[e] - X_THROAT) / (X_EXIT - X_THROAT)
+    h[e] = H_THROAT + 0.5 * (H_EXIT - H_THROAT) * (1.0 - np.cos(np.pi * t))
+    return h
+
+
+def area_ratio_mach(ratio: float, gamma: float, supersonic: bool) -> float:
+    """Mach number for A/A* = ratio (isentropic), by bisection."""
+    def f(m):
+        g1 = (gamma + 1.0) / (2.0 * (gamma - 1.0))
+        return (1.0 / m) * ((2.0 / (gamma + 1.0)) * (1.0 + 0.5 * (gamma - 1.0) * m * m)) ** g1 - ratio
+
+    lo, hi = (1.0, 50.0) if supersonic else (1e-6, 1.0)
+    for _ in range(200):
+        mid = 0.5 * (lo + hi)
+        if (f(mid) > 0) == (not supersonic):
+            lo = mid
+        else:
+            hi = mid
+    return 0.5 * (lo + hi)
+
+
+@dataclass
+class Mesh:
+    coor: np.ndarray          # (NNT, 2) float64
+    cells: np.ndarray         # (NE, 3) int64, 1-based node ids, counter-clockwise
+    boundaries: List[tuple]   # [(itype, (nb,2) int64 1-based node pairs)]
+    nx: int
+    ny: int
+
+    @property
+    def ne(self) -> int:
+        return int(self.cells.shape[0])
+
+    @property
+    def nnt(self) -> int:
+        return int(self.coor.shape[0])
+
+    @property
+    def nf(self) -> int:
+        # Euler: interior edges + boundary edges for a triangulated quad grid
+        nx, ny = self.nx, self.ny
+        return nx * (ny + 1) + ny * (nx + 1) + nx * ny
+
+
+def _color_order(cells: np.ndarray, nnt: int) -> np.ndarray:
+    """Natural order inside colour classes of a greedy edge-adjacency colouring."""
+    ne = cells.shape[0]
+    edges = np.concatenate([cells[:, [0, 1]], cells[:, [1, 2]], cells[:, [2, 0]]])
+    owner = np.concatenate([np.arange(ne)] * 3)
+    key = np.minimum(edges[:, 0], edges[:, 1]).astype(np.int64) * (nnt + 1) + np.maximum(edges[:, 0], edges[:, 1])
+    order = np.argsort(key, kind="stable")
+    ks, ow = key[order], owner[order]
+    same = ks[1:] == ks[:-1]
+    a, b = ow[:-1][same], ow[1:][same]
+    adj: List[List[int]] = [[] for _ in range(ne)]
+    for u, v in zip(a.tolist(), b.tolist()):
+        adj[u].append(v)
+        adj[v].append(u)
+    color = np.full(ne, -1, dtype=np.int64)
+    for c in range(ne):
+        used = {color[n] for n in adj[c] if color[n] >= 0}
+        k = 0
+        while k in used:
+            k += 1
+        color[c] = k
+    return np.lexsort((np.arange(ne), color))
+
+
+def nozzle_mesh(nx: int, ny: int, seed: int, order: str = "natural", wall_type: int = 6,
+                jitter: float = 0.10) -> Mesh:
+    """Seeded triangulated nozzle: (nx*ny*2) triangles, ordering per `order`."""
+    rng = np.random.default_rng(seed)
+    xs = np.linspace(0.0, X_EXIT, nx + 1)
+    hx = half_height(xs)
+    jj = np.arange(ny + 1) / ny
+    X = np.repeat(xs[:, None], ny + 1, axis=1)
+    Y = hx[:, None] * jj[None, :]
+    dxl = X_EXIT / nx
+    dyl = hx[:, None] / ny * np.ones((1, ny + 1))
+    jx = rng.uniform(-jitter, jitter, size=X.shape) * dxl
+    jy = rng.uniform(-jitter, jitter, size=X.shape) * dyl
+    interior = np.zeros(X.shape, dtype=bool)
+    interior[1:-1, 1:-1] = True
+    X = np.where(interior, X + jx, X)
+    Y = np.where(interior, Y + jy, Y)
+    # node id (i, j) -> i*(ny+1) + j + 1
+    nid = lambda i, j: i * (ny + 1) + j + 1  # noqa: E731
+    coor = np.stack([X.ravel(), Y.ravel()], axis=1)
+    I, J = np.meshgrid(np.arange(nx), np.arange(ny), indexing="ij")
+    I, J = I.ravel(), J.ravel()
+    a, b, c, d = nid(I, J), nid(I + 1, J), nid(I + 1, J + 1), nid(I, J + 1)
+    diag_ac = ((I + J) % 2) == 0
+    t1 = np.where(diag_ac[:, None], np.stack([a, b, c], 1), np.stack([a, b, d], 1))
+    t2 = np.where(diag_ac[:, None], np.stack([a, c, d], 1), np.stack([b, c, d], 1))
+    cells = np.stack([t1, t2], axis=1).reshape(-1, 3).astype(np.int64)
+    if order == "natural":
+        pass
+    elif order == "colored":
+        cells = cells[_color_order(cells, coor.shape[0])]
+    elif order == "random":
+        cells = cells[np.random.default_rng(seed + 1000).permutation(cells.shape[0])]
+    else:
+        raise ValueError(f"unknown cell order {order!r}")
+    i_all = np.arange(nx)
+    j_all = np.arange(ny)
+    axis = np.stack([nid(i_all, 0), nid(i_all + 1, 0)], 1)
+    wall = np.stack([nid(i_all + 1, ny), nid(i_all, ny)], 1)
+    inlet = np.stack([nid(0, j_all + 1), nid(0, j_all)], 1)
+    outlet = np.stack([nid(nx, j_all), nid(nx, j_all + 1)], 1)
+    boundaries = [(2, axis), (wall_type, wall), (3, inlet), (5, outlet)]
+    return Mesh(coor=coor, cells=cells, boundaries=boundaries, nx=nx, ny=ny)
+
+
+def write_grid(path: str, mesh: Mesh) -> None:
+    """grid1.in in the layout read by ReadMesh (src/mesh.f90:10-65)."""
+    ne, nnt, nf = mesh.ne, mesh.nnt, mesh.nf
+    with open(path, "w") as f:
+        f.write(f"{ne} {ne} {nnt} {nnt} {nf} {nf}\n")
+        cells = np.concatenate([np.full((ne, 1), 3, dtype=np.int64), mesh.cells], axis=1)
+        np.savetxt(f, cells, fmt="%d")
+        cz = np.concatenate([mesh.coor, np.zeros((nnt, 2))], axis=1)
+        np.savetxt(f, cz, fmt=["%.17g", "%.17g", "%d", "%d"])
+        f.write("0\n")  # NConE
+        nbmax = max(len(p) for _, p in mesh.boundaries)
+        f.write(f"{len(mesh.boundaries)} {nbmax}\n")
+        for itype, pairs in mesh.boundaries:
+            f.write(f"{itype} {len(pairs)}\n")
+            np.savetxt(f, pairs, fmt="%d")
+        f.write("0\n")  # NCon
+
+
+# ----------------------------------------------------------------- physics --
+@dataclass
+class Species:
+    names: List[str]
+    mole_weight: List[float]
+
+
+def _fmt(x: float) -> str:
+    return repr(float(x))
+
+
+def write_species(d: str, sp: Species) -> None:
+    with open(os.path.join(d, "combustion", "species.in"), "w") as f:
+        f.write("# number of species\n")
+        f.write(f"{len(sp.names)}\n")
+        f.write("# species name, mole weight (kg/mol)\n")
+        for n, m in zip(sp.names, sp.mole_weight):
+            f.write(f"{n} , {_fmt(m)}\n")
+        f.write("# gas constant R (J/mol/K)\n")
+        f.write(f"{_fmt(R_UNIVERSAL)}\n")
+
+
+def write_thermo(d: str, low: np.ndarray, high: np.ndarray, b1: Sequence[float],
+                 trange=(200.0, 1000.0, 60000.0)) -> None:
+    """thermo.in (thermo_property.f90:95-136); coefficient arrays are (Nsp, 7)."""
+    nsp = low.shape[0]
+    with open(os.path.join(d, "combustion", "thermo.in"), "w") as f:
+        f.write("# reference temperature\n298.15\n# order of Cp polynomial\n7\n")
+        f.write("# Cp polynomial coefficients\n")
+        f.write(", ".join(_fmt(t) for t in trange) + "\n")
+        for i in range(nsp):
+            f.write(", ".join(_fmt(v) for v in low[i]) + "\n")
+            f.write(_fmt(b1[i]) + "\n")
+            f.write(", ".join(_fmt(v) for v in high[i]) + "\n")
+            f.write(_fmt(b1[i]) + "\n")
+        f.write("# heat of formation (J/mol) unused?\n")
+        for i in range(nsp):
+            f.write("0\n")
+
+
+# Shipped property data of the H2/O2/H2O/Ar mixture (src/combustion/*.in).
+H2O2_SPECIES = Species(["H2", "O2", "H2O", "Ar"], [2.0e-3, 32.0e-3, 18.0e-3, 40.0e-3])
+H2O2_TRANSPORT = [
+    [0.57388074E0, -0.98544160E2, 0.20012204E4, 0.17536015E1],
+    [0.65074534E0, 0.23936771E2, -0.22020183E5, 0.11244058E1],
+    [0.11770360E1, -0.17422121E3, 0.22865563E5, -0.55146852E0],
+    [0.49214767E0, -0.91598343E3, 0.87265127E5, 0.48489412E1],
+    [0.61936357E0, -0.44608607E2, -0.13460714E4, 0.19597562E1],
+    [0.63839563E0, -0.12344438E1, -0.22885810E5, 0.18056937E1],
+    [0.81595343E0, -0.34366856E2, 0.22785080E4, 0.10050999E1],
+    [0.80805788E0, 0.11982181E3, -0.47335931E5, 0.95189193E0],
+    [0.54330318E0, -0.18823898E3, 0.88726567E4, 0.24499362E1],
+    [0.65318879E0, 0.51738759E2, -0.62834882E5, 0.15227045E1],
+    [0.53726173E0, -0.49928331E3, 0.37397504E5, 0.32903619E1],
+    [0.66068182E0, -0.12741845E3, -0.81580328E5, 0.21817907E1],
+    [0.78387780E0, -0.38260408E3, 0.49040158E5, 0.85222785E0],
+    [0.50714993E0, -0.68966913E3, 0.87454750E5, 0.30285155E1],
+    [0.15541443E1, 0.66106305E2, 0.55969886E4, -0.39259598E1],
+    [0.79349503E0, -0.13340063E4, 0.37864327E6, 0.23591474E1],
+]
+H2O2_DIFFUSION = [(3.758, 148.6), (3.467, 106.7), (3.941, 195.2), (2.641, 809.1)]
+# 2 H2 + O2 -> 2 H2O; global rate constants (chemical_kinetics.in:4-9)
+H2O2_STOICH = [(2.0, 0.0), (1.0, 0.0), (0.0, 2.0), (0.0, 0.0)]
+H2O2_RATE = (2.12e11, 0.0, 2.025e5)
+H2O_HOF_J_PER_MOL = -241826.0  # thermo.in:16,18
+
+
+def write_transport(d: str, rows: List[List[float]]) -> None:
+    with open(os.path.join(d, "combustion", "transport.in"), "w") as f:
+        f.write("# transport_lowest_tem,transport_critical_tem,transport_highest_tem\n")
+        f.write("200.0, 1000.0, 50000.0\n# low_mu_A,low_mu_B,low_mu_C,low_mu_D\n")
+        for r in rows:
+            f.write(", ".join(_fmt(v) for v in r) + "\n")
+
+
+def write_diffusion(d: str, pairs) -> None:
+    with open(os.path.join(d, "combustion", "diffusion.in"), "w") as f:
+        f.write("# Boltzmann's constant k_B (m2*kg*s-2*K-1)\n1.38064852E-23\n")
+        f.write("# hard-sphere collision diameter sigma (A), Lennard-Jones energy epsilon/k_B (K)\n")
+        for s, e in pairs:
+            f.write(f"{_fmt(s)}, {_fmt(e)}\n")
+
+
+def write_kinetics(d: str, stoich, rate, model: int) -> None:
+    with open(os.path.join(d, "combustion", "chemical_kinetics.in"), "w") as f:
+        f.write("# number of reactions\n")
+        f.write(f"1, {model}\n")
+        f.write("# forwar reaction coefficient, reverse reaction coefficient\n")
+        for a, b in stoich:
+            f.write(f"{_fmt(a)}, {_fmt(b)}\n")
+        f.write("# pre-exponential factor, temperature exponent, activation energy (J)\n")
+        f.write(", ".join(_fmt(v) for v in rate) + "\n")
+        f.write("# entropy change, enthalpy change unused?\n0., 0.\n# p_a\n1.0e5\n")
+
+
+def write_inlet(path: str, Y: Sequence[float], T: float, p: float, mflow: float, what: str) -> None:
+    with open(path, "w") as f:
+        f.write(f"# {what} mass fraction\n")
+        for y in Y:
+            f.write(_fmt(y) + "\n")
+        f.write("# temperature (K), pressure (K)\n")
+        f.write(f"{_fmt(T)}, {_fmt(p)}\n# mass flow rate (kg/s)\n{_fmt(mflow)}\n")
+
+
+def write_flow_info(d: str, combustion: bool, viscous: bool, cfl: float, nstep: int,
+                    limit_id: int, p_out_ratio: float) -> None:
+    L = lambda b: ".true." if b else ".false."  # noqa: E731
+    with open(os.path.join(d, "flow", "flow_solver_info.in"), "w") as f:
+        f.write(f"# If_turn_on_combustion, chemical model\n{L(combustion)}\n")
+        f.write("# IfRightDomain\n.false.\n# NPreviousPar\n1\n# Npar, number of processors\n1\n")
+        f.write("# unit\n1.0\n")
+        f.write(f"# IfSteady, IfViscous, IfReadBackup, IfExplicit\n.true., {L(viscous)}, .true., .false.\n")
+        f.write("# implicit_time_method: 1-> Implicit Runge-Kutta, 2-> Trapezoidal, 3-> Euler, 4-> Midpoint, 5-> BDF2\n5\n")
+        f.write(f"# cfl,totaltime,nstep_max,save_start_time, save_end_time\n{_fmt(cfl)}, 1.0, {nstep}, 0.0, 0.5\n")
+        f.write("# IfFixDt\n.false.\n# InLoop, InnerLoop, relTol\n1, 1, 1.0e-8\n")
+        f.write("# NScreenOutput,NFileOutput,NFileBackup,NWriteMonitor\n100,100000,100000,100000\n")
+        f.write(f"# rc_detector\n3.0\n# n_wbap,limit_ID: 0-> no limiter, 1-> WBAP, 2-> WBAP_Char\n10, {limit_id}\n")
+        f.write("# number of monitor points\n1\n# x_monitor_point, y_monitor_point\n0,0\n")
+        f.write(f"# exit pressure ratio, A_p, f_p\n{_fmt(p_out_ratio)}, 0., 5000.0\n")
+
+
+def write_backup(path: str, mesh: Mesh, PA: np.ndarray) -> None:
+    """fvp1.sav (output.f90:256-273): ttime, NE, then x y PA(1:NVar) per cell."""
+    cxy = mesh.coor[mesh.cells - 1].mean(axis=1)
+    with open(path, "w") as f:
+        f.write("0.0\n")
+        f.write(f"{mesh.ne}\n")
+        np.savetxt(f, np.concatenate([cxy, PA], axis=1), fmt="%.17g")
+
+
+# --------------------------------------------------------------- configs ---
+@dataclass
+class CaseConfig:
+    """One synthetic nozzle case; `name` keys the presets below."""
+    name: str
+    nx: int
+    ny: int
+    seed: int
+    order: str = "colored"
+    nsp: int = 1
+    viscous: bool = False
+    combustion: bool = False
+    p0: float = 2.0e6
+    T0: float = 3000.0
+    cfl: float = 5.0
+    nstep: int = 2000
+    limit_id: int = 1
+    thermo_seed: int = 3
+    perturb_seed: int = 4
+    perturb: float = 0.0
+    chem_model: int = 0
+    of_ratio: float = 6.0
+    inlet_burnt: float = 1.0   # fraction of O2 already converted at the inlet
+    closed: bool = False       # every boundary a wall, fluid initially at rest (test case)
+
+    @property
+    def n_cells(self) -> int:
+        return 2 * self.nx * self.ny
+
+
+PRESETS: Dict[str, CaseConfig] = {
+    # small inviscid perfect-gas nozzle (about 20k triangles)
+    "c1": CaseConfig("c1", nx=250, ny=40, seed=1),
+    # reacting viscous nozzle (about 120k triangles)
+    "c2": CaseConfig("c2", nx=600, ny=100, seed=2, nsp=4, viscous=True, combustion=True,
+                     p0=5.0e6, T0=3500.0, perturb=0.02),
+    # large reacting viscous nozzle (2M triangles)
+    "c4": CaseConfig("c4", nx=2500, ny=400, seed=6, nsp=4, viscous=True, combustion=True,
+                     p0=5.0e6, T0=3500.0, perturb=0.02, nstep=500),
+    # tiny cases for tests
+    "t1": CaseConfig("t1", nx=24, ny=6, seed=11),
+    "t2": CaseConfig("t2", nx=24, ny=6, seed=12, nsp=4, viscous=True, combustion=True,
+                     p0=5.0e6, T0=3500.0, perturb=0.02),
+}
+
+
+def synthetic_cp(nsp: int, seed: int) -> np.ndarray:
+    """Seeded smooth cp/R = a3 + a4 T + a5 T^2, rising from a3 in [3.5, 3.7] at
+    T -> 0 to a maximum in [4.2, 4.5] at 4000 K (coefficient slots 3..5 of the
+    7-term polynomial, thermo_property.f90:162-172)."""
+    rng = np.random.default_rng(seed)
+    coef = np.zeros((nsp, 7))
+    for i in range(nsp):
+        a3 = rng.uniform(3.5, 3.7)
+        top = rng.uniform(4.2, 4.5)
+        a5 = (a3 - top) / 16.0e6
+        coef[i, 2] = a3
+        coef[i, 3] = -8000.0 * a5
+        coef[i, 4] = a5
+    return coef
+
+
+def inlet_state(cfg: CaseConfig, R: float, gamma: float):
+    """Static inlet state of the subsonic chamber for total (p0, T0) at the
+    chamber-to-throat area ratio: returns (p, T, u, mass flux)."""
+    M = area_ratio_mach(H_CHAMBER / H_THROAT, gamma, supersonic=False)
+    T = cfg.T0 / (1.0 + 0.5 * (gamma - 1.0) * M * M)
+    p = cfg.p0 * (T / cfg.T0) ** (gamma / (gamma - 1.0))
+    rho = p / (R * T)
+    u = M * math.sqrt(gamma * R * T)
+    return p, T, u, rho * u
+
+
+def exit_pressure_ratio(gamma: float) -> float:
+    M = area_ratio_mach(H_EXIT / H_THROAT, gamma, supersonic=True)
+    return (1.0 + 0.5 * (gamma - 1.0) * M * M) ** (-gamma / (gamma - 1.0))
+
+
+def write_case(d: str, cfg: CaseConfig, mesh: Optional[Mesh] = None) -> Mesh:
+    """Write a complete case directory for `cfg`; returns the mesh."""
+    os.makedirs(os.path.join(d, "combustion"), exist_ok=True)
+    os.makedirs(os.path.join(d, "flow"), exist_ok=True)
+    if mesh is None:
+        mesh = nozzle_mesh(cfg.nx, cfg.ny, cfg.seed, cfg.order, wall_type=1 if cfg.viscous else 6)
+    if cfg.closed:
+        wall = 1 if cfg.viscous else 6
+        mesh.boundaries = [(wall, pairs) for _, pairs in mesh.boundaries]
+    write_grid(os.path.join(d, "grid1.in"), mesh)
+    if cfg.nsp == 1:
+        # single calorically perfect gas, gamma = 1.4, R = 287
+        sp = Species(["AIR"], [R_UNIVERSAL / 287.0])
+        low = np.zeros((1, 7)); low[0, 2] = 3.5
+        write_species(d, sp)
+        write_thermo(d, low, low, [0.0])
+        write_transport(d, H2O2_TRANSPORT[0:4])
+        write_diffusion(d, H2O2_DIFFUSION[0:1])
+        write_kinetics(d, [(0.0, 0.0)], H2O2_RATE, cfg.chem_model)
+        Yin = [1.0]
+        Rmix = R_UNIVERSAL / sp.mole_weight[0]
+        gamma = 1.4
+    else:
+        sp = H2O2_SPECIES
+        coef = synthetic_cp(4, cfg.thermo_seed)
+        # b1 in kelvin: the formula R_k (T sum a_j basis_j + b1) expects it; the
+        # shipped value in J/mol is divided by R.
+        b1 = [0.0, 0.0, H2O_HOF_J_PER_MOL / R_UNIVERSAL, 0.0]
+        write_species(d, sp)
+        write_thermo(d, coef, coef, b1)
+        write_transport(d, H2O2_TRANSPORT)
+        write_diffusion(d, H2O2_DIFFUSION)
+        write_kinetics(d, H2O2_STOICH, H2O2_RATE, cfg.chem_model)
+        # propellant O/F by mass, with a fraction of the O2 already converted
+        y_h2, y_o2 = 1.0 / (1.0 + cfg.of_ratio), cfg.of_ratio / (1.0 + cfg.of_ratio)
+        burnt = cfg.inlet_burnt * y_o2
+        Yin = [y_h2 - burnt * (4.0 / 32.0), y_o2 - burnt, burnt * (36.0 / 32.0), 0.0]
+        Rs = [R_UNIVERSAL / m for m in sp.mole_weight]
+        Rmix = sum(y * r for y, r in zip(Yin, Rs))
+        cpm = sum(y * r * (coef[i, 2] + coef[i, 3] * cfg.T0 + coef[i, 4] * cfg.T0 ** 2)
+                  for i, (y, r) in enumerate(zip(Yin, Rs)))
+        gamma = cpm / (cpm - Rmix)
+    p_in, T_in, u_in, mflux = inlet_state(cfg, Rmix, gamma)
+    # oxidizer inlet carries the chamber mixture; the reference divides the .in
+    # mass flow by the measured inlet diameter 2*(ymax-ymin) (initialization.f90:22)
+    write_inlet(os.path.join(d, "combustion", "oxidizer.in"), Yin, T_in, cfg.p0,
+                mflux * 2.0 * H_CHAMBER, "oxidizer")
+    write_inlet(os.path.join(d, "combustion", "fuel.in"), Yin, T_in, cfg.p0, 0.37, "fuel")
+    pr = exit_pressure_ratio(gamma)
+    write_flow_info(d, cfg.combustion, cfg.viscous, cfg.cfl, cfg.nstep, cfg.limit_id, pr)
+    # initial field: uniform inlet (chamber) state, optionally perturbed Y
+    nv = 4 + len(Yin) - 1
+    PA = np.zeros((mesh.ne, nv))
+    PA[:, 0], PA[:, 1], PA[:, 2], PA[:, 3] = p_in, (0.0 if cfg.closed else u_in), 0.0, T_in
+    if len(Yin) > 1:
+        Y = np.tile(np.asarray(Yin), (mesh.ne, 1))
+        if cfg.perturb > 0:
+            rng = np.random.default_rng(cfg.perturb_seed)
+            Y = Y * (1.0 + rng.uniform(-cfg.perturb, cfg.perturb, size=Y.shape))
+            Y = Y / Y.sum(axis=1, keepdims=True)
+        PA[:, 4:] = Y[:, :-1]
+    write_backup(os.path.join(d, "fvp1.sav"), mesh, PA)
+    with open(os.path.join(d, "case.json"), "w") as f:
+        import json
+        json.dump(asdict(cfg), f, indent=1)
+    return mesh
+
+
+def make_case(d: str, name: str, **over) -> CaseConfig:
+    """Write preset `name` (with field overrides) into directory `d`."""
+    cfg = CaseConfig(**{**asdict(PRESETS[name]), **over})
+    write_case(d, cfg)
+    return cfg

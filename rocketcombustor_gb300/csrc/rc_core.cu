@@ -1,0 +1,1286 @@
+// GB300 (sm_103a) kernels and C ABI for the steady LU-SGS iteration of
+// RocketCombustor (lu_sgs_stage, src/Time_LUSGS_steady.f90:74-100).
+//
+// Device layout (structure of arrays, reference cell/face order, 0-based):
+//   cell arrays  X[k*NE + i]  (PA, WA, hWA, cell gas state, sources)
+//   gradients    G[(2k+r)*NE + i]  (r = x, y in reflen-scaled coordinates)
+//   face arrays  F[k*NF + f]  (inviscid and viscous face fluxes)
+//   stencils     per cell up to 4 slots, slot q at [q*NE + i], in NeighF order.
+//
+// One iteration is five kernel kinds (captured in one CUDA graph):
+//   k_ts_face   per face:  spectral radius of TimeStep                (TimeStep.f90:16-92)
+//   k_cell      per cell:  local step and LU-SGS diagonal, ghost states, LS gradient,
+//                          Barth limiter, cell gas state, chemical source
+//   k_face_flux per face:  Lax/Rusanov flux and viscous flux           (flux_lax.f90, flux_viscous.f90)
+//   k_sweep     per level: forward sweep (with the residual gather) / backward sweep
+//   k_update    per cell:  WA += dU and the Newton temperature update
+// Face contributions are gathered per cell in NeighF order, which is the
+// reference's scatter order, so no atomics are used and the sums are the
+// reference's sums.  The sweeps run level by level over the reference cell
+// order and compute the reference's Gauss-Seidel recurrences exactly.
+//
+// Built with --fmad=false: no FMA contraction, matching the reference build.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "rc_gpu.h"
+#include "rc_thermo.cuh"
+
+namespace rc {
+
+constexpr int MAXF = 4;  // faces per cell (triangles and quadrilaterals)
+
+struct Dev {
+  int NE, NF, NG;
+  // cells
+  const double* vol;
+  const double* rinv;            // [2*NE] 1./reflen
+  const unsigned char* nface;    // KFace
+  const unsigned char* cleft;    // bit q: cell is Neighbor(1,.) of its face q
+  const int* cface;              // [4*NE] NeighF, 0-based
+  const int* cother;             // [4*NE] cell across face q, -1 on a boundary
+  const unsigned char* nnei;     // Neigh
+  const int* cnei;               // [4*NE] NeighC(1:Neigh), 0-based
+  const unsigned char* ngh;      // Num_ghostcell
+  const int* cgh;                // [4*NE] Ghostcell, 0-based
+  const double* wdis;            // [4*NE]
+  const double* amls;            // [8*NE] AMLS(r,q,i) at (2q+r)*NE+i
+  const double* lvvh;            // [8*NE] limiter basis values at the face midpoints
+  // faces
+  const int* fNL;                // 0-based
+  const int* fNR;                // 0-based cell, or -BC code
+  const double* fvec;            // [2*NF] VECX
+  const double* fsav;            // max(|VECX|, small)
+  const double* fsn;             // [2*NF] unit normal
+  const double* fss;             // sqrt(dx*dx+dy*dy)
+  const double* fs2;             // dx*dx+dy*dy
+  const double* fvL;             // [2*NF] fbaseAll at the Gauss point for NL
+  const double* fvR;             // [2*NF] fbaseAll at the Gauss point for NR
+  const double* fdxk;            // |(x_L - x_R).n|
+  const double* fysn;            // [2*NF] yita*n
+  // ghosts
+  const int* gtype;
+  const double* gsn;             // [2*NG] ghost-face unit normal
+  // state and work arrays
+  double* PA;
+  double* WA;
+  double* hWA;
+  double* grad;
+  double* GPA;
+  double* step;
+  double* dd;
+  double* cst;                   // [(3+NSP)*NE]: rho, gamma, rho*E, h_k
+  double* src;                   // [(NSP-1)*NE]: vol*omega_k
+  double* alpa;
+  double* visL;
+  double* visR;
+  double* alpaF;
+  double* Finv;                  // [V*NF]
+  double* Fvis;                  // [(V-1)*NF], component 1 is identically zero
+  unsigned* err;
+};
+
+__device__ __forceinline__ void flag(const Dev& d, unsigned e) {
+  if (e) atomicOr(d.err, e);
+}
+
+__device__ __forceinline__ void removedirection(double& vx, double& vy, double nx, double ny) {
+  const double vn = vx * nx + vy * ny;  // flux_viscous.f90:352-361
+  vx = vx - vn * nx;
+  vy = vy - vn * ny;
+}
+
+// oxidizer_inlet_bc / fuel_inlet_bc (oxidizer.f90:367-382, fuel.f90:437-452)
+template <int NSP>
+__device__ __forceinline__ void inlet_bc(const ThermoDev<NSP>& th, int w, double pl, double& pr, double& ur,
+                                         double& vr, double& tr, double& rr, double* Yr, double& Cpr,
+                                         double& gamar, double& Rcpcvr, unsigned& err) {
+#pragma unroll
+  for (int k = 0; k < NSP; ++k) Yr[k] = th.inY[w][k];
+  tr = th.inT[w];
+  gas<NSP>(th, Yr, tr, Cpr, gamar, Rcpcvr, err);
+  pr = pl;
+  rr = pr / (Rcpcvr * tr);
+  ur = th.inMflow[w] / rr;
+  vr = 0.0;
+}
+
+// ----------------------------------------------------------- TimeStep ------
+template <int NSP, bool VISC>
+__global__ void __launch_bounds__(128) k_ts_face(const Dev d, const ThermoDev<NSP> th) {
+  constexpr int V = 3 + NSP;
+  const int f = blockIdx.x * blockDim.x + threadIdx.x;
+  if (f >= d.NF) return;
+  unsigned err = 0;
+  const int NE = d.NE, NL = d.fNL[f], NR = d.fNR[f];
+  double P[V], yy[NSP];
+  if (NR >= 0) {
+#pragma unroll
+    for (int k = 0; k < V; ++k) P[k] = 0.5 * (d.PA[k * NE + NL] + d.PA[k * NE + NR]);
+  } else {
+#pragma unroll
+    for (int k = 0; k < V; ++k) P[k] = d.PA[k * NE + NL];
+  }
+  double s = 0.0;
+#pragma unroll
+  for (int k = 0; k < NSP - 1; ++k) { yy[k] = P[4 + k]; s = s + yy[k]; }
+  yy[NSP - 1] = 1.0 - s;
+  const double pp = P[0], uu = P[1], vv = P[2], tt = P[3];
+  double Cp, gama, Rcpcv;
+  gas<NSP>(th, yy, tt, Cp, gama, Rcpcv, err);
+  const double rr = pp / (Rcpcv * tt);
+  if (rr < 0. || pp < 0. || tt < 0.) err |= ERR_NEG_TIMESTEP;
+  const double unormal = uu * d.fvec[f] + vv * d.fvec[d.NF + f];
+  const double alpa = fabs(unormal) + sqrt(gama * pp / rr) * d.fss[f];
+  d.alpa[f] = alpa;
+  if (VISC) {
+    double vmul, akmu;
+    transport<NSP>(th, tt, yy, vmul, akmu, err);
+    const double prl = vmul * Cp / akmu;
+    const double alpaVis = 2. * d.fs2[f] * fmax2(4. / 3., gama / prl) * vmul / rr;
+    const double vl = alpaVis / d.vol[NL];
+    d.visL[f] = vl;
+    d.visR[f] = (NR >= 0) ? alpaVis / d.vol[NR] : 0.0;
+    d.alpaF[f] = alpa + vl;
+  } else {
+    d.alpaF[f] = alpa;
+  }
+  flag(d, err);
+}
+
+// --------------------------------------------------------- cell kernel -----
+// step/dd (TimeStep.f90:94-96, Time_LUSGS_steady.f90:116-123), ghost states
+// (update_flow_variables.f90:195-377), gradient (gradient.f90:4-45), Barth
+// limiter (limiter.f90:5-107), cell gas state and source (sourceterm.f90:2-70).
+template <int NSP>
+__global__ void __launch_bounds__(128) k_cell(const Dev d, const ThermoDev<NSP> th, int do_step, int do_recon,
+                                              int limit, int comb, int visc) {
+  constexpr int V = 3 + NSP;
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= d.NE) return;
+  const int NE = d.NE;
+  unsigned err = 0;
+  const int nf = d.nface[i];
+  const double vol = d.vol[i];
+  if (do_step) {
+    const unsigned lb = d.cleft[i];
+    double acc = 0.0;
+    for (int q = 0; q < nf; ++q) {
+      const int f = d.cface[q * NE + i];
+      if (visc) acc = acc + d.alpa[f] + (((lb >> q) & 1u) ? d.visL[f] : d.visR[f]);
+      else acc = acc + d.alpa[f];
+    }
+    const double st = th.cfl * vol / acc;
+    double dsum = 0.0;
+    for (int q = 0; q < nf; ++q) dsum = dsum + 0.5 * d.alpaF[d.cface[q * NE + i]];
+    d.step[i] = st;
+    d.dd[i] = dsum + vol / st;
+  }
+  if (!do_recon) { flag(d, err); return; }
+  double P[V], Y[NSP];
+#pragma unroll
+  for (int k = 0; k < V; ++k) P[k] = d.PA[k * NE + i];
+  double s = 0.0;
+#pragma unroll
+  for (int k = 0; k < NSP - 1; ++k) { Y[k] = P[4 + k]; s = s + Y[k]; }
+  Y[NSP - 1] = 1.0 - s;
+  double Cp, gama, Rcpcv, entha[NSP];
+  gas<NSP>(th, Y, P[3], Cp, gama, Rcpcv, err);
+  const double rr = P[0] / (Rcpcv * P[3]);
+  enthalpy<NSP>(th, P[3], entha, err);
+  double hh = 0.0;
+#pragma unroll
+  for (int k = 0; k < NSP; ++k) hh = hh + Y[k] * entha[k];
+  d.cst[0 * NE + i] = rr;
+  d.cst[1 * NE + i] = gama;
+  d.cst[2 * NE + i] = rr * (hh + 0.5 * (P[1] * P[1] + P[2] * P[2])) - P[0];
+#pragma unroll
+  for (int k = 0; k < NSP; ++k) d.cst[(3 + k) * NE + i] = entha[k];
+
+  // gradient with running min/max of the stencil
+  double g0[V], g1[V], mn[V], mx[V];
+#pragma unroll
+  for (int k = 0; k < V; ++k) { g0[k] = 0.0; g1[k] = 0.0; mn[k] = P[k]; mx[k] = P[k]; }
+  const int nn = d.nnei[i];
+  for (int q = 0; q < nn; ++q) {
+    const int j = d.cnei[q * NE + i];
+    const double w = d.wdis[q * NE + i], a0 = d.amls[(2 * q) * NE + i], a1 = d.amls[(2 * q + 1) * NE + i];
+#pragma unroll
+    for (int k = 0; k < V; ++k) {
+      const double x = d.PA[k * NE + j];
+      const double c = w * (x - P[k]);
+      g0[k] = g0[k] + a0 * c;
+      g1[k] = g1[k] + a1 * c;
+      mn[k] = fmin2(mn[k], x);
+      mx[k] = fmax2(mx[k], x);
+    }
+  }
+  const int ng = d.ngh[i];
+  for (int q = 0; q < ng; ++q) {
+    const int gj = d.cgh[q * NE + i];
+    const double s1n = d.gsn[gj], s2n = d.gsn[d.NG + gj];
+    const double pl = P[0], ul = P[1], vl = P[2], tl = P[3];
+    const double ac = sqrt(gama * pl / rr);
+    double G[V], Yr[NSP];
+    double pr = pl, ur = ul, vr = vl, tr = tl, vn;
+#pragma unroll
+    for (int k = 0; k < NSP; ++k) Yr[k] = Y[k];
+    switch (d.gtype[gj]) {
+      case 1: ur = -ul; vr = -vl; break;
+      case 2:
+      case 6:
+        vn = ul * s1n + vl * s2n;
+        ur = ul - 2 * vn * s1n;
+        vr = vl - 2 * vn * s2n;
+        break;
+      case 3:
+      case 4: {
+        double rrb, Cpb, gab, Rb;
+        inlet_bc<NSP>(th, d.gtype[gj] == 3 ? 0 : 1, pl, pr, ur, vr, tr, rrb, Yr, Cpb, gab, Rb, err);
+        break;
+      }
+      case 5:
+        vn = ul * s1n + vl * s2n;
+        if (!(fabs(vn) > ac)) pr = th.p_out;
+        break;
+      default: err |= ERR_BCTYPE;
+    }
+    G[0] = pr; G[1] = ur; G[2] = vr; G[3] = tr;
+#pragma unroll
+    for (int k = 0; k < NSP - 1; ++k) G[4 + k] = Yr[k];
+#pragma unroll
+    for (int k = 0; k < V; ++k) d.GPA[k * d.NG + gj] = G[k];
+    const int m = nn + q;
+    const double w = d.wdis[m * NE + i], a0 = d.amls[(2 * m) * NE + i], a1 = d.amls[(2 * m + 1) * NE + i];
+#pragma unroll
+    for (int k = 0; k < V; ++k) {
+      const double c = w * (G[k] - P[k]);
+      g0[k] = g0[k] + a0 * c;
+      g1[k] = g1[k] + a1 * c;
+      mn[k] = fmin2(mn[k], G[k]);
+      mx[k] = fmax2(mx[k], G[k]);
+    }
+  }
+  if (limit > 0) {
+    double lv0[MAXF], lv1[MAXF];
+    for (int q = 0; q < nf; ++q) { lv0[q] = d.lvvh[(2 * q) * NE + i]; lv1[q] = d.lvvh[(2 * q + 1) * NE + i]; }
+#pragma unroll
+    for (int k = 0; k < V; ++k) {
+      double phi = 1.0;
+      for (int q = 0; q < nf; ++q) {
+        const double fv = P[k] + (g0[k] * lv0[q] + g1[k] * lv1[q]);
+        double pf;
+        if (fv > P[k]) pf = fmin2(1.0, (mx[k] - P[k]) / (fv - P[k]));
+        else if (fv < P[k]) pf = fmin2(1.0, (mn[k] - P[k]) / (fv - P[k]));
+        else pf = 1.0;
+        phi = fmin2(phi, pf);
+      }
+      g0[k] = phi * g0[k];
+      g1[k] = phi * g1[k];
+    }
+  }
+#pragma unroll
+  for (int k = 0; k < V; ++k) {
+    d.grad[(2 * k) * NE + i] = g0[k];
+    d.grad[(2 * k + 1) * NE + i] = g1[k];
+  }
+  if (comb) {
+    double prod[NSP];
+    production<NSP>(th, P[3], rr, Y, prod);
+#pragma unroll
+    for (int k = 0; k < NSP - 1; ++k) d.src[k * NE + i] = vol * prod[k];
+  }
+  flag(d, err);
+}
+
+// ------------------------------------------------------------ face flux ----
+template <int NSP>
+__device__ __forceinline__ void recon(const Dev& d, int c, double v0, double v1, double* u) {
+  constexpr int V = 3 + NSP;
+  const int NE = d.NE;
+#pragma unroll
+  for (int k = 0; k < V; ++k)
+    u[k] = d.PA[k * NE + c] + (d.grad[(2 * k) * NE + c] * v0 + d.grad[(2 * k + 1) * NE + c] * v1);
+}
+
+template <int NSP, bool VISC>
+__global__ void __launch_bounds__(128) k_face_flux(const Dev d, const ThermoDev<NSP> th) {
+  constexpr int V = 3 + NSP;
+  const int f = blockIdx.x * blockDim.x + threadIdx.x;
+  if (f >= d.NF) return;
+  unsigned err = 0;
+  const int NE = d.NE, NF = d.NF;
+  const int NL = d.fNL[f], NR = d.fNR[f];
+  const double sav1 = d.fvec[f], sav2 = d.fvec[NF + f], sav = d.fsav[f];
+  const double sav1n = d.fsn[f], sav2n = d.fsn[NF + f];
+  double uL[V], uR[V], Yl0[NSP], Yr0[NSP];
+  recon<NSP>(d, NL, d.fvL[f], d.fvL[NF + f], uL);
+  double s = 0.0;
+#pragma unroll
+  for (int k = 0; k < NSP - 1; ++k) { Yl0[k] = uL[4 + k]; s = s + Yl0[k]; }
+  Yl0[NSP - 1] = 1.0 - s;
+  double Cpl0, gamal0, Rl0;
+  gas<NSP>(th, Yl0, uL[3], Cpl0, gamal0, Rl0, err);
+  const double rl0 = uL[0] / (Rl0 * uL[3]);
+  double Cpr0 = 0.0, gamar0 = 0.0, Rr0 = 0.0, rr0 = 0.0;
+  if (NR >= 0) {
+    recon<NSP>(d, NR, d.fvR[f], d.fvR[NF + f], uR);
+    s = 0.0;
+#pragma unroll
+    for (int k = 0; k < NSP - 1; ++k) { Yr0[k] = uR[4 + k]; s = s + Yr0[k]; }
+    Yr0[NSP - 1] = 1.0 - s;
+    gas<NSP>(th, Yr0, uR[3], Cpr0, gamar0, Rr0, err);
+    rr0 = uR[0] / (Rr0 * uR[3]);
+  } else {
+#pragma unroll
+    for (int k = 0; k < V; ++k) uR[k] = uL[k];
+  }
+
+  // ---- Lax/Rusanov flux (flux_lax.f90:17-293)
+  {
+    double pl = uL[0], ul = uL[1], vl = uL[2], tl = uL[3], rl = rl0, gamal = gamal0, Rcl = Rl0, Cpl = Cpl0;
+    double pr, ur, vr, tr, rr, gamar, Rcr, Cpr, vn;
+    double Yl[NSP], Yr[NSP];
+#pragma unroll
+    for (int k = 0; k < NSP; ++k) Yl[k] = Yl0[k];
+    if (NR >= 0) {
+      pr = uR[0]; ur = uR[1]; vr = uR[2]; tr = uR[3]; rr = rr0; gamar = gamar0; Rcr = Rr0; Cpr = Cpr0;
+#pragma unroll
+      for (int k = 0; k < NSP; ++k) Yr[k] = Yr0[k];
+    } else if (NR == -3 || NR == -4) {
+      inlet_bc<NSP>(th, NR == -3 ? 0 : 1, pl, pr, ur, vr, tr, rr, Yr, Cpr, gamar, Rcr, err);
+      pl = pr; ul = ur; vl = vr; tl = tr; rl = rr;
+#pragma unroll
+      for (int k = 0; k < NSP; ++k) Yl[k] = Yr[k];
+      Cpl = Cpr; gamal = gamar; Rcl = Rcr;
+    } else {
+      rr = rl; pr = pl; tr = tl; ur = ul; vr = vl;
+      if (NR == -1) { ur = -ul; vr = -vl; }
+      else if (NR == -2 || NR == -6) {
+        vn = ul * sav1n + vl * sav2n;
+        ur = ul - 2 * vn * sav1n;
+        vr = vl - 2 * vn * sav2n;
+      } else if (NR == -5) {
+        const double ac = sqrt(gamal * pl / rl);
+        vn = ul * sav1n + vl * sav2n;
+        if (!(fabs(vn) > ac)) {
+          pr = th.p_out;
+          ur = ul + sav1n * (pl - pr) / (rl * ac);
+          vr = vl + sav2n * (pl - pr) / (rl * ac);
+          rr = rl + (pr - pl) / (ac * ac);
+          tr = pr / (Rcl * rr);
+          pl = pr; ul = ur; vl = vr; tl = tr; rl = rr;
+        }
+      } else {
+        err |= ERR_BCTYPE;
+      }
+#pragma unroll
+      for (int k = 0; k < NSP; ++k) Yr[k] = Yl[k];
+      gamar = gamal; Rcr = Rcl; Cpr = Cpl;
+    }
+    (void)Cpr; (void)Rcr; (void)Cpl;
+    if (rl < 0. || pl < 0. || (NR >= 0 && (rr < 0. || pr < 0.))) err |= ERR_NEG_FACE;
+    double entha[NSP];
+    enthalpy<NSP>(th, tl, entha, err);
+    double hl = 0.0;
+#pragma unroll
+    for (int k = 0; k < NSP; ++k) hl = hl + Yl[k] * entha[k];
+    enthalpy<NSP>(th, tr, entha, err);
+    double hr = 0.0;
+#pragma unroll
+    for (int k = 0; k < NSP; ++k) hr = hr + Yr[k] * entha[k];
+    const double vaml = ul * ul + vl * vl, vamr = ur * ur + vr * vr;
+    hl = hl + 0.5 * vaml;
+    hr = hr + 0.5 * vamr;
+    const double el = hl - pl / rl, er = hr - pr / rr;
+    const double acl = sqrt(gamal * pl / rl), acr = sqrt(gamar * pr / rr);
+    const double ulnormal = (sav1 * ul + sav2 * vl), urnormal = (sav1 * ur + sav2 * vr);
+    const double coex = fmax2(fabs(ulnormal) + acl * sav, fabs(urnormal) + acr * sav);
+    const double rul = rl * ulnormal, rur = rr * urnormal;
+    d.Finv[0 * NF + f] = 0.5 * (rul + rur - coex * (rr - rl));
+    d.Finv[1 * NF + f] = 0.5 * (rul * ul + rur * ur + sav1 * (pl + pr) - coex * (rr * ur - rl * ul));
+    d.Finv[2 * NF + f] = 0.5 * (rul * vl + rur * vr + sav2 * (pl + pr) - coex * (rr * vr - rl * vl));
+    d.Finv[3 * NF + f] = 0.5 * (rul * hl + rur * hr - coex * (rr * er - rl * el));
+#pragma unroll
+    for (int k = 0; k < NSP - 1; ++k)
+      d.Finv[(4 + k) * NF + f] = 0.5 * (rul * Yl[k] + rur * Yr[k] - coex * (rr * Yr[k] - rl * Yl[k]));
+  }
+
+  // ---- viscous flux (flux_viscous.f90:25-343)
+  if (VISC) {
+    double pl = uL[0], ul = uL[1], vl = uL[2], tl = uL[3], rl = rl0;
+    double pr, ur, vr, tr;
+    double Yl[NSP], Yr[NSP];
+#pragma unroll
+    for (int k = 0; k < NSP; ++k) Yl[k] = Yl0[k];
+    if (NR >= 0) {
+      pr = uR[0]; ur = uR[1]; vr = uR[2]; tr = uR[3];
+#pragma unroll
+      for (int k = 0; k < NSP; ++k) Yr[k] = Yr0[k];
+    } else if (NR == -3 || NR == -4) {
+      double rr, Cpr, gamar, Rcr;
+      inlet_bc<NSP>(th, NR == -3 ? 0 : 1, pl, pr, ur, vr, tr, rr, Yr, Cpr, gamar, Rcr, err);
+      pl = pr; ul = ur; vl = vr; tl = tr; rl = rr;
+#pragma unroll
+      for (int k = 0; k < NSP; ++k) Yl[k] = Yr[k];
+    } else {
+      if (NR == -1) { ul = 0.; vl = 0.; }
+      else if (NR == -2 || NR == -6 || NR == -7) removedirection(ul, vl, sav1n, sav2n);
+      pr = pl; tr = tl; ur = ul; vr = vl;
+      if (NR == -5) {
+        const double ac = sqrt(gamal0 * pl / rl);
+        const double vn = ul * sav1n + vl * sav2n;
+        if (!(fabs(vn) > ac)) {
+          pr = th.p_out;
+          ur = ul + sav1n * (pl - pr) / (rl * ac);
+          vr = vl + sav2n * (pl - pr) / (rl * ac);
+          const double rrb = rl + (pr - pl) / (ac * ac);
+          tr = pr / (Rl0 * rrb);
+          pl = pr; ul = ur; vl = vr; tl = tr;
+        }
+      } else if (NR == -7) {
+        pr = 2.0e6; tr = 700; ur = -100; vr = 0;
+      }
+#pragma unroll
+      for (int k = 0; k < NSP; ++k) Yr[k] = Yl[k];
+    }
+    (void)rl;
+    const double pp = 0.5 * (pl + pr), uu = 0.5 * (ul + ur), vv = 0.5 * (vl + vr), tem = 0.5 * (tl + tr);
+    double YY[NSP];
+#pragma unroll
+    for (int k = 0; k < NSP; ++k) YY[k] = 0.5 * (Yl[k] + Yr[k]);
+    double Cp, gama, Rcpcv;
+    gas<NSP>(th, YY, tem, Cp, gama, Rcpcv, err);
+    const double rr = pp / (Rcpcv * tem);
+    // face gradient (flux_viscous.f90:201-224), signed zeros of the dropped
+    // g*0.0 basis terms aside
+    double t0[V], t1[V];
+    {
+      const double dxl = d.rinv[NL], dyl = d.rinv[NE + NL];
+#pragma unroll
+      for (int k = 0; k < V; ++k) {
+        t0[k] = d.grad[(2 * k) * NE + NL] * dxl;
+        t1[k] = d.grad[(2 * k + 1) * NE + NL] * dyl;
+      }
+    }
+    if (NR >= 0) {
+      const double dxk = d.fdxk[f], y1 = d.fysn[f], y2 = d.fysn[NF + f];
+      const double dxr = d.rinv[NR], dyr = d.rinv[NE + NR];
+#pragma unroll
+      for (int k = 0; k < V; ++k) {
+        const double du = uR[k] - uL[k];
+        t0[k] = 0.5 * (t0[k] + d.grad[(2 * k) * NE + NR] * dxr) + y1 * du / dxk;
+        t1[k] = 0.5 * (t1[k] + d.grad[(2 * k + 1) * NE + NR] * dyr) + y2 * du / dxk;
+      }
+    }
+    double dudx = t0[1], dudy = t1[1], dvdx = t0[2], dvdy = t1[2], dtdx = t0[3], dtdy = t1[3];
+    double dYdx[NSP], dYdy[NSP];
+#pragma unroll
+    for (int k = 0; k < NSP - 1; ++k) { dYdx[k] = t0[4 + k]; dYdy[k] = t1[4 + k]; }
+    if (NR == -1 || NR == -6) removedirection(dtdx, dtdy, sav1n, sav2n);
+    if (NR == -2) {
+      const double snx = sav1n, sny = sav2n, stx = -sny, sty = snx;
+      removedirection(dtdx, dtdy, snx, sny);
+#pragma unroll
+      for (int k = 0; k < NSP - 1; ++k) removedirection(dYdx[k], dYdy[k], snx, sny);
+      double dutdx = dudx * stx + dvdx * sty, dutdy = dudy * stx + dvdy * sty;
+      double dundx = dudx * snx + dvdx * sny, dundy = dudy * snx + dvdy * sny;
+      removedirection(dutdx, dutdy, snx, sny);
+      removedirection(dundx, dundy, stx, sty);
+      dudx = dutdx * stx + dundx * snx;
+      dudy = dutdy * stx + dundy * snx;
+      dvdx = dutdx * sty + dundx * sny;
+      dvdy = dutdy * sty + dundy * sny;
+    }
+    {
+      double sx = 0.0, sy = 0.0;
+#pragma unroll
+      for (int k = 0; k < NSP - 1; ++k) { sx = sx + dYdx[k]; sy = sy + dYdy[k]; }
+      dYdx[NSP - 1] = -sx;
+      dYdy[NSP - 1] = -sy;
+    }
+    double entha[NSP], Dk[NSP], vmulc, akmu;
+    enthalpy<NSP>(th, tem, entha, err);
+    transport<NSP>(th, tem, YY, vmulc, akmu, err);
+    diffusion<NSP>(th, pp, tem, YY, Dk);
+    double uicx = 0.0, uicy = 0.0;
+#pragma unroll
+    for (int k = 0; k < NSP; ++k) uicx = uicx + Dk[k] * dYdx[k];
+#pragma unroll
+    for (int k = 0; k < NSP; ++k) uicy = uicy + Dk[k] * dYdy[k];
+    const double vlac = -2. / 3. * vmulc;
+    const double div = dudx + dvdy;
+    const double txx = 2. * vmulc * dudx + vlac * div;
+    const double tyy = 2. * vmulc * dvdy + vlac * div;
+    const double txy = vmulc * (dudy + dvdx);
+    double sx = 0.0, sy = 0.0;
+#pragma unroll
+    for (int k = 0; k < NSP; ++k) sx = sx + (Dk[k] * dYdx[k] - YY[k] * uicx) * entha[k];
+#pragma unroll
+    for (int k = 0; k < NSP; ++k) sy = sy + (Dk[k] * dYdy[k] - YY[k] * uicy) * entha[k];
+    const double qx = -akmu * dtdx - rr * sx;
+    const double qy = -akmu * dtdy - rr * sy;
+    const double btx = uu * txx + vv * txy - qx;
+    const double bty = uu * txy + vv * tyy - qy;
+    d.Fvis[0 * NF + f] = -(sav1 * txx + sav2 * txy);
+    d.Fvis[1 * NF + f] = -(sav1 * txy + sav2 * tyy);
+    d.Fvis[2 * NF + f] = -(sav1 * btx + sav2 * bty);
+#pragma unroll
+    for (int k = 0; k < NSP - 1; ++k) {
+      const double spx = rr * (Dk[k] * dYdx[k] - YY[k] * uicx);
+      const double spy = rr * (Dk[k] * dYdy[k] - YY[k] * uicy);
+      d.Fvis[(3 + k) * NF + f] = -(sav1 * spx + sav2 * spy);
+    }
+  }
+  flag(d, err);
+}
+
+// Residual of cell i: inviscid faces, then viscous faces, in NeighF order,
+// then the chemical source (fvm2d.f90:196-224, sourceterm.f90:51).
+template <int NSP>
+__device__ __forceinline__ void gather_residual(const Dev& d, int i, int visc, int comb, double* R) {
+  constexpr int V = 3 + NSP;
+  const int NE = d.NE, NF = d.NF, nf = d.nface[i];
+  const unsigned lb = d.cleft[i];
+#pragma unroll
+  for (int k = 0; k < V; ++k) R[k] = 0.0;
+  for (int q = 0; q < nf; ++q) {
+    const int f = d.cface[q * NE + i];
+    const bool left = (lb >> q) & 1u;
+#pragma unroll
+    for (int k = 0; k < V; ++k) {
+      const double F = d.Finv[k * NF + f];
+      R[k] = left ? R[k] - F : R[k] + F;
+    }
+  }
+  if (visc)
+    for (int q = 0; q < nf; ++q) {
+      const int f = d.cface[q * NE + i];
+      const bool left = (lb >> q) & 1u;
+#pragma unroll
+      for (int k = 1; k < V; ++k) {
+        const double F = d.Fvis[(k - 1) * NF + f];
+        R[k] = left ? R[k] - F : R[k] + F;
+      }
+    }
+  if (comb) {
+#pragma unroll
+    for (int k = 0; k < NSP - 1; ++k) R[4 + k] = R[4 + k] + d.src[k * NE + i];
+  }
+}
+
+template <int NSP>
+__global__ void __launch_bounds__(128) k_gather(const Dev d, int visc, int comb) {
+  constexpr int V = 3 + NSP;
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= d.NE) return;
+  double R[V];
+  gather_residual<NSP>(d, i, visc, comb, R);
+#pragma unroll
+  for (int k = 0; k < V; ++k) d.hWA[k * d.NE + i] = R[k];
+}
+
+// ---------------------------------------------------------------- LU-SGS ---
+// One cell of the forward (FWD) or backward sweep (Time_LUSGS_steady.f90:125-260).
+template <int NSP, bool FWD>
+__global__ void __launch_bounds__(128) k_sweep(const Dev d, const ThermoDev<NSP> th, const int* __restrict__ cells,
+                                               int n, int gather, int visc, int comb) {
+  constexpr int V = 3 + NSP;
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= n) return;
+  const int i = cells[t];
+  const int NE = d.NE, NF = d.NF, nf = d.nface[i];
+  const unsigned lb = d.cleft[i];
+  double R[V], df[V];
+  if (FWD && gather) {
+    gather_residual<NSP>(d, i, visc, comb, R);
+  } else {
+#pragma unroll
+    for (int k = 0; k < V; ++k) R[k] = d.hWA[k * NE + i];
+  }
+#pragma unroll
+  for (int k = 0; k < V; ++k) df[k] = 0.0;
+  for (int q = 0; q < nf; ++q) {
+    const int j = d.cother[q * NE + i];
+    if (j < 0 || (FWD ? !(j < i) : !(j > i))) continue;
+    const int f = d.cface[q * NE + i];
+    double dx = d.fvec[f], dy = d.fvec[NF + f];
+    if (!((lb >> q) & 1u)) { dx = -dx; dy = -dy; }
+    const double pp = d.PA[0 * NE + j], uu = d.PA[1 * NE + j], vv = d.PA[2 * NE + j], tt = d.PA[3 * NE + j];
+    const double rr = d.cst[0 * NE + j], gama = d.cst[1 * NE + j], roe = d.cst[2 * NE + j];
+    const double rou = rr * uu, rov = rr * vv;
+    const double drr = d.hWA[0 * NE + j], dru = d.hWA[1 * NE + j], drv = d.hWA[2 * NE + j],
+                 dre = d.hWA[3 * NE + j];
+    double dry[NSP], s = 0.0;
+#pragma unroll
+    for (int k = 0; k < NSP - 1; ++k) { dry[k] = d.hWA[(4 + k) * NE + j]; s = s + dry[k]; }
+    dry[NSP - 1] = drr - s;
+    const double duu = (dru - uu * drr) / rr;
+    const double dvv = (drv - vv * drr) / rr;
+    double s1 = 0.0, s2 = 0.0;
+#pragma unroll
+    for (int k = 0; k < NSP; ++k) s1 = s1 + d.cst[(3 + k) * NE + j] * dry[k];
+#pragma unroll
+    for (int k = 0; k < NSP; ++k) s2 = s2 + th.R[k] * dry[k];
+    const double dpp =
+        (gama - 1) * (dre - s1 + tt * s2 * gama / (gama - 1) - 0.5 * (dru * uu + duu * rou + drv * vv + dvv * rov));
+    const double unormal = uu * dx + vv * dy;
+    const double dunormal = duu * dx + dvv * dy;
+    const double aF = d.alpaF[f];
+    df[0] = df[0] + 0.5 * (-aF * drr + dru * dx + drv * dy);
+    df[1] = df[1] + 0.5 * (-aF * dru + dru * unormal + rou * dunormal + dpp * dx);
+    df[2] = df[2] + 0.5 * (-aF * drv + drv * unormal + rov * dunormal + dpp * dy);
+    df[3] = df[3] + 0.5 * (-aF * dre + dunormal * (roe + pp) + unormal * (dre + dpp));
+#pragma unroll
+    for (int k = 0; k < NSP - 1; ++k) {
+      const double ry = rr * d.PA[(4 + k) * NE + j];
+      df[4 + k] = df[4 + k] + 0.5 * (-aF * dry[k] + dry[k] * unormal + ry * dunormal);
+    }
+  }
+  const double ddi = d.dd[i];
+#pragma unroll
+  for (int k = 0; k < V; ++k) d.hWA[k * NE + i] = FWD ? (R[k] - df[k]) / ddi : R[k] - df[k] / ddi;
+}
+
+// WA += hWA and update_primitve_variables (update_flow_variables.f90:112-156).
+template <int NSP>
+__global__ void __launch_bounds__(128) k_update(const Dev d, const ThermoDev<NSP> th) {
+  constexpr int V = 3 + NSP;
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= d.NE) return;
+  const int NE = d.NE;
+  unsigned err = 0;
+  double W[V];
+#pragma unroll
+  for (int k = 0; k < V; ++k) {
+    W[k] = d.WA[k * NE + i] + d.hWA[k * NE + i];
+    d.WA[k * NE + i] = W[k];
+  }
+  const double rho = W[0], u = W[1] / rho, v = W[2] / rho;
+  double Y[NSP], s = 0.0;
+#pragma unroll
+  for (int k = 0; k < NSP - 1; ++k) { Y[k] = W[4 + k] / rho; s = s + Y[k]; }
+  Y[NSP - 1] = 1.0 - s;
+  double Rcpcv;
+  const double t = newton_T<NSP>(th, W[3] / rho - 0.5 * (u * u + v * v), Y, d.PA[3 * NE + i], Rcpcv, err);
+  d.PA[0 * NE + i] = rho * Rcpcv * t;
+  d.PA[1 * NE + i] = u;
+  d.PA[2 * NE + i] = v;
+  d.PA[3 * NE + i] = t;
+#pragma unroll
+  for (int k = 0; k < NSP - 1; ++k) d.PA[(4 + k) * NE + i] = Y[k];
+  if (i == 0 && isnan(W[0])) err |= ERR_NAN;
+  flag(d, err);
+}
+
+// ------------------------------------------------------------ utilities ----
+// Residual norms: fixed-shape deterministic reduction (block partials then one
+// block over the partials).  out[k] = sum vol*|hWA_k|, out[V] = max WA_1.
+constexpr int NRM_BLOCKS = 304, NRM_THREADS = 256;
+__global__ void __launch_bounds__(NRM_THREADS) k_norm_partial(const double* __restrict__ hWA,
+                                                              const double* __restrict__ WA,
+                                                              const double* __restrict__ vol, int NE, int V,
+                                                              double* part) {
+  __shared__ double sh[NRM_THREADS];
+  const int per = (NE + NRM_BLOCKS - 1) / NRM_BLOCKS;
+  const int lo = blockIdx.x * per, hi = min(NE, lo + per);
+  for (int k = 0; k <= V; ++k) {
+    double a = (k == V) ? 0.0 : 0.0;
+    for (int i = lo + threadIdx.x; i < hi; i += NRM_THREADS)
+      a = (k == V) ? fmax2(a, WA[i]) : a + vol[i] * fabs(hWA[k * NE + i]);
+    sh[threadIdx.x] = a;
+    __syncthreads();
+    for (int w = NRM_THREADS / 2; w > 0; w >>= 1) {
+      if (threadIdx.x < w) sh[threadIdx.x] = (k == V) ? fmax2(sh[threadIdx.x], sh[threadIdx.x + w])
+                                                      : sh[threadIdx.x] + sh[threadIdx.x + w];
+      __syncthreads();
+    }
+    if (threadIdx.x == 0) part[k * NRM_BLOCKS + blockIdx.x] = sh[0];
+    __syncthreads();
+  }
+}
+__global__ void k_norm_final(const double* part, int V, double total_volume, double* out) {
+  const int k = threadIdx.x;
+  if (k > V) return;
+  double a = 0.0;
+  for (int b = 0; b < NRM_BLOCKS; ++b) a = (k == V) ? fmax2(a, part[k * NRM_BLOCKS + b]) : a + part[k * NRM_BLOCKS + b];
+  out[k] = (k == V) ? a : a / total_volume;
+}
+
+// Fortran (V,N) <-> device (V planes of N)
+__global__ void k_aos_to_soa(const double* __restrict__ a, double* __restrict__ s, int N, int V) {
+  const long t = (long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= (long)N * V) return;
+  const int i = (int)(t / V), k = (int)(t % V);
+  s[(long)k * N + i] = a[t];
+}
+__global__ void k_soa_to_aos(const double* __restrict__ s, double* __restrict__ a, int N, int V) {
+  const long t = (long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= (long)N * V) return;
+  const int i = (int)(t / V), k = (int)(t % V);
+  a[t] = s[(long)k * N + i];
+}
+
+}  // namespace rc
+
+// ======================================================== host context =====
+using namespace rc;
+
+struct rc_ctx {
+  int NE = 0, NF = 0, NG = 0, NSP = 0, V = 0;
+  int visc = 0, comb = 0, limit = 0, precision = 0, device = 0;
+  double total_volume = 0;
+  cudaStream_t stream = nullptr;
+  bool own_stream = false;
+  Dev d{};
+  std::vector<void*> allocs;
+  std::vector<char> thermo;  // ThermoDev<NSP> bytes
+  int* fwd_cells = nullptr;
+  int* bwd_cells = nullptr;
+  std::vector<int> fwd_off, bwd_off;
+  double* norm_part = nullptr;
+  double* norm_out = nullptr;
+  double* staging = nullptr;  // (V*max(NE,NF,NG)) for layout conversion
+  cudaGraphExec_t graph = nullptr;
+  long long graph_kernels = 0;
+  long long launches = 0;
+  std::string err;
+  int latched = 0;
+};
+
+namespace {
+
+int cuda_fail(rc_ctx* c, cudaError_t e, const char* what) {
+  if (e == cudaSuccess) return RC_OK;
+  if (c) c->err = std::string(what) + ": " + cudaGetErrorString(e);
+  return RC_ERR_CUDA;
+}
+#define RC_CU(call)                                         \
+  do {                                                      \
+    cudaError_t e_ = (call);                                \
+    if (e_ != cudaSuccess) return cuda_fail(c, e_, #call);  \
+  } while (0)
+
+template <class T>
+int dev_upload(rc_ctx* c, const std::vector<T>& h, T** out) {
+  void* p = nullptr;
+  size_t bytes = std::max<size_t>(h.size(), 1) * sizeof(T);
+  RC_CU(cudaMalloc(&p, bytes));
+  c->allocs.push_back(p);
+  if (!h.empty()) RC_CU(cudaMemcpy(p, h.data(), h.size() * sizeof(T), cudaMemcpyHostToDevice));
+  *out = static_cast<T*>(p);
+  return RC_OK;
+}
+int dev_zeros(rc_ctx* c, size_t n, double** out) {
+  void* p = nullptr;
+  RC_CU(cudaMalloc(&p, std::max<size_t>(n, 1) * sizeof(double)));
+  c->allocs.push_back(p);
+  RC_CU(cudaMemset(p, 0, std::max<size_t>(n, 1) * sizeof(double)));
+  *out = static_cast<double*>(p);
+  return RC_OK;
+}
+
+double hmax(double a, double b) { return (b > a) ? b : a; }
+
+template <int NSP>
+void fill_thermo(const rc_thermo* t, const rc_config* g, ThermoDev<NSP>& th) {
+  std::memset(&th, 0, sizeof(th));
+  for (int i = 0; i < NSP; ++i) { th.R[i] = t->R_species[i]; th.mw[i] = t->mole_weight[i]; }
+  th.Rconstant = t->Rconstant;
+  th.tlo = t->thermo_lowest_tem; th.tcrit = t->thermo_critical_tem; th.thi = t->thermo_highest_tem;
+  for (int j = 0; j < 7; ++j)
+    for (int i = 0; i < NSP; ++i) {
+      th.cl[j][i] = t->low_coef_Cp_species[j + 7 * i];
+      th.ch[j][i] = t->high_coef_Cp_species[j + 7 * i];
+    }
+  for (int i = 0; i < NSP; ++i) { th.b1l[i] = t->low_enthalpy_b1[i]; th.b1h[i] = t->high_enthalpy_b1[i]; }
+  th.trlo = t->transport_lowest_tem; th.trcrit = t->transport_critical_tem; th.trhi = t->transport_highest_tem;
+  for (int a = 0; a < 4; ++a)
+    for (int i = 0; i < NSP; ++i) {
+      th.mu[0][a][i] = t->mu_K[a][i];
+      th.mu[1][a][i] = t->mu_K[4 + a][i];
+      th.kk[0][a][i] = t->mu_K[8 + a][i];
+      th.kk[1][a][i] = t->mu_K[12 + a][i];
+    }
+  for (int i = 0; i < NSP; ++i)
+    for (int j = 0; j < NSP; ++j) {
+      const double mi = t->mole_weight[i], mj = t->mole_weight[j];
+      th.wc[i][j] = std::pow(mj / mi, 0.25);
+      th.wd[i][j] = std::sqrt(1. + mi / mj);
+      th.dlj[i][j] = std::sqrt(t->LJ_energy[i] * t->LJ_energy[j]);
+      th.dmw[i][j] = std::sqrt(2. / (1. / mi + 1. / mj) * 1000);
+      const double cd = 0.5 * (t->collision_diameter[i] + t->collision_diameter[j]);
+      th.dcd[i][j] = cd * cd;
+    }
+  th.model = t->code_chemical_model;
+  th.Af = t->Af_react; th.E = t->E_react;
+  for (int k = 0; k < NSP; ++k)
+    th.prodc[k] = 1000 * t->mole_weight[k] * (t->coef_r_react[k] - t->coef_f_react[k]);
+  th.mw1000[0] = t->mole_weight[0] * 1000;
+  th.mw1000[1] = t->mole_weight[NSP > 1 ? 1 : 0] * 1000;
+  for (int k = 0; k < NSP; ++k) { th.inY[0][k] = t->oxidizer_mass_fraction[k]; th.inY[1][k] = t->fuel_mass_fraction[k]; }
+  th.inT[0] = t->oxidizer_temp_in; th.inMflow[0] = t->oxidizer_mass_flow;
+  th.inT[1] = t->fuel_temp_in; th.inMflow[1] = t->fuel_mass_flow;
+  th.p_out = g->p_out; th.cfl = g->cfl;
+}
+
+inline unsigned blocks(long n, int t) { return (unsigned)((n + t - 1) / t); }
+
+template <int NSP>
+const ThermoDev<NSP>& TH(const rc_ctx* c) { return *reinterpret_cast<const ThermoDev<NSP>*>(c->thermo.data()); }
+
+// --- the pieces of one iteration, enqueued on c->stream
+template <int NSP>
+void q_timestep_face(rc_ctx* c) {
+  if (c->visc) k_ts_face<NSP, true><<<blocks(c->NF, 128), 128, 0, c->stream>>>(c->d, TH<NSP>(c));
+  else k_ts_face<NSP, false><<<blocks(c->NF, 128), 128, 0, c->stream>>>(c->d, TH<NSP>(c));
+  c->launches++;
+}
+template <int NSP>
+void q_cell(rc_ctx* c, int do_step, int do_recon) {
+  k_cell<NSP><<<blocks(c->NE, 128), 128, 0, c->stream>>>(c->d, TH<NSP>(c), do_step, do_recon, c->limit, c->comb,
+                                                          c->visc);
+  c->launches++;
+}
+template <int NSP>
+void q_face_flux(rc_ctx* c) {
+  if (c->visc) k_face_flux<NSP, true><<<blocks(c->NF, 128), 128, 0, c->stream>>>(c->d, TH<NSP>(c));
+  else k_face_flux<NSP, false><<<blocks(c->NF, 128), 128, 0, c->stream>>>(c->d, TH<NSP>(c));
+  c->launches++;
+}
+template <int NSP>
+void q_sweeps(rc_ctx* c, int gather) {
+  for (size_t l = 0; l + 1 < c->fwd_off.size(); ++l) {
+    const int n = c->fwd_off[l + 1] - c->fwd_off[l];
+    k_sweep<NSP, true><<<blocks(n, 128), 128, 0, c->stream>>>(c->d, TH<NSP>(c), c->fwd_cells + c->fwd_off[l], n,
+                                                              gather, c->visc, c->comb);
+    c->launches++;
+  }
+  for (size_t l = 0; l + 1 < c->bwd_off.size(); ++l) {
+    const int n = c->bwd_off[l + 1] - c->bwd_off[l];
+    k_sweep<NSP, false><<<blocks(n, 128), 128, 0, c->stream>>>(c->d, TH<NSP>(c), c->bwd_cells + c->bwd_off[l], n,
+                                                               0, c->visc, c->comb);
+    c->launches++;
+  }
+  k_update<NSP><<<blocks(c->NE, 128), 128, 0, c->stream>>>(c->d, TH<NSP>(c));
+  c->launches++;
+}
+template <int NSP>
+void q_gather(rc_ctx* c) {
+  k_gather<NSP><<<blocks(c->NE, 128), 128, 0, c->stream>>>(c->d, c->visc, c->comb);
+  c->launches++;
+}
+template <int NSP>
+void q_stage(rc_ctx* c) {
+  q_timestep_face<NSP>(c);
+  q_cell<NSP>(c, 1, 1);
+  q_face_flux<NSP>(c);
+  q_sweeps<NSP>(c, 1);
+}
+
+#define RC_DISPATCH(c, fn, ...)                  \
+  switch ((c)->NSP) {                            \
+    case 1: fn<1>(__VA_ARGS__); break;           \
+    case 4: fn<4>(__VA_ARGS__); break;           \
+    default: break;                              \
+  }
+
+int check_launch(rc_ctx* c, const char* what) {
+  cudaError_t e = cudaGetLastError();
+  return cuda_fail(c, e, what);
+}
+
+int latch(rc_ctx* c) {
+  unsigned h = 0;
+  RC_CU(cudaMemcpyAsync(&h, c->d.err, sizeof(unsigned), cudaMemcpyDeviceToHost, c->stream));
+  RC_CU(cudaStreamSynchronize(c->stream));
+  c->latched |= (int)h;
+  if (h && c->err.empty()) c->err = "device-detected stop condition, code " + std::to_string(h);
+  return c->latched;
+}
+
+}  // namespace
+
+// ================================================================ C ABI =====
+extern "C" {
+
+int rc_init(const rc_mesh* m, const rc_thermo* t, const rc_config* g, rc_ctx** out) {
+  if (!m || !t || !g || !out) return RC_ERR_ARG;
+  *out = nullptr;
+  rc_ctx* c = new rc_ctx();
+  auto bail = [&](int code, const std::string& msg) {
+    std::fprintf(stderr, "rc_init: %s\n", msg.c_str());
+    rc_finalize(c);
+    return code;
+  };
+  c->NE = m->NE; c->NF = m->NF; c->NG = m->Nghostcell; c->NSP = t->Nsp; c->V = 3 + t->Nsp;
+  c->visc = g->IfViscous != 0; c->comb = g->If_turn_on_combustion != 0; c->limit = g->limit_ID;
+  c->precision = g->precision; c->device = g->device; c->total_volume = m->total_volume;
+  if (c->NSP != 1 && c->NSP != 4) return bail(RC_ERR_ARG, "Nsp must be 1 or 4 in this build");
+  if (c->comb && c->NSP < 2) return bail(RC_ERR_ARG, "combustion needs at least two species");
+  if (t->order_of_cp_polynomial != 7) return bail(RC_ERR_ARG, "order_of_cp_polynomial must be 7");
+  if (m->MaxNei > MAXF) return bail(RC_ERR_ARG, "cells with more than 4 faces");
+  if (g->precision != RC_PREC_FP64) return bail(RC_ERR_ARG, "precision mode not available in this build");
+  if (cudaSetDevice(g->device) != cudaSuccess) return bail(RC_ERR_CUDA, "cudaSetDevice failed");
+  if (cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking) != cudaSuccess)
+    return bail(RC_ERR_CUDA, "cudaStreamCreate failed");
+  c->own_stream = true;
+  const int NE = m->NE, NF = m->NF, NG = m->Nghostcell, M = m->MaxNei, V = c->V;
+  const double small = 1.0e-16;
+  auto C2 = [&](const double* a, int d, int i) { return a[(size_t)(d - 1) + 2 * (size_t)(i - 1)]; };
+
+  // ---- faces
+  std::vector<int> fNL(NF), fNR(NF);
+  std::vector<double> fvec(2 * (size_t)NF), fsav(NF), fsn(2 * (size_t)NF), fss(NF), fs2(NF), fvL(2 * (size_t)NF),
+      fvR(2 * (size_t)NF), fdxk(NF), fysn(2 * (size_t)NF);
+  for (int f = 1; f <= NF; ++f) {
+    const int L = m->Neighbor[2 * (f - 1)], R = m->Neighbor[2 * (f - 1) + 1];
+    if (m->FProperty[f - 1] == 100) return bail(RC_ERR_ARG, "periodic faces are not supported");
+    if (L < 1 || L > NE || R > NE) return bail(RC_ERR_ARG, "Neighbor out of range");
+    const int fi = f - 1;
+    fNL[fi] = L - 1;
+    fNR[fi] = R > 0 ? R - 1 : R;
+    const double dx = C2(m->VECX, 1, f), dy = C2(m->VECX, 2, f);
+    fvec[fi] = dx; fvec[NF + fi] = dy;
+    const double sav = hmax(std::sqrt(dx * dx + dy * dy), small);
+    fsav[fi] = sav;
+    fsn[fi] = dx / sav; fsn[NF + fi] = dy / sav;
+    fss[fi] = std::sqrt(dx * dx + dy * dy);
+    fs2[fi] = dx * dx + dy * dy;
+    const int n1 = m->FNode[2 * (f - 1)], n2 = m->FNode[2 * (f - 1) + 1];
+    // Gauss point xy = Coor(n1) + wxx*(Coor(n2)-Coor(n1)), wxx = 0.5 (initParam.f90:169)
+    const double x = C2(m->COOR, 1, n1) + 0.5 * (C2(m->COOR, 1, n2) - C2(m->COOR, 1, n1));
+    const double y = C2(m->COOR, 2, n1) + 0.5 * (C2(m->COOR, 2, n2) - C2(m->COOR, 2, n1));
+    fvL[fi] = (x - C2(m->CELLXY, 1, L)) / C2(m->reflen, 1, L);
+    fvL[NF + fi] = (y - C2(m->CELLXY, 2, L)) / C2(m->reflen, 2, L);
+    if (R > 0) {
+      fvR[fi] = (x - (C2(m->CELLXY, 1, R) - C2(m->SideOfs, 1, f))) / C2(m->reflen, 1, R);
+      fvR[NF + fi] = (y - (C2(m->CELLXY, 2, R) - C2(m->SideOfs, 2, f))) / C2(m->reflen, 2, R);
+      const double dlrx = C2(m->CELLXY, 1, L) - (C2(m->CELLXY, 1, R) - C2(m->SideOfs, 1, f));
+      const double dlry = C2(m->CELLXY, 2, L) - (C2(m->CELLXY, 2, R) - C2(m->SideOfs, 2, f));
+      fdxk[fi] = std::fabs(dlrx * fsn[fi] + dlry * fsn[NF + fi]);
+    }
+    const double yita = 4. / 3;
+    fysn[fi] = yita * fsn[fi];
+    fysn[NF + fi] = yita * fsn[NF + fi];
+  }
+  // ---- cells
+  std::vector<unsigned char> nface(NE), cleft(NE, 0), nnei(NE), ngh(NE);
+  std::vector<int> cface(4 * (size_t)NE, 0), cother(4 * (size_t)NE, -1), cnei(4 * (size_t)NE, 0), cgh(4 * (size_t)NE, 0);
+  std::vector<double> vol(NE), rinv(2 * (size_t)NE), wd(4 * (size_t)NE, 0.0), am(8 * (size_t)NE, 0.0),
+      lvvh(8 * (size_t)NE, 0.0);
+  for (int i = 1; i <= NE; ++i) {
+    const int ii = i - 1, kf = m->KFace[ii];
+    if (kf < 3 || kf > 4) return bail(RC_ERR_ARG, "KFace must be 3 or 4");
+    nface[ii] = (unsigned char)kf;
+    vol[ii] = m->VOL[ii];
+    rinv[ii] = 1. / C2(m->reflen, 1, i);
+    rinv[NE + ii] = 1. / C2(m->reflen, 2, i);
+    for (int q = 0; q < kf; ++q) {
+      const int f = m->NeighF[4 * (size_t)ii + q];
+      if (f < 1 || f > NF) return bail(RC_ERR_ARG, "NeighF out of range");
+      cface[(size_t)q * NE + ii] = f - 1;
+      const int L = m->Neighbor[2 * (f - 1)], R = m->Neighbor[2 * (f - 1) + 1];
+      if (L == i) {
+        cleft[ii] |= (unsigned char)(1u << q);
+        cother[(size_t)q * NE + ii] = R > 0 ? R - 1 : -1;
+      } else {
+        cother[(size_t)q * NE + ii] = L - 1;
+      }
+      const int n1 = m->FNode[2 * (f - 1)], n2 = m->FNode[2 * (f - 1) + 1];
+      const double x = 0.5 * (C2(m->COOR, 1, n1) + C2(m->COOR, 1, n2));
+      const double y = 0.5 * (C2(m->COOR, 2, n1) + C2(m->COOR, 2, n2));
+      lvvh[(size_t)(2 * q) * NE + ii] = (x - C2(m->CELLXY, 1, i)) / C2(m->reflen, 1, i);
+      lvvh[(size_t)(2 * q + 1) * NE + ii] = (y - C2(m->CELLXY, 2, i)) / C2(m->reflen, 2, i);
+    }
+    const int nn = m->Neigh[ii], ng = m->Num_ghostcell[ii];
+    if (nn + ng != kf) return bail(RC_ERR_ARG, "Neigh + Num_ghostcell /= KFace");
+    nnei[ii] = (unsigned char)nn;
+    ngh[ii] = (unsigned char)ng;
+    for (int q = 0; q < nn; ++q) {
+      const int j = m->NeighC[(size_t)(M + 1) * ii + q + 1];
+      if (j < 1 || j > NE) return bail(RC_ERR_ARG, "NeighC out of range");
+      cnei[(size_t)q * NE + ii] = j - 1;
+    }
+    for (int q = 0; q < ng; ++q) {
+      const int gj = m->Ghostcell[(size_t)M * ii + q];
+      if (gj < 1 || gj > NG || m->Hostcell[gj - 1] != i) return bail(RC_ERR_ARG, "Ghostcell/Hostcell mismatch");
+      cgh[(size_t)q * NE + ii] = gj - 1;
+    }
+    for (int q = 0; q < kf; ++q) {
+      wd[(size_t)q * NE + ii] = m->wdis[(size_t)M * ii + q];
+      am[(size_t)(2 * q) * NE + ii] = m->AMLS[(size_t)2 * M * ii + 2 * q];
+      am[(size_t)(2 * q + 1) * NE + ii] = m->AMLS[(size_t)2 * M * ii + 2 * q + 1];
+    }
+  }
+  // ---- ghosts: unit normal of the ghost face (update_flow_variables.f90:222-236)
+  std::vector<int> gtype(NG);
+  std::vector<double> gsn(2 * (size_t)NG);
+  for (int j = 0; j < NG; ++j) {
+    gtype[j] = m->BCtype_Ghostcell[j];
+    const double* G = &m->Coor_Ghostnode[8 * (size_t)j];
+    const double sav1 = G[3] - G[1];
+    const double sav2 = -(G[2] - G[0]);
+    const double sav = hmax(std::sqrt(sav1 * sav1 + sav2 * sav2), small);
+    gsn[j] = sav1 / sav;
+    gsn[NG + j] = sav2 / sav;
+  }
+  // ---- LU-SGS levels over the reference cell order
+  std::vector<int> lf(NE, 0), lbk(NE, 0);
+  int mf = 0, mb = 0;
+  for (int i = 0; i < NE; ++i) {
+    int l = 0;
+    for (int q = 0; q < nface[i]; ++q) {
+      const int j = cother[(size_t)q * NE + i];
+      if (j >= 0 && j < i) l = std::max(l, lf[j] + 1);
+    }
+    lf[i] = l; mf = std::max(mf, l);
+  }
+  for (int i = NE - 1; i >= 0; --i) {
+    int l = 0;
+    for (int q = 0; q < nface[i]; ++q) {
+      const int j = cother[(size_t)q * NE + i];
+      if (j > i) l = std::max(l, lbk[j] + 1);
+    }
+    lbk[i] = l; mb = std::max(mb, l);
+  }
+  auto group = [&](const std::vector<int>& lev, int mx, std::vector<int>& cells, std::vector<int>& off) {
+    off.assign(mx + 2, 0);
+    for (int i = 0; i < NE; ++i) off[lev[i] + 1]++;
+    for (int l = 0; l <= mx; ++l) off[l + 1] += off[l];
+    cells.assign(NE, 0);
+    std::vector<int> p(off.begin(), off.end() - 1);
+    for (int i = 0; i < NE; ++i) cells[p[lev[i]]++] = i;
+  };
+  std::vector<int> fc, bc;
+  group(lf, mf, fc, c->fwd_off);
+  group(lbk, mb, bc, c->bwd_off);
+
+  // ---- thermo tables
+  if (c->NSP == 1) {
+    c->thermo.resize(sizeof(ThermoDev<1>));
+    fill_thermo<1>(t, g, *reinterpret_cast<ThermoDev<1>*>(c->thermo.data()));
+  } else {
+    c->thermo.resize(sizeof(ThermoDev<4>));
+    fill_thermo<4>(t, g, *reinterpret_cast<ThermoDev<4>*>(c->thermo.data()));
+  }
+
+  // ---- upload
+  Dev& d = c->d;
+  d.NE = NE; d.NF = NF; d.NG = NG;
+  int st = 0;
+  double* p;
+  unsigned char* u8;
+  int* i32;
+  st |= dev_upload(c, vol, &p); d.vol = p;
+  st |= dev_upload(c, rinv, &p); d.rinv = p;
+  st |= dev_upload(c, nface, &u8); d.nface = u8;
+  st |= dev_upload(c, cleft, &u8); d.cleft = u8;
+  st |= dev_upload(c, cface, &i32); d.cface = i32;
+  st |= dev_upload(c, cother, &i32); d.cother = i32;
+  st |= dev_upload(c, nnei, &u8); d.nnei = u8;
+  st |= dev_upload(c, cnei, &i32); d.cnei = i32;
+  st |= dev_upload(c, ngh, &u8); d.ngh = u8;
+  st |= dev_upload(c, cgh, &i32); d.cgh = i32;
+  st |= dev_upload(c, wd, &p); d.wdis = p;
+  st |= dev_upload(c, am, &p); d.amls = p;
+  st |= dev_upload(c, lvvh, &p); d.lvvh = p;
+  st |= dev_upload(c, fNL, &i32); d.fNL = i32;
+  st |= dev_upload(c, fNR, &i32); d.fNR = i32;
+  st |= dev_upload(c, fvec, &p); d.fvec = p;
+  st |= dev_upload(c, fsav, &p); d.fsav = p;
+  st |= dev_upload(c, fsn, &p); d.fsn = p;
+  st |= dev_upload(c, fss, &p); d.fss = p;
+  st |= dev_upload(c, fs2, &p); d.fs2 = p;
+  st |= dev_upload(c, fvL, &p); d.fvL = p;
+  st |= dev_upload(c, fvR, &p); d.fvR = p;
+  st |= dev_upload(c, fdxk, &p); d.fdxk = p;
+  st |= dev_upload(c, fysn, &p); d.fysn = p;
+  st |= dev_upload(c, gtype, &i32); d.gtype = i32;
+  st |= dev_upload(c, gsn, &p); d.gsn = p;
+  st |= dev_upload(c, fc, &c->fwd_cells);
+  st |= dev_upload(c, bc, &c->bwd_cells);
+  st |= dev_zeros(c, (size_t)V * NE, &d.PA);
+  st |= dev_zeros(c, (size_t)V * NE, &d.WA);
+  st |= dev_zeros(c, (size_t)V * NE, &d.hWA);
+  st |= dev_zeros(c, (size_t)2 * V * NE, &d.grad);
+  st |= dev_zeros(c, (size_t)V * std::max(NG, 1), &d.GPA);
+  st |= dev_zeros(c, (size_t)NE, &d.step);
+  st |= dev_zeros(c, (size_t)NE, &d.dd);
+  st |= dev_zeros(c, (size_t)(3 + c->NSP) * NE, &d.cst);
+  st |= dev_zeros(c, (size_t)std::max(c->NSP - 1, 1) * NE, &d.src);
+  st |= dev_zeros(c, (size_t)NF, &d.alpa);
+  st |= dev_zeros(c, (size_t)NF, &d.visL);
+  st |= dev_zeros(c, (size_t)NF, &d.visR);
+  st |= dev_zeros(c, (size_t)NF, &d.alpaF);
+  st |= dev_zeros(c, (size_t)V * NF, &d.Finv);
+  st |= dev_zeros(c, (size_t)(V - 1) * NF, &d.Fvis);
+  st |= dev_zeros(c, (size_t)(V + 1) * NRM_BLOCKS, &c->norm_part);
+  st |= dev_zeros(c, (size_t)(V + 1), &c->norm_out);
+  st |= dev_zeros(c, (size_t)2 * V * std::max(std::max(NE, NF), NG), &c->staging);
+  double* e;
+  st |= dev_zeros(c, 1, &e);
+  d.err = reinterpret_cast<unsigned*>(e);
+  if (st) return bail(st, c->err);
+  *out = c;
+  return RC_OK;
+}
+
+int rc_finalize(rc_ctx* c) {
+  if (!c) return RC_OK;
+  if (c->graph) cudaGraphExecDestroy(c->graph);
+  for (void* p : c->allocs) cudaFree(p);
+  if (c->own_stream && c->stream) cudaStreamDestroy(c->stream);
+  delete c;
+  return RC_OK;
+}
+
+int rc_set_stream(rc_ctx* c, void* s) {
+  if (!c) return RC_ERR_ARG;
+  if (c->graph) { cudaGraphExecDestroy(c->graph); c->graph = nullptr; }
+  if (c->own_stream && c->stream) cudaStreamDestroy(c->stream);
+  c->stream = static_cast<cudaStream_t>(s);
+  c->own_stream = false;
+  return RC_OK;
+}
+void* rc_get_stream(rc_ctx* c) { return c ? (void*)c->stream : nullptr; }
+
+static int put_soa(rc_ctx* c, const double* host, double* dst, int N, int V) {
+  RC_CU(cudaMemcpyAsync(c->staging, host, sizeof(double) * (size_t)N * V, cudaMemcpyHostToDevice, c->stream));
+  k_aos_to_soa<<<blocks((long)N * V, 256), 256, 0, c->stream>>>(c->staging, dst, N, V);
+  c->launches++;
+  return check_launch(c, "k_aos_to_soa");
+}
+static int get_soa(rc_ctx* c, const double* src, double* host, int N, int V) {
+  k_soa_to_aos<<<blocks((long)N * V, 256), 256, 0, c->stream>>>(src, c->staging, N, V);
+  c->launches++;
+  RC_CU(cudaMemcpyAsync(host, c->staging, sizeof(double) * (size_t)N * V, cudaMemcpyDeviceToHost, c->stream));
+  RC_CU(cudaStreamSynchronize(c->stream));
+  return check_launch(c, "k_soa_to_aos");
+}
+
+int rc_set_state(rc_ctx* c, const double* PA, const double* WA) {
+  if (!c) return RC_ERR_ARG;
+  int st = 0;
+  if (PA) st |= put_soa(c, PA, c->d.PA, c->NE, c->V);
+  if (WA) st |= put_soa(c, WA, c->d.WA, c->NE, c->V);
+  return st;
+}
+int rc_get_state(rc_ctx* c, double* PA, double* WA) {
+  if (!c) return RC_ERR_ARG;
+  int st = 0;
+  if (PA) st |= get_soa(c, c->d.PA, PA, c->NE, c->V);
+  if (WA) st |= get_soa(c, c->d.WA, WA, c->NE, c->V);
+  return st ? st : latch(c);
+}
+
+static int array_desc(rc_ctx* c, const std::string& s, double** ptr, int* N, int* V, int* grad) {
+  *grad = 0;
+  if (s == "PA") { *ptr = c->d.PA; *N = c->NE; *V = c->V; }
+  else if (s == "WA") { *ptr = c->d.WA; *N = c->NE; *V = c->V; }
+  else if (s == "hWA") { *ptr = c->d.hWA; *N = c->NE; *V = c->V; }
+  else if (s == "GradC") { *ptr = c->d.grad; *N = c->NE; *V = 2 * c->V; *grad = 1; }
+  else if (s == "GPA") { *ptr = c->d.GPA; *N = c->NG; *V = c->V; }
+  else if (s == "alpaF") { *ptr = c->d.alpaF; *N = c->NF; *V = 1; }
+  else if (s == "step") { *ptr = c->d.step; *N = c->NE; *V = 1; }
+  else return RC_ERR_ARG;
+  return RC_OK;
+}
+int rc_get_array(rc_ctx* c, const char* name, double* out) {
+  if (!c || !name || !out) return RC_ERR_ARG;
+  double* p; int N, V, gr;
+  if (array_desc(c, name, &p, &N, &V, &gr)) return RC_ERR_ARG;
+  int st = get_soa(c, p, out, N, V);  // GradC(2,NVar,NE): planes (2k+r) are the fastest (V=2*NVar) index
+  return st ? st : latch(c);
+}
+int rc_set_array(rc_ctx* c, const char* name, const double* in) {
+  if (!c || !name || !in) return RC_ERR_ARG;
+  double* p; int N, V, gr;
+  if (array_desc(c, name, &p, &N, &V, &gr)) return RC_ERR_ARG;
+  if (c->graph) { cudaGraphExecDestroy(c->graph); c->graph = nullptr; }
+  return put_soa(c, in, p, N, V);
+}
+
+#define RC_NSP_OK(c) \
+  if (!(c)) return RC_ERR_ARG;
+
+int rc_timestep(rc_ctx* c) {
+  RC_NSP_OK(c);
+  RC_DISPATCH(c, q_timestep_face, c);
+  RC_DISPATCH(c, q_cell, c, 1, 0);
+  return check_launch(c, "rc_timestep");
+}
+int rc_reconstruction(rc_ctx* c) {
+  RC_NSP_OK(c);
+  RC_DISPATCH(c, q_cell, c, 0, 1);
+  return check_launch(c, "rc_reconstruction");
+}
+int rc_flux_sourceterm(rc_ctx* c) {
+  RC_NSP_OK(c);
+  RC_DISPATCH(c, q_face_flux, c);
+  RC_DISPATCH(c, q_gather, c);
+  return check_launch(c, "rc_flux_sourceterm");
+}
+int rc_lusgs_steady(rc_ctx* c) {
+  RC_NSP_OK(c);
+  RC_DISPATCH(c, q_sweeps, c, 0);
+  return check_launch(c, "rc_lusgs_steady");
+}
+int rc_lusgs_stage(rc_ctx* c, int istep) {
+  (void)istep;
+  RC_NSP_OK(c);
+  if (!c->graph) {
+    cudaGraph_t gph;
+    const long long before = c->launches;
+    RC_CU(cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal));
+    RC_DISPATCH(c, q_stage, c);
+    cudaError_t e = cudaStreamEndCapture(c->stream, &gph);
+    if (e != cudaSuccess) return cuda_fail(c, e, "capture of lu_sgs_stage");
+    c->graph_kernels = c->launches - before;
+    c->launches = before;
+    e = cudaGraphInstantiate(&c->graph, gph, 0);
+    cudaGraphDestroy(gph);
+    if (e != cudaSuccess) return cuda_fail(c, e, "cudaGraphInstantiate");
+  }
+  RC_CU(cudaGraphLaunch(c->graph, c->stream));
+  c->launches += c->graph_kernels;
+  return RC_OK;
+}
+
+int rc_sync(rc_ctx* c) {
+  if (!c) return RC_ERR_ARG;
+  RC_CU(cudaStreamSynchronize(c->stream));
+  return latch(c);
+}
+
+int rc_residual(rc_ctx* c, double* res, double* romax) {
+  if (!c || !res || !romax) return RC_ERR_ARG;
+  k_norm_partial<<<NRM_BLOCKS, NRM_THREADS, 0, c->stream>>>(c->d.hWA, c->d.WA, c->d.vol, c->NE, c->V, c->norm_part);
+  k_norm_final<<<1, 32, 0, c->stream>>>(c->norm_part, c->V, c->total_volume, c->norm_out);
+  c->launches += 2;
+  std::vector<double> h(c->V + 1);
+  RC_CU(cudaMemcpyAsync(h.data(), c->norm_out, sizeof(double) * (c->V + 1), cudaMemcpyDeviceToHost, c->stream));
+  RC_CU(cudaStreamSynchronize(c->stream));
+  for (int k = 0; k < c->V; ++k) res[k] = h[k];
+  *romax = h[c->V];
+  int st = check_launch(c, "rc_residual");
+  return st ? st : latch(c);
+}
+
+int rc_stats(rc_ctx* c, long long* launches, int* fwd, int* bwd) {
+  if (!c) return RC_ERR_ARG;
+  if (launches) *launches = c->launches;
+  if (fwd) *fwd = (int)c->fwd_off.size() - 1;
+  if (bwd) *bwd = (int)c->bwd_off.size() - 1;
+  return RC_OK;
+}
+
+const char* rc_last_error(rc_ctx* c) { return c ? c->err.c_str() : "no context"; }
+
+}  // extern "C"

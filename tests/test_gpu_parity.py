@@ -1,0 +1,139 @@
+"""GPU parity of the plain FP64 path against the CPU oracle (needs a GB300).
+
+Tolerances: the FP64 kernels keep the reference's operation order with FMA
+contraction off, so +,-,*,/ and sqrt round exactly as on the CPU; exp, log and
+pow come from the CUDA math library and may differ from glibc by an ulp or two.
+Hence: a single subroutine agrees to 1e-12 relative L-infinity per field (the
+inviscid perfect-gas time step, which needs none of those functions, is
+bit-exact), and after 100 iterations the state agrees to 1e-9 relative
+L-infinity per field, the bar of the reference comparison.
+"""
+import numpy as np
+import pytest
+
+import oracle
+import rocketcombustor_gb300 as rc
+from conftest import make_case
+
+pytestmark = pytest.mark.gpu
+
+ONE_CALL_RTOL = 1e-12
+ITER_RTOL = 1e-9
+
+
+def rel_linf(a, b):
+    """max |a-b| / max |b| per trailing column (per field)."""
+    a = np.asarray(a, dtype=np.float64)
+    b = np.asarray(b, dtype=np.float64)
+    a2 = a.reshape(a.shape[0], -1) if a.ndim > 1 else a[:, None]
+    b2 = b.reshape(b.shape[0], -1) if b.ndim > 1 else b[:, None]
+    den = np.maximum(np.abs(b2).max(axis=0), 1e-300)
+    return (np.abs(a2 - b2).max(axis=0) / den)
+
+
+def solver_and_oracle(d, threads=4):
+    c = rc.Case(d)
+    s = rc.Solver(c)
+    o = oracle.Oracle(d, threads=threads)
+    return c, s, o
+
+
+@pytest.mark.parametrize("name", ["t1", "t2"])
+def test_subroutines_match_oracle(case_root, name):
+    d = make_case(case_root, name)
+    c, s, o = solver_and_oracle(d)
+    s.timestep(); o.call("timestep")
+    r = rel_linf(s.get_array("alpaF"), o.array("alpaF")).max()
+    if name == "t1":
+        assert np.array_equal(s.get_array("alpaF"), o.array("alpaF"))
+        assert np.array_equal(s.get_array("step"), o.array("step"))
+    assert r <= ONE_CALL_RTOL
+    assert rel_linf(s.get_array("step"), o.array("step")).max() <= ONE_CALL_RTOL
+    s.reconstruction(); o.call("reconstruction")
+    assert rel_linf(s.get_array("GPA"), o.array("GPA")).max() <= ONE_CALL_RTOL
+    assert rel_linf(s.get_array("GradC"), o.array("GradC")).max() <= ONE_CALL_RTOL
+    s.flux_sourceterm(); o.call("flux_sourceterm")
+    assert rel_linf(s.get_array("hWA"), o.array("hWA")).max() <= 1e-11
+    s.lu_sgs_steady(); o.call("lu_sgs_steady")
+    assert rel_linf(s.get_array("hWA"), o.array("hWA")).max() <= 1e-10
+    PA, WA = s.get_state()
+    assert rel_linf(PA, o.array("PA")).max() <= ONE_CALL_RTOL
+    assert rel_linf(WA, o.array("WA")).max() <= ONE_CALL_RTOL
+
+
+@pytest.mark.parametrize("name,over", [("t1", {}), ("t2", {}), ("t1", {"order": "random"}),
+                                       ("t2", {"order": "colored"})])
+def test_100_iterations_match_oracle(case_root, name, over):
+    d = make_case(case_root, name, **over)
+    c, s, o = solver_and_oracle(d)
+    s.run(100)
+    o.run(100)
+    PA, WA = s.get_state()
+    err_pa = rel_linf(PA, o.array("PA"))
+    err_wa = rel_linf(WA, o.array("WA"))
+    assert err_pa.max() <= ITER_RTOL, err_pa
+    assert err_wa.max() <= ITER_RTOL, err_wa
+    r_gpu, m_gpu = s.residual()
+    r_cpu, m_cpu = o.residual()
+    np.testing.assert_allclose(r_gpu, r_cpu, rtol=1e-7, atol=1e-300)
+    assert m_gpu == pytest.approx(m_cpu, rel=1e-9)
+
+
+def test_stage_graph_equals_subroutine_calls(case_t2):
+    c = rc.Case(case_t2)
+    a = rc.Solver(c)
+    b = rc.Solver(c)
+    for it in range(1, 4):
+        a.lu_sgs_stage(it)
+        b.timestep(); b.reconstruction(); b.flux_sourceterm(); b.lu_sgs_steady()
+    pa, wa = a.get_state()
+    pb, wb = b.get_state()
+    assert np.array_equal(pa, pb) and np.array_equal(wa, wb)
+
+
+def test_bit_reproducible_run_to_run(case_root):
+    d = make_case(case_root, "c1", nx=80, ny=16)
+    c = rc.Case(d)
+    out = []
+    for _ in range(2):
+        s = rc.Solver(c)
+        s.run(50)
+        out.append(s.get_state()[0].tobytes())
+        s.close()
+    assert out[0] == out[1]
+
+
+def test_full_size_c1_100_iterations(case_root):
+    """The 20k-triangle inviscid nozzle at its full size, 100 iterations."""
+    d = make_case(case_root, "c1")
+    c, s, o = solver_and_oracle(d, threads=oracle.Oracle.max_threads())
+    s.run(100)
+    o.run(100)
+    PA, WA = s.get_state()
+    assert rel_linf(PA, o.array("PA")).max() <= ITER_RTOL
+    assert rel_linf(WA, o.array("WA")).max() <= ITER_RTOL
+
+
+def test_full_size_c2_few_iterations(case_root):
+    """The 120k-triangle reacting viscous nozzle at its full size, 3 iterations."""
+    d = make_case(case_root, "c2")
+    c, s, o = solver_and_oracle(d, threads=oracle.Oracle.max_threads())
+    s.run(3)
+    o.run(3)
+    PA, WA = s.get_state()
+    assert rel_linf(PA, o.array("PA")).max() <= ITER_RTOL
+    assert rel_linf(WA, o.array("WA")).max() <= ITER_RTOL
+
+
+def test_device_stop_condition_is_reported(case_t1):
+    """A negative pressure planted in the host state is caught by TimeStep's
+    check (TimeStep.f90:66-70) and reported at the next synchronising call."""
+    c = rc.Case(case_t1)
+    s = rc.Solver(c)
+    PA = c.array("PA").copy()
+    PA[5, 0] = -PA[5, 0]
+    s.set_state(PA, c.array("WA"))
+    s.timestep()
+    with pytest.raises(rc.RcError) as e:
+        s.sync()
+    assert e.value.code & 4

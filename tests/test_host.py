@@ -1,0 +1,64 @@
+"""Host side of the product (no GPU): set-up arrays and the C ABI surface.
+
+librc_gpu.so carries the host set-up (rc_host.h) next to the kernels; loading it
+needs only the CUDA runtime library, not a GPU.  The set-up is checked bit for
+bit against the oracle's independent restatement, and the library must export
+every function declared in include/*.h.
+"""
+import ctypes
+import os
+import re
+
+import numpy as np
+import pytest
+
+import oracle
+import rocketcombustor_gb300 as rc
+from conftest import ROOT, make_case
+
+SETUP_ARRAYS = ["KFace", "Neighbor", "FNode", "NeighF", "Neigh", "NeighC", "Ghostcell", "Num_ghostcell",
+                "Hostcell", "Hostface", "BCtype_Ghostcell", "COOR", "VECX", "VOL", "CELLXY", "reflen", "wdis",
+                "AMLS", "Coor_Ghostnode", "CellXY_Ghostcell", "vol_Ghostcell", "XYH", "PA", "WA"]
+
+
+def declared_functions():
+    names = []
+    for h in sorted(os.listdir(os.path.join(ROOT, "include"))):
+        if h.endswith(".h"):
+            txt = open(os.path.join(ROOT, "include", h)).read()
+            names += re.findall(r"^\s*(?:const\s+)?[\w\s\*]+?\b(rc_\w+)\s*\(", txt, flags=re.M)
+    return sorted(set(names))
+
+
+def test_library_exports_every_declared_symbol():
+    L = rc.load()
+    names = declared_functions()
+    assert len(names) >= 20
+    for n in names:
+        assert hasattr(L, n), n
+    assert set(names) == set(rc.SIGNATURES), set(names) ^ set(rc.SIGNATURES)
+
+
+@pytest.mark.parametrize("name,over", [("t1", {}), ("t2", {}), ("t1", {"order": "random"}),
+                                       ("c1", {"nx": 60, "ny": 12})])
+def test_setup_matches_oracle_bitwise(case_root, name, over):
+    d = make_case(case_root, name, **over)
+    o = oracle.Oracle(d)
+    c = rc.Case(d)
+    assert (c.NE, c.NF, c.NVar, c.Nghost, c.MaxNei) == (o.NE, o.NF, o.NVar, o.Nghost, o.MaxNei)
+    for nm in SETUP_ARRAYS:
+        a, b = c.array(nm), o.array(nm)
+        if nm == "NeighC":
+            b = b  # (0:MaxNei, NE) in both
+        assert a.shape == b.shape, nm
+        assert np.array_equal(a, b), nm
+    m, t, g = c.views()
+    assert abs(m.total_volume - o.total_volume) == 0.0
+    assert g.p_out == o.p_out and g.cfl == o.cfl
+    assert t.oxidizer_mass_flow == o.oxidizer_mass_flow
+    assert bool(g.IfViscous) == o.viscous and bool(g.If_turn_on_combustion) == o.combustion
+
+
+def test_bad_case_reports_error(tmp_path):
+    with pytest.raises(rc.RcError):
+        rc.Case(str(tmp_path / "missing"))

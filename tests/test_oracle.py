@@ -1,0 +1,126 @@
+"""Self-checks of the FP64 CPU oracle (no GPU).
+
+The reference ships no tests or golden vectors and cannot be built here, so the
+oracle is pinned by the reference's own runtime invariants and by physics
+identities: a fluid at rest in a closed box has zero residual, the weighted
+least-squares gradient is exact for linear fields, the global reaction
+conserves mass, the Newton solve inverts the energy relation, and the serial
+(reference loop structure) and parallel (gather + level schedule) modes agree
+bit for bit.
+"""
+import numpy as np
+import pytest
+
+import oracle
+from conftest import make_case
+from rocketcombustor_gb300 import cases
+
+
+def test_invariants_of_setup(case_t1):
+    o = oracle.Oracle(case_t1)
+    vol = o.array("VOL")
+    assert (vol > 0).all()
+    assert np.abs(o.array("XYH")).sum(axis=1).max() < 1e-8            # reconstruction_initialization.f90:241
+    # every cell: neighbours + ghosts = faces (ghostcell.f90:163)
+    assert (o.array("Neigh") + o.array("Num_ghostcell") == o.array("KFace")).all()
+    # polygonal area of the nozzle section
+    xs = np.linspace(0, cases.X_EXIT, 25)
+    area = np.trapezoid(cases.half_height(xs), xs)
+    assert abs(o.total_volume - area) / area < 2e-3
+    # NeighF ascending face ids (the scatter order the gather kernels rely on)
+    nf = o.array("NeighF")
+    for i in range(o.NE):
+        k = o.array("KFace")[i]
+        assert (np.diff(nf[i, :k]) > 0).all()
+
+
+def test_gamma_of_perfect_gas(case_t1):
+    o = oracle.Oracle(case_t1)
+    Cp, gama, R = o.gas(np.array([1.0]), 1500.0)
+    assert abs(gama - 1.4) < 1e-14
+    assert abs(R - 287.0) < 1e-10
+    assert abs(Cp - 3.5 * R) < 1e-9
+
+
+def test_rest_state_has_zero_residual(case_root):
+    for name in ("t1", "t2"):
+        d = make_case(case_root, name, closed=True, perturb=0.0)
+        o = oracle.Oracle(d)
+        o.call("timestep")
+        o.call("reconstruction")
+        # no chemistry: compare the flux part only
+        o.call("flux_lax")
+        hWA = o.array("hWA")
+        assert np.abs(hWA).max() == 0.0 or np.abs(hWA[:, 1:3]).max() / (o.array("PA")[:, 0].max() * 1e-2) < 1e-9
+        np.testing.assert_allclose(hWA[:, 0], 0.0, atol=1e-12)
+        assert np.abs(o.array("GradC")).max() < 1e-6
+
+
+def test_linear_field_gradient_is_exact(case_t2):
+    o = oracle.Oracle(case_t2)
+    PA = o.array("PA")
+    C = o.array("CELLXY")
+    L = o.array("reflen")
+    a = np.array([1.0e6, 100.0, -50.0, 2000.0, 0.1, 0.2, 0.3])
+    bx = np.array([3.0e6, 1e3, 2e3, 4e3, 0.5, -0.4, 0.2])
+    by = np.array([-1.0e6, 5e2, -3e2, 1e3, -0.3, 0.1, 0.6])
+    PA[:] = a[None, :] + C[:, :1] * bx[None, :] + C[:, 1:2] * by[None, :]
+    o.call("gradient")
+    G = o.array("GradC")
+    inner = o.array("Num_ghostcell") == 0
+    gx = G[inner, :, 0] / L[inner, 0:1]
+    gy = G[inner, :, 1] / L[inner, 1:2]
+    np.testing.assert_allclose(gx, np.broadcast_to(bx, gx.shape), rtol=1e-9, atol=1e-9 * np.abs(bx).max())
+    np.testing.assert_allclose(gy, np.broadcast_to(by, gy.shape), rtol=1e-9, atol=1e-9 * np.abs(by).max())
+
+
+def test_global_reaction_conserves_mass(case_t2):
+    o = oracle.Oracle(case_t2)
+    rng = np.random.default_rng(0)
+    for _ in range(50):
+        Y = rng.dirichlet(np.ones(4))
+        T = rng.uniform(800, 3500)
+        w = o.production(T, 2.0, Y)
+        assert abs(w.sum()) <= 1e-12 * np.abs(w).max() + 1e-300
+        assert w[1] <= 0 and w[2] >= 0
+
+
+def test_newton_inverts_energy(case_t2):
+    o = oracle.Oracle(case_t2)
+    rng = np.random.default_rng(1)
+    for _ in range(50):
+        Y = rng.dirichlet(np.ones(4))
+        T = rng.uniform(300, 5000)
+        h = o.enthalpy(T)
+        _, _, R = o.gas(Y, T)
+        et = float(Y @ h) - R * T
+        Tn = o.newton(et, Y, T * rng.uniform(0.7, 1.3))
+        assert abs(Tn - T) < 1e-4
+
+
+def test_transport_positive_and_finite(case_t2):
+    o = oracle.Oracle(case_t2)
+    for T in (300.0, 999.0, 1001.0, 3500.0):
+        mu, k = o.transport(T, np.array([0.1, 0.6, 0.3, 0.0]))
+        assert 1e-6 < mu < 1e-3 and 1e-3 < k < 10
+        D = o.diffusion(5e6, T, np.array([0.1, 0.6, 0.3, 0.0]))
+        assert np.isfinite(D).all() and (D > 0).all()
+
+
+@pytest.mark.parametrize("name", ["t1", "t2"])
+def test_serial_and_parallel_modes_agree_bitwise(case_root, name):
+    d = make_case(case_root, name)
+    a = oracle.Oracle(d, threads=1)
+    b = oracle.Oracle(d, threads=4)
+    ha = a.run(20, history=True)
+    hb = b.run(20, history=True)
+    for nm in ("PA", "WA", "hWA", "GradC", "alpaF", "step"):
+        assert np.array_equal(a.array(nm), b.array(nm)), nm
+    assert np.array_equal(ha, hb)
+
+
+def test_level_counts_of_orders(case_root):
+    nat = oracle.Oracle(make_case(case_root, "t1", order="natural"))
+    col = oracle.Oracle(make_case(case_root, "t1", order="colored"))
+    assert col.nlev_fwd <= 4 and col.nlev_bwd <= 4
+    assert nat.nlev_fwd > col.nlev_fwd
