@@ -320,7 +320,7 @@ class CaseConfig:
     nx: int
     ny: int
     seed: int
-    order: str = "colored"
+    order: str = "natural"
     nsp: int = 1
     viscous: bool = False
     combustion: bool = False
