@@ -153,6 +153,33 @@ int rc_stats(rc_ctx* ctx, long long* kernel_launches, int* fwd_levels, int* bwd_
 
 const char* rc_last_error(rc_ctx* ctx);
 
+/*
+ * Residual norms of device arrays that the caller owns, computed without any
+ * device allocation.  No counterpart in the reference: it serves hosts that
+ * cannot call cudaMalloc, such as a Fortran host whose device arrays are all
+ * managed by its own CUDA Fortran/OpenACC runtime, or a solver loop that must
+ * not allocate (cudaMalloc can synchronise the whole device) once it is set up.
+ *
+ * Inputs: d_hWA and d_WA in the Fortran layout (NVar,NE) and d_VOL (NE), all in
+ * device memory of the current device; the result is the same as rc_residual:
+ * res(k) = sum(VOL*|hWA(k,:)|)/total_volume, romax = max(WA(1,:)), written to
+ * host memory.  The work runs on cuda_stream (NULL = legacy default stream) and
+ * the call returns after it has finished.
+ *
+ * Scratch: a fixed array compiled into the library, sized for NVar up to
+ * RC_NOALLOC_MAX_NVAR (about 41 KB, held by every GPU that loads the library
+ * until the process exits); a larger NVar is rejected with RC_ERR_ARG and a
+ * message on stderr.  The first call on a device looks up the array's device
+ * address (cudaGetSymbolAddress) with that device current; make that first call
+ * before any stream capture.  Every value read from the scratch is written
+ * earlier in the same call, so nothing has to be cleared between calls, but all
+ * calls share the one array: calls whose work overlaps on the GPU (other
+ * streams, other host threads) race and must be serialised by the caller.
+ */
+#define RC_NOALLOC_MAX_NVAR 16
+int rc_residual_noalloc(const double* d_hWA, const double* d_WA, const double* d_VOL, int NE, int NVar,
+                        double total_volume, void* cuda_stream, double* res, double* romax);
+
 #ifdef __cplusplus
 }
 #endif

@@ -92,6 +92,7 @@ SIGNATURES = {
     "rc_case_WA": (_DP, [_vp]),
     "rc_case_array": (_vp, [_vp, _cp, ctypes.POINTER(_l)]),
     "rc_run_steady": (_i, [_vp, _i, _i, _l, _l, _DP]),
+    "rc_residual_noalloc": (_i, [_vp, _vp, _vp, _i, _i, _d, _vp, _DP, _DP]),
 }
 
 _lib: Optional[ctypes.CDLL] = None

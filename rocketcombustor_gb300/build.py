@@ -24,6 +24,7 @@ NVCC_COMMON = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC,-ffp-contr
 # translation unit -> extra flags
 UNITS = {
     "rc_core.cu": ["--fmad=false"],
+    "rc_noalloc.cu": ["--fmad=false"],
 }
 HOST_UNITS = ["rc_host.cpp"]
 
