@@ -334,8 +334,11 @@ class CaseConfig:
     perturb: float = 0.0
     chem_model: int = 0
     of_ratio: float = 6.0
-    inlet_burnt: float = 1.0   # fraction of O2 already converted at the inlet
+    inlet_burnt: float = 0.99  # fraction of the O2 already converted at the inlet
     closed: bool = False       # every boundary a wall, fluid initially at rest (test case)
+    p_out_factor: float = 1.0  # exit pressure as a multiple of the isentropic design exit pressure
+    jitter: float = 0.10       # interior node jitter, fraction of the local spacing
+    init: str = "uniform"      # initial field: "uniform" inlet state or "isentropic" quasi-1D nozzle flow
 
     @property
     def n_cells(self) -> int:
@@ -347,14 +350,14 @@ PRESETS: Dict[str, CaseConfig] = {
     "c1": CaseConfig("c1", nx=250, ny=40, seed=1),
     # reacting viscous nozzle (about 120k triangles)
     "c2": CaseConfig("c2", nx=600, ny=100, seed=2, nsp=4, viscous=True, combustion=True,
-                     p0=5.0e6, T0=3500.0, perturb=0.02),
+                     p0=5.0e6, T0=3500.0, perturb=0.02, init="isentropic"),
     # large reacting viscous nozzle (2M triangles)
     "c4": CaseConfig("c4", nx=2500, ny=400, seed=6, nsp=4, viscous=True, combustion=True,
-                     p0=5.0e6, T0=3500.0, perturb=0.02, nstep=500),
+                     p0=5.0e6, T0=3500.0, perturb=0.02, nstep=500, init="isentropic"),
     # tiny cases for tests
     "t1": CaseConfig("t1", nx=24, ny=6, seed=11),
     "t2": CaseConfig("t2", nx=24, ny=6, seed=12, nsp=4, viscous=True, combustion=True,
-                     p0=5.0e6, T0=3500.0, perturb=0.02),
+                     p0=5.0e6, T0=3500.0, perturb=0.02, init="isentropic"),
 }
 
 
@@ -395,7 +398,8 @@ def write_case(d: str, cfg: CaseConfig, mesh: Optional[Mesh] = None) -> Mesh:
     os.makedirs(os.path.join(d, "combustion"), exist_ok=True)
     os.makedirs(os.path.join(d, "flow"), exist_ok=True)
     if mesh is None:
-        mesh = nozzle_mesh(cfg.nx, cfg.ny, cfg.seed, cfg.order, wall_type=1 if cfg.viscous else 6)
+        mesh = nozzle_mesh(cfg.nx, cfg.ny, cfg.seed, cfg.order, wall_type=1 if cfg.viscous else 6,
+                           jitter=cfg.jitter)
     if cfg.closed:
         wall = 1 if cfg.viscous else 6
         mesh.boundaries = [(wall, pairs) for _, pairs in mesh.boundaries]
@@ -438,12 +442,31 @@ def write_case(d: str, cfg: CaseConfig, mesh: Optional[Mesh] = None) -> Mesh:
     write_inlet(os.path.join(d, "combustion", "oxidizer.in"), Yin, T_in, cfg.p0,
                 mflux * 2.0 * H_CHAMBER, "oxidizer")
     write_inlet(os.path.join(d, "combustion", "fuel.in"), Yin, T_in, cfg.p0, 0.37, "fuel")
-    pr = exit_pressure_ratio(gamma)
+    pr = exit_pressure_ratio(gamma) * cfg.p_out_factor
     write_flow_info(d, cfg.combustion, cfg.viscous, cfg.cfl, cfg.nstep, cfg.limit_id, pr)
-    # initial field: uniform inlet (chamber) state, optionally perturbed Y
+    # initial field: uniform inlet (chamber) state, or the quasi-1D isentropic
+    # nozzle flow (subsonic up to the throat, supersonic after it) with the
+    # velocity tilted along y/h * dh/dx; species optionally perturbed
     nv = 4 + len(Yin) - 1
     PA = np.zeros((mesh.ne, nv))
     PA[:, 0], PA[:, 1], PA[:, 2], PA[:, 3] = p_in, (0.0 if cfg.closed else u_in), 0.0, T_in
+    if cfg.init == "isentropic" and not cfg.closed:
+        cxy = mesh.coor[mesh.cells - 1].mean(axis=1)
+        x, y = cxy[:, 0], cxy[:, 1]
+        h = half_height(x)
+        eps = 1e-6
+        dh = (half_height(x + eps) - half_height(x - eps)) / (2 * eps)
+        M = np.array([area_ratio_mach(max(hh / H_THROAT, 1.0 + 1e-9), gamma, supersonic=(xx > X_THROAT))
+                      for hh, xx in zip(h, x)])
+        T = cfg.T0 / (1.0 + 0.5 * (gamma - 1.0) * M * M)
+        p = cfg.p0 * (T / cfg.T0) ** (gamma / (gamma - 1.0))
+        q = M * np.sqrt(gamma * Rmix * T)
+        slope = y / h * dh
+        PA[:, 0], PA[:, 3] = p, T
+        PA[:, 1] = q / np.sqrt(1.0 + slope * slope)
+        PA[:, 2] = PA[:, 1] * slope
+    elif cfg.init != "uniform" and not cfg.closed:
+        raise ValueError(f"unknown init {cfg.init!r}")
     if len(Yin) > 1:
         Y = np.tile(np.asarray(Yin), (mesh.ne, 1))
         if cfg.perturb > 0:
