@@ -108,6 +108,14 @@ class ClockSampler:
                 "reasons": reasons, "samples": len(rows)}
 
 
+def case_overrides(args) -> dict:
+    over = {}
+    for k in ("order", "nx", "ny"):
+        if getattr(args, k) is not None:
+            over[k] = getattr(args, k)
+    return over
+
+
 def make_workload(name: str, tmp: str, **over):
     from rocketcombustor_gb300 import cases
     d = os.path.join(tmp, name)
@@ -139,7 +147,7 @@ def run_reference(args, rank, world):
     if rank != 0:
         return 0
     with tempfile.TemporaryDirectory() as tmp:
-        d, cfg = make_workload(args.case, tmp, **({"order": args.order} if args.order else {}))
+        d, cfg = make_workload(args.case, tmp, **case_overrides(args))
         threads = oracle.Oracle.max_threads()
         o = oracle.Oracle(d, threads=threads)
         o.run(args.warmup)
@@ -176,6 +184,8 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--case", default="c2")
     ap.add_argument("--order", default=None)
+    ap.add_argument("--nx", type=int, default=None, help="override the preset's cells along the axis")
+    ap.add_argument("--ny", type=int, default=None, help="override the preset's cells across")
     ap.add_argument("--precision", default="fp64", choices=["fp64", "mixed"])
     ap.add_argument("--e2e-steps", type=int, default=10)
     ap.add_argument("--cpu-budget", type=float, default=15.0)
@@ -205,7 +215,7 @@ def main():
     flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=f"cuda:{local}")
     prec = rc.RC_PREC_MIXED if args.precision == "mixed" else rc.RC_PREC_FP64
     with tempfile.TemporaryDirectory() as tmp:
-        d, cfg = make_workload(args.case, tmp, **({"order": args.order} if args.order else {}))
+        d, cfg = make_workload(args.case, tmp, **case_overrides(args))
         case = rc.Case(d)
         s = rc.Solver(case, precision=prec, device=local, stream=stream.cuda_stream)
         NE, NF, V = case.NE, case.NF, case.NVar

@@ -17,6 +17,11 @@
  * rc_get_state, rc_get_array, rc_sync).  rc_last_error() gives a message.
  *
  * Threading: one host thread per context; each context owns one CUDA stream.
+ *
+ * LU-SGS schedule: by default both sweeps of an iteration run as one
+ * cooperative kernel with a grid barrier between levels; setting the
+ * environment variable RC_LUSGS_SCHEDULE=levels before rc_init launches one
+ * kernel per level instead.  Both compute the same recurrences bit for bit.
  */
 #ifndef RC_GPU_H
 #define RC_GPU_H
@@ -32,12 +37,15 @@ extern "C" {
 #define RC_ERR_NEG_FACE 8      /* rho or p < 0 at a face in flux_lax (flux_lax.f90:239-242) */
 #define RC_ERR_NAN 16          /* NaN in WA(1,1) after a stage (Time_LUSGS_steady.f90:94-97) */
 #define RC_ERR_BCTYPE 32       /* unknown boundary code (flux_lax.f90:232-235, update_flow_variables.f90:364-367) */
+#define RC_ERR_SYNC 64         /* a grid barrier of the persistent LU-SGS kernel gave up waiting (bounded spin) */
 #define RC_ERR_ARG 1024        /* invalid argument or unsupported configuration */
 #define RC_ERR_CUDA 2048       /* CUDA runtime failure */
 
 #define RC_PREC_FP64 0         /* plain FP64 path, operation order of the reference */
-#define RC_PREC_MIXED 1        /* FP32 reconstruction/limiter/flux with compensated accumulation;
-                                  FP64 diagonal, chemistry, Newton and norms */
+#define RC_PREC_MIXED 1        /* FP32 reconstruction/limiter/flux with compensated accumulation and
+                                  FP32 LU-SGS off-diagonal terms; FP64 diagonal, chemistry, Newton, norms */
+#define RC_PREC_MIXED_DC 2     /* defect correction: the FP64 residual of RC_PREC_FP64 driving the
+                                  FP32 LU-SGS sweeps of RC_PREC_MIXED (FP64 fixed point) */
 
 typedef struct rc_ctx rc_ctx;
 
@@ -129,6 +137,12 @@ int rc_reconstruction(rc_ctx* ctx);    /* reconstruction      fvm2d.f90:183 (gra
 int rc_flux_sourceterm(rc_ctx* ctx);   /* flux_sourceterm     fvm2d.f90:196 (flux_lax + flux_viscous + sourceterm) */
 int rc_lusgs_steady(rc_ctx* ctx);      /* LU_SGS_steady       Time_LUSGS_steady.f90:102 (incl. update_primitve_variables) */
 int rc_lusgs_stage(rc_ctx* ctx, int istep); /* lu_sgs_stage   Time_LUSGS_steady.f90:74, one captured graph */
+
+/* Switch the precision of the following calls: RC_PREC_FP64 on any context,
+ * RC_PREC_MIXED / RC_PREC_MIXED_DC on contexts created with a mixed mode.  A
+ * driver switches MIXED -> MIXED_DC when the FP32 residual stops decreasing.
+ * No counterpart in the reference (it has a single FP64 path). */
+int rc_set_precision(rc_ctx* ctx, int precision);
 
 /* Residual + step_residual norms (residual.f90:4-21, 61-79): res(k) =
  * sum(vol*|hWA(k,:)|)/total_volume, romax = max(WA(1,:)).  Synchronises. */

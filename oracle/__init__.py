@@ -19,13 +19,15 @@ SRC = os.path.join(HERE, "rc_oracle.cpp")
 
 # The oracle's arithmetic must not contract a*b+c into FMA: the reference's
 # x86-64 build (src/Makefile:43, no -march) has no FMA.
-CXXFLAGS = ["-O2", "-ffp-contract=off", "-fno-fast-math", "-fopenmp", "-fPIC", "-shared", "-std=c++17"]
+INCLUDE = os.path.join(os.path.dirname(HERE), "include")
+CXXFLAGS = ["-O2", "-ffp-contract=off", "-fno-fast-math", "-fopenmp", "-fPIC", "-shared", "-std=c++17", f"-I{INCLUDE}"]
 
 
 def build(force: bool = False) -> str:
     """Compile the oracle into oracle/_build/librc_oracle.so (seconds)."""
     os.makedirs(BUILD, exist_ok=True)
-    if not force and os.path.exists(LIB) and os.path.getmtime(LIB) >= os.path.getmtime(SRC):
+    srcs = [SRC, os.path.join(INCLUDE, "rc_math.h")]
+    if not force and os.path.exists(LIB) and all(os.path.getmtime(LIB) >= os.path.getmtime(x) for x in srcs):
         return LIB
     tmp = LIB + f".tmp{os.getpid()}"
     subprocess.run(["g++", *CXXFLAGS, "-o", tmp, SRC], check=True)
@@ -62,8 +64,18 @@ def lib() -> ctypes.CDLL:
         L.orc_diffusion.argtypes = [vp, d, d, dp, dp]
         L.orc_production.argtypes = [vp, d, d, dp, dp]
         L.orc_newton.restype = d; L.orc_newton.argtypes = [vp, d, dp, d]
+        L.orc_math.argtypes = [i, dp, dp, dp, l]
         _lib = L
     return _lib
+
+
+def math(which: str, x, y=None) -> np.ndarray:
+    """include/rc_math.h exp/log/pow evaluated on the host, elementwise."""
+    x = np.ascontiguousarray(x, dtype=np.float64)
+    y = np.ascontiguousarray(np.zeros_like(x) if y is None else y, dtype=np.float64)
+    out = np.empty_like(x)
+    lib().orc_math({"exp": 0, "log": 1, "pow": 2}[which], _dp(x), _dp(y), _dp(out), x.size)
+    return out
 
 
 def _dp(a: np.ndarray):

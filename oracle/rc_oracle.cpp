@@ -46,6 +46,10 @@
 #include <omp.h>
 #endif
 
+// exp/log/pow of the hot path: the portable implementation shared with the
+// GPU (include/rc_math.h), so that one input gives one output on both.
+#include "rc_math.h"
+
 namespace orc {
 
 // ---------------------------------------------------------------- arrays ----
@@ -419,7 +423,7 @@ struct Oracle {
     const int P = order_of_cp_polynomial;
     double basis[16];
     basis[0] = -powi(tem, -2);
-    basis[1] = std::log(tem) / tem;
+    basis[1] = rcm::log(tem) / tem;
     for (int j = 3; j <= P; ++j) basis[j - 1] = powi(tem, j - 3) / (double)(j - 2);
     const FA2<double>* coef;
     const std::vector<double>* b1;
@@ -472,14 +476,14 @@ struct Oracle {
       kA = &high_K_A; kB = &high_K_B; kC = &high_K_C; kD = &high_K_D;
     }
     for (int i = 0; i < Nsp; ++i) {
-      mul[i] = std::exp((*mA)[i] * std::log(tem) + (*mB)[i] / tem + (*mC)[i] / powi(tem, 2) + (*mD)[i]);
-      Kl[i] = std::exp((*kA)[i] * std::log(tem) + (*kB)[i] / tem + (*kC)[i] / powi(tem, 2) + (*kD)[i]);
+      mul[i] = rcm::exp((*mA)[i] * rcm::log(tem) + (*mB)[i] / tem + (*mC)[i] / powi(tem, 2) + (*mD)[i]);
+      Kl[i] = rcm::exp((*kA)[i] * rcm::log(tem) + (*kB)[i] / tem + (*kC)[i] / powi(tem, 2) + (*kD)[i]);
     }
     for (int i = 0; i < Nsp; ++i) { mul[i] = mul[i] * 1.0e-7; Kl[i] = Kl[i] * 1.0e-4; }
     for (int i = 0; i < Nsp; ++i) {
       phil[i] = 0.0;
       for (int j = 0; j < Nsp; ++j) {
-        double q = 1.0 + std::sqrt(mul[i] / mul[j]) * std::pow(mole_weight[j] / mole_weight[i], 0.25);
+        double q = 1.0 + std::sqrt(mul[i] / mul[j]) * rcm::pow(mole_weight[j] / mole_weight[i], 0.25);
         phil[i] = phil[i] + xx[j] * (q * q) / std::sqrt(1.0 + mole_weight[i] / mole_weight[j]);
       }
       phil[i] = (0.25 * std::sqrt(2.0)) * phil[i];
@@ -505,8 +509,8 @@ struct Oracle {
         double mw = 2.0 / (1.0 / mole_weight[i] + 1.0 / mole_weight[j]) * 1000;
         double cd = 0.5 * (collision_diameter[i] + collision_diameter[j]);
         double tstar = tem / std::sqrt(LJ_energy[i] * LJ_energy[j]);
-        double omega_d = A * std::pow(tstar, -B) + C * std::exp(-D * tstar) + E * std::exp(-F * tstar) +
-                         G * std::exp(-H * tstar);
+        double omega_d = A * rcm::pow(tstar, -B) + C * rcm::exp(-D * tstar) + E * rcm::exp(-F * tstar) +
+                         G * rcm::exp(-H * tstar);
         Dij[j] = 0.0266 * std::sqrt(powi(tem, 3)) / (pp * std::sqrt(mw) * powi(cd, 2) * omega_d);
       }
       double xdsum = 0.0;
@@ -521,9 +525,9 @@ struct Oracle {
     for (int i = 0; i < Nsp; ++i) { Y[i] = fmax2(0.0, Y2[i]); Y[i] = fmin2(1.0, Y[i]); }
     double kf;
     if (code_chemical_model == 0) {
-      kf = Af_react[0] * std::exp(-E_react[0] / (Rconstant * T));
-      kf = kf * std::pow(Y[0] * rho / (mole_weight[0] * 1000), 0.2);
-      kf = kf * std::pow(Y[1] * rho / (mole_weight[1] * 1000), 1.3);
+      kf = Af_react[0] * rcm::exp(-E_react[0] / (Rconstant * T));
+      kf = kf * rcm::pow(Y[0] * rho / (mole_weight[0] * 1000), 0.2);
+      kf = kf * rcm::pow(Y[1] * rho / (mole_weight[1] * 1000), 1.3);
     } else if (code_chemical_model == 1) {
       kf = 0.0;
       if (T > 710.0) kf = 1e4;
@@ -1745,6 +1749,11 @@ void orc_diffusion(void* h, double p, double T, const double* Y, double* Dk) {
 }
 void orc_production(void* h, double T, double rho, const double* Y, double* prod) {
   static_cast<Oracle*>(h)->compute_production_rate(T, rho, Y, prod);
+}
+// which: 0 exp(x), 1 log(x), 2 pow(x, y) of include/rc_math.h, elementwise.
+void orc_math(int which, const double* x, const double* y, double* out, long n) {
+  for (long i = 0; i < n; ++i)
+    out[i] = which == 0 ? rcm::exp(x[i]) : which == 1 ? rcm::log(x[i]) : rcm::pow(x[i], y[i]);
 }
 double orc_newton(void* h, double et, const double* Y, double t0) {
   double t, a, b, c;

@@ -29,8 +29,9 @@ from . import build as _build
 RC_OK = 0
 RC_ERR = {1: "thermo T out of range", 2: "transport T out of range", 4: "negative rho/p/T in TimeStep",
           8: "negative rho/p at a face", 16: "NaN in WA(1,1)", 32: "unknown boundary code",
+          64: "grid barrier timed out",
           1024: "invalid argument", 2048: "CUDA error"}
-RC_PREC_FP64, RC_PREC_MIXED = 0, 1
+RC_PREC_FP64, RC_PREC_MIXED, RC_PREC_MIXED_DC = 0, 1, 2
 
 _i, _d, _l, _vp, _cp = ctypes.c_int, ctypes.c_double, ctypes.c_long, ctypes.c_void_p, ctypes.c_char_p
 _IP, _DP = ctypes.POINTER(ctypes.c_int), ctypes.POINTER(ctypes.c_double)
@@ -93,6 +94,7 @@ SIGNATURES = {
     "rc_case_array": (_vp, [_vp, _cp, ctypes.POINTER(_l)]),
     "rc_run_steady": (_i, [_vp, _i, _i, _l, _l, _DP]),
     "rc_residual_noalloc": (_i, [_vp, _vp, _vp, _i, _i, _d, _vp, _DP, _DP]),
+    "rc_set_precision": (_i, [_vp, _i]),
 }
 
 _lib: Optional[ctypes.CDLL] = None
@@ -205,6 +207,7 @@ class Solver:
         if st:
             raise RcError(st, "rc_init")
         self._h = h
+        self.precision = int(precision)
         self.NE, self.NF, self.NVar, self.Nghost = case.NE, case.NF, case.NVar, case.Nghost
         if stream is not None:
             self._check(L.rc_set_stream(h, _vp(stream)))
@@ -231,6 +234,11 @@ class Solver:
 
     def lu_sgs_stage(self, istep: int = 1):
         return self._check(load().rc_lusgs_stage(self._h, int(istep)))
+
+    def set_precision(self, precision: int):
+        """RC_PREC_FP64, RC_PREC_MIXED or RC_PREC_MIXED_DC for the following calls."""
+        self._check(load().rc_set_precision(self._h, int(precision)))
+        self.precision = int(precision)
 
     def run(self, nsteps: int):
         for it in range(1, nsteps + 1):

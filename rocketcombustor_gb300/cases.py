@@ -56,20 +56,22 @@ def half_height(x: np.ndarray) -> np.ndarray:
     return h
 
 
-def area_ratio_mach(ratio: float, gamma: float, supersonic: bool) -> float:
-    """Mach number for A/A* = ratio (isentropic), by bisection."""
-    def f(m):
-        g1 = (gamma + 1.0) / (2.0 * (gamma - 1.0))
-        return (1.0 / m) * ((2.0 / (gamma + 1.0)) * (1.0 + 0.5 * (gamma - 1.0) * m * m)) ** g1 - ratio
-
-    lo, hi = (1.0, 50.0) if supersonic else (1e-6, 1.0)
+def area_ratio_mach(ratio, gamma: float, supersonic):
+    """Mach number(s) for A/A* = ratio (isentropic), by bisection; `ratio` and
+    `supersonic` may be arrays."""
+    ratio = np.asarray(ratio, dtype=np.float64)
+    sup = np.broadcast_to(np.asarray(supersonic, dtype=bool), ratio.shape)
+    g1 = (gamma + 1.0) / (2.0 * (gamma - 1.0))
+    lo = np.where(sup, 1.0, 1e-6)
+    hi = np.where(sup, 50.0, 1.0)
     for _ in range(200):
         mid = 0.5 * (lo + hi)
-        if (f(mid) > 0) == (not supersonic):
-            lo = mid
-        else:
-            hi = mid
-    return 0.5 * (lo + hi)
+        f = (1.0 / mid) * ((2.0 / (gamma + 1.0)) * (1.0 + 0.5 * (gamma - 1.0) * mid * mid)) ** g1 - ratio
+        go_up = (f > 0) == (~sup)
+        lo = np.where(go_up, mid, lo)
+        hi = np.where(go_up, hi, mid)
+    m = 0.5 * (lo + hi)
+    return float(m) if m.ndim == 0 else m
 
 
 @dataclass
@@ -456,8 +458,7 @@ def write_case(d: str, cfg: CaseConfig, mesh: Optional[Mesh] = None) -> Mesh:
         h = half_height(x)
         eps = 1e-6
         dh = (half_height(x + eps) - half_height(x - eps)) / (2 * eps)
-        M = np.array([area_ratio_mach(max(hh / H_THROAT, 1.0 + 1e-9), gamma, supersonic=(xx > X_THROAT))
-                      for hh, xx in zip(h, x)])
+        M = area_ratio_mach(np.maximum(h / H_THROAT, 1.0 + 1e-9), gamma, supersonic=(x > X_THROAT))
         T = cfg.T0 / (1.0 + 0.5 * (gamma - 1.0) * M * M)
         p = cfg.p0 * (T / cfg.T0) ** (gamma / (gamma - 1.0))
         q = M * np.sqrt(gamma * Rmix * T)

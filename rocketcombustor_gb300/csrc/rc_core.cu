@@ -25,76 +25,15 @@
 #include <algorithm>
 #include <cmath>
 #include <cstdio>
+#include <cstdlib>
 #include <cstring>
 #include <string>
 #include <vector>
 
 #include "rc_gpu.h"
-#include "rc_thermo.cuh"
+#include "rc_dev.cuh"
 
 namespace rc {
-
-constexpr int MAXF = 4;  // faces per cell (triangles and quadrilaterals)
-
-struct Dev {
-  int NE, NF, NG;
-  // cells
-  const double* vol;
-  const double* rinv;            // [2*NE] 1./reflen
-  const unsigned char* nface;    // KFace
-  const unsigned char* cleft;    // bit q: cell is Neighbor(1,.) of its face q
-  const int* cface;              // [4*NE] NeighF, 0-based
-  const int* cother;             // [4*NE] cell across face q, -1 on a boundary
-  const unsigned char* nnei;     // Neigh
-  const int* cnei;               // [4*NE] NeighC(1:Neigh), 0-based
-  const unsigned char* ngh;      // Num_ghostcell
-  const int* cgh;                // [4*NE] Ghostcell, 0-based
-  const double* wdis;            // [4*NE]
-  const double* amls;            // [8*NE] AMLS(r,q,i) at (2q+r)*NE+i
-  const double* lvvh;            // [8*NE] limiter basis values at the face midpoints
-  // faces
-  const int* fNL;                // 0-based
-  const int* fNR;                // 0-based cell, or -BC code
-  const double* fvec;            // [2*NF] VECX
-  const double* fsav;            // max(|VECX|, small)
-  const double* fsn;             // [2*NF] unit normal
-  const double* fss;             // sqrt(dx*dx+dy*dy)
-  const double* fs2;             // dx*dx+dy*dy
-  const double* fvL;             // [2*NF] fbaseAll at the Gauss point for NL
-  const double* fvR;             // [2*NF] fbaseAll at the Gauss point for NR
-  const double* fdxk;            // |(x_L - x_R).n|
-  const double* fysn;            // [2*NF] yita*n
-  // ghosts
-  const int* gtype;
-  const double* gsn;             // [2*NG] ghost-face unit normal
-  // state and work arrays
-  double* PA;
-  double* WA;
-  double* hWA;
-  double* grad;
-  double* GPA;
-  double* step;
-  double* dd;
-  double* cst;                   // [(3+NSP)*NE]: rho, gamma, rho*E, h_k
-  double* src;                   // [(NSP-1)*NE]: vol*omega_k
-  double* alpa;
-  double* visL;
-  double* visR;
-  double* alpaF;
-  double* Finv;                  // [V*NF]
-  double* Fvis;                  // [(V-1)*NF], component 1 is identically zero
-  unsigned* err;
-};
-
-__device__ __forceinline__ void flag(const Dev& d, unsigned e) {
-  if (e) atomicOr(d.err, e);
-}
-
-__device__ __forceinline__ void removedirection(double& vx, double& vy, double nx, double ny) {
-  const double vn = vx * nx + vy * ny;  // flux_viscous.f90:352-361
-  vx = vx - vn * nx;
-  vy = vy - vn * ny;
-}
 
 // oxidizer_inlet_bc / fuel_inlet_bc (oxidizer.f90:367-382, fuel.f90:437-452)
 template <int NSP>
@@ -648,34 +587,130 @@ __global__ void __launch_bounds__(128) k_sweep(const Dev d, const ThermoDev<NSP>
   for (int k = 0; k < V; ++k) d.hWA[k * NE + i] = FWD ? (R[k] - df[k]) / ddi : R[k] - df[k] / ddi;
 }
 
-// WA += hWA and update_primitve_variables (update_flow_variables.f90:112-156).
+// Same sweep step with four lanes per cell, one per face slot: each lane
+// evaluates its neighbour's term of dflux, the terms are then added in slot
+// order (the NeighF order of the reference) by every lane of the quad, and the
+// lanes share the final divisions.  The residual R is already in hWA (the
+// forward gather runs as a separate, fully parallel kernel).
+// sweep_step: cell t of a level list (t >= n: lanes that only join the
+// shuffles); q is the lane's face slot.  Called by whole warps.
+template <int NSP, bool FWD>
+__device__ __forceinline__ void sweep_step(const Dev& d, const ThermoDev<NSP>& th, const int* __restrict__ cells,
+                                           int n, int t, int q) {
+  constexpr int V = 3 + NSP;
+  const bool valid = t < n;
+  const int i = valid ? cells[t] : 0;
+  const int NE = d.NE, NF = d.NF;
+  double c[V];
+#pragma unroll
+  for (int k = 0; k < V; ++k) c[k] = 0.0;
+  bool act = false;
+  if (valid && q < d.nface[i]) {
+    const int j = d.cother[q * NE + i];
+    act = j >= 0 && (FWD ? j < i : j > i);
+    if (act) {
+      const int f = d.cface[q * NE + i];
+      double dx = d.fvec[f], dy = d.fvec[NF + f];
+      if (!((d.cleft[i] >> q) & 1u)) { dx = -dx; dy = -dy; }
+      const double pp = d.PA[0 * NE + j], uu = d.PA[1 * NE + j], vv = d.PA[2 * NE + j], tt = d.PA[3 * NE + j];
+      const double rr = d.cst[0 * NE + j], gama = d.cst[1 * NE + j], roe = d.cst[2 * NE + j];
+      const double rou = rr * uu, rov = rr * vv;
+      const double drr = d.hWA[0 * NE + j], dru = d.hWA[1 * NE + j], drv = d.hWA[2 * NE + j],
+                   dre = d.hWA[3 * NE + j];
+      double dry[NSP], s = 0.0;
+#pragma unroll
+      for (int k = 0; k < NSP - 1; ++k) { dry[k] = d.hWA[(4 + k) * NE + j]; s = s + dry[k]; }
+      dry[NSP - 1] = drr - s;
+      const double duu = (dru - uu * drr) / rr;
+      const double dvv = (drv - vv * drr) / rr;
+      double s1 = 0.0, s2 = 0.0;
+#pragma unroll
+      for (int k = 0; k < NSP; ++k) s1 = s1 + d.cst[(3 + k) * NE + j] * dry[k];
+#pragma unroll
+      for (int k = 0; k < NSP; ++k) s2 = s2 + th.R[k] * dry[k];
+      const double dpp = (gama - 1) *
+                         (dre - s1 + tt * s2 * gama / (gama - 1) - 0.5 * (dru * uu + duu * rou + drv * vv + dvv * rov));
+      const double unormal = uu * dx + vv * dy;
+      const double dunormal = duu * dx + dvv * dy;
+      const double aF = d.alpaF[f];
+      c[0] = 0.5 * (-aF * drr + dru * dx + drv * dy);
+      c[1] = 0.5 * (-aF * dru + dru * unormal + rou * dunormal + dpp * dx);
+      c[2] = 0.5 * (-aF * drv + drv * unormal + rov * dunormal + dpp * dy);
+      c[3] = 0.5 * (-aF * dre + dunormal * (roe + pp) + unormal * (dre + dpp));
+#pragma unroll
+      for (int k = 0; k < NSP - 1; ++k) {
+        const double ry = rr * d.PA[(4 + k) * NE + j];
+        c[4 + k] = 0.5 * (-aF * dry[k] + dry[k] * unormal + ry * dunormal);
+      }
+    }
+  }
+  const int base = (threadIdx.x & 31) & ~3;
+  double df[V];
+#pragma unroll
+  for (int k = 0; k < V; ++k) df[k] = 0.0;
+#pragma unroll
+  for (int s = 0; s < 4; ++s) {
+    const bool a = __shfl_sync(0xffffffffu, act, base + s);
+#pragma unroll
+    for (int k = 0; k < V; ++k) {
+      const double cs = __shfl_sync(0xffffffffu, c[k], base + s);
+      if (a) df[k] = df[k] + cs;
+    }
+  }
+  if (!valid) return;
+  const double ddi = d.dd[i];
+#pragma unroll
+  for (int k = 0; k < V; ++k)
+    if ((k & 3) == q) {
+      const double R = d.hWA[k * NE + i];
+      d.hWA[k * NE + i] = FWD ? (R - df[k]) / ddi : R - df[k] / ddi;
+    }
+}
+
+template <int NSP, bool FWD>
+__global__ void __launch_bounds__(32) k_sweep4(const Dev d, const ThermoDev<NSP> th, const int* __restrict__ cells,
+                                               int n) {
+  const int gt = blockIdx.x * blockDim.x + threadIdx.x;
+  sweep_step<NSP, FWD>(d, th, cells, n, gt >> 2, gt & 3);
+}
+
 template <int NSP>
 __global__ void __launch_bounds__(128) k_update(const Dev d, const ThermoDev<NSP> th) {
-  constexpr int V = 3 + NSP;
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= d.NE) return;
-  const int NE = d.NE;
   unsigned err = 0;
-  double W[V];
-#pragma unroll
-  for (int k = 0; k < V; ++k) {
-    W[k] = d.WA[k * NE + i] + d.hWA[k * NE + i];
-    d.WA[k * NE + i] = W[k];
+  update_cell<NSP>(d, th, i, err);
+  flag(d, err);
+}
+
+// Both LU-SGS sweeps and the update in one cooperative launch: every level of
+// the forward sweep, then of the backward sweep, separated by grid barriers,
+// then the Newton update of all cells.  A level is cut into warps of 8 cells
+// (4 lanes each) that are dealt out to blocks first, so a small level spreads
+// over as many SMs as it has warps.
+constexpr int PERS_THREADS = 256;
+template <int NSP>
+__global__ void __launch_bounds__(PERS_THREADS) k_lusgs_persistent(const Dev d, const ThermoDev<NSP> th,
+                                                                   const int* __restrict__ fcells,
+                                                                   const int* __restrict__ foff, int nf,
+                                                                   const int* __restrict__ bcells,
+                                                                   const int* __restrict__ boff, int nb,
+                                                                   unsigned* count) {
+  const int G = gridDim.x, wpb = PERS_THREADS / 32, w = threadIdx.x >> 5;
+  const int lt = (threadIdx.x & 31) >> 2, q = threadIdx.x & 3;
+  unsigned seq = 0;
+  for (int l = 0; l < nf; ++l) {
+    const int lo = foff[l], n = foff[l + 1] - lo, nch = (n + 7) >> 3;
+    for (int c = blockIdx.x + w * G; c < nch; c += G * wpb) sweep_step<NSP, true>(d, th, fcells + lo, n, c * 8 + lt, q);
+    if (!grid_sync(count, seq++, d.err)) return;
   }
-  const double rho = W[0], u = W[1] / rho, v = W[2] / rho;
-  double Y[NSP], s = 0.0;
-#pragma unroll
-  for (int k = 0; k < NSP - 1; ++k) { Y[k] = W[4 + k] / rho; s = s + Y[k]; }
-  Y[NSP - 1] = 1.0 - s;
-  double Rcpcv;
-  const double t = newton_T<NSP>(th, W[3] / rho - 0.5 * (u * u + v * v), Y, d.PA[3 * NE + i], Rcpcv, err);
-  d.PA[0 * NE + i] = rho * Rcpcv * t;
-  d.PA[1 * NE + i] = u;
-  d.PA[2 * NE + i] = v;
-  d.PA[3 * NE + i] = t;
-#pragma unroll
-  for (int k = 0; k < NSP - 1; ++k) d.PA[(4 + k) * NE + i] = Y[k];
-  if (i == 0 && isnan(W[0])) err |= ERR_NAN;
+  for (int l = 0; l < nb; ++l) {
+    const int lo = boff[l], n = boff[l + 1] - lo, nch = (n + 7) >> 3;
+    for (int c = blockIdx.x + w * G; c < nch; c += G * wpb) sweep_step<NSP, false>(d, th, bcells + lo, n, c * 8 + lt, q);
+    if (!grid_sync(count, seq++, d.err)) return;
+  }
+  unsigned err = 0;
+  for (int i = blockIdx.x * PERS_THREADS + threadIdx.x; i < d.NE; i += G * PERS_THREADS) update_cell<NSP>(d, th, i, err);
   flag(d, err);
 }
 
@@ -727,6 +762,18 @@ __global__ void k_soa_to_aos(const double* __restrict__ s, double* __restrict__ 
   a[t] = s[(long)k * N + i];
 }
 
+// Mixed-precision launchers (rc_mixed.cu).
+template <int NSP> void mixed_ts_face(const Dev&, const void*, int, cudaStream_t);
+template <int NSP> void mixed_cell(const Dev&, const void*, const ThermoDev<NSP>&, int, int, int, int, cudaStream_t);
+template <int NSP> void mixed_face_flux(const Dev&, const void*, int, cudaStream_t);
+template <int NSP> void mixed_gather(const Dev&, int, int, cudaStream_t);
+template <int NSP> void mixed_sweep(const Dev&, const void*, bool, const int*, int, cudaStream_t);
+template <int NSP> size_t mixed_thermo(const void*, void*);
+template <int NSP>
+cudaError_t mixed_lusgs_persistent(const Dev&, const void*, const ThermoDev<NSP>&, const int*, const int*, int,
+                                   const int*, const int*, int, unsigned*, int, cudaStream_t);
+template <int NSP> int mixed_persistent_occupancy();
+
 }  // namespace rc
 
 // ======================================================== host context =====
@@ -740,14 +787,23 @@ struct rc_ctx {
   bool own_stream = false;
   Dev d{};
   std::vector<void*> allocs;
-  std::vector<char> thermo;  // ThermoDev<NSP> bytes
+  std::vector<char> thermo;    // ThermoDev<NSP> bytes
+  std::vector<char> thermo32;  // ThermoDev32<NSP> bytes (mixed precision)
+  int mode = RC_PREC_FP64;     // current precision mode
   int* fwd_cells = nullptr;
   int* bwd_cells = nullptr;
   std::vector<int> fwd_off, bwd_off;
+  bool persistent = true;       // LU-SGS sweeps as one cooperative launch (else one launch per level)
+  int pers_grid = 0;             // blocks of the persistent launch (one per SM)
+  unsigned* bar_count = nullptr; // grid-barrier counter of the persistent launch
+  int* fwd_off_dev = nullptr;
+  int* bwd_off_dev = nullptr;
   double* norm_part = nullptr;
   double* norm_out = nullptr;
   double* staging = nullptr;  // (V*max(NE,NF,NG)) for layout conversion
-  cudaGraphExec_t graph = nullptr;
+  cudaGraphExec_t graph = nullptr;       // graph of the current mode
+  cudaGraphExec_t graphs[3] = {nullptr, nullptr, nullptr};
+  long long graph_kernels_of[3] = {0, 0, 0};
   long long graph_kernels = 0;
   long long launches = 0;
   std::string err;
@@ -811,7 +867,7 @@ void fill_thermo(const rc_thermo* t, const rc_config* g, ThermoDev<NSP>& th) {
   for (int i = 0; i < NSP; ++i)
     for (int j = 0; j < NSP; ++j) {
       const double mi = t->mole_weight[i], mj = t->mole_weight[j];
-      th.wc[i][j] = std::pow(mj / mi, 0.25);
+      th.wc[i][j] = rcm::pow(mj / mi, 0.25);
       th.wd[i][j] = std::sqrt(1. + mi / mj);
       th.dlj[i][j] = std::sqrt(t->LJ_energy[i] * t->LJ_energy[j]);
       th.dmw[i][j] = std::sqrt(2. / (1. / mi + 1. / mj) * 1000);
@@ -855,17 +911,37 @@ void q_face_flux(rc_ctx* c) {
   c->launches++;
 }
 template <int NSP>
+void q_persistent(rc_ctx* c) {
+  cudaMemsetAsync(c->bar_count, 0, sizeof(unsigned), c->stream);
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = dim3((unsigned)c->pers_grid);
+  cfg.blockDim = dim3(PERS_THREADS);
+  cfg.stream = c->stream;
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeCooperative;
+  attr[0].val.cooperative = 1;
+  cfg.attrs = attr;
+  cfg.numAttrs = 1;
+  cudaLaunchKernelEx(&cfg, k_lusgs_persistent<NSP>, c->d, TH<NSP>(c), (const int*)c->fwd_cells,
+                     (const int*)c->fwd_off_dev, (int)c->fwd_off.size() - 1, (const int*)c->bwd_cells,
+                     (const int*)c->bwd_off_dev, (int)c->bwd_off.size() - 1, c->bar_count);
+  c->launches++;
+}
+template <int NSP>
 void q_sweeps(rc_ctx* c, int gather) {
+  if (gather) {
+    k_gather<NSP><<<blocks(c->NE, 128), 128, 0, c->stream>>>(c->d, c->visc, c->comb);
+    c->launches++;
+  }
+  if (c->persistent) { q_persistent<NSP>(c); return; }
   for (size_t l = 0; l + 1 < c->fwd_off.size(); ++l) {
     const int n = c->fwd_off[l + 1] - c->fwd_off[l];
-    k_sweep<NSP, true><<<blocks(n, 128), 128, 0, c->stream>>>(c->d, TH<NSP>(c), c->fwd_cells + c->fwd_off[l], n,
-                                                              gather, c->visc, c->comb);
+    k_sweep4<NSP, true><<<blocks(4L * n, 32), 32, 0, c->stream>>>(c->d, TH<NSP>(c), c->fwd_cells + c->fwd_off[l], n);
     c->launches++;
   }
   for (size_t l = 0; l + 1 < c->bwd_off.size(); ++l) {
     const int n = c->bwd_off[l + 1] - c->bwd_off[l];
-    k_sweep<NSP, false><<<blocks(n, 128), 128, 0, c->stream>>>(c->d, TH<NSP>(c), c->bwd_cells + c->bwd_off[l], n,
-                                                               0, c->visc, c->comb);
+    k_sweep4<NSP, false><<<blocks(4L * n, 32), 32, 0, c->stream>>>(c->d, TH<NSP>(c), c->bwd_cells + c->bwd_off[l], n);
     c->launches++;
   }
   k_update<NSP><<<blocks(c->NE, 128), 128, 0, c->stream>>>(c->d, TH<NSP>(c));
@@ -876,12 +952,81 @@ void q_gather(rc_ctx* c) {
   k_gather<NSP><<<blocks(c->NE, 128), 128, 0, c->stream>>>(c->d, c->visc, c->comb);
   c->launches++;
 }
+// Sweeps of the mixed-precision modes: FP32 off-diagonal terms, FP64 division.
+template <int NSP>
+void q_sweeps32(rc_ctx* c) {
+  if (c->persistent) {
+    mixed_lusgs_persistent<NSP>(c->d, c->thermo32.data(), TH<NSP>(c), c->fwd_cells, c->fwd_off_dev,
+                                (int)c->fwd_off.size() - 1, c->bwd_cells, c->bwd_off_dev, (int)c->bwd_off.size() - 1,
+                                c->bar_count, c->pers_grid, c->stream);
+    c->launches++;
+    return;
+  }
+  for (size_t l = 0; l + 1 < c->fwd_off.size(); ++l) {
+    mixed_sweep<NSP>(c->d, c->thermo32.data(), true, c->fwd_cells + c->fwd_off[l], c->fwd_off[l + 1] - c->fwd_off[l],
+                     c->stream);
+    c->launches++;
+  }
+  for (size_t l = 0; l + 1 < c->bwd_off.size(); ++l) {
+    mixed_sweep<NSP>(c->d, c->thermo32.data(), false, c->bwd_cells + c->bwd_off[l], c->bwd_off[l + 1] - c->bwd_off[l],
+                     c->stream);
+    c->launches++;
+  }
+  k_update<NSP><<<blocks(c->NE, 128), 128, 0, c->stream>>>(c->d, TH<NSP>(c));
+  c->launches++;
+}
+// The subroutines of one iteration in the current precision mode.
+template <int NSP>
+void q_timestep_mode(rc_ctx* c) {
+  if (c->mode == RC_PREC_FP64) { q_timestep_face<NSP>(c); q_cell<NSP>(c, 1, 0); return; }
+  mixed_ts_face<NSP>(c->d, c->thermo32.data(), c->visc, c->stream);
+  c->launches++;
+  q_cell<NSP>(c, 1, 0);
+}
+template <int NSP>
+void q_reconstruction_mode(rc_ctx* c) {
+  if (c->mode == RC_PREC_MIXED) {
+    mixed_cell<NSP>(c->d, c->thermo32.data(), TH<NSP>(c), 0, c->limit, c->comb, c->visc, c->stream);
+    c->launches++;
+  } else {
+    q_cell<NSP>(c, 0, 1);
+  }
+}
+template <int NSP>
+void q_flux_mode(rc_ctx* c) {
+  if (c->mode == RC_PREC_MIXED) {
+    mixed_face_flux<NSP>(c->d, c->thermo32.data(), c->visc, c->stream);
+    mixed_gather<NSP>(c->d, c->visc, c->comb, c->stream);
+    c->launches += 2;
+  } else {
+    q_face_flux<NSP>(c);
+    q_gather<NSP>(c);
+  }
+}
+template <int NSP>
+void q_lusgs_mode(rc_ctx* c) {
+  if (c->mode == RC_PREC_FP64) q_sweeps<NSP>(c, 0);
+  else q_sweeps32<NSP>(c);
+}
 template <int NSP>
 void q_stage(rc_ctx* c) {
-  q_timestep_face<NSP>(c);
-  q_cell<NSP>(c, 1, 1);
-  q_face_flux<NSP>(c);
-  q_sweeps<NSP>(c, 1);
+  if (c->mode == RC_PREC_FP64) {
+    q_timestep_face<NSP>(c);
+    q_cell<NSP>(c, 1, 1);
+    q_face_flux<NSP>(c);
+    q_sweeps<NSP>(c, 1);
+    return;
+  }
+  mixed_ts_face<NSP>(c->d, c->thermo32.data(), c->visc, c->stream);
+  c->launches++;
+  if (c->mode == RC_PREC_MIXED) {
+    mixed_cell<NSP>(c->d, c->thermo32.data(), TH<NSP>(c), 1, c->limit, c->comb, c->visc, c->stream);
+    c->launches++;
+  } else {
+    q_cell<NSP>(c, 1, 1);
+  }
+  q_flux_mode<NSP>(c);
+  q_sweeps32<NSP>(c);
 }
 
 #define RC_DISPATCH(c, fn, ...)                  \
@@ -926,7 +1071,8 @@ int rc_init(const rc_mesh* m, const rc_thermo* t, const rc_config* g, rc_ctx** o
   if (c->comb && c->NSP < 2) return bail(RC_ERR_ARG, "combustion needs at least two species");
   if (t->order_of_cp_polynomial != 7) return bail(RC_ERR_ARG, "order_of_cp_polynomial must be 7");
   if (m->MaxNei > MAXF) return bail(RC_ERR_ARG, "cells with more than 4 faces");
-  if (g->precision != RC_PREC_FP64) return bail(RC_ERR_ARG, "precision mode not available in this build");
+  if (g->precision != RC_PREC_FP64 && g->precision != RC_PREC_MIXED && g->precision != RC_PREC_MIXED_DC)
+    return bail(RC_ERR_ARG, "unknown precision mode");
   if (cudaSetDevice(g->device) != cudaSuccess) return bail(RC_ERR_CUDA, "cudaSetDevice failed");
   if (cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking) != cudaSuccess)
     return bail(RC_ERR_CUDA, "cudaStreamCreate failed");
@@ -1066,10 +1212,15 @@ int rc_init(const rc_mesh* m, const rc_thermo* t, const rc_config* g, rc_ctx** o
   if (c->NSP == 1) {
     c->thermo.resize(sizeof(ThermoDev<1>));
     fill_thermo<1>(t, g, *reinterpret_cast<ThermoDev<1>*>(c->thermo.data()));
+    c->thermo32.resize(mixed_thermo<1>(nullptr, nullptr));
+    mixed_thermo<1>(c->thermo.data(), c->thermo32.data());
   } else {
     c->thermo.resize(sizeof(ThermoDev<4>));
     fill_thermo<4>(t, g, *reinterpret_cast<ThermoDev<4>*>(c->thermo.data()));
+    c->thermo32.resize(mixed_thermo<4>(nullptr, nullptr));
+    mixed_thermo<4>(c->thermo.data(), c->thermo32.data());
   }
+  c->mode = g->precision;
 
   // ---- upload
   Dev& d = c->d;
@@ -1124,17 +1275,47 @@ int rc_init(const rc_mesh* m, const rc_thermo* t, const rc_config* g, rc_ctx** o
   st |= dev_zeros(c, (size_t)(V + 1) * NRM_BLOCKS, &c->norm_part);
   st |= dev_zeros(c, (size_t)(V + 1), &c->norm_out);
   st |= dev_zeros(c, (size_t)2 * V * std::max(std::max(NE, NF), NG), &c->staging);
+  if (g->precision != RC_PREC_FP64) {  // FP32 work arrays of the mixed modes
+    double* f32;
+    st |= dev_zeros(c, ((size_t)2 * V * NE + 1) / 2, &f32); d.grad32 = reinterpret_cast<float*>(f32);
+    st |= dev_zeros(c, ((size_t)V * std::max(NG, 1) + 1) / 2, &f32); d.GPA32 = reinterpret_cast<float*>(f32);
+    st |= dev_zeros(c, ((size_t)V * NF + 1) / 2, &f32); d.Finv32 = reinterpret_cast<float*>(f32);
+    st |= dev_zeros(c, ((size_t)(V - 1) * NF + 1) / 2, &f32); d.Fvis32 = reinterpret_cast<float*>(f32);
+  }
   double* e;
   st |= dev_zeros(c, 1, &e);
   d.err = reinterpret_cast<unsigned*>(e);
+  st |= dev_zeros(c, 1, &e);
+  c->bar_count = reinterpret_cast<unsigned*>(e);
+  st |= dev_upload(c, c->fwd_off, &c->fwd_off_dev);
+  st |= dev_upload(c, c->bwd_off, &c->bwd_off_dev);
   if (st) return bail(st, c->err);
+  // LU-SGS schedule: one cooperative launch per iteration when every SM can
+  // hold a block of the persistent kernels; RC_LUSGS_SCHEDULE=levels selects
+  // one launch per level instead.
+  {
+    int nsm = 0, occ64 = 0, occ32 = 0, coop = 0;
+    cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, g->device);
+    cudaDeviceGetAttribute(&coop, cudaDevAttrCooperativeLaunch, g->device);
+    if (c->NSP == 1) {
+      cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ64, k_lusgs_persistent<1>, PERS_THREADS, 0);
+      occ32 = mixed_persistent_occupancy<1>();
+    } else {
+      cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ64, k_lusgs_persistent<4>, PERS_THREADS, 0);
+      occ32 = mixed_persistent_occupancy<4>();
+    }
+    const char* sched = std::getenv("RC_LUSGS_SCHEDULE");
+    c->pers_grid = nsm;
+    c->persistent = coop && nsm > 0 && occ64 >= 1 && occ32 >= 1 && !(sched && std::string(sched) == "levels");
+  }
   *out = c;
   return RC_OK;
 }
 
 int rc_finalize(rc_ctx* c) {
   if (!c) return RC_OK;
-  if (c->graph) cudaGraphExecDestroy(c->graph);
+  for (auto& gx : c->graphs)
+    if (gx) cudaGraphExecDestroy(gx);
   for (void* p : c->allocs) cudaFree(p);
   if (c->own_stream && c->stream) cudaStreamDestroy(c->stream);
   delete c;
@@ -1143,7 +1324,9 @@ int rc_finalize(rc_ctx* c) {
 
 int rc_set_stream(rc_ctx* c, void* s) {
   if (!c) return RC_ERR_ARG;
-  if (c->graph) { cudaGraphExecDestroy(c->graph); c->graph = nullptr; }
+  for (auto& gx : c->graphs)
+    if (gx) { cudaGraphExecDestroy(gx); gx = nullptr; }
+  c->graph = nullptr;
   if (c->own_stream && c->stream) cudaStreamDestroy(c->stream);
   c->stream = static_cast<cudaStream_t>(s);
   c->own_stream = false;
@@ -1203,7 +1386,6 @@ int rc_set_array(rc_ctx* c, const char* name, const double* in) {
   if (!c || !name || !in) return RC_ERR_ARG;
   double* p; int N, V, gr;
   if (array_desc(c, name, &p, &N, &V, &gr)) return RC_ERR_ARG;
-  if (c->graph) { cudaGraphExecDestroy(c->graph); c->graph = nullptr; }
   return put_soa(c, in, p, N, V);
 }
 
@@ -1212,25 +1394,35 @@ int rc_set_array(rc_ctx* c, const char* name, const double* in) {
 
 int rc_timestep(rc_ctx* c) {
   RC_NSP_OK(c);
-  RC_DISPATCH(c, q_timestep_face, c);
-  RC_DISPATCH(c, q_cell, c, 1, 0);
+  RC_DISPATCH(c, q_timestep_mode, c);
   return check_launch(c, "rc_timestep");
 }
 int rc_reconstruction(rc_ctx* c) {
   RC_NSP_OK(c);
-  RC_DISPATCH(c, q_cell, c, 0, 1);
+  RC_DISPATCH(c, q_reconstruction_mode, c);
   return check_launch(c, "rc_reconstruction");
 }
 int rc_flux_sourceterm(rc_ctx* c) {
   RC_NSP_OK(c);
-  RC_DISPATCH(c, q_face_flux, c);
-  RC_DISPATCH(c, q_gather, c);
+  RC_DISPATCH(c, q_flux_mode, c);
   return check_launch(c, "rc_flux_sourceterm");
 }
 int rc_lusgs_steady(rc_ctx* c) {
   RC_NSP_OK(c);
-  RC_DISPATCH(c, q_sweeps, c, 0);
+  RC_DISPATCH(c, q_lusgs_mode, c);
   return check_launch(c, "rc_lusgs_steady");
+}
+int rc_set_precision(rc_ctx* c, int precision) {
+  if (!c) return RC_ERR_ARG;
+  if (precision != RC_PREC_FP64 && precision != RC_PREC_MIXED && precision != RC_PREC_MIXED_DC) return RC_ERR_ARG;
+  if (precision != RC_PREC_FP64 && !c->d.grad32) {
+    c->err = "mixed-precision modes need a context created with RC_PREC_MIXED or RC_PREC_MIXED_DC";
+    return RC_ERR_ARG;
+  }
+  c->mode = precision;
+  c->graph = c->graphs[precision];
+  c->graph_kernels = c->graph_kernels_of[precision];
+  return RC_OK;
 }
 int rc_lusgs_stage(rc_ctx* c, int istep) {
   (void)istep;
@@ -1247,6 +1439,8 @@ int rc_lusgs_stage(rc_ctx* c, int istep) {
     e = cudaGraphInstantiate(&c->graph, gph, 0);
     cudaGraphDestroy(gph);
     if (e != cudaSuccess) return cuda_fail(c, e, "cudaGraphInstantiate");
+    c->graphs[c->mode] = c->graph;
+    c->graph_kernels_of[c->mode] = c->graph_kernels;
   }
   RC_CU(cudaGraphLaunch(c->graph, c->stream));
   c->launches += c->graph_kernels;

@@ -1,0 +1,137 @@
+// Device layout shared by the FP64 and mixed-precision kernels.
+#pragma once
+#include <cstdint>
+
+#include "rc_thermo.cuh"
+
+namespace rc {
+
+constexpr int MAXF = 4;  // faces per cell (triangles and quadrilaterals)
+
+struct Dev {
+  int NE, NF, NG;
+  // cells
+  const double* vol;
+  const double* rinv;            // [2*NE] 1./reflen
+  const unsigned char* nface;    // KFace
+  const unsigned char* cleft;    // bit q: cell is Neighbor(1,.) of its face q
+  const int* cface;              // [4*NE] NeighF, 0-based
+  const int* cother;             // [4*NE] cell across face q, -1 on a boundary
+  const unsigned char* nnei;     // Neigh
+  const int* cnei;               // [4*NE] NeighC(1:Neigh), 0-based
+  const unsigned char* ngh;      // Num_ghostcell
+  const int* cgh;                // [4*NE] Ghostcell, 0-based
+  const double* wdis;            // [4*NE]
+  const double* amls;            // [8*NE] AMLS(r,q,i) at (2q+r)*NE+i
+  const double* lvvh;            // [8*NE] limiter basis values at the face midpoints
+  // faces
+  const int* fNL;                // 0-based
+  const int* fNR;                // 0-based cell, or -BC code
+  const double* fvec;            // [2*NF] VECX
+  const double* fsav;            // max(|VECX|, small)
+  const double* fsn;             // [2*NF] unit normal
+  const double* fss;             // sqrt(dx*dx+dy*dy)
+  const double* fs2;             // dx*dx+dy*dy
+  const double* fvL;             // [2*NF] fbaseAll at the Gauss point for NL
+  const double* fvR;             // [2*NF] fbaseAll at the Gauss point for NR
+  const double* fdxk;            // |(x_L - x_R).n|
+  const double* fysn;            // [2*NF] yita*n
+  // ghosts
+  const int* gtype;
+  const double* gsn;             // [2*NG] ghost-face unit normal
+  // state and work arrays
+  double* PA;
+  double* WA;
+  double* hWA;
+  double* grad;
+  double* GPA;
+  double* step;
+  double* dd;
+  double* cst;                   // [(3+NSP)*NE]: rho, gamma, rho*E, h_k
+  double* src;                   // [(NSP-1)*NE]: vol*omega_k
+  double* alpa;
+  double* visL;
+  double* visR;
+  double* alpaF;
+  double* Finv;                  // [V*NF]
+  double* Fvis;                  // [(V-1)*NF], component 1 is identically zero
+  unsigned* err;
+  // mixed precision (allocated only for RC_PREC_MIXED)
+  float* grad32;                 // [2*V*NE]
+  float* GPA32;                  // [V*NG]
+  float* Finv32;                 // [V*NF]
+  float* Fvis32;                 // [(V-1)*NF]
+};
+
+__device__ __forceinline__ void flag(const Dev& d, unsigned e) {
+  if (e) atomicOr(d.err, e);
+}
+
+__device__ __forceinline__ void removedirection(double& vx, double& vy, double nx, double ny) {
+  const double vn = vx * nx + vy * ny;  // flux_viscous.f90:352-361
+  vx = vx - vn * nx;
+  vy = vy - vn * ny;
+}
+
+__device__ __forceinline__ unsigned ld_acquire(const unsigned* p) {
+  unsigned v;
+  asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+  return v;
+}
+
+// Grid-wide barrier of a cooperative (all blocks co-resident) launch.  `count`
+// is zeroed before the launch and `seq` numbers the barriers of the launch.
+// The wait is bounded: after about 2^22 polls, or as soon as another block has
+// given up, ERR_SYNC is latched and every block returns false so the kernel
+// can exit instead of waiting forever.
+__device__ __forceinline__ bool grid_sync(unsigned* count, unsigned seq, unsigned* err) {
+  __shared__ int ok;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    __threadfence();
+    atomicAdd(count, 1u);
+    const unsigned target = (seq + 1u) * gridDim.x;
+    int good = 1;
+    for (unsigned spin = 0; ld_acquire(count) < target; ++spin) {
+      if (spin > (1u << 22) || (ld_acquire(err) & ERR_SYNC)) {
+        atomicOr(err, ERR_SYNC);
+        good = 0;
+        break;
+      }
+      __nanosleep(32);
+    }
+    __threadfence();
+    ok = good;
+  }
+  __syncthreads();
+  return ok != 0;
+}
+
+// WA += hWA and update_primitve_variables (update_flow_variables.f90:112-156).
+template <int NSP>
+__device__ __forceinline__ void update_cell(const Dev& d, const ThermoDev<NSP>& th, int i, unsigned& err) {
+  constexpr int V = 3 + NSP;
+  const int NE = d.NE;
+  double W[V];
+#pragma unroll
+  for (int k = 0; k < V; ++k) {
+    W[k] = d.WA[k * NE + i] + d.hWA[k * NE + i];
+    d.WA[k * NE + i] = W[k];
+  }
+  const double rho = W[0], u = W[1] / rho, v = W[2] / rho;
+  double Y[NSP], s = 0.0;
+#pragma unroll
+  for (int k = 0; k < NSP - 1; ++k) { Y[k] = W[4 + k] / rho; s = s + Y[k]; }
+  Y[NSP - 1] = 1.0 - s;
+  double Rcpcv;
+  const double t = newton_T<NSP>(th, W[3] / rho - 0.5 * (u * u + v * v), Y, d.PA[3 * NE + i], Rcpcv, err);
+  d.PA[0 * NE + i] = rho * Rcpcv * t;
+  d.PA[1 * NE + i] = u;
+  d.PA[2 * NE + i] = v;
+  d.PA[3 * NE + i] = t;
+#pragma unroll
+  for (int k = 0; k < NSP - 1; ++k) d.PA[(4 + k) * NE + i] = Y[k];
+  if (i == 0 && isnan(W[0])) err |= ERR_NAN;
+}
+
+}  // namespace rc

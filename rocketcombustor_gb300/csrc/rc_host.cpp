@@ -17,6 +17,7 @@
 #include <vector>
 
 #include "rc_host.h"
+#include "rc_math.h"
 
 namespace {
 
@@ -417,7 +418,7 @@ void rc_case::gas(const double* Y, double T, double& Cp, double& gama, double& R
 // compute_enthalpy (thermo_property.f90:191-221), host copy.
 void rc_case::enthalpy(double T, double* h) const {
   const double t2 = T * T;
-  const double e[7] = {-(1.0 / t2), std::log(T) / T, 1.0, T / 2.0, t2 / 3.0, (T * t2) / 4.0, (t2 * t2) / 5.0};
+  const double e[7] = {-(1.0 / t2), rcm::log(T) / T, 1.0, T / 2.0, t2 / 3.0, (T * t2) / 4.0, (t2 * t2) / 5.0};
   const bool low = (tlo <= T && T <= tcr);
   if (!low && !(tcr < T && T <= thi)) throw std::runtime_error("temperature out of the thermo range");
   const std::vector<double>& c = low ? cl : ch;

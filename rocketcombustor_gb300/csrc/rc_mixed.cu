@@ -1,0 +1,689 @@
+// Mixed-precision form of the steady iteration (RC_PREC_MIXED / RC_PREC_MIXED_DC).
+//
+//   FP32: spectral radius, reconstruction (ghost states, LS gradient, Barth
+//         limiter), Lax/Rusanov and viscous face fluxes, and the LU-SGS
+//         off-diagonal terms;
+//   FP64: the state (PA, WA), the local step and the LU-SGS diagonal with its
+//         division, the chemical source, the per-cell residual after a
+//         compensated (Neumaier) FP32 gather, the Newton update and the norms.
+// In the defect-correction phase (RC_PREC_MIXED_DC) the residual comes from the
+// FP64 kernels of rc_core.cu while the LU-SGS sweeps stay in FP32, so the fixed
+// point is the FP64 one.
+//
+// Built with --use_fast_math (FP32 SFU math, FMA contraction); double
+// arithmetic is unaffected by that flag apart from contraction.
+#include <cuda_runtime.h>
+
+#include "rc_dev.cuh"
+#include "rc_thermo32.cuh"
+
+namespace rc {
+
+// ----------------------------------------------------------- TimeStep ------
+template <int NSP, bool VISC>
+__global__ void __launch_bounds__(128) k_ts_face32(const Dev d, const ThermoDev32<NSP> th) {
+  constexpr int V = 3 + NSP;
+  const int f = blockIdx.x * blockDim.x + threadIdx.x;
+  if (f >= d.NF) return;
+  unsigned err = 0;
+  const int NE = d.NE, NL = d.fNL[f], NR = d.fNR[f];
+  float P[V], yy[NSP];
+#pragma unroll
+  for (int k = 0; k < V; ++k)
+    P[k] = (NR >= 0) ? (float)(0.5 * (d.PA[k * NE + NL] + d.PA[k * NE + NR])) : (float)d.PA[k * NE + NL];
+  float s = 0.f;
+#pragma unroll
+  for (int k = 0; k < NSP - 1; ++k) { yy[k] = P[4 + k]; s += yy[k]; }
+  yy[NSP - 1] = 1.f - s;
+  float Cp, gama, Rc;
+  gas32<NSP>(th, yy, P[3], Cp, gama, Rc, err);
+  const float rr = P[0] / (Rc * P[3]);
+  if (rr < 0.f || P[0] < 0.f || P[3] < 0.f) err |= ERR_NEG_TIMESTEP;
+  const float un = P[1] * (float)d.fvec[f] + P[2] * (float)d.fvec[d.NF + f];
+  const float alpa = fabsf(un) + sqrtf(gama * P[0] / rr) * (float)d.fss[f];
+  d.alpa[f] = alpa;
+  if (VISC) {
+    float vmul, akmu;
+    transport32<NSP>(th, P[3], yy, vmul, akmu, err);
+    const float prl = vmul * Cp / akmu;
+    const double vis = (double)(2.f * (float)d.fs2[f] * fmax2f(4.f / 3.f, gama / prl) * vmul / rr);
+    const double vl = vis / d.vol[NL];
+    d.visL[f] = vl;
+    d.visR[f] = (NR >= 0) ? vis / d.vol[NR] : 0.0;
+    d.alpaF[f] = (double)alpa + vl;
+  } else {
+    d.alpaF[f] = alpa;
+  }
+  if (err) atomicOr(d.err, err);
+}
+
+// --------------------------------------------------------- cell kernel -----
+template <int NSP>
+__global__ void __launch_bounds__(128) k_cell32(const Dev d, const ThermoDev32<NSP> th, const ThermoDev<NSP> th64,
+                                                int do_step, int limit, int comb, int visc) {
+  constexpr int V = 3 + NSP;
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= d.NE) return;
+  const int NE = d.NE;
+  unsigned err = 0;
+  const int nf = d.nface[i];
+  const double vol = d.vol[i];
+  if (do_step) {  // FP64: local step and LU-SGS diagonal
+    const unsigned lb = d.cleft[i];
+    double acc = 0.0, dsum = 0.0;
+    for (int q = 0; q < nf; ++q) {
+      const int f = d.cface[q * NE + i];
+      acc = visc ? acc + d.alpa[f] + (((lb >> q) & 1u) ? d.visL[f] : d.visR[f]) : acc + d.alpa[f];
+      dsum += 0.5 * d.alpaF[f];
+    }
+    const double st = th64.cfl * vol / acc;
+    d.step[i] = st;
+    d.dd[i] = dsum + vol / st;
+  }
+  double P64[V];
+  float P[V], Y[NSP];
+#pragma unroll
+  for (int k = 0; k < V; ++k) { P64[k] = d.PA[k * NE + i]; P[k] = (float)P64[k]; }
+  float s = 0.f;
+#pragma unroll
+  for (int k = 0; k < NSP - 1; ++k) { Y[k] = P[4 + k]; s += Y[k]; }
+  Y[NSP - 1] = 1.f - s;
+  float Cp, gama, Rc, entha[NSP];
+  gas32<NSP>(th, Y, P[3], Cp, gama, Rc, err);
+  const float rr = P[0] / (Rc * P[3]);
+  enthalpy32<NSP>(th, P[3], entha, err);
+  float hh = 0.f;
+#pragma unroll
+  for (int k = 0; k < NSP; ++k) hh += Y[k] * entha[k];
+  d.cst[0 * NE + i] = rr;
+  d.cst[1 * NE + i] = gama;
+  d.cst[2 * NE + i] = rr * (hh + 0.5f * (P[1] * P[1] + P[2] * P[2])) - P[0];
+#pragma unroll
+  for (int k = 0; k < NSP; ++k) d.cst[(3 + k) * NE + i] = entha[k];
+  // gradient: differences in FP64, weights and sums in FP32
+  float g0[V], g1[V], mn[V], mx[V];
+#pragma unroll
+  for (int k = 0; k < V; ++k) { g0[k] = 0.f; g1[k] = 0.f; mn[k] = 0.f; mx[k] = 0.f; }
+  const int nn = d.nnei[i];
+  for (int q = 0; q < nn; ++q) {
+    const int j = d.cnei[q * NE + i];
+    const float w = (float)d.wdis[q * NE + i], a0 = (float)d.amls[(2 * q) * NE + i],
+                a1 = (float)d.amls[(2 * q + 1) * NE + i];
+#pragma unroll
+    for (int k = 0; k < V; ++k) {
+      const float dlt = (float)(d.PA[k * NE + j] - P64[k]);
+      const float c = w * dlt;
+      g0[k] += a0 * c;
+      g1[k] += a1 * c;
+      mn[k] = fmin2f(mn[k], dlt);
+      mx[k] = fmax2f(mx[k], dlt);
+    }
+  }
+  const int ng = d.ngh[i];
+  for (int q = 0; q < ng; ++q) {
+    const int gj = d.cgh[q * NE + i];
+    const float s1n = (float)d.gsn[gj], s2n = (float)d.gsn[d.NG + gj];
+    const float pl = P[0], ul = P[1], vl = P[2], tl = P[3];
+    const float ac = sqrtf(gama * pl / rr);
+    float G[V], Yr[NSP];
+    float pr = pl, ur = ul, vr = vl, tr = tl, vn;
+#pragma unroll
+    for (int k = 0; k < NSP; ++k) Yr[k] = Y[k];
+    switch (d.gtype[gj]) {
+      case 1: ur = -ul; vr = -vl; break;
+      case 2:
+      case 6:
+        vn = ul * s1n + vl * s2n;
+        ur = ul - 2.f * vn * s1n;
+        vr = vl - 2.f * vn * s2n;
+        break;
+      case 3:
+      case 4: {
+        const int w = d.gtype[gj] == 3 ? 0 : 1;
+#pragma unroll
+        for (int k = 0; k < NSP; ++k) Yr[k] = th.inY[w][k];
+        tr = th.inT[w];
+        float Cb, gb, Rb;
+        gas32<NSP>(th, Yr, tr, Cb, gb, Rb, err);
+        const float rb = pr / (Rb * tr);
+        ur = th.inMflow[w] / rb;
+        vr = 0.f;
+        break;
+      }
+      case 5:
+        vn = ul * s1n + vl * s2n;
+        if (!(fabsf(vn) > ac)) pr = th.p_out;
+        break;
+      default: err |= ERR_BCTYPE;
+    }
+    G[0] = pr; G[1] = ur; G[2] = vr; G[3] = tr;
+#pragma unroll
+    for (int k = 0; k < NSP - 1; ++k) G[4 + k] = Yr[k];
+#pragma unroll
+    for (int k = 0; k < V; ++k) d.GPA32[k * d.NG + gj] = G[k];
+    const int m = nn + q;
+    const float w = (float)d.wdis[m * NE + i], a0 = (float)d.amls[(2 * m) * NE + i],
+                a1 = (float)d.amls[(2 * m + 1) * NE + i];
+#pragma unroll
+    for (int k = 0; k < V; ++k) {
+      const float dlt = G[k] - P[k];
+      const float c = w * dlt;
+      g0[k] += a0 * c;
+      g1[k] += a1 * c;
+      mn[k] = fmin2f(mn[k], dlt);
+      mx[k] = fmax2f(mx[k], dlt);
+    }
+  }
+  if (limit > 0) {  // Barth: phi = min over faces of min(1, (max-P)/(f-P)) or (min-P)/(f-P)
+    float lv0[MAXF], lv1[MAXF];
+    for (int q = 0; q < nf; ++q) { lv0[q] = (float)d.lvvh[(2 * q) * NE + i]; lv1[q] = (float)d.lvvh[(2 * q + 1) * NE + i]; }
+#pragma unroll
+    for (int k = 0; k < V; ++k) {
+      float phi = 1.f;
+      for (int q = 0; q < nf; ++q) {
+        const float df = g0[k] * lv0[q] + g1[k] * lv1[q];
+        float pf = 1.f;
+        if (df > 0.f) pf = fmin2f(1.f, mx[k] / df);
+        else if (df < 0.f) pf = fmin2f(1.f, mn[k] / df);
+        phi = fmin2f(phi, pf);
+      }
+      g0[k] *= phi;
+      g1[k] *= phi;
+    }
+  }
+#pragma unroll
+  for (int k = 0; k < V; ++k) {
+    d.grad32[(2 * k) * NE + i] = g0[k];
+    d.grad32[(2 * k + 1) * NE + i] = g1[k];
+  }
+  if (comb) {  // FP64 chemistry
+    double Y64[NSP], s64 = 0.0, R64 = 0.0;
+#pragma unroll
+    for (int k = 0; k < NSP - 1; ++k) { Y64[k] = P64[4 + k]; s64 += Y64[k]; }
+    Y64[NSP - 1] = 1.0 - s64;
+#pragma unroll
+    for (int k = 0; k < NSP; ++k) R64 += th64.R[k] * Y64[k];
+    double prod[NSP];
+    production<NSP>(th64, P64[3], P64[0] / (R64 * P64[3]), Y64, prod);
+#pragma unroll
+    for (int k = 0; k < NSP - 1; ++k) d.src[k * NE + i] = vol * prod[k];
+  }
+  if (err) atomicOr(d.err, err);
+}
+
+// ------------------------------------------------------------ face flux ----
+template <int NSP, bool VISC>
+__global__ void __launch_bounds__(128) k_face_flux32(const Dev d, const ThermoDev32<NSP> th) {
+  constexpr int V = 3 + NSP;
+  const int f = blockIdx.x * blockDim.x + threadIdx.x;
+  if (f >= d.NF) return;
+  unsigned err = 0;
+  const int NE = d.NE, NF = d.NF;
+  const int NL = d.fNL[f], NR = d.fNR[f];
+  const float sav1 = (float)d.fvec[f], sav2 = (float)d.fvec[NF + f], sav = (float)d.fsav[f];
+  const float sn1 = (float)d.fsn[f], sn2 = (float)d.fsn[NF + f];
+  float uL[V], uR[V], YL0[NSP], YR0[NSP];
+  {
+    const float v0 = (float)d.fvL[f], v1 = (float)d.fvL[NF + f];
+#pragma unroll
+    for (int k = 0; k < V; ++k)
+      uL[k] = (float)d.PA[k * NE + NL] + (d.grad32[(2 * k) * NE + NL] * v0 + d.grad32[(2 * k + 1) * NE + NL] * v1);
+  }
+  float s = 0.f;
+#pragma unroll
+  for (int k = 0; k < NSP - 1; ++k) { YL0[k] = uL[4 + k]; s += YL0[k]; }
+  YL0[NSP - 1] = 1.f - s;
+  float Cl0, gl0, Rl0;
+  gas32<NSP>(th, YL0, uL[3], Cl0, gl0, Rl0, err);
+  const float rl0 = uL[0] / (Rl0 * uL[3]);
+  float gr0 = 0.f, Rr0 = 0.f, rr0 = 0.f;
+  if (NR >= 0) {
+    const float v0 = (float)d.fvR[f], v1 = (float)d.fvR[NF + f];
+#pragma unroll
+    for (int k = 0; k < V; ++k)
+      uR[k] = (float)d.PA[k * NE + NR] + (d.grad32[(2 * k) * NE + NR] * v0 + d.grad32[(2 * k + 1) * NE + NR] * v1);
+    s = 0.f;
+#pragma unroll
+    for (int k = 0; k < NSP - 1; ++k) { YR0[k] = uR[4 + k]; s += YR0[k]; }
+    YR0[NSP - 1] = 1.f - s;
+    float Cr0;
+    gas32<NSP>(th, YR0, uR[3], Cr0, gr0, Rr0, err);
+    rr0 = uR[0] / (Rr0 * uR[3]);
+  } else {
+#pragma unroll
+    for (int k = 0; k < V; ++k) uR[k] = uL[k];
+  }
+  // ---- Lax/Rusanov flux
+  {
+    float pl = uL[0], ul = uL[1], vl = uL[2], tl = uL[3], rl = rl0, gl = gl0, Rl = Rl0;
+    float pr, ur, vr, tr, rr, gr, vn;
+    float Yl[NSP], Yr[NSP];
+#pragma unroll
+    for (int k = 0; k < NSP; ++k) Yl[k] = YL0[k];
+    if (NR >= 0) {
+      pr = uR[0]; ur = uR[1]; vr = uR[2]; tr = uR[3]; rr = rr0; gr = gr0;
+#pragma unroll
+      for (int k = 0; k < NSP; ++k) Yr[k] = YR0[k];
+    } else if (NR == -3 || NR == -4) {
+      const int w = NR == -3 ? 0 : 1;
+#pragma unroll
+      for (int k = 0; k < NSP; ++k) Yr[k] = th.inY[w][k];
+      tr = th.inT[w];
+      float Cb, Rb;
+      gas32<NSP>(th, Yr, tr, Cb, gr, Rb, err);
+      pr = pl;
+      rr = pr / (Rb * tr);
+      ur = th.inMflow[w] / rr;
+      vr = 0.f;
+      pl = pr; ul = ur; vl = vr; tl = tr; rl = rr; gl = gr; Rl = Rb;
+#pragma unroll
+      for (int k = 0; k < NSP; ++k) Yl[k] = Yr[k];
+    } else {
+      rr = rl; pr = pl; tr = tl; ur = ul; vr = vl; gr = gl;
+      if (NR == -1) { ur = -ul; vr = -vl; }
+      else if (NR == -2 || NR == -6) {
+        vn = ul * sn1 + vl * sn2;
+        ur = ul - 2.f * vn * sn1;
+        vr = vl - 2.f * vn * sn2;
+      } else if (NR == -5) {
+        const float ac = sqrtf(gl * pl / rl);
+        vn = ul * sn1 + vl * sn2;
+        if (!(fabsf(vn) > ac)) {
+          pr = th.p_out;
+          ur = ul + sn1 * (pl - pr) / (rl * ac);
+          vr = vl + sn2 * (pl - pr) / (rl * ac);
+          rr = rl + (pr - pl) / (ac * ac);
+          tr = pr / (Rl * rr);
+          pl = pr; ul = ur; vl = vr; tl = tr; rl = rr;
+        }
+      } else {
+        err |= ERR_BCTYPE;
+      }
+#pragma unroll
+      for (int k = 0; k < NSP; ++k) Yr[k] = Yl[k];
+    }
+    if (rl < 0.f || pl < 0.f || (NR >= 0 && (rr < 0.f || pr < 0.f))) err |= ERR_NEG_FACE;
+    float entha[NSP];
+    enthalpy32<NSP>(th, tl, entha, err);
+    float hl = 0.f;
+#pragma unroll
+    for (int k = 0; k < NSP; ++k) hl += Yl[k] * entha[k];
+    enthalpy32<NSP>(th, tr, entha, err);
+    float hr = 0.f;
+#pragma unroll
+    for (int k = 0; k < NSP; ++k) hr += Yr[k] * entha[k];
+    hl += 0.5f * (ul * ul + vl * vl);
+    hr += 0.5f * (ur * ur + vr * vr);
+    const float el = hl - pl / rl, er = hr - pr / rr;
+    const float acl = sqrtf(gl * pl / rl), acr = sqrtf(gr * pr / rr);
+    const float uln = sav1 * ul + sav2 * vl, urn = sav1 * ur + sav2 * vr;
+    const float coex = fmax2f(fabsf(uln) + acl * sav, fabsf(urn) + acr * sav);
+    const float rul = rl * uln, rur = rr * urn;
+    d.Finv32[0 * NF + f] = 0.5f * (rul + rur - coex * (rr - rl));
+    d.Finv32[1 * NF + f] = 0.5f * (rul * ul + rur * ur + sav1 * (pl + pr) - coex * (rr * ur - rl * ul));
+    d.Finv32[2 * NF + f] = 0.5f * (rul * vl + rur * vr + sav2 * (pl + pr) - coex * (rr * vr - rl * vl));
+    d.Finv32[3 * NF + f] = 0.5f * (rul * hl + rur * hr - coex * (rr * er - rl * el));
+#pragma unroll
+    for (int k = 0; k < NSP - 1; ++k)
+      d.Finv32[(4 + k) * NF + f] = 0.5f * (rul * Yl[k] + rur * Yr[k] - coex * (rr * Yr[k] - rl * Yl[k]));
+  }
+  // ---- viscous flux
+  if (VISC) {
+    float pl = uL[0], ul = uL[1], vl = uL[2], tl = uL[3];
+    float pr, ur, vr, tr;
+    float Yl[NSP], Yr[NSP];
+#pragma unroll
+    for (int k = 0; k < NSP; ++k) Yl[k] = YL0[k];
+    if (NR >= 0) {
+      pr = uR[0]; ur = uR[1]; vr = uR[2]; tr = uR[3];
+#pragma unroll
+      for (int k = 0; k < NSP; ++k) Yr[k] = YR0[k];
+    } else if (NR == -3 || NR == -4) {
+      const int w = NR == -3 ? 0 : 1;
+#pragma unroll
+      for (int k = 0; k < NSP; ++k) Yr[k] = th.inY[w][k];
+      tr = th.inT[w];
+      float Cb, gb, Rb;
+      gas32<NSP>(th, Yr, tr, Cb, gb, Rb, err);
+      pr = pl;
+      ur = th.inMflow[w] / (pr / (Rb * tr));
+      vr = 0.f;
+      pl = pr; ul = ur; vl = vr; tl = tr;
+#pragma unroll
+      for (int k = 0; k < NSP; ++k) Yl[k] = Yr[k];
+    } else {
+      if (NR == -1) { ul = 0.f; vl = 0.f; }
+      else if (NR == -2 || NR == -6 || NR == -7) {
+        const float vn = ul * sn1 + vl * sn2;
+        ul -= vn * sn1;
+        vl -= vn * sn2;
+      }
+      pr = pl; tr = tl; ur = ul; vr = vl;
+      if (NR == -5) {
+        const float ac = sqrtf(gl0 * pl / rl0);
+        const float vn = ul * sn1 + vl * sn2;
+        if (!(fabsf(vn) > ac)) {
+          pr = th.p_out;
+          ur = ul + sn1 * (pl - pr) / (rl0 * ac);
+          vr = vl + sn2 * (pl - pr) / (rl0 * ac);
+          tr = pr / (Rl0 * (rl0 + (pr - pl) / (ac * ac)));
+          pl = pr; ul = ur; vl = vr; tl = tr;
+        }
+      } else if (NR == -7) {
+        pr = 2.0e6f; tr = 700.f; ur = -100.f; vr = 0.f;
+      }
+#pragma unroll
+      for (int k = 0; k < NSP; ++k) Yr[k] = Yl[k];
+    }
+    const float pp = 0.5f * (pl + pr), uu = 0.5f * (ul + ur), vv = 0.5f * (vl + vr), tem = 0.5f * (tl + tr);
+    float YY[NSP];
+#pragma unroll
+    for (int k = 0; k < NSP; ++k) YY[k] = 0.5f * (Yl[k] + Yr[k]);
+    float Cp, gama, Rc;
+    gas32<NSP>(th, YY, tem, Cp, gama, Rc, err);
+    const float rr = pp / (Rc * tem);
+    float t0[V], t1[V];
+    {
+      const float dxl = (float)d.rinv[NL], dyl = (float)d.rinv[NE + NL];
+#pragma unroll
+      for (int k = 0; k < V; ++k) {
+        t0[k] = d.grad32[(2 * k) * NE + NL] * dxl;
+        t1[k] = d.grad32[(2 * k + 1) * NE + NL] * dyl;
+      }
+    }
+    if (NR >= 0) {
+      const float rdxk = 1.f / (float)d.fdxk[f], y1 = (float)d.fysn[f], y2 = (float)d.fysn[NF + f];
+      const float dxr = (float)d.rinv[NR], dyr = (float)d.rinv[NE + NR];
+#pragma unroll
+      for (int k = 0; k < V; ++k) {
+        const float du = (uR[k] - uL[k]) * rdxk;
+        t0[k] = 0.5f * (t0[k] + d.grad32[(2 * k) * NE + NR] * dxr) + y1 * du;
+        t1[k] = 0.5f * (t1[k] + d.grad32[(2 * k + 1) * NE + NR] * dyr) + y2 * du;
+      }
+    }
+    float dudx = t0[1], dudy = t1[1], dvdx = t0[2], dvdy = t1[2], dtdx = t0[3], dtdy = t1[3];
+    float dYdx[NSP], dYdy[NSP];
+#pragma unroll
+    for (int k = 0; k < NSP - 1; ++k) { dYdx[k] = t0[4 + k]; dYdy[k] = t1[4 + k]; }
+    auto rmv = [](float& vx, float& vy, float nx, float ny) {
+      const float vn = vx * nx + vy * ny;
+      vx -= vn * nx;
+      vy -= vn * ny;
+    };
+    if (NR == -1 || NR == -6) rmv(dtdx, dtdy, sn1, sn2);
+    if (NR == -2) {
+      const float snx = sn1, sny = sn2, stx = -sny, sty = snx;
+      rmv(dtdx, dtdy, snx, sny);
+#pragma unroll
+      for (int k = 0; k < NSP - 1; ++k) rmv(dYdx[k], dYdy[k], snx, sny);
+      float dutdx = dudx * stx + dvdx * sty, dutdy = dudy * stx + dvdy * sty;
+      float dundx = dudx * snx + dvdx * sny, dundy = dudy * snx + dvdy * sny;
+      rmv(dutdx, dutdy, snx, sny);
+      rmv(dundx, dundy, stx, sty);
+      dudx = dutdx * stx + dundx * snx;
+      dudy = dutdy * stx + dundy * snx;
+      dvdx = dutdx * sty + dundx * sny;
+      dvdy = dutdy * sty + dundy * sny;
+    }
+    {
+      float sx = 0.f, sy = 0.f;
+#pragma unroll
+      for (int k = 0; k < NSP - 1; ++k) { sx += dYdx[k]; sy += dYdy[k]; }
+      dYdx[NSP - 1] = -sx;
+      dYdy[NSP - 1] = -sy;
+    }
+    float entha[NSP], Dk[NSP], vmulc, akmu;
+    enthalpy32<NSP>(th, tem, entha, err);
+    transport32<NSP>(th, tem, YY, vmulc, akmu, err);
+    diffusion32<NSP>(th, pp, tem, YY, Dk);
+    float uicx = 0.f, uicy = 0.f;
+#pragma unroll
+    for (int k = 0; k < NSP; ++k) { uicx += Dk[k] * dYdx[k]; uicy += Dk[k] * dYdy[k]; }
+    const float vlac = -2.f / 3.f * vmulc;
+    const float div = dudx + dvdy;
+    const float txx = 2.f * vmulc * dudx + vlac * div;
+    const float tyy = 2.f * vmulc * dvdy + vlac * div;
+    const float txy = vmulc * (dudy + dvdx);
+    float sx = 0.f, sy = 0.f;
+#pragma unroll
+    for (int k = 0; k < NSP; ++k) {
+      sx += (Dk[k] * dYdx[k] - YY[k] * uicx) * entha[k];
+      sy += (Dk[k] * dYdy[k] - YY[k] * uicy) * entha[k];
+    }
+    const float qx = -akmu * dtdx - rr * sx;
+    const float qy = -akmu * dtdy - rr * sy;
+    const float btx = uu * txx + vv * txy - qx;
+    const float bty = uu * txy + vv * tyy - qy;
+    d.Fvis32[0 * NF + f] = -(sav1 * txx + sav2 * txy);
+    d.Fvis32[1 * NF + f] = -(sav1 * txy + sav2 * tyy);
+    d.Fvis32[2 * NF + f] = -(sav1 * btx + sav2 * bty);
+#pragma unroll
+    for (int k = 0; k < NSP - 1; ++k) {
+      const float spx = rr * (Dk[k] * dYdx[k] - YY[k] * uicx);
+      const float spy = rr * (Dk[k] * dYdy[k] - YY[k] * uicy);
+      d.Fvis32[(3 + k) * NF + f] = -(sav1 * spx + sav2 * spy);
+    }
+  }
+  if (err) atomicOr(d.err, err);
+}
+
+// Neumaier-compensated FP32 gather of the face fluxes into the FP64 residual.
+__device__ __forceinline__ void neumaier(float& s, float& c, float x) {
+  const float t = s + x;
+  c += (fabsf(s) >= fabsf(x)) ? ((s - t) + x) : ((x - t) + s);
+  s = t;
+}
+
+template <int NSP>
+__global__ void __launch_bounds__(128) k_gather32(const Dev d, int visc, int comb) {
+  constexpr int V = 3 + NSP;
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= d.NE) return;
+  const int NE = d.NE, NF = d.NF, nf = d.nface[i];
+  const unsigned lb = d.cleft[i];
+  float s[V], c[V];
+#pragma unroll
+  for (int k = 0; k < V; ++k) { s[k] = 0.f; c[k] = 0.f; }
+  for (int q = 0; q < nf; ++q) {
+    const int f = d.cface[q * NE + i];
+    const float sg = ((lb >> q) & 1u) ? -1.f : 1.f;
+#pragma unroll
+    for (int k = 0; k < V; ++k) neumaier(s[k], c[k], sg * d.Finv32[k * NF + f]);
+    if (visc) {
+#pragma unroll
+      for (int k = 1; k < V; ++k) neumaier(s[k], c[k], sg * d.Fvis32[(k - 1) * NF + f]);
+    }
+  }
+#pragma unroll
+  for (int k = 0; k < V; ++k) {
+    double R = (double)s[k] + (double)c[k];
+    if (comb && k >= 4) R += d.src[(k - 4) * NE + i];
+    d.hWA[k * NE + i] = R;
+  }
+}
+
+// ---------------------------------------------------------------- LU-SGS ---
+// Four lanes per cell as in the FP64 sweep; the off-diagonal terms in FP32,
+// the diagonal division in FP64.
+template <int NSP, bool FWD>
+__device__ __forceinline__ void sweep_step32(const Dev& d, const ThermoDev32<NSP>& th, const int* __restrict__ cells,
+                                             int n, int t, int q) {
+  constexpr int V = 3 + NSP;
+  const bool valid = t < n;
+  const int i = valid ? cells[t] : 0;
+  const int NE = d.NE, NF = d.NF;
+  float c[V];
+#pragma unroll
+  for (int k = 0; k < V; ++k) c[k] = 0.f;
+  if (valid && q < d.nface[i]) {
+    const int j = d.cother[q * NE + i];
+    if (j >= 0 && (FWD ? j < i : j > i)) {
+      const int f = d.cface[q * NE + i];
+      float dx = (float)d.fvec[f], dy = (float)d.fvec[NF + f];
+      if (!((d.cleft[i] >> q) & 1u)) { dx = -dx; dy = -dy; }
+      const float pp = (float)d.PA[0 * NE + j], uu = (float)d.PA[1 * NE + j], vv = (float)d.PA[2 * NE + j],
+                  tt = (float)d.PA[3 * NE + j];
+      const float rr = (float)d.cst[0 * NE + j], gama = (float)d.cst[1 * NE + j], roe = (float)d.cst[2 * NE + j];
+      const float rou = rr * uu, rov = rr * vv;
+      const float drr = (float)d.hWA[0 * NE + j], dru = (float)d.hWA[1 * NE + j], drv = (float)d.hWA[2 * NE + j],
+                  dre = (float)d.hWA[3 * NE + j];
+      float dry[NSP], s = 0.f;
+#pragma unroll
+      for (int k = 0; k < NSP - 1; ++k) { dry[k] = (float)d.hWA[(4 + k) * NE + j]; s += dry[k]; }
+      dry[NSP - 1] = drr - s;
+      const float rinv = 1.f / rr;
+      const float duu = (dru - uu * drr) * rinv;
+      const float dvv = (drv - vv * drr) * rinv;
+      float s1 = 0.f, s2 = 0.f;
+#pragma unroll
+      for (int k = 0; k < NSP; ++k) {
+        s1 += (float)d.cst[(3 + k) * NE + j] * dry[k];
+        s2 += th.R[k] * dry[k];
+      }
+      const float gm1 = gama - 1.f;
+      const float dpp = gm1 * (dre - s1 + tt * s2 * gama / gm1 - 0.5f * (dru * uu + duu * rou + drv * vv + dvv * rov));
+      const float un = uu * dx + vv * dy, dun = duu * dx + dvv * dy;
+      const float aF = (float)d.alpaF[f];
+      c[0] = 0.5f * (-aF * drr + dru * dx + drv * dy);
+      c[1] = 0.5f * (-aF * dru + dru * un + rou * dun + dpp * dx);
+      c[2] = 0.5f * (-aF * drv + drv * un + rov * dun + dpp * dy);
+      c[3] = 0.5f * (-aF * dre + dun * (roe + pp) + un * (dre + dpp));
+#pragma unroll
+      for (int k = 0; k < NSP - 1; ++k)
+        c[4 + k] = 0.5f * (-aF * dry[k] + dry[k] * un + rr * (float)d.PA[(4 + k) * NE + j] * dun);
+    }
+  }
+  const int base = (threadIdx.x & 31) & ~3;
+  float df[V];
+#pragma unroll
+  for (int k = 0; k < V; ++k) df[k] = 0.f;
+#pragma unroll
+  for (int sl = 0; sl < 4; ++sl)
+#pragma unroll
+    for (int k = 0; k < V; ++k) df[k] += __shfl_sync(0xffffffffu, c[k], base + sl);
+  if (!valid) return;
+  const double ddi = d.dd[i];
+#pragma unroll
+  for (int k = 0; k < V; ++k)
+    if ((k & 3) == q) {
+      const double R = d.hWA[k * NE + i];
+      d.hWA[k * NE + i] = FWD ? (R - (double)df[k]) / ddi : R - (double)df[k] / ddi;
+    }
+}
+
+template <int NSP, bool FWD>
+__global__ void __launch_bounds__(32) k_sweep32(const Dev d, const ThermoDev32<NSP> th, const int* __restrict__ cells,
+                                                int n) {
+  const int gt = blockIdx.x * blockDim.x + threadIdx.x;
+  sweep_step32<NSP, FWD>(d, th, cells, n, gt >> 2, gt & 3);
+}
+
+// Both sweeps and the FP64 update in one cooperative launch (as the FP64
+// persistent kernel of rc_core.cu).
+constexpr int PERS32_THREADS = 256;
+template <int NSP>
+__global__ void __launch_bounds__(PERS32_THREADS) k_lusgs_persistent32(const Dev d, const ThermoDev32<NSP> th,
+                                                                       const ThermoDev<NSP> th64,
+                                                                       const int* __restrict__ fcells,
+                                                                       const int* __restrict__ foff, int nf,
+                                                                       const int* __restrict__ bcells,
+                                                                       const int* __restrict__ boff, int nb,
+                                                                       unsigned* count) {
+  const int G = gridDim.x, wpb = PERS32_THREADS / 32, w = threadIdx.x >> 5;
+  const int lt = (threadIdx.x & 31) >> 2, q = threadIdx.x & 3;
+  unsigned seq = 0;
+  for (int l = 0; l < nf; ++l) {
+    const int lo = foff[l], n = foff[l + 1] - lo, nch = (n + 7) >> 3;
+    for (int c = blockIdx.x + w * G; c < nch; c += G * wpb)
+      sweep_step32<NSP, true>(d, th, fcells + lo, n, c * 8 + lt, q);
+    if (!grid_sync(count, seq++, d.err)) return;
+  }
+  for (int l = 0; l < nb; ++l) {
+    const int lo = boff[l], n = boff[l + 1] - lo, nch = (n + 7) >> 3;
+    for (int c = blockIdx.x + w * G; c < nch; c += G * wpb)
+      sweep_step32<NSP, false>(d, th, bcells + lo, n, c * 8 + lt, q);
+    if (!grid_sync(count, seq++, d.err)) return;
+  }
+  unsigned err = 0;
+  for (int i = blockIdx.x * PERS32_THREADS + threadIdx.x; i < d.NE; i += G * PERS32_THREADS)
+    update_cell<NSP>(d, th64, i, err);
+  if (err) atomicOr(d.err, err);
+}
+
+// ------------------------------------------------------- host launchers ----
+inline unsigned nblk(long n, int t) { return (unsigned)((n + t - 1) / t); }
+
+template <int NSP>
+void mixed_ts_face(const Dev& d, const void* th32, int visc, cudaStream_t s) {
+  const auto& th = *static_cast<const ThermoDev32<NSP>*>(th32);
+  if (visc) k_ts_face32<NSP, true><<<nblk(d.NF, 128), 128, 0, s>>>(d, th);
+  else k_ts_face32<NSP, false><<<nblk(d.NF, 128), 128, 0, s>>>(d, th);
+}
+template <int NSP>
+void mixed_cell(const Dev& d, const void* th32, const ThermoDev<NSP>& th64, int do_step, int limit, int comb,
+                int visc, cudaStream_t s) {
+  k_cell32<NSP><<<nblk(d.NE, 128), 128, 0, s>>>(d, *static_cast<const ThermoDev32<NSP>*>(th32), th64, do_step,
+                                                 limit, comb, visc);
+}
+template <int NSP>
+void mixed_face_flux(const Dev& d, const void* th32, int visc, cudaStream_t s) {
+  const auto& th = *static_cast<const ThermoDev32<NSP>*>(th32);
+  if (visc) k_face_flux32<NSP, true><<<nblk(d.NF, 128), 128, 0, s>>>(d, th);
+  else k_face_flux32<NSP, false><<<nblk(d.NF, 128), 128, 0, s>>>(d, th);
+}
+template <int NSP>
+void mixed_gather(const Dev& d, int visc, int comb, cudaStream_t s) {
+  k_gather32<NSP><<<nblk(d.NE, 128), 128, 0, s>>>(d, visc, comb);
+}
+template <int NSP>
+void mixed_sweep(const Dev& d, const void* th32, bool fwd, const int* cells, int n, cudaStream_t s) {
+  const auto& th = *static_cast<const ThermoDev32<NSP>*>(th32);
+  if (fwd) k_sweep32<NSP, true><<<nblk(4L * n, 32), 32, 0, s>>>(d, th, cells, n);
+  else k_sweep32<NSP, false><<<nblk(4L * n, 32), 32, 0, s>>>(d, th, cells, n);
+}
+// Cooperative launch of the persistent sweeps (count zeroed first, in stream order).
+template <int NSP>
+cudaError_t mixed_lusgs_persistent(const Dev& d, const void* th32, const ThermoDev<NSP>& th64, const int* fc,
+                                   const int* fo, int nf, const int* bc, const int* bo, int nb, unsigned* count,
+                                   int grid, cudaStream_t s) {
+  cudaError_t e = cudaMemsetAsync(count, 0, sizeof(unsigned), s);
+  if (e != cudaSuccess) return e;
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = dim3((unsigned)grid);
+  cfg.blockDim = dim3(PERS32_THREADS);
+  cfg.stream = s;
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeCooperative;
+  attr[0].val.cooperative = 1;
+  cfg.attrs = attr;
+  cfg.numAttrs = 1;
+  return cudaLaunchKernelEx(&cfg, k_lusgs_persistent32<NSP>, d, *static_cast<const ThermoDev32<NSP>*>(th32), th64, fc,
+                            fo, nf, bc, bo, nb, count);
+}
+template <int NSP>
+int mixed_persistent_occupancy() {
+  int nb = 0;
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_lusgs_persistent32<NSP>, PERS32_THREADS, 0);
+  return nb;
+}
+template <int NSP>
+size_t mixed_thermo(const void* th64, void* out) {
+  if (out) make_thermo32<NSP>(*static_cast<const ThermoDev<NSP>*>(th64), *static_cast<ThermoDev32<NSP>*>(out));
+  return sizeof(ThermoDev32<NSP>);
+}
+
+#define RC_MIXED_INST(N)                                                                                        \
+  template void mixed_ts_face<N>(const Dev&, const void*, int, cudaStream_t);                                   \
+  template void mixed_cell<N>(const Dev&, const void*, const ThermoDev<N>&, int, int, int, int, cudaStream_t);  \
+  template void mixed_face_flux<N>(const Dev&, const void*, int, cudaStream_t);                                 \
+  template void mixed_gather<N>(const Dev&, int, int, cudaStream_t);                                            \
+  template void mixed_sweep<N>(const Dev&, const void*, bool, const int*, int, cudaStream_t);                   \
+  template size_t mixed_thermo<N>(const void*, void*);                                                       \
+  template cudaError_t mixed_lusgs_persistent<N>(const Dev&, const void*, const ThermoDev<N>&, const int*,       \
+                                                 const int*, int, const int*, const int*, int, unsigned*, int,  \
+                                                 cudaStream_t);                                                 \
+  template int mixed_persistent_occupancy<N>();
+RC_MIXED_INST(1)
+RC_MIXED_INST(4)
+
+}  // namespace rc

@@ -2,18 +2,20 @@
 //
 // Each function keeps the operation order of the reference routine it cites,
 // so that with FMA contraction disabled (--fmad=false) +,-,*,/ and sqrt give
-// the reference's IEEE results; only exp/log/pow may differ from the host libm
-// by an ulp.  Constants that depend on species data only (pair terms of the
+// the reference's IEEE results; exp/log/pow come from include/rc_math.h, the
+// same code the CPU oracle runs, so the results are bit-identical.  Constants that depend on species data only (pair terms of the
 // Wilke and Chapman-Enskog sums) are evaluated once on the host with the
 // reference's expressions and passed in ThermoDev.
 #pragma once
 #include <cstdint>
 
+#include "rc_math.h"
+
 namespace rc {
 
 enum : unsigned {
   ERR_THERMO_T = 1u, ERR_TRANSPORT_T = 2u, ERR_NEG_TIMESTEP = 4u, ERR_NEG_FACE = 8u,
-  ERR_NAN = 16u, ERR_BCTYPE = 32u
+  ERR_NAN = 16u, ERR_BCTYPE = 32u, ERR_SYNC = 64u
 };
 
 template <int NSP>
@@ -74,7 +76,7 @@ __device__ __forceinline__ void gas(const ThermoDev<NSP>& th, const double* Y, d
 template <int NSP>
 __device__ __forceinline__ void enthalpy(const ThermoDev<NSP>& th, double tem, double* entha, unsigned& err) {
   const double t2 = tem * tem;
-  const double e[7] = {-(1.0 / t2), log(tem) / tem, 1.0, tem / 2.0, t2 / 3.0, (tem * t2) / 4.0, (t2 * t2) / 5.0};
+  const double e[7] = {-(1.0 / t2), rcm::log(tem) / tem, 1.0, tem / 2.0, t2 / 3.0, (tem * t2) / 4.0, (t2 * t2) / 5.0};
   const bool low = (th.tlo <= tem && tem <= th.tcrit);
   if (!low && !(th.tcrit < tem && tem <= th.thi)) err |= ERR_THERMO_T;
 #pragma unroll
@@ -124,12 +126,12 @@ __device__ __forceinline__ void transport(const ThermoDev<NSP>& th, double tem2,
   const bool low = (th.trlo <= tem && tem <= th.trcrit);
   if (!low && !(th.trcrit < tem && tem <= th.trhi)) err |= ERR_TRANSPORT_T;
   const int rg = low ? 0 : 1;
-  const double lt = log(tem);
+  const double lt = rcm::log(tem);
   const double t2 = tem * tem;
 #pragma unroll
   for (int i = 0; i < NSP; ++i) {
-    mul[i] = exp(th.mu[rg][0][i] * lt + th.mu[rg][1][i] / tem + th.mu[rg][2][i] / t2 + th.mu[rg][3][i]);
-    Kl[i] = exp(th.kk[rg][0][i] * lt + th.kk[rg][1][i] / tem + th.kk[rg][2][i] / t2 + th.kk[rg][3][i]);
+    mul[i] = rcm::exp(th.mu[rg][0][i] * lt + th.mu[rg][1][i] / tem + th.mu[rg][2][i] / t2 + th.mu[rg][3][i]);
+    Kl[i] = rcm::exp(th.kk[rg][0][i] * lt + th.kk[rg][1][i] / tem + th.kk[rg][2][i] / t2 + th.kk[rg][3][i]);
   }
 #pragma unroll
   for (int i = 0; i < NSP; ++i) { mul[i] = mul[i] * 1.0e-7; Kl[i] = Kl[i] * 1.0e-4; }
@@ -176,8 +178,8 @@ __device__ __forceinline__ void diffusion(const ThermoDev<NSP>& th, double pp, d
 #pragma unroll
     for (int j = i + 1; j < NSP; ++j) {
       const double tstar = tem / th.dlj[i][j];
-      const double om = 1.06036 * pow(tstar, -0.15610) + 0.19300 * exp(-0.47635 * tstar) +
-                        1.03587 * exp(-1.52996 * tstar) + 1.76474 * exp(-3.89411 * tstar);
+      const double om = 1.06036 * rcm::pow(tstar, -0.15610) + 0.19300 * rcm::exp(-0.47635 * tstar) +
+                        1.03587 * rcm::exp(-1.52996 * tstar) + 1.76474 * rcm::exp(-3.89411 * tstar);
       const double d = num / (pp * th.dmw[i][j] * th.dcd[i][j] * om);
       D[i][j] = d;
       D[j][i] = d;
@@ -200,9 +202,9 @@ __device__ __forceinline__ void production(const ThermoDev<NSP>& th, double T, d
   const double y0 = fmin2(1.0, fmax2(0.0, Y2[0]));
   if (th.model == 0) {
     const double y1 = fmin2(1.0, fmax2(0.0, Y2[NSP > 1 ? 1 : 0]));
-    kf = th.Af * exp(-th.E / (th.Rconstant * T));
-    kf = kf * pow(y0 * rho / th.mw1000[0], 0.2);
-    kf = kf * pow(y1 * rho / th.mw1000[1], 1.3);
+    kf = th.Af * rcm::exp(-th.E / (th.Rconstant * T));
+    kf = kf * rcm::pow(y0 * rho / th.mw1000[0], 0.2);
+    kf = kf * rcm::pow(y1 * rho / th.mw1000[1], 1.3);
   } else {
     kf = (T > 710.0) ? 1e4 : 0.0;
     kf = kf * (y0 * rho / th.mw1000[0]);
