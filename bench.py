@@ -28,7 +28,6 @@ import shutil
 import subprocess
 import sys
 import tempfile
-import threading
 import time
 
 ROOT = os.path.dirname(os.path.abspath(__file__))
@@ -186,7 +185,8 @@ def main():
     ap.add_argument("--order", default=None)
     ap.add_argument("--nx", type=int, default=None, help="override the preset's cells along the axis")
     ap.add_argument("--ny", type=int, default=None, help="override the preset's cells across")
-    ap.add_argument("--precision", default="fp64", choices=["fp64", "mixed"])
+    ap.add_argument("--precision", default="both", choices=["fp64", "mixed", "both"],
+                    help="both: FP64 headline plus the mixed form with its error against FP64")
     ap.add_argument("--e2e-steps", type=int, default=10)
     ap.add_argument("--cpu-budget", type=float, default=15.0)
     ap.add_argument("--no-cpu", action="store_true")
@@ -213,70 +213,31 @@ def main():
     torch.cuda.set_device(local)
     stream = torch.cuda.Stream(device=local)
     flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=f"cuda:{local}")
-    prec = rc.RC_PREC_MIXED if args.precision == "mixed" else rc.RC_PREC_FP64
+    forms_req = ["fp64", "mixed"] if args.precision == "both" else [args.precision]
     with tempfile.TemporaryDirectory() as tmp:
         d, cfg = make_workload(args.case, tmp, **case_overrides(args))
         case = rc.Case(d)
-        s = rc.Solver(case, precision=prec, device=local, stream=stream.cuda_stream)
         NE, NF, V = case.NE, case.NF, case.NVar
-        with torch.cuda.stream(stream):
-            for it in range(args.warmup):
-                s.lu_sgs_stage(it + 1)
-            s.sync()
-            ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
-                  for _ in range(args.steps)]
-            if dist:
-                dist.barrier()
-            torch.cuda.synchronize()
-            l0 = s.stats()["kernel_launches"]
-            with ClockSampler(local) as clk:
-                for it in range(args.steps):
-                    flush.zero_()
-                    ev[it][0].record(stream)
-                    s.lu_sgs_stage(args.warmup + it + 1)
-                    ev[it][1].record(stream)
-                s.sync()
-                torch.cuda.synchronize()
-            launches = s.stats()["kernel_launches"] - l0
-            ms = [a.elapsed_time(b) for a, b in ev]
-            t_local = sum(ms) / 1e3
-            res, romax = s.residual()
-            # per-subroutine timing (same stream, events), L2 flushed before each
-            sub = {}
-            for name, fn in (("timestep", s.timestep), ("reconstruction", s.reconstruction),
-                             ("flux_sourceterm", s.flux_sourceterm), ("lu_sgs_steady", s.lu_sgs_steady)):
-                sub[name] = []
-            nrep = max(3, min(args.steps, 20))
-            for _ in range(nrep):
-                for name, fn in (("timestep", s.timestep), ("reconstruction", s.reconstruction),
-                                 ("flux_sourceterm", s.flux_sourceterm), ("lu_sgs_steady", s.lu_sgs_steady)):
-                    flush.zero_()
-                    a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-                    a.record(stream)
-                    fn()
-                    b.record(stream)
-                    sub[name].append((a, b))
-            s.sync()
-            torch.cuda.synchronize()
-            sub_ms = {k: float(np.mean([a.elapsed_time(b) for a, b in v])) for k, v in sub.items()}
-        # end-to-end through the C ABI with pinned host buffers
-        PA_h = torch.empty((NE, V), dtype=torch.float64, pin_memory=True).numpy()
-        WA_h = torch.empty((NE, V), dtype=torch.float64, pin_memory=True).numpy()
-        PA_h[:], WA_h[:] = s.get_state()
-        s.sync()
-        t0 = time.perf_counter()
-        for it in range(args.e2e_steps):
-            s.set_state(PA_h, WA_h)
-            s.lu_sgs_stage(it + 1)
-            s.residual()
-            s.get_state(PA_h, WA_h)
-        e2e_dt = time.perf_counter() - t0
-        stats = s.stats()
-        s.close()
-
-        t_max = t_local
+        results = {}
+        states = {}
+        clk = None
+        for form in forms_req:
+            prec = rc.RC_PREC_MIXED if form == "mixed" else rc.RC_PREC_FP64
+            s = rc.Solver(case, precision=prec, device=local, stream=stream.cuda_stream)
+            r, clk_f = time_form(s, args, stream, flush, dist, torch, rc)
+            if clk is None:
+                clk = clk_f
+            states[form] = s.get_state()
+            if form == forms_req[0]:
+                r.update(subroutine_times(s, args, stream, flush, torch))
+            r["e2e"] = e2e_through_abi(s, args, NE, V, torch)
+            r["levels"] = {k: v for k, v in s.stats().items() if k != "kernel_launches"}
+            s.close()
+            results[form] = r
+        head = results[forms_req[0]]
+        t_max = head["t_local"]
         if dist:
-            tt = torch.tensor([t_local], dtype=torch.float64)
+            tt = torch.tensor([t_max], dtype=torch.float64)
             dist.all_reduce(tt, op=dist.ReduceOp.MAX)
             t_max = float(tt[0])
         if rank != 0:
@@ -286,26 +247,42 @@ def main():
         value = world * NE * args.steps / t_max
         peak, peak_kind = read_peaks()
         ab = algo_bytes_per_cell(V, NF / NE, cfg.viscous, cfg.combustion)
+        sub_ms = head["subroutine_ms"]
         dom = max(sub_ms, key=sub_ms.get)
         achieved = ab[dom] * NE / (sub_ms[dom] * 1e-3) / 1e9
         line = {
             "metric": "cell-iters/s", "value": value, "unit": "cell-iters/s", "n_gpus": world,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * t_max / args.steps,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
-            "dtype": "f64" if prec == rc.RC_PREC_FP64 else "f32+f64", "data": "synthetic",
+            "dtype": "f64" if forms_req[0] == "fp64" else "f32+f64", "data": "synthetic",
             "config": workload_config(cfg, NE, NF, f"replicas x{world}" if world > 1 else "single GPU"),
-            "e2e": {"value": NE * args.e2e_steps / e2e_dt, "unit": "cell-iters/s",
-                    "h2d_bytes_per_step": 2 * NE * V * 8, "d2h_bytes_per_step": 2 * NE * V * 8 + (V + 1) * 8},
-            "gpu_launches": int(launches),
+            "e2e": head["e2e"],
+            "gpu_launches": head["launches"],
             "roofline": {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": peak, "unit": "GB/s",
                          "frac": achieved / peak, "peak_source": peak_kind,
-                         "algorithmic_bytes_per_cell": ab[dom], "traffic": None},
+                         "algorithmic_bytes_per_cell": ab[dom], "traffic": None,
+                         "note": "FP64 kernels are FP64-issue bound on GB300 (FP64 pipe 81-88% busy, DRAM < 2%)"},
             "subroutine_ms": sub_ms,
-            "stage_algorithmic_gbs": ab["stage"] * NE / (1e-3 * 1e3 * t_max / args.steps) / 1e9,
-            "levels": {"fwd": stats["fwd_levels"], "bwd": stats["bwd_levels"]},
-            "residual": [float(x) for x in res], "romax": romax,
+            "stage_algorithmic_gbs": ab["stage"] * NE / (t_max / args.steps) / 1e9,
+            "levels": head["levels"],
         }
-        line["clocks"] = clk.summary()
+        if len(forms_req) > 1:
+            ref = states["fp64"][0]
+            forms = {}
+            for form in forms_req:
+                r = results[form]
+                f = {"value": NE * args.steps / r["t_local"], "ms_per_step": 1e3 * r["t_local"] / args.steps,
+                     "e2e": r["e2e"]["value"], "gpu_launches": r["launches"]}
+                if form != "fp64":
+                    st = states[form][0]
+                    den = np.maximum(np.abs(ref).max(axis=0), 1e-300)
+                    e = np.abs(st - ref).max(axis=0) / den
+                    f["rel_linf_vs_fp64"] = {"p": float(e[0]), "T": float(e[3]),
+                                             "Y": [float(x) for x in e[4:]],
+                                             "after_iterations": args.warmup + args.steps}
+                forms[form] = f
+            line["forms"] = forms
+        line["clocks"] = clk
         if not args.no_cpu:
             line["cpu_baseline"] = cpu_baseline(d, args.cpu_budget)
         print(json.dumps(line), flush=True)
@@ -313,6 +290,76 @@ def main():
         dist.barrier()
         dist.destroy_process_group()
     return 0
+
+
+def gpu_id(torch):
+    """nvidia-smi --id for the current device (its UUID when torch exposes it)."""
+    dev = torch.cuda.current_device()
+    try:
+        u = str(torch.cuda.get_device_properties(dev).uuid)
+        return u if u.startswith("GPU-") else "GPU-" + u
+    except Exception:
+        return str(dev)
+
+
+def time_form(s, args, stream, flush, dist, torch, rc):
+    """W warm-up iterations, then K device-timed iterations (L2 flushed between)."""
+    with torch.cuda.stream(stream):
+        for it in range(args.warmup):
+            s.lu_sgs_stage(it + 1)
+        s.sync()
+        ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
+        if dist:
+            dist.barrier()
+        torch.cuda.synchronize()
+        l0 = s.stats()["kernel_launches"]
+        with ClockSampler(gpu_id(torch)) as clk:
+            for it in range(args.steps):
+                flush.zero_()
+                ev[it][0].record(stream)
+                s.lu_sgs_stage(args.warmup + it + 1)
+                ev[it][1].record(stream)
+            s.sync()
+            torch.cuda.synchronize()
+        launches = s.stats()["kernel_launches"] - l0
+        ms = [a.elapsed_time(b) for a, b in ev]
+    return {"t_local": sum(ms) / 1e3, "launches": int(launches)}, clk.summary()
+
+
+def subroutine_times(s, args, stream, flush, torch):
+    """Each reference subroutine timed with CUDA events on the solver stream."""
+    subs = (("timestep", s.timestep), ("reconstruction", s.reconstruction),
+            ("flux_sourceterm", s.flux_sourceterm), ("lu_sgs_steady", s.lu_sgs_steady))
+    rec = {k: [] for k, _ in subs}
+    with torch.cuda.stream(stream):
+        for _ in range(max(3, min(args.steps, 20))):
+            for name, fn in subs:
+                flush.zero_()
+                a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+                a.record(stream)
+                fn()
+                b.record(stream)
+                rec[name].append((a, b))
+        s.sync()
+        torch.cuda.synchronize()
+    return {"subroutine_ms": {k: float(np.mean([a.elapsed_time(b) for a, b in v])) for k, v in rec.items()}}
+
+
+def e2e_through_abi(s, args, NE, V, torch):
+    """Per step: PA, WA host->device from pinned memory, the stage, the residual
+    norms and PA, WA device->host into pinned memory (wall clock)."""
+    PA_h = torch.empty((NE, V), dtype=torch.float64, pin_memory=True).numpy()
+    WA_h = torch.empty((NE, V), dtype=torch.float64, pin_memory=True).numpy()
+    s.get_state(PA_h, WA_h)
+    t0 = time.perf_counter()
+    for it in range(args.e2e_steps):
+        s.set_state(PA_h, WA_h)
+        s.lu_sgs_stage(it + 1)
+        s.residual()
+        s.get_state(PA_h, WA_h)
+    dt = time.perf_counter() - t0
+    return {"value": NE * args.e2e_steps / dt, "unit": "cell-iters/s",
+            "h2d_bytes_per_step": 2 * NE * V * 8, "d2h_bytes_per_step": 2 * NE * V * 8 + (V + 1) * 8}
 
 
 if __name__ == "__main__":

@@ -592,86 +592,86 @@ __global__ void __launch_bounds__(128) k_sweep(const Dev d, const ThermoDev<NSP>
 // order (the NeighF order of the reference) by every lane of the quad, and the
 // lanes share the final divisions.  The residual R is already in hWA (the
 // forward gather runs as a separate, fully parallel kernel).
-// sweep_step: cell t of a level list (t >= n: lanes that only join the
-// shuffles); q is the lane's face slot.  Called by whole warps.
+// One cell of a sweep at level position t (t >= tend: lanes that only join
+// the shuffles), lane q = face slot.  All indices come from the sweep tables in
+// one load; the cell's own residual and diagonal are fetched up front.
+// Called by whole warps.
 template <int NSP, bool FWD>
-__device__ __forceinline__ void sweep_step(const Dev& d, const ThermoDev<NSP>& th, const int* __restrict__ cells,
-                                           int n, int t, int q) {
+__device__ __forceinline__ void sweep_step(const Dev& d, const ThermoDev<NSP>& th, int t, int tend, int q) {
   constexpr int V = 3 + NSP;
-  const bool valid = t < n;
-  const int i = valid ? cells[t] : 0;
+  constexpr int DIR = FWD ? 0 : 1;
+  const bool valid = t < tend;
   const int NE = d.NE, NF = d.NF;
+  const int i = valid ? d.swi[DIR][t] : 0;
+  const int j = valid ? d.swj[DIR][q * NE + t] : -1;
+  const int fs = valid ? d.swf[DIR][q * NE + t] : 0;
+  double R0 = 0.0, R1 = 0.0, ddi = 1.0;
+  if (valid) {  // own residual (variables q and q+4) and diagonal
+    R0 = d.hWA[q * NE + i];
+    if (q + 4 < V) R1 = d.hWA[(q + 4) * NE + i];
+    ddi = d.dd[i];
+  }
   double c[V];
 #pragma unroll
   for (int k = 0; k < V; ++k) c[k] = 0.0;
-  bool act = false;
-  if (valid && q < d.nface[i]) {
-    const int j = d.cother[q * NE + i];
-    act = j >= 0 && (FWD ? j < i : j > i);
-    if (act) {
-      const int f = d.cface[q * NE + i];
-      double dx = d.fvec[f], dy = d.fvec[NF + f];
-      if (!((d.cleft[i] >> q) & 1u)) { dx = -dx; dy = -dy; }
-      const double pp = d.PA[0 * NE + j], uu = d.PA[1 * NE + j], vv = d.PA[2 * NE + j], tt = d.PA[3 * NE + j];
-      const double rr = d.cst[0 * NE + j], gama = d.cst[1 * NE + j], roe = d.cst[2 * NE + j];
-      const double rou = rr * uu, rov = rr * vv;
-      const double drr = d.hWA[0 * NE + j], dru = d.hWA[1 * NE + j], drv = d.hWA[2 * NE + j],
-                   dre = d.hWA[3 * NE + j];
-      double dry[NSP], s = 0.0;
+  const bool act = j >= 0;
+  if (act) {
+    const int f = fs >= 0 ? fs : ~fs;
+    double dx = d.fvec[f], dy = d.fvec[NF + f];
+    if (fs < 0) { dx = -dx; dy = -dy; }
+    const double pp = d.PA[0 * NE + j], uu = d.PA[1 * NE + j], vv = d.PA[2 * NE + j], tt = d.PA[3 * NE + j];
+    const double rr = d.cst[0 * NE + j], gama = d.cst[1 * NE + j], roe = d.cst[2 * NE + j];
+    const double rou = rr * uu, rov = rr * vv;
+    const double drr = d.hWA[0 * NE + j], dru = d.hWA[1 * NE + j], drv = d.hWA[2 * NE + j],
+                 dre = d.hWA[3 * NE + j];
+    double dry[NSP], s = 0.0;
 #pragma unroll
-      for (int k = 0; k < NSP - 1; ++k) { dry[k] = d.hWA[(4 + k) * NE + j]; s = s + dry[k]; }
-      dry[NSP - 1] = drr - s;
-      const double duu = (dru - uu * drr) / rr;
-      const double dvv = (drv - vv * drr) / rr;
-      double s1 = 0.0, s2 = 0.0;
+    for (int k = 0; k < NSP - 1; ++k) { dry[k] = d.hWA[(4 + k) * NE + j]; s = s + dry[k]; }
+    dry[NSP - 1] = drr - s;
+    const double duu = (dru - uu * drr) / rr;
+    const double dvv = (drv - vv * drr) / rr;
+    double s1 = 0.0, s2 = 0.0;
 #pragma unroll
-      for (int k = 0; k < NSP; ++k) s1 = s1 + d.cst[(3 + k) * NE + j] * dry[k];
+    for (int k = 0; k < NSP; ++k) s1 = s1 + d.cst[(3 + k) * NE + j] * dry[k];
 #pragma unroll
-      for (int k = 0; k < NSP; ++k) s2 = s2 + th.R[k] * dry[k];
-      const double dpp = (gama - 1) *
-                         (dre - s1 + tt * s2 * gama / (gama - 1) - 0.5 * (dru * uu + duu * rou + drv * vv + dvv * rov));
-      const double unormal = uu * dx + vv * dy;
-      const double dunormal = duu * dx + dvv * dy;
-      const double aF = d.alpaF[f];
-      c[0] = 0.5 * (-aF * drr + dru * dx + drv * dy);
-      c[1] = 0.5 * (-aF * dru + dru * unormal + rou * dunormal + dpp * dx);
-      c[2] = 0.5 * (-aF * drv + drv * unormal + rov * dunormal + dpp * dy);
-      c[3] = 0.5 * (-aF * dre + dunormal * (roe + pp) + unormal * (dre + dpp));
+    for (int k = 0; k < NSP; ++k) s2 = s2 + th.R[k] * dry[k];
+    const double dpp =
+        (gama - 1) * (dre - s1 + tt * s2 * gama / (gama - 1) - 0.5 * (dru * uu + duu * rou + drv * vv + dvv * rov));
+    const double unormal = uu * dx + vv * dy;
+    const double dunormal = duu * dx + dvv * dy;
+    const double aF = d.alpaF[f];
+    c[0] = 0.5 * (-aF * drr + dru * dx + drv * dy);
+    c[1] = 0.5 * (-aF * dru + dru * unormal + rou * dunormal + dpp * dx);
+    c[2] = 0.5 * (-aF * drv + drv * unormal + rov * dunormal + dpp * dy);
+    c[3] = 0.5 * (-aF * dre + dunormal * (roe + pp) + unormal * (dre + dpp));
 #pragma unroll
-      for (int k = 0; k < NSP - 1; ++k) {
-        const double ry = rr * d.PA[(4 + k) * NE + j];
-        c[4 + k] = 0.5 * (-aF * dry[k] + dry[k] * unormal + ry * dunormal);
-      }
+    for (int k = 0; k < NSP - 1; ++k) {
+      const double ry = rr * d.PA[(4 + k) * NE + j];
+      c[4 + k] = 0.5 * (-aF * dry[k] + dry[k] * unormal + ry * dunormal);
     }
   }
+  // terms in slot order (NeighF order); lane q keeps the sums of its variables q, q+4
   const int base = (threadIdx.x & 31) & ~3;
-  double df[V];
+  double df0 = 0.0, df1 = 0.0;
 #pragma unroll
-  for (int k = 0; k < V; ++k) df[k] = 0.0;
-#pragma unroll
-  for (int s = 0; s < 4; ++s) {
-    const bool a = __shfl_sync(0xffffffffu, act, base + s);
+  for (int sl = 0; sl < 4; ++sl) {
+    const bool a = __shfl_sync(0xffffffffu, act, base + sl);
 #pragma unroll
     for (int k = 0; k < V; ++k) {
-      const double cs = __shfl_sync(0xffffffffu, c[k], base + s);
-      if (a) df[k] = df[k] + cs;
+      const double cs = __shfl_sync(0xffffffffu, c[k], base + sl);
+      if (a && k == q) df0 = df0 + cs;
+      if (a && k == q + 4) df1 = df1 + cs;
     }
   }
   if (!valid) return;
-  const double ddi = d.dd[i];
-#pragma unroll
-  for (int k = 0; k < V; ++k)
-    if ((k & 3) == q) {
-      const double R = d.hWA[k * NE + i];
-      d.hWA[k * NE + i] = FWD ? (R - df[k]) / ddi : R - df[k] / ddi;
-    }
+  d.hWA[q * NE + i] = FWD ? (R0 - df0) / ddi : R0 - df0 / ddi;
+  if (q + 4 < V) d.hWA[(q + 4) * NE + i] = FWD ? (R1 - df1) / ddi : R1 - df1 / ddi;
 }
 
 template <int NSP, bool FWD>
-__global__ void __launch_bounds__(32) k_sweep4(const Dev d, const ThermoDev<NSP> th, const int* __restrict__ cells,
-                                               int n) {
+__global__ void __launch_bounds__(32) k_sweep4(const Dev d, const ThermoDev<NSP> th, int t0, int t1) {
   const int gt = blockIdx.x * blockDim.x + threadIdx.x;
-  sweep_step<NSP, FWD>(d, th, cells, n, gt >> 2, gt & 3);
+  sweep_step<NSP, FWD>(d, th, t0 + (gt >> 2), t1, gt & 3);
 }
 
 template <int NSP>
@@ -683,30 +683,28 @@ __global__ void __launch_bounds__(128) k_update(const Dev d, const ThermoDev<NSP
   flag(d, err);
 }
 
-// Both LU-SGS sweeps and the update in one cooperative launch: every level of
-// the forward sweep, then of the backward sweep, separated by grid barriers,
-// then the Newton update of all cells.  A level is cut into warps of 8 cells
-// (4 lanes each) that are dealt out to blocks first, so a small level spreads
-// over as many SMs as it has warps.
+// Both LU-SGS sweeps and the Newton update in one cooperative launch: the
+// levels of the forward sweep, then of the backward sweep, separated by grid
+// barriers (bounded waits), then the update of all cells.  A level is cut into
+// warps of 8 cells (4 lanes each) dealt out to blocks first, so a small level
+// spreads over as many SMs as it has warps.
 constexpr int PERS_THREADS = 256;
 template <int NSP>
 __global__ void __launch_bounds__(PERS_THREADS) k_lusgs_persistent(const Dev d, const ThermoDev<NSP> th,
-                                                                   const int* __restrict__ fcells,
                                                                    const int* __restrict__ foff, int nf,
-                                                                   const int* __restrict__ bcells,
                                                                    const int* __restrict__ boff, int nb,
                                                                    unsigned* count) {
   const int G = gridDim.x, wpb = PERS_THREADS / 32, w = threadIdx.x >> 5;
   const int lt = (threadIdx.x & 31) >> 2, q = threadIdx.x & 3;
   unsigned seq = 0;
   for (int l = 0; l < nf; ++l) {
-    const int lo = foff[l], n = foff[l + 1] - lo, nch = (n + 7) >> 3;
-    for (int c = blockIdx.x + w * G; c < nch; c += G * wpb) sweep_step<NSP, true>(d, th, fcells + lo, n, c * 8 + lt, q);
+    const int t0 = foff[l], t1 = foff[l + 1], nch = (t1 - t0 + 7) >> 3;
+    for (int c = blockIdx.x + w * G; c < nch; c += G * wpb) sweep_step<NSP, true>(d, th, t0 + c * 8 + lt, t1, q);
     if (!grid_sync(count, seq++, d.err)) return;
   }
   for (int l = 0; l < nb; ++l) {
-    const int lo = boff[l], n = boff[l + 1] - lo, nch = (n + 7) >> 3;
-    for (int c = blockIdx.x + w * G; c < nch; c += G * wpb) sweep_step<NSP, false>(d, th, bcells + lo, n, c * 8 + lt, q);
+    const int t0 = boff[l], t1 = boff[l + 1], nch = (t1 - t0 + 7) >> 3;
+    for (int c = blockIdx.x + w * G; c < nch; c += G * wpb) sweep_step<NSP, false>(d, th, t0 + c * 8 + lt, t1, q);
     if (!grid_sync(count, seq++, d.err)) return;
   }
   unsigned err = 0;
@@ -767,11 +765,12 @@ template <int NSP> void mixed_ts_face(const Dev&, const void*, int, cudaStream_t
 template <int NSP> void mixed_cell(const Dev&, const void*, const ThermoDev<NSP>&, int, int, int, int, cudaStream_t);
 template <int NSP> void mixed_face_flux(const Dev&, const void*, int, cudaStream_t);
 template <int NSP> void mixed_gather(const Dev&, int, int, cudaStream_t);
-template <int NSP> void mixed_sweep(const Dev&, const void*, bool, const int*, int, cudaStream_t);
+template <int NSP> void mixed_pack(const Dev&, cudaStream_t);
+template <int NSP> void mixed_sweep(const Dev&, const void*, bool, int, int, cudaStream_t);
 template <int NSP> size_t mixed_thermo(const void*, void*);
 template <int NSP>
-cudaError_t mixed_lusgs_persistent(const Dev&, const void*, const ThermoDev<NSP>&, const int*, const int*, int,
-                                   const int*, const int*, int, unsigned*, int, cudaStream_t);
+cudaError_t mixed_lusgs_persistent(const Dev&, const void*, const int*, int, const int*, int, unsigned*, int,
+                                   cudaStream_t);
 template <int NSP> int mixed_persistent_occupancy();
 
 }  // namespace rc
@@ -798,6 +797,7 @@ struct rc_ctx {
   unsigned* bar_count = nullptr; // grid-barrier counter of the persistent launch
   int* fwd_off_dev = nullptr;
   int* bwd_off_dev = nullptr;
+
   double* norm_part = nullptr;
   double* norm_out = nullptr;
   double* staging = nullptr;  // (V*max(NE,NF,NG)) for layout conversion
@@ -922,9 +922,9 @@ void q_persistent(rc_ctx* c) {
   attr[0].val.cooperative = 1;
   cfg.attrs = attr;
   cfg.numAttrs = 1;
-  cudaLaunchKernelEx(&cfg, k_lusgs_persistent<NSP>, c->d, TH<NSP>(c), (const int*)c->fwd_cells,
-                     (const int*)c->fwd_off_dev, (int)c->fwd_off.size() - 1, (const int*)c->bwd_cells,
-                     (const int*)c->bwd_off_dev, (int)c->bwd_off.size() - 1, c->bar_count);
+  cudaLaunchKernelEx(&cfg, k_lusgs_persistent<NSP>, c->d, TH<NSP>(c), (const int*)c->fwd_off_dev,
+                     (int)c->fwd_off.size() - 1, (const int*)c->bwd_off_dev, (int)c->bwd_off.size() - 1,
+                     c->bar_count);
   c->launches++;
 }
 template <int NSP>
@@ -936,12 +936,13 @@ void q_sweeps(rc_ctx* c, int gather) {
   if (c->persistent) { q_persistent<NSP>(c); return; }
   for (size_t l = 0; l + 1 < c->fwd_off.size(); ++l) {
     const int n = c->fwd_off[l + 1] - c->fwd_off[l];
-    k_sweep4<NSP, true><<<blocks(4L * n, 32), 32, 0, c->stream>>>(c->d, TH<NSP>(c), c->fwd_cells + c->fwd_off[l], n);
+    k_sweep4<NSP, true><<<blocks(4L * n, 32), 32, 0, c->stream>>>(c->d, TH<NSP>(c), c->fwd_off[l], c->fwd_off[l + 1]);
     c->launches++;
   }
   for (size_t l = 0; l + 1 < c->bwd_off.size(); ++l) {
     const int n = c->bwd_off[l + 1] - c->bwd_off[l];
-    k_sweep4<NSP, false><<<blocks(4L * n, 32), 32, 0, c->stream>>>(c->d, TH<NSP>(c), c->bwd_cells + c->bwd_off[l], n);
+    k_sweep4<NSP, false><<<blocks(4L * n, 32), 32, 0, c->stream>>>(c->d, TH<NSP>(c), c->bwd_off[l],
+                                                                    c->bwd_off[l + 1]);
     c->launches++;
   }
   k_update<NSP><<<blocks(c->NE, 128), 128, 0, c->stream>>>(c->d, TH<NSP>(c));
@@ -956,20 +957,19 @@ void q_gather(rc_ctx* c) {
 template <int NSP>
 void q_sweeps32(rc_ctx* c) {
   if (c->persistent) {
-    mixed_lusgs_persistent<NSP>(c->d, c->thermo32.data(), TH<NSP>(c), c->fwd_cells, c->fwd_off_dev,
-                                (int)c->fwd_off.size() - 1, c->bwd_cells, c->bwd_off_dev, (int)c->bwd_off.size() - 1,
-                                c->bar_count, c->pers_grid, c->stream);
-    c->launches++;
+    cudaMemsetAsync(c->bar_count, 0, sizeof(unsigned), c->stream);
+    mixed_lusgs_persistent<NSP>(c->d, c->thermo32.data(), c->fwd_off_dev, (int)c->fwd_off.size() - 1, c->bwd_off_dev,
+                                (int)c->bwd_off.size() - 1, c->bar_count, c->pers_grid, c->stream);
+    k_update<NSP><<<blocks(c->NE, 128), 128, 0, c->stream>>>(c->d, TH<NSP>(c));
+    c->launches += 2;
     return;
   }
   for (size_t l = 0; l + 1 < c->fwd_off.size(); ++l) {
-    mixed_sweep<NSP>(c->d, c->thermo32.data(), true, c->fwd_cells + c->fwd_off[l], c->fwd_off[l + 1] - c->fwd_off[l],
-                     c->stream);
+    mixed_sweep<NSP>(c->d, c->thermo32.data(), true, c->fwd_off[l], c->fwd_off[l + 1], c->stream);
     c->launches++;
   }
   for (size_t l = 0; l + 1 < c->bwd_off.size(); ++l) {
-    mixed_sweep<NSP>(c->d, c->thermo32.data(), false, c->bwd_cells + c->bwd_off[l], c->bwd_off[l + 1] - c->bwd_off[l],
-                     c->stream);
+    mixed_sweep<NSP>(c->d, c->thermo32.data(), false, c->bwd_off[l], c->bwd_off[l + 1], c->stream);
     c->launches++;
   }
   k_update<NSP><<<blocks(c->NE, 128), 128, 0, c->stream>>>(c->d, TH<NSP>(c));
@@ -990,6 +990,10 @@ void q_reconstruction_mode(rc_ctx* c) {
     c->launches++;
   } else {
     q_cell<NSP>(c, 0, 1);
+    if (c->mode == RC_PREC_MIXED_DC) {
+      mixed_pack<NSP>(c->d, c->stream);
+      c->launches++;
+    }
   }
 }
 template <int NSP>
@@ -1024,6 +1028,8 @@ void q_stage(rc_ctx* c) {
     c->launches++;
   } else {
     q_cell<NSP>(c, 1, 1);
+    mixed_pack<NSP>(c->d, c->stream);
+    c->launches++;
   }
   q_flux_mode<NSP>(c);
   q_sweeps32<NSP>(c);
@@ -1281,6 +1287,13 @@ int rc_init(const rc_mesh* m, const rc_thermo* t, const rc_config* g, rc_ctx** o
     st |= dev_zeros(c, ((size_t)V * std::max(NG, 1) + 1) / 2, &f32); d.GPA32 = reinterpret_cast<float*>(f32);
     st |= dev_zeros(c, ((size_t)V * NF + 1) / 2, &f32); d.Finv32 = reinterpret_cast<float*>(f32);
     st |= dev_zeros(c, ((size_t)(V - 1) * NF + 1) / 2, &f32); d.Fvis32 = reinterpret_cast<float*>(f32);
+    st |= dev_zeros(c, ((size_t)V * NE + 1) / 2, &f32); d.PA32 = reinterpret_cast<float*>(f32);
+    st |= dev_zeros(c, ((size_t)(3 + c->NSP) * NE + 1) / 2, &f32); d.cst32 = reinterpret_cast<float*>(f32);
+    st |= dev_zeros(c, ((size_t)V * NE + 1) / 2, &f32); d.dU32 = reinterpret_cast<float*>(f32);
+    st |= dev_zeros(c, ((size_t)NF + 1) / 2, &f32); d.alpaF32 = reinterpret_cast<float*>(f32);
+    std::vector<float> fv32(fvec.begin(), fvec.end());
+    float* fv;
+    st |= dev_upload(c, fv32, &fv); d.fvec32 = fv;
   }
   double* e;
   st |= dev_zeros(c, 1, &e);
@@ -1289,6 +1302,28 @@ int rc_init(const rc_mesh* m, const rc_thermo* t, const rc_config* g, rc_ctx** o
   c->bar_count = reinterpret_cast<unsigned*>(e);
   st |= dev_upload(c, c->fwd_off, &c->fwd_off_dev);
   st |= dev_upload(c, c->bwd_off, &c->bwd_off_dev);
+  {  // sweep tables in level order
+    for (int dir = 0; dir < 2; ++dir) {
+      const std::vector<int>& lst = dir == 0 ? fc : bc;
+      std::vector<int> ti(NE), tj(4 * (size_t)NE, -1), tf(4 * (size_t)NE, 0);
+      for (int t = 0; t < NE; ++t) {
+        const int i = lst[t];
+        ti[t] = i;
+        for (int q = 0; q < nface[i]; ++q) {
+          const int j = cother[(size_t)q * NE + i];
+          if (j >= 0 && (dir == 0 ? j < i : j > i)) {
+            tj[(size_t)q * NE + t] = j;
+            const int f = cface[(size_t)q * NE + i];
+            tf[(size_t)q * NE + t] = ((cleft[i] >> q) & 1u) ? f : ~f;
+          }
+        }
+      }
+      int* p;
+      st |= dev_upload(c, ti, &p); d.swi[dir] = p;
+      st |= dev_upload(c, tj, &p); d.swj[dir] = p;
+      st |= dev_upload(c, tf, &p); d.swf[dir] = p;
+    }
+  }
   if (st) return bail(st, c->err);
   // LU-SGS schedule: one cooperative launch per iteration when every SM can
   // hold a block of the persistent kernels; RC_LUSGS_SCHEDULE=levels selects

@@ -61,6 +61,18 @@ struct Dev {
   float* GPA32;                  // [V*NG]
   float* Finv32;                 // [V*NF]
   float* Fvis32;                 // [(V-1)*NF]
+  float* PA32;                   // [V*NE] FP32 copy of PA read by the FP32 sweeps
+  float* cst32;                  // [(3+NSP)*NE] FP32 cell gas state
+  float* dU32;                   // [V*NE] FP32 copy of dU written by the FP32 sweeps
+  float* alpaF32;                // [NF]
+  float* fvec32;                 // [2*NF]
+  // LU-SGS sweep tables in level order, [0] forward / [1] backward: position t
+  // holds cell swi[t]; slot q holds the neighbour read in that sweep
+  // (swj[q*NE+t], -1 if none) and its face (swf[q*NE+t], bitwise-complemented
+  // when the cell is the face's right cell, i.e. the normal is reversed).
+  const int* swi[2];
+  const int* swj[2];
+  const int* swf[2];
 };
 
 __device__ __forceinline__ void flag(const Dev& d, unsigned e) {
@@ -134,4 +146,23 @@ __device__ __forceinline__ void update_cell(const Dev& d, const ThermoDev<NSP>& 
   if (i == 0 && isnan(W[0])) err |= ERR_NAN;
 }
 
+// Wait until *f becomes non-zero (a cell's sweep result is published).
+// Bounded: after 2^24 polls, or once another waiter has given up, ERR_SYNC is
+// latched and false returned; the caller then goes on with stale data and the
+// host sees the error at its next synchronising call.
+__device__ __forceinline__ bool wait_flag(const unsigned* f, unsigned* err) {
+  for (unsigned spin = 0; ld_acquire(f) == 0u; ++spin) {
+    if ((spin & 255u) == 255u && (spin > (1u << 24) || (ld_acquire(err) & ERR_SYNC))) {
+      atomicOr(err, ERR_SYNC);
+      return false;
+    }
+  }
+  return true;
+}
+__device__ __forceinline__ void publish_flag(unsigned* f) {
+  __threadfence();
+  asm volatile("st.release.gpu.global.u32 [%0], %1;" ::"l"(f), "r"(1u) : "memory");
+}
+
 }  // namespace rc
+

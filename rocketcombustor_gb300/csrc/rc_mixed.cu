@@ -51,8 +51,10 @@ __global__ void __launch_bounds__(128) k_ts_face32(const Dev d, const ThermoDev3
     d.visL[f] = vl;
     d.visR[f] = (NR >= 0) ? vis / d.vol[NR] : 0.0;
     d.alpaF[f] = (double)alpa + vl;
+    d.alpaF32[f] = (float)((double)alpa + vl);
   } else {
     d.alpaF[f] = alpa;
+    d.alpaF32[f] = alpa;
   }
   if (err) atomicOr(d.err, err);
 }
@@ -95,11 +97,13 @@ __global__ void __launch_bounds__(128) k_cell32(const Dev d, const ThermoDev32<N
   float hh = 0.f;
 #pragma unroll
   for (int k = 0; k < NSP; ++k) hh += Y[k] * entha[k];
-  d.cst[0 * NE + i] = rr;
-  d.cst[1 * NE + i] = gama;
-  d.cst[2 * NE + i] = rr * (hh + 0.5f * (P[1] * P[1] + P[2] * P[2])) - P[0];
+  d.cst32[0 * NE + i] = rr;
+  d.cst32[1 * NE + i] = gama;
+  d.cst32[2 * NE + i] = rr * (hh + 0.5f * (P[1] * P[1] + P[2] * P[2])) - P[0];
 #pragma unroll
-  for (int k = 0; k < NSP; ++k) d.cst[(3 + k) * NE + i] = entha[k];
+  for (int k = 0; k < NSP; ++k) d.cst32[(3 + k) * NE + i] = entha[k];
+#pragma unroll
+  for (int k = 0; k < V; ++k) d.PA32[k * NE + i] = P[k];
   // gradient: differences in FP64, weights and sums in FP32
   float g0[V], g1[V], mn[V], mx[V];
 #pragma unroll
@@ -506,108 +510,120 @@ __global__ void __launch_bounds__(128) k_gather32(const Dev d, int visc, int com
 // Four lanes per cell as in the FP64 sweep; the off-diagonal terms in FP32,
 // the diagonal division in FP64.
 template <int NSP, bool FWD>
-__device__ __forceinline__ void sweep_step32(const Dev& d, const ThermoDev32<NSP>& th, const int* __restrict__ cells,
-                                             int n, int t, int q) {
+__device__ __forceinline__ void sweep_step32(const Dev& d, const ThermoDev32<NSP>& th, int t, int tend, int q) {
   constexpr int V = 3 + NSP;
-  const bool valid = t < n;
-  const int i = valid ? cells[t] : 0;
+  constexpr int DIR = FWD ? 0 : 1;
+  const bool valid = t < tend;
   const int NE = d.NE, NF = d.NF;
+  const int i = valid ? d.swi[DIR][t] : 0;
+  const int j = valid ? d.swj[DIR][q * NE + t] : -1;
+  const int fs = valid ? d.swf[DIR][q * NE + t] : 0;
+  double R0 = 0.0, R1 = 0.0, rdd = 0.0;
+  if (valid) {  // own residual (variables q, q+4) and FP64 diagonal, issued early
+    R0 = d.hWA[q * NE + i];
+    if (q + 4 < V) R1 = d.hWA[(q + 4) * NE + i];
+    rdd = 1.0 / d.dd[i];
+  }
   float c[V];
 #pragma unroll
   for (int k = 0; k < V; ++k) c[k] = 0.f;
-  if (valid && q < d.nface[i]) {
-    const int j = d.cother[q * NE + i];
-    if (j >= 0 && (FWD ? j < i : j > i)) {
-      const int f = d.cface[q * NE + i];
-      float dx = (float)d.fvec[f], dy = (float)d.fvec[NF + f];
-      if (!((d.cleft[i] >> q) & 1u)) { dx = -dx; dy = -dy; }
-      const float pp = (float)d.PA[0 * NE + j], uu = (float)d.PA[1 * NE + j], vv = (float)d.PA[2 * NE + j],
-                  tt = (float)d.PA[3 * NE + j];
-      const float rr = (float)d.cst[0 * NE + j], gama = (float)d.cst[1 * NE + j], roe = (float)d.cst[2 * NE + j];
-      const float rou = rr * uu, rov = rr * vv;
-      const float drr = (float)d.hWA[0 * NE + j], dru = (float)d.hWA[1 * NE + j], drv = (float)d.hWA[2 * NE + j],
-                  dre = (float)d.hWA[3 * NE + j];
-      float dry[NSP], s = 0.f;
+  const bool act = j >= 0;
+  if (act) {
+    const int f = fs >= 0 ? fs : ~fs;
+    float dx = d.fvec32[f], dy = d.fvec32[NF + f];
+    if (fs < 0) { dx = -dx; dy = -dy; }
+    const float pp = d.PA32[0 * NE + j], uu = d.PA32[1 * NE + j], vv = d.PA32[2 * NE + j], tt = d.PA32[3 * NE + j];
+    const float rr = d.cst32[0 * NE + j], gama = d.cst32[1 * NE + j], roe = d.cst32[2 * NE + j];
+    const float rou = rr * uu, rov = rr * vv;
+    const float drr = d.dU32[0 * NE + j], dru = d.dU32[1 * NE + j], drv = d.dU32[2 * NE + j],
+                dre = d.dU32[3 * NE + j];
+    float dry[NSP], s = 0.f;
 #pragma unroll
-      for (int k = 0; k < NSP - 1; ++k) { dry[k] = (float)d.hWA[(4 + k) * NE + j]; s += dry[k]; }
-      dry[NSP - 1] = drr - s;
-      const float rinv = 1.f / rr;
-      const float duu = (dru - uu * drr) * rinv;
-      const float dvv = (drv - vv * drr) * rinv;
-      float s1 = 0.f, s2 = 0.f;
+    for (int k = 0; k < NSP - 1; ++k) { dry[k] = d.dU32[(4 + k) * NE + j]; s += dry[k]; }
+    dry[NSP - 1] = drr - s;
+    const float rinv = 1.f / rr;
+    const float duu = (dru - uu * drr) * rinv;
+    const float dvv = (drv - vv * drr) * rinv;
+    float s1 = 0.f, s2 = 0.f;
 #pragma unroll
-      for (int k = 0; k < NSP; ++k) {
-        s1 += (float)d.cst[(3 + k) * NE + j] * dry[k];
-        s2 += th.R[k] * dry[k];
-      }
-      const float gm1 = gama - 1.f;
-      const float dpp = gm1 * (dre - s1 + tt * s2 * gama / gm1 - 0.5f * (dru * uu + duu * rou + drv * vv + dvv * rov));
-      const float un = uu * dx + vv * dy, dun = duu * dx + dvv * dy;
-      const float aF = (float)d.alpaF[f];
-      c[0] = 0.5f * (-aF * drr + dru * dx + drv * dy);
-      c[1] = 0.5f * (-aF * dru + dru * un + rou * dun + dpp * dx);
-      c[2] = 0.5f * (-aF * drv + drv * un + rov * dun + dpp * dy);
-      c[3] = 0.5f * (-aF * dre + dun * (roe + pp) + un * (dre + dpp));
-#pragma unroll
-      for (int k = 0; k < NSP - 1; ++k)
-        c[4 + k] = 0.5f * (-aF * dry[k] + dry[k] * un + rr * (float)d.PA[(4 + k) * NE + j] * dun);
+    for (int k = 0; k < NSP; ++k) {
+      s1 += d.cst32[(3 + k) * NE + j] * dry[k];
+      s2 += th.R[k] * dry[k];
     }
+    const float gm1 = gama - 1.f;
+    const float dpp = gm1 * (dre - s1 + tt * s2 * gama / gm1 - 0.5f * (dru * uu + duu * rou + drv * vv + dvv * rov));
+    const float un = uu * dx + vv * dy, dun = duu * dx + dvv * dy;
+    const float aF = d.alpaF32[f];
+    c[0] = 0.5f * (-aF * drr + dru * dx + drv * dy);
+    c[1] = 0.5f * (-aF * dru + dru * un + rou * dun + dpp * dx);
+    c[2] = 0.5f * (-aF * drv + drv * un + rov * dun + dpp * dy);
+    c[3] = 0.5f * (-aF * dre + dun * (roe + pp) + un * (dre + dpp));
+#pragma unroll
+    for (int k = 0; k < NSP - 1; ++k) c[4 + k] = 0.5f * (-aF * dry[k] + dry[k] * un + rr * d.PA32[(4 + k) * NE + j] * dun);
   }
   const int base = (threadIdx.x & 31) & ~3;
-  float df[V];
-#pragma unroll
-  for (int k = 0; k < V; ++k) df[k] = 0.f;
+  float df0 = 0.f, df1 = 0.f;
 #pragma unroll
   for (int sl = 0; sl < 4; ++sl)
 #pragma unroll
-    for (int k = 0; k < V; ++k) df[k] += __shfl_sync(0xffffffffu, c[k], base + sl);
-  if (!valid) return;
-  const double ddi = d.dd[i];
-#pragma unroll
-  for (int k = 0; k < V; ++k)
-    if ((k & 3) == q) {
-      const double R = d.hWA[k * NE + i];
-      d.hWA[k * NE + i] = FWD ? (R - (double)df[k]) / ddi : R - (double)df[k] / ddi;
+    for (int k = 0; k < V; ++k) {
+      const float cs = __shfl_sync(0xffffffffu, c[k], base + sl);
+      if (k == q) df0 += cs;
+      if (k == q + 4) df1 += cs;
     }
+  if (!valid) return;
+  const double u0 = FWD ? (R0 - (double)df0) * rdd : R0 - (double)df0 * rdd;
+  d.hWA[q * NE + i] = u0;
+  d.dU32[q * NE + i] = (float)u0;
+  if (q + 4 < V) {
+    const double u1 = FWD ? (R1 - (double)df1) * rdd : R1 - (double)df1 * rdd;
+    d.hWA[(q + 4) * NE + i] = u1;
+    d.dU32[(q + 4) * NE + i] = (float)u1;
+  }
+}
+
+// FP32 copies for the FP32 sweeps when the residual comes from the FP64
+// kernels (defect-correction phase).
+template <int NSP>
+__global__ void __launch_bounds__(128) k_pack32(const Dev d) {
+  constexpr int V = 3 + NSP;
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= d.NE) return;
+  const int NE = d.NE;
+#pragma unroll
+  for (int k = 0; k < V; ++k) d.PA32[k * NE + i] = (float)d.PA[k * NE + i];
+#pragma unroll
+  for (int k = 0; k < 3 + NSP; ++k) d.cst32[k * NE + i] = (float)d.cst[k * NE + i];
 }
 
 template <int NSP, bool FWD>
-__global__ void __launch_bounds__(32) k_sweep32(const Dev d, const ThermoDev32<NSP> th, const int* __restrict__ cells,
-                                                int n) {
+__global__ void __launch_bounds__(32) k_sweep32(const Dev d, const ThermoDev32<NSP> th, int t0, int t1) {
   const int gt = blockIdx.x * blockDim.x + threadIdx.x;
-  sweep_step32<NSP, FWD>(d, th, cells, n, gt >> 2, gt & 3);
+  sweep_step32<NSP, FWD>(d, th, t0 + (gt >> 2), t1, gt & 3);
 }
 
-// Both sweeps and the FP64 update in one cooperative launch (as the FP64
-// persistent kernel of rc_core.cu).
+// Both FP32 sweeps in one cooperative launch with level barriers (the
+// schedule of the FP64 persistent kernel in rc_core.cu); the FP64 update runs
+// afterwards as its own kernel.
 constexpr int PERS32_THREADS = 256;
 template <int NSP>
 __global__ void __launch_bounds__(PERS32_THREADS) k_lusgs_persistent32(const Dev d, const ThermoDev32<NSP> th,
-                                                                       const ThermoDev<NSP> th64,
-                                                                       const int* __restrict__ fcells,
                                                                        const int* __restrict__ foff, int nf,
-                                                                       const int* __restrict__ bcells,
                                                                        const int* __restrict__ boff, int nb,
                                                                        unsigned* count) {
   const int G = gridDim.x, wpb = PERS32_THREADS / 32, w = threadIdx.x >> 5;
   const int lt = (threadIdx.x & 31) >> 2, q = threadIdx.x & 3;
   unsigned seq = 0;
   for (int l = 0; l < nf; ++l) {
-    const int lo = foff[l], n = foff[l + 1] - lo, nch = (n + 7) >> 3;
-    for (int c = blockIdx.x + w * G; c < nch; c += G * wpb)
-      sweep_step32<NSP, true>(d, th, fcells + lo, n, c * 8 + lt, q);
+    const int t0 = foff[l], t1 = foff[l + 1], nch = (t1 - t0 + 7) >> 3;
+    for (int c = blockIdx.x + w * G; c < nch; c += G * wpb) sweep_step32<NSP, true>(d, th, t0 + c * 8 + lt, t1, q);
     if (!grid_sync(count, seq++, d.err)) return;
   }
   for (int l = 0; l < nb; ++l) {
-    const int lo = boff[l], n = boff[l + 1] - lo, nch = (n + 7) >> 3;
-    for (int c = blockIdx.x + w * G; c < nch; c += G * wpb)
-      sweep_step32<NSP, false>(d, th, bcells + lo, n, c * 8 + lt, q);
+    const int t0 = boff[l], t1 = boff[l + 1], nch = (t1 - t0 + 7) >> 3;
+    for (int c = blockIdx.x + w * G; c < nch; c += G * wpb) sweep_step32<NSP, false>(d, th, t0 + c * 8 + lt, t1, q);
     if (!grid_sync(count, seq++, d.err)) return;
   }
-  unsigned err = 0;
-  for (int i = blockIdx.x * PERS32_THREADS + threadIdx.x; i < d.NE; i += G * PERS32_THREADS)
-    update_cell<NSP>(d, th64, i, err);
-  if (err) atomicOr(d.err, err);
 }
 
 // ------------------------------------------------------- host launchers ----
@@ -632,22 +648,23 @@ void mixed_face_flux(const Dev& d, const void* th32, int visc, cudaStream_t s) {
   else k_face_flux32<NSP, false><<<nblk(d.NF, 128), 128, 0, s>>>(d, th);
 }
 template <int NSP>
+void mixed_pack(const Dev& d, cudaStream_t s) {
+  k_pack32<NSP><<<nblk(d.NE, 128), 128, 0, s>>>(d);
+}
+template <int NSP>
 void mixed_gather(const Dev& d, int visc, int comb, cudaStream_t s) {
   k_gather32<NSP><<<nblk(d.NE, 128), 128, 0, s>>>(d, visc, comb);
 }
 template <int NSP>
-void mixed_sweep(const Dev& d, const void* th32, bool fwd, const int* cells, int n, cudaStream_t s) {
+void mixed_sweep(const Dev& d, const void* th32, bool fwd, int t0, int t1, cudaStream_t s) {
   const auto& th = *static_cast<const ThermoDev32<NSP>*>(th32);
-  if (fwd) k_sweep32<NSP, true><<<nblk(4L * n, 32), 32, 0, s>>>(d, th, cells, n);
-  else k_sweep32<NSP, false><<<nblk(4L * n, 32), 32, 0, s>>>(d, th, cells, n);
+  if (fwd) k_sweep32<NSP, true><<<nblk(4L * (t1 - t0), 32), 32, 0, s>>>(d, th, t0, t1);
+  else k_sweep32<NSP, false><<<nblk(4L * (t1 - t0), 32), 32, 0, s>>>(d, th, t0, t1);
 }
-// Cooperative launch of the persistent sweeps (count zeroed first, in stream order).
+// Cooperative launch of the persistent FP32 sweeps (barrier counter zeroed by the caller).
 template <int NSP>
-cudaError_t mixed_lusgs_persistent(const Dev& d, const void* th32, const ThermoDev<NSP>& th64, const int* fc,
-                                   const int* fo, int nf, const int* bc, const int* bo, int nb, unsigned* count,
-                                   int grid, cudaStream_t s) {
-  cudaError_t e = cudaMemsetAsync(count, 0, sizeof(unsigned), s);
-  if (e != cudaSuccess) return e;
+cudaError_t mixed_lusgs_persistent(const Dev& d, const void* th32, const int* foff, int nf, const int* boff, int nb,
+                                   unsigned* count, int grid, cudaStream_t s) {
   cudaLaunchConfig_t cfg = {};
   cfg.gridDim = dim3((unsigned)grid);
   cfg.blockDim = dim3(PERS32_THREADS);
@@ -657,8 +674,8 @@ cudaError_t mixed_lusgs_persistent(const Dev& d, const void* th32, const ThermoD
   attr[0].val.cooperative = 1;
   cfg.attrs = attr;
   cfg.numAttrs = 1;
-  return cudaLaunchKernelEx(&cfg, k_lusgs_persistent32<NSP>, d, *static_cast<const ThermoDev32<NSP>*>(th32), th64, fc,
-                            fo, nf, bc, bo, nb, count);
+  return cudaLaunchKernelEx(&cfg, k_lusgs_persistent32<NSP>, d, *static_cast<const ThermoDev32<NSP>*>(th32), foff, nf,
+                            boff, nb, count);
 }
 template <int NSP>
 int mixed_persistent_occupancy() {
@@ -677,11 +694,11 @@ size_t mixed_thermo(const void* th64, void* out) {
   template void mixed_cell<N>(const Dev&, const void*, const ThermoDev<N>&, int, int, int, int, cudaStream_t);  \
   template void mixed_face_flux<N>(const Dev&, const void*, int, cudaStream_t);                                 \
   template void mixed_gather<N>(const Dev&, int, int, cudaStream_t);                                            \
-  template void mixed_sweep<N>(const Dev&, const void*, bool, const int*, int, cudaStream_t);                   \
+  template void mixed_pack<N>(const Dev&, cudaStream_t);                                                        \
+  template void mixed_sweep<N>(const Dev&, const void*, bool, int, int, cudaStream_t);                          \
   template size_t mixed_thermo<N>(const void*, void*);                                                       \
-  template cudaError_t mixed_lusgs_persistent<N>(const Dev&, const void*, const ThermoDev<N>&, const int*,       \
-                                                 const int*, int, const int*, const int*, int, unsigned*, int,  \
-                                                 cudaStream_t);                                                 \
+  template cudaError_t mixed_lusgs_persistent<N>(const Dev&, const void*, const int*, int, const int*, int,       \
+                                                 unsigned*, int, cudaStream_t);                                 \
   template int mixed_persistent_occupancy<N>();
 RC_MIXED_INST(1)
 RC_MIXED_INST(4)
