@@ -47,6 +47,9 @@ extern "C" {
 #define RC_PREC_MIXED_DC 2     /* defect correction: the FP64 residual of RC_PREC_FP64 driving the
                                   FP32 LU-SGS sweeps of RC_PREC_MIXED (FP64 fixed point) */
 
+#define RC_CHEM_EXPLICIT 0     /* chemical source = vol*omega, the reference's explicit rate (sourceterm.f90:43-51) */
+#define RC_CHEM_INTEGRATED 1   /* chemical source = vol*rho*(Y(step)-Y)/step from the per-cell integrator */
+
 typedef struct rc_ctx rc_ctx;
 
 /*
@@ -143,6 +146,25 @@ int rc_lusgs_stage(rc_ctx* ctx, int istep); /* lu_sgs_stage   Time_LUSGS_steady.
  * driver switches MIXED -> MIXED_DC when the FP32 residual stops decreasing.
  * No counterpart in the reference (it has a single FP64 path). */
 int rc_set_precision(rc_ctx* ctx, int precision);
+
+/* Chemistry source of the following iterations (all precision modes; the
+ * chemistry is FP64 in each).  RC_CHEM_INTEGRATED integrates each cell's
+ * constant-volume adiabatic reactor over its pseudo time step with linearly
+ * implicit substeps built on Compute_Con_to_Pri_Jaco (Con_to_Pri_Jacobian.f90:1)
+ * and compute_derivative_production_rate (chemical_kinetics.f90:167); tol is
+ * the relative change allowed per substep (0.05 by default), max_substeps the
+ * cap (200).  The reference has no such integrator: it is new.  Needs
+ * If_turn_on_combustion. */
+int rc_set_chemistry(rc_ctx* ctx, int mode, double tol, int max_substeps);
+/* Accepted substeps per cell of the last integrated source (NE ints, host);
+ * zeros before the first one.  Synchronises. */
+int rc_chem_substeps(rc_ctx* ctx, int* nsub);
+/* Integrate n primitive states over their own dt with the same integrator:
+ * d_P and d_out are DEVICE arrays in SoA layout (component k of state i at
+ * [k*n + i], NVar components), d_dt and d_nsub device arrays of n.  Runs on the
+ * context's stream; stop conditions latch like the other calls. */
+int rc_chem_integrate(rc_ctx* ctx, const double* d_P, const double* d_dt, int n, double* d_out, int* d_nsub,
+                      double tol, int max_substeps);
 
 /* Residual + step_residual norms (residual.f90:4-21, 61-79): res(k) =
  * sum(vol*|hWA(k,:)|)/total_volume, romax = max(WA(1,:)).  Synchronises. */

@@ -65,6 +65,13 @@ def lib() -> ctypes.CDLL:
         L.orc_production.argtypes = [vp, d, d, dp, dp]
         L.orc_newton.restype = d; L.orc_newton.argtypes = [vp, d, dp, d]
         L.orc_math.argtypes = [i, dp, dp, dp, l]
+        ip = ctypes.POINTER(ctypes.c_int)
+        L.orc_con_to_pri_jaco.argtypes = [vp, dp, dp]
+        L.orc_dwdp.argtypes = [vp, dp, dp]
+        L.orc_chem_integrate.restype = i
+        L.orc_chem_integrate.argtypes = [vp, l, dp, dp, dp, ip, d, i]
+        L.orc_set_chemistry.argtypes = [vp, i, d, i]
+        L.orc_chem_nsub.restype = ip; L.orc_chem_nsub.argtypes = [vp]
         _lib = L
     return _lib
 
@@ -205,6 +212,42 @@ class Oracle:
         o = np.zeros(self.Nsp)
         lib().orc_production(self._h, float(T), float(rho), _dp(Y), _dp(o))
         return o
+
+    def con_to_pri_jaco(self, pri):
+        pri = np.ascontiguousarray(pri, dtype=np.float64)
+        o = np.zeros((self.NVar, self.NVar))
+        lib().orc_con_to_pri_jaco(self._h, _dp(pri), _dp(o))
+        return o
+
+    def dwdp(self, pri):
+        pri = np.ascontiguousarray(pri, dtype=np.float64)
+        o = np.zeros((self.Nsp - 1, self.NVar))
+        lib().orc_dwdp(self._h, _dp(pri), _dp(o))
+        return o
+
+    def chem_integrate(self, P, dt, tol=0.05, maxsub=200):
+        """Integrate n primitive states (n x NVar) over dt (n); returns
+        (states after dt, accepted substep counts)."""
+        P = np.ascontiguousarray(np.atleast_2d(P), dtype=np.float64)
+        dt = np.ascontiguousarray(np.broadcast_to(np.asarray(dt, dtype=np.float64), (P.shape[0],)))
+        out = np.empty_like(P)
+        nsub = np.zeros(P.shape[0], dtype=np.int32)
+        e = lib().orc_chem_integrate(self._h, P.shape[0], _dp(P), _dp(dt), _dp(out),
+                                     nsub.ctypes.data_as(ctypes.POINTER(ctypes.c_int)), float(tol), int(maxsub))
+        if e:
+            raise RuntimeError(f"oracle error {e}: " + self.last_error())
+        return out, nsub
+
+    def set_chemistry(self, mode, tol=0.05, maxsub=200):
+        """Source mode: 0 explicit rate (the reference), 1 integrated over the
+        cell's pseudo time step."""
+        lib().orc_set_chemistry(self._h, int(mode), float(tol), int(maxsub))
+
+    def chem_nsub(self):
+        p = lib().orc_chem_nsub(self._h)
+        if not p:
+            return None
+        return np.ctypeslib.as_array(p, shape=(self.NE,)).copy()
 
     def newton(self, et, Y, t0):
         Y = np.ascontiguousarray(Y, dtype=np.float64)

@@ -540,6 +540,211 @@ struct Oracle {
     for (int ks = 1; ks <= Nsp; ++ks)
       prod[ks - 1] = 1000 * mole_weight[ks - 1] * (coef_r_react(ks, 1) - coef_f_react(ks, 1)) * kf;
   }
+  // Compute_Con_to_Pri_Jaco (Con_to_Pri_Jacobian.f90:1-87): jaco[r*NVar+c] =
+  // dU_r/dP_c, U = (rho, rho u, rho v, rho E, rho Y_1..), P = (p, u, v, T, Y_1..).
+  void Compute_Con_to_Pri_Jaco(const double* pri, double* jaco) {
+    const int nv = NVar, ns1 = Nsp - 1;
+    const double p = pri[0], u = pri[1], v = pri[2], t = pri[3];
+    const double* y = pri + NFlow;
+    double y2[16], entha[16], dhdy[16], drdy[16], Cp, gama, Rcpcv;
+    double s = 0.0;
+    for (int i = 0; i < ns1; ++i) { y2[i] = y[i]; s = s + y[i]; }
+    y2[Nsp - 1] = 1. - s;
+    ComputeGasParameter(y2, t, Cp, gama, Rcpcv);
+    const double r = p / (Rcpcv * t);
+    compute_enthalpy(t, entha);
+    double h = entha[Nsp - 1];
+    for (int i = 0; i < ns1; ++i) {
+      h = h + y[i] * (entha[i] - entha[Nsp - 1]);
+      dhdy[i] = entha[i] - entha[Nsp - 1];
+    }
+    const double drdp = 1. / (Rcpcv * t), drdt = -p / (Rcpcv * t * t);
+    for (int i = 0; i < ns1; ++i) drdy[i] = -(R_species[i] - R_species[Nsp - 1]) * p / (t * Rcpcv * Rcpcv);
+    const double ke = h + 0.5 * (u * u + v * v);
+    for (int k = 0; k < nv * nv; ++k) jaco[k] = 0.0;
+    double* J0 = jaco;
+    double* J1 = jaco + nv;
+    double* J2 = jaco + 2 * nv;
+    double* J3 = jaco + 3 * nv;
+    J0[0] = drdp; J0[3] = drdt;
+    J1[0] = u * drdp; J1[1] = r; J1[3] = u * drdt;
+    J2[0] = v * drdp; J2[2] = r; J2[3] = v * drdt;
+    J3[0] = ke * drdp - 1.; J3[1] = r * u; J3[2] = r * v; J3[3] = r * Cp + ke * drdt;
+    for (int i = 0; i < ns1; ++i) {
+      J0[NFlow + i] = drdy[i];
+      J1[NFlow + i] = u * drdy[i];
+      J2[NFlow + i] = v * drdy[i];
+      J3[NFlow + i] = ke * drdy[i] + r * dhdy[i];
+      double* Ji = jaco + (NFlow + i) * nv;
+      Ji[0] = drdp * y[i];
+      Ji[3] = drdt * y[i];
+      for (int j = 0; j < ns1; ++j) Ji[NFlow + j] = (j == i) ? r + y[i] * drdy[i] : y[i] * drdy[j];
+    }
+  }
+  // compute_derivative_production_rate (chemical_kinetics.f90:167-265):
+  // dwdp[i*NVar+c] = d omega_i / dP_c for the Nsp-1 transported species.
+  // Model 1 leaves dkfdy(3:) unset in the reference (:231-246); it is taken
+  // here as dkfdr*drdy(3:), the expression of model 0.
+  void compute_derivative_production_rate(const double* pri, double* dwdp) {
+    const int nv = NVar, ns1 = Nsp - 1;
+    const double epsilon = 1.0e-12;
+    const double p = pri[0], T = pri[3];
+    double y[16], y2[16], drdy[16], dkf[32], Cp, gama, Rcpcv;
+    double s = 0.0;
+    for (int i = 0; i < ns1; ++i) { y[i] = pri[NFlow + i]; y2[i] = y[i]; s = s + y[i]; }
+    y2[Nsp - 1] = 1. - s;
+    ComputeGasParameter(y2, T, Cp, gama, Rcpcv);
+    const double rho = p / (Rcpcv * T);
+    for (int i = 0; i < ns1; ++i) { y[i] = fmax2(0., y[i]); y[i] = fmin2(1., y[i]); }
+    if (y[0] < epsilon) {
+      for (int c = 0; c < nv; ++c) dkf[c] = 0.;
+    } else {
+      double af = Af_react[0] * rcm::exp(-E_react[0] / (Rconstant * T));
+      const double r1 = y[0] * rho / (mole_weight[0] * 1000);
+      const double dr1dr = y[0] / (mole_weight[0] * 1000);
+      const double dr1dy1 = rho / (mole_weight[0] * 1000);
+      const double y1 = ns1 > 1 ? y[1] : 0.0;
+      const double r2 = y1 * rho / (mole_weight[1] * 1000);
+      const double dr2dr = y1 / (mole_weight[1] * 1000);
+      const double dr2dy2 = rho / (mole_weight[1] * 1000);
+      const double drdp = rho / p, drdT = -rho / T;
+      for (int i = 0; i < ns1; ++i) drdy[i] = -(R_species[i] - R_species[Nsp - 1]) * rho / Rcpcv;
+      double dkfdr, dkfdT, dkfdy[16];
+      if (code_chemical_model == 0) {
+        const double dter1_dr = 0.2 * rcm::pow(rho, -0.8) * rcm::pow(dr1dr, 0.2);
+        dkfdr = af * (rcm::pow(r1, 0.2) * 1.3 * rcm::pow(r2, 0.3) * dr2dr + dter1_dr * rcm::pow(r2, 1.3));
+        dkfdT = af * rcm::pow(r1, 0.2) * rcm::pow(r2, 1.3) * E_react[0] / (Rconstant * T * T) + dkfdr * drdT;
+        dkfdy[0] = af * 0.2 * rcm::pow(r1, -0.8) * dr1dy1 * rcm::pow(r2, 1.3) + dkfdr * drdy[0];
+        if (ns1 > 1) dkfdy[1] = af * rcm::pow(r1, 0.2) * 1.3 * rcm::pow(r2, 0.3) * dr2dy2 + dkfdr * drdy[1];
+      } else {
+        af = 0.0;
+        if (T > 710.0) af = 1e4;
+        const double dter1_dr = dr1dr;                 // 1*rho**0*dr1dr**1
+        dkfdr = af * (r1 * 0 * dr2dr + dter1_dr);       // (r1**1)*0*(r2**0)*dr2dr + dter1_dr*(r2**0)
+        dkfdT = 0.;
+        dkfdy[0] = af * dr1dy1 + dkfdr * drdy[0];       // af*1*(r1**0)*dr1dy1*(r2**0)
+        if (ns1 > 1) dkfdy[1] = af * r1 * 0 * dr2dy2 + dkfdr * drdy[1];
+      }
+      for (int i = 2; i < ns1; ++i) dkfdy[i] = dkfdr * drdy[i];
+      dkf[0] = dkfdr * drdp; dkf[1] = 0.; dkf[2] = 0.; dkf[3] = dkfdT;
+      for (int i = 0; i < ns1; ++i) dkf[NFlow + i] = dkfdy[i];
+    }
+    for (int i = 0; i < ns1; ++i) {
+      const double c = 1000 * mole_weight[i] * (coef_r_react(i + 1, 1) - coef_f_react(i + 1, 1));
+      for (int k = 0; k < nv; ++k) dwdp[i * nv + k] = c * dkf[k];
+    }
+  }
+
+  // ---- per-cell chemistry integrator (new: the reference has none) --------
+  // Integrates the isolated, constant-volume, adiabatic reactor of one cell
+  // over dt: rho, u, v and the internal energy e = h - R_mix T stay fixed,
+  // dY_k/dt = omega_k(T, rho, Y)/rho.  Each substep of length hs is one
+  // linearly implicit (Rosenbrock-Euler) step in primitive variables built on
+  // the reference's own Jacobians:
+  //   (dU/dP - hs * d omega/dP) dP = hs * (0, 0, 0, 0, omega_1..omega_{Nsp-1})
+  // (dU/dP: Compute_Con_to_Pri_Jaco; d omega/dP:
+  // compute_derivative_production_rate, in the species rows), solved by
+  // Gaussian elimination with partial pivoting.  The flow rows make the
+  // increment keep rho, rho u, rho v, rho E.  Y += dP_Y, then T from
+  // Newton_temperature at the fixed e (guess T + dP_T, clamped to the thermo
+  // range), p = rho R_mix T.
+  // Step control: with d = max(max_k |dY_k| / (tol (|Y_k| + 1e-3)),
+  // |dT| / (0.1 tol T)), a substep with d > 1 is rejected and shortened to
+  // hs * max(0.2, 0.9/d); an accepted one lets the next grow to
+  // hs * min(2, 0.9/d).  The
+  // substep that would be number maxsub, or any attempt after 2*maxsub
+  // attempts, takes the remaining time unconditionally (implicit Euler is
+  // L-stable).  Returns the accepted substep count.
+  static int gepp_solve(int n, double* A, double* b) {
+    for (int k = 0; k < n; ++k) {
+      int piv = k;
+      double best = std::fabs(A[k * n + k]);
+      for (int r = k + 1; r < n; ++r) {
+        const double a = std::fabs(A[r * n + k]);
+        if (a > best) { best = a; piv = r; }
+      }
+      if (!(best > 0.0)) return 1;
+      if (piv != k) {
+        for (int c = 0; c < n; ++c) std::swap(A[k * n + c], A[piv * n + c]);
+        std::swap(b[k], b[piv]);
+      }
+      const double d = A[k * n + k];
+      for (int r = k + 1; r < n; ++r) {
+        const double f = A[r * n + k] / d;
+        for (int c = k + 1; c < n; ++c) A[r * n + c] = A[r * n + c] - f * A[k * n + c];
+        b[r] = b[r] - f * b[k];
+      }
+    }
+    for (int k = n - 1; k >= 0; --k) {
+      double s = b[k];
+      for (int c = k + 1; c < n; ++c) s = s - A[k * n + c] * b[c];
+      b[k] = s / A[k * n + k];
+    }
+    return 0;
+  }
+  int chem_integrate(const double* P0, double dt, double* P1, double tol, int maxsub) {
+    const int nv = NVar, ns1 = Nsp - 1;
+    double P[32], Y2[16], entha[16], A[32 * 32], b[32], J[32 * 32], D[16 * 32], prod[16], Cp, gama, Rcpcv;
+    for (int k = 0; k < nv; ++k) P[k] = P0[k];
+    double s = 0.0;
+    for (int i = 0; i < ns1; ++i) { Y2[i] = P[NFlow + i]; s = s + Y2[i]; }
+    Y2[Nsp - 1] = 1. - s;
+    ComputeGasParameter(Y2, P[3], Cp, gama, Rcpcv);
+    const double rho = P[0] / (Rcpcv * P[3]);
+    compute_enthalpy(P[3], entha);
+    double h = 0.0;
+    for (int i = 0; i < Nsp; ++i) h = h + Y2[i] * entha[i];
+    const double e = h - Rcpcv * P[3];
+    double rem = dt, hs = dt;
+    int nacc = 0, natt = 0;
+    while (rem > 0.0) {
+      const bool last = nacc + 1 >= maxsub || natt >= 2 * maxsub;
+      if (last || hs > rem) hs = rem;
+      // rho from the current primitive state (p was set from rho R T)
+      Compute_Con_to_Pri_Jaco(P, J);
+      compute_derivative_production_rate(P, D);
+      double yc[16], sc = 0.0;
+      for (int i = 0; i < ns1; ++i) { yc[i] = P[NFlow + i]; sc = sc + yc[i]; }
+      yc[Nsp - 1] = 1. - sc;
+      compute_production_rate(P[3], rho, yc, prod);
+      for (int k = 0; k < nv * nv; ++k) A[k] = J[k];
+      for (int i = 0; i < ns1; ++i)
+        for (int c = 0; c < nv; ++c) A[(NFlow + i) * nv + c] = A[(NFlow + i) * nv + c] - hs * D[i * nv + c];
+      for (int k = 0; k < NFlow; ++k) b[k] = 0.0;
+      for (int i = 0; i < ns1; ++i) b[NFlow + i] = hs * prod[i];
+      if (gepp_solve(nv, A, b)) { fail(E_NAN, "chem_integrate: singular substep matrix"); break; }
+      ++natt;
+      double d = std::fabs(b[3]) / (0.1 * tol * P[3]);
+      for (int i = 0; i < ns1; ++i) d = fmax2(d, std::fabs(b[NFlow + i]) / (tol * (std::fabs(P[NFlow + i]) + 1.0e-3)));
+      if (d > 1.0 && !last) {
+        hs = hs * fmax2(0.2, 0.9 / d);
+        continue;
+      }
+      for (int i = 0; i < ns1; ++i) P[NFlow + i] = P[NFlow + i] + b[NFlow + i];
+      s = 0.0;
+      for (int i = 0; i < ns1; ++i) { Y2[i] = P[NFlow + i]; s = s + Y2[i]; }
+      Y2[Nsp - 1] = 1. - s;
+      double t;
+      const double tg = fmin2(fmax2(P[3] + b[3], thermo_lowest_tem), thermo_highest_tem);
+      Newton_temperature(e, Y2, t, tg, Cp, gama, Rcpcv);
+      P[3] = t;
+      P[0] = rho * Rcpcv * t;
+      rem = rem - hs;
+      ++nacc;
+      if (d > 0.0) hs = hs * fmin2(2.0, 0.9 / d);
+      else hs = 2.0 * hs;
+      if (rem - hs < 0.01 * hs) hs = rem;
+    }
+    for (int k = 0; k < nv; ++k) P1[k] = P[k];
+    return nacc;
+  }
+  // chemistry source mode of sourceterm: 0 = the reference's explicit rate
+  // (sourceterm.f90:43-51); 1 = mean rate of chem_integrate over the cell's
+  // pseudo time step, rho * (Y(step) - Y(0)) / step.
+  int chem_mode = 0, chem_maxsub = 200;
+  double chem_tol = 0.05;
+  std::vector<int> chem_nsub;
+
   // oxidizer_inlet_bc / fuel_inlet_bc (oxidizer.f90:367-382, fuel.f90:437-452)
   void inlet_bc(bool oxid, double pl, double& pr, double& ur, double& vr, double& tr, double& rr, double* Yr,
                 double& Cpr, double& gamar, double& Rcpcvr) {
@@ -1486,13 +1691,23 @@ struct Oracle {
     cell_Y(PA, i, Y);
     ComputeGasParameter(Y, t, Cp, gama, Rcpcv);
     double rho = p / (t * Rcpcv);
+    if (chem_mode == 1) {
+      double P0[32], P1[32];
+      for (int k = 1; k <= NVar; ++k) P0[k - 1] = PA(k, i);
+      const double dt = step(i);
+      chem_nsub[i - 1] = chem_integrate(P0, dt, P1, chem_tol, chem_maxsub);
+      for (int k = 1; k <= NVar - NFlow; ++k)
+        hWA(NFlow + k, i) = hWA(NFlow + k, i) + VOL(i) * (rho * ((P1[NFlow + k - 1] - P0[NFlow + k - 1]) / dt));
+      return;
+    }
     compute_production_rate(t, rho, Y, prod);
     for (int k = 1; k <= NFlow; ++k) hWA(k, i) = hWA(k, i) + VOL(i) * 0.0;
     for (int k = 1; k <= NVar - NFlow; ++k) hWA(NFlow + k, i) = hWA(NFlow + k, i) + VOL(i) * prod[k - 1];
   }
   void sourceterm() {
     if (!If_turn_on_combustion) return;
-#pragma omp parallel for schedule(static) num_threads(nthreads) if (nthreads > 1)
+    if (chem_mode == 1 && (long)chem_nsub.size() != NE) chem_nsub.assign(NE, 0);
+#pragma omp parallel for schedule(dynamic, 64) num_threads(nthreads) if (nthreads > 1)
     for (long i = 1; i <= NE; ++i) source_one(i);
   }
   // flux_sourceterm (fvm2d.f90:196-224); the flux_difference diagnostics are
@@ -1754,6 +1969,34 @@ void orc_production(void* h, double T, double rho, const double* Y, double* prod
 void orc_math(int which, const double* x, const double* y, double* out, long n) {
   for (long i = 0; i < n; ++i)
     out[i] = which == 0 ? rcm::exp(x[i]) : which == 1 ? rcm::log(x[i]) : rcm::pow(x[i], y[i]);
+}
+// Chemistry integrator (new) and the reference Jacobians it is built on.
+void orc_con_to_pri_jaco(void* h, const double* pri, double* jaco) {
+  static_cast<Oracle*>(h)->Compute_Con_to_Pri_Jaco(pri, jaco);
+}
+void orc_dwdp(void* h, const double* pri, double* dwdp) {
+  static_cast<Oracle*>(h)->compute_derivative_production_rate(pri, dwdp);
+}
+// n states P (n x NVar, row per state) integrated over dt[i]; nsub[i] substeps.
+int orc_chem_integrate(void* h, long n, const double* P, const double* dt, double* out, int* nsub, double tol,
+                       int maxsub) {
+  auto* o = static_cast<Oracle*>(h);
+  const int nv = o->NVar;
+#pragma omp parallel for schedule(dynamic, 16) num_threads(o->nthreads) if (o->nthreads > 1)
+  for (long i = 0; i < n; ++i)
+    nsub[i] = o->chem_integrate(P + (size_t)i * nv, dt[i], out + (size_t)i * nv, tol, maxsub);
+  return o->err.load();
+}
+void orc_set_chemistry(void* h, int mode, double tol, int maxsub) {
+  auto* o = static_cast<Oracle*>(h);
+  o->chem_mode = mode;
+  o->chem_tol = tol;
+  o->chem_maxsub = maxsub;
+}
+// Substep counts of the last integrated source pass (NE ints), or null.
+const int* orc_chem_nsub(void* h) {
+  auto* o = static_cast<Oracle*>(h);
+  return o->chem_nsub.empty() ? nullptr : o->chem_nsub.data();
 }
 double orc_newton(void* h, double et, const double* Y, double t0) {
   double t, a, b, c;

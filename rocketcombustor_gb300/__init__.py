@@ -32,6 +32,7 @@ RC_ERR = {1: "thermo T out of range", 2: "transport T out of range", 4: "negativ
           64: "grid barrier timed out",
           1024: "invalid argument", 2048: "CUDA error"}
 RC_PREC_FP64, RC_PREC_MIXED, RC_PREC_MIXED_DC = 0, 1, 2
+RC_CHEM_EXPLICIT, RC_CHEM_INTEGRATED = 0, 1
 
 _i, _d, _l, _vp, _cp = ctypes.c_int, ctypes.c_double, ctypes.c_long, ctypes.c_void_p, ctypes.c_char_p
 _IP, _DP = ctypes.POINTER(ctypes.c_int), ctypes.POINTER(ctypes.c_double)
@@ -95,6 +96,9 @@ SIGNATURES = {
     "rc_run_steady": (_i, [_vp, _i, _i, _l, _l, _DP]),
     "rc_residual_noalloc": (_i, [_vp, _vp, _vp, _i, _i, _d, _vp, _DP, _DP]),
     "rc_set_precision": (_i, [_vp, _i]),
+    "rc_set_chemistry": (_i, [_vp, _i, _d, _i]),
+    "rc_chem_substeps": (_i, [_vp, _IP]),
+    "rc_chem_integrate": (_i, [_vp, _vp, _vp, _i, _vp, _vp, _d, _i]),
 }
 
 _lib: Optional[ctypes.CDLL] = None
@@ -239,6 +243,36 @@ class Solver:
         """RC_PREC_FP64, RC_PREC_MIXED or RC_PREC_MIXED_DC for the following calls."""
         self._check(load().rc_set_precision(self._h, int(precision)))
         self.precision = int(precision)
+
+    def set_chemistry(self, mode: int, tol: float = 0.05, max_substeps: int = 200):
+        """RC_CHEM_EXPLICIT (the reference's vol*omega) or RC_CHEM_INTEGRATED
+        (mean rate of the per-cell integrator over the pseudo time step)."""
+        self._check(load().rc_set_chemistry(self._h, int(mode), float(tol), int(max_substeps)))
+
+    def chem_substeps(self) -> np.ndarray:
+        out = np.zeros(self.NE, dtype=np.int32)
+        self._check(load().rc_chem_substeps(self._h, out.ctypes.data_as(_IP)))
+        return out
+
+    def chem_integrate(self, P, dt, tol: float = 0.05, max_substeps: int = 200):
+        """Integrate n primitive states (CUDA torch tensors: P (NVar, n) SoA,
+        dt (n,), float64) on the solver's stream; returns (P_out, nsub) as
+        CUDA tensors.  Synchronises the stream."""
+        import torch
+        if not (P.is_cuda and dt.is_cuda) or P.dtype != torch.float64 or dt.dtype != torch.float64:
+            raise ValueError("P and dt must be float64 CUDA tensors")
+        P = P.contiguous()
+        dt = dt.contiguous()
+        n = P.shape[1]
+        if P.shape[0] != self.NVar or dt.shape != (n,):
+            raise ValueError("P must be (NVar, n) and dt (n,)")
+        out = torch.empty_like(P)
+        nsub = torch.zeros(n, dtype=torch.int32, device=P.device)
+        torch.cuda.synchronize(P.device)  # the tensors were made on torch's stream
+        self._check(load().rc_chem_integrate(self._h, P.data_ptr(), dt.data_ptr(), n, out.data_ptr(),
+                                             nsub.data_ptr(), float(tol), int(max_substeps)))
+        self.sync()
+        return out, nsub
 
     def run(self, nsteps: int):
         for it in range(1, nsteps + 1):

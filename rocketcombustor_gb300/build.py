@@ -25,6 +25,7 @@ NVCC_COMMON = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC,-ffp-contr
 UNITS = {
     "rc_core.cu": ["--fmad=false"],
     "rc_noalloc.cu": ["--fmad=false"],
+    "rc_chem.cu": ["--fmad=false"],
     "rc_mixed.cu": ["--use_fast_math"],
 }
 HOST_UNITS = ["rc_host.cpp"]

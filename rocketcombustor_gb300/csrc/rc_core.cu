@@ -772,6 +772,11 @@ template <int NSP>
 cudaError_t mixed_lusgs_persistent(const Dev&, const void*, const int*, int, const int*, int, unsigned*, int,
                                    cudaStream_t);
 template <int NSP> int mixed_persistent_occupancy();
+template <int NSP>
+void chem_source(const Dev&, const void*, double, int, int*, unsigned*, cudaStream_t);
+template <int NSP>
+void chem_batch(const void*, const double*, const double*, int, double*, int*, double, int, unsigned*, unsigned*,
+                cudaStream_t);
 
 }  // namespace rc
 
@@ -797,6 +802,14 @@ struct rc_ctx {
   unsigned* bar_count = nullptr; // grid-barrier counter of the persistent launch
   int* fwd_off_dev = nullptr;
   int* bwd_off_dev = nullptr;
+  // chemistry source mode (RC_CHEM_*) and the integrator's work arrays
+  int chem = RC_CHEM_EXPLICIT;
+  double chem_tol = 0.05;
+  int chem_maxsub = 200;
+  int* chem_nsub = nullptr;           // [NE] accepted substeps of the last integrated source
+  unsigned* chem_counter = nullptr;   // work-queue counter
+  cudaStream_t stream2 = nullptr;     // side stream: the integrated source runs beside the face fluxes
+  cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
 
   double* norm_part = nullptr;
   double* norm_out = nullptr;
@@ -833,12 +846,13 @@ int dev_upload(rc_ctx* c, const std::vector<T>& h, T** out) {
   *out = static_cast<T*>(p);
   return RC_OK;
 }
-int dev_zeros(rc_ctx* c, size_t n, double** out) {
+template <class T>
+int dev_zeros(rc_ctx* c, size_t n, T** out) {
   void* p = nullptr;
-  RC_CU(cudaMalloc(&p, std::max<size_t>(n, 1) * sizeof(double)));
+  RC_CU(cudaMalloc(&p, std::max<size_t>(n, 1) * sizeof(T)));
   c->allocs.push_back(p);
-  RC_CU(cudaMemset(p, 0, std::max<size_t>(n, 1) * sizeof(double)));
-  *out = static_cast<double*>(p);
+  RC_CU(cudaMemset(p, 0, std::max<size_t>(n, 1) * sizeof(T)));
+  *out = static_cast<T*>(p);
   return RC_OK;
 }
 
@@ -900,8 +914,8 @@ void q_timestep_face(rc_ctx* c) {
 }
 template <int NSP>
 void q_cell(rc_ctx* c, int do_step, int do_recon) {
-  k_cell<NSP><<<blocks(c->NE, 128), 128, 0, c->stream>>>(c->d, TH<NSP>(c), do_step, do_recon, c->limit, c->comb,
-                                                          c->visc);
+  k_cell<NSP><<<blocks(c->NE, 128), 128, 0, c->stream>>>(c->d, TH<NSP>(c), do_step, do_recon, c->limit,
+                                                          c->comb && c->chem == RC_CHEM_EXPLICIT, c->visc);
   c->launches++;
 }
 template <int NSP>
@@ -948,6 +962,21 @@ void q_sweeps(rc_ctx* c, int gather) {
   k_update<NSP><<<blocks(c->NE, 128), 128, 0, c->stream>>>(c->d, TH<NSP>(c));
   c->launches++;
 }
+// Integrated chemical source on the side stream, forked after the cell pass
+// and joined before the gather, so that it overlaps the face fluxes.
+template <int NSP>
+void q_chem_fork(rc_ctx* c) {
+  if (!c->comb || c->chem != RC_CHEM_INTEGRATED) return;
+  cudaEventRecord(c->ev_fork, c->stream);
+  cudaStreamWaitEvent(c->stream2, c->ev_fork, 0);
+  chem_source<NSP>(c->d, c->thermo.data(), c->chem_tol, c->chem_maxsub, c->chem_nsub, c->chem_counter, c->stream2);
+  c->launches++;
+  cudaEventRecord(c->ev_join, c->stream2);
+}
+void q_chem_join(rc_ctx* c) {
+  if (!c->comb || c->chem != RC_CHEM_INTEGRATED) return;
+  cudaStreamWaitEvent(c->stream, c->ev_join, 0);
+}
 template <int NSP>
 void q_gather(rc_ctx* c) {
   k_gather<NSP><<<blocks(c->NE, 128), 128, 0, c->stream>>>(c->d, c->visc, c->comb);
@@ -986,7 +1015,8 @@ void q_timestep_mode(rc_ctx* c) {
 template <int NSP>
 void q_reconstruction_mode(rc_ctx* c) {
   if (c->mode == RC_PREC_MIXED) {
-    mixed_cell<NSP>(c->d, c->thermo32.data(), TH<NSP>(c), 0, c->limit, c->comb, c->visc, c->stream);
+    mixed_cell<NSP>(c->d, c->thermo32.data(), TH<NSP>(c), 0, c->limit, c->comb && c->chem == RC_CHEM_EXPLICIT,
+                    c->visc, c->stream);
     c->launches++;
   } else {
     q_cell<NSP>(c, 0, 1);
@@ -998,12 +1028,15 @@ void q_reconstruction_mode(rc_ctx* c) {
 }
 template <int NSP>
 void q_flux_mode(rc_ctx* c) {
+  q_chem_fork<NSP>(c);
   if (c->mode == RC_PREC_MIXED) {
     mixed_face_flux<NSP>(c->d, c->thermo32.data(), c->visc, c->stream);
+    q_chem_join(c);
     mixed_gather<NSP>(c->d, c->visc, c->comb, c->stream);
     c->launches += 2;
   } else {
     q_face_flux<NSP>(c);
+    q_chem_join(c);
     q_gather<NSP>(c);
   }
 }
@@ -1017,14 +1050,17 @@ void q_stage(rc_ctx* c) {
   if (c->mode == RC_PREC_FP64) {
     q_timestep_face<NSP>(c);
     q_cell<NSP>(c, 1, 1);
+    q_chem_fork<NSP>(c);
     q_face_flux<NSP>(c);
+    q_chem_join(c);
     q_sweeps<NSP>(c, 1);
     return;
   }
   mixed_ts_face<NSP>(c->d, c->thermo32.data(), c->visc, c->stream);
   c->launches++;
   if (c->mode == RC_PREC_MIXED) {
-    mixed_cell<NSP>(c->d, c->thermo32.data(), TH<NSP>(c), 1, c->limit, c->comb, c->visc, c->stream);
+    mixed_cell<NSP>(c->d, c->thermo32.data(), TH<NSP>(c), 1, c->limit, c->comb && c->chem == RC_CHEM_EXPLICIT,
+                    c->visc, c->stream);
     c->launches++;
   } else {
     q_cell<NSP>(c, 1, 1);
@@ -1353,6 +1389,9 @@ int rc_finalize(rc_ctx* c) {
     if (gx) cudaGraphExecDestroy(gx);
   for (void* p : c->allocs) cudaFree(p);
   if (c->own_stream && c->stream) cudaStreamDestroy(c->stream);
+  if (c->stream2) cudaStreamDestroy(c->stream2);
+  if (c->ev_fork) cudaEventDestroy(c->ev_fork);
+  if (c->ev_join) cudaEventDestroy(c->ev_join);
   delete c;
   return RC_OK;
 }
@@ -1458,6 +1497,51 @@ int rc_set_precision(rc_ctx* c, int precision) {
   c->graph = c->graphs[precision];
   c->graph_kernels = c->graph_kernels_of[precision];
   return RC_OK;
+}
+int rc_set_chemistry(rc_ctx* c, int mode, double tol, int max_substeps) {
+  if (!c) return RC_ERR_ARG;
+  if (mode != RC_CHEM_EXPLICIT && mode != RC_CHEM_INTEGRATED) return RC_ERR_ARG;
+  if (!(tol > 0.0) || max_substeps < 1) return RC_ERR_ARG;
+  if (mode != RC_CHEM_EXPLICIT && !c->comb) {
+    c->err = "the integrated source needs If_turn_on_combustion";
+    return RC_ERR_ARG;
+  }
+  if (mode == RC_CHEM_INTEGRATED && !c->chem_nsub) {
+    if (int st = dev_zeros(c, (size_t)c->NE, &c->chem_nsub)) return st;
+    if (int st = dev_zeros(c, (size_t)1, &c->chem_counter)) return st;
+    RC_CU(cudaStreamCreateWithFlags(&c->stream2, cudaStreamNonBlocking));
+    RC_CU(cudaEventCreateWithFlags(&c->ev_fork, cudaEventDisableTiming));
+    RC_CU(cudaEventCreateWithFlags(&c->ev_join, cudaEventDisableTiming));
+  }
+  c->chem = mode;
+  c->chem_tol = tol;
+  c->chem_maxsub = max_substeps;
+  for (int k = 0; k < 3; ++k)
+    if (c->graphs[k]) { cudaGraphExecDestroy(c->graphs[k]); c->graphs[k] = nullptr; }
+  c->graph = nullptr;
+  return RC_OK;
+}
+int rc_chem_substeps(rc_ctx* c, int* out) {
+  if (!c || !out) return RC_ERR_ARG;
+  if (!c->chem_nsub) {
+    for (int i = 0; i < c->NE; ++i) out[i] = 0;
+    return RC_OK;
+  }
+  RC_CU(cudaMemcpyAsync(out, c->chem_nsub, sizeof(int) * (size_t)c->NE, cudaMemcpyDeviceToHost, c->stream));
+  RC_CU(cudaStreamSynchronize(c->stream));
+  return latch(c);
+}
+int rc_chem_integrate(rc_ctx* c, const double* d_P, const double* d_dt, int n, double* d_out, int* d_nsub,
+                      double tol, int max_substeps) {
+  if (!c || n < 0 || (n > 0 && (!d_P || !d_dt || !d_out || !d_nsub))) return RC_ERR_ARG;
+  if (c->NSP < 2 || !(tol > 0.0) || max_substeps < 1) return RC_ERR_ARG;
+  if (n == 0) return RC_OK;
+  if (!c->chem_counter)
+    if (int st = dev_zeros(c, (size_t)1, &c->chem_counter)) return st;
+  RC_DISPATCH(c, chem_batch, c->thermo.data(), d_P, d_dt, n, d_out, d_nsub, tol, max_substeps, c->chem_counter,
+              c->d.err, c->stream);
+  c->launches++;
+  return check_launch(c, "rc_chem_integrate");
 }
 int rc_lusgs_stage(rc_ctx* c, int istep) {
   (void)istep;
