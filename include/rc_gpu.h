@@ -130,6 +130,19 @@ typedef struct rc_config {
 int rc_init(const rc_mesh* mesh, const rc_thermo* thermo, const rc_config* cfg, rc_ctx** out);
 int rc_finalize(rc_ctx* ctx);
 
+/* A batch of ncase independent cases in one context (one launch per kernel
+ * for all of them): meshes[k], thermos[k], cfgs[k] describe case k as rc_init
+ * takes them.  Gas data and solver flags must agree; inlets and p_out may
+ * differ.  The cases are renumbered into one mesh, case k's cells following
+ * those of cases 0..k-1; states (rc_set_state/rc_get_state, rc_get_array) use
+ * that numbering, i.e. the cases' Fortran arrays concatenated.  Each case runs
+ * the recurrences it runs alone (the LU-SGS levels never mix cases), so its
+ * results are bit-identical to a single-case context.  No counterpart in the
+ * reference (one case per run). */
+int rc_init_batch(int ncase, const rc_mesh* meshes, const rc_thermo* thermos, const rc_config* cfgs, rc_ctx** out);
+/* Number of cases and the ncase+1 cell offsets of the numbering. */
+int rc_batch_info(rc_ctx* ctx, int* ncase, int* cell_offsets);
+
 /* PA(NVar,NE), WA(NVar,NE) in the Fortran layout (module.f90:54). */
 int rc_set_state(rc_ctx* ctx, const double* PA, const double* WA);
 int rc_get_state(rc_ctx* ctx, double* PA, double* WA);
@@ -169,6 +182,9 @@ int rc_chem_integrate(rc_ctx* ctx, const double* d_P, const double* d_dt, int n,
 /* Residual + step_residual norms (residual.f90:4-21, 61-79): res(k) =
  * sum(vol*|hWA(k,:)|)/total_volume, romax = max(WA(1,:)).  Synchronises. */
 int rc_residual(rc_ctx* ctx, double* res, double* romax);
+/* The same norms per case of a batch: res(NVar, ncase), romax(ncase).  A case
+ * gets the bits it gets alone.  Synchronises. */
+int rc_residual_batch(rc_ctx* ctx, double* res, double* romax);
 
 /* Wait for queued work; returns the latched device error bits. */
 int rc_sync(rc_ctx* ctx);

@@ -97,6 +97,10 @@ SIGNATURES = {
     "rc_residual_noalloc": (_i, [_vp, _vp, _vp, _i, _i, _d, _vp, _DP, _DP]),
     "rc_set_precision": (_i, [_vp, _i]),
     "rc_set_chemistry": (_i, [_vp, _i, _d, _i]),
+    "rc_init_batch": (_i, [_i, ctypes.POINTER(RcMesh), ctypes.POINTER(RcThermo), ctypes.POINTER(RcConfig),
+                           ctypes.POINTER(_vp)]),
+    "rc_batch_info": (_i, [_vp, _IP, _IP]),
+    "rc_residual_batch": (_i, [_vp, _DP, _DP]),
     "rc_chem_substeps": (_i, [_vp, _IP]),
     "rc_chem_integrate": (_i, [_vp, _vp, _vp, _i, _vp, _vp, _d, _i]),
 }
@@ -336,3 +340,49 @@ class Solver:
             self.close()
         except Exception:
             pass
+
+
+class BatchSolver(Solver):
+    """Several independent cases in one context: every kernel launch of an
+    iteration covers all of them.  States are the cases' arrays concatenated
+    (case k's cells after those of cases 0..k-1)."""
+
+    def __init__(self, cases, precision: int = RC_PREC_FP64, device: int = 0, stream: Optional[int] = None):
+        L = load()
+        self.cases = list(cases)
+        n = len(self.cases)
+        views = [c.views(precision, device) for c in self.cases]
+        ms = (RcMesh * n)(*[v[0] for v in views])
+        ts = (RcThermo * n)(*[v[1] for v in views])
+        gs = (RcConfig * n)(*[v[2] for v in views])
+        self._keep = (views, ms, ts, gs)
+        h = _vp()
+        st = L.rc_init_batch(n, ms, ts, gs, ctypes.byref(h))
+        if st:
+            raise RcError(st, "rc_init_batch")
+        self._h = h
+        self.case = self.cases[0]
+        self.precision = int(precision)
+        self.ncase = n
+        self.NE = sum(c.NE for c in self.cases)
+        self.NF = sum(c.NF for c in self.cases)
+        self.Nghost = sum(c.Nghost for c in self.cases)
+        self.NVar = self.cases[0].NVar
+        off = np.zeros(n + 1, dtype=np.int32)
+        nc = _i()
+        L.rc_batch_info(h, ctypes.byref(nc), off.ctypes.data_as(_IP))
+        self.offsets = off
+        if stream is not None:
+            self._check(L.rc_set_stream(h, _vp(stream)))
+        self.set_state(np.concatenate([c.array("PA") for c in self.cases]),
+                       np.concatenate([c.array("WA") for c in self.cases]))
+
+    def residual(self):
+        """Per-case norms: (ncase, NVar) and romax (ncase,)."""
+        r = np.zeros((self.ncase, self.NVar))
+        m = np.zeros(self.ncase)
+        self._check(load().rc_residual_batch(self._h, _dp(r), _dp(m)))
+        return r, m
+
+    def case_slice(self, k: int) -> slice:
+        return slice(int(self.offsets[k]), int(self.offsets[k + 1]))

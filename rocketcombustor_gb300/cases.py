@@ -43,7 +43,7 @@ X_CHAMBER, X_THROAT, X_EXIT = 0.10, 0.15, 0.25
 H_CHAMBER, H_THROAT, H_EXIT = 0.04, 0.01, 0.03
 
 
-def half_height(x: np.ndarray) -> np.ndarray:
+def half_height(x: np.ndarray, h_exit: float = H_EXIT, x_exit: float = X_EXIT) -> np.ndarray:
     """Nozzle wall y = h(x): flat chamber, cosine contraction and expansion."""
     x = np.asarray(x, dtype=np.float64)
     h = np.full_like(x, H_CHAMBER)
@@ -51,8 +51,8 @@ def half_height(x: np.ndarray) -> np.ndarray:
     t = (x[c] - X_CHAMBER) / (X_THROAT - X_CHAMBER)
     h[c] = H_THROAT + 0.5 * (H_CHAMBER - H_THROAT) * (1.0 + np.cos(np.pi * t))
     e = x > X_THROAT
-    t = (x[e] - X_THROAT) / (X_EXIT - X_THROAT)
-    h[e] = H_THROAT + 0.5 * (H_EXIT - H_THROAT) * (1.0 - np.cos(np.pi * t))
+    t = (x[e] - X_THROAT) / (x_exit - X_THROAT)
+    h[e] = H_THROAT + 0.5 * (h_exit - H_THROAT) * (1.0 - np.cos(np.pi * t))
     return h
 
 
@@ -122,15 +122,15 @@ def _color_order(cells: np.ndarray, nnt: int) -> np.ndarray:
 
 
 def nozzle_mesh(nx: int, ny: int, seed: int, order: str = "natural", wall_type: int = 6,
-                jitter: float = 0.10) -> Mesh:
+                jitter: float = 0.10, h_exit: float = H_EXIT, x_exit: float = X_EXIT) -> Mesh:
     """Seeded triangulated nozzle: (nx*ny*2) triangles, ordering per `order`."""
     rng = np.random.default_rng(seed)
-    xs = np.linspace(0.0, X_EXIT, nx + 1)
-    hx = half_height(xs)
+    xs = np.linspace(0.0, x_exit, nx + 1)
+    hx = half_height(xs, h_exit, x_exit)
     jj = np.arange(ny + 1) / ny
     X = np.repeat(xs[:, None], ny + 1, axis=1)
     Y = hx[:, None] * jj[None, :]
-    dxl = X_EXIT / nx
+    dxl = x_exit / nx
     dyl = hx[:, None] / ny * np.ones((1, ny + 1))
     jx = rng.uniform(-jitter, jitter, size=X.shape) * dxl
     jy = rng.uniform(-jitter, jitter, size=X.shape) * dyl
@@ -341,6 +341,9 @@ class CaseConfig:
     p_out_factor: float = 1.0  # exit pressure as a multiple of the isentropic design exit pressure
     jitter: float = 0.10       # interior node jitter, fraction of the local spacing
     init: str = "uniform"      # initial field: "uniform" inlet state or "isentropic" quasi-1D nozzle flow
+    h_exit: float = H_EXIT     # exit half-height (area ratio h_exit / 0.01)
+    wall: int = 0              # wall BC code: 0 = no-slip (1) when viscous, else slip (6)
+    x_exit: float = X_EXIT     # exit station (divergent length x_exit - 0.15)
 
     @property
     def n_cells(self) -> int:
@@ -390,8 +393,8 @@ def inlet_state(cfg: CaseConfig, R: float, gamma: float):
     return p, T, u, rho * u
 
 
-def exit_pressure_ratio(gamma: float) -> float:
-    M = area_ratio_mach(H_EXIT / H_THROAT, gamma, supersonic=True)
+def exit_pressure_ratio(gamma: float, h_exit: float = H_EXIT) -> float:
+    M = area_ratio_mach(h_exit / H_THROAT, gamma, supersonic=True)
     return (1.0 + 0.5 * (gamma - 1.0) * M * M) ** (-gamma / (gamma - 1.0))
 
 
@@ -400,10 +403,11 @@ def write_case(d: str, cfg: CaseConfig, mesh: Optional[Mesh] = None) -> Mesh:
     os.makedirs(os.path.join(d, "combustion"), exist_ok=True)
     os.makedirs(os.path.join(d, "flow"), exist_ok=True)
     if mesh is None:
-        mesh = nozzle_mesh(cfg.nx, cfg.ny, cfg.seed, cfg.order, wall_type=1 if cfg.viscous else 6,
-                           jitter=cfg.jitter)
+        wall = cfg.wall or (1 if cfg.viscous else 6)
+        mesh = nozzle_mesh(cfg.nx, cfg.ny, cfg.seed, cfg.order, wall_type=wall, jitter=cfg.jitter,
+                           h_exit=cfg.h_exit, x_exit=cfg.x_exit)
     if cfg.closed:
-        wall = 1 if cfg.viscous else 6
+        wall = cfg.wall or (1 if cfg.viscous else 6)
         mesh.boundaries = [(wall, pairs) for _, pairs in mesh.boundaries]
     write_grid(os.path.join(d, "grid1.in"), mesh)
     if cfg.nsp == 1:
@@ -444,7 +448,7 @@ def write_case(d: str, cfg: CaseConfig, mesh: Optional[Mesh] = None) -> Mesh:
     write_inlet(os.path.join(d, "combustion", "oxidizer.in"), Yin, T_in, cfg.p0,
                 mflux * 2.0 * H_CHAMBER, "oxidizer")
     write_inlet(os.path.join(d, "combustion", "fuel.in"), Yin, T_in, cfg.p0, 0.37, "fuel")
-    pr = exit_pressure_ratio(gamma) * cfg.p_out_factor
+    pr = exit_pressure_ratio(gamma, cfg.h_exit) * cfg.p_out_factor
     write_flow_info(d, cfg.combustion, cfg.viscous, cfg.cfl, cfg.nstep, cfg.limit_id, pr)
     # initial field: uniform inlet (chamber) state, or the quasi-1D isentropic
     # nozzle flow (subsonic up to the throat, supersonic after it) with the
@@ -455,9 +459,9 @@ def write_case(d: str, cfg: CaseConfig, mesh: Optional[Mesh] = None) -> Mesh:
     if cfg.init == "isentropic" and not cfg.closed:
         cxy = mesh.coor[mesh.cells - 1].mean(axis=1)
         x, y = cxy[:, 0], cxy[:, 1]
-        h = half_height(x)
+        h = half_height(x, cfg.h_exit, cfg.x_exit)
         eps = 1e-6
-        dh = (half_height(x + eps) - half_height(x - eps)) / (2 * eps)
+        dh = (half_height(x + eps, cfg.h_exit, cfg.x_exit) - half_height(x - eps, cfg.h_exit, cfg.x_exit)) / (2 * eps)
         M = area_ratio_mach(np.maximum(h / H_THROAT, 1.0 + 1e-9), gamma, supersonic=(x > X_THROAT))
         T = cfg.T0 / (1.0 + 0.5 * (gamma - 1.0) * M * M)
         p = cfg.p0 * (T / cfg.T0) ** (gamma / (gamma - 1.0))
@@ -487,3 +491,36 @@ def make_case(d: str, name: str, **over) -> CaseConfig:
     cfg = CaseConfig(**{**asdict(PRESETS[name]), **over})
     write_case(d, cfg)
     return cfg
+
+
+def batch_configs(n: int = 64, seed: int = 5, ne_min: int = 2000, ne_max: int = 60000,
+                  **over) -> List[CaseConfig]:
+    """n independent reacting viscous nozzle cases of uneven size (the batched
+    workload): cells log-uniform in [ne_min, ne_max] (nx = 6 ny), chamber
+    pressure uniform in 1-10 MPa, O/F uniform in 4-8 and area ratio uniform in
+    4-25 through the exit half-height, with the divergent section lengthened
+    in proportion so that the wall keeps the base nozzle's steepest slope; the
+    physics of preset c2 otherwise."""
+    rng = np.random.default_rng(seed)
+    base = asdict(PRESETS["c2"])
+    out = []
+    for c in range(n):
+        ne = math.exp(rng.uniform(math.log(ne_min), math.log(ne_max)))
+        ny = max(4, int(round(math.sqrt(ne / 12.0))))
+        cfg = {**base, "name": f"b{c:02d}", "nx": 6 * ny, "ny": ny, "seed": seed * 1000 + c,
+               "p0": float(rng.uniform(1.0e6, 1.0e7)), "of_ratio": float(rng.uniform(4.0, 8.0)),
+               "h_exit": float(rng.uniform(4.0, 25.0)) * H_THROAT, "perturb_seed": seed * 1000 + 500 + c}
+        cfg["x_exit"] = X_THROAT + (X_EXIT - X_THROAT) * (cfg["h_exit"] - H_THROAT) / (H_EXIT - H_THROAT)
+        cfg.update(over)
+        out.append(CaseConfig(**cfg))
+    return out
+
+
+def make_batch(d: str, n: int = 64, seed: int = 5, **over) -> List[str]:
+    """Write the batch of `batch_configs` as d/bNN case directories."""
+    dirs = []
+    for cfg in batch_configs(n, seed, **over):
+        cd = os.path.join(d, cfg.name)
+        write_case(cd, cfg)
+        dirs.append(cd)
+    return dirs

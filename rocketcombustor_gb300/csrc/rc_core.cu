@@ -36,17 +36,18 @@
 namespace rc {
 
 // oxidizer_inlet_bc / fuel_inlet_bc (oxidizer.f90:367-382, fuel.f90:437-452)
+// with the inlet data of row bc of the case table (w = 0 oxidizer, 1 fuel).
 template <int NSP>
-__device__ __forceinline__ void inlet_bc(const ThermoDev<NSP>& th, int w, double pl, double& pr, double& ur,
-                                         double& vr, double& tr, double& rr, double* Yr, double& Cpr,
+__device__ __forceinline__ void inlet_bc(const ThermoDev<NSP>& th, const double* bc, int w, double pl, double& pr,
+                                         double& ur, double& vr, double& tr, double& rr, double* Yr, double& Cpr,
                                          double& gamar, double& Rcpcvr, unsigned& err) {
 #pragma unroll
-  for (int k = 0; k < NSP; ++k) Yr[k] = th.inY[w][k];
-  tr = th.inT[w];
+  for (int k = 0; k < NSP; ++k) Yr[k] = bc[BC_Y + w * BC_NSPMAX + k];
+  tr = bc[BC_T + w];
   gas<NSP>(th, Yr, tr, Cpr, gamar, Rcpcvr, err);
   pr = pl;
   rr = pr / (Rcpcvr * tr);
-  ur = th.inMflow[w] / rr;
+  ur = bc[BC_MFLOW + w] / rr;
   vr = 0.0;
 }
 
@@ -181,12 +182,13 @@ __global__ void __launch_bounds__(128) k_cell(const Dev d, const ThermoDev<NSP> 
       case 3:
       case 4: {
         double rrb, Cpb, gab, Rb;
-        inlet_bc<NSP>(th, d.gtype[gj] == 3 ? 0 : 1, pl, pr, ur, vr, tr, rrb, Yr, Cpb, gab, Rb, err);
+        inlet_bc<NSP>(th, bc_row(d, d.gcase, gj), d.gtype[gj] == 3 ? 0 : 1, pl, pr, ur, vr, tr, rrb, Yr, Cpb, gab,
+                      Rb, err);
         break;
       }
       case 5:
         vn = ul * s1n + vl * s2n;
-        if (!(fabs(vn) > ac)) pr = th.p_out;
+        if (!(fabs(vn) > ac)) pr = bc_row(d, d.gcase, gj)[BC_POUT];
         break;
       default: err |= ERR_BCTYPE;
     }
@@ -293,7 +295,7 @@ __global__ void __launch_bounds__(128) k_face_flux(const Dev d, const ThermoDev<
 #pragma unroll
       for (int k = 0; k < NSP; ++k) Yr[k] = Yr0[k];
     } else if (NR == -3 || NR == -4) {
-      inlet_bc<NSP>(th, NR == -3 ? 0 : 1, pl, pr, ur, vr, tr, rr, Yr, Cpr, gamar, Rcr, err);
+      inlet_bc<NSP>(th, bc_row(d, d.fcase, f), NR == -3 ? 0 : 1, pl, pr, ur, vr, tr, rr, Yr, Cpr, gamar, Rcr, err);
       pl = pr; ul = ur; vl = vr; tl = tr; rl = rr;
 #pragma unroll
       for (int k = 0; k < NSP; ++k) Yl[k] = Yr[k];
@@ -309,7 +311,7 @@ __global__ void __launch_bounds__(128) k_face_flux(const Dev d, const ThermoDev<
         const double ac = sqrt(gamal * pl / rl);
         vn = ul * sav1n + vl * sav2n;
         if (!(fabs(vn) > ac)) {
-          pr = th.p_out;
+          pr = bc_row(d, d.fcase, f)[BC_POUT];
           ur = ul + sav1n * (pl - pr) / (rl * ac);
           vr = vl + sav2n * (pl - pr) / (rl * ac);
           rr = rl + (pr - pl) / (ac * ac);
@@ -364,7 +366,7 @@ __global__ void __launch_bounds__(128) k_face_flux(const Dev d, const ThermoDev<
       for (int k = 0; k < NSP; ++k) Yr[k] = Yr0[k];
     } else if (NR == -3 || NR == -4) {
       double rr, Cpr, gamar, Rcr;
-      inlet_bc<NSP>(th, NR == -3 ? 0 : 1, pl, pr, ur, vr, tr, rr, Yr, Cpr, gamar, Rcr, err);
+      inlet_bc<NSP>(th, bc_row(d, d.fcase, f), NR == -3 ? 0 : 1, pl, pr, ur, vr, tr, rr, Yr, Cpr, gamar, Rcr, err);
       pl = pr; ul = ur; vl = vr; tl = tr; rl = rr;
 #pragma unroll
       for (int k = 0; k < NSP; ++k) Yl[k] = Yr[k];
@@ -376,7 +378,7 @@ __global__ void __launch_bounds__(128) k_face_flux(const Dev d, const ThermoDev<
         const double ac = sqrt(gamal0 * pl / rl);
         const double vn = ul * sav1n + vl * sav2n;
         if (!(fabs(vn) > ac)) {
-          pr = th.p_out;
+          pr = bc_row(d, d.fcase, f)[BC_POUT];
           ur = ul + sav1n * (pl - pr) / (rl * ac);
           vr = vl + sav2n * (pl - pr) / (rl * ac);
           const double rrb = rl + (pr - pl) / (ac * ac);
@@ -716,17 +718,24 @@ __global__ void __launch_bounds__(PERS_THREADS) k_lusgs_persistent(const Dev d, 
 // Residual norms: fixed-shape deterministic reduction (block partials then one
 // block over the partials).  out[k] = sum vol*|hWA_k|, out[V] = max WA_1.
 constexpr int NRM_BLOCKS = 304, NRM_THREADS = 256;
+// Case blockIdx.y covers cells [coff[y], coff[y+1]) (coff null: [0, NE)); the
+// arrays have plane stride NE.  The order of the sums depends only on the
+// case's own cells, so a case gives the same norms alone and in a batch.
 __global__ void __launch_bounds__(NRM_THREADS) k_norm_partial(const double* __restrict__ hWA,
                                                               const double* __restrict__ WA,
                                                               const double* __restrict__ vol, int NE, int V,
-                                                              double* part) {
+                                                              const int* __restrict__ coff, double* part) {
   __shared__ double sh[NRM_THREADS];
-  const int per = (NE + NRM_BLOCKS - 1) / NRM_BLOCKS;
-  const int lo = blockIdx.x * per, hi = min(NE, lo + per);
+  const int c0 = coff ? coff[blockIdx.y] : 0, n = coff ? coff[blockIdx.y + 1] - c0 : NE;
+  part += (size_t)blockIdx.y * (V + 1) * NRM_BLOCKS;
+  const int per = (n + NRM_BLOCKS - 1) / NRM_BLOCKS;
+  const int lo = blockIdx.x * per, hi = min(n, lo + per);
   for (int k = 0; k <= V; ++k) {
     double a = (k == V) ? 0.0 : 0.0;
-    for (int i = lo + threadIdx.x; i < hi; i += NRM_THREADS)
+    for (int ii = lo + threadIdx.x; ii < hi; ii += NRM_THREADS) {
+      const int i = c0 + ii;
       a = (k == V) ? fmax2(a, WA[i]) : a + vol[i] * fabs(hWA[k * NE + i]);
+    }
     sh[threadIdx.x] = a;
     __syncthreads();
     for (int w = NRM_THREADS / 2; w > 0; w >>= 1) {
@@ -738,12 +747,14 @@ __global__ void __launch_bounds__(NRM_THREADS) k_norm_partial(const double* __re
     __syncthreads();
   }
 }
-__global__ void k_norm_final(const double* part, int V, double total_volume, double* out) {
+__global__ void k_norm_final(const double* part, int V, const double* __restrict__ total_volume, double* out) {
   const int k = threadIdx.x;
   if (k > V) return;
+  part += (size_t)blockIdx.x * (V + 1) * NRM_BLOCKS;
+  out += (size_t)blockIdx.x * (V + 1);
   double a = 0.0;
   for (int b = 0; b < NRM_BLOCKS; ++b) a = (k == V) ? fmax2(a, part[k * NRM_BLOCKS + b]) : a + part[k * NRM_BLOCKS + b];
-  out[k] = (k == V) ? a : a / total_volume;
+  out[k] = (k == V) ? a : a / total_volume[blockIdx.x];
 }
 
 // Fortran (V,N) <-> device (V planes of N)
@@ -802,6 +813,12 @@ struct rc_ctx {
   unsigned* bar_count = nullptr; // grid-barrier counter of the persistent launch
   int* fwd_off_dev = nullptr;
   int* bwd_off_dev = nullptr;
+  // batch of independent cases sharing the numbering (ncase == 1: one case)
+  int ncase = 1;
+  std::vector<int> case_off;         // [ncase+1] cell offsets
+  std::vector<double> case_vol;      // [ncase] total_volume of each case
+  int* case_off_dev = nullptr;
+  double* case_vol_dev = nullptr;
   // chemistry source mode (RC_CHEM_*) and the integrator's work arrays
   int chem = RC_CHEM_EXPLICIT;
   double chem_tol = 0.05;
@@ -894,10 +911,7 @@ void fill_thermo(const rc_thermo* t, const rc_config* g, ThermoDev<NSP>& th) {
     th.prodc[k] = 1000 * t->mole_weight[k] * (t->coef_r_react[k] - t->coef_f_react[k]);
   th.mw1000[0] = t->mole_weight[0] * 1000;
   th.mw1000[1] = t->mole_weight[NSP > 1 ? 1 : 0] * 1000;
-  for (int k = 0; k < NSP; ++k) { th.inY[0][k] = t->oxidizer_mass_fraction[k]; th.inY[1][k] = t->fuel_mass_fraction[k]; }
-  th.inT[0] = t->oxidizer_temp_in; th.inMflow[0] = t->oxidizer_mass_flow;
-  th.inT[1] = t->fuel_temp_in; th.inMflow[1] = t->fuel_mass_flow;
-  th.p_out = g->p_out; th.cfl = g->cfl;
+  th.cfl = g->cfl;
 }
 
 inline unsigned blocks(long n, int t) { return (unsigned)((n + t - 1) / t); }
@@ -1097,8 +1111,140 @@ int latch(rc_ctx* c) {
 // ================================================================ C ABI =====
 extern "C" {
 
-int rc_init(const rc_mesh* m, const rc_thermo* t, const rc_config* g, rc_ctx** out) {
-  if (!m || !t || !g || !out) return RC_ERR_ARG;
+}  // extern "C"
+
+namespace {
+
+// Boundary data and case layout of a context: one row of bctab per case (the
+// BC_* offsets of rc_dev.cuh); fcase / gcase / case_off only for batches.
+struct BatchDesc {
+  std::vector<double> bctab;
+  std::vector<int> fcase, gcase, case_off;
+  std::vector<double> case_vol;
+  int ncase() const { return (int)case_vol.size(); }
+};
+
+void bc_row_of(const rc_thermo* t, const rc_config* g, std::vector<double>& tab) {
+  const size_t r = tab.size();
+  tab.resize(r + BCS, 0.0);
+  for (int k = 0; k < t->Nsp && k < BC_NSPMAX; ++k) {
+    tab[r + BC_Y + k] = t->oxidizer_mass_fraction[k];
+    tab[r + BC_Y + BC_NSPMAX + k] = t->fuel_mass_fraction[k];
+  }
+  tab[r + BC_T] = t->oxidizer_temp_in;
+  tab[r + BC_T + 1] = t->fuel_temp_in;
+  tab[r + BC_MFLOW] = t->oxidizer_mass_flow;
+  tab[r + BC_MFLOW + 1] = t->fuel_mass_flow;
+  tab[r + BC_POUT] = g->p_out;
+}
+
+// The module arrays of several cases renumbered into one mesh: cells, faces,
+// nodes and ghosts of case c follow those of cases 0..c-1; every 1-based id is
+// shifted by its case's offset, boundary codes (negative) are kept.
+struct MergedMesh {
+  rc_mesh m{};
+  std::vector<int> KFace, Neighbor, FNode, FProperty, NeighF, Neigh, NeighC, Ghostcell, Num_ghostcell, Hostcell,
+      BCtype;
+  std::vector<double> COOR, VECX, SideOfs, VOL, CELLXY, reflen, wdis, AMLS, CoorG;
+};
+
+std::string merge_meshes(int n, const rc_mesh* ms, MergedMesh& o, BatchDesc& b) {
+  const int M = ms[0].MaxNei;
+  long long NE = 0, NF = 0, NNT = 0, NG = 0;
+  for (int c = 0; c < n; ++c) {
+    if (ms[c].MaxNei != M) return "MaxNei differs between cases";
+    NE += ms[c].NE; NF += ms[c].NF; NNT += ms[c].NNT; NG += ms[c].Nghostcell;
+  }
+  if (NE > (1LL << 30) || NF > (1LL << 30) || NNT > (1LL << 30) || NG > (1LL << 30)) return "batch too large";
+  auto sh = [](int v, int off) { return v > 0 ? v + off : v; };
+  int oc = 0, of = 0, on = 0, og = 0;
+  b.case_off.assign(1, 0);
+  double vt = 0.0;
+  for (int c = 0; c < n; ++c) {
+    const rc_mesh& m = ms[c];
+    for (int i = 0; i < m.NE; ++i) {
+      o.KFace.push_back(m.KFace[i]);
+      o.Neigh.push_back(m.Neigh[i]);
+      o.Num_ghostcell.push_back(m.Num_ghostcell[i]);
+      for (int q = 0; q < 4; ++q) o.NeighF.push_back(sh(m.NeighF[4 * (size_t)i + q], of));
+      for (int q = 0; q <= M; ++q) o.NeighC.push_back(sh(m.NeighC[(size_t)(M + 1) * i + q], oc));
+      for (int q = 0; q < M; ++q) o.Ghostcell.push_back(sh(m.Ghostcell[(size_t)M * i + q], og));
+      o.VOL.push_back(m.VOL[i]);
+      for (int r = 0; r < 2; ++r) {
+        o.CELLXY.push_back(m.CELLXY[2 * (size_t)i + r]);
+        o.reflen.push_back(m.reflen[2 * (size_t)i + r]);
+      }
+      for (int q = 0; q < M; ++q) o.wdis.push_back(m.wdis[(size_t)M * i + q]);
+      for (int q = 0; q < 2 * M; ++q) o.AMLS.push_back(m.AMLS[(size_t)2 * M * i + q]);
+    }
+    for (int f = 0; f < m.NF; ++f) {
+      o.Neighbor.push_back(sh(m.Neighbor[2 * (size_t)f], oc));
+      o.Neighbor.push_back(sh(m.Neighbor[2 * (size_t)f + 1], oc));
+      o.FNode.push_back(sh(m.FNode[2 * (size_t)f], on));
+      o.FNode.push_back(sh(m.FNode[2 * (size_t)f + 1], on));
+      o.FProperty.push_back(m.FProperty[f]);
+      for (int r = 0; r < 2; ++r) {
+        o.VECX.push_back(m.VECX[2 * (size_t)f + r]);
+        o.SideOfs.push_back(m.SideOfs[2 * (size_t)f + r]);
+      }
+      b.fcase.push_back(c);
+    }
+    for (int k = 0; k < 2 * m.NNT; ++k) o.COOR.push_back(m.COOR[k]);
+    for (int j = 0; j < m.Nghostcell; ++j) {
+      o.Hostcell.push_back(sh(m.Hostcell[j], oc));
+      o.BCtype.push_back(m.BCtype_Ghostcell[j]);
+      for (int k = 0; k < 8; ++k) o.CoorG.push_back(m.Coor_Ghostnode[8 * (size_t)j + k]);
+      b.gcase.push_back(c);
+    }
+    oc += m.NE; of += m.NF; on += m.NNT; og += m.Nghostcell;
+    b.case_off.push_back(oc);
+    b.case_vol.push_back(m.total_volume);
+    vt = vt + m.total_volume;
+  }
+  rc_mesh& r = o.m;
+  r.NE = oc; r.NF = of; r.NNT = on; r.MaxNei = M; r.Nghostcell = og;
+  r.KFace = o.KFace.data(); r.Neighbor = o.Neighbor.data(); r.FNode = o.FNode.data();
+  r.FProperty = o.FProperty.data(); r.NeighF = o.NeighF.data(); r.Neigh = o.Neigh.data();
+  r.NeighC = o.NeighC.data(); r.Ghostcell = o.Ghostcell.data(); r.Num_ghostcell = o.Num_ghostcell.data();
+  r.Hostcell = o.Hostcell.data(); r.BCtype_Ghostcell = o.BCtype.data(); r.COOR = o.COOR.data();
+  r.VECX = o.VECX.data(); r.SideOfs = o.SideOfs.data(); r.VOL = o.VOL.data(); r.CELLXY = o.CELLXY.data();
+  r.reflen = o.reflen.data(); r.wdis = o.wdis.data(); r.AMLS = o.AMLS.data(); r.Coor_Ghostnode = o.CoorG.data();
+  r.total_volume = vt;
+  return "";
+}
+
+// Species, thermo, transport, diffusion and kinetics data must agree between
+// the cases of a batch (one ThermoDev); inlets and exit pressure may differ.
+std::string same_gas(const rc_thermo* a, const rc_thermo* b, const rc_config* ga, const rc_config* gb) {
+  if (a->Nsp != b->Nsp || a->order_of_cp_polynomial != b->order_of_cp_polynomial) return "species differ";
+  const int n = a->Nsp, P = a->order_of_cp_polynomial;
+  auto eq = [](const double* x, const double* y, int k) {
+    for (int i = 0; i < k; ++i)
+      if (!(x[i] == y[i])) return false;
+    return true;
+  };
+  bool ok = a->Rconstant == b->Rconstant && eq(a->mole_weight, b->mole_weight, n) &&
+            eq(a->R_species, b->R_species, n) && a->thermo_lowest_tem == b->thermo_lowest_tem &&
+            a->thermo_critical_tem == b->thermo_critical_tem && a->thermo_highest_tem == b->thermo_highest_tem &&
+            eq(a->low_coef_Cp_species, b->low_coef_Cp_species, n * P) &&
+            eq(a->high_coef_Cp_species, b->high_coef_Cp_species, n * P) &&
+            eq(a->low_enthalpy_b1, b->low_enthalpy_b1, n) && eq(a->high_enthalpy_b1, b->high_enthalpy_b1, n) &&
+            a->transport_lowest_tem == b->transport_lowest_tem &&
+            a->transport_critical_tem == b->transport_critical_tem &&
+            a->transport_highest_tem == b->transport_highest_tem &&
+            eq(a->collision_diameter, b->collision_diameter, n) && eq(a->LJ_energy, b->LJ_energy, n) &&
+            a->code_chemical_model == b->code_chemical_model && eq(a->coef_f_react, b->coef_f_react, n) &&
+            eq(a->coef_r_react, b->coef_r_react, n) && a->Af_react == b->Af_react && a->E_react == b->E_react;
+  for (int k = 0; k < 16 && ok; ++k) ok = eq(a->mu_K[k], b->mu_K[k], n);
+  if (!ok) return "gas data differ between cases";
+  if (ga->IfViscous != gb->IfViscous || ga->If_turn_on_combustion != gb->If_turn_on_combustion ||
+      ga->limit_ID != gb->limit_ID || ga->cfl != gb->cfl || ga->precision != gb->precision ||
+      ga->device != gb->device)
+    return "solver flags differ between cases (only p_out may)";
+  return "";
+}
+
+int init_impl(const rc_mesh* m, const rc_thermo* t, const rc_config* g, const BatchDesc& b, rc_ctx** out) {
   *out = nullptr;
   rc_ctx* c = new rc_ctx();
   auto bail = [&](int code, const std::string& msg) {
@@ -1109,6 +1255,7 @@ int rc_init(const rc_mesh* m, const rc_thermo* t, const rc_config* g, rc_ctx** o
   c->NE = m->NE; c->NF = m->NF; c->NG = m->Nghostcell; c->NSP = t->Nsp; c->V = 3 + t->Nsp;
   c->visc = g->IfViscous != 0; c->comb = g->If_turn_on_combustion != 0; c->limit = g->limit_ID;
   c->precision = g->precision; c->device = g->device; c->total_volume = m->total_volume;
+  if ((int)b.bctab.size() != BCS * b.ncase() || b.ncase() < 1) return bail(RC_ERR_ARG, "bad case table");
   if (c->NSP != 1 && c->NSP != 4) return bail(RC_ERR_ARG, "Nsp must be 1 or 4 in this build");
   if (c->comb && c->NSP < 2) return bail(RC_ERR_ARG, "combustion needs at least two species");
   if (t->order_of_cp_polynomial != 7) return bail(RC_ERR_ARG, "order_of_cp_polynomial must be 7");
@@ -1314,8 +1461,8 @@ int rc_init(const rc_mesh* m, const rc_thermo* t, const rc_config* g, rc_ctx** o
   st |= dev_zeros(c, (size_t)NF, &d.alpaF);
   st |= dev_zeros(c, (size_t)V * NF, &d.Finv);
   st |= dev_zeros(c, (size_t)(V - 1) * NF, &d.Fvis);
-  st |= dev_zeros(c, (size_t)(V + 1) * NRM_BLOCKS, &c->norm_part);
-  st |= dev_zeros(c, (size_t)(V + 1), &c->norm_out);
+  st |= dev_zeros(c, (size_t)b.ncase() * (V + 1) * NRM_BLOCKS, &c->norm_part);
+  st |= dev_zeros(c, (size_t)b.ncase() * (V + 1), &c->norm_out);
   st |= dev_zeros(c, (size_t)2 * V * std::max(std::max(NE, NF), NG), &c->staging);
   if (g->precision != RC_PREC_FP64) {  // FP32 work arrays of the mixed modes
     double* f32;
@@ -1360,6 +1507,21 @@ int rc_init(const rc_mesh* m, const rc_thermo* t, const rc_config* g, rc_ctx** o
       st |= dev_upload(c, tf, &p); d.swf[dir] = p;
     }
   }
+  {  // boundary data per case, case layout
+    std::vector<float> tab32(b.bctab.begin(), b.bctab.end());
+    double* tp;
+    float* tp32;
+    st |= dev_upload(c, b.bctab, &tp); d.bctab = tp;
+    st |= dev_upload(c, tab32, &tp32); d.bctab32 = tp32;
+    c->ncase = b.ncase();
+    c->case_off = b.case_off;
+    c->case_vol = b.case_vol;
+    st |= dev_upload(c, c->case_off, &c->case_off_dev);
+    st |= dev_upload(c, c->case_vol, &c->case_vol_dev);
+    int* ip;
+    if (!b.fcase.empty()) { st |= dev_upload(c, b.fcase, &ip); d.fcase = ip; }
+    if (!b.gcase.empty()) { st |= dev_upload(c, b.gcase, &ip); d.gcase = ip; }
+  }
   if (st) return bail(st, c->err);
   // LU-SGS schedule: one cooperative launch per iteration when every SM can
   // hold a block of the persistent kernels; RC_LUSGS_SCHEDULE=levels selects
@@ -1381,6 +1543,41 @@ int rc_init(const rc_mesh* m, const rc_thermo* t, const rc_config* g, rc_ctx** o
   }
   *out = c;
   return RC_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int rc_init(const rc_mesh* m, const rc_thermo* t, const rc_config* g, rc_ctx** out) {
+  if (!m || !t || !g || !out) return RC_ERR_ARG;
+  BatchDesc b;
+  bc_row_of(t, g, b.bctab);
+  b.case_off = {0, m->NE};
+  b.case_vol = {m->total_volume};
+  return init_impl(m, t, g, b, out);
+}
+
+int rc_init_batch(int ncase, const rc_mesh* meshes, const rc_thermo* thermos, const rc_config* cfgs, rc_ctx** out) {
+  if (ncase < 1 || !meshes || !thermos || !cfgs || !out) return RC_ERR_ARG;
+  *out = nullptr;
+  for (int k = 1; k < ncase; ++k) {
+    const std::string e = same_gas(&thermos[0], &thermos[k], &cfgs[0], &cfgs[k]);
+    if (!e.empty()) {
+      std::fprintf(stderr, "rc_init_batch: case %d: %s\n", k, e.c_str());
+      return RC_ERR_ARG;
+    }
+  }
+  MergedMesh mm;
+  BatchDesc b;
+  const std::string e = merge_meshes(ncase, meshes, mm, b);
+  if (!e.empty()) {
+    std::fprintf(stderr, "rc_init_batch: %s\n", e.c_str());
+    return RC_ERR_ARG;
+  }
+  for (int k = 0; k < ncase; ++k) bc_row_of(&thermos[k], &cfgs[k], b.bctab);
+  if (ncase == 1) { b.fcase.clear(); b.gcase.clear(); }
+  return init_impl(&mm.m, &thermos[0], &cfgs[0], b, out);
 }
 
 int rc_finalize(rc_ctx* c) {
@@ -1572,18 +1769,48 @@ int rc_sync(rc_ctx* c) {
   return latch(c);
 }
 
+// Norms of every case into norm_out ([case][V+1]); synchronises.
+static int norms(rc_ctx* c, std::vector<double>& h) {
+  const int nc = c->ncase;
+  k_norm_partial<<<dim3(NRM_BLOCKS, nc), NRM_THREADS, 0, c->stream>>>(c->d.hWA, c->d.WA, c->d.vol, c->NE, c->V,
+                                                                       nc > 1 ? c->case_off_dev : nullptr,
+                                                                       c->norm_part);
+  k_norm_final<<<nc, 32, 0, c->stream>>>(c->norm_part, c->V, c->case_vol_dev, c->norm_out);
+  c->launches += 2;
+  h.resize((size_t)nc * (c->V + 1));
+  RC_CU(cudaMemcpyAsync(h.data(), c->norm_out, sizeof(double) * h.size(), cudaMemcpyDeviceToHost, c->stream));
+  RC_CU(cudaStreamSynchronize(c->stream));
+  return check_launch(c, "norms");
+}
 int rc_residual(rc_ctx* c, double* res, double* romax) {
   if (!c || !res || !romax) return RC_ERR_ARG;
-  k_norm_partial<<<NRM_BLOCKS, NRM_THREADS, 0, c->stream>>>(c->d.hWA, c->d.WA, c->d.vol, c->NE, c->V, c->norm_part);
-  k_norm_final<<<1, 32, 0, c->stream>>>(c->norm_part, c->V, c->total_volume, c->norm_out);
-  c->launches += 2;
-  std::vector<double> h(c->V + 1);
-  RC_CU(cudaMemcpyAsync(h.data(), c->norm_out, sizeof(double) * (c->V + 1), cudaMemcpyDeviceToHost, c->stream));
-  RC_CU(cudaStreamSynchronize(c->stream));
+  if (c->ncase != 1) {
+    c->err = "rc_residual on a batch: use rc_residual_batch";
+    return RC_ERR_ARG;
+  }
+  std::vector<double> h;
+  if (int st = norms(c, h)) return st;
   for (int k = 0; k < c->V; ++k) res[k] = h[k];
   *romax = h[c->V];
-  int st = check_launch(c, "rc_residual");
-  return st ? st : latch(c);
+  return latch(c);
+}
+int rc_residual_batch(rc_ctx* c, double* res, double* romax) {
+  if (!c || !res || !romax) return RC_ERR_ARG;
+  std::vector<double> h;
+  if (int st = norms(c, h)) return st;
+  const int V = c->V;
+  for (int b = 0; b < c->ncase; ++b) {
+    for (int k = 0; k < V; ++k) res[(size_t)b * V + k] = h[(size_t)b * (V + 1) + k];
+    romax[b] = h[(size_t)b * (V + 1) + V];
+  }
+  return latch(c);
+}
+int rc_batch_info(rc_ctx* c, int* ncase, int* cell_offsets) {
+  if (!c) return RC_ERR_ARG;
+  if (ncase) *ncase = c->ncase;
+  if (cell_offsets)
+    for (int b = 0; b <= c->ncase; ++b) cell_offsets[b] = c->case_off[b];
+  return RC_OK;
 }
 
 int rc_stats(rc_ctx* c, long long* launches, int* fwd, int* bwd) {

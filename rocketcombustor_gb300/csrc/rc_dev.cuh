@@ -73,7 +73,26 @@ struct Dev {
   const int* swi[2];
   const int* swj[2];
   const int* swf[2];
+  // boundary data per case (a batch of independent cases shares one mesh
+  // numbering): row c of bctab holds case c's oxidizer / fuel inlet Y, T and
+  // mass flux and its exit pressure (BC_* offsets); fcase / gcase give the case
+  // of a face / ghost cell, or are null for a single case (row 0).
+  const double* bctab;
+  const float* bctab32;
+  const int* fcase;
+  const int* gcase;
 };
+
+constexpr int BCS = 13;                 // doubles per bctab row
+constexpr int BC_Y = 0, BC_T = 8, BC_MFLOW = 10, BC_POUT = 12;  // + w*NSPMAX (Y) or + w (T, mass flux)
+constexpr int BC_NSPMAX = 4;
+
+__device__ __forceinline__ const double* bc_row(const Dev& d, const int* ids, int i) {
+  return d.bctab + (ids ? ids[i] : 0) * BCS;
+}
+__device__ __forceinline__ const float* bc_row32(const Dev& d, const int* ids, int i) {
+  return d.bctab32 + (ids ? ids[i] : 0) * BCS;
+}
 
 __device__ __forceinline__ void flag(const Dev& d, unsigned e) {
   if (e) atomicOr(d.err, e);

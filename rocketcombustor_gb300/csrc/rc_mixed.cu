@@ -144,19 +144,20 @@ __global__ void __launch_bounds__(128) k_cell32(const Dev d, const ThermoDev32<N
       case 3:
       case 4: {
         const int w = d.gtype[gj] == 3 ? 0 : 1;
+        const float* bc = bc_row32(d, d.gcase, gj);
 #pragma unroll
-        for (int k = 0; k < NSP; ++k) Yr[k] = th.inY[w][k];
-        tr = th.inT[w];
+        for (int k = 0; k < NSP; ++k) Yr[k] = bc[BC_Y + w * BC_NSPMAX + k];
+        tr = bc[BC_T + w];
         float Cb, gb, Rb;
         gas32<NSP>(th, Yr, tr, Cb, gb, Rb, err);
         const float rb = pr / (Rb * tr);
-        ur = th.inMflow[w] / rb;
+        ur = bc[BC_MFLOW + w] / rb;
         vr = 0.f;
         break;
       }
       case 5:
         vn = ul * s1n + vl * s2n;
-        if (!(fabsf(vn) > ac)) pr = th.p_out;
+        if (!(fabsf(vn) > ac)) pr = bc_row32(d, d.gcase, gj)[BC_POUT];
         break;
       default: err |= ERR_BCTYPE;
     }
@@ -270,14 +271,15 @@ __global__ void __launch_bounds__(128) k_face_flux32(const Dev d, const ThermoDe
       for (int k = 0; k < NSP; ++k) Yr[k] = YR0[k];
     } else if (NR == -3 || NR == -4) {
       const int w = NR == -3 ? 0 : 1;
+      const float* bc = bc_row32(d, d.fcase, f);
 #pragma unroll
-      for (int k = 0; k < NSP; ++k) Yr[k] = th.inY[w][k];
-      tr = th.inT[w];
+      for (int k = 0; k < NSP; ++k) Yr[k] = bc[BC_Y + w * BC_NSPMAX + k];
+      tr = bc[BC_T + w];
       float Cb, Rb;
       gas32<NSP>(th, Yr, tr, Cb, gr, Rb, err);
       pr = pl;
       rr = pr / (Rb * tr);
-      ur = th.inMflow[w] / rr;
+      ur = bc[BC_MFLOW + w] / rr;
       vr = 0.f;
       pl = pr; ul = ur; vl = vr; tl = tr; rl = rr; gl = gr; Rl = Rb;
 #pragma unroll
@@ -293,7 +295,7 @@ __global__ void __launch_bounds__(128) k_face_flux32(const Dev d, const ThermoDe
         const float ac = sqrtf(gl * pl / rl);
         vn = ul * sn1 + vl * sn2;
         if (!(fabsf(vn) > ac)) {
-          pr = th.p_out;
+          pr = bc_row32(d, d.fcase, f)[BC_POUT];
           ur = ul + sn1 * (pl - pr) / (rl * ac);
           vr = vl + sn2 * (pl - pr) / (rl * ac);
           rr = rl + (pr - pl) / (ac * ac);
@@ -344,13 +346,14 @@ __global__ void __launch_bounds__(128) k_face_flux32(const Dev d, const ThermoDe
       for (int k = 0; k < NSP; ++k) Yr[k] = YR0[k];
     } else if (NR == -3 || NR == -4) {
       const int w = NR == -3 ? 0 : 1;
+      const float* bc = bc_row32(d, d.fcase, f);
 #pragma unroll
-      for (int k = 0; k < NSP; ++k) Yr[k] = th.inY[w][k];
-      tr = th.inT[w];
+      for (int k = 0; k < NSP; ++k) Yr[k] = bc[BC_Y + w * BC_NSPMAX + k];
+      tr = bc[BC_T + w];
       float Cb, gb, Rb;
       gas32<NSP>(th, Yr, tr, Cb, gb, Rb, err);
       pr = pl;
-      ur = th.inMflow[w] / (pr / (Rb * tr));
+      ur = bc[BC_MFLOW + w] / (pr / (Rb * tr));
       vr = 0.f;
       pl = pr; ul = ur; vl = vr; tl = tr;
 #pragma unroll
@@ -367,7 +370,7 @@ __global__ void __launch_bounds__(128) k_face_flux32(const Dev d, const ThermoDe
         const float ac = sqrtf(gl0 * pl / rl0);
         const float vn = ul * sn1 + vl * sn2;
         if (!(fabsf(vn) > ac)) {
-          pr = th.p_out;
+          pr = bc_row32(d, d.fcase, f)[BC_POUT];
           ur = ul + sn1 * (pl - pr) / (rl0 * ac);
           vr = vl + sn2 * (pl - pr) / (rl0 * ac);
           tr = pr / (Rl0 * (rl0 + (pr - pl) / (ac * ac)));

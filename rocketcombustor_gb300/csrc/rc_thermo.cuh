@@ -38,9 +38,7 @@ struct ThermoDev {
   double Af, E;                  // Af_react(1), E_react(1)
   double prodc[NSP];             // 1000*mole_weight(ks)*(coef_r-coef_f)
   double mw1000[2];              // mole_weight(1..2)*1000
-  double inY[2][NSP];            // oxidizer / fuel inlet mass fractions
-  double inT[2], inMflow[2];     // inlet temperature and mass flux
-  double p_out, cfl;
+  double cfl;
 };
 
 __device__ __forceinline__ double fmin2(double a, double b) { return (b < a) ? b : a; }

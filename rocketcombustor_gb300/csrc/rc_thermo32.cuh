@@ -19,8 +19,7 @@ struct ThermoDev32 {
   float mu[2][4][NSP], kk[2][4][NSP];
   float wc[NSP][NSP], wd[NSP][NSP];
   float dlj[NSP][NSP], dmw[NSP][NSP], dcd[NSP][NSP];
-  float inY[2][NSP], inT[2], inMflow[2];
-  float p_out, cfl;
+  float cfl;
 };
 
 template <int NSP>
@@ -37,12 +36,9 @@ void make_thermo32(const ThermoDev<NSP>& a, ThermoDev32<NSP>& b) {
       b.wc[i][j] = (float)a.wc[i][j]; b.wd[i][j] = (float)a.wd[i][j];
       b.dlj[i][j] = (float)a.dlj[i][j]; b.dmw[i][j] = (float)a.dmw[i][j]; b.dcd[i][j] = (float)a.dcd[i][j];
     }
-    for (int w = 0; w < 2; ++w) b.inY[w][i] = (float)a.inY[w][i];
   }
   b.tlo = (float)a.tlo; b.tcrit = (float)a.tcrit; b.thi = (float)a.thi;
   b.trlo = (float)a.trlo; b.trcrit = (float)a.trcrit; b.trhi = (float)a.trhi;
-  for (int w = 0; w < 2; ++w) { b.inT[w] = (float)a.inT[w]; b.inMflow[w] = (float)a.inMflow[w]; }
-  b.p_out = (float)a.p_out;
   b.cfl = (float)a.cfl;
 }
 

@@ -123,3 +123,14 @@ def test_integrated_source_mode_runs(case_root):
     # same physics, another discretisation of the source
     assert not np.array_equal(pa, pb)
     assert pb[:, 3].min() > 200 and pb[:, 3].max() < 6000
+
+
+def test_batch_configs_span_the_stated_ranges():
+    from rocketcombustor_gb300 import cases
+    cs = cases.batch_configs()
+    ne = np.array([c.n_cells for c in cs])
+    assert len(cs) == 64 and ne.min() >= 1800 and ne.max() <= 62000 and ne.max() > 10 * ne.min()
+    p0 = np.array([c.p0 for c in cs]); of = np.array([c.of_ratio for c in cs])
+    ar = np.array([c.h_exit / 0.01 for c in cs])
+    assert p0.min() >= 1e6 and p0.max() <= 1e7 and of.min() >= 4 and of.max() <= 8
+    assert ar.min() >= 4 and ar.max() <= 25
