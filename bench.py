@@ -192,6 +192,9 @@ def main():
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--chem", default="explicit", choices=["explicit", "integrated"],
                     help="chemical source: the reference's explicit rate or the per-cell integrator")
+    ap.add_argument("--no-batch", action="store_true",
+                    help="skip the batched form (64 uneven reacting cases in one context)")
+    ap.add_argument("--batch-cases", type=int, default=64)
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
 
@@ -292,6 +295,8 @@ def main():
                                              "after_iterations": args.warmup + args.steps}
                 forms[form] = f
             line["forms"] = forms
+        if not args.no_batch and world == 1:
+            line.setdefault("forms", {})["batched"] = batched_form(args, stream, flush, torch, rc, tmp)
         line["clocks"] = clk
         if not args.no_cpu:
             line["cpu_baseline"] = cpu_baseline(d, args.cpu_budget)
@@ -334,6 +339,37 @@ def time_form(s, args, stream, flush, dist, torch, rc):
         launches = s.stats()["kernel_launches"] - l0
         ms = [a.elapsed_time(b) for a, b in ev]
     return {"t_local": sum(ms) / 1e3, "launches": int(launches)}, clk.summary()
+
+
+def batched_form(args, stream, flush, torch, rc, tmp):
+    """The batched workload: `--batch-cases` independent reacting viscous
+    nozzles of uneven size (2k-60k triangles, 1-10 MPa, O/F 4-8, area ratio
+    4-25, seed 5) in one context, with the per-cell chemistry integrator, in
+    FP64 and mixed precision; launch configuration chosen by the autotuner."""
+    from rocketcombustor_gb300 import cases
+    dirs = cases.make_batch(os.path.join(tmp, "batch"), args.batch_cases, 5)
+    cs = [rc.Case(d) for d in dirs]
+    ne = sum(c.NE for c in cs)
+    out = {"workload": f"{len(cs)} cases, {ne} triangles in total ({min(c.NE for c in cs)}-"
+                       f"{max(c.NE for c in cs)} per case), integrated chemistry",
+           "cells": ne}
+    states = {}
+    for form, prec in (("fp64", rc.RC_PREC_FP64), ("mixed", rc.RC_PREC_MIXED)):
+        b = rc.BatchSolver(cs, precision=prec, stream=stream.cuda_stream)
+        b.set_chemistry(rc.RC_CHEM_INTEGRATED)
+        tune = b.autotune(3)
+        r, _ = time_form(b, args, stream, flush, None, torch, rc)
+        ns = b.chem_substeps()
+        states[form] = b.get_state()[0]
+        out[form] = {"value": ne * args.steps / r["t_local"], "ms_per_step": 1e3 * r["t_local"] / args.steps,
+                     "gpu_launches": r["launches"], "autotune": tune,
+                     "chem_substeps": {"min": int(ns.min()), "mean": float(ns.mean()), "max": int(ns.max())}}
+        b.close()
+    den = np.maximum(np.abs(states["fp64"]).max(axis=0), 1e-300)
+    e = np.abs(states["mixed"] - states["fp64"]).max(axis=0) / den
+    out["mixed"]["rel_linf_vs_fp64"] = {"p": float(e[0]), "T": float(e[3]), "Y": [float(x) for x in e[4:]],
+                                        "after_iterations": args.warmup + args.steps}
+    return out
 
 
 def subroutine_times(s, args, stream, flush, torch):

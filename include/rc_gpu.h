@@ -160,6 +160,13 @@ int rc_lusgs_stage(rc_ctx* ctx, int istep); /* lu_sgs_stage   Time_LUSGS_steady.
  * No counterpart in the reference (it has a single FP64 path). */
 int rc_set_precision(rc_ctx* ctx, int precision);
 
+/* Autotuner: times `iters` iterations of every launch configuration (LU-SGS
+ * as one cooperative kernel or one kernel per level; 32, 64 or 128 threads
+ * per block for the cell and face kernels) on the current state, keeps the
+ * fastest and restores the state.  The configurations compute the same bits.
+ * report (may be null) gets one line of timings.  Synchronises. */
+int rc_autotune(rc_ctx* ctx, int iters, char* report, int report_len);
+
 /* Chemistry source of the following iterations (all precision modes; the
  * chemistry is FP64 in each).  RC_CHEM_INTEGRATED integrates each cell's
  * constant-volume adiabatic reactor over its pseudo time step with linearly

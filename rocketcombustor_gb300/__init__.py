@@ -101,6 +101,7 @@ SIGNATURES = {
                            ctypes.POINTER(_vp)]),
     "rc_batch_info": (_i, [_vp, _IP, _IP]),
     "rc_residual_batch": (_i, [_vp, _DP, _DP]),
+    "rc_autotune": (_i, [_vp, _i, _cp, _i]),
     "rc_chem_substeps": (_i, [_vp, _IP]),
     "rc_chem_integrate": (_i, [_vp, _vp, _vp, _i, _vp, _vp, _d, _i]),
 }
@@ -252,6 +253,13 @@ class Solver:
         """RC_CHEM_EXPLICIT (the reference's vol*omega) or RC_CHEM_INTEGRATED
         (mean rate of the per-cell integrator over the pseudo time step)."""
         self._check(load().rc_set_chemistry(self._h, int(mode), float(tol), int(max_substeps)))
+
+    def autotune(self, iters: int = 5) -> str:
+        """Pick the fastest launch configuration on the current state (the
+        state is restored); returns the timing report."""
+        buf = ctypes.create_string_buffer(1024)
+        self._check(load().rc_autotune(self._h, int(iters), buf, len(buf)))
+        return buf.value.decode()
 
     def chem_substeps(self) -> np.ndarray:
         out = np.zeros(self.NE, dtype=np.int32)

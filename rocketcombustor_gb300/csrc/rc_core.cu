@@ -528,76 +528,14 @@ __global__ void __launch_bounds__(128) k_gather(const Dev d, int visc, int comb)
 }
 
 // ---------------------------------------------------------------- LU-SGS ---
-// One cell of the forward (FWD) or backward sweep (Time_LUSGS_steady.f90:125-260).
-template <int NSP, bool FWD>
-__global__ void __launch_bounds__(128) k_sweep(const Dev d, const ThermoDev<NSP> th, const int* __restrict__ cells,
-                                               int n, int gather, int visc, int comb) {
-  constexpr int V = 3 + NSP;
-  const int t = blockIdx.x * blockDim.x + threadIdx.x;
-  if (t >= n) return;
-  const int i = cells[t];
-  const int NE = d.NE, NF = d.NF, nf = d.nface[i];
-  const unsigned lb = d.cleft[i];
-  double R[V], df[V];
-  if (FWD && gather) {
-    gather_residual<NSP>(d, i, visc, comb, R);
-  } else {
-#pragma unroll
-    for (int k = 0; k < V; ++k) R[k] = d.hWA[k * NE + i];
-  }
-#pragma unroll
-  for (int k = 0; k < V; ++k) df[k] = 0.0;
-  for (int q = 0; q < nf; ++q) {
-    const int j = d.cother[q * NE + i];
-    if (j < 0 || (FWD ? !(j < i) : !(j > i))) continue;
-    const int f = d.cface[q * NE + i];
-    double dx = d.fvec[f], dy = d.fvec[NF + f];
-    if (!((lb >> q) & 1u)) { dx = -dx; dy = -dy; }
-    const double pp = d.PA[0 * NE + j], uu = d.PA[1 * NE + j], vv = d.PA[2 * NE + j], tt = d.PA[3 * NE + j];
-    const double rr = d.cst[0 * NE + j], gama = d.cst[1 * NE + j], roe = d.cst[2 * NE + j];
-    const double rou = rr * uu, rov = rr * vv;
-    const double drr = d.hWA[0 * NE + j], dru = d.hWA[1 * NE + j], drv = d.hWA[2 * NE + j],
-                 dre = d.hWA[3 * NE + j];
-    double dry[NSP], s = 0.0;
-#pragma unroll
-    for (int k = 0; k < NSP - 1; ++k) { dry[k] = d.hWA[(4 + k) * NE + j]; s = s + dry[k]; }
-    dry[NSP - 1] = drr - s;
-    const double duu = (dru - uu * drr) / rr;
-    const double dvv = (drv - vv * drr) / rr;
-    double s1 = 0.0, s2 = 0.0;
-#pragma unroll
-    for (int k = 0; k < NSP; ++k) s1 = s1 + d.cst[(3 + k) * NE + j] * dry[k];
-#pragma unroll
-    for (int k = 0; k < NSP; ++k) s2 = s2 + th.R[k] * dry[k];
-    const double dpp =
-        (gama - 1) * (dre - s1 + tt * s2 * gama / (gama - 1) - 0.5 * (dru * uu + duu * rou + drv * vv + dvv * rov));
-    const double unormal = uu * dx + vv * dy;
-    const double dunormal = duu * dx + dvv * dy;
-    const double aF = d.alpaF[f];
-    df[0] = df[0] + 0.5 * (-aF * drr + dru * dx + drv * dy);
-    df[1] = df[1] + 0.5 * (-aF * dru + dru * unormal + rou * dunormal + dpp * dx);
-    df[2] = df[2] + 0.5 * (-aF * drv + drv * unormal + rov * dunormal + dpp * dy);
-    df[3] = df[3] + 0.5 * (-aF * dre + dunormal * (roe + pp) + unormal * (dre + dpp));
-#pragma unroll
-    for (int k = 0; k < NSP - 1; ++k) {
-      const double ry = rr * d.PA[(4 + k) * NE + j];
-      df[4 + k] = df[4 + k] + 0.5 * (-aF * dry[k] + dry[k] * unormal + ry * dunormal);
-    }
-  }
-  const double ddi = d.dd[i];
-#pragma unroll
-  for (int k = 0; k < V; ++k) d.hWA[k * NE + i] = FWD ? (R[k] - df[k]) / ddi : R[k] - df[k] / ddi;
-}
-
-// Same sweep step with four lanes per cell, one per face slot: each lane
-// evaluates its neighbour's term of dflux, the terms are then added in slot
-// order (the NeighF order of the reference) by every lane of the quad, and the
-// lanes share the final divisions.  The residual R is already in hWA (the
-// forward gather runs as a separate, fully parallel kernel).
-// One cell of a sweep at level position t (t >= tend: lanes that only join
-// the shuffles), lane q = face slot.  All indices come from the sweep tables in
-// one load; the cell's own residual and diagonal are fetched up front.
-// Called by whole warps.
+// LU-SGS forward / backward sweeps (Time_LUSGS_steady.f90:125-260).
+// A quad of 4 lanes handles one cell: lane q evaluates the dflux term of the
+// neighbour in face slot q, the terms are added in slot order (the NeighF
+// order of the reference) and the lanes share the final divisions.  The
+// residual R is already in hWA (the gather runs before, fully parallel).
+// sweep_step: the cell at level position t (t >= tend: lanes that only join
+// the shuffles).  All indices come from the sweep tables in one load; the
+// cell's own residual and diagonal are fetched up front.  Called by whole warps.
 template <int NSP, bool FWD>
 __device__ __forceinline__ void sweep_step(const Dev& d, const ThermoDev<NSP>& th, int t, int tend, int q) {
   constexpr int V = 3 + NSP;
@@ -809,6 +747,7 @@ struct rc_ctx {
   int* bwd_cells = nullptr;
   std::vector<int> fwd_off, bwd_off;
   bool persistent = true;       // LU-SGS sweeps as one cooperative launch (else one launch per level)
+  bool can_persistent = false;  // the device can co-schedule the persistent LU-SGS grid
   int pers_grid = 0;             // blocks of the persistent launch (one per SM)
   unsigned* bar_count = nullptr; // grid-barrier counter of the persistent launch
   int* fwd_off_dev = nullptr;
@@ -922,20 +861,20 @@ const ThermoDev<NSP>& TH(const rc_ctx* c) { return *reinterpret_cast<const Therm
 // --- the pieces of one iteration, enqueued on c->stream
 template <int NSP>
 void q_timestep_face(rc_ctx* c) {
-  if (c->visc) k_ts_face<NSP, true><<<blocks(c->NF, 128), 128, 0, c->stream>>>(c->d, TH<NSP>(c));
-  else k_ts_face<NSP, false><<<blocks(c->NF, 128), 128, 0, c->stream>>>(c->d, TH<NSP>(c));
+  if (c->visc) k_ts_face<NSP, true><<<blocks(c->NF, c->d.bs), c->d.bs, 0, c->stream>>>(c->d, TH<NSP>(c));
+  else k_ts_face<NSP, false><<<blocks(c->NF, c->d.bs), c->d.bs, 0, c->stream>>>(c->d, TH<NSP>(c));
   c->launches++;
 }
 template <int NSP>
 void q_cell(rc_ctx* c, int do_step, int do_recon) {
-  k_cell<NSP><<<blocks(c->NE, 128), 128, 0, c->stream>>>(c->d, TH<NSP>(c), do_step, do_recon, c->limit,
+  k_cell<NSP><<<blocks(c->NE, c->d.bs), c->d.bs, 0, c->stream>>>(c->d, TH<NSP>(c), do_step, do_recon, c->limit,
                                                           c->comb && c->chem == RC_CHEM_EXPLICIT, c->visc);
   c->launches++;
 }
 template <int NSP>
 void q_face_flux(rc_ctx* c) {
-  if (c->visc) k_face_flux<NSP, true><<<blocks(c->NF, 128), 128, 0, c->stream>>>(c->d, TH<NSP>(c));
-  else k_face_flux<NSP, false><<<blocks(c->NF, 128), 128, 0, c->stream>>>(c->d, TH<NSP>(c));
+  if (c->visc) k_face_flux<NSP, true><<<blocks(c->NF, c->d.bs), c->d.bs, 0, c->stream>>>(c->d, TH<NSP>(c));
+  else k_face_flux<NSP, false><<<blocks(c->NF, c->d.bs), c->d.bs, 0, c->stream>>>(c->d, TH<NSP>(c));
   c->launches++;
 }
 template <int NSP>
@@ -958,7 +897,7 @@ void q_persistent(rc_ctx* c) {
 template <int NSP>
 void q_sweeps(rc_ctx* c, int gather) {
   if (gather) {
-    k_gather<NSP><<<blocks(c->NE, 128), 128, 0, c->stream>>>(c->d, c->visc, c->comb);
+    k_gather<NSP><<<blocks(c->NE, c->d.bs), c->d.bs, 0, c->stream>>>(c->d, c->visc, c->comb);
     c->launches++;
   }
   if (c->persistent) { q_persistent<NSP>(c); return; }
@@ -973,7 +912,7 @@ void q_sweeps(rc_ctx* c, int gather) {
                                                                     c->bwd_off[l + 1]);
     c->launches++;
   }
-  k_update<NSP><<<blocks(c->NE, 128), 128, 0, c->stream>>>(c->d, TH<NSP>(c));
+  k_update<NSP><<<blocks(c->NE, c->d.bs), c->d.bs, 0, c->stream>>>(c->d, TH<NSP>(c));
   c->launches++;
 }
 // Integrated chemical source on the side stream, forked after the cell pass
@@ -993,7 +932,7 @@ void q_chem_join(rc_ctx* c) {
 }
 template <int NSP>
 void q_gather(rc_ctx* c) {
-  k_gather<NSP><<<blocks(c->NE, 128), 128, 0, c->stream>>>(c->d, c->visc, c->comb);
+  k_gather<NSP><<<blocks(c->NE, c->d.bs), c->d.bs, 0, c->stream>>>(c->d, c->visc, c->comb);
   c->launches++;
 }
 // Sweeps of the mixed-precision modes: FP32 off-diagonal terms, FP64 division.
@@ -1003,7 +942,7 @@ void q_sweeps32(rc_ctx* c) {
     cudaMemsetAsync(c->bar_count, 0, sizeof(unsigned), c->stream);
     mixed_lusgs_persistent<NSP>(c->d, c->thermo32.data(), c->fwd_off_dev, (int)c->fwd_off.size() - 1, c->bwd_off_dev,
                                 (int)c->bwd_off.size() - 1, c->bar_count, c->pers_grid, c->stream);
-    k_update<NSP><<<blocks(c->NE, 128), 128, 0, c->stream>>>(c->d, TH<NSP>(c));
+    k_update<NSP><<<blocks(c->NE, c->d.bs), c->d.bs, 0, c->stream>>>(c->d, TH<NSP>(c));
     c->launches += 2;
     return;
   }
@@ -1015,7 +954,7 @@ void q_sweeps32(rc_ctx* c) {
     mixed_sweep<NSP>(c->d, c->thermo32.data(), false, c->bwd_off[l], c->bwd_off[l + 1], c->stream);
     c->launches++;
   }
-  k_update<NSP><<<blocks(c->NE, 128), 128, 0, c->stream>>>(c->d, TH<NSP>(c));
+  k_update<NSP><<<blocks(c->NE, c->d.bs), c->d.bs, 0, c->stream>>>(c->d, TH<NSP>(c));
   c->launches++;
 }
 // The subroutines of one iteration in the current precision mode.
@@ -1414,6 +1353,7 @@ int init_impl(const rc_mesh* m, const rc_thermo* t, const rc_config* g, const Ba
   // ---- upload
   Dev& d = c->d;
   d.NE = NE; d.NF = NF; d.NG = NG;
+  d.bs = 128;
   int st = 0;
   double* p;
   unsigned char* u8;
@@ -1539,7 +1479,8 @@ int init_impl(const rc_mesh* m, const rc_thermo* t, const rc_config* g, const Ba
     }
     const char* sched = std::getenv("RC_LUSGS_SCHEDULE");
     c->pers_grid = nsm;
-    c->persistent = coop && nsm > 0 && occ64 >= 1 && occ32 >= 1 && !(sched && std::string(sched) == "levels");
+    c->can_persistent = coop && nsm > 0 && occ64 >= 1 && occ32 >= 1;
+    c->persistent = c->can_persistent && !(sched && std::string(sched) == "levels");
   }
   *out = c;
   return RC_OK;
@@ -1695,6 +1636,66 @@ int rc_set_precision(rc_ctx* c, int precision) {
   c->graph_kernels = c->graph_kernels_of[precision];
   return RC_OK;
 }
+static void drop_graphs(rc_ctx* c) {
+  for (int k = 0; k < 3; ++k)
+    if (c->graphs[k]) { cudaGraphExecDestroy(c->graphs[k]); c->graphs[k] = nullptr; }
+  c->graph = nullptr;
+}
+int rc_autotune(rc_ctx* c, int iters, char* report, int report_len) {
+  if (!c || iters < 1) return RC_ERR_ARG;
+  const size_t n = (size_t)c->V * c->NE;
+  double* save = nullptr;
+  RC_CU(cudaMalloc(&save, 2 * n * sizeof(double)));
+  auto restore = [&]() {
+    cudaMemcpyAsync(c->d.PA, save, n * sizeof(double), cudaMemcpyDeviceToDevice, c->stream);
+    cudaMemcpyAsync(c->d.WA, save + n, n * sizeof(double), cudaMemcpyDeviceToDevice, c->stream);
+  };
+  cudaMemcpyAsync(save, c->d.PA, n * sizeof(double), cudaMemcpyDeviceToDevice, c->stream);
+  cudaMemcpyAsync(save + n, c->d.WA, n * sizeof(double), cudaMemcpyDeviceToDevice, c->stream);
+  struct Cand { bool pers; int bs; };
+  std::vector<Cand> cands;
+  for (int pers = c->can_persistent ? 1 : 0; pers >= 0; --pers)
+    for (int bs : {128, 64, 32}) cands.push_back({pers != 0, bs});
+  cudaEvent_t e0, e1;
+  cudaEventCreate(&e0);
+  cudaEventCreate(&e1);
+  std::string rep;
+  double best = 1e300;
+  Cand bc = {c->persistent, c->d.bs};
+  int st = RC_OK;
+  for (const Cand& k : cands) {
+    c->persistent = k.pers;
+    c->d.bs = k.bs;
+    drop_graphs(c);
+    restore();
+    for (int w = 0; w < 2 && !st; ++w) st = rc_lusgs_stage(c, 1);
+    cudaEventRecord(e0, c->stream);
+    for (int it = 0; it < iters && !st; ++it) st = rc_lusgs_stage(c, 1);
+    cudaEventRecord(e1, c->stream);
+    cudaEventSynchronize(e1);
+    if (st) break;
+    float ms = 0.f;
+    cudaEventElapsedTime(&ms, e0, e1);
+    const double per = ms / iters;
+    rep += std::string(k.pers ? "persistent" : "levels") + " bs=" + std::to_string(k.bs) + ": " +
+           std::to_string(per) + " ms; ";
+    if (per < best) { best = per; bc = k; }
+  }
+  c->persistent = bc.pers;
+  c->d.bs = bc.bs;
+  drop_graphs(c);
+  restore();
+  cudaStreamSynchronize(c->stream);
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  cudaFree(save);
+  rep += std::string("chosen: ") + (bc.pers ? "persistent" : "levels") + " bs=" + std::to_string(bc.bs);
+  if (report && report_len > 0) {
+    std::snprintf(report, (size_t)report_len, "%s", rep.c_str());
+  }
+  if (st) return st;
+  return latch(c);
+}
 int rc_set_chemistry(rc_ctx* c, int mode, double tol, int max_substeps) {
   if (!c) return RC_ERR_ARG;
   if (mode != RC_CHEM_EXPLICIT && mode != RC_CHEM_INTEGRATED) return RC_ERR_ARG;
@@ -1713,9 +1714,7 @@ int rc_set_chemistry(rc_ctx* c, int mode, double tol, int max_substeps) {
   c->chem = mode;
   c->chem_tol = tol;
   c->chem_maxsub = max_substeps;
-  for (int k = 0; k < 3; ++k)
-    if (c->graphs[k]) { cudaGraphExecDestroy(c->graphs[k]); c->graphs[k] = nullptr; }
-  c->graph = nullptr;
+  drop_graphs(c);
   return RC_OK;
 }
 int rc_chem_substeps(rc_ctx* c, int* out) {

@@ -10,6 +10,7 @@ constexpr int MAXF = 4;  // faces per cell (triangles and quadrilaterals)
 
 struct Dev {
   int NE, NF, NG;
+  int bs;                        // threads per block of the cell and face kernels (32, 64 or 128)
   // cells
   const double* vol;
   const double* rinv;            // [2*NE] 1./reflen

@@ -635,28 +635,28 @@ inline unsigned nblk(long n, int t) { return (unsigned)((n + t - 1) / t); }
 template <int NSP>
 void mixed_ts_face(const Dev& d, const void* th32, int visc, cudaStream_t s) {
   const auto& th = *static_cast<const ThermoDev32<NSP>*>(th32);
-  if (visc) k_ts_face32<NSP, true><<<nblk(d.NF, 128), 128, 0, s>>>(d, th);
-  else k_ts_face32<NSP, false><<<nblk(d.NF, 128), 128, 0, s>>>(d, th);
+  if (visc) k_ts_face32<NSP, true><<<nblk(d.NF, d.bs), d.bs, 0, s>>>(d, th);
+  else k_ts_face32<NSP, false><<<nblk(d.NF, d.bs), d.bs, 0, s>>>(d, th);
 }
 template <int NSP>
 void mixed_cell(const Dev& d, const void* th32, const ThermoDev<NSP>& th64, int do_step, int limit, int comb,
                 int visc, cudaStream_t s) {
-  k_cell32<NSP><<<nblk(d.NE, 128), 128, 0, s>>>(d, *static_cast<const ThermoDev32<NSP>*>(th32), th64, do_step,
+  k_cell32<NSP><<<nblk(d.NE, d.bs), d.bs, 0, s>>>(d, *static_cast<const ThermoDev32<NSP>*>(th32), th64, do_step,
                                                  limit, comb, visc);
 }
 template <int NSP>
 void mixed_face_flux(const Dev& d, const void* th32, int visc, cudaStream_t s) {
   const auto& th = *static_cast<const ThermoDev32<NSP>*>(th32);
-  if (visc) k_face_flux32<NSP, true><<<nblk(d.NF, 128), 128, 0, s>>>(d, th);
-  else k_face_flux32<NSP, false><<<nblk(d.NF, 128), 128, 0, s>>>(d, th);
+  if (visc) k_face_flux32<NSP, true><<<nblk(d.NF, d.bs), d.bs, 0, s>>>(d, th);
+  else k_face_flux32<NSP, false><<<nblk(d.NF, d.bs), d.bs, 0, s>>>(d, th);
 }
 template <int NSP>
 void mixed_pack(const Dev& d, cudaStream_t s) {
-  k_pack32<NSP><<<nblk(d.NE, 128), 128, 0, s>>>(d);
+  k_pack32<NSP><<<nblk(d.NE, d.bs), d.bs, 0, s>>>(d);
 }
 template <int NSP>
 void mixed_gather(const Dev& d, int visc, int comb, cudaStream_t s) {
-  k_gather32<NSP><<<nblk(d.NE, 128), 128, 0, s>>>(d, visc, comb);
+  k_gather32<NSP><<<nblk(d.NE, d.bs), d.bs, 0, s>>>(d, visc, comb);
 }
 template <int NSP>
 void mixed_sweep(const Dev& d, const void* th32, bool fwd, int t0, int t1, cudaStream_t s) {

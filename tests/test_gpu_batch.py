@@ -62,3 +62,14 @@ def test_batch_uneven_sizes_and_conditions(batch_dirs):
     assert max(ne) > 2 * min(ne)
     cfgs = cases.batch_configs(n=5, seed=9, ne_min=300, ne_max=3000)
     assert len({round(c.p0) for c in cfgs}) == 5 and len({c.h_exit for c in cfgs}) == 5
+
+
+def test_autotune_keeps_the_bits(batch_dirs):
+    cs = [rc.Case(d) for d in batch_dirs]
+    a = rc.BatchSolver(cs)
+    b = rc.BatchSolver(cs)
+    rep = b.autotune(2)
+    assert "chosen" in rep
+    a.run(15)
+    b.run(15)
+    assert np.array_equal(a.get_state()[0], b.get_state()[0])
