@@ -49,6 +49,8 @@ extern "C" {
 
 #define RC_CHEM_EXPLICIT 0     /* chemical source = vol*omega, the reference's explicit rate (sourceterm.f90:43-51) */
 #define RC_CHEM_INTEGRATED 1   /* chemical source = vol*rho*(Y(step)-Y)/step from the per-cell integrator */
+#define RC_CHEM_SURROGATE 2    /* the same from the learned surrogate (rc_mlp.h), the integrator where the
+                                  surrogate's error indicator rejects a cell */
 
 typedef struct rc_ctx rc_ctx;
 
@@ -185,6 +187,21 @@ int rc_chem_substeps(rc_ctx* ctx, int* nsub);
  * context's stream; stop conditions latch like the other calls. */
 int rc_chem_integrate(rc_ctx* ctx, const double* d_P, const double* d_dt, int n, double* d_out, int* d_nsub,
                       double tol, int max_substeps);
+
+/* Learned surrogate of the integrator (needs Nsp = 4).  The network (rc_mlp.h)
+ * is owned by the caller and must outlive its use.  A cell goes back to the
+ * integrator when its state is outside the network's training domain, when
+ * the predicted rate ratios of the reacting species differ by more than
+ * spread_tol, or when the prediction leaves Y in [0, 1]. */
+struct rc_mlp;
+int rc_set_surrogate(rc_ctx* ctx, struct rc_mlp* net, double spread_tol);
+/* Cells of the last surrogate source served by the network / by the integrator. */
+int rc_surrogate_stats(rc_ctx* ctx, unsigned* n_surrogate, unsigned* n_fallback);
+/* Training pairs from integrated states: d_P0, d_P1 (NVar x n SoA, before and
+ * after d_dt) -> raw features d_x (n x 7: T, p, Y_1..Y_4, dt) and targets d_t
+ * (n x 4: mean-rate ratios).  Device pointers; on the context's stream. */
+int rc_surrogate_samples(rc_ctx* ctx, const double* d_P0, const double* d_P1, const double* d_dt, int n, float* d_x,
+                         float* d_t);
 
 /* Residual + step_residual norms (residual.f90:4-21, 61-79): res(k) =
  * sum(vol*|hWA(k,:)|)/total_volume, romax = max(WA(1,:)).  Synchronises. */

@@ -32,7 +32,7 @@ RC_ERR = {1: "thermo T out of range", 2: "transport T out of range", 4: "negativ
           64: "grid barrier timed out",
           1024: "invalid argument", 2048: "CUDA error"}
 RC_PREC_FP64, RC_PREC_MIXED, RC_PREC_MIXED_DC = 0, 1, 2
-RC_CHEM_EXPLICIT, RC_CHEM_INTEGRATED = 0, 1
+RC_CHEM_EXPLICIT, RC_CHEM_INTEGRATED, RC_CHEM_SURROGATE = 0, 1, 2
 
 _i, _d, _l, _vp, _cp = ctypes.c_int, ctypes.c_double, ctypes.c_long, ctypes.c_void_p, ctypes.c_char_p
 _IP, _DP = ctypes.POINTER(ctypes.c_int), ctypes.POINTER(ctypes.c_double)
@@ -102,6 +102,19 @@ SIGNATURES = {
     "rc_batch_info": (_i, [_vp, _IP, _IP]),
     "rc_residual_batch": (_i, [_vp, _DP, _DP]),
     "rc_autotune": (_i, [_vp, _i, _cp, _i]),
+    "rc_set_surrogate": (_i, [_vp, _vp, _d]),
+    "rc_surrogate_stats": (_i, [_vp, ctypes.POINTER(ctypes.c_uint), ctypes.POINTER(ctypes.c_uint)]),
+    "rc_surrogate_samples": (_i, [_vp, _vp, _vp, _vp, _i, _vp, _vp]),
+    "rc_mlp_create": (_i, [_i, ctypes.POINTER(_vp)]),
+    "rc_mlp_destroy": (_i, [_vp]),
+    "rc_mlp_set_params": (_i, [_vp, ctypes.POINTER(ctypes.c_float)]),
+    "rc_mlp_get_params": (_i, [_vp, ctypes.POINTER(ctypes.c_float)]),
+    "rc_mlp_set_norm": (_i, [_vp, ctypes.POINTER(ctypes.c_float), ctypes.POINTER(ctypes.c_float),
+                             ctypes.POINTER(ctypes.c_float)]),
+    "rc_mlp_forward": (_i, [_vp, _vp, _i, _vp, _vp]),
+    "rc_mlp_gradient": (_i, [_vp, _vp, _vp, _i, _vp, ctypes.POINTER(ctypes.c_float), _vp]),
+    "rc_mlp_adam": (_i, [_vp, _vp, ctypes.c_float, ctypes.c_float, ctypes.c_float, ctypes.c_float, _vp]),
+    "rc_mlp_last_error": (_cp, [_vp]),
     "rc_chem_substeps": (_i, [_vp, _IP]),
     "rc_chem_integrate": (_i, [_vp, _vp, _vp, _i, _vp, _vp, _d, _i]),
 }
@@ -260,6 +273,31 @@ class Solver:
         buf = ctypes.create_string_buffer(1024)
         self._check(load().rc_autotune(self._h, int(iters), buf, len(buf)))
         return buf.value.decode()
+
+    def set_surrogate(self, net, spread_tol: float = 0.02):
+        """Use the surrogate `net` (rocketcombustor_gb300.surrogate.MLP) for
+        RC_CHEM_SURROGATE; it must outlive this solver's use of it."""
+        self._check(load().rc_set_surrogate(self._h, net.handle, float(spread_tol)))
+        self._net = net
+
+    def surrogate_stats(self):
+        """(cells served by the network, cells sent to the integrator) of the last source."""
+        a, b = ctypes.c_uint(), ctypes.c_uint()
+        self._check(load().rc_surrogate_stats(self._h, ctypes.byref(a), ctypes.byref(b)))
+        return a.value, b.value
+
+    def surrogate_samples(self, P0, P1, dt):
+        """Training pairs from states before (P0) and after (P1) dt: CUDA float64
+        tensors (NVar, n) and (n,) -> raw features (n, 7) and targets (n, 4)."""
+        import torch
+        n = P0.shape[1]
+        x = torch.empty((n, 7), dtype=torch.float32, device=P0.device)
+        t = torch.empty((n, 4), dtype=torch.float32, device=P0.device)
+        torch.cuda.synchronize(P0.device)
+        self._check(load().rc_surrogate_samples(self._h, P0.contiguous().data_ptr(), P1.contiguous().data_ptr(),
+                                                dt.contiguous().data_ptr(), n, x.data_ptr(), t.data_ptr()))
+        self.sync()
+        return x, t
 
     def chem_substeps(self) -> np.ndarray:
         out = np.zeros(self.NE, dtype=np.int32)

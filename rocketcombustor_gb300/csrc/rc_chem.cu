@@ -24,32 +24,54 @@ __device__ __forceinline__ int next_chunk(unsigned* counter) {
 // the mean rate over the cell's pseudo time step):
 //   src_k = vol * (rho * ((Y_k(step) - Y_k) / step)).
 template <int NSP>
+__device__ __forceinline__ void integrate_cell(const Dev& d, const ThermoDev<NSP>& th, int i, double tol, int maxsub,
+                                               int* nsub, unsigned& err) {
+  constexpr int V = 3 + NSP;
+  const int NE = d.NE;
+  double P[V], P0[V], Y[NSP], Cp, gama, Rcpcv;
+#pragma unroll
+  for (int k = 0; k < V; ++k) { P[k] = d.PA[k * NE + i]; P0[k] = P[k]; }
+  double s = 0.0;
+#pragma unroll
+  for (int k = 0; k < NSP - 1; ++k) { Y[k] = P[4 + k]; s = s + Y[k]; }
+  Y[NSP - 1] = 1.0 - s;
+  gas<NSP>(th, Y, P[3], Cp, gama, Rcpcv, err);
+  const double rho = P[0] / (P[3] * Rcpcv);
+  const double dt = d.step[i];
+  nsub[i] = chem_integrate<NSP>(th, P, dt, tol, maxsub, err);
+  const double vol = d.vol[i];
+#pragma unroll
+  for (int k = 0; k < NSP - 1; ++k) d.src[k * NE + i] = vol * (rho * ((P[4 + k] - P0[4 + k]) / dt));
+}
+
+template <int NSP>
 __global__ void __launch_bounds__(CHEM_THREADS) k_chem_source(const Dev d, const ThermoDev<NSP> th, double tol,
                                                               int maxsub, int* __restrict__ nsub,
                                                               unsigned* counter) {
-  constexpr int V = 3 + NSP;
   const int NE = d.NE;
   unsigned err = 0;
   for (;;) {
     const int base = next_chunk(counter);
     if (base >= NE) break;
     const int i = base + (threadIdx.x & 31);
-    if (i < NE) {
-      double P[V], P0[V], Y[NSP], Cp, gama, Rcpcv;
-#pragma unroll
-      for (int k = 0; k < V; ++k) { P[k] = d.PA[k * NE + i]; P0[k] = P[k]; }
-      double s = 0.0;
-#pragma unroll
-      for (int k = 0; k < NSP - 1; ++k) { Y[k] = P[4 + k]; s = s + Y[k]; }
-      Y[NSP - 1] = 1.0 - s;
-      gas<NSP>(th, Y, P[3], Cp, gama, Rcpcv, err);
-      const double rho = P[0] / (P[3] * Rcpcv);
-      const double dt = d.step[i];
-      nsub[i] = chem_integrate<NSP>(th, P, dt, tol, maxsub, err);
-      const double vol = d.vol[i];
-#pragma unroll
-      for (int k = 0; k < NSP - 1; ++k) d.src[k * NE + i] = vol * (rho * ((P[4 + k] - P0[4 + k]) / dt));
-    }
+    if (i < NE) integrate_cell<NSP>(d, th, i, tol, maxsub, nsub, err);
+  }
+  flag(d, err);
+}
+
+// The same for the cells list[0 .. *nlist) (the surrogate's fallbacks).
+template <int NSP>
+__global__ void __launch_bounds__(CHEM_THREADS) k_chem_list(const Dev d, const ThermoDev<NSP> th, double tol,
+                                                            int maxsub, int* __restrict__ nsub,
+                                                            const int* __restrict__ list,
+                                                            const unsigned* __restrict__ nlist, unsigned* counter) {
+  const int n = (int)min(*nlist, (unsigned)d.NE);
+  unsigned err = 0;
+  for (;;) {
+    const int base = next_chunk(counter);
+    if (base >= n) break;
+    const int q = base + (threadIdx.x & 31);
+    if (q < n) integrate_cell<NSP>(d, th, list[q], tol, maxsub, nsub, err);
   }
   flag(d, err);
 }
@@ -101,6 +123,15 @@ void chem_source(const Dev& d, const void* th, double tol, int maxsub, int* nsub
 }
 
 template <int NSP>
+void chem_list(const Dev& d, const void* th, double tol, int maxsub, int* nsub, const int* list,
+               const unsigned* nlist, unsigned* counter, cudaStream_t s) {
+  const int grid = chem_grid(k_chem_list<NSP>, d.NE);
+  cudaMemsetAsync(counter, 0, sizeof(unsigned), s);
+  k_chem_list<NSP><<<grid, CHEM_THREADS, 0, s>>>(d, *static_cast<const ThermoDev<NSP>*>(th), tol, maxsub, nsub, list,
+                                                 nlist, counter);
+}
+
+template <int NSP>
 void chem_batch(const void* th, const double* P, const double* dt, int n, double* out, int* nsub, double tol,
                 int maxsub, unsigned* counter, unsigned* errp, cudaStream_t s) {
   cudaMemsetAsync(counter, 0, sizeof(unsigned), s);
@@ -111,6 +142,8 @@ void chem_batch(const void* th, const double* P, const double* dt, int n, double
 
 #define RC_CHEM_INST(N)                                                                                  \
   template void chem_source<N>(const Dev&, const void*, double, int, int*, unsigned*, cudaStream_t);     \
+  template void chem_list<N>(const Dev&, const void*, double, int, int*, const int*, const unsigned*,      \
+                             unsigned*, cudaStream_t);                                                   \
   template void chem_batch<N>(const void*, const double*, const double*, int, double*, int*, double, int, \
                               unsigned*, unsigned*, cudaStream_t);
 RC_CHEM_INST(1)

@@ -31,6 +31,7 @@
 #include <vector>
 
 #include "rc_gpu.h"
+#include "rc_mlp.h"
 #include "rc_dev.cuh"
 
 namespace rc {
@@ -726,6 +727,13 @@ void chem_source(const Dev&, const void*, double, int, int*, unsigned*, cudaStre
 template <int NSP>
 void chem_batch(const void*, const double*, const double*, int, double*, int*, double, int, unsigned*, unsigned*,
                 cudaStream_t);
+template <int NSP>
+void chem_list(const Dev&, const void*, double, int, int*, const int*, const unsigned*, unsigned*, cudaStream_t);
+cudaError_t surrogate_source(const Dev&, const void*, const rc_mlp*, float, int*, unsigned*, unsigned*,
+                             cudaStream_t);
+cudaError_t surrogate_prepare();
+cudaError_t surrogate_samples(const void*, const double*, const double*, const double*, int, float*, float*,
+                              cudaStream_t);
 
 }  // namespace rc
 
@@ -764,6 +772,10 @@ struct rc_ctx {
   int chem_maxsub = 200;
   int* chem_nsub = nullptr;           // [NE] accepted substeps of the last integrated source
   unsigned* chem_counter = nullptr;   // work-queue counter
+  const rc_mlp* net = nullptr;        // surrogate (RC_CHEM_SURROGATE)
+  float spread_tol = 0.02f;
+  int* sur_list = nullptr;            // [NE] cells handed back to the integrator
+  unsigned* sur_counts = nullptr;     // [2]: fallback cells, surrogate cells
   cudaStream_t stream2 = nullptr;     // side stream: the integrated source runs beside the face fluxes
   cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
 
@@ -917,17 +929,29 @@ void q_sweeps(rc_ctx* c, int gather) {
 }
 // Integrated chemical source on the side stream, forked after the cell pass
 // and joined before the gather, so that it overlaps the face fluxes.
+// With the surrogate, the network serves every cell it can and the
+// integrator takes the cells its error indicator rejects.
 template <int NSP>
 void q_chem_fork(rc_ctx* c) {
-  if (!c->comb || c->chem != RC_CHEM_INTEGRATED) return;
+  if (!c->comb || c->chem == RC_CHEM_EXPLICIT) return;
   cudaEventRecord(c->ev_fork, c->stream);
   cudaStreamWaitEvent(c->stream2, c->ev_fork, 0);
-  chem_source<NSP>(c->d, c->thermo.data(), c->chem_tol, c->chem_maxsub, c->chem_nsub, c->chem_counter, c->stream2);
-  c->launches++;
+  if (c->chem == RC_CHEM_SURROGATE) {
+    cudaMemsetAsync(c->sur_counts, 0, 2 * sizeof(unsigned), c->stream2);
+    surrogate_source(c->d, c->thermo.data(), c->net, c->spread_tol, c->sur_list, c->sur_counts, c->sur_counts + 1,
+                     c->stream2);
+    chem_list<NSP>(c->d, c->thermo.data(), c->chem_tol, c->chem_maxsub, c->chem_nsub, c->sur_list, c->sur_counts,
+                   c->chem_counter, c->stream2);
+    c->launches += 2;
+  } else {
+    chem_source<NSP>(c->d, c->thermo.data(), c->chem_tol, c->chem_maxsub, c->chem_nsub, c->chem_counter,
+                     c->stream2);
+    c->launches++;
+  }
   cudaEventRecord(c->ev_join, c->stream2);
 }
 void q_chem_join(rc_ctx* c) {
-  if (!c->comb || c->chem != RC_CHEM_INTEGRATED) return;
+  if (!c->comb || c->chem == RC_CHEM_EXPLICIT) return;
   cudaStreamWaitEvent(c->stream, c->ev_join, 0);
 }
 template <int NSP>
@@ -1696,15 +1720,55 @@ int rc_autotune(rc_ctx* c, int iters, char* report, int report_len) {
   if (st) return st;
   return latch(c);
 }
+int rc_set_surrogate(rc_ctx* c, rc_mlp* net, double spread_tol) {
+  if (!c || !net || !(spread_tol > 0.0)) return RC_ERR_ARG;
+  if (c->NSP != 4) {
+    c->err = "the surrogate is built for 4 species";
+    return RC_ERR_ARG;
+  }
+  if (!c->sur_list) {
+    if (int st = dev_zeros(c, (size_t)c->NE, &c->sur_list)) return st;
+    if (int st = dev_zeros(c, (size_t)2, &c->sur_counts)) return st;
+  }
+  RC_CU(surrogate_prepare());
+  c->net = net;
+  c->spread_tol = (float)spread_tol;
+  drop_graphs(c);
+  return RC_OK;
+}
+int rc_surrogate_stats(rc_ctx* c, unsigned* n_surrogate, unsigned* n_fallback) {
+  if (!c) return RC_ERR_ARG;
+  unsigned h[2] = {0, 0};
+  if (c->sur_counts) {
+    RC_CU(cudaMemcpyAsync(h, c->sur_counts, sizeof(h), cudaMemcpyDeviceToHost, c->stream));
+    RC_CU(cudaStreamSynchronize(c->stream));
+  }
+  if (n_fallback) *n_fallback = h[0];
+  if (n_surrogate) *n_surrogate = h[1];
+  return latch(c);
+}
+int rc_surrogate_samples(rc_ctx* c, const double* d_P0, const double* d_P1, const double* d_dt, int n, float* d_x,
+                         float* d_t) {
+  if (!c || n < 0 || (n > 0 && (!d_P0 || !d_P1 || !d_dt || !d_x || !d_t))) return RC_ERR_ARG;
+  if (c->NSP != 4) return RC_ERR_ARG;
+  if (n == 0) return RC_OK;
+  RC_CU(surrogate_samples(c->thermo.data(), d_P0, d_P1, d_dt, n, d_x, d_t, c->stream));
+  c->launches++;
+  return RC_OK;
+}
 int rc_set_chemistry(rc_ctx* c, int mode, double tol, int max_substeps) {
   if (!c) return RC_ERR_ARG;
-  if (mode != RC_CHEM_EXPLICIT && mode != RC_CHEM_INTEGRATED) return RC_ERR_ARG;
+  if (mode != RC_CHEM_EXPLICIT && mode != RC_CHEM_INTEGRATED && mode != RC_CHEM_SURROGATE) return RC_ERR_ARG;
   if (!(tol > 0.0) || max_substeps < 1) return RC_ERR_ARG;
   if (mode != RC_CHEM_EXPLICIT && !c->comb) {
     c->err = "the integrated source needs If_turn_on_combustion";
     return RC_ERR_ARG;
   }
-  if (mode == RC_CHEM_INTEGRATED && !c->chem_nsub) {
+  if (mode == RC_CHEM_SURROGATE && !c->net) {
+    c->err = "RC_CHEM_SURROGATE needs rc_set_surrogate first";
+    return RC_ERR_ARG;
+  }
+  if (mode != RC_CHEM_EXPLICIT && !c->chem_nsub) {
     if (int st = dev_zeros(c, (size_t)c->NE, &c->chem_nsub)) return st;
     if (int st = dev_zeros(c, (size_t)1, &c->chem_counter)) return st;
     RC_CU(cudaStreamCreateWithFlags(&c->stream2, cudaStreamNonBlocking));

@@ -1,0 +1,872 @@
+// The learned chemistry surrogate (new; the reference has no counterpart).
+//
+// Network: 7 raw inputs (T, p, Y_1..Y_4, dt) -> features (T, log10 p, Y, log10 dt)
+// normalised -> layer 0 (7 -> 128, GELU) -> three 128 -> 128 GELU layers -> 4
+// outputs.  Layer 0 and the output layer are thin and run on the CUDA cores in
+// FP32; the three 128 x 128 layers run on the tcgen05 tensor cores with BF16
+// operands staged in shared memory (128-byte swizzle) and FP32 accumulators in
+// TMEM.  GELU is the tanh form of Hendrycks & Gimpel evaluated with the
+// tanh.approx.f32 instruction.
+//
+// Kernels:
+//   k_mlp_fused<Io>   inference, persistent over tiles of 128 samples: the 3
+//                     hidden weight tiles stay in shared memory, activations
+//                     never leave the SM (inputs and outputs through Io);
+//   k_gemm<EPI>       training GEMMs, one 128 x 128 output tile per CTA, K in
+//                     chunks of 128, optional split-K: forward layers (bias +
+//                     GELU epilogue), backward data (x GELU' epilogue) and
+//                     weight gradients (FP32 partials);
+//   k_layer0, k_head, k_small_grads, k_reduce_dw, k_adam, k_pack: the thin
+//                     layers, the loss, the small reductions and Adam.
+// Every reduction has a fixed order, so gradients are reproducible run to run.
+#include <cuda_runtime.h>
+#include <cuda_bf16.h>
+
+#include <cmath>
+#include <cstdio>
+#include <string>
+#include <vector>
+
+#include "rc_dev.cuh"
+#include "rc_gpu.h"
+#include "rc_mlp.h"
+#include "rc_umma.cuh"
+
+namespace rc {
+namespace mlp {
+
+constexpr int H = 128, NIN = 7, NOUT = 4;
+constexpr int OFF_W0 = 0, OFF_B0 = H * NIN;
+__host__ __device__ constexpr int off_w(int l) { return H * NIN + H + (l - 1) * (H * H + H); }  // l = 1..3
+__host__ __device__ constexpr int off_b(int l) { return off_w(l) + H * H; }
+constexpr int OFF_W4 = off_w(4), OFF_B4 = OFF_W4 + NOUT * H, NPARAM = OFF_B4 + NOUT;
+static_assert(NPARAM == RC_MLP_NPARAM, "parameter layout");
+constexpr uint32_t IDESC = umma::idesc_bf16(128, 128);
+constexpr int TILE_BYTES = 128 * 128 * 2;
+
+struct Norm {
+  float mean[NIN], stdv[NIN];
+  float dom[6];  // T_lo, T_hi, p_lo, p_hi, dt_lo, dt_hi
+};
+
+__device__ __forceinline__ float tanh_fast(float x) {
+  float y;
+  asm("tanh.approx.f32 %0, %1;" : "=f"(y) : "f"(x));
+  return y;
+}
+constexpr float GK0 = 0.7978845608f, GK1 = 0.044715f;  // sqrt(2/pi), cubic coefficient
+__device__ __forceinline__ float gelu(float h) {
+  const float t = tanh_fast(GK0 * (h + GK1 * h * h * h));
+  return 0.5f * h * (1.f + t);
+}
+__device__ __forceinline__ float gelu_d(float h) {
+  const float t = tanh_fast(GK0 * (h + GK1 * h * h * h));
+  return 0.5f * (1.f + t) + 0.5f * h * (1.f - t * t) * GK0 * (1.f + 3.f * GK1 * h * h);
+}
+__device__ __forceinline__ uint32_t bf2(float a, float b) {
+  __nv_bfloat162 p = __floats2bfloat162_rn(a, b);
+  return *reinterpret_cast<uint32_t*>(&p);
+}
+__device__ __forceinline__ uint4 pack8(const float* v) {
+  return make_uint4(bf2(v[0], v[1]), bf2(v[2], v[3]), bf2(v[4], v[5]), bf2(v[6], v[7]));
+}
+// raw (T, p, Y1..Y4, dt) -> normalised features
+__device__ __forceinline__ void features(const float* raw, const Norm& nr, float* xn) {
+#pragma unroll
+  for (int i = 0; i < NIN; ++i) {
+    float f = raw[i];
+    if (i == 1 || i == 6) f = log10f(fmaxf(f, 1e-30f));
+    xn[i] = (f - nr.mean[i]) / nr.stdv[i];
+  }
+}
+
+// ------------------------------------------------------------ fused forward
+constexpr int FS_W0 = 4 * TILE_BYTES;                 // 3 weight tiles + activation tile
+constexpr int FS_BIAS = FS_W0 + H * NIN * 4;          // b0..b3
+constexpr int FS_W4 = FS_BIAS + 4 * H * 4;
+constexpr int FS_B4 = FS_W4 + NOUT * H * 4;
+constexpr int FS_BAR = FS_B4 + 16;
+constexpr int FS_SLOT = FS_BAR + 8;
+constexpr int FS_OK = FS_SLOT + 4;
+constexpr int FUSED_SMEM = FS_OK + 4 + 1024;          // + alignment slack
+static_assert(FS_BAR % 8 == 0, "mbarrier alignment");
+
+template <class Io>
+__global__ void __launch_bounds__(128, 1) k_mlp_fused(const float* __restrict__ params,
+                                                      const __nv_bfloat16* __restrict__ Wb, Norm nr, Io io, int n,
+                                                      unsigned* err) {
+  extern __shared__ uint8_t smem_raw[];
+  uint8_t* base = smem_raw + ((1024u - (umma::smem_u32(smem_raw) & 1023u)) & 1023u);
+  const uint32_t sbase = umma::smem_u32(base);
+  float* W0 = reinterpret_cast<float*>(base + FS_W0);
+  float* bias = reinterpret_cast<float*>(base + FS_BIAS);
+  float* W4 = reinterpret_cast<float*>(base + FS_W4);
+  float* b4 = reinterpret_cast<float*>(base + FS_B4);
+  uint64_t* bar = reinterpret_cast<uint64_t*>(base + FS_BAR);
+  uint32_t* slot = reinterpret_cast<uint32_t*>(base + FS_SLOT);
+  int* s_ok = reinterpret_cast<int*>(base + FS_OK);
+  const int t = threadIdx.x, warp = t >> 5;
+
+  // the three hidden-layer weight tiles (B operands: row = output, K = input)
+  for (int q = t; q < 3 * 2048; q += 128) {
+    const int l = q >> 11, r = (q >> 4) & 127, c = q & 15;
+    const uint4 v = reinterpret_cast<const uint4*>(Wb)[q];
+    *reinterpret_cast<uint4*>(base + l * TILE_BYTES + umma::sw128_offset(r, c * 8, 128)) = v;
+  }
+  for (int q = t; q < H * NIN; q += 128) W0[q] = params[OFF_W0 + q];
+  for (int q = t; q < H; q += 128) {
+    bias[q] = params[OFF_B0 + q];
+    for (int l = 1; l <= 3; ++l) bias[l * H + q] = params[off_b(l) + q];
+  }
+  for (int q = t; q < NOUT * H; q += 128) W4[q] = params[OFF_W4 + q];
+  if (t < NOUT) b4[t] = params[OFF_B4 + t];
+  if (t == 0) umma::mbar_init(bar, 1);
+  if (warp == 0) {
+    umma::tmem_alloc(slot, 128);
+    umma::tmem_relinquish();
+  }
+  umma::tc_fence_before();
+  __syncthreads();
+  umma::tc_fence_after();
+  const uint32_t tmem = *slot;
+  const uint32_t act = sbase + 3 * TILE_BYTES;
+  uint8_t* actp = base + 3 * TILE_BYTES;
+  uint32_t phase = 0;
+  bool ok = true;
+  const int ntiles = (n + 127) / 128;
+  for (int tile = blockIdx.x; tile < ntiles && ok; tile += gridDim.x) {
+    const int s = tile * 128 + t;
+    float xn[NIN];
+    typename Io::Local loc;
+    io.load(s, s < n, nr, xn, loc);
+    // layer 0 on the CUDA cores -> row t of the activation tile
+    for (int c8 = 0; c8 < 16; ++c8) {
+      float a[8];
+#pragma unroll
+      for (int e = 0; e < 8; ++e) {
+        const int o = c8 * 8 + e;
+        float h = bias[o];
+#pragma unroll
+        for (int i = 0; i < NIN; ++i) h = fmaf(W0[o * NIN + i], xn[i], h);
+        a[e] = gelu(h);
+      }
+      *reinterpret_cast<uint4*>(actp + umma::sw128_offset(t, c8 * 8, 128)) = pack8(a);
+    }
+    float out[NOUT] = {0.f, 0.f, 0.f, 0.f};
+    for (int l = 1; l <= 3; ++l) {
+      umma::fence_async_smem();
+      umma::tc_fence_before();
+      __syncthreads();
+      if (t == 0) {
+        umma::tc_fence_after();
+#pragma unroll
+        for (int kk = 0; kk < 8; ++kk)
+          umma::mma_bf16(tmem, umma::sdesc_k(act, 128, kk), umma::sdesc_k(sbase + (l - 1) * TILE_BYTES, 128, kk),
+                         IDESC, kk > 0 ? 1u : 0u);
+        umma::mma_commit(bar);
+        *s_ok = umma::mbar_wait(bar, phase) ? 1 : 0;
+      }
+      __syncthreads();
+      phase ^= 1u;
+      umma::tc_fence_after();
+      if (!*s_ok) { ok = false; break; }
+      const float* bl = bias + l * H;
+      for (int c = 0; c < 4; ++c) {
+        float v[32];
+        umma::tmem_ld32(tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)(c * 32), v);
+        if (l < 3) {
+#pragma unroll
+          for (int c8 = 0; c8 < 4; ++c8) {
+            float a[8];
+#pragma unroll
+            for (int e = 0; e < 8; ++e) a[e] = gelu(v[c8 * 8 + e] + bl[c * 32 + c8 * 8 + e]);
+            *reinterpret_cast<uint4*>(actp + umma::sw128_offset(t, c * 32 + c8 * 8, 128)) = pack8(a);
+          }
+        } else {
+#pragma unroll
+          for (int j = 0; j < 32; ++j) {
+            const float a = gelu(v[j] + bl[c * 32 + j]);
+#pragma unroll
+            for (int m = 0; m < NOUT; ++m) out[m] = fmaf(a, W4[m * H + c * 32 + j], out[m]);
+          }
+        }
+      }
+    }
+    if (!ok) break;
+#pragma unroll
+    for (int m = 0; m < NOUT; ++m) out[m] += b4[m];
+    io.store(s, s < n, out, loc);
+  }
+  if (!ok && t == 0) atomicOr(err, ERR_SYNC);
+  umma::tc_fence_before();
+  __syncthreads();
+  if (warp == 0) {
+    umma::tc_fence_after();
+    umma::tmem_dealloc(tmem, 128);
+  }
+}
+
+// raw features in, outputs out (row-major n x 7 / n x 4)
+struct IoRaw {
+  const float* x;
+  float* y;
+  struct Local {};
+  __device__ void load(int s, bool valid, const Norm& nr, float* xn, Local&) const {
+    float raw[NIN];
+#pragma unroll
+    for (int i = 0; i < NIN; ++i) raw[i] = valid ? x[(size_t)s * NIN + i] : nr.mean[i];
+    if (!valid) { raw[1] = 1.f; raw[6] = 1.f; }
+    features(raw, nr, xn);
+  }
+  __device__ void store(int s, bool valid, const float* out, const Local&) const {
+    if (valid)
+#pragma unroll
+      for (int m = 0; m < NOUT; ++m) y[(size_t)s * NOUT + m] = out[m];
+  }
+};
+
+// The surrogate source of the steady iteration: cell s of the solver.  The
+// explicit rate omega_k and rho come from the FP64 state (production,
+// sourceterm.f90:2-70); the network gives the mean-rate ratios r_k, and
+// src_k = vol * r_k * omega_k (= vol * rho * dY_k / step).  A cell is handed to
+// the FP64 integrator instead (appended to `list`) when its state lies outside
+// the training domain, when the ratios of the reacting species disagree by
+// more than spread_tol (one global reaction: they are equal for the exact
+// integrator), when the mean ratio is outside [-0.01, 3], or when Y + dY
+// leaves [0, 1] by more than 1e-6.
+struct IoSolver {
+  Dev d;
+  ThermoDev<4> th;
+  float spread_tol;
+  int* list;
+  unsigned* nlist;
+  unsigned* nsurr;
+  struct Local {
+    double om[4], Y[4], dt, rho, vol;
+    bool dom;
+  };
+  __device__ void load(int i, bool valid, const Norm& nr, float* xn, Local& L) const {
+    const int NE = d.NE;
+    float raw[NIN];
+    if (!valid) {
+      for (int k = 0; k < NIN; ++k) raw[k] = nr.mean[k];
+      raw[1] = 1.f; raw[6] = 1.f;
+      features(raw, nr, xn);
+      L.dom = false;
+      return;
+    }
+    unsigned e = 0;
+    const double p = d.PA[i], T = d.PA[3 * NE + i];
+    double s = 0.0;
+#pragma unroll
+    for (int k = 0; k < 3; ++k) { L.Y[k] = d.PA[(4 + k) * NE + i]; s = s + L.Y[k]; }
+    L.Y[3] = 1.0 - s;
+    double Cp, gama, R;
+    gas<4>(th, L.Y, T, Cp, gama, R, e);
+    L.rho = p / (T * R);
+    production<4>(th, T, L.rho, L.Y, L.om);
+    L.dt = d.step[i];
+    L.vol = d.vol[i];
+    L.dom = e == 0 && T >= nr.dom[0] && T <= nr.dom[1] && p >= nr.dom[2] && p <= nr.dom[3] && L.dt >= nr.dom[4] &&
+            L.dt <= nr.dom[5];
+    raw[0] = (float)T; raw[1] = (float)p;
+#pragma unroll
+    for (int k = 0; k < 4; ++k) raw[2 + k] = (float)L.Y[k];
+    raw[6] = (float)L.dt;
+    features(raw, nr, xn);
+  }
+  __device__ void store(int i, bool valid, const float* r, const Local& L) const {
+    if (!valid) return;
+    const int NE = d.NE;
+    bool any = false;
+#pragma unroll
+    for (int k = 0; k < 3; ++k) any = any || L.om[k] != 0.0;
+    if (!any) {
+#pragma unroll
+      for (int k = 0; k < 3; ++k) d.src[k * NE + i] = 0.0;
+      atomicAdd(nsurr, 1u);
+      return;
+    }
+    const float rbar = (r[0] + r[1] + r[2]) * (1.f / 3.f);
+    float spread = 0.f;
+#pragma unroll
+    for (int k = 0; k < 3; ++k) spread = fmaxf(spread, fabsf(r[k] - rbar));
+    bool fall = !L.dom || !(spread <= spread_tol) || !(rbar >= -0.01f && rbar <= 3.f);
+    double src[3];
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+      const double dY = (double)r[k] * L.dt * L.om[k] / L.rho;
+      const double Yn = L.Y[k] + dY;
+      fall = fall || !(Yn >= -1e-6 && Yn <= 1.0 + 1e-6);
+      src[k] = L.vol * ((double)r[k] * L.om[k]);
+    }
+    if (fall) {
+      const unsigned slot = atomicAdd(nlist, 1u);
+      list[slot] = i;
+      return;
+    }
+    atomicAdd(nsurr, 1u);
+#pragma unroll
+    for (int k = 0; k < 3; ++k) d.src[k * NE + i] = src[k];
+  }
+};
+
+// -------------------------------------------------------- training kernels --
+struct GemmArgs {
+  const __nv_bfloat16* A; int lda;   // M x K, K contiguous
+  const __nv_bfloat16* B; int ldb;   // N x K, K contiguous
+  int M, N, K;                       // multiples of 128; K split evenly over gridDim.z
+  const float* bias;                 // EPI_FWD [N]
+  const float* Hin;                  // EPI_BWD pre-activation [M][N]
+  float* Hout;                       // EPI_FWD pre-activation [M][N]
+  __nv_bfloat16* Orow;               // [M][N]
+  __nv_bfloat16* Ocol;               // [N][M]
+  float* C;                          // EPI_F32 [gridDim.z][M][N]
+  unsigned* err;
+};
+enum { EPI_FWD = 0, EPI_BWD = 1, EPI_F32 = 2 };
+constexpr int GS_BAR = 2 * TILE_BYTES, GS_SLOT = GS_BAR + 8, GS_OK = GS_SLOT + 4, GEMM_SMEM = GS_OK + 4 + 1024;
+
+template <int EPI>
+__global__ void __launch_bounds__(128) k_gemm(GemmArgs g) {
+  extern __shared__ uint8_t smem_raw[];
+  uint8_t* base = smem_raw + ((1024u - (umma::smem_u32(smem_raw) & 1023u)) & 1023u);
+  const uint32_t sA = umma::smem_u32(base), sB = sA + TILE_BYTES;
+  uint64_t* bar = reinterpret_cast<uint64_t*>(base + GS_BAR);
+  uint32_t* slot = reinterpret_cast<uint32_t*>(base + GS_SLOT);
+  int* s_ok = reinterpret_cast<int*>(base + GS_OK);
+  const int t = threadIdx.x, warp = t >> 5;
+  const int m0 = blockIdx.y * 128, n0 = blockIdx.x * 128;
+  const int kper = g.K / gridDim.z, kb = blockIdx.z * kper;
+  if (t == 0) umma::mbar_init(bar, 1);
+  if (warp == 0) {
+    umma::tmem_alloc(slot, 128);
+    umma::tmem_relinquish();
+  }
+  umma::tc_fence_before();
+  __syncthreads();
+  umma::tc_fence_after();
+  const uint32_t tmem = *slot;
+  uint32_t phase = 0;
+  bool ok = true;
+  for (int k0 = kb; k0 < kb + kper; k0 += 128) {
+    for (int q = t; q < 2048; q += 128) {
+      const int r = q >> 4, c = q & 15;
+      const uint4 va = *reinterpret_cast<const uint4*>(g.A + (size_t)(m0 + r) * g.lda + k0 + c * 8);
+      const uint4 vb = *reinterpret_cast<const uint4*>(g.B + (size_t)(n0 + r) * g.ldb + k0 + c * 8);
+      *reinterpret_cast<uint4*>(base + umma::sw128_offset(r, c * 8, 128)) = va;
+      *reinterpret_cast<uint4*>(base + TILE_BYTES + umma::sw128_offset(r, c * 8, 128)) = vb;
+    }
+    umma::fence_async_smem();
+    umma::tc_fence_before();
+    __syncthreads();
+    if (t == 0) {
+      umma::tc_fence_after();
+#pragma unroll
+      for (int kk = 0; kk < 8; ++kk)
+        umma::mma_bf16(tmem, umma::sdesc_k(sA, 128, kk), umma::sdesc_k(sB, 128, kk), IDESC,
+                       (k0 > kb || kk > 0) ? 1u : 0u);
+      umma::mma_commit(bar);
+      *s_ok = umma::mbar_wait(bar, phase) ? 1 : 0;
+    }
+    __syncthreads();
+    phase ^= 1u;
+    umma::tc_fence_after();
+    if (!*s_ok) { ok = false; break; }
+  }
+  if (ok) {
+    const int m = m0 + warp * 32 + (t & 31);
+    for (int c = 0; c < 4; ++c) {
+      float v[32];
+      umma::tmem_ld32(tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)(c * 32), v);
+      const int nc = n0 + c * 32;
+      if (EPI == EPI_F32) {
+        float* dst = g.C + (size_t)blockIdx.z * g.M * g.N + (size_t)m * g.N + nc;
+#pragma unroll
+        for (int j = 0; j < 32; j += 4) *reinterpret_cast<float4*>(dst + j) = make_float4(v[j], v[j + 1], v[j + 2], v[j + 3]);
+      } else {
+        float o[32];
+        if (EPI == EPI_FWD) {
+          float* hd = g.Hout + (size_t)m * g.N + nc;
+#pragma unroll
+          for (int j = 0; j < 32; ++j) {
+            const float h = v[j] + g.bias[nc + j];
+            hd[j] = h;
+            o[j] = gelu(h);
+          }
+        } else {
+          const float* hs = g.Hin + (size_t)m * g.N + nc;
+#pragma unroll
+          for (int j = 0; j < 32; ++j) o[j] = v[j] * gelu_d(hs[j]);
+        }
+        uint4* rd = reinterpret_cast<uint4*>(g.Orow + (size_t)m * g.N + nc);
+#pragma unroll
+        for (int j = 0; j < 4; ++j) rd[j] = pack8(o + 8 * j);
+#pragma unroll
+        for (int j = 0; j < 32; ++j) g.Ocol[(size_t)(nc + j) * g.M + m] = __float2bfloat16_rn(o[j]);
+      }
+    }
+  } else if (t == 0) {
+    atomicOr(g.err, ERR_SYNC);
+  }
+  umma::tc_fence_before();
+  __syncthreads();
+  if (warp == 0) {
+    umma::tc_fence_after();
+    umma::tmem_dealloc(tmem, 128);
+  }
+}
+
+// layer 0 for a training batch: xn (n x 7), H0 (n x 128 FP32), A0 row / column (BF16)
+__global__ void k_layer0(const float* __restrict__ x, Norm nr, const float* __restrict__ P, int n, float* xn,
+                         float* H0, __nv_bfloat16* Arow, __nv_bfloat16* Acol) {
+  const int s = blockIdx.x * blockDim.x + threadIdx.x;
+  if (s >= n) return;
+  float f[NIN];
+  features(x + (size_t)s * NIN, nr, f);
+#pragma unroll
+  for (int i = 0; i < NIN; ++i) xn[(size_t)s * NIN + i] = f[i];
+  for (int c8 = 0; c8 < 16; ++c8) {
+    float a[8];
+    for (int e = 0; e < 8; ++e) {
+      const int o = c8 * 8 + e;
+      float h = P[OFF_B0 + o];
+#pragma unroll
+      for (int i = 0; i < NIN; ++i) h = fmaf(P[OFF_W0 + o * NIN + i], f[i], h);
+      H0[(size_t)s * H + o] = h;
+      a[e] = gelu(h);
+      Acol[(size_t)o * n + s] = __float2bfloat16_rn(a[e]);
+    }
+    reinterpret_cast<uint4*>(Arow + (size_t)s * H)[c8] = pack8(a);
+  }
+}
+
+// output layer, loss and its gradient down to dH3: y = W4 gelu(H3) + b4,
+// L = mean((y - t)^2) over n x 4, dy = 2 (y - t) / (4 n)
+constexpr int HEAD_THREADS = 128;
+__global__ void __launch_bounds__(HEAD_THREADS) k_head(const float* __restrict__ H3, const float* __restrict__ tgt,
+                                                       const float* __restrict__ P, int n, float* dy,
+                                                       __nv_bfloat16* dHrow, __nv_bfloat16* dHcol, float* loss_part) {
+  __shared__ float red[HEAD_THREADS];
+  const int s = blockIdx.x * blockDim.x + threadIdx.x;
+  float l2 = 0.f;
+  if (s < n) {
+    const float* h = H3 + (size_t)s * H;
+    float y[NOUT];
+#pragma unroll
+    for (int m = 0; m < NOUT; ++m) y[m] = 0.f;
+    for (int i = 0; i < H; ++i) {
+      const float a = gelu(h[i]);
+#pragma unroll
+      for (int m = 0; m < NOUT; ++m) y[m] = fmaf(a, P[OFF_W4 + m * H + i], y[m]);
+    }
+    float g[NOUT];
+    const float sc = 2.f / (4.f * (float)n);
+#pragma unroll
+    for (int m = 0; m < NOUT; ++m) {
+      const float e = y[m] + P[OFF_B4 + m] - tgt[(size_t)s * NOUT + m];
+      l2 = fmaf(e, e, l2);
+      g[m] = sc * e;
+      dy[(size_t)s * NOUT + m] = g[m];
+    }
+    for (int c8 = 0; c8 < 16; ++c8) {
+      float o[8];
+      for (int e = 0; e < 8; ++e) {
+        const int i = c8 * 8 + e;
+        float da = 0.f;
+#pragma unroll
+        for (int m = 0; m < NOUT; ++m) da = fmaf(P[OFF_W4 + m * H + i], g[m], da);
+        o[e] = da * gelu_d(h[i]);
+        dHcol[(size_t)i * n + s] = __float2bfloat16_rn(o[e]);
+      }
+      reinterpret_cast<uint4*>(dHrow + (size_t)s * H)[c8] = pack8(o);
+    }
+  }
+  red[threadIdx.x] = l2;
+  __syncthreads();
+  for (int w = HEAD_THREADS / 2; w > 0; w >>= 1) {
+    if (threadIdx.x < w) red[threadIdx.x] += red[threadIdx.x + w];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) loss_part[blockIdx.x] = red[0];
+}
+
+// gradients of W0, b0..b3, W4, b4 (one thread per parameter, samples in order)
+__global__ void k_small_grads(const float* __restrict__ xn, const __nv_bfloat16* __restrict__ dH0,
+                              const __nv_bfloat16* __restrict__ dH1, const __nv_bfloat16* __restrict__ dH2,
+                              const __nv_bfloat16* __restrict__ dH3, const float* __restrict__ H3,
+                              const float* __restrict__ dy, int n, float* grad) {
+  const int q = blockIdx.x * blockDim.x + threadIdx.x;
+  constexpr int NW0 = H * NIN, NB = 4 * H, NW4 = NOUT * H;
+  if (q < NW0) {
+    const int o = q / NIN, i = q % NIN;
+    float a = 0.f;
+    for (int s = 0; s < n; ++s) a = fmaf(__bfloat162float(dH0[(size_t)s * H + o]), xn[(size_t)s * NIN + i], a);
+    grad[OFF_W0 + q] = a;
+  } else if (q < NW0 + NB) {
+    const int l = (q - NW0) / H, o = (q - NW0) % H;
+    const __nv_bfloat16* d = l == 0 ? dH0 : l == 1 ? dH1 : l == 2 ? dH2 : dH3;
+    float a = 0.f;
+    for (int s = 0; s < n; ++s) a += __bfloat162float(d[(size_t)s * H + o]);
+    grad[(l == 0 ? OFF_B0 : off_b(l)) + o] = a;
+  } else if (q < NW0 + NB + NW4) {
+    const int m = (q - NW0 - NB) / H, i = (q - NW0 - NB) % H;
+    float a = 0.f;
+    for (int s = 0; s < n; ++s) a = fmaf(dy[(size_t)s * NOUT + m], gelu(H3[(size_t)s * H + i]), a);
+    grad[OFF_W4 + m * H + i] = a;
+  } else if (q < NW0 + NB + NW4 + NOUT) {
+    const int m = q - NW0 - NB - NW4;
+    float a = 0.f;
+    for (int s = 0; s < n; ++s) a += dy[(size_t)s * NOUT + m];
+    grad[OFF_B4 + m] = a;
+  }
+}
+
+// dW_l = sum over the split-K partials, in order
+__global__ void k_reduce_dw(const float* __restrict__ part, int z, float* grad) {
+  const int q = blockIdx.x * blockDim.x + threadIdx.x;
+  if (q >= 3 * H * H) return;
+  const int l = q / (H * H), e = q % (H * H);
+  const float* p = part + (size_t)l * z * H * H;
+  float a = 0.f;
+  for (int k = 0; k < z; ++k) a += p[(size_t)k * H * H + e];
+  grad[off_w(l + 1) + e] = a;
+}
+
+__global__ void k_loss_final(const float* part, int nb, int n, float* loss) {
+  if (threadIdx.x != 0 || blockIdx.x != 0) return;
+  float a = 0.f;
+  for (int b = 0; b < nb; ++b) a += part[b];
+  *loss = a / (4.f * (float)n);
+}
+
+__global__ void k_adam(float* p, float* m1, float* m2, const float* __restrict__ g, float lr, float b1, float b2,
+                       float eps, float bc1, float bc2) {
+  const int q = blockIdx.x * blockDim.x + threadIdx.x;
+  if (q >= NPARAM) return;
+  const float gq = g[q];
+  const float a = b1 * m1[q] + (1.f - b1) * gq;
+  const float b = b2 * m2[q] + (1.f - b2) * gq * gq;
+  m1[q] = a;
+  m2[q] = b;
+  p[q] -= lr * (a / bc1) / (sqrtf(b / bc2) + eps);
+}
+
+// BF16 copies of the hidden weights: Wb[l][o][i] and WbT[l][i][o]
+__global__ void k_pack(const float* __restrict__ p, __nv_bfloat16* Wb, __nv_bfloat16* WbT) {
+  const int q = blockIdx.x * blockDim.x + threadIdx.x;
+  if (q >= 3 * H * H) return;
+  const int l = q / (H * H), o = (q % (H * H)) / H, i = q % H;
+  const __nv_bfloat16 w = __float2bfloat16_rn(p[off_w(l + 1) + o * H + i]);
+  Wb[q] = w;
+  WbT[(size_t)l * H * H + i * H + o] = w;
+}
+
+}  // namespace mlp
+
+// samples for training: raw features (T, p, Y1..Y4, dt) and targets r_k from
+// pairs of states (P before, P after dt) given in SoA layout
+__global__ void k_surrogate_samples(const ThermoDev<4> th, const double* __restrict__ P0,
+                                    const double* __restrict__ P1, const double* __restrict__ dt, int n, float* x,
+                                    float* tgt) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  unsigned e = 0;
+  double Y[4], s = 0.0, Cp, gama, R, om[4];
+  for (int k = 0; k < 3; ++k) { Y[k] = P0[(size_t)(4 + k) * n + i]; s = s + Y[k]; }
+  Y[3] = 1.0 - s;
+  const double p = P0[i], T = P0[(size_t)3 * n + i];
+  gas<4>(th, Y, T, Cp, gama, R, e);
+  const double rho = p / (T * R);
+  production<4>(th, T, rho, Y, om);
+  float* xi = x + (size_t)i * 7;
+  xi[0] = (float)T; xi[1] = (float)p;
+  for (int k = 0; k < 4; ++k) xi[2 + k] = (float)Y[k];
+  xi[6] = (float)dt[i];
+  for (int k = 0; k < 4; ++k) {
+    float r = 1.f;
+    if (k < 3 && om[k] != 0.0) {
+      const double dY = P1[(size_t)(4 + k) * n + i] - P0[(size_t)(4 + k) * n + i];
+      r = (float)(dY / (dt[i] * om[k] / rho));
+    }
+    tgt[(size_t)i * 4 + k] = r;
+  }
+}
+
+}  // namespace rc
+
+using namespace rc;
+
+struct rc_mlp {
+  int device = 0;
+  float* params = nullptr;
+  float* m1 = nullptr;
+  float* m2 = nullptr;
+  __nv_bfloat16* Wb = nullptr;
+  __nv_bfloat16* WbT = nullptr;
+  unsigned* derr = nullptr;
+  mlp::Norm norm{};
+  int step = 0;
+  // training work buffers for up to cap samples
+  int cap = 0, zsplit = 1;
+  std::vector<void*> work;
+  float *xn = nullptr, *Hs[4] = {}, *dy = nullptr, *loss_part = nullptr, *loss = nullptr, *part = nullptr,
+        *grad = nullptr;
+  __nv_bfloat16 *Arow[3] = {}, *Acol[3] = {}, *dHrow[4] = {}, *dHcol[4] = {};
+  std::string err;
+};
+
+namespace {
+
+int mlp_fail(rc_mlp* m, cudaError_t e, const char* what) {
+  if (e == cudaSuccess) return RC_OK;
+  if (m) m->err = std::string(what) + ": " + cudaGetErrorString(e);
+  return RC_ERR_CUDA;
+}
+#define MLP_CU(call)                                          \
+  do {                                                        \
+    cudaError_t e_ = (call);                                  \
+    if (e_ != cudaSuccess) return mlp_fail(m, e_, #call);     \
+  } while (0)
+
+int fused_grid(rc_mlp* m, int n) {
+  int nsm = 0;
+  cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, m->device);
+  const int tiles = (n + 127) / 128;
+  return tiles < nsm ? (tiles > 0 ? tiles : 1) : nsm;
+}
+
+template <class T>
+int alloc_work(rc_mlp* m, size_t count, T** out) {
+  void* p = nullptr;
+  MLP_CU(cudaMalloc(&p, std::max<size_t>(count, 1) * sizeof(T)));
+  m->work.push_back(p);
+  *out = static_cast<T*>(p);
+  return RC_OK;
+}
+
+int ensure_work(rc_mlp* m, int n) {
+  if (n <= m->cap) return RC_OK;
+  for (void* p : m->work) cudaFree(p);
+  m->work.clear();
+  const size_t N = (size_t)n, Hh = mlp::H;
+  int st = 0;
+  st |= alloc_work(m, N * mlp::NIN, &m->xn);
+  for (int l = 0; l < 4; ++l) st |= alloc_work(m, N * Hh, &m->Hs[l]);
+  for (int l = 0; l < 3; ++l) {
+    st |= alloc_work(m, N * Hh, &m->Arow[l]);
+    st |= alloc_work(m, N * Hh, &m->Acol[l]);
+  }
+  for (int l = 0; l < 4; ++l) {
+    st |= alloc_work(m, N * Hh, &m->dHrow[l]);
+    st |= alloc_work(m, N * Hh, &m->dHcol[l]);
+  }
+  st |= alloc_work(m, N * mlp::NOUT, &m->dy);
+  st |= alloc_work(m, (N + 127) / 128, &m->loss_part);
+  st |= alloc_work(m, (size_t)1, &m->loss);
+  // split-K partials of the weight gradients, for up to n / 1024 splits
+  m->zsplit = std::max(1, n / 1024);
+  st |= alloc_work(m, (size_t)3 * m->zsplit * Hh * Hh, &m->part);
+  if (st) return st;
+  m->cap = n;
+  return RC_OK;
+}
+
+}  // namespace
+
+namespace rc {
+// inference over the cells of a solver context (NSP must be 4)
+cudaError_t surrogate_source(const Dev& d, const void* th, const rc_mlp* net, float spread_tol, int* list,
+                             unsigned* nlist, unsigned* nsurr, cudaStream_t s) {
+  int nsm = 0;
+  cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, net->device);
+  const int tiles = (d.NE + 127) / 128;
+  const int grid = tiles < nsm ? tiles : nsm;
+  mlp::IoSolver io{d, *static_cast<const ThermoDev<4>*>(th), spread_tol, list, nlist, nsurr};
+  mlp::k_mlp_fused<mlp::IoSolver><<<grid > 0 ? grid : 1, 128, mlp::FUSED_SMEM, s>>>(net->params, net->Wb, net->norm,
+                                                                                    io, d.NE, d.err);
+  return cudaGetLastError();
+}
+// outside stream capture, once per context
+cudaError_t surrogate_prepare() {
+  return cudaFuncSetAttribute(mlp::k_mlp_fused<mlp::IoSolver>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                              mlp::FUSED_SMEM);
+}
+cudaError_t surrogate_samples(const void* th, const double* P0, const double* P1, const double* dt, int n, float* x,
+                              float* t, cudaStream_t s) {
+  k_surrogate_samples<<<(n + 127) / 128, 128, 0, s>>>(*static_cast<const ThermoDev<4>*>(th), P0, P1, dt, n, x, t);
+  return cudaGetLastError();
+}
+}  // namespace rc
+
+extern "C" {
+
+int rc_mlp_create(int device, rc_mlp** out) {
+  if (!out) return RC_ERR_ARG;
+  *out = nullptr;
+  rc_mlp* m = new rc_mlp();
+  m->device = device;
+  auto bail = [&](int st) {
+    rc_mlp_destroy(m);
+    return st;
+  };
+  if (cudaSetDevice(device) != cudaSuccess) return bail(RC_ERR_CUDA);
+  const size_t P = mlp::NPARAM;
+  if (cudaMalloc(&m->params, P * sizeof(float)) != cudaSuccess || cudaMalloc(&m->m1, P * sizeof(float)) != cudaSuccess ||
+      cudaMalloc(&m->m2, P * sizeof(float)) != cudaSuccess || cudaMalloc(&m->grad, P * sizeof(float)) != cudaSuccess ||
+      cudaMalloc(&m->Wb, 3 * mlp::H * mlp::H * sizeof(__nv_bfloat16)) != cudaSuccess ||
+      cudaMalloc(&m->WbT, 3 * mlp::H * mlp::H * sizeof(__nv_bfloat16)) != cudaSuccess ||
+      cudaMalloc(&m->derr, sizeof(unsigned)) != cudaSuccess)
+    return bail(RC_ERR_CUDA);
+  cudaMemset(m->params, 0, P * sizeof(float));
+  cudaMemset(m->m1, 0, P * sizeof(float));
+  cudaMemset(m->m2, 0, P * sizeof(float));
+  cudaMemset(m->derr, 0, sizeof(unsigned));
+  for (int i = 0; i < mlp::NIN; ++i) { m->norm.mean[i] = 0.f; m->norm.stdv[i] = 1.f; }
+  const float dom[6] = {300.f, 3800.f, 5.0e4f, 1.0e7f, 1.0e-9f, 1.0e-5f};
+  for (int i = 0; i < 6; ++i) m->norm.dom[i] = dom[i];
+  if (cudaFuncSetAttribute(mlp::k_mlp_fused<mlp::IoRaw>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                           mlp::FUSED_SMEM) != cudaSuccess ||
+      cudaFuncSetAttribute(mlp::k_gemm<mlp::EPI_FWD>, cudaFuncAttributeMaxDynamicSharedMemorySize, mlp::GEMM_SMEM) !=
+          cudaSuccess ||
+      cudaFuncSetAttribute(mlp::k_gemm<mlp::EPI_BWD>, cudaFuncAttributeMaxDynamicSharedMemorySize, mlp::GEMM_SMEM) !=
+          cudaSuccess ||
+      cudaFuncSetAttribute(mlp::k_gemm<mlp::EPI_F32>, cudaFuncAttributeMaxDynamicSharedMemorySize, mlp::GEMM_SMEM) !=
+          cudaSuccess)
+    return bail(RC_ERR_CUDA);
+  *out = m;
+  return RC_OK;
+}
+
+int rc_mlp_destroy(rc_mlp* m) {
+  if (!m) return RC_OK;
+  for (void* p : m->work) cudaFree(p);
+  cudaFree(m->params); cudaFree(m->m1); cudaFree(m->m2); cudaFree(m->grad);
+  cudaFree(m->Wb); cudaFree(m->WbT); cudaFree(m->derr);
+  delete m;
+  return RC_OK;
+}
+
+const char* rc_mlp_last_error(rc_mlp* m) { return m ? m->err.c_str() : "no network"; }
+
+int rc_mlp_set_params(rc_mlp* m, const float* params) {
+  if (!m || !params) return RC_ERR_ARG;
+  MLP_CU(cudaMemcpy(m->params, params, sizeof(float) * mlp::NPARAM, cudaMemcpyHostToDevice));
+  MLP_CU(cudaMemset(m->m1, 0, sizeof(float) * mlp::NPARAM));
+  MLP_CU(cudaMemset(m->m2, 0, sizeof(float) * mlp::NPARAM));
+  m->step = 0;
+  mlp::k_pack<<<(3 * mlp::H * mlp::H + 255) / 256, 256>>>(m->params, m->Wb, m->WbT);
+  MLP_CU(cudaGetLastError());
+  MLP_CU(cudaDeviceSynchronize());
+  return RC_OK;
+}
+
+int rc_mlp_get_params(rc_mlp* m, float* params) {
+  if (!m || !params) return RC_ERR_ARG;
+  MLP_CU(cudaMemcpy(params, m->params, sizeof(float) * mlp::NPARAM, cudaMemcpyDeviceToHost));
+  return RC_OK;
+}
+
+int rc_mlp_set_norm(rc_mlp* m, const float* mean, const float* stdv, const float* domain) {
+  if (!m || !mean || !stdv) return RC_ERR_ARG;
+  for (int i = 0; i < mlp::NIN; ++i) {
+    if (!(stdv[i] > 0.f)) return RC_ERR_ARG;
+    m->norm.mean[i] = mean[i];
+    m->norm.stdv[i] = stdv[i];
+  }
+  if (domain)
+    for (int i = 0; i < 6; ++i) m->norm.dom[i] = domain[i];
+  return RC_OK;
+}
+
+int rc_mlp_forward(rc_mlp* m, const float* d_x, int n, float* d_y, void* stream) {
+  if (!m || n < 0 || (n > 0 && (!d_x || !d_y))) return RC_ERR_ARG;
+  if (n == 0) return RC_OK;
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  mlp::IoRaw io{d_x, d_y};
+  mlp::k_mlp_fused<mlp::IoRaw><<<fused_grid(m, n), 128, mlp::FUSED_SMEM, s>>>(m->params, m->Wb, m->norm, io, n,
+                                                                              m->derr);
+  MLP_CU(cudaGetLastError());
+  return RC_OK;
+}
+
+int rc_mlp_gradient(rc_mlp* m, const float* d_x, const float* d_t, int n, float* d_grad, float* loss,
+                    void* stream) {
+  if (!m || !d_x || !d_t || !d_grad || n <= 0 || n % 128) return RC_ERR_ARG;
+  if (int st = ensure_work(m, n)) return st;
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  using namespace mlp;
+  // split-K of the weight gradients: about 8 chunks of 128 samples per CTA,
+  // an exact divisor of the n / 128 chunks (each split a whole number of chunks)
+  int z = std::max(1, std::min(m->zsplit, n / 1024));
+  while ((n / 128) % z) --z;
+  k_layer0<<<(n + 127) / 128, 128, 0, s>>>(d_x, m->norm, m->params, n, m->xn, m->Hs[0], m->Arow[0], m->Acol[0]);
+  // hidden layers 1..3 forward: H_l = A_{l-1} W_l^T + b_l
+  for (int l = 1; l <= 3; ++l) {
+    GemmArgs g{};
+    g.A = m->Arow[l - 1]; g.lda = H;
+    g.B = m->Wb + (size_t)(l - 1) * H * H; g.ldb = H;
+    g.M = n; g.N = H; g.K = H;
+    g.bias = m->params + off_b(l);
+    g.Hout = m->Hs[l];
+    g.Orow = l < 3 ? m->Arow[l] : m->dHrow[3];   // A3 row is not needed (the head recomputes it)
+    g.Ocol = l < 3 ? m->Acol[l] : m->dHcol[3];   // scratch for l = 3, overwritten by the head
+    g.err = m->derr;
+    k_gemm<EPI_FWD><<<dim3(1, n / 128, 1), 128, GEMM_SMEM, s>>>(g);
+  }
+  k_head<<<(n + HEAD_THREADS - 1) / HEAD_THREADS, HEAD_THREADS, 0, s>>>(m->Hs[3], d_t, m->params, n, m->dy,
+                                                                         m->dHrow[3], m->dHcol[3], m->loss_part);
+  // backward data: dH_{l-1} = (dH_l W_l) * gelu'(H_{l-1})
+  for (int l = 3; l >= 1; --l) {
+    GemmArgs g{};
+    g.A = m->dHrow[l]; g.lda = H;
+    g.B = m->WbT + (size_t)(l - 1) * H * H; g.ldb = H;
+    g.M = n; g.N = H; g.K = H;
+    g.Hin = m->Hs[l - 1];
+    g.Orow = m->dHrow[l - 1];
+    g.Ocol = m->dHcol[l - 1];
+    g.err = m->derr;
+    k_gemm<EPI_BWD><<<dim3(1, n / 128, 1), 128, GEMM_SMEM, s>>>(g);
+  }
+  // weight gradients of the hidden layers: dW_l = dH_l^T A_{l-1} (split-K partials)
+  for (int l = 1; l <= 3; ++l) {
+    GemmArgs g{};
+    g.A = m->dHcol[l]; g.lda = n;
+    g.B = m->Acol[l - 1]; g.ldb = n;
+    g.M = H; g.N = H; g.K = n;
+    g.C = m->part + (size_t)(l - 1) * z * H * H;
+    g.err = m->derr;
+    k_gemm<EPI_F32><<<dim3(1, 1, z), 128, GEMM_SMEM, s>>>(g);
+  }
+  k_reduce_dw<<<(3 * H * H + 255) / 256, 256, 0, s>>>(m->part, z, d_grad);
+  const int nsmall = H * NIN + 4 * H + NOUT * H + NOUT;
+  k_small_grads<<<(nsmall + 127) / 128, 128, 0, s>>>(m->xn, m->dHrow[0], m->dHrow[1], m->dHrow[2], m->dHrow[3],
+                                                     m->Hs[3], m->dy, n, d_grad);
+  k_loss_final<<<1, 32, 0, s>>>(m->loss_part, (n + HEAD_THREADS - 1) / HEAD_THREADS, n, m->loss);
+  MLP_CU(cudaGetLastError());
+  if (loss) {
+    MLP_CU(cudaMemcpyAsync(loss, m->loss, sizeof(float), cudaMemcpyDeviceToHost, s));
+    unsigned e = 0;
+    MLP_CU(cudaMemcpyAsync(&e, m->derr, sizeof(unsigned), cudaMemcpyDeviceToHost, s));
+    MLP_CU(cudaStreamSynchronize(s));
+    if (e) {
+      m->err = "tensor-core wait gave up";
+      return (int)e;
+    }
+  }
+  return RC_OK;
+}
+
+int rc_mlp_adam(rc_mlp* m, const float* d_grad, float lr, float beta1, float beta2, float eps, void* stream) {
+  if (!m || !d_grad) return RC_ERR_ARG;
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  m->step += 1;
+  const float bc1 = 1.f - std::pow(beta1, (float)m->step), bc2 = 1.f - std::pow(beta2, (float)m->step);
+  mlp::k_adam<<<(mlp::NPARAM + 255) / 256, 256, 0, s>>>(m->params, m->m1, m->m2, d_grad, lr, beta1, beta2, eps, bc1,
+                                                       bc2);
+  mlp::k_pack<<<(3 * mlp::H * mlp::H + 255) / 256, 256, 0, s>>>(m->params, m->Wb, m->WbT);
+  MLP_CU(cudaGetLastError());
+  return RC_OK;
+}
+
+}  // extern "C"
