@@ -191,7 +191,7 @@ int rc_chem_integrate(rc_ctx* ctx, const double* d_P, const double* d_dt, int n,
 /* Learned surrogate of the integrator (needs Nsp = 4).  The network (rc_mlp.h)
  * is owned by the caller and must outlive its use.  A cell goes back to the
  * integrator when its state is outside the network's training domain, when
- * the predicted rate ratios of the reacting species differ by more than
+ * the predicted normalised changes of the reacting species differ by more than
  * spread_tol, or when the prediction leaves Y in [0, 1]. */
 struct rc_mlp;
 int rc_set_surrogate(rc_ctx* ctx, struct rc_mlp* net, double spread_tol);
@@ -199,7 +199,8 @@ int rc_set_surrogate(rc_ctx* ctx, struct rc_mlp* net, double spread_tol);
 int rc_surrogate_stats(rc_ctx* ctx, unsigned* n_surrogate, unsigned* n_fallback);
 /* Training pairs from integrated states: d_P0, d_P1 (NVar x n SoA, before and
  * after d_dt) -> raw features d_x (n x 7: T, p, Y_1..Y_4, dt) and targets d_t
- * (n x 4: mean-rate ratios).  Device pointers; on the context's stream. */
+ * (n x 4: the normalised changes z_k of rc_mlp.h).  Device pointers; on the
+ * context's stream. */
 int rc_surrogate_samples(rc_ctx* ctx, const double* d_P0, const double* d_P1, const double* d_dt, int n, float* d_x,
                          float* d_t);
 

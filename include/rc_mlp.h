@@ -1,12 +1,18 @@
 /*
  * rc_mlp.h -- the learned chemistry surrogate: a small MLP
- *   7 inputs (T, log10 p, Y_1..Y_4, log10 dt) -> 4 x 128 hidden (GELU) -> 4 outputs
+ *   7 inputs (T, p, Y_1..Y_4, dt) -> 4 x 128 hidden (GELU) -> 4 outputs
  * with BF16 weights and activations and FP32 accumulation on the tcgen05
  * tensor cores, trained on the GPU by the project's own forward, backward and
- * Adam kernels.  The outputs are, per species k, the ratio
- *   r_k = (dY_k / dt) / (omega_k(T, rho, Y) / rho)
- * of the mean reaction rate over dt (from the per-cell integrator) to the
- * explicit rate at the start of the step; dY_k = r_k * dt * omega_k / rho.
+ * Adam kernels.  The inputs enter as the features (1000/T, log10 p,
+ * log10(Y_k + 1e-10), log10 dt), normalised by a mean and standard deviation
+ * set with the network.  The outputs are, per species k,
+ *   z_k = dY_k / (c_k xi_s),
+ * the change over dt from the per-cell integrator normalised by the progress
+ * scale of the one global reaction: omega_k = c_k k_f (c_k = 1000 M_k
+ * (nu''_k - nu'_k)), and xi_s is the smaller of the explicit progress
+ * dt k_f / rho and the progress min(Y_k / -c_k) that exhausts the limiting
+ * reactant.  z_k is near 1 while the explicit rate holds and is the consumed
+ * fraction of the limiting reactant once it runs out.
  *
  * The reference has no surrogate and no chemistry integrator: both are new.
  * All d_* arguments are DEVICE pointers; stream may be null (default stream).
@@ -32,7 +38,7 @@ int rc_mlp_destroy(rc_mlp* net);
 /* host FP32 parameter vectors of RC_MLP_NPARAM values */
 int rc_mlp_set_params(rc_mlp* net, const float* params);
 int rc_mlp_get_params(rc_mlp* net, float* params);
-/* feature normalisation x_n = (x - mean) / std (7 + 7 values) and the
+/* feature normalisation x_n = (f - mean) / std (7 + 7 values, f the features) and the
  * training domain used by the surrogate's error indicator: T_lo, T_hi,
  * p_lo, p_hi, dt_lo, dt_hi (6 values, raw units) */
 int rc_mlp_set_norm(rc_mlp* net, const float* mean, const float* std, const float* domain);

@@ -44,9 +44,13 @@ def unpack(p):
 
 
 def features(x, mean, std):
-    f = np.array(x, dtype=np.float64)
-    f[:, 1] = np.log10(np.maximum(f[:, 1], 1e-30))
-    f[:, 6] = np.log10(np.maximum(f[:, 6], 1e-30))
+    """(T, p, Y_1..Y_4, dt) -> (1000/T, log10 p, log10(Y + 1e-10), log10 dt), normalised."""
+    x = np.asarray(x, dtype=np.float64)
+    f = np.empty_like(x)
+    f[:, 0] = 1000.0 / np.maximum(x[:, 0], 1.0)
+    f[:, 1] = np.log10(np.maximum(x[:, 1], 1e-30))
+    f[:, 2:6] = np.log10(np.maximum(x[:, 2:6], 0.0) + 1e-10)
+    f[:, 6] = np.log10(np.maximum(x[:, 6], 1e-30))
     return (f - mean) / std
 
 

@@ -1,7 +1,7 @@
 // The learned chemistry surrogate (new; the reference has no counterpart).
 //
-// Network: 7 raw inputs (T, p, Y_1..Y_4, dt) -> features (T, log10 p, Y, log10 dt)
-// normalised -> layer 0 (7 -> 128, GELU) -> three 128 -> 128 GELU layers -> 4
+// Network: 7 raw inputs (T, p, Y_1..Y_4, dt) -> features (1000/T, log10 p,
+// log10(Y + 1e-10), log10 dt) normalised -> layer 0 (7 -> 128, GELU) -> three 128 -> 128 GELU layers -> 4
 // outputs.  Layer 0 and the output layer are thin and run on the CUDA cores in
 // FP32; the three 128 x 128 layers run on the tcgen05 tensor cores with BF16
 // operands staged in shared memory (128-byte swizzle) and FP32 accumulators in
@@ -70,12 +70,18 @@ __device__ __forceinline__ uint32_t bf2(float a, float b) {
 __device__ __forceinline__ uint4 pack8(const float* v) {
   return make_uint4(bf2(v[0], v[1]), bf2(v[2], v[3]), bf2(v[4], v[5]), bf2(v[6], v[7]));
 }
-// raw (T, p, Y1..Y4, dt) -> normalised features
+// raw (T, p, Y1..Y4, dt) -> normalised features (1000/T, log10 p,
+// log10(Y_k + 1e-10), log10 dt): in these the log of the Damkoehler number of
+// the global reaction is linear, so the mean-rate ratio is a smooth function
+// of one linear combination of the features.
+constexpr float YFLOOR = 1e-10f;
 __device__ __forceinline__ void features(const float* raw, const Norm& nr, float* xn) {
 #pragma unroll
   for (int i = 0; i < NIN; ++i) {
-    float f = raw[i];
-    if (i == 1 || i == 6) f = log10f(fmaxf(f, 1e-30f));
+    float f;
+    if (i == 0) f = 1000.f / fmaxf(raw[0], 1.f);
+    else if (i == 1 || i == 6) f = log10f(fmaxf(raw[i], 1e-30f));
+    else f = log10f(fmaxf(raw[i], 0.f) + YFLOOR);
     xn[i] = (f - nr.mean[i]) / nr.stdv[i];
   }
 }
@@ -225,15 +231,38 @@ struct IoRaw {
   }
 };
 
+// Progress scale of the one global reaction over dt: omega_k = c_k kf with
+// c_k = 1000 M_k (nu''_k - nu'_k) (production, chemical_kinetics.f90:109-165),
+// so dY_k = c_k xi for a progress xi.  The scale is the smaller of the
+// explicit progress dt kf / rho and the progress that exhausts the limiting
+// reactant, min_k(Y_k / -c_k) over c_k < 0; 0 when nothing reacts.  The
+// network's outputs are z_k = dY_k / (c_k xi_s): near 1 while the explicit
+// rate holds, the consumed fraction of the limiting reactant once it runs
+// out, so both ends stay O(1) and bounded.
+__device__ __forceinline__ double progress_scale(const ThermoDev<4>& th, const double* Y, const double* om,
+                                                 double dt, double rho) {
+  double kf = 0.0, xmax = 1e300;
+  bool react = false;
+#pragma unroll
+  for (int k = 0; k < 3; ++k)
+    if (th.prodc[k] < 0.0) {
+      react = true;
+      kf = om[k] / th.prodc[k];
+      xmax = fmin(xmax, fmax(Y[k], 0.0) / -th.prodc[k]);
+    }
+  if (!react) return 0.0;
+  return fmin(dt * kf / rho, xmax);
+}
+
 // The surrogate source of the steady iteration: cell s of the solver.  The
-// explicit rate omega_k and rho come from the FP64 state (production,
-// sourceterm.f90:2-70); the network gives the mean-rate ratios r_k, and
-// src_k = vol * r_k * omega_k (= vol * rho * dY_k / step).  A cell is handed to
-// the FP64 integrator instead (appended to `list`) when its state lies outside
-// the training domain, when the ratios of the reacting species disagree by
-// more than spread_tol (one global reaction: they are equal for the exact
-// integrator), when the mean ratio is outside [-0.01, 3], or when Y + dY
-// leaves [0, 1] by more than 1e-6.
+// explicit rate and rho come from the FP64 state (sourceterm.f90:2-70); the
+// network gives z_k, dY_k = z_k c_k xi_s (progress_scale) and
+// src_k = vol * rho * dY_k / step.  A cell is handed to the FP64 integrator
+// instead (appended to `list`) when its state lies outside the training
+// domain, when the z_k of the reacting species disagree by more than
+// spread_tol (one global reaction: they are equal for the exact integrator),
+// when their mean is outside [-0.01, 3], or when Y + dY leaves [0, 1] by more
+// than 1e-6.
 struct IoSolver {
   Dev d;
   ThermoDev<4> th;
@@ -242,7 +271,7 @@ struct IoSolver {
   unsigned* nlist;
   unsigned* nsurr;
   struct Local {
-    double om[4], Y[4], dt, rho, vol;
+    double Y[4], dt, rho, vol, xs;
     bool dom;
   };
   __device__ void load(int i, bool valid, const Norm& nr, float* xn, Local& L) const {
@@ -261,11 +290,12 @@ struct IoSolver {
 #pragma unroll
     for (int k = 0; k < 3; ++k) { L.Y[k] = d.PA[(4 + k) * NE + i]; s = s + L.Y[k]; }
     L.Y[3] = 1.0 - s;
-    double Cp, gama, R;
+    double Cp, gama, R, om[4];
     gas<4>(th, L.Y, T, Cp, gama, R, e);
     L.rho = p / (T * R);
-    production<4>(th, T, L.rho, L.Y, L.om);
+    production<4>(th, T, L.rho, L.Y, om);
     L.dt = d.step[i];
+    L.xs = progress_scale(th, L.Y, om, L.dt, L.rho);
     L.vol = d.vol[i];
     L.dom = e == 0 && T >= nr.dom[0] && T <= nr.dom[1] && p >= nr.dom[2] && p <= nr.dom[3] && L.dt >= nr.dom[4] &&
             L.dt <= nr.dom[5];
@@ -278,10 +308,7 @@ struct IoSolver {
   __device__ void store(int i, bool valid, const float* r, const Local& L) const {
     if (!valid) return;
     const int NE = d.NE;
-    bool any = false;
-#pragma unroll
-    for (int k = 0; k < 3; ++k) any = any || L.om[k] != 0.0;
-    if (!any) {
+    if (!(L.xs != 0.0)) {  // nothing reacts (or a reactant is exhausted)
 #pragma unroll
       for (int k = 0; k < 3; ++k) d.src[k * NE + i] = 0.0;
       atomicAdd(nsurr, 1u);
@@ -295,10 +322,10 @@ struct IoSolver {
     double src[3];
 #pragma unroll
     for (int k = 0; k < 3; ++k) {
-      const double dY = (double)r[k] * L.dt * L.om[k] / L.rho;
+      const double dY = (double)r[k] * th.prodc[k] * L.xs;
       const double Yn = L.Y[k] + dY;
       fall = fall || !(Yn >= -1e-6 && Yn <= 1.0 + 1e-6);
-      src[k] = L.vol * ((double)r[k] * L.om[k]);
+      src[k] = L.vol * (L.rho * (dY / L.dt));
     }
     if (fall) {
       const unsigned slot = atomicAdd(nlist, 1u);
@@ -564,7 +591,9 @@ __global__ void k_pack(const float* __restrict__ p, __nv_bfloat16* Wb, __nv_bflo
 
 }  // namespace mlp
 
-// samples for training: raw features (T, p, Y1..Y4, dt) and targets r_k from
+// samples for training: raw features (T, p, Y1..Y4, dt) and targets
+// z_k = dY_k / (c_k xi_s) (mlp::progress_scale; 1 where c_k xi_s is below
+// the rounding of Y_k) from
 // pairs of states (P before, P after dt) given in SoA layout
 __global__ void k_surrogate_samples(const ThermoDev<4> th, const double* __restrict__ P0,
                                     const double* __restrict__ P1, const double* __restrict__ dt, int n, float* x,
@@ -583,13 +612,17 @@ __global__ void k_surrogate_samples(const ThermoDev<4> th, const double* __restr
   xi[0] = (float)T; xi[1] = (float)p;
   for (int k = 0; k < 4; ++k) xi[2 + k] = (float)Y[k];
   xi[6] = (float)dt[i];
+  const double xs = mlp::progress_scale(th, Y, om, dt[i], rho);
   for (int k = 0; k < 4; ++k) {
-    float r = 1.f;
-    if (k < 3 && om[k] != 0.0) {
+    float z = 1.f;
+    const double sc = k < 3 ? th.prodc[k] * xs : 0.0;
+    // below 1e-10 of the mass fraction the change is lost in the rounding of
+    // Y and the explicit limit z = 1 is exact to that order
+    if (fabs(sc) > 1e-10 * fmax(fabs(Y[k]), 1e-3)) {
       const double dY = P1[(size_t)(4 + k) * n + i] - P0[(size_t)(4 + k) * n + i];
-      r = (float)(dY / (dt[i] * om[k] / rho));
+      z = (float)(dY / sc);
     }
-    tgt[(size_t)i * 4 + k] = r;
+    tgt[(size_t)i * 4 + k] = z;
   }
 }
 
@@ -723,7 +756,7 @@ int rc_mlp_create(int device, rc_mlp** out) {
   cudaMemset(m->m2, 0, P * sizeof(float));
   cudaMemset(m->derr, 0, sizeof(unsigned));
   for (int i = 0; i < mlp::NIN; ++i) { m->norm.mean[i] = 0.f; m->norm.stdv[i] = 1.f; }
-  const float dom[6] = {300.f, 3800.f, 5.0e4f, 1.0e7f, 1.0e-9f, 1.0e-5f};
+  const float dom[6] = {300.f, 6000.f, 1.0e2f, 2.0e7f, 1.0e-10f, 1.0e-4f};
   for (int i = 0; i < 6; ++i) m->norm.dom[i] = dom[i];
   if (cudaFuncSetAttribute(mlp::k_mlp_fused<mlp::IoRaw>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                            mlp::FUSED_SMEM) != cudaSuccess ||

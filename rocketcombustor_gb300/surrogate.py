@@ -1,7 +1,9 @@
 """Learned chemistry surrogate: host side of include/rc_mlp.h.
 
-The network maps (T, p, Y_1..Y_4, dt) to the mean-rate ratios
-r_k = (dY_k/dt) / (omega_k/rho) of the per-cell integrator; it is trained on
+The network maps (T, p, Y_1..Y_4, dt) to the normalised changes z_k of the
+per-cell integrator (include/rc_mlp.h: dY_k over the progress scale of the
+global reaction, the smaller of its explicit progress and the progress that
+exhausts the limiting reactant); it is trained on
 the GPU by the project's own kernels (forward, backward, Adam) on pairs the
 integrator produces from solver states.  Nothing here is in the reference.
 """
@@ -60,7 +62,7 @@ class MLP:
         self.set_params(init_params(seed))
         self.mean = np.zeros(NIN, dtype=np.float32)
         self.std = np.ones(NIN, dtype=np.float32)
-        self.domain = np.array([300.0, 3800.0, 5.0e4, 1.0e7, 1.0e-9, 1.0e-5], dtype=np.float32)
+        self.domain = np.array([*T_RANGE, *P_RANGE, *DT_RANGE], dtype=np.float32)
 
     def _check(self, st):
         if st:
@@ -84,15 +86,13 @@ class MLP:
         self._check(load().rc_mlp_set_norm(self.handle, _fp(self.mean), _fp(self.std), _fp(self.domain)))
 
     def fit_norm(self, x):
-        """Feature mean/std (T, log10 p, Y, log10 dt) of raw samples x (torch (n, 7))."""
-        import torch
-        f = x.double().clone()
-        f[:, 1] = torch.log10(f[:, 1].clamp_min(1e-30))
-        f[:, 6] = torch.log10(f[:, 6].clamp_min(1e-30))
+        """Feature mean/std of raw samples x (torch (n, 7)); the features are
+        (1000/T, log10 p, log10(Y_k + 1e-10), log10 dt)."""
+        f = features(x)
         m = f.mean(0).cpu().numpy()
         s = f.std(0).cpu().numpy()
         s = np.where(s > 1e-6, s, 1.0)
-        self.set_norm(m, s)
+        self.set_norm(m, s, self.domain)
 
     def forward(self, x):
         """x: CUDA float32 (n, 7) raw features -> (n, 4) on torch's current stream."""
@@ -154,8 +154,23 @@ class MLP:
             pass
 
 
-def sample_states(pool, n: int, seed: int, t_range=(300.0, 3800.0), p_range=(5.0e4, 1.0e7),
-                  dt_range=(1e-9, 1e-5), keep: float = 0.5):
+def features(x):
+    """Un-normalised network features of raw samples (torch (n, 7): T, p, Y_1..Y_4, dt)."""
+    f = x.double().clone()
+    f[:, 0] = 1000.0 / f[:, 0].clamp_min(1.0)
+    f[:, 1] = f[:, 1].clamp_min(1e-30).log10()
+    f[:, 2:6] = (f[:, 2:6].clamp_min(0.0) + 1e-10).log10()
+    f[:, 6] = f[:, 6].clamp_min(1e-30).log10()
+    return f
+
+
+# sampled training domain: T, p, dt (the solver's nozzle states reach 6000 K
+# in the exit corner and 1e2 Pa at the exit of the large area ratios)
+T_RANGE, P_RANGE, DT_RANGE = (300.0, 6000.0), (1.0e2, 2.0e7), (1.0e-10, 1.0e-4)
+
+
+def sample_states(pool, n: int, seed: int, t_range=T_RANGE, p_range=P_RANGE, dt_range=DT_RANGE,
+                  keep: float = 0.5):
     """n (state, dt) samples from a pool of solver states (torch (NVar, m),
     float64, CUDA): species from the pool, T and p kept with probability
     `keep` and otherwise drawn uniform / log-uniform over the ranges, dt
@@ -173,3 +188,49 @@ def sample_states(pool, n: int, seed: int, t_range=(300.0, 3800.0), p_range=(5.0
     P[0] = torch.where(u() < keep, P[0].clamp(*p_range), newp)
     dt = torch.exp(np.log(dt_range[0]) + (np.log(dt_range[1]) - np.log(dt_range[0])) * u())
     return P.contiguous(), dt.contiguous()
+
+
+def collect_pool(solver, iters: int, every: int):
+    """Solver states (NVar, NE * snapshots) on the GPU, one snapshot every
+    `every` iterations of `iters` (the solver keeps its chemistry mode)."""
+    import torch
+    snaps = []
+    for it in range(1, iters + 1):
+        solver.lu_sgs_stage(it)
+        if it % every == 0:
+            PA, _ = solver.get_state()
+            snaps.append(torch.tensor(PA.T.copy(), device="cuda"))
+    return torch.cat(snaps, 1).contiguous()
+
+
+def build_dataset(solver, pool, n: int, seed: int, tol: float = 0.005, max_substeps: int = 2000,
+                  chunk: int = 1 << 20):
+    """n training pairs: states sampled from `pool` (sample_states), integrated
+    over their dt by the FP64 integrator of `solver` at a tolerance ten times
+    tighter than the solver's default (the targets then carry about a tenth
+    of the integrator's own error), turned into raw features and normalised
+    changes.  Returns (x (n', 7), t (n', 4), substeps); samples
+    whose target is not finite or outside [-1, 10] are dropped."""
+    import torch
+    xs, ts, ns = [], [], []
+    for k in range(0, n, chunk):
+        m = min(chunk, n - k)
+        P0, dt = sample_states(pool, m, seed * 7919 + k)
+        P1, nsub = solver.chem_integrate(P0, dt, tol, max_substeps)
+        x, t = solver.surrogate_samples(P0, P1, dt)
+        ok = torch.isfinite(t).all(1) & (t[:, :3] > -1).all(1) & (t[:, :3] < 10).all(1)
+        xs.append(x[ok]); ts.append(t[ok]); ns.append(nsub[ok])
+    return torch.cat(xs).contiguous(), torch.cat(ts).contiguous(), torch.cat(ns)
+
+
+def validate(net, x, t):
+    """Errors of the network's normalised changes against the integrator's on
+    held-out pairs: max and 99th percentile of |r - r_int| over the reacting
+    species, and the fraction the error indicator's spread test would accept."""
+    import torch
+    y = net.forward(x)
+    e = (y[:, :3] - t[:, :3]).abs().max(1).values
+    rbar = y[:, :3].mean(1, keepdim=True)
+    spread = (y[:, :3] - rbar).abs().max(1).values
+    return {"max_abs_err": float(e.max()), "p99_abs_err": float(torch.quantile(e.float(), 0.99)),
+            "median_abs_err": float(e.median()), "spread_p99": float(torch.quantile(spread.float(), 0.99))}
