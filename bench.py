@@ -49,6 +49,12 @@ def algo_bytes_per_cell(V: int, nf_ne: float, viscous: bool, combustion: bool) -
     return b
 
 
+# DRAM bytes per cell of one launch of the dominant kernel of each subroutine
+# (dram__bytes_read.sum + dram__bytes_write.sum over the 30,000 cells of the
+# capture in profiles/kernels_c2_30k_full.md; the traffic grows with the cells)
+NCU_DRAM_PER_CELL = {"lu_sgs_steady": (10.29e6 + 0.48e6) / 30000, "flux_sourceterm": 10.61e6 / 30000}
+
+
 def read_peaks():
     p = os.path.join(ROOT, "MEASURED_PEAKS.json")
     if os.path.exists(p):
@@ -195,6 +201,10 @@ def main():
     ap.add_argument("--no-batch", action="store_true",
                     help="skip the batched form (64 uneven reacting cases in one context)")
     ap.add_argument("--batch-cases", type=int, default=64)
+    ap.add_argument("--no-surrogate", action="store_true",
+                    help="skip the surrogate form (network trained here on integrator pairs)")
+    ap.add_argument("--sur-samples", type=int, default=10_000_000)
+    ap.add_argument("--sur-steps", type=int, default=4000)
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
 
@@ -270,8 +280,12 @@ def main():
             "gpu_launches": head["launches"],
             "roofline": {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": peak, "unit": "GB/s",
                          "frac": achieved / peak, "peak_source": peak_kind,
-                         "algorithmic_bytes_per_cell": ab[dom], "traffic": None,
-                         "note": "FP64 kernels are FP64-issue bound on GB300 (FP64 pipe 81-88% busy, DRAM < 2%)"},
+                         "algorithmic_bytes_per_cell": ab[dom],
+                         "traffic": NCU_DRAM_PER_CELL[dom] * NE if dom in NCU_DRAM_PER_CELL else None,
+                         "traffic_source": "ncu capture at 30,000 cells scaled by cells (profiles/)",
+                         "note": "LU-SGS is latency bound on its level barriers (natural cell order: 301+301 "
+                                 "levels); the face and cell kernels are FP64-issue bound (FP64 pipe 85-88%, "
+                                 "DRAM < 2%)"},
             "subroutine_ms": sub_ms,
             "stage_algorithmic_gbs": ab["stage"] * NE / (t_max / args.steps) / 1e9,
             "levels": head["levels"],
@@ -297,6 +311,8 @@ def main():
             line["forms"] = forms
         if not args.no_batch and world == 1:
             line.setdefault("forms", {})["batched"] = batched_form(args, stream, flush, torch, rc, tmp)
+        if not args.no_surrogate and world == 1 and cfg.combustion and cfg.nsp == 4:
+            line.setdefault("forms", {})["surrogate"] = surrogate_form(args, stream, flush, torch, rc, case)
         line["clocks"] = clk
         if not args.no_cpu:
             line["cpu_baseline"] = cpu_baseline(d, args.cpu_budget)
@@ -370,6 +386,89 @@ def batched_form(args, stream, flush, torch, rc, tmp):
     out["mixed"]["rel_linf_vs_fp64"] = {"p": float(e[0]), "T": float(e[3]), "Y": [float(x) for x in e[4:]],
                                         "after_iterations": args.warmup + args.steps}
     return out
+
+
+def surrogate_form(args, stream, flush, torch, rc, case):
+    """The learned-surrogate workload on the same nozzle: pairs from the FP64
+    integrator on states of this case's trajectory (integrated source), the
+    network trained on the GPU by the project's kernels, its inference
+    throughput, and the steady iteration with the surrogate source against
+    the one with the integrated source."""
+    from rocketcombustor_gb300 import surrogate
+    out = {}
+    ref = rc.Solver(case, stream=stream.cuda_stream)
+    ref.set_chemistry(rc.RC_CHEM_INTEGRATED)
+    t0 = time.perf_counter()
+    pool = surrogate.collect_pool(ref, iters=20, every=5)
+    x, t, nsub = surrogate.build_dataset(ref, pool, args.sur_samples, seed=7)
+    torch.cuda.synchronize()
+    out["data"] = {"samples": int(x.shape[0]), "seconds": time.perf_counter() - t0,
+                   "integrator_substeps": {"mean": float(nsub.float().mean()), "max": int(nsub.max())},
+                   "domain": {"T": surrogate.T_RANGE, "p": surrogate.P_RANGE, "dt": surrogate.DT_RANGE}}
+    ntr = x.shape[0] - min(1 << 20, x.shape[0] // 10)
+    net = surrogate.MLP(seed=7)
+    net.fit_norm(x[:ntr])
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    hist = net.train(x[:ntr], t[:ntr], steps=args.sur_steps, batch=8192, lr=2e-3, lr_end=3e-5,
+                     log_every=max(1, args.sur_steps // 4))
+    torch.cuda.synchronize()
+    t_train = time.perf_counter() - t0
+    flops_sample = 2 * (7 * 128 + 3 * 128 * 128 + 128 * 4)
+    out["training"] = {"steps": args.sur_steps, "batch": 8192, "seconds": t_train,
+                       "loss": [[int(a), float(b)] for a, b in hist],
+                       "tflops": 3 * flops_sample * 8192 * args.sur_steps / t_train / 1e12}
+    out["validation_vs_integrator"] = surrogate.validate(net, x[ntr:], t[ntr:])
+    xi = x[:min(1 << 22, x.shape[0])].contiguous()
+    net.forward(xi)
+    ev = [torch.cuda.Event(enable_timing=True) for _ in range(2)]
+    torch.cuda.synchronize()
+    ev[0].record()
+    for _ in range(10):
+        net.forward(xi)
+    ev[1].record()
+    torch.cuda.synchronize()
+    t_inf = ev[0].elapsed_time(ev[1]) / 1e3 / 10
+    peak = read_peaks_tensor()
+    out["inference"] = {"samples": int(xi.shape[0]), "samples_per_s": xi.shape[0] / t_inf,
+                        "tflops": flops_sample * xi.shape[0] / t_inf / 1e12, "peak_bf16_tflops": peak,
+                        "note": "fused kernel: layer 0 and the output layer on the CUDA cores, the three 128x128 "
+                                "layers on tcgen05; FLOP counted for the whole network"}
+    # steady iterations: integrated source vs surrogate source, same start
+    forms = {}
+    states = {}
+    for name in ("integrated", "surrogate"):
+        s = rc.Solver(case, stream=stream.cuda_stream)
+        if name == "surrogate":
+            s.set_surrogate(net)
+            s.set_chemistry(rc.RC_CHEM_SURROGATE)
+        else:
+            s.set_chemistry(rc.RC_CHEM_INTEGRATED)
+        r, _ = time_form(s, args, stream, flush, None, torch, rc)
+        states[name] = s.get_state()[0]
+        forms[name] = {"value": case.NE * args.steps / r["t_local"], "ms_per_step": 1e3 * r["t_local"] / args.steps,
+                       "gpu_launches": r["launches"]}
+        if name == "surrogate":
+            a, b = s.surrogate_stats()
+            forms[name]["cells_network"], forms[name]["cells_integrator"] = a, b
+        s.close()
+    den = np.maximum(np.abs(states["integrated"]).max(axis=0), 1e-300)
+    e = np.abs(states["surrogate"] - states["integrated"]).max(axis=0) / den
+    forms["surrogate"]["rel_linf_vs_integrated"] = {"p": float(e[0]), "T": float(e[3]),
+                                                    "Y": [float(v) for v in e[4:]],
+                                                    "after_iterations": args.warmup + args.steps}
+    out["steady"] = forms
+    net.close()
+    ref.close()
+    return out
+
+
+def read_peaks_tensor():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        with open(p) as f:
+            return float(json.load(f)["bf16_tflops"])
+    return 1900.0
 
 
 def subroutine_times(s, args, stream, flush, torch):
