@@ -205,6 +205,10 @@ def main():
                     help="skip the surrogate form (network trained here on integrator pairs)")
     ap.add_argument("--sur-samples", type=int, default=10_000_000)
     ap.add_argument("--sur-steps", type=int, default=4000)
+    ap.add_argument("--converge", type=int, default=0,
+                    help="instead of the throughput line: N iterations per form with the residual history, "
+                         "iterations and wall time to each residual level")
+    ap.add_argument("--every", type=int, default=10)
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
 
@@ -225,6 +229,8 @@ def main():
     import torch
     import rocketcombustor_gb300 as rc
 
+    if args.converge:
+        return converge(args, rc, torch)
     torch.cuda.set_device(local)
     stream = torch.cuda.Stream(device=local)
     flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=f"cuda:{local}")
@@ -386,6 +392,81 @@ def batched_form(args, stream, flush, torch, rc, tmp):
     out["mixed"]["rel_linf_vs_fp64"] = {"p": float(e[0]), "T": float(e[3]), "Y": [float(x) for x in e[4:]],
                                         "after_iterations": args.warmup + args.steps}
     return out
+
+
+LEVELS = (1e-1, 5e-2, 3e-2, 1e-2, 1e-3, 1e-8)
+
+
+def reach(hist, every, levels=LEVELS):
+    """Iteration at which max_k Res_k / Res_k(first check) first falls to each level."""
+    r0 = np.where(hist[0, :-1] > 0, hist[0, :-1], 1.0)
+    rel = np.where(hist[0, :-1] > 0, hist[:, :-1] / r0, 0.0).max(axis=1)
+    out = {}
+    for lv in levels:
+        hit = np.nonzero(rel <= lv)[0]
+        out[f"{lv:g}"] = int((hit[0] + 1) * every) if hit.size else None
+    return out, float(rel.min()), float(rel[-1])
+
+
+def converge(args, rc, torch):
+    """Residual histories of the forms on the same case: iterations and wall
+    time to each level of max_k Res_k/Res_k(first), the lowest level reached
+    (the reference's Barth limiter stalls the steady residual), and the final
+    state against the FP64 one."""
+    out = {"mode": "converge", "iterations": args.converge, "every": args.every, "levels": list(LEVELS)}
+    with tempfile.TemporaryDirectory() as tmp:
+        d, cfg = make_workload(args.case, tmp, **case_overrides(args))
+        out["config"] = workload_config(cfg, 0, 0, "single GPU")
+        finals = {}
+        for form in ("fp64", "mixed", "mixed_dc"):
+            case = rc.Case(d)
+            t0 = time.perf_counter()
+            sw = None
+            if form == "mixed_dc":
+                hist, sw = case.run_steady_dc(args.converge, args.every, window=5)
+            else:
+                hist = case.run_steady(args.converge, args.every,
+                                       rc.RC_PREC_FP64 if form == "fp64" else rc.RC_PREC_MIXED)
+            wall = time.perf_counter() - t0
+            lv, best, last = reach(hist, args.every)
+            per_it = wall / args.converge
+            finals[form] = case.array("PA").copy()
+            out[form] = {"wall_s": wall, "iterations_to": lv,
+                         "seconds_to": {k: (v * per_it if v else None) for k, v in lv.items()},
+                         "lowest_level": best, "final_level": last}
+            if sw is not None:
+                out[form]["switched_to_dc_at"] = sw
+            case.close()
+        ref = finals["fp64"]
+        den = np.maximum(np.abs(ref).max(axis=0), 1e-300)
+        for form in ("mixed", "mixed_dc"):
+            e = np.abs(finals[form] - ref).max(axis=0) / den
+            out[form]["final_rel_linf_vs_fp64"] = {"p": float(e[0]), "T": float(e[3]),
+                                                  "Y": [float(x) for x in e[4:]]}
+        if not args.no_batch:
+            from rocketcombustor_gb300 import cases
+            dirs = cases.make_batch(os.path.join(tmp, "batch"), args.batch_cases, 5)
+            cs = [rc.Case(x) for x in dirs]
+            b = rc.BatchSolver(cs)
+            b.set_chemistry(rc.RC_CHEM_INTEGRATED)
+            n_it = min(args.converge, 1000)
+            hists = []
+            t0 = time.perf_counter()
+            for it in range(1, n_it + 1):
+                b.lu_sgs_stage(it)
+                if it % args.every == 0:
+                    hists.append(np.concatenate([b.residual()[0], np.zeros((len(cs), 1))], axis=1))
+            wall = time.perf_counter() - t0
+            H = np.stack(hists, axis=1)  # case, check, V+1
+            per = []
+            for k in range(len(cs)):
+                lv, best, _ = reach(H[k], args.every, (1e-1, 5e-2))
+                per.append({"cells": cs[k].NE, "iterations_to": lv, "lowest_level": best})
+            out["batched"] = {"cases": len(cs), "iterations": n_it, "wall_s": wall,
+                              "ms_per_iteration": 1e3 * wall / n_it, "per_case": per,
+                              "reached_1e-1": sum(1 for p in per if p["iterations_to"]["0.1"])}
+    print(json.dumps(out), flush=True)
+    return 0
 
 
 def surrogate_form(args, stream, flush, torch, rc, case):

@@ -56,6 +56,13 @@ const void* rc_case_array(const rc_case* c, const char* name, long* count);
  * copied back into the case.  Returns the RC status. */
 int rc_run_steady(rc_case* c, int precision, int device, long nsteps, long every, double* hist);
 
+/* The same driver for the mixed-precision form with defect correction: runs
+ * RC_PREC_MIXED and switches once to RC_PREC_MIXED_DC when the residual
+ * (checked every `every` steps) has not dropped below 0.99 times its best
+ * value for `window` checks in a row; switched_at gets the switch iteration
+ * (0 if it never stalled).  No counterpart in the reference. */
+int rc_run_steady_dc(rc_case* c, int device, long nsteps, long every, int window, double* hist, long* switched_at);
+
 #ifdef __cplusplus
 }
 #endif

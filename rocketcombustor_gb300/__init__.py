@@ -94,6 +94,7 @@ SIGNATURES = {
     "rc_case_WA": (_DP, [_vp]),
     "rc_case_array": (_vp, [_vp, _cp, ctypes.POINTER(_l)]),
     "rc_run_steady": (_i, [_vp, _i, _i, _l, _l, _DP]),
+    "rc_run_steady_dc": (_i, [_vp, _i, _l, _l, _i, _DP, ctypes.POINTER(_l)]),
     "rc_residual_noalloc": (_i, [_vp, _vp, _vp, _i, _i, _d, _vp, _DP, _DP]),
     "rc_set_precision": (_i, [_vp, _i]),
     "rc_set_chemistry": (_i, [_vp, _i, _d, _i]),
@@ -196,6 +197,27 @@ class Case:
         dims = (self.NE, self.NF, self.NNT, self.NVar, self.Nsp, self.MaxNei, self.Nghost)
         buf = (ctypes.c_byte * (n.value * np.dtype(dt).itemsize)).from_address(p)
         return np.frombuffer(buf, dtype=dt).reshape(shp(dims))
+
+    def run_steady(self, nsteps: int, every: int = 10, precision: int = RC_PREC_FP64, device: int = 0):
+        """The steady driver (rc_run_steady): nsteps iterations on the GPU from
+        the case's state, which it replaces; returns the residual history
+        (nsteps // every rows of Res(1:NVar), romax)."""
+        hist = np.zeros((nsteps // every, self.NVar + 1))
+        st = load().rc_run_steady(self._h, int(precision), int(device), int(nsteps), int(every), _dp(hist))
+        if st:
+            raise RcError(st, load().rc_case_error(self._h).decode())
+        return hist
+
+    def run_steady_dc(self, nsteps: int, every: int = 10, window: int = 5, device: int = 0):
+        """Mixed precision with the defect-correction switch (rc_run_steady_dc);
+        returns (history, iteration of the switch or 0)."""
+        hist = np.zeros((nsteps // every, self.NVar + 1))
+        sw = _l(0)
+        st = load().rc_run_steady_dc(self._h, int(device), int(nsteps), int(every), int(window), _dp(hist),
+                                     ctypes.byref(sw))
+        if st:
+            raise RcError(st, load().rc_case_error(self._h).decode())
+        return hist, int(sw.value)
 
     def views(self, precision: int = RC_PREC_FP64, device: int = 0):
         m, t, g = RcMesh(), RcThermo(), RcConfig()

@@ -706,4 +706,56 @@ int rc_run_steady(rc_case* c, int precision, int device, long nsteps, long every
   return st;
 }
 
+// Mixed precision with defect correction: iterate in RC_PREC_MIXED and switch
+// once to RC_PREC_MIXED_DC (FP64 residual, FP32 sweeps) when the FP32
+// residual stalls: at every residual check r = max_k Res_k / Res_k(first
+// check) over the non-zero columns; a check that does not bring r below 0.99
+// times its best value so far counts towards the stall, `window` such checks
+// in a row switch.  switched_at gets the iteration of the switch (0: none).
+int rc_run_steady_dc(rc_case* c, int device, long nsteps, long every, int window, double* hist, long* switched_at) {
+  if (!c || every < 1 || window < 1) return RC_ERR_ARG;
+  rc_mesh m;
+  rc_thermo t;
+  rc_config g;
+  rc_case_views(c, RC_PREC_MIXED_DC, device, &m, &t, &g);
+  rc_ctx* ctx = nullptr;
+  int st = rc_init(&m, &t, &g, &ctx);
+  if (st) { c->err = "rc_init failed"; return st; }
+  st = rc_set_precision(ctx, RC_PREC_MIXED);
+  if (!st) st = rc_set_state(ctx, c->PA.data(), c->WA.data());
+  const int V = c->NVar;
+  std::vector<double> res(V), res0;
+  double best = 1e300, romax = 0.0;
+  int since = 0;
+  long row = 0, sw = 0;
+  for (long it = 1; it <= nsteps && !st; ++it) {
+    st = rc_lusgs_stage(ctx, (int)it);
+    if (st || it % every) continue;
+    st = rc_residual(ctx, res.data(), &romax);
+    if (st) break;
+    if (hist) {
+      for (int k = 0; k < V; ++k) hist[(size_t)row * (V + 1) + k] = res[k];
+      hist[(size_t)row * (V + 1) + V] = romax;
+    }
+    ++row;
+    if (res0.empty()) res0 = res;
+    double r = 0.0;
+    for (int k = 0; k < V; ++k)
+      if (res0[k] > 0.0) r = std::max(r, res[k] / res0[k]);
+    if (sw) continue;
+    if (r < 0.99 * best) {
+      best = r;
+      since = 0;
+    } else if (++since >= window) {
+      st = rc_set_precision(ctx, RC_PREC_MIXED_DC);
+      sw = it;
+    }
+  }
+  if (switched_at) *switched_at = sw;
+  if (!st) st = rc_get_state(ctx, c->PA.data(), c->WA.data());
+  if (st) c->err = rc_last_error(ctx);
+  rc_finalize(ctx);
+  return st;
+}
+
 }  // extern "C"

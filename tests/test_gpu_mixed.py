@@ -81,3 +81,26 @@ def test_mode_switching_keeps_graphs_apart(case_t1):
     plain = rc.Solver(c)
     with pytest.raises(rc.RcError):
         plain.set_precision(rc.RC_PREC_MIXED)
+
+
+def test_steady_driver_fp64_equals_solver_run(case_root):
+    """rc_run_steady (the host driver of fvm2d.f90's steady loop) runs the
+    same graph as Solver.run: identical states."""
+    d = make_case(case_root, "t2")
+    a = rc.Case(d)
+    hist = a.run_steady(40, every=10)
+    b = rc.Solver(rc.Case(d))
+    b.run(40)
+    assert hist.shape == (4, a.NVar + 1)
+    assert np.array_equal(a.array("PA"), b.get_state()[0])
+
+
+def test_defect_correction_switch(case_root):
+    """Mixed precision switches to the FP64 residual once the FP32 residual
+    stalls; afterwards the iteration continues from the mixed state."""
+    d = make_case(case_root, "c1", nx=60, ny=12)
+    c = rc.Case(d)
+    hist, sw = c.run_steady_dc(600, every=10, window=3)
+    assert 0 < sw <= 600, sw
+    assert np.all(np.isfinite(c.array("PA")))
+    assert np.all(np.isfinite(hist))
