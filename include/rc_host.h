@@ -50,6 +50,15 @@ const double* rc_case_WA(const rc_case* c);
  * "VOL", "Neighbor"); returns a pointer and the element count, or NULL. */
 const void* rc_case_array(const rc_case* c, const char* name, long* count);
 
+/* Replace the case's host state (e.g. with what rc_get_state read back). */
+int rc_case_set_state(rc_case* c, const double* PA, const double* WA);
+/* BackupData (src/output.f90:256): fvp-format restart file of the case's state,
+ * readable by Read_Backup (and by rc_case_open); 17 significant digits. */
+int rc_case_write_backup(rc_case* c, const char* path, double ttime);
+/* output_vtk (src/output.f90:4): legacy ASCII VTK of the cell-centred rho, u,
+ * v, p, T, Ma, Y_k and production rates of the case's state. */
+int rc_case_write_vtk(rc_case* c, const char* path);
+
 /* Steady driver: rc_init on `device`, nsteps lu_sgs_stage iterations, residual
  * history (step_residual columns Res(1:NVar), romax) written to hist every
  * `every` steps when hist != NULL (hist holds nsteps/every rows), final PA/WA

@@ -94,6 +94,9 @@ SIGNATURES = {
     "rc_case_WA": (_DP, [_vp]),
     "rc_case_array": (_vp, [_vp, _cp, ctypes.POINTER(_l)]),
     "rc_run_steady": (_i, [_vp, _i, _i, _l, _l, _DP]),
+    "rc_case_set_state": (_i, [_vp, _DP, _DP]),
+    "rc_case_write_backup": (_i, [_vp, _cp, _d]),
+    "rc_case_write_vtk": (_i, [_vp, _cp]),
     "rc_run_steady_dc": (_i, [_vp, _i, _l, _l, _i, _DP, ctypes.POINTER(_l)]),
     "rc_residual_noalloc": (_i, [_vp, _vp, _vp, _i, _i, _d, _vp, _DP, _DP]),
     "rc_set_precision": (_i, [_vp, _i]),
@@ -197,6 +200,28 @@ class Case:
         dims = (self.NE, self.NF, self.NNT, self.NVar, self.Nsp, self.MaxNei, self.Nghost)
         buf = (ctypes.c_byte * (n.value * np.dtype(dt).itemsize)).from_address(p)
         return np.frombuffer(buf, dtype=dt).reshape(shp(dims))
+
+    def set_state(self, PA: np.ndarray, WA: np.ndarray):
+        """Replace the case's host state (PA, WA as (NE, NVar))."""
+        PA = np.ascontiguousarray(PA, dtype=np.float64)
+        WA = np.ascontiguousarray(WA, dtype=np.float64)
+        if PA.shape != (self.NE, self.NVar) or WA.shape != (self.NE, self.NVar):
+            raise ValueError("PA and WA must be (NE, NVar)")
+        st = load().rc_case_set_state(self._h, _dp(PA), _dp(WA))
+        if st:
+            raise RcError(st, load().rc_case_error(self._h).decode())
+
+    def write_backup(self, path: str, ttime: float = 0.0):
+        """BackupData: restart file of the case's state (fvp format)."""
+        st = load().rc_case_write_backup(self._h, path.encode(), float(ttime))
+        if st:
+            raise RcError(st, load().rc_case_error(self._h).decode())
+
+    def write_vtk(self, path: str):
+        """output_vtk: legacy ASCII VTK of the case's state."""
+        st = load().rc_case_write_vtk(self._h, path.encode())
+        if st:
+            raise RcError(st, load().rc_case_error(self._h).decode())
 
     def run_steady(self, nsteps: int, every: int = 10, precision: int = RC_PREC_FP64, device: int = 0):
         """The steady driver (rc_run_steady): nsteps iterations on the GPU from
@@ -388,6 +413,18 @@ class Solver:
     def set_array(self, name: str, a: np.ndarray):
         a = np.ascontiguousarray(a, dtype=np.float64).reshape(self._SHAPES[name](self))
         self._check(load().rc_set_array(self._h, name.encode(), _dp(a)))
+
+    def write_backup(self, path: str, ttime: float = 0.0):
+        """The device state as a restart file (BackupData, output.f90:256-273)."""
+        PA, WA = self.get_state()
+        self.case.set_state(PA, WA)
+        self.case.write_backup(path, ttime)
+
+    def write_vtk(self, path: str):
+        """The device state as a VTK file (output_vtk, output.f90:4-227)."""
+        PA, WA = self.get_state()
+        self.case.set_state(PA, WA)
+        self.case.write_vtk(path)
 
     def stream(self) -> int:
         return load().rc_get_stream(self._h) or 0

@@ -534,35 +534,72 @@ __global__ void __launch_bounds__(128) k_gather(const Dev d, int visc, int comb)
 // neighbour in face slot q, the terms are added in slot order (the NeighF
 // order of the reference) and the lanes share the final divisions.  The
 // residual R is already in hWA (the gather runs before, fully parallel).
-// sweep_step: the cell at level position t (t >= tend: lanes that only join
-// the shuffles).  All indices come from the sweep tables in one load; the
-// cell's own residual and diagonal are fetched up front.  Called by whole warps.
+// sweep_load / sweep_compute: the cell at level position t (t >= tend: lanes
+// that only join the reduction).  sweep_load reads what the sweep does not
+// change (tables, the neighbour's state and gas state, the face, the
+// diagonal), so it can be issued before the previous level is complete;
+// sweep_compute reads the residuals / increments and does the reference's
+// arithmetic in the reference's order.  Called by whole warps.
+template <int NSP>
+struct SweepPre {
+  int i;
+  bool valid, act;
+  int j;
+  double dx, dy, pp, uu, vv, tt, rr, gama, roe, aF, ddi;
+  // products of the constants above, formed before the wait with the same
+  // operations as the reference expressions use them
+  double rou, rov, gm1, roepp, unormal;
+  double cs[NSP];          // h_k of the neighbour (cst planes 3..)
+  double ry[NSP > 1 ? NSP - 1 : 1];  // rr * Y_k of the neighbour
+};
 template <int NSP, bool FWD>
-__device__ __forceinline__ void sweep_step(const Dev& d, const ThermoDev<NSP>& th, int t, int tend, int q) {
-  constexpr int V = 3 + NSP;
+__device__ __forceinline__ SweepPre<NSP> sweep_load(const Dev& d, int t, int tend, int q) {
   constexpr int DIR = FWD ? 0 : 1;
-  const bool valid = t < tend;
+  SweepPre<NSP> p;
+  p.valid = t < tend;
   const int NE = d.NE, NF = d.NF;
-  const int i = valid ? d.swi[DIR][t] : 0;
-  const int j = valid ? d.swj[DIR][q * NE + t] : -1;
-  const int fs = valid ? d.swf[DIR][q * NE + t] : 0;
-  double R0 = 0.0, R1 = 0.0, ddi = 1.0;
-  if (valid) {  // own residual (variables q and q+4) and diagonal
-    R0 = d.hWA[q * NE + i];
-    if (q + 4 < V) R1 = d.hWA[(q + 4) * NE + i];
-    ddi = d.dd[i];
+  p.i = p.valid ? d.swi[DIR][t] : 0;
+  p.j = p.valid ? d.swj[DIR][q * NE + t] : -1;
+  const int fs = p.valid ? d.swf[DIR][q * NE + t] : 0;
+  p.ddi = p.valid ? d.dd[p.i] : 1.0;
+  p.act = p.j >= 0;
+  if (p.act) {
+    const int j = p.j, f = fs >= 0 ? fs : ~fs;
+    p.dx = d.fvec[f];
+    p.dy = d.fvec[NF + f];
+    if (fs < 0) { p.dx = -p.dx; p.dy = -p.dy; }
+    p.pp = d.PA[0 * NE + j]; p.uu = d.PA[1 * NE + j]; p.vv = d.PA[2 * NE + j]; p.tt = d.PA[3 * NE + j];
+    p.rr = d.cst[0 * NE + j]; p.gama = d.cst[1 * NE + j]; p.roe = d.cst[2 * NE + j];
+    p.aF = d.alpaF[f];
+#pragma unroll
+    for (int k = 0; k < NSP; ++k) p.cs[k] = d.cst[(3 + k) * NE + j];
+#pragma unroll
+    for (int k = 0; k < NSP - 1; ++k) p.ry[k] = p.rr * d.PA[(4 + k) * NE + j];
+    p.rou = p.rr * p.uu;
+    p.rov = p.rr * p.vv;
+    p.gm1 = p.gama - 1;
+    p.roepp = p.roe + p.pp;
+    p.unormal = p.uu * p.dx + p.vv * p.dy;
+  }
+  return p;
+}
+template <int NSP, bool FWD>
+__device__ __forceinline__ void sweep_compute(const Dev& d, const ThermoDev<NSP>& th, const SweepPre<NSP>& p, int q,
+                                              double* wsm) {
+  constexpr int V = 3 + NSP;
+  const int NE = d.NE;
+  double R0 = 0.0, R1 = 0.0;
+  if (p.valid) {  // own residual (variables q and q+4)
+    R0 = d.hWA[q * NE + p.i];
+    if (q + 4 < V) R1 = d.hWA[(q + 4) * NE + p.i];
   }
   double c[V];
 #pragma unroll
   for (int k = 0; k < V; ++k) c[k] = 0.0;
-  const bool act = j >= 0;
-  if (act) {
-    const int f = fs >= 0 ? fs : ~fs;
-    double dx = d.fvec[f], dy = d.fvec[NF + f];
-    if (fs < 0) { dx = -dx; dy = -dy; }
-    const double pp = d.PA[0 * NE + j], uu = d.PA[1 * NE + j], vv = d.PA[2 * NE + j], tt = d.PA[3 * NE + j];
-    const double rr = d.cst[0 * NE + j], gama = d.cst[1 * NE + j], roe = d.cst[2 * NE + j];
-    const double rou = rr * uu, rov = rr * vv;
+  if (p.act) {
+    const int j = p.j;
+    const double dx = p.dx, dy = p.dy, uu = p.uu, vv = p.vv, tt = p.tt, rr = p.rr, gama = p.gama;
+    const double rou = p.rou, rov = p.rov;
     const double drr = d.hWA[0 * NE + j], dru = d.hWA[1 * NE + j], drv = d.hWA[2 * NE + j],
                  dre = d.hWA[3 * NE + j];
     double dry[NSP], s = 0.0;
@@ -573,46 +610,54 @@ __device__ __forceinline__ void sweep_step(const Dev& d, const ThermoDev<NSP>& t
     const double dvv = (drv - vv * drr) / rr;
     double s1 = 0.0, s2 = 0.0;
 #pragma unroll
-    for (int k = 0; k < NSP; ++k) s1 = s1 + d.cst[(3 + k) * NE + j] * dry[k];
+    for (int k = 0; k < NSP; ++k) s1 = s1 + p.cs[k] * dry[k];
 #pragma unroll
     for (int k = 0; k < NSP; ++k) s2 = s2 + th.R[k] * dry[k];
-    const double dpp =
-        (gama - 1) * (dre - s1 + tt * s2 * gama / (gama - 1) - 0.5 * (dru * uu + duu * rou + drv * vv + dvv * rov));
-    const double unormal = uu * dx + vv * dy;
+    const double gm1 = p.gm1;
+    const double dpp = gm1 * (dre - s1 + tt * s2 * gama / gm1 - 0.5 * (dru * uu + duu * rou + drv * vv + dvv * rov));
+    const double unormal = p.unormal;
     const double dunormal = duu * dx + dvv * dy;
-    const double aF = d.alpaF[f];
+    const double aF = p.aF;
     c[0] = 0.5 * (-aF * drr + dru * dx + drv * dy);
     c[1] = 0.5 * (-aF * dru + dru * unormal + rou * dunormal + dpp * dx);
     c[2] = 0.5 * (-aF * drv + drv * unormal + rov * dunormal + dpp * dy);
-    c[3] = 0.5 * (-aF * dre + dunormal * (roe + pp) + unormal * (dre + dpp));
+    c[3] = 0.5 * (-aF * dre + dunormal * p.roepp + unormal * (dre + dpp));
 #pragma unroll
-    for (int k = 0; k < NSP - 1; ++k) {
-      const double ry = rr * d.PA[(4 + k) * NE + j];
-      c[4 + k] = 0.5 * (-aF * dry[k] + dry[k] * unormal + ry * dunormal);
-    }
+    for (int k = 0; k < NSP - 1; ++k) c[4 + k] = 0.5 * (-aF * dry[k] + dry[k] * unormal + p.ry[k] * dunormal);
   }
-  // terms in slot order (NeighF order); lane q keeps the sums of its variables q, q+4
-  const int base = (threadIdx.x & 31) & ~3;
+  // terms in slot order (NeighF order) through the warp's shared scratch; lane
+  // q sums its variables q and q+4 over the 4 slots of its quad.  Inactive
+  // slots contribute +0.0, which leaves the sums bit-identical to adding the
+  // active terms only (the sums start at +0.0, so -0.0 never occurs).
+  const int lane = threadIdx.x & 31, base = lane & ~3;
+  __syncwarp();
+#pragma unroll
+  for (int k = 0; k < V; ++k) wsm[k * 32 + lane] = c[k];
+  __syncwarp();
   double df0 = 0.0, df1 = 0.0;
 #pragma unroll
   for (int sl = 0; sl < 4; ++sl) {
-    const bool a = __shfl_sync(0xffffffffu, act, base + sl);
-#pragma unroll
-    for (int k = 0; k < V; ++k) {
-      const double cs = __shfl_sync(0xffffffffu, c[k], base + sl);
-      if (a && k == q) df0 = df0 + cs;
-      if (a && k == q + 4) df1 = df1 + cs;
-    }
+    df0 = df0 + wsm[q * 32 + base + sl];
+    if (q + 4 < V) df1 = df1 + wsm[(q + 4) * 32 + base + sl];
   }
-  if (!valid) return;
-  d.hWA[q * NE + i] = FWD ? (R0 - df0) / ddi : R0 - df0 / ddi;
-  if (q + 4 < V) d.hWA[(q + 4) * NE + i] = FWD ? (R1 - df1) / ddi : R1 - df1 / ddi;
+  if (!p.valid) return;
+  const double ddi = p.ddi;
+  d.hWA[q * NE + p.i] = FWD ? (R0 - df0) / ddi : R0 - df0 / ddi;
+  if (q + 4 < V) d.hWA[(q + 4) * NE + p.i] = FWD ? (R1 - df1) / ddi : R1 - df1 / ddi;
+}
+template <int NSP, bool FWD>
+__device__ __forceinline__ void sweep_step(const Dev& d, const ThermoDev<NSP>& th, int t, int tend, int q,
+                                           double* wsm) {
+  const SweepPre<NSP> p = sweep_load<NSP, FWD>(d, t, tend, q);
+  sweep_compute<NSP, FWD>(d, th, p, q, wsm);
 }
 
+// one level of a sweep: block b (one warp) takes cells t0 + b*cpw .. + cpw-1
 template <int NSP, bool FWD>
 __global__ void __launch_bounds__(32) k_sweep4(const Dev d, const ThermoDev<NSP> th, int t0, int t1) {
-  const int gt = blockIdx.x * blockDim.x + threadIdx.x;
-  sweep_step<NSP, FWD>(d, th, t0 + (gt >> 2), t1, gt & 3);
+  const int lt = threadIdx.x >> 2;
+  __shared__ double wsm[32 * (3 + NSP)];
+  sweep_step<NSP, FWD>(d, th, lt < d.cpw ? t0 + blockIdx.x * d.cpw + lt : t1, t1, threadIdx.x & 3, wsm);
 }
 
 template <int NSP>
@@ -624,30 +669,62 @@ __global__ void __launch_bounds__(128) k_update(const Dev d, const ThermoDev<NSP
   flag(d, err);
 }
 
-// Both LU-SGS sweeps and the Newton update in one cooperative launch: the
-// levels of the forward sweep, then of the backward sweep, separated by grid
-// barriers (bounded waits), then the update of all cells.  A level is cut into
-// warps of 8 cells (4 lanes each) dealt out to blocks first, so a small level
-// spreads over as many SMs as it has warps.
+// Both LU-SGS sweeps and the Newton update in one cooperative launch.  The
+// levels of the forward sweep, then of the backward sweep, are cut into
+// chunks of cpw cells (4 lanes each) dealt to the warps of the grid; a warp
+// loads its next chunk's constant data, waits (bounded) until every chunk of
+// the previous level is counted done, computes and counts its chunk.  Only
+// warps with work in a level wait for the one before it, and each level's
+// wait implies all earlier levels (each warp runs its levels in order).  The
+// Newton update of all cells follows the last backward level.  cnt holds one
+// counter per level (nf + nb), zeroed before the launch.
 constexpr int PERS_THREADS = 256;
 template <int NSP>
 __global__ void __launch_bounds__(PERS_THREADS) k_lusgs_persistent(const Dev d, const ThermoDev<NSP> th,
                                                                    const int* __restrict__ foff, int nf,
                                                                    const int* __restrict__ boff, int nb,
-                                                                   unsigned* count) {
+                                                                   unsigned* cnt) {
   const int G = gridDim.x, wpb = PERS_THREADS / 32, w = threadIdx.x >> 5;
+  const int gw = blockIdx.x + w * G, nw = G * wpb;
   const int lt = (threadIdx.x & 31) >> 2, q = threadIdx.x & 3;
-  unsigned seq = 0;
-  for (int l = 0; l < nf; ++l) {
-    const int t0 = foff[l], t1 = foff[l + 1], nch = (t1 - t0 + 7) >> 3;
-    for (int c = blockIdx.x + w * G; c < nch; c += G * wpb) sweep_step<NSP, true>(d, th, t0 + c * 8 + lt, t1, q);
-    if (!grid_sync(count, seq++, d.err)) return;
+  __shared__ double wsm_all[PERS_THREADS / 32][32 * (3 + NSP)];
+  double* wsm = wsm_all[w];
+  const int nl = nf + nb;
+  // level L covers positions [lo(L), lo(L) + len(L)) of its sweep's tables
+  auto lo = [&](int L) { return L < nf ? foff[L] : boff[L - nf]; };
+  const int cpw = d.cpw;
+  auto nchunks = [&](int L) {
+    const int a = L < nf ? foff[L] : boff[L - nf], b = L < nf ? foff[L + 1] : boff[L - nf + 1];
+    return (unsigned)((b - a + cpw - 1) / cpw);
+  };
+  for (int L = 0; L < nl; ++L) {
+    const bool fwd = L < nf;
+    const int t0 = lo(L), t1 = fwd ? foff[L + 1] : boff[L - nf + 1];
+    const int nch = (t1 - t0 + cpw - 1) / cpw;
+    if (gw >= nch) continue;
+    bool waited = L == 0;
+    for (int c = gw; c < nch; c += nw) {
+      const int t = lt < cpw ? t0 + c * cpw + lt : t1;
+      if (fwd) {
+        const SweepPre<NSP> p = sweep_load<NSP, true>(d, t, t1, q);
+        if (!waited) {
+          if (!wait_count(cnt + L - 1, nchunks(L - 1), d.err)) return;
+          waited = true;
+        }
+        sweep_compute<NSP, true>(d, th, p, q, wsm);
+      } else {
+        const SweepPre<NSP> p = sweep_load<NSP, false>(d, t, t1, q);
+        if (!waited) {
+          if (!wait_count(cnt + L - 1, nchunks(L - 1), d.err)) return;
+          waited = true;
+        }
+        sweep_compute<NSP, false>(d, th, p, q, wsm);
+      }
+      count_done(cnt + L);
+    }
   }
-  for (int l = 0; l < nb; ++l) {
-    const int t0 = boff[l], t1 = boff[l + 1], nch = (t1 - t0 + 7) >> 3;
-    for (int c = blockIdx.x + w * G; c < nch; c += G * wpb) sweep_step<NSP, false>(d, th, t0 + c * 8 + lt, t1, q);
-    if (!grid_sync(count, seq++, d.err)) return;
-  }
+  // the update needs the whole backward sweep
+  if (!wait_count(cnt + nl - 1, nchunks(nl - 1), d.err)) return;
   unsigned err = 0;
   for (int i = blockIdx.x * PERS_THREADS + threadIdx.x; i < d.NE; i += G * PERS_THREADS) update_cell<NSP>(d, th, i, err);
   flag(d, err);
@@ -757,7 +834,8 @@ struct rc_ctx {
   bool persistent = true;       // LU-SGS sweeps as one cooperative launch (else one launch per level)
   bool can_persistent = false;  // the device can co-schedule the persistent LU-SGS grid
   int pers_grid = 0;             // blocks of the persistent launch (one per SM)
-  unsigned* bar_count = nullptr; // grid-barrier counter of the persistent launch
+  unsigned* lvl_count = nullptr; // per-level completion counters of the persistent launch
+  int nlevels = 0;
   int* fwd_off_dev = nullptr;
   int* bwd_off_dev = nullptr;
   // batch of independent cases sharing the numbering (ncase == 1: one case)
@@ -891,7 +969,7 @@ void q_face_flux(rc_ctx* c) {
 }
 template <int NSP>
 void q_persistent(rc_ctx* c) {
-  cudaMemsetAsync(c->bar_count, 0, sizeof(unsigned), c->stream);
+  cudaMemsetAsync(c->lvl_count, 0, sizeof(unsigned) * c->nlevels, c->stream);
   cudaLaunchConfig_t cfg = {};
   cfg.gridDim = dim3((unsigned)c->pers_grid);
   cfg.blockDim = dim3(PERS_THREADS);
@@ -903,7 +981,7 @@ void q_persistent(rc_ctx* c) {
   cfg.numAttrs = 1;
   cudaLaunchKernelEx(&cfg, k_lusgs_persistent<NSP>, c->d, TH<NSP>(c), (const int*)c->fwd_off_dev,
                      (int)c->fwd_off.size() - 1, (const int*)c->bwd_off_dev, (int)c->bwd_off.size() - 1,
-                     c->bar_count);
+                     c->lvl_count);
   c->launches++;
 }
 template <int NSP>
@@ -915,13 +993,14 @@ void q_sweeps(rc_ctx* c, int gather) {
   if (c->persistent) { q_persistent<NSP>(c); return; }
   for (size_t l = 0; l + 1 < c->fwd_off.size(); ++l) {
     const int n = c->fwd_off[l + 1] - c->fwd_off[l];
-    k_sweep4<NSP, true><<<blocks(4L * n, 32), 32, 0, c->stream>>>(c->d, TH<NSP>(c), c->fwd_off[l], c->fwd_off[l + 1]);
+    k_sweep4<NSP, true><<<blocks(n, c->d.cpw), 32, 0, c->stream>>>(c->d, TH<NSP>(c), c->fwd_off[l],
+                                                                    c->fwd_off[l + 1]);
     c->launches++;
   }
   for (size_t l = 0; l + 1 < c->bwd_off.size(); ++l) {
     const int n = c->bwd_off[l + 1] - c->bwd_off[l];
-    k_sweep4<NSP, false><<<blocks(4L * n, 32), 32, 0, c->stream>>>(c->d, TH<NSP>(c), c->bwd_off[l],
-                                                                    c->bwd_off[l + 1]);
+    k_sweep4<NSP, false><<<blocks(n, c->d.cpw), 32, 0, c->stream>>>(c->d, TH<NSP>(c), c->bwd_off[l],
+                                                                     c->bwd_off[l + 1]);
     c->launches++;
   }
   k_update<NSP><<<blocks(c->NE, c->d.bs), c->d.bs, 0, c->stream>>>(c->d, TH<NSP>(c));
@@ -963,9 +1042,9 @@ void q_gather(rc_ctx* c) {
 template <int NSP>
 void q_sweeps32(rc_ctx* c) {
   if (c->persistent) {
-    cudaMemsetAsync(c->bar_count, 0, sizeof(unsigned), c->stream);
+    cudaMemsetAsync(c->lvl_count, 0, sizeof(unsigned) * c->nlevels, c->stream);
     mixed_lusgs_persistent<NSP>(c->d, c->thermo32.data(), c->fwd_off_dev, (int)c->fwd_off.size() - 1, c->bwd_off_dev,
-                                (int)c->bwd_off.size() - 1, c->bar_count, c->pers_grid, c->stream);
+                                (int)c->bwd_off.size() - 1, c->lvl_count, c->pers_grid, c->stream);
     k_update<NSP><<<blocks(c->NE, c->d.bs), c->d.bs, 0, c->stream>>>(c->d, TH<NSP>(c));
     c->launches += 2;
     return;
@@ -1378,6 +1457,11 @@ int init_impl(const rc_mesh* m, const rc_thermo* t, const rc_config* g, const Ba
   Dev& d = c->d;
   d.NE = NE; d.NF = NF; d.NG = NG;
   d.bs = 128;
+  d.cpw = 8;
+  if (const char* e = std::getenv("RC_LUSGS_CPW")) {
+    const int v = std::atoi(e);
+    if (v == 1 || v == 2 || v == 4 || v == 8) d.cpw = v;
+  }
   int st = 0;
   double* p;
   unsigned char* u8;
@@ -1445,8 +1529,8 @@ int init_impl(const rc_mesh* m, const rc_thermo* t, const rc_config* g, const Ba
   double* e;
   st |= dev_zeros(c, 1, &e);
   d.err = reinterpret_cast<unsigned*>(e);
-  st |= dev_zeros(c, 1, &e);
-  c->bar_count = reinterpret_cast<unsigned*>(e);
+  c->nlevels = (int)(c->fwd_off.size() + c->bwd_off.size()) - 2;
+  st |= dev_zeros(c, (size_t)std::max(c->nlevels, 1), &c->lvl_count);
   st |= dev_upload(c, c->fwd_off, &c->fwd_off_dev);
   st |= dev_upload(c, c->bwd_off, &c->bwd_off_dev);
   {  // sweep tables in level order
@@ -1676,20 +1760,22 @@ int rc_autotune(rc_ctx* c, int iters, char* report, int report_len) {
   };
   cudaMemcpyAsync(save, c->d.PA, n * sizeof(double), cudaMemcpyDeviceToDevice, c->stream);
   cudaMemcpyAsync(save + n, c->d.WA, n * sizeof(double), cudaMemcpyDeviceToDevice, c->stream);
-  struct Cand { bool pers; int bs; };
+  struct Cand { bool pers; int bs; int cpw; };
   std::vector<Cand> cands;
   for (int pers = c->can_persistent ? 1 : 0; pers >= 0; --pers)
-    for (int bs : {128, 64, 32}) cands.push_back({pers != 0, bs});
+    for (int cpw : {8, 4, 2, 1})
+      for (int bs : {128, 64}) cands.push_back({pers != 0, bs, cpw});
   cudaEvent_t e0, e1;
   cudaEventCreate(&e0);
   cudaEventCreate(&e1);
   std::string rep;
   double best = 1e300;
-  Cand bc = {c->persistent, c->d.bs};
+  Cand bc = {c->persistent, c->d.bs, c->d.cpw};
   int st = RC_OK;
   for (const Cand& k : cands) {
     c->persistent = k.pers;
     c->d.bs = k.bs;
+    c->d.cpw = k.cpw;
     drop_graphs(c);
     restore();
     for (int w = 0; w < 2 && !st; ++w) st = rc_lusgs_stage(c, 1);
@@ -1701,19 +1787,21 @@ int rc_autotune(rc_ctx* c, int iters, char* report, int report_len) {
     float ms = 0.f;
     cudaEventElapsedTime(&ms, e0, e1);
     const double per = ms / iters;
-    rep += std::string(k.pers ? "persistent" : "levels") + " bs=" + std::to_string(k.bs) + ": " +
-           std::to_string(per) + " ms; ";
+    rep += std::string(k.pers ? "persistent" : "levels") + " bs=" + std::to_string(k.bs) + " cpw=" +
+           std::to_string(k.cpw) + ": " + std::to_string(per) + " ms; ";
     if (per < best) { best = per; bc = k; }
   }
   c->persistent = bc.pers;
   c->d.bs = bc.bs;
+  c->d.cpw = bc.cpw;
   drop_graphs(c);
   restore();
   cudaStreamSynchronize(c->stream);
   cudaEventDestroy(e0);
   cudaEventDestroy(e1);
   cudaFree(save);
-  rep += std::string("chosen: ") + (bc.pers ? "persistent" : "levels") + " bs=" + std::to_string(bc.bs);
+  rep += std::string("chosen: ") + (bc.pers ? "persistent" : "levels") + " bs=" + std::to_string(bc.bs) +
+         " cpw=" + std::to_string(bc.cpw);
   if (report && report_len > 0) {
     std::snprintf(report, (size_t)report_len, "%s", rep.c_str());
   }

@@ -11,6 +11,7 @@ constexpr int MAXF = 4;  // faces per cell (triangles and quadrilaterals)
 struct Dev {
   int NE, NF, NG;
   int bs;                        // threads per block of the cell and face kernels (32, 64 or 128)
+  int cpw;                       // LU-SGS cells per warp (1, 2, 4 or 8; 4 lanes per cell)
   // cells
   const double* vol;
   const double* rinv;            // [2*NE] 1./reflen
@@ -111,34 +112,6 @@ __device__ __forceinline__ unsigned ld_acquire(const unsigned* p) {
   return v;
 }
 
-// Grid-wide barrier of a cooperative (all blocks co-resident) launch.  `count`
-// is zeroed before the launch and `seq` numbers the barriers of the launch.
-// The wait is bounded: after about 2^22 polls, or as soon as another block has
-// given up, ERR_SYNC is latched and every block returns false so the kernel
-// can exit instead of waiting forever.
-__device__ __forceinline__ bool grid_sync(unsigned* count, unsigned seq, unsigned* err) {
-  __shared__ int ok;
-  __syncthreads();
-  if (threadIdx.x == 0) {
-    __threadfence();
-    atomicAdd(count, 1u);
-    const unsigned target = (seq + 1u) * gridDim.x;
-    int good = 1;
-    for (unsigned spin = 0; ld_acquire(count) < target; ++spin) {
-      if (spin > (1u << 22) || (ld_acquire(err) & ERR_SYNC)) {
-        atomicOr(err, ERR_SYNC);
-        good = 0;
-        break;
-      }
-      __nanosleep(32);
-    }
-    __threadfence();
-    ok = good;
-  }
-  __syncthreads();
-  return ok != 0;
-}
-
 // WA += hWA and update_primitve_variables (update_flow_variables.f90:112-156).
 template <int NSP>
 __device__ __forceinline__ void update_cell(const Dev& d, const ThermoDev<NSP>& th, int i, unsigned& err) {
@@ -166,22 +139,33 @@ __device__ __forceinline__ void update_cell(const Dev& d, const ThermoDev<NSP>& 
   if (i == 0 && isnan(W[0])) err |= ERR_NAN;
 }
 
-// Wait until *f becomes non-zero (a cell's sweep result is published).
-// Bounded: after 2^24 polls, or once another waiter has given up, ERR_SYNC is
-// latched and false returned; the caller then goes on with stale data and the
-// host sees the error at its next synchronising call.
-__device__ __forceinline__ bool wait_flag(const unsigned* f, unsigned* err) {
-  for (unsigned spin = 0; ld_acquire(f) == 0u; ++spin) {
-    if ((spin & 255u) == 255u && (spin > (1u << 24) || (ld_acquire(err) & ERR_SYNC))) {
-      atomicOr(err, ERR_SYNC);
-      return false;
+// Level ordering of the persistent LU-SGS kernels.  wait_count: lane 0 of a
+// warp waits until the completion count of the previous level reaches its
+// number of chunks; the warp then reads what that level wrote.  The wait is
+// bounded: after about 2^24 polls, or as soon as another waiter has given up,
+// ERR_SYNC is latched and false returned, and the kernel returns.
+__device__ __forceinline__ bool wait_count(const unsigned* c, unsigned target, unsigned* err) {
+  int ok = 1;
+  if ((threadIdx.x & 31) == 0) {
+    for (unsigned spin = 0; ld_acquire(c) < target; ++spin) {
+      if ((spin & 255u) == 255u && (spin > (1u << 24) || (ld_acquire(err) & ERR_SYNC))) {
+        atomicOr(err, ERR_SYNC);
+        ok = 0;
+        break;
+      }
     }
   }
-  return true;
-}
-__device__ __forceinline__ void publish_flag(unsigned* f) {
+  ok = __shfl_sync(0xffffffffu, ok, 0);
+  __syncwarp();
   __threadfence();
-  asm volatile("st.release.gpu.global.u32 [%0], %1;" ::"l"(f), "r"(1u) : "memory");
+  return ok != 0;
+}
+// count_done: a warp's chunk of a level is done; every lane's stores are
+// made visible, then lane 0 counts the chunk.
+__device__ __forceinline__ void count_done(unsigned* c) {
+  __threadfence();
+  __syncwarp();
+  if ((threadIdx.x & 31) == 0) atomicAdd(c, 1u);
 }
 
 }  // namespace rc

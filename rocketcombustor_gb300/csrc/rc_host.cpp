@@ -683,6 +683,152 @@ const void* rc_case_array(const rc_case* c, const char* name, long* count) {
   return nullptr;
 }
 
+int rc_case_set_state(rc_case* c, const double* PA, const double* WA) {
+  if (!c || !PA || !WA) return RC_ERR_ARG;
+  std::copy(PA, PA + (size_t)c->NVar * c->NE, c->PA.begin());
+  std::copy(WA, WA + (size_t)c->NVar * c->NE, c->WA.begin());
+  return RC_OK;
+}
+
+// BackupData (output.f90:256-273): ttime, NE, then per cell x, y, PA(1:NVar).
+// List-directed in the reference; written here with 17 significant digits so
+// that Read_Backup (output.f90:276-338) restores the state bit for bit.
+int rc_case_write_backup(rc_case* c, const char* path, double ttime) {
+  if (!c || !path) return RC_ERR_ARG;
+  std::FILE* f = std::fopen(path, "w");
+  if (!f) { c->err = std::string("cannot write ") + path; return RC_ERR_ARG; }
+  std::fprintf(f, " %.17E\n %d\n", ttime, c->NE);
+  for (int i = 0; i < c->NE; ++i) {
+    std::fprintf(f, " %.17E %.17E", c->CELLXY[2 * (size_t)i], c->CELLXY[2 * (size_t)i + 1]);
+    for (int k = 0; k < c->NVar; ++k) std::fprintf(f, " %.17E", c->PA[(size_t)i * c->NVar + k]);
+    std::fputc('\n', f);
+  }
+  const bool ok = std::fclose(f) == 0;
+  if (!ok) { c->err = std::string("cannot write ") + path; return RC_ERR_ARG; }
+  return RC_OK;
+}
+
+namespace {
+// Fortran Ew.d edit descriptor: 0.d1d2..dd E+xx (leading zero, d digits)
+std::string fortran_e(double x, int d, int w) {
+  char m[64];
+  std::string out;
+  if (x == 0.0 || !std::isfinite(x)) {
+    std::snprintf(m, sizeof m, "%.*f", d, 0.0);
+    out = std::isfinite(x) ? std::string(m) + "E+00" : (x != x ? "NaN" : (x > 0 ? "Infinity" : "-Infinity"));
+  } else {
+    int e = (int)std::floor(std::log10(std::fabs(x))) + 1;
+    double mant = x / std::pow(10.0, e);
+    if (std::fabs(mant) >= 1.0) { mant /= 10.0; ++e; }
+    if (std::fabs(mant) < 0.1) { mant *= 10.0; --e; }
+    std::snprintf(m, sizeof m, "%.*f", d, mant);
+    if (std::fabs(std::atof(m)) >= 1.0) { mant /= 10.0; ++e; std::snprintf(m, sizeof m, "%.*f", d, mant); }
+    char ex[16];
+    std::snprintf(ex, sizeof ex, "E%c%02d", e < 0 ? '-' : '+', std::abs(e));
+    out = std::string(m) + ex;
+  }
+  if ((int)out.size() < w) out = std::string((size_t)w - out.size(), ' ') + out;
+  return out;
+}
+std::string ltrim(const std::string& s) {
+  const size_t a = s.find_first_not_of(' ');
+  return a == std::string::npos ? std::string() : s.substr(a);
+}
+}  // namespace
+
+// output_vtk (output.f90:4-227): legacy ASCII VTK of the cell-centred rho, u,
+// v, p, T, Ma, Y_1..Y_Nsp and the production rates of the transported species
+// (compute_production_rate, chemical_kinetics.f90:109-165, at the state; the
+// reference writes its module copy from the last sourceterm).  Values below
+// 1e-15 are written as 0 as in the reference (:52-56).
+int rc_case_write_vtk(rc_case* c, const char* path) {
+  if (!c || !path) return RC_ERR_ARG;
+  const int NE = c->NE, Nsp = c->Nsp, NVar = c->NVar;
+  std::vector<double> rho(NE), ma(NE), Y((size_t)Nsp * NE), prod((size_t)Nsp * NE, 0.0);
+  std::vector<double> y(Nsp), w(Nsp);
+  try {
+    for (int i = 0; i < NE; ++i) {
+      const double* P = &c->PA[(size_t)i * NVar];
+      double s = 0.0;
+      for (int k = 0; k < Nsp - 1; ++k) { y[k] = P[4 + k]; s = s + y[k]; }
+      y[Nsp - 1] = 1.0 - s;
+      double Cp, gama, R;
+      c->gas(y.data(), P[3], Cp, gama, R);
+      rho[i] = P[0] / (R * P[3]);
+      const double ac = std::sqrt(gama * R * P[3]);
+      ma[i] = std::sqrt(P[1] * P[1] + P[2] * P[2]) / ac;
+      if (P[0] < 0 || rho[i] < 0 || P[3] < 0) {
+        c->err = "negative density/pressure/temperature in cell " + std::to_string(i + 1);
+        return RC_ERR_NEG_TIMESTEP;
+      }
+      if (c->combustion && Nsp > 1) {  // compute_production_rate, model 0 or 1
+        const double y0 = std::min(1.0, std::max(0.0, y[0])), y1 = std::min(1.0, std::max(0.0, y[1]));
+        double kf;
+        if (c->model == 0) {
+          kf = c->Af * rcm::exp(-c->E / (c->Rconstant * P[3]));
+          kf = kf * rcm::pow(y0 * rho[i] / (c->mw[0] * 1000), 0.2);
+          kf = kf * rcm::pow(y1 * rho[i] / (c->mw[1] * 1000), 1.3);
+        } else {
+          kf = (P[3] > 710.0) ? 1e4 : 0.0;
+          kf = kf * (y0 * rho[i] / (c->mw[0] * 1000));
+        }
+        for (int k = 0; k < Nsp; ++k) w[k] = 1000 * c->mw[k] * (c->cr[k] - c->cf[k]) * kf;
+        if (std::fabs(w[0]) < 1.0e-15)
+          for (int k = 0; k < Nsp; ++k) w[k] = 0.0;
+        for (int k = 0; k < Nsp; ++k) prod[(size_t)k * NE + i] = w[k];
+      }
+      for (int k = 0; k < Nsp; ++k) {
+        double v = y[k];
+        if (k < Nsp - 1 && std::fabs(v) < 1.0e-15) v = 0.0;
+        Y[(size_t)k * NE + i] = v;
+      }
+    }
+  } catch (const std::exception& e) {
+    c->err = e.what();
+    return RC_ERR_THERMO_T;
+  }
+  std::FILE* f = std::fopen(path, "w");
+  if (!f) { c->err = std::string("cannot write ") + path; return RC_ERR_ARG; }
+  std::fprintf(f, "# vtk DataFile Version 1.0\nUnstructured Grid Format\nASCII\nDATASET UNSTRUCTURED_GRID\n");
+  std::fprintf(f, "POINTS %d double\n", c->NNT);
+  for (int n = 0; n < c->NNT; ++n)
+    std::fprintf(f, "%s\n", ltrim(fortran_e(c->COOR[2 * (size_t)n], 8, 15) + fortran_e(c->COOR[2 * (size_t)n + 1], 8, 15) +
+                                   fortran_e(0.0, 8, 15)).c_str());
+  long nsize = NE;
+  for (int i = 0; i < NE; ++i) nsize += c->KFace[i];
+  std::fprintf(f, "CELLS %d %ld\n", NE, nsize);
+  for (int i = 0; i < NE; ++i) {
+    std::fprintf(f, "%d", c->KFace[i]);
+    for (int k = 0; k < c->KFace[i]; ++k) std::fprintf(f, " %d", c->N[(size_t)k + 4 * (size_t)i] - 1);
+    std::fputc('\n', f);
+  }
+  std::fprintf(f, "CELL_TYPES %d\n", NE);
+  for (int i = 0; i < NE; ++i) std::fprintf(f, "%d\n", c->KFace[i] == 3 ? 5 : 9);
+  std::fprintf(f, "CELL_DATA %d\n", NE);
+  auto scalars = [&](const char* name, const double* v, size_t stride, int d, int wdt) {
+    std::fprintf(f, "SCALARS %s double\nLOOKUP_TABLE default\n", name);
+    for (int i = 0; i < NE; ++i) std::fprintf(f, "%s\n", ltrim(fortran_e(v[(size_t)i * stride], d, wdt)).c_str());
+  };
+  std::vector<double> col(NE);
+  scalars("rho", rho.data(), 1, 8, 20);
+  for (int q = 0; q < 4; ++q) {
+    for (int i = 0; i < NE; ++i) col[i] = c->PA[(size_t)i * NVar + (q == 0 ? 1 : q == 1 ? 2 : q == 2 ? 0 : 3)];
+    scalars(q == 0 ? "u" : q == 1 ? "v" : q == 2 ? "p" : "T", col.data(), 1, 8, 20);
+  }
+  scalars("Ma", ma.data(), 1, 8, 20);
+  for (int k = 0; k < Nsp; ++k) {
+    const std::string nm = "Y" + std::to_string(k + 1);
+    scalars(nm.c_str(), &Y[(size_t)k * NE], 1, 12, 30);
+  }
+  for (int k = 0; k < Nsp - 1; ++k) {
+    const std::string nm = "Production_rate_" + std::to_string(k + 1);
+    scalars(nm.c_str(), &prod[(size_t)k * NE], 1, 12, 30);
+  }
+  const bool ok = std::fclose(f) == 0;
+  if (!ok) { c->err = std::string("cannot write ") + path; return RC_ERR_ARG; }
+  return RC_OK;
+}
+
 int rc_run_steady(rc_case* c, int precision, int device, long nsteps, long every, double* hist) {
   rc_mesh m;
   rc_thermo t;

@@ -512,31 +512,62 @@ __global__ void __launch_bounds__(128) k_gather32(const Dev d, int visc, int com
 // ---------------------------------------------------------------- LU-SGS ---
 // Four lanes per cell as in the FP64 sweep; the off-diagonal terms in FP32,
 // the diagonal division in FP64.
+// The FP32 sweep step, split like the FP64 one (rc_core.cu): sweep_load32
+// reads the data the sweep does not change (and forms the FP64 reciprocal of
+// the diagonal), sweep_compute32 the increments and the arithmetic.
+template <int NSP>
+struct SweepPre32 {
+  int i;
+  bool valid, act;
+  int j;
+  float dx, dy, pp, uu, vv, tt, rr, gama, roe, aF;
+  double rdd;
+  float cs[NSP];
+  float Yk[NSP > 1 ? NSP - 1 : 1];
+};
 template <int NSP, bool FWD>
-__device__ __forceinline__ void sweep_step32(const Dev& d, const ThermoDev32<NSP>& th, int t, int tend, int q) {
-  constexpr int V = 3 + NSP;
+__device__ __forceinline__ SweepPre32<NSP> sweep_load32(const Dev& d, int t, int tend, int q) {
   constexpr int DIR = FWD ? 0 : 1;
-  const bool valid = t < tend;
+  SweepPre32<NSP> p;
+  p.valid = t < tend;
   const int NE = d.NE, NF = d.NF;
-  const int i = valid ? d.swi[DIR][t] : 0;
-  const int j = valid ? d.swj[DIR][q * NE + t] : -1;
-  const int fs = valid ? d.swf[DIR][q * NE + t] : 0;
-  double R0 = 0.0, R1 = 0.0, rdd = 0.0;
-  if (valid) {  // own residual (variables q, q+4) and FP64 diagonal, issued early
-    R0 = d.hWA[q * NE + i];
-    if (q + 4 < V) R1 = d.hWA[(q + 4) * NE + i];
-    rdd = 1.0 / d.dd[i];
+  p.i = p.valid ? d.swi[DIR][t] : 0;
+  p.j = p.valid ? d.swj[DIR][q * NE + t] : -1;
+  const int fs = p.valid ? d.swf[DIR][q * NE + t] : 0;
+  p.rdd = p.valid ? 1.0 / d.dd[p.i] : 0.0;
+  p.act = p.j >= 0;
+  if (p.act) {
+    const int j = p.j, f = fs >= 0 ? fs : ~fs;
+    p.dx = d.fvec32[f];
+    p.dy = d.fvec32[NF + f];
+    if (fs < 0) { p.dx = -p.dx; p.dy = -p.dy; }
+    p.pp = d.PA32[0 * NE + j]; p.uu = d.PA32[1 * NE + j]; p.vv = d.PA32[2 * NE + j]; p.tt = d.PA32[3 * NE + j];
+    p.rr = d.cst32[0 * NE + j]; p.gama = d.cst32[1 * NE + j]; p.roe = d.cst32[2 * NE + j];
+    p.aF = d.alpaF32[f];
+#pragma unroll
+    for (int k = 0; k < NSP; ++k) p.cs[k] = d.cst32[(3 + k) * NE + j];
+#pragma unroll
+    for (int k = 0; k < NSP - 1; ++k) p.Yk[k] = d.PA32[(4 + k) * NE + j];
+  }
+  return p;
+}
+template <int NSP, bool FWD>
+__device__ __forceinline__ void sweep_compute32(const Dev& d, const ThermoDev32<NSP>& th, const SweepPre32<NSP>& p,
+                                                int q, float* wsm) {
+  constexpr int V = 3 + NSP;
+  const int NE = d.NE;
+  double R0 = 0.0, R1 = 0.0;
+  if (p.valid) {
+    R0 = d.hWA[q * NE + p.i];
+    if (q + 4 < V) R1 = d.hWA[(q + 4) * NE + p.i];
   }
   float c[V];
 #pragma unroll
   for (int k = 0; k < V; ++k) c[k] = 0.f;
-  const bool act = j >= 0;
-  if (act) {
-    const int f = fs >= 0 ? fs : ~fs;
-    float dx = d.fvec32[f], dy = d.fvec32[NF + f];
-    if (fs < 0) { dx = -dx; dy = -dy; }
-    const float pp = d.PA32[0 * NE + j], uu = d.PA32[1 * NE + j], vv = d.PA32[2 * NE + j], tt = d.PA32[3 * NE + j];
-    const float rr = d.cst32[0 * NE + j], gama = d.cst32[1 * NE + j], roe = d.cst32[2 * NE + j];
+  if (p.act) {
+    const int j = p.j;
+    const float dx = p.dx, dy = p.dy, pp = p.pp, uu = p.uu, vv = p.vv, tt = p.tt, rr = p.rr, gama = p.gama,
+                roe = p.roe;
     const float rou = rr * uu, rov = rr * vv;
     const float drr = d.dU32[0 * NE + j], dru = d.dU32[1 * NE + j], drv = d.dU32[2 * NE + j],
                 dre = d.dU32[3 * NE + j];
@@ -550,39 +581,48 @@ __device__ __forceinline__ void sweep_step32(const Dev& d, const ThermoDev32<NSP
     float s1 = 0.f, s2 = 0.f;
 #pragma unroll
     for (int k = 0; k < NSP; ++k) {
-      s1 += d.cst32[(3 + k) * NE + j] * dry[k];
+      s1 += p.cs[k] * dry[k];
       s2 += th.R[k] * dry[k];
     }
     const float gm1 = gama - 1.f;
     const float dpp = gm1 * (dre - s1 + tt * s2 * gama / gm1 - 0.5f * (dru * uu + duu * rou + drv * vv + dvv * rov));
     const float un = uu * dx + vv * dy, dun = duu * dx + dvv * dy;
-    const float aF = d.alpaF32[f];
+    const float aF = p.aF;
     c[0] = 0.5f * (-aF * drr + dru * dx + drv * dy);
     c[1] = 0.5f * (-aF * dru + dru * un + rou * dun + dpp * dx);
     c[2] = 0.5f * (-aF * drv + drv * un + rov * dun + dpp * dy);
     c[3] = 0.5f * (-aF * dre + dun * (roe + pp) + un * (dre + dpp));
 #pragma unroll
-    for (int k = 0; k < NSP - 1; ++k) c[4 + k] = 0.5f * (-aF * dry[k] + dry[k] * un + rr * d.PA32[(4 + k) * NE + j] * dun);
+    for (int k = 0; k < NSP - 1; ++k) c[4 + k] = 0.5f * (-aF * dry[k] + dry[k] * un + rr * p.Yk[k] * dun);
   }
-  const int base = (threadIdx.x & 31) & ~3;
+  // terms in slot order through the warp's shared scratch (see sweep_compute)
+  const int lane = threadIdx.x & 31, base = lane & ~3;
+  __syncwarp();
+#pragma unroll
+  for (int k = 0; k < V; ++k) wsm[k * 32 + lane] = c[k];
+  __syncwarp();
   float df0 = 0.f, df1 = 0.f;
 #pragma unroll
-  for (int sl = 0; sl < 4; ++sl)
-#pragma unroll
-    for (int k = 0; k < V; ++k) {
-      const float cs = __shfl_sync(0xffffffffu, c[k], base + sl);
-      if (k == q) df0 += cs;
-      if (k == q + 4) df1 += cs;
-    }
-  if (!valid) return;
+  for (int sl = 0; sl < 4; ++sl) {
+    df0 += wsm[q * 32 + base + sl];
+    if (q + 4 < V) df1 += wsm[(q + 4) * 32 + base + sl];
+  }
+  if (!p.valid) return;
+  const double rdd = p.rdd;
   const double u0 = FWD ? (R0 - (double)df0) * rdd : R0 - (double)df0 * rdd;
-  d.hWA[q * NE + i] = u0;
-  d.dU32[q * NE + i] = (float)u0;
+  d.hWA[q * NE + p.i] = u0;
+  d.dU32[q * NE + p.i] = (float)u0;
   if (q + 4 < V) {
     const double u1 = FWD ? (R1 - (double)df1) * rdd : R1 - (double)df1 * rdd;
-    d.hWA[(q + 4) * NE + i] = u1;
-    d.dU32[(q + 4) * NE + i] = (float)u1;
+    d.hWA[(q + 4) * NE + p.i] = u1;
+    d.dU32[(q + 4) * NE + p.i] = (float)u1;
   }
+}
+template <int NSP, bool FWD>
+__device__ __forceinline__ void sweep_step32(const Dev& d, const ThermoDev32<NSP>& th, int t, int tend, int q,
+                                             float* wsm) {
+  const SweepPre32<NSP> p = sweep_load32<NSP, FWD>(d, t, tend, q);
+  sweep_compute32<NSP, FWD>(d, th, p, q, wsm);
 }
 
 // FP32 copies for the FP32 sweeps when the residual comes from the FP64
@@ -601,31 +641,55 @@ __global__ void __launch_bounds__(128) k_pack32(const Dev d) {
 
 template <int NSP, bool FWD>
 __global__ void __launch_bounds__(32) k_sweep32(const Dev d, const ThermoDev32<NSP> th, int t0, int t1) {
-  const int gt = blockIdx.x * blockDim.x + threadIdx.x;
-  sweep_step32<NSP, FWD>(d, th, t0 + (gt >> 2), t1, gt & 3);
+  const int lt = threadIdx.x >> 2;
+  __shared__ float wsm[32 * (3 + NSP)];
+  sweep_step32<NSP, FWD>(d, th, lt < d.cpw ? t0 + blockIdx.x * d.cpw + lt : t1, t1, threadIdx.x & 3, wsm);
 }
 
-// Both FP32 sweeps in one cooperative launch with level barriers (the
-// schedule of the FP64 persistent kernel in rc_core.cu); the FP64 update runs
-// afterwards as its own kernel.
+// Both FP32 sweeps in one cooperative launch (chunks of d.cpw cells), ordered by per-level completion
+// counters (the schedule of k_lusgs_persistent in rc_core.cu); the FP64
+// update runs afterwards as its own kernel.
 constexpr int PERS32_THREADS = 256;
 template <int NSP>
 __global__ void __launch_bounds__(PERS32_THREADS) k_lusgs_persistent32(const Dev d, const ThermoDev32<NSP> th,
                                                                        const int* __restrict__ foff, int nf,
                                                                        const int* __restrict__ boff, int nb,
-                                                                       unsigned* count) {
+                                                                       unsigned* cnt) {
   const int G = gridDim.x, wpb = PERS32_THREADS / 32, w = threadIdx.x >> 5;
+  const int gw = blockIdx.x + w * G, nw = G * wpb;
   const int lt = (threadIdx.x & 31) >> 2, q = threadIdx.x & 3;
-  unsigned seq = 0;
-  for (int l = 0; l < nf; ++l) {
-    const int t0 = foff[l], t1 = foff[l + 1], nch = (t1 - t0 + 7) >> 3;
-    for (int c = blockIdx.x + w * G; c < nch; c += G * wpb) sweep_step32<NSP, true>(d, th, t0 + c * 8 + lt, t1, q);
-    if (!grid_sync(count, seq++, d.err)) return;
-  }
-  for (int l = 0; l < nb; ++l) {
-    const int t0 = boff[l], t1 = boff[l + 1], nch = (t1 - t0 + 7) >> 3;
-    for (int c = blockIdx.x + w * G; c < nch; c += G * wpb) sweep_step32<NSP, false>(d, th, t0 + c * 8 + lt, t1, q);
-    if (!grid_sync(count, seq++, d.err)) return;
+  __shared__ float wsm_all[PERS32_THREADS / 32][32 * (3 + NSP)];
+  float* wsm = wsm_all[w];
+  const int nl = nf + nb, cpw = d.cpw;
+  auto nchunks = [&](int L) {
+    const int a = L < nf ? foff[L] : boff[L - nf], b = L < nf ? foff[L + 1] : boff[L - nf + 1];
+    return (unsigned)((b - a + cpw - 1) / cpw);
+  };
+  for (int L = 0; L < nl; ++L) {
+    const bool fwd = L < nf;
+    const int t0 = fwd ? foff[L] : boff[L - nf], t1 = fwd ? foff[L + 1] : boff[L - nf + 1];
+    const int nch = (t1 - t0 + cpw - 1) / cpw;
+    if (gw >= nch) continue;
+    bool waited = L == 0;
+    for (int c = gw; c < nch; c += nw) {
+      const int t = lt < cpw ? t0 + c * cpw + lt : t1;
+      if (fwd) {
+        const SweepPre32<NSP> p = sweep_load32<NSP, true>(d, t, t1, q);
+        if (!waited) {
+          if (!wait_count(cnt + L - 1, nchunks(L - 1), d.err)) return;
+          waited = true;
+        }
+        sweep_compute32<NSP, true>(d, th, p, q, wsm);
+      } else {
+        const SweepPre32<NSP> p = sweep_load32<NSP, false>(d, t, t1, q);
+        if (!waited) {
+          if (!wait_count(cnt + L - 1, nchunks(L - 1), d.err)) return;
+          waited = true;
+        }
+        sweep_compute32<NSP, false>(d, th, p, q, wsm);
+      }
+      count_done(cnt + L);
+    }
   }
 }
 
@@ -661,10 +725,10 @@ void mixed_gather(const Dev& d, int visc, int comb, cudaStream_t s) {
 template <int NSP>
 void mixed_sweep(const Dev& d, const void* th32, bool fwd, int t0, int t1, cudaStream_t s) {
   const auto& th = *static_cast<const ThermoDev32<NSP>*>(th32);
-  if (fwd) k_sweep32<NSP, true><<<nblk(4L * (t1 - t0), 32), 32, 0, s>>>(d, th, t0, t1);
-  else k_sweep32<NSP, false><<<nblk(4L * (t1 - t0), 32), 32, 0, s>>>(d, th, t0, t1);
+  if (fwd) k_sweep32<NSP, true><<<nblk(t1 - t0, d.cpw), 32, 0, s>>>(d, th, t0, t1);
+  else k_sweep32<NSP, false><<<nblk(t1 - t0, d.cpw), 32, 0, s>>>(d, th, t0, t1);
 }
-// Cooperative launch of the persistent FP32 sweeps (barrier counter zeroed by the caller).
+// Cooperative launch of the persistent FP32 sweeps (level counters zeroed by the caller).
 template <int NSP>
 cudaError_t mixed_lusgs_persistent(const Dev& d, const void* th32, const int* foff, int nf, const int* boff, int nb,
                                    unsigned* count, int grid, cudaStream_t s) {

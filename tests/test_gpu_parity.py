@@ -165,16 +165,20 @@ def test_device_stop_condition_is_reported(case_t1):
 
 @pytest.mark.parametrize("precision", [rc.RC_PREC_FP64, rc.RC_PREC_MIXED])
 def test_persistent_and_per_level_schedules_agree(case_root, precision, monkeypatch):
-    """The cooperative one-launch LU-SGS and the one-launch-per-level LU-SGS
-    run the same recurrences: identical states after 30 iterations."""
-    d = make_case(case_root, "t2")
+    """The cooperative one-launch LU-SGS and the one-launch-per-level LU-SGS,
+    with 8 or 1 cells per warp, run the same recurrences: identical states
+    after 30 iterations."""
+    d = make_case(case_root, "c1", nx=40, ny=8)
     c = rc.Case(d)
     states = []
     for sched in ("persistent", "levels"):
-        monkeypatch.setenv("RC_LUSGS_SCHEDULE", sched)
-        s = rc.Solver(c, precision=precision)
-        s.run(30)
-        states.append(s.get_state())
-        s.close()
-    assert np.array_equal(states[0][0], states[1][0])
-    assert np.array_equal(states[0][1], states[1][1])
+        for cpw in ("8", "1"):
+            monkeypatch.setenv("RC_LUSGS_SCHEDULE", sched)
+            monkeypatch.setenv("RC_LUSGS_CPW", cpw)
+            s = rc.Solver(c, precision=precision)
+            s.run(30)
+            states.append(s.get_state())
+            s.close()
+    for st in states[1:]:
+        assert np.array_equal(states[0][0], st[0])
+        assert np.array_equal(states[0][1], st[1])

@@ -62,3 +62,37 @@ def test_setup_matches_oracle_bitwise(case_root, name, over):
 def test_bad_case_reports_error(tmp_path):
     with pytest.raises(rc.RcError):
         rc.Case(str(tmp_path / "missing"))
+
+
+def test_backup_round_trip(case_root, tmp_path):
+    """BackupData then Read_Backup (through rc_case_open) restores the state bit for bit."""
+    import shutil
+    d = make_case(case_root, "t2")
+    c = rc.Case(d)
+    PA = c.array("PA").copy()
+    rng = np.random.default_rng(0)
+    PA[:, 3] *= 1 + 1e-3 * rng.standard_normal(c.NE)  # a state that is not the file's
+    c.set_state(PA, c.array("WA").copy())
+    d2 = str(tmp_path / "copy")
+    shutil.copytree(d, d2)
+    c.write_backup(d2 + "/fvp1.sav", ttime=1.25)
+    c2 = rc.Case(d2)
+    assert np.array_equal(c2.array("PA"), PA)
+
+
+def test_vtk_writer(case_root, tmp_path):
+    d = make_case(case_root, "t2")
+    c = rc.Case(d)
+    path = str(tmp_path / "out.vtk")
+    c.write_vtk(path)
+    lines = open(path).read().split("\n")
+    assert lines[0] == "# vtk DataFile Version 1.0" and lines[3] == "DATASET UNSTRUCTURED_GRID"
+    assert lines[4] == f"POINTS {c.NNT} double"
+    i = lines.index(f"CELL_DATA {c.NE}")
+    names = [ln.split()[1] for ln in lines[i:] if ln.startswith("SCALARS")]
+    assert names == ["rho", "u", "v", "p", "T", "Ma", "Y1", "Y2", "Y3", "Y4",
+                     "Production_rate_1", "Production_rate_2", "Production_rate_3"]
+    k = lines.index("SCALARS p double")
+    p = np.array([float(x) for x in lines[k + 2:k + 2 + c.NE]])
+    np.testing.assert_allclose(p, c.array("PA")[:, 0], rtol=1e-7)  # e20.8: 8 significant digits
+    assert lines[lines.index(f"CELLS {c.NE} {4 * c.NE}") + 1].split()[0] == "3"
