@@ -247,7 +247,9 @@ def main():
             s = rc.Solver(case, precision=prec, device=local, stream=stream.cuda_stream)
             if args.chem == "integrated":
                 s.set_chemistry(rc.RC_CHEM_INTEGRATED)
+            tune = s.autotune(3) if not os.environ.get("RC_LUSGS_SCHEDULE") else "fixed by RC_LUSGS_SCHEDULE"
             r, clk_f = time_form(s, args, stream, flush, dist, torch, rc)
+            r["autotune"] = tune
             if clk is None:
                 clk = clk_f
             states[form] = s.get_state()
@@ -295,6 +297,7 @@ def main():
             "subroutine_ms": sub_ms,
             "stage_algorithmic_gbs": ab["stage"] * NE / (t_max / args.steps) / 1e9,
             "levels": head["levels"],
+            "autotune": head.get("autotune"),
         }
         if args.chem == "integrated":
             line["config"]["chemistry"] = "integrated (per-cell linearly implicit substeps, tol 0.05)"
@@ -305,7 +308,7 @@ def main():
             for form in forms_req:
                 r = results[form]
                 f = {"value": NE * args.steps / r["t_local"], "ms_per_step": 1e3 * r["t_local"] / args.steps,
-                     "e2e": r["e2e"]["value"], "gpu_launches": r["launches"]}
+                     "e2e": r["e2e"]["value"], "gpu_launches": r["launches"], "autotune": r.get("autotune")}
                 if form != "fp64":
                     st = states[form][0]
                     den = np.maximum(np.abs(ref).max(axis=0), 1e-300)
@@ -525,6 +528,7 @@ def surrogate_form(args, stream, flush, torch, rc, case):
             s.set_chemistry(rc.RC_CHEM_SURROGATE)
         else:
             s.set_chemistry(rc.RC_CHEM_INTEGRATED)
+        s.autotune(3)
         r, _ = time_form(s, args, stream, flush, None, torch, rc)
         states[name] = s.get_state()[0]
         forms[name] = {"value": case.NE * args.steps / r["t_local"], "ms_per_step": 1e3 * r["t_local"] / args.steps,

@@ -87,20 +87,33 @@ __device__ __forceinline__ void features(const float* raw, const Norm& nr, float
 }
 
 // ------------------------------------------------------------ fused forward
-constexpr int FS_W0 = 4 * TILE_BYTES;                 // 3 weight tiles + activation tile
+// FG warp groups of 4 warps per CTA, each with its own activation tile, TMEM
+// accumulator (128 columns) and mbarrier, work on different tiles of 128
+// samples: one group's CUDA-core epilogue overlaps another group's MMAs.  The
+// three hidden weight tiles are shared.
+constexpr int FG = 3;
+constexpr int FS_ACT = 3 * TILE_BYTES;                // + g * TILE_BYTES
+constexpr int FS_W0 = FS_ACT + FG * TILE_BYTES;
 constexpr int FS_BIAS = FS_W0 + H * NIN * 4;          // b0..b3
 constexpr int FS_W4 = FS_BIAS + 4 * H * 4;
 constexpr int FS_B4 = FS_W4 + NOUT * H * 4;
-constexpr int FS_BAR = FS_B4 + 16;
-constexpr int FS_SLOT = FS_BAR + 8;
-constexpr int FS_OK = FS_SLOT + 4;
-constexpr int FUSED_SMEM = FS_OK + 4 + 1024;          // + alignment slack
+constexpr int FS_BAR = FS_B4 + 16;                    // FG mbarriers
+constexpr int FS_SLOT = FS_BAR + 8 * FG;
+constexpr int FS_OK = FS_SLOT + 4;                    // FG flags
+constexpr int FUSED_SMEM = FS_OK + 4 * FG + 1024;     // + alignment slack
+constexpr uint32_t FUSED_TMEM_COLS = FG * 128 <= 256 ? 256 : 512;
 static_assert(FS_BAR % 8 == 0, "mbarrier alignment");
+static_assert(FUSED_SMEM <= 227 * 1024, "shared memory");
+
+// barrier of the 128 threads of group g (named barrier 1 + g; 0 is __syncthreads)
+__device__ __forceinline__ void group_sync(int g) {
+  asm volatile("bar.sync %0, 128;" ::"r"(1 + g) : "memory");
+}
 
 template <class Io>
-__global__ void __launch_bounds__(128, 1) k_mlp_fused(const float* __restrict__ params,
-                                                      const __nv_bfloat16* __restrict__ Wb, Norm nr, Io io, int n,
-                                                      unsigned* err) {
+__global__ void __launch_bounds__(128 * FG, 1) k_mlp_fused(const float* __restrict__ params,
+                                                           const __nv_bfloat16* __restrict__ Wb, Norm nr, Io io,
+                                                           int n, unsigned* err) {
   extern __shared__ uint8_t smem_raw[];
   uint8_t* base = smem_raw + ((1024u - (umma::smem_u32(smem_raw) & 1023u)) & 1023u);
   const uint32_t sbase = umma::smem_u32(base);
@@ -108,44 +121,44 @@ __global__ void __launch_bounds__(128, 1) k_mlp_fused(const float* __restrict__ 
   float* bias = reinterpret_cast<float*>(base + FS_BIAS);
   float* W4 = reinterpret_cast<float*>(base + FS_W4);
   float* b4 = reinterpret_cast<float*>(base + FS_B4);
-  uint64_t* bar = reinterpret_cast<uint64_t*>(base + FS_BAR);
   uint32_t* slot = reinterpret_cast<uint32_t*>(base + FS_SLOT);
-  int* s_ok = reinterpret_cast<int*>(base + FS_OK);
-  const int t = threadIdx.x, warp = t >> 5;
+  const int g = threadIdx.x >> 7, t = threadIdx.x & 127, warp = t >> 5;
+  uint64_t* bar = reinterpret_cast<uint64_t*>(base + FS_BAR) + g;
+  int* s_ok = reinterpret_cast<int*>(base + FS_OK) + g;
 
   // the three hidden-layer weight tiles (B operands: row = output, K = input)
-  for (int q = t; q < 3 * 2048; q += 128) {
+  for (int q = threadIdx.x; q < 3 * 2048; q += 128 * FG) {
     const int l = q >> 11, r = (q >> 4) & 127, c = q & 15;
     const uint4 v = reinterpret_cast<const uint4*>(Wb)[q];
     *reinterpret_cast<uint4*>(base + l * TILE_BYTES + umma::sw128_offset(r, c * 8, 128)) = v;
   }
-  for (int q = t; q < H * NIN; q += 128) W0[q] = params[OFF_W0 + q];
-  for (int q = t; q < H; q += 128) {
+  for (int q = threadIdx.x; q < H * NIN; q += 128 * FG) W0[q] = params[OFF_W0 + q];
+  for (int q = threadIdx.x; q < H; q += 128 * FG) {
     bias[q] = params[OFF_B0 + q];
     for (int l = 1; l <= 3; ++l) bias[l * H + q] = params[off_b(l) + q];
   }
-  for (int q = t; q < NOUT * H; q += 128) W4[q] = params[OFF_W4 + q];
-  if (t < NOUT) b4[t] = params[OFF_B4 + t];
+  for (int q = threadIdx.x; q < NOUT * H; q += 128 * FG) W4[q] = params[OFF_W4 + q];
+  if (threadIdx.x < NOUT) b4[threadIdx.x] = params[OFF_B4 + threadIdx.x];
   if (t == 0) umma::mbar_init(bar, 1);
-  if (warp == 0) {
-    umma::tmem_alloc(slot, 128);
+  if (threadIdx.x < 32) {
+    umma::tmem_alloc(slot, FUSED_TMEM_COLS);
     umma::tmem_relinquish();
   }
   umma::tc_fence_before();
   __syncthreads();
   umma::tc_fence_after();
-  const uint32_t tmem = *slot;
-  const uint32_t act = sbase + 3 * TILE_BYTES;
-  uint8_t* actp = base + 3 * TILE_BYTES;
+  const uint32_t tmem = *slot, tmem_g = tmem + (uint32_t)(g * 128);
+  const uint32_t act = sbase + FS_ACT + g * TILE_BYTES;
+  uint8_t* actp = base + FS_ACT + g * TILE_BYTES;
   uint32_t phase = 0;
   bool ok = true;
   const int ntiles = (n + 127) / 128;
-  for (int tile = blockIdx.x; tile < ntiles && ok; tile += gridDim.x) {
+  for (int tile = blockIdx.x * FG + g; tile < ntiles && ok; tile += gridDim.x * FG) {
     const int s = tile * 128 + t;
     float xn[NIN];
     typename Io::Local loc;
     io.load(s, s < n, nr, xn, loc);
-    // layer 0 on the CUDA cores -> row t of the activation tile
+    // layer 0 on the CUDA cores -> row t of the group's activation tile
     for (int c8 = 0; c8 < 16; ++c8) {
       float a[8];
 #pragma unroll
@@ -162,24 +175,24 @@ __global__ void __launch_bounds__(128, 1) k_mlp_fused(const float* __restrict__ 
     for (int l = 1; l <= 3; ++l) {
       umma::fence_async_smem();
       umma::tc_fence_before();
-      __syncthreads();
+      group_sync(g);
       if (t == 0) {
         umma::tc_fence_after();
 #pragma unroll
         for (int kk = 0; kk < 8; ++kk)
-          umma::mma_bf16(tmem, umma::sdesc_k(act, 128, kk), umma::sdesc_k(sbase + (l - 1) * TILE_BYTES, 128, kk),
+          umma::mma_bf16(tmem_g, umma::sdesc_k(act, 128, kk), umma::sdesc_k(sbase + (l - 1) * TILE_BYTES, 128, kk),
                          IDESC, kk > 0 ? 1u : 0u);
         umma::mma_commit(bar);
         *s_ok = umma::mbar_wait(bar, phase) ? 1 : 0;
       }
-      __syncthreads();
+      group_sync(g);
       phase ^= 1u;
       umma::tc_fence_after();
       if (!*s_ok) { ok = false; break; }
       const float* bl = bias + l * H;
       for (int c = 0; c < 4; ++c) {
         float v[32];
-        umma::tmem_ld32(tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)(c * 32), v);
+        umma::tmem_ld32(tmem_g + ((uint32_t)(warp * 32) << 16) + (uint32_t)(c * 32), v);
         if (l < 3) {
 #pragma unroll
           for (int c8 = 0; c8 < 4; ++c8) {
@@ -206,9 +219,9 @@ __global__ void __launch_bounds__(128, 1) k_mlp_fused(const float* __restrict__ 
   if (!ok && t == 0) atomicOr(err, ERR_SYNC);
   umma::tc_fence_before();
   __syncthreads();
-  if (warp == 0) {
+  if (threadIdx.x < 32) {
     umma::tc_fence_after();
-    umma::tmem_dealloc(tmem, 128);
+    umma::tmem_dealloc(tmem, FUSED_TMEM_COLS);
   }
 }
 
@@ -662,11 +675,11 @@ int mlp_fail(rc_mlp* m, cudaError_t e, const char* what) {
     if (e_ != cudaSuccess) return mlp_fail(m, e_, #call);     \
   } while (0)
 
-int fused_grid(rc_mlp* m, int n) {
+int fused_grid(int device, int n) {
   int nsm = 0;
-  cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, m->device);
-  const int tiles = (n + 127) / 128;
-  return tiles < nsm ? (tiles > 0 ? tiles : 1) : nsm;
+  cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, device);
+  const int ctas = ((n + 127) / 128 + mlp::FG - 1) / mlp::FG;
+  return ctas < nsm ? (ctas > 0 ? ctas : 1) : nsm;
 }
 
 template <class T>
@@ -711,13 +724,9 @@ namespace rc {
 // inference over the cells of a solver context (NSP must be 4)
 cudaError_t surrogate_source(const Dev& d, const void* th, const rc_mlp* net, float spread_tol, int* list,
                              unsigned* nlist, unsigned* nsurr, cudaStream_t s) {
-  int nsm = 0;
-  cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, net->device);
-  const int tiles = (d.NE + 127) / 128;
-  const int grid = tiles < nsm ? tiles : nsm;
   mlp::IoSolver io{d, *static_cast<const ThermoDev<4>*>(th), spread_tol, list, nlist, nsurr};
-  mlp::k_mlp_fused<mlp::IoSolver><<<grid > 0 ? grid : 1, 128, mlp::FUSED_SMEM, s>>>(net->params, net->Wb, net->norm,
-                                                                                    io, d.NE, d.err);
+  mlp::k_mlp_fused<mlp::IoSolver><<<fused_grid(net->device, d.NE), 128 * mlp::FG, mlp::FUSED_SMEM, s>>>(
+      net->params, net->Wb, net->norm, io, d.NE, d.err);
   return cudaGetLastError();
 }
 // outside stream capture, once per context
@@ -817,8 +826,8 @@ int rc_mlp_forward(rc_mlp* m, const float* d_x, int n, float* d_y, void* stream)
   if (n == 0) return RC_OK;
   cudaStream_t s = static_cast<cudaStream_t>(stream);
   mlp::IoRaw io{d_x, d_y};
-  mlp::k_mlp_fused<mlp::IoRaw><<<fused_grid(m, n), 128, mlp::FUSED_SMEM, s>>>(m->params, m->Wb, m->norm, io, n,
-                                                                              m->derr);
+  mlp::k_mlp_fused<mlp::IoRaw><<<fused_grid(m->device, n), 128 * mlp::FG, mlp::FUSED_SMEM, s>>>(m->params, m->Wb,
+                                                                                                m->norm, io, n, m->derr);
   MLP_CU(cudaGetLastError());
   return RC_OK;
 }
