@@ -28,6 +28,7 @@
 #include <cstdlib>
 #include <cstring>
 #include <string>
+#include <utility>
 #include <vector>
 
 #include "rc_gpu.h"
@@ -652,16 +653,23 @@ __device__ __forceinline__ void sweep_step(const Dev& d, const ThermoDev<NSP>& t
   sweep_compute<NSP, FWD>(d, th, p, q, wsm);
 }
 
-// one level of a sweep: block b (one warp) takes cells t0 + b*cpw .. + cpw-1
+// one level of a sweep: block b (one warp) takes cells t0 + b*cpw .. + cpw-1.
+// Launched as a programmatic dependent of the previous level: it lets the
+// next level start, loads what the sweep does not change, and only then
+// waits for the previous level.
 template <int NSP, bool FWD>
 __global__ void __launch_bounds__(32) k_sweep4(const Dev d, const ThermoDev<NSP> th, int t0, int t1) {
+  pdl_launch_dependents();
   const int lt = threadIdx.x >> 2;
   __shared__ double wsm[32 * (3 + NSP)];
-  sweep_step<NSP, FWD>(d, th, lt < d.cpw ? t0 + blockIdx.x * d.cpw + lt : t1, t1, threadIdx.x & 3, wsm);
+  const SweepPre<NSP> p = sweep_load<NSP, FWD>(d, lt < d.cpw ? t0 + blockIdx.x * d.cpw + lt : t1, t1, threadIdx.x & 3);
+  pdl_wait();
+  sweep_compute<NSP, FWD>(d, th, p, threadIdx.x & 3, wsm);
 }
 
 template <int NSP>
 __global__ void __launch_bounds__(128) k_update(const Dev d, const ThermoDev<NSP> th) {
+  pdl_wait();
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= d.NE) return;
   unsigned err = 0;
@@ -984,6 +992,20 @@ void q_persistent(rc_ctx* c) {
                      c->lvl_count);
   c->launches++;
 }
+// launch as a programmatic dependent of the previous kernel of the stream
+template <class... Args, class... Act>
+void launch_pdl(void (*kernel)(Args...), unsigned grid, unsigned block, cudaStream_t s, Act&&... args) {
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = dim3(grid);
+  cfg.blockDim = dim3(block);
+  cfg.stream = s;
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+  attr[0].val.programmaticStreamSerializationAllowed = 1;
+  cfg.attrs = attr;
+  cfg.numAttrs = 1;
+  cudaLaunchKernelEx(&cfg, kernel, std::forward<Act>(args)...);
+}
 template <int NSP>
 void q_sweeps(rc_ctx* c, int gather) {
   if (gather) {
@@ -993,17 +1015,17 @@ void q_sweeps(rc_ctx* c, int gather) {
   if (c->persistent) { q_persistent<NSP>(c); return; }
   for (size_t l = 0; l + 1 < c->fwd_off.size(); ++l) {
     const int n = c->fwd_off[l + 1] - c->fwd_off[l];
-    k_sweep4<NSP, true><<<blocks(n, c->d.cpw), 32, 0, c->stream>>>(c->d, TH<NSP>(c), c->fwd_off[l],
-                                                                    c->fwd_off[l + 1]);
+    launch_pdl(k_sweep4<NSP, true>, blocks(n, c->d.cpw), 32, c->stream, c->d, TH<NSP>(c), c->fwd_off[l],
+               c->fwd_off[l + 1]);
     c->launches++;
   }
   for (size_t l = 0; l + 1 < c->bwd_off.size(); ++l) {
     const int n = c->bwd_off[l + 1] - c->bwd_off[l];
-    k_sweep4<NSP, false><<<blocks(n, c->d.cpw), 32, 0, c->stream>>>(c->d, TH<NSP>(c), c->bwd_off[l],
-                                                                     c->bwd_off[l + 1]);
+    launch_pdl(k_sweep4<NSP, false>, blocks(n, c->d.cpw), 32, c->stream, c->d, TH<NSP>(c), c->bwd_off[l],
+               c->bwd_off[l + 1]);
     c->launches++;
   }
-  k_update<NSP><<<blocks(c->NE, c->d.bs), c->d.bs, 0, c->stream>>>(c->d, TH<NSP>(c));
+  launch_pdl(k_update<NSP>, blocks(c->NE, c->d.bs), c->d.bs, c->stream, c->d, TH<NSP>(c));
   c->launches++;
 }
 // Integrated chemical source on the side stream, forked after the cell pass
@@ -1057,7 +1079,7 @@ void q_sweeps32(rc_ctx* c) {
     mixed_sweep<NSP>(c->d, c->thermo32.data(), false, c->bwd_off[l], c->bwd_off[l + 1], c->stream);
     c->launches++;
   }
-  k_update<NSP><<<blocks(c->NE, c->d.bs), c->d.bs, 0, c->stream>>>(c->d, TH<NSP>(c));
+  launch_pdl(k_update<NSP>, blocks(c->NE, c->d.bs), c->d.bs, c->stream, c->d, TH<NSP>(c));
   c->launches++;
 }
 // The subroutines of one iteration in the current precision mode.

@@ -106,6 +106,16 @@ __device__ __forceinline__ void removedirection(double& vx, double& vy, double n
   vy = vy - vn * ny;
 }
 
+// Programmatic dependent launch (kernels launched with
+// cudaLaunchAttributeProgrammaticStreamSerialization): let the next kernel of
+// the stream start its prologue now / wait until the previous kernel of the
+// stream has completed and its writes are visible.  Without the attribute
+// both are no-ops.
+__device__ __forceinline__ void pdl_launch_dependents() {
+  asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
+}
+__device__ __forceinline__ void pdl_wait() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
+
 __device__ __forceinline__ unsigned ld_acquire(const unsigned* p) {
   unsigned v;
   asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");

@@ -639,11 +639,16 @@ __global__ void __launch_bounds__(128) k_pack32(const Dev d) {
   for (int k = 0; k < 3 + NSP; ++k) d.cst32[k * NE + i] = (float)d.cst[k * NE + i];
 }
 
+// one level, launched as a programmatic dependent of the previous one (see k_sweep4)
 template <int NSP, bool FWD>
 __global__ void __launch_bounds__(32) k_sweep32(const Dev d, const ThermoDev32<NSP> th, int t0, int t1) {
+  pdl_launch_dependents();
   const int lt = threadIdx.x >> 2;
   __shared__ float wsm[32 * (3 + NSP)];
-  sweep_step32<NSP, FWD>(d, th, lt < d.cpw ? t0 + blockIdx.x * d.cpw + lt : t1, t1, threadIdx.x & 3, wsm);
+  const SweepPre32<NSP> p =
+      sweep_load32<NSP, FWD>(d, lt < d.cpw ? t0 + blockIdx.x * d.cpw + lt : t1, t1, threadIdx.x & 3);
+  pdl_wait();
+  sweep_compute32<NSP, FWD>(d, th, p, threadIdx.x & 3, wsm);
 }
 
 // Both FP32 sweeps in one cooperative launch (chunks of d.cpw cells), ordered by per-level completion
@@ -725,8 +730,17 @@ void mixed_gather(const Dev& d, int visc, int comb, cudaStream_t s) {
 template <int NSP>
 void mixed_sweep(const Dev& d, const void* th32, bool fwd, int t0, int t1, cudaStream_t s) {
   const auto& th = *static_cast<const ThermoDev32<NSP>*>(th32);
-  if (fwd) k_sweep32<NSP, true><<<nblk(t1 - t0, d.cpw), 32, 0, s>>>(d, th, t0, t1);
-  else k_sweep32<NSP, false><<<nblk(t1 - t0, d.cpw), 32, 0, s>>>(d, th, t0, t1);
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = dim3(nblk(t1 - t0, d.cpw));
+  cfg.blockDim = dim3(32);
+  cfg.stream = s;
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+  attr[0].val.programmaticStreamSerializationAllowed = 1;
+  cfg.attrs = attr;
+  cfg.numAttrs = 1;
+  if (fwd) cudaLaunchKernelEx(&cfg, k_sweep32<NSP, true>, d, th, t0, t1);
+  else cudaLaunchKernelEx(&cfg, k_sweep32<NSP, false>, d, th, t0, t1);
 }
 // Cooperative launch of the persistent FP32 sweeps (level counters zeroed by the caller).
 template <int NSP>
