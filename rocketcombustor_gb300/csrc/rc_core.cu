@@ -646,6 +646,74 @@ __device__ __forceinline__ void sweep_compute(const Dev& d, const ThermoDev<NSP>
   d.hWA[q * NE + p.i] = FWD ? (R0 - df0) / ddi : R0 - df0 / ddi;
   if (q + 4 < V) d.hWA[(q + 4) * NE + p.i] = FWD ? (R1 - df1) / ddi : R1 - df1 / ddi;
 }
+// The same cell step with 8 lanes per cell: lanes r = 0..3 (slot r) form the
+// terms that need dp (c1, c2, c3), lanes r = 4..7 (slot r-4) the others (c0,
+// c4..); both compute the velocity increments they share.  Then lane r adds
+// variable r over the 4 slots in slot order and divides.  The same
+// expressions in the same order as sweep_compute, so the same bits, with
+// about a third fewer FP64 instructions per lane.  wsm: 4 cells x V x 4 slots.
+template <int NSP, bool FWD>
+__device__ __forceinline__ void sweep_compute8(const Dev& d, const ThermoDev<NSP>& th, const SweepPre<NSP>& p,
+                                               int r, int cell, double* wsm) {
+  constexpr int V = 3 + NSP;
+  const int NE = d.NE, q = r & 3;
+  const bool dpart = r < 4;
+  double R = 0.0;
+  if (p.valid && r < V) R = d.hWA[r * NE + p.i];
+  double c[V];
+#pragma unroll
+  for (int k = 0; k < V; ++k) c[k] = 0.0;
+  if (p.act) {
+    const int j = p.j;
+    const double dx = p.dx, dy = p.dy, uu = p.uu, vv = p.vv, rr = p.rr;
+    const double drr = d.hWA[0 * NE + j], dru = d.hWA[1 * NE + j], drv = d.hWA[2 * NE + j];
+    double dry[NSP], s = 0.0;
+#pragma unroll
+    for (int k = 0; k < NSP - 1; ++k) { dry[k] = d.hWA[(4 + k) * NE + j]; s = s + dry[k]; }
+    dry[NSP - 1] = drr - s;
+    const double duu = (dru - uu * drr) / rr;
+    const double dvv = (drv - vv * drr) / rr;
+    const double unormal = p.unormal;
+    const double dunormal = duu * dx + dvv * dy;
+    const double aF = p.aF;
+    if (dpart) {
+      const double dre = d.hWA[3 * NE + j], tt = p.tt, gama = p.gama, rou = p.rou, rov = p.rov;
+      double s1 = 0.0, s2 = 0.0;
+#pragma unroll
+      for (int k = 0; k < NSP; ++k) s1 = s1 + p.cs[k] * dry[k];
+#pragma unroll
+      for (int k = 0; k < NSP; ++k) s2 = s2 + th.R[k] * dry[k];
+      const double gm1 = p.gm1;
+      const double dpp =
+          gm1 * (dre - s1 + tt * s2 * gama / gm1 - 0.5 * (dru * uu + duu * rou + drv * vv + dvv * rov));
+      c[1] = 0.5 * (-aF * dru + dru * unormal + rou * dunormal + dpp * dx);
+      c[2] = 0.5 * (-aF * drv + drv * unormal + rov * dunormal + dpp * dy);
+      c[3] = 0.5 * (-aF * dre + dunormal * p.roepp + unormal * (dre + dpp));
+    } else {
+      c[0] = 0.5 * (-aF * drr + dru * dx + drv * dy);
+#pragma unroll
+      for (int k = 0; k < NSP - 1; ++k) c[4 + k] = 0.5 * (-aF * dry[k] + dry[k] * unormal + p.ry[k] * dunormal);
+    }
+  }
+  double* w = wsm + cell * V * 4;  // [k][slot]
+  __syncwarp();
+  if (dpart) {
+#pragma unroll
+    for (int k = 1; k < 4; ++k) w[k * 4 + q] = c[k];
+  } else {
+    w[q] = c[0];
+#pragma unroll
+    for (int k = 4; k < V; ++k) w[k * 4 + q] = c[k];
+  }
+  __syncwarp();
+  if (!p.valid || r >= V) return;
+  double df = 0.0;
+#pragma unroll
+  for (int sl = 0; sl < 4; ++sl) df = df + w[r * 4 + sl];
+  const double ddi = p.ddi;
+  d.hWA[r * NE + p.i] = FWD ? (R - df) / ddi : R - df / ddi;
+}
+
 template <int NSP, bool FWD>
 __device__ __forceinline__ void sweep_step(const Dev& d, const ThermoDev<NSP>& th, int t, int tend, int q,
                                            double* wsm) {
@@ -657,6 +725,16 @@ __device__ __forceinline__ void sweep_step(const Dev& d, const ThermoDev<NSP>& t
 // Launched as a programmatic dependent of the previous level: it lets the
 // next level start, loads what the sweep does not change, and only then
 // waits for the previous level.
+// one level with 8 lanes per cell: block b (one warp) takes cells t0 + 4b .. + 3
+template <int NSP, bool FWD>
+__global__ void __launch_bounds__(32) k_sweep8(const Dev d, const ThermoDev<NSP> th, int t0, int t1) {
+  pdl_launch_dependents();
+  const int cell = threadIdx.x >> 3, r = threadIdx.x & 7;
+  __shared__ double wsm[4 * (3 + NSP) * 4];
+  const SweepPre<NSP> p = sweep_load<NSP, FWD>(d, t0 + blockIdx.x * 4 + cell, t1, r & 3);
+  pdl_wait();
+  sweep_compute8<NSP, FWD>(d, th, p, r, cell, wsm);
+}
 template <int NSP, bool FWD>
 __global__ void __launch_bounds__(32) k_sweep4(const Dev d, const ThermoDev<NSP> th, int t0, int t1) {
   pdl_launch_dependents();
@@ -841,6 +919,7 @@ struct rc_ctx {
   std::vector<int> fwd_off, bwd_off;
   bool persistent = true;       // LU-SGS sweeps as one cooperative launch (else one launch per level)
   bool can_persistent = false;  // the device can co-schedule the persistent LU-SGS grid
+  bool wide = false;            // FP64 per-level sweeps with 8 lanes per cell (k_sweep8)
   int pers_grid = 0;             // blocks of the persistent launch (one per SM)
   unsigned* lvl_count = nullptr; // per-level completion counters of the persistent launch
   int nlevels = 0;
@@ -1015,14 +1094,18 @@ void q_sweeps(rc_ctx* c, int gather) {
   if (c->persistent) { q_persistent<NSP>(c); return; }
   for (size_t l = 0; l + 1 < c->fwd_off.size(); ++l) {
     const int n = c->fwd_off[l + 1] - c->fwd_off[l];
-    launch_pdl(k_sweep4<NSP, true>, blocks(n, c->d.cpw), 32, c->stream, c->d, TH<NSP>(c), c->fwd_off[l],
-               c->fwd_off[l + 1]);
+    if (c->wide) launch_pdl(k_sweep8<NSP, true>, blocks(n, 4), 32, c->stream, c->d, TH<NSP>(c), c->fwd_off[l],
+                            c->fwd_off[l + 1]);
+    else launch_pdl(k_sweep4<NSP, true>, blocks(n, c->d.cpw), 32, c->stream, c->d, TH<NSP>(c), c->fwd_off[l],
+                    c->fwd_off[l + 1]);
     c->launches++;
   }
   for (size_t l = 0; l + 1 < c->bwd_off.size(); ++l) {
     const int n = c->bwd_off[l + 1] - c->bwd_off[l];
-    launch_pdl(k_sweep4<NSP, false>, blocks(n, c->d.cpw), 32, c->stream, c->d, TH<NSP>(c), c->bwd_off[l],
-               c->bwd_off[l + 1]);
+    if (c->wide) launch_pdl(k_sweep8<NSP, false>, blocks(n, 4), 32, c->stream, c->d, TH<NSP>(c), c->bwd_off[l],
+                            c->bwd_off[l + 1]);
+    else launch_pdl(k_sweep4<NSP, false>, blocks(n, c->d.cpw), 32, c->stream, c->d, TH<NSP>(c), c->bwd_off[l],
+                    c->bwd_off[l + 1]);
     c->launches++;
   }
   launch_pdl(k_update<NSP>, blocks(c->NE, c->d.bs), c->d.bs, c->stream, c->d, TH<NSP>(c));
@@ -1610,7 +1693,9 @@ int init_impl(const rc_mesh* m, const rc_thermo* t, const rc_config* g, const Ba
     const char* sched = std::getenv("RC_LUSGS_SCHEDULE");
     c->pers_grid = nsm;
     c->can_persistent = coop && nsm > 0 && occ64 >= 1 && occ32 >= 1;
-    c->persistent = c->can_persistent && !(sched && std::string(sched) == "levels");
+    const bool lv = sched && (std::string(sched) == "levels" || std::string(sched) == "levels8");
+    c->persistent = c->can_persistent && !lv;
+    c->wide = sched && std::string(sched) == "levels8";
   }
   *out = c;
   return RC_OK;
@@ -1782,22 +1867,24 @@ int rc_autotune(rc_ctx* c, int iters, char* report, int report_len) {
   };
   cudaMemcpyAsync(save, c->d.PA, n * sizeof(double), cudaMemcpyDeviceToDevice, c->stream);
   cudaMemcpyAsync(save + n, c->d.WA, n * sizeof(double), cudaMemcpyDeviceToDevice, c->stream);
-  struct Cand { bool pers; int bs; int cpw; };
+  struct Cand { bool pers; int bs; int cpw; bool wide; };
   std::vector<Cand> cands;
   for (int pers = c->can_persistent ? 1 : 0; pers >= 0; --pers)
-    for (int cpw : {8, 4, 2, 1})
-      for (int bs : {128, 64}) cands.push_back({pers != 0, bs, cpw});
+    for (int cpw : {8, 4, 2})
+      for (int bs : {128, 64}) cands.push_back({pers != 0, bs, cpw, false});
+  for (int bs : {128, 64}) cands.push_back({false, bs, 8, true});
   cudaEvent_t e0, e1;
   cudaEventCreate(&e0);
   cudaEventCreate(&e1);
   std::string rep;
   double best = 1e300;
-  Cand bc = {c->persistent, c->d.bs, c->d.cpw};
+  Cand bc = {c->persistent, c->d.bs, c->d.cpw, c->wide};
   int st = RC_OK;
   for (const Cand& k : cands) {
     c->persistent = k.pers;
     c->d.bs = k.bs;
     c->d.cpw = k.cpw;
+    c->wide = k.wide;
     drop_graphs(c);
     restore();
     for (int w = 0; w < 2 && !st; ++w) st = rc_lusgs_stage(c, 1);
@@ -1809,21 +1896,22 @@ int rc_autotune(rc_ctx* c, int iters, char* report, int report_len) {
     float ms = 0.f;
     cudaEventElapsedTime(&ms, e0, e1);
     const double per = ms / iters;
-    rep += std::string(k.pers ? "persistent" : "levels") + " bs=" + std::to_string(k.bs) + " cpw=" +
-           std::to_string(k.cpw) + ": " + std::to_string(per) + " ms; ";
+    rep += std::string(k.pers ? "persistent" : k.wide ? "levels8" : "levels") + " bs=" + std::to_string(k.bs) +
+           " cpw=" + std::to_string(k.wide ? 4 : k.cpw) + ": " + std::to_string(per) + " ms; ";
     if (per < best) { best = per; bc = k; }
   }
   c->persistent = bc.pers;
   c->d.bs = bc.bs;
   c->d.cpw = bc.cpw;
+  c->wide = bc.wide;
   drop_graphs(c);
   restore();
   cudaStreamSynchronize(c->stream);
   cudaEventDestroy(e0);
   cudaEventDestroy(e1);
   cudaFree(save);
-  rep += std::string("chosen: ") + (bc.pers ? "persistent" : "levels") + " bs=" + std::to_string(bc.bs) +
-         " cpw=" + std::to_string(bc.cpw);
+  rep += std::string("chosen: ") + (bc.pers ? "persistent" : bc.wide ? "levels8" : "levels") + " bs=" +
+         std::to_string(bc.bs) + " cpw=" + std::to_string(bc.wide ? 4 : bc.cpw);
   if (report && report_len > 0) {
     std::snprintf(report, (size_t)report_len, "%s", rep.c_str());
   }
