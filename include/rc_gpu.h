@@ -162,6 +162,13 @@ int rc_lusgs_stage(rc_ctx* ctx, int istep); /* lu_sgs_stage   Time_LUSGS_steady.
  * No counterpart in the reference (it has a single FP64 path). */
 int rc_set_precision(rc_ctx* ctx, int precision);
 
+/* Polls after which a level wait of the persistent LU-SGS kernels gives up
+ * (default 2^24): the kernel then latches RC_ERR_SYNC and returns, leaving the
+ * context usable.  A small limit forces the timeout path (fault tests). */
+int rc_set_wait_limit(rc_ctx* ctx, unsigned polls);
+/* Clear the latched stop conditions (after the caller has dealt with them). */
+int rc_clear_error(rc_ctx* ctx);
+
 /* Autotuner: times `iters` iterations of every launch configuration (LU-SGS
  * as one cooperative kernel or one kernel per level; 32, 64 or 128 threads
  * per block for the cell and face kernels) on the current state, keeps the

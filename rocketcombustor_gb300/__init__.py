@@ -106,6 +106,8 @@ SIGNATURES = {
     "rc_batch_info": (_i, [_vp, _IP, _IP]),
     "rc_residual_batch": (_i, [_vp, _DP, _DP]),
     "rc_autotune": (_i, [_vp, _i, _cp, _i]),
+    "rc_set_wait_limit": (_i, [_vp, ctypes.c_uint]),
+    "rc_clear_error": (_i, [_vp]),
     "rc_set_surrogate": (_i, [_vp, _vp, _d]),
     "rc_surrogate_stats": (_i, [_vp, ctypes.POINTER(ctypes.c_uint), ctypes.POINTER(ctypes.c_uint)]),
     "rc_surrogate_samples": (_i, [_vp, _vp, _vp, _vp, _i, _vp, _vp]),
@@ -313,6 +315,13 @@ class Solver:
         """RC_CHEM_EXPLICIT (the reference's vol*omega) or RC_CHEM_INTEGRATED
         (mean rate of the per-cell integrator over the pseudo time step)."""
         self._check(load().rc_set_chemistry(self._h, int(mode), float(tol), int(max_substeps)))
+
+    def set_wait_limit(self, polls: int):
+        """Polls before a level wait of the persistent LU-SGS gives up (RC_ERR_SYNC)."""
+        self._check(load().rc_set_wait_limit(self._h, int(polls)))
+
+    def clear_error(self):
+        self._check(load().rc_clear_error(self._h))
 
     def autotune(self, iters: int = 5) -> str:
         """Pick the fastest launch configuration on the current state (the

@@ -794,14 +794,14 @@ __global__ void __launch_bounds__(PERS_THREADS) k_lusgs_persistent(const Dev d, 
       if (fwd) {
         const SweepPre<NSP> p = sweep_load<NSP, true>(d, t, t1, q);
         if (!waited) {
-          if (!wait_count(cnt + L - 1, nchunks(L - 1), d.err)) return;
+          if (!wait_count(cnt + L - 1, nchunks(L - 1), d.err, d.spin_limit)) return;
           waited = true;
         }
         sweep_compute<NSP, true>(d, th, p, q, wsm);
       } else {
         const SweepPre<NSP> p = sweep_load<NSP, false>(d, t, t1, q);
         if (!waited) {
-          if (!wait_count(cnt + L - 1, nchunks(L - 1), d.err)) return;
+          if (!wait_count(cnt + L - 1, nchunks(L - 1), d.err, d.spin_limit)) return;
           waited = true;
         }
         sweep_compute<NSP, false>(d, th, p, q, wsm);
@@ -810,7 +810,7 @@ __global__ void __launch_bounds__(PERS_THREADS) k_lusgs_persistent(const Dev d, 
     }
   }
   // the update needs the whole backward sweep
-  if (!wait_count(cnt + nl - 1, nchunks(nl - 1), d.err)) return;
+  if (!wait_count(cnt + nl - 1, nchunks(nl - 1), d.err, d.spin_limit)) return;
   unsigned err = 0;
   for (int i = blockIdx.x * PERS_THREADS + threadIdx.x; i < d.NE; i += G * PERS_THREADS) update_cell<NSP>(d, th, i, err);
   flag(d, err);
@@ -1563,6 +1563,7 @@ int init_impl(const rc_mesh* m, const rc_thermo* t, const rc_config* g, const Ba
   d.NE = NE; d.NF = NF; d.NG = NG;
   d.bs = 128;
   d.cpw = 8;
+  d.spin_limit = 1u << 24;
   if (const char* e = std::getenv("RC_LUSGS_CPW")) {
     const int v = std::atoi(e);
     if (v == 1 || v == 2 || v == 4 || v == 8) d.cpw = v;
@@ -1952,6 +1953,21 @@ int rc_surrogate_samples(rc_ctx* c, const double* d_P0, const double* d_P1, cons
   if (n == 0) return RC_OK;
   RC_CU(surrogate_samples(c->thermo.data(), d_P0, d_P1, d_dt, n, d_x, d_t, c->stream));
   c->launches++;
+  return RC_OK;
+}
+int rc_set_wait_limit(rc_ctx* c, unsigned polls) {
+  if (!c || polls < 1) return RC_ERR_ARG;
+  c->d.spin_limit = polls;
+  drop_graphs(c);
+  return RC_OK;
+}
+int rc_clear_error(rc_ctx* c) {
+  if (!c) return RC_ERR_ARG;
+  RC_CU(cudaStreamSynchronize(c->stream));
+  RC_CU(cudaMemsetAsync(c->d.err, 0, sizeof(unsigned), c->stream));
+  RC_CU(cudaStreamSynchronize(c->stream));
+  c->latched = 0;
+  c->err.clear();
   return RC_OK;
 }
 int rc_set_chemistry(rc_ctx* c, int mode, double tol, int max_substeps) {

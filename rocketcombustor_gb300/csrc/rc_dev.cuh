@@ -12,6 +12,7 @@ struct Dev {
   int NE, NF, NG;
   int bs;                        // threads per block of the cell and face kernels (32, 64 or 128)
   int cpw;                       // LU-SGS cells per warp (1, 2, 4 or 8; 4 lanes per cell)
+  unsigned spin_limit;           // polls before a level wait of the persistent LU-SGS gives up
   // cells
   const double* vol;
   const double* rinv;            // [2*NE] 1./reflen
@@ -152,13 +153,13 @@ __device__ __forceinline__ void update_cell(const Dev& d, const ThermoDev<NSP>& 
 // Level ordering of the persistent LU-SGS kernels.  wait_count: lane 0 of a
 // warp waits until the completion count of the previous level reaches its
 // number of chunks; the warp then reads what that level wrote.  The wait is
-// bounded: after about 2^24 polls, or as soon as another waiter has given up,
+// bounded: after about `limit` polls, or as soon as another waiter has given up,
 // ERR_SYNC is latched and false returned, and the kernel returns.
-__device__ __forceinline__ bool wait_count(const unsigned* c, unsigned target, unsigned* err) {
+__device__ __forceinline__ bool wait_count(const unsigned* c, unsigned target, unsigned* err, unsigned limit) {
   int ok = 1;
   if ((threadIdx.x & 31) == 0) {
     for (unsigned spin = 0; ld_acquire(c) < target; ++spin) {
-      if ((spin & 255u) == 255u && (spin > (1u << 24) || (ld_acquire(err) & ERR_SYNC))) {
+      if (spin >= limit || ((spin & 255u) == 255u && (ld_acquire(err) & ERR_SYNC))) {
         atomicOr(err, ERR_SYNC);
         ok = 0;
         break;

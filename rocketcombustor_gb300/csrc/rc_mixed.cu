@@ -681,14 +681,14 @@ __global__ void __launch_bounds__(PERS32_THREADS) k_lusgs_persistent32(const Dev
       if (fwd) {
         const SweepPre32<NSP> p = sweep_load32<NSP, true>(d, t, t1, q);
         if (!waited) {
-          if (!wait_count(cnt + L - 1, nchunks(L - 1), d.err)) return;
+          if (!wait_count(cnt + L - 1, nchunks(L - 1), d.err, d.spin_limit)) return;
           waited = true;
         }
         sweep_compute32<NSP, true>(d, th, p, q, wsm);
       } else {
         const SweepPre32<NSP> p = sweep_load32<NSP, false>(d, t, t1, q);
         if (!waited) {
-          if (!wait_count(cnt + L - 1, nchunks(L - 1), d.err)) return;
+          if (!wait_count(cnt + L - 1, nchunks(L - 1), d.err, d.spin_limit)) return;
           waited = true;
         }
         sweep_compute32<NSP, false>(d, th, p, q, wsm);

@@ -182,3 +182,39 @@ def test_persistent_and_per_level_schedules_agree(case_root, precision, monkeypa
     for st in states[1:]:
         assert np.array_equal(states[0][0], st[0])
         assert np.array_equal(states[0][1], st[1])
+
+
+def test_forced_level_wait_timeout_is_reported(case_root, monkeypatch):
+    """A tiny poll limit makes the persistent LU-SGS give up waiting for the
+    previous level: RC_ERR_SYNC is reported, the kernel returns, and the
+    context stays usable after the error is cleared."""
+    monkeypatch.setenv("RC_LUSGS_SCHEDULE", "persistent")
+    d = make_case(case_root, "c1", nx=60, ny=12)
+    c = rc.Case(d)
+    s = rc.Solver(c)
+    s.set_wait_limit(1)
+    s.lu_sgs_stage(1)
+    with pytest.raises(rc.RcError) as e:
+        s.sync()
+    assert e.value.code & 64
+    s.clear_error()
+    s.set_wait_limit(1 << 24)
+    s.set_state(c.array("PA"), c.array("WA"))
+    s.run(5)
+    o = oracle.Oracle(d, threads=4)
+    o.run(5)
+    assert np.array_equal(s.get_state()[0], o.array("PA"))
+
+
+def test_out_of_range_temperature_is_reported(case_t1):
+    """T beyond the thermo fit in one cell stops at the next synchronising call
+    (ComputeGasParameter, thermo_property.f90:174-177)."""
+    c = rc.Case(case_t1)
+    s = rc.Solver(c)
+    PA = c.array("PA").copy()
+    PA[3, 3] = 1.0e6
+    s.set_state(PA, c.array("WA"))
+    s.timestep()
+    with pytest.raises(rc.RcError) as e:
+        s.sync()
+    assert e.value.code & 1
