@@ -92,9 +92,11 @@ class Mesh:
 
     @property
     def nf(self) -> int:
-        # Euler: interior edges + boundary edges for a triangulated quad grid
-        nx, ny = self.nx, self.ny
-        return nx * (ny + 1) + ny * (nx + 1) + nx * ny
+        """Number of distinct cell edges."""
+        c = self.cells
+        e = np.concatenate([c[:, [0, 1]], c[:, [1, 2]], c[:, [2, 0]]])
+        e.sort(axis=1)
+        return int(np.unique(e, axis=0).shape[0])
 
 
 def _color_order(cells: np.ndarray, nnt: int) -> np.ndarray:
