@@ -389,6 +389,7 @@ def batched_form(args, stream, flush, torch, rc, tmp):
         out[form] = {"value": ne * args.steps / r["t_local"], "ms_per_step": 1e3 * r["t_local"] / args.steps,
                      "gpu_launches": r["launches"], "autotune": tune,
                      "chem_substeps": {"min": int(ns.min()), "mean": float(ns.mean()), "max": int(ns.max())}}
+        out[form].update(subroutine_times(b, args, stream, flush, torch))
         b.close()
     den = np.maximum(np.abs(states["fp64"]).max(axis=0), 1e-300)
     e = np.abs(states["mixed"] - states["fp64"]).max(axis=0) / den

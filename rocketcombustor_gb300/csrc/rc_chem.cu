@@ -44,19 +44,47 @@ __device__ __forceinline__ void integrate_cell(const Dev& d, const ThermoDev<NSP
   for (int k = 0; k < NSP - 1; ++k) d.src[k * NE + i] = vol * (rho * ((P[4 + k] - P0[4 + k]) / dt));
 }
 
+// Cells are taken in `order` (longest previous integration first, so the long
+// cells start early and warps hold cells of similar cost), or in cell order
+// when order is null.
 template <int NSP>
 __global__ void __launch_bounds__(CHEM_THREADS) k_chem_source(const Dev d, const ThermoDev<NSP> th, double tol,
                                                               int maxsub, int* __restrict__ nsub,
-                                                              unsigned* counter) {
+                                                              const int* __restrict__ order, unsigned* counter) {
   const int NE = d.NE;
   unsigned err = 0;
   for (;;) {
     const int base = next_chunk(counter);
     if (base >= NE) break;
-    const int i = base + (threadIdx.x & 31);
-    if (i < NE) integrate_cell<NSP>(d, th, i, tol, maxsub, nsub, err);
+    const int q = base + (threadIdx.x & 31);
+    if (q < NE) integrate_cell<NSP>(d, th, order ? order[q] : q, tol, maxsub, nsub, err);
   }
   flag(d, err);
+}
+
+// Counting sort of the cells by their previous substep count, descending
+// (bucket 255 - min(nsub, 255)); the order inside a bucket does not matter.
+constexpr int NBUCKET = 256;
+__global__ void k_chem_hist(const int* __restrict__ nsub, int n, unsigned* hist) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) atomicAdd(&hist[NBUCKET - 1 - min(max(nsub[i], 0), NBUCKET - 1)], 1u);
+}
+__global__ void k_chem_scan(unsigned* hist) {  // one block of NBUCKET threads: exclusive scan in place
+  __shared__ unsigned sh[NBUCKET];
+  const int t = threadIdx.x;
+  sh[t] = hist[t];
+  __syncthreads();
+  for (int o = 1; o < NBUCKET; o <<= 1) {
+    const unsigned v = t >= o ? sh[t - o] : 0u;
+    __syncthreads();
+    sh[t] += v;
+    __syncthreads();
+  }
+  hist[t] = t ? sh[t - 1] : 0u;
+}
+__global__ void k_chem_scatter(const int* __restrict__ nsub, int n, unsigned* cursor, int* __restrict__ order) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) order[atomicAdd(&cursor[NBUCKET - 1 - min(max(nsub[i], 0), NBUCKET - 1)], 1u)] = i;
 }
 
 // The same for the cells list[0 .. *nlist) (the surrogate's fallbacks).
@@ -113,13 +141,21 @@ static int chem_grid(K kernel, int items) {
   return g < need ? g : (need > 0 ? need : 1);
 }
 
+// order/hist: work arrays of NE ints and NBUCKET unsigned (order null: cell order)
 template <int NSP>
-void chem_source(const Dev& d, const void* th, double tol, int maxsub, int* nsub, unsigned* counter,
-                 cudaStream_t s) {
+void chem_source(const Dev& d, const void* th, double tol, int maxsub, int* nsub, int* order, unsigned* hist,
+                 unsigned* counter, cudaStream_t s) {
+  if (order) {
+    const int nb = (d.NE + 255) / 256;
+    cudaMemsetAsync(hist, 0, sizeof(unsigned) * NBUCKET, s);
+    k_chem_hist<<<nb, 256, 0, s>>>(nsub, d.NE, hist);
+    k_chem_scan<<<1, NBUCKET, 0, s>>>(hist);
+    k_chem_scatter<<<nb, 256, 0, s>>>(nsub, d.NE, hist, order);
+  }
   const int grid = chem_grid(k_chem_source<NSP>, d.NE);
   cudaMemsetAsync(counter, 0, sizeof(unsigned), s);
   k_chem_source<NSP><<<grid, CHEM_THREADS, 0, s>>>(d, *static_cast<const ThermoDev<NSP>*>(th), tol, maxsub, nsub,
-                                                   counter);
+                                                   order, counter);
 }
 
 template <int NSP>
@@ -141,7 +177,8 @@ void chem_batch(const void* th, const double* P, const double* dt, int n, double
 }
 
 #define RC_CHEM_INST(N)                                                                                  \
-  template void chem_source<N>(const Dev&, const void*, double, int, int*, unsigned*, cudaStream_t);     \
+  template void chem_source<N>(const Dev&, const void*, double, int, int*, int*, unsigned*, unsigned*,   \
+                               cudaStream_t);                                                            \
   template void chem_list<N>(const Dev&, const void*, double, int, int*, const int*, const unsigned*,      \
                              unsigned*, cudaStream_t);                                                   \
   template void chem_batch<N>(const void*, const double*, const double*, int, double*, int*, double, int, \

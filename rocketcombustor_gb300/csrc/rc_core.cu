@@ -886,7 +886,7 @@ cudaError_t mixed_lusgs_persistent(const Dev&, const void*, const int*, int, con
                                    cudaStream_t);
 template <int NSP> int mixed_persistent_occupancy();
 template <int NSP>
-void chem_source(const Dev&, const void*, double, int, int*, unsigned*, cudaStream_t);
+void chem_source(const Dev&, const void*, double, int, int*, int*, unsigned*, unsigned*, cudaStream_t);
 template <int NSP>
 void chem_batch(const void*, const double*, const double*, int, double*, int*, double, int, unsigned*, unsigned*,
                 cudaStream_t);
@@ -936,6 +936,8 @@ struct rc_ctx {
   double chem_tol = 0.05;
   int chem_maxsub = 200;
   int* chem_nsub = nullptr;           // [NE] accepted substeps of the last integrated source
+  int* chem_order = nullptr;          // [NE] cells by previous substeps, descending
+  unsigned* chem_hist = nullptr;      // [256] bucket counts / cursors of that sort
   unsigned* chem_counter = nullptr;   // work-queue counter
   const rc_mlp* net = nullptr;        // surrogate (RC_CHEM_SURROGATE)
   float spread_tol = 0.02f;
@@ -1128,9 +1130,9 @@ void q_chem_fork(rc_ctx* c) {
                    c->chem_counter, c->stream2);
     c->launches += 2;
   } else {
-    chem_source<NSP>(c->d, c->thermo.data(), c->chem_tol, c->chem_maxsub, c->chem_nsub, c->chem_counter,
-                     c->stream2);
-    c->launches++;
+    chem_source<NSP>(c->d, c->thermo.data(), c->chem_tol, c->chem_maxsub, c->chem_nsub, c->chem_order,
+                     c->chem_hist, c->chem_counter, c->stream2);
+    c->launches += 4;
   }
   cudaEventRecord(c->ev_join, c->stream2);
 }
@@ -1984,6 +1986,8 @@ int rc_set_chemistry(rc_ctx* c, int mode, double tol, int max_substeps) {
   }
   if (mode != RC_CHEM_EXPLICIT && !c->chem_nsub) {
     if (int st = dev_zeros(c, (size_t)c->NE, &c->chem_nsub)) return st;
+    if (int st = dev_zeros(c, (size_t)c->NE, &c->chem_order)) return st;
+    if (int st = dev_zeros(c, (size_t)256, &c->chem_hist)) return st;
     if (int st = dev_zeros(c, (size_t)1, &c->chem_counter)) return st;
     RC_CU(cudaStreamCreateWithFlags(&c->stream2, cudaStreamNonBlocking));
     RC_CU(cudaEventCreateWithFlags(&c->ev_fork, cudaEventDisableTiming));
