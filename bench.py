@@ -204,7 +204,7 @@ def main():
     ap.add_argument("--no-surrogate", action="store_true",
                     help="skip the surrogate form (network trained here on integrator pairs)")
     ap.add_argument("--sur-samples", type=int, default=10_000_000)
-    ap.add_argument("--sur-steps", type=int, default=4000)
+    ap.add_argument("--sur-steps", type=int, default=8000)
     ap.add_argument("--converge", type=int, default=0,
                     help="instead of the throughput line: N iterations per form with the residual history, "
                          "iterations and wall time to each residual level")
@@ -253,8 +253,7 @@ def main():
             if clk is None:
                 clk = clk_f
             states[form] = s.get_state()
-            if form == forms_req[0]:
-                r.update(subroutine_times(s, args, stream, flush, torch))
+            r.update(subroutine_times(s, args, stream, flush, torch))
             r["e2e"] = e2e_through_abi(s, args, NE, V, torch)
             r["levels"] = {k: v for k, v in s.stats().items() if k != "kernel_launches"}
             if args.chem == "integrated":
@@ -308,7 +307,8 @@ def main():
             for form in forms_req:
                 r = results[form]
                 f = {"value": NE * args.steps / r["t_local"], "ms_per_step": 1e3 * r["t_local"] / args.steps,
-                     "e2e": r["e2e"]["value"], "gpu_launches": r["launches"], "autotune": r.get("autotune")}
+                     "e2e": r["e2e"]["value"], "gpu_launches": r["launches"], "autotune": r.get("autotune"),
+                     "subroutine_ms": r["subroutine_ms"]}
                 if form != "fp64":
                     st = states[form][0]
                     den = np.maximum(np.abs(ref).max(axis=0), 1e-300)
@@ -318,10 +318,17 @@ def main():
                                              "after_iterations": args.warmup + args.steps}
                 forms[form] = f
             line["forms"] = forms
+        bat = None
         if not args.no_batch and world == 1:
-            line.setdefault("forms", {})["batched"] = batched_form(args, stream, flush, torch, rc, tmp)
+            bat = batched_form(args, stream, flush, torch, rc, tmp)
+            line.setdefault("forms", {})["batched"] = bat[0]
         if not args.no_surrogate and world == 1 and cfg.combustion and cfg.nsp == 4:
-            line.setdefault("forms", {})["surrogate"] = surrogate_form(args, stream, flush, torch, rc, case)
+            extra = torch.tensor(bat[2].T.copy(), device="cuda") if bat else None
+            sur, net = surrogate_form(args, stream, flush, torch, rc, case, extra)
+            line.setdefault("forms", {})["surrogate"] = sur
+            if bat:
+                bat[0]["surrogate"] = batched_surrogate(args, stream, flush, torch, rc, bat[1], bat[2], net)
+            net.close()
         line["clocks"] = clk
         if not args.no_cpu:
             line["cpu_baseline"] = cpu_baseline(d, args.cpu_budget)
@@ -395,6 +402,28 @@ def batched_form(args, stream, flush, torch, rc, tmp):
     e = np.abs(states["mixed"] - states["fp64"]).max(axis=0) / den
     out["mixed"]["rel_linf_vs_fp64"] = {"p": float(e[0]), "T": float(e[3]), "Y": [float(x) for x in e[4:]],
                                         "after_iterations": args.warmup + args.steps}
+    return out, cs, states["fp64"]
+
+
+def batched_surrogate(args, stream, flush, torch, rc, cs, ref_state, net):
+    """The batched workload with the surrogate chemistry (FP64 otherwise),
+    against the batched FP64 run with the integrator after the same
+    iterations."""
+    b = rc.BatchSolver(cs, stream=stream.cuda_stream)
+    b.set_surrogate(net)
+    b.set_chemistry(rc.RC_CHEM_SURROGATE)
+    tune = b.autotune(3)
+    r, _ = time_form(b, args, stream, flush, None, torch, rc)
+    st = b.get_state()[0]
+    n_net, n_fb = b.surrogate_stats()
+    ne = b.NE
+    den = np.maximum(np.abs(ref_state).max(axis=0), 1e-300)
+    e = np.abs(st - ref_state).max(axis=0) / den
+    out = {"value": ne * args.steps / r["t_local"], "ms_per_step": 1e3 * r["t_local"] / args.steps,
+           "gpu_launches": r["launches"], "autotune": tune, "cells_network": n_net, "cells_integrator": n_fb,
+           "rel_linf_vs_integrated_fp64": {"p": float(e[0]), "T": float(e[3]), "Y": [float(x) for x in e[4:]],
+                                           "after_iterations": args.warmup + args.steps}}
+    b.close()
     return out
 
 
@@ -473,18 +502,21 @@ def converge(args, rc, torch):
     return 0
 
 
-def surrogate_form(args, stream, flush, torch, rc, case):
+def surrogate_form(args, stream, flush, torch, rc, case, extra_pool=None):
     """The learned-surrogate workload on the same nozzle: pairs from the FP64
-    integrator on states of this case's trajectory (integrated source), the
-    network trained on the GPU by the project's kernels, its inference
-    throughput, and the steady iteration with the surrogate source against
-    the one with the integrated source."""
+    integrator on states of this case's trajectory (integrated source) and,
+    when given, the batched cases' states, the network trained on the GPU by
+    the project's kernels, its inference throughput, and the steady iteration
+    with the surrogate source against the one with the integrated source.
+    Returns (results, network)."""
     from rocketcombustor_gb300 import surrogate
     out = {}
     ref = rc.Solver(case, stream=stream.cuda_stream)
     ref.set_chemistry(rc.RC_CHEM_INTEGRATED)
     t0 = time.perf_counter()
     pool = surrogate.collect_pool(ref, iters=20, every=5)
+    if extra_pool is not None:
+        pool = torch.cat([pool, extra_pool], 1).contiguous()
     x, t, nsub = surrogate.build_dataset(ref, pool, args.sur_samples, seed=7)
     torch.cuda.synchronize()
     out["data"] = {"samples": int(x.shape[0]), "seconds": time.perf_counter() - t0,
@@ -544,9 +576,8 @@ def surrogate_form(args, stream, flush, torch, rc, case):
                                                     "Y": [float(v) for v in e[4:]],
                                                     "after_iterations": args.warmup + args.steps}
     out["steady"] = forms
-    net.close()
     ref.close()
-    return out
+    return out, net
 
 
 def read_peaks_tensor():
