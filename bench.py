@@ -205,6 +205,9 @@ def main():
                     help="skip the surrogate form (network trained here on integrator pairs)")
     ap.add_argument("--sur-samples", type=int, default=10_000_000)
     ap.add_argument("--sur-steps", type=int, default=8000)
+    ap.add_argument("--no-bdf2", action="store_true",
+                    help="skip the unsteady form (dual-time BDF2, the reference's shipped time scheme)")
+    ap.add_argument("--bdf2-steps", type=int, default=10)
     ap.add_argument("--converge", type=int, default=0,
                     help="instead of the throughput line: N iterations per form with the residual history, "
                          "iterations and wall time to each residual level")
@@ -329,6 +332,8 @@ def main():
             if bat:
                 bat[0]["surrogate"] = batched_surrogate(args, stream, flush, torch, rc, bat[1], bat[2], net)
             net.close()
+        if not args.no_bdf2 and world == 1:
+            line.setdefault("forms", {})["bdf2"] = bdf2_form(args, stream, torch, rc, tmp)
         line["clocks"] = clk
         if not args.no_cpu:
             line["cpu_baseline"] = cpu_baseline(d, args.cpu_budget)
@@ -403,6 +408,68 @@ def batched_form(args, stream, flush, torch, rc, tmp):
     out["mixed"]["rel_linf_vs_fp64"] = {"p": float(e[0]), "T": float(e[3]), "Y": [float(x) for x in e[4:]],
                                         "after_iterations": args.warmup + args.steps}
     return out, cs, states["fp64"]
+
+
+def bdf2_form(args, stream, torch, rc, tmp):
+    """The reference's shipped time scheme (flow_solver_info.in: dual-time
+    BDF2, CFL 10, dt = 1e-8 s, up to 10 inner iterations to relTol 1e-3) on
+    the 120k-cell reacting viscous nozzle: physical steps through
+    Solver.bdf2_stage (one graph launch per inner iteration, a host read of
+    the inner residual after each), the BDF2_LU_SGS pieces timed alone, and
+    one step of the CPU oracle on all host threads beside it."""
+    import time as _time
+    d, cfg = make_workload("c2u", tmp)
+    case = rc.Case(d)
+    u = case.unsteady
+    s = rc.Solver(case, stream=stream.cuda_stream)
+    s.set_p_out(u["p_static"])
+    warm = 2
+    for i in range(1, warm + 1):
+        s.bdf2_stage(i, u["dt"], u["inner_loop"], u["rel_tol"])
+    s.sync()
+    l0 = s.stats()["kernel_launches"]
+    inner = []
+    t0 = _time.perf_counter()
+    for i in range(warm + 1, warm + args.bdf2_steps + 1):
+        inner.append(s.bdf2_stage(i, u["dt"], u["inner_loop"], u["rel_tol"]))
+    s.sync()
+    wall = _time.perf_counter() - t0
+    launches = s.stats()["kernel_launches"] - l0
+    # one inner iteration's BDF2_LU_SGS alone, device-timed (residual assembled first)
+    ev = [torch.cuda.Event(enable_timing=True) for _ in range(3)]
+    with torch.cuda.stream(stream):
+        s.timestep(); s.reconstruction(); s.flux_sourceterm()
+        s.sync()
+        ev[0].record(stream)
+        s.flux_sourceterm()
+        ev[1].record(stream)
+        s.bdf2_lusgs(2, 0.5, u["dt"])
+        ev[2].record(stream)
+        s.sync()
+    n_inner = sum(inner)
+    out = {"workload": f"c2u: {case.NE} triangles, reacting viscous, BDF2 dt {u['dt']:.3g} s, "
+                       f"InnerLoop {u['inner_loop']}, relTol {u['rel_tol']:g}",
+           "physical_steps": args.bdf2_steps, "inner_iterations": inner,
+           "ms_per_step": 1e3 * wall / args.bdf2_steps, "ms_per_inner_iteration": 1e3 * wall / n_inner,
+           "cell_inner_iters_per_s": case.NE * n_inner / wall, "gpu_launches": int(launches),
+           "timing": "wall clock around the steps (the stage reads the inner residual on the host "
+                     "after every inner iteration)",
+           "subroutine_ms": {"flux_sourceterm": ev[0].elapsed_time(ev[1]),
+                             "bdf2_lu_sgs": ev[1].elapsed_time(ev[2])},
+           "levels": {k: v for k, v in s.stats().items() if k != "kernel_launches"}}
+    s.close()
+    if not args.no_cpu:
+        import oracle
+        o = oracle.Oracle(d, threads=oracle.Oracle.max_threads())
+        t0 = _time.perf_counter()
+        n_cpu = o.unsteady_step(1)[0]
+        t_cpu = _time.perf_counter() - t0
+        out["cpu_oracle"] = {"ms_per_inner_iteration": 1e3 * t_cpu / n_cpu, "inner_iterations": n_cpu,
+                             "threads": oracle.Oracle.max_threads(),
+                             "cell_inner_iters_per_s": case.NE * n_cpu / t_cpu}
+        o.close()
+    case.close()
+    return out
 
 
 def batched_surrogate(args, stream, flush, torch, rc, cs, ref_state, net):

@@ -38,6 +38,7 @@ extern "C" {
 #define RC_ERR_NAN 16          /* NaN in WA(1,1) after a stage (Time_LUSGS_steady.f90:94-97) */
 #define RC_ERR_BCTYPE 32       /* unknown boundary code (flux_lax.f90:232-235, update_flow_variables.f90:364-367) */
 #define RC_ERR_SYNC 64         /* a grid barrier of the persistent LU-SGS kernel gave up waiting (bounded spin) */
+#define RC_ERR_LINSOLVE 128    /* a BDF2 cell system is singular to working precision (dgesvx info /= 0, la_math.f90:176-211) */
 #define RC_ERR_ARG 1024        /* invalid argument or unsupported configuration */
 #define RC_ERR_CUDA 2048       /* CUDA runtime failure */
 
@@ -211,6 +212,37 @@ int rc_surrogate_stats(rc_ctx* ctx, unsigned* n_surrogate, unsigned* n_fallback)
 int rc_surrogate_samples(rc_ctx* ctx, const double* d_P0, const double* d_P1, const double* d_dt, int n, float* d_x,
                          float* d_t);
 
+/*
+ * Unsteady dual-time BDF2 (implicit_time_method 5): the reference's shipped
+ * time scheme.  One context, one case, FP64, explicit chemical source.
+ *
+ * rc_set_p_out replaces the exit pressure of each case (ncase values) for the
+ * following calls: the host's compute_p_out (fvm2d.f90:229-239) result at the
+ * current time.
+ *
+ * rc_bdf2_stage = BDF2_stage (Time_BDF2.f90:4-71): shifts the time levels
+ * (istep 1: WP = WP2 = WA, phi = 0; later WP2 = WP, WP = WA, phi = 1/2), then
+ * up to inner_loop inner iterations of timestep, reconstruction,
+ * flux_sourceterm and BDF2_LU_SGS, each one CUDA graph launch, stopped when
+ * the species rows of the normalised residual of the primitive increments
+ * drop below rel_tol times their value at the first inner iteration
+ * (inner_iteration_residual, residual.f90:23-59), and ends with one more
+ * reconstruction and flux_sourceterm.  dt is the physical time step (the
+ * driver shortens the last one, fvm2d.f90:52-56).  *inner_done gets the inner
+ * iterations taken.  Synchronises once per inner iteration.
+ *
+ * rc_bdf2_lusgs = BDF2_LU_SGS (Time_BDF2.f90:73-337) alone, for per-subroutine
+ * checks: on inner_rk 1 the source term vol/dt ((1+2 phi) WP - phi WP2) is
+ * formed from the time levels "WP" and "WP2" (rc_set_array), then the
+ * primitive-variable LU-SGS sweeps with the per-cell 7x7 solves of
+ * advanced_linear_solve_lapack (la_math.f90:120-215) and the update of PA and
+ * WA.  A cell system singular to working precision latches RC_ERR_LINSOLVE
+ * (the reference stops).
+ */
+int rc_set_p_out(rc_ctx* ctx, const double* p_out);
+int rc_bdf2_stage(rc_ctx* ctx, int istep, double dt, int inner_loop, double rel_tol, int* inner_done);
+int rc_bdf2_lusgs(rc_ctx* ctx, int inner_rk, double phi, double dt);
+
 /* Residual + step_residual norms (residual.f90:4-21, 61-79): res(k) =
  * sum(vol*|hWA(k,:)|)/total_volume, romax = max(WA(1,:)).  Synchronises. */
 int rc_residual(rc_ctx* ctx, double* res, double* romax);
@@ -223,7 +255,8 @@ int rc_sync(rc_ctx* ctx);
 
 /* Intermediate arrays in the Fortran layout, for per-subroutine checks:
  * "PA","WA","hWA" (NVar,NE); "GradC" (2,NVar,NE); "alpaF" (NF); "step" (NE);
- * "GPA" (NVar,Nghostcell).  rc_set_array accepts the same names. */
+ * "GPA" (NVar,Nghostcell); "WP", "WP2" (NVar,NE), the BDF2 time levels.
+ * rc_set_array accepts the same names. */
 int rc_get_array(rc_ctx* ctx, const char* name, double* out);
 int rc_set_array(rc_ctx* ctx, const char* name, const double* in);
 

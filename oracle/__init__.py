@@ -72,6 +72,10 @@ def lib() -> ctypes.CDLL:
         L.orc_chem_integrate.argtypes = [vp, l, dp, dp, dp, ip, d, i]
         L.orc_set_chemistry.argtypes = [vp, i, d, i]
         L.orc_chem_nsub.restype = ip; L.orc_chem_nsub.argtypes = [vp]
+        L.orc_unsteady_scalars.argtypes = [vp, dp]
+        L.orc_bdf2_lusgs.restype = i; L.orc_bdf2_lusgs.argtypes = [vp, i, d]
+        L.orc_unsteady_step.restype = i; L.orc_unsteady_step.argtypes = [vp, l, ip, ip]
+        L.orc_dgesvx.restype = i; L.orc_dgesvx.argtypes = [i, dp, dp, dp, cp, dp]
         _lib = L
     return _lib
 
@@ -108,7 +112,22 @@ _SHAPES = {
     "Ghostcell": (np.int32, lambda d: (d[0], d[5])), "Num_ghostcell": (np.int32, lambda d: (d[0],)),
     "Hostcell": (np.int32, lambda d: (d[6],)), "Hostface": (np.int32, lambda d: (d[6],)),
     "BCtype_Ghostcell": (np.int32, lambda d: (d[6],)),
+    "WP": (np.float64, lambda d: (d[0], d[3])), "WP2": (np.float64, lambda d: (d[0], d[3])),
+    "fixed": (np.float64, lambda d: (d[0], d[3])),
 }
+
+
+def dgesvx(a, b):
+    """The oracle's restatement of LAPACK dgesvx('E', 'N') on one system:
+    returns (x, info, equed, rcond)."""
+    a = np.asfortranarray(a, dtype=np.float64)
+    b = np.ascontiguousarray(b, dtype=np.float64)
+    n = b.shape[0]
+    x = np.zeros(n)
+    eq = ctypes.create_string_buffer(1)
+    rc = np.zeros(1)
+    info = lib().orc_dgesvx(n, a.ctypes.data_as(ctypes.POINTER(ctypes.c_double)), _dp(b), _dp(x), eq, _dp(rc))
+    return x, info, eq.raw.decode(), float(rc[0])
 
 
 class Oracle:
@@ -248,6 +267,26 @@ class Oracle:
         if not p:
             return None
         return np.ctypeslib.as_array(p, shape=(self.NE,)).copy()
+
+    # unsteady dual-time BDF2
+    def unsteady(self) -> dict:
+        s = np.zeros(11)
+        lib().orc_unsteady_scalars(self._h, _dp(s))
+        return {"ttime": s[0], "dt": s[1], "p_out": s[2], "p_static": s[3], "rel_tol": s[4],
+                "inner_loop": int(s[5]), "steady": bool(s[6]), "A_p": s[7], "f_p": s[8],
+                "totaltime": s[9], "nstep_max": int(s[10])}
+
+    def bdf2_lusgs(self, inner_rk: int, phi: float) -> int:
+        return lib().orc_bdf2_lusgs(self._h, int(inner_rk), float(phi))
+
+    def unsteady_step(self, istep: int):
+        """One physical BDF2 step; returns (inner iterations, last step)."""
+        inner = ctypes.c_int()
+        stop = ctypes.c_int()
+        e = lib().orc_unsteady_step(self._h, int(istep), ctypes.byref(inner), ctypes.byref(stop))
+        if e:
+            raise RuntimeError(f"oracle error {e}: " + self.last_error())
+        return inner.value, bool(stop.value)
 
     def newton(self, et, Y, t0):
         Y = np.ascontiguousarray(Y, dtype=np.float64)

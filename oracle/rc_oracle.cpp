@@ -146,7 +146,276 @@ static long toi(const std::string& s) { return std::strtol(s.c_str(), nullptr, 1
 
 // ------------------------------------------------------------- errors ------
 enum Err { E_OK = 0, E_THERMO_T = 1, E_TRANSPORT_T = 2, E_NEG_TIMESTEP = 4, E_NEG_FLUX = 8,
-           E_NAN = 16, E_BCTYPE = 32, E_SETUP = 64 };
+           E_NAN = 16, E_BCTYPE = 32, E_SETUP = 64, E_LINSOLVE = 128 };
+
+// ------------------------------------------ LAPACK dgesvx restatement -----
+// advanced_linear_solve_lapack (la_math.f90:120-215) solves the per-cell
+// system of the BDF2 sweeps with LAPACK's expert driver
+//   dgesvx('E', 'N', n, 1, A, n, AF, n, ipiv, equed, r, c, b, n, x, n, rcond, ferr, berr, ...)
+// and stops unless info == 0.  LAPACK is linked as -llapack (src/Makefile:43)
+// without a pinned version; this restates reference LAPACK 3.12 / reference
+// BLAS (netlib): dgeequ + dlaqge (equilibration), dgetrf (partial pivoting;
+// the recursive dgetrf2 and the unblocked dgetf2 perform the same operations
+// on every entry for n <= 64), dgecon (rcond: dlacn2's Hager-Higham estimate
+// over triangular solves), dgetrs and dgerfs's iterative refinement.  The
+// forward-error estimate of dgerfs and the pivot growth only inform and do
+// not change x; they are not restated.  dlatrs, inside dgecon, is restated by
+// its unscaled branch (dtrsv), which it takes unless a solve can overflow.
+// Matrices are column-major: A(i,j) = a[i + n*j], 0-based.
+namespace lap {
+constexpr double EPS = 1.1102230246251565e-16;     // dlamch('E') = 2^-53
+constexpr double SFMIN = 2.2250738585072014e-308;  // dlamch('S') = 2^-1022
+constexpr double PREC = 2.220446049250313e-16;     // dlamch('P') = 2^-52
+inline double mx(double a, double b) { return (b > a) ? b : a; }  // Fortran MAX/MIN
+inline double mn(double a, double b) { return (b < a) ? b : a; }
+inline int idamax(int n, const double* x) {
+  int k = 0;
+  double m = std::fabs(x[0]);
+  for (int i = 1; i < n; ++i)
+    if (std::fabs(x[i]) > m) { k = i; m = std::fabs(x[i]); }
+  return k;
+}
+inline double dasum(int n, const double* x) {
+  double t = 0.0;
+  for (int i = 0; i < n; ++i) t = t + std::fabs(x[i]);
+  return t;
+}
+// dgeequ: row and column scale factors; returns 0 or the 1-based index of a
+// zero row (i) or column (n + j).
+inline int dgeequ(int n, const double* a, double* r, double* c, double& rowcnd, double& colcnd, double& amax) {
+  const double smlnum = SFMIN, bignum = 1.0 / smlnum;
+  for (int i = 0; i < n; ++i) r[i] = 0.0;
+  for (int j = 0; j < n; ++j)
+    for (int i = 0; i < n; ++i) r[i] = mx(r[i], std::fabs(a[i + n * j]));
+  double rcmin = bignum, rcmax = 0.0;
+  for (int i = 0; i < n; ++i) { rcmax = mx(rcmax, r[i]); rcmin = mn(rcmin, r[i]); }
+  amax = rcmax;
+  if (rcmin == 0.0) {
+    for (int i = 0; i < n; ++i)
+      if (r[i] == 0.0) return i + 1;
+  }
+  for (int i = 0; i < n; ++i) r[i] = 1.0 / mn(mx(r[i], smlnum), bignum);
+  rowcnd = mx(rcmin, smlnum) / mn(rcmax, bignum);
+  for (int j = 0; j < n; ++j) c[j] = 0.0;
+  for (int j = 0; j < n; ++j)
+    for (int i = 0; i < n; ++i) c[j] = mx(c[j], std::fabs(a[i + n * j]) * r[i]);
+  rcmin = bignum; rcmax = 0.0;
+  for (int j = 0; j < n; ++j) { rcmin = mn(rcmin, c[j]); rcmax = mx(rcmax, c[j]); }
+  if (rcmin == 0.0) {
+    for (int j = 0; j < n; ++j)
+      if (c[j] == 0.0) return n + j + 1;
+  }
+  for (int j = 0; j < n; ++j) c[j] = 1.0 / mn(mx(c[j], smlnum), bignum);
+  colcnd = mx(rcmin, smlnum) / mn(rcmax, bignum);
+  return 0;
+}
+// dlaqge: scale A by rows and/or columns; returns equed 'N', 'R', 'C' or 'B'.
+inline char dlaqge(int n, double* a, const double* r, const double* c, double rowcnd, double colcnd, double amax) {
+  const double thresh = 0.1, small = SFMIN / PREC, large = 1.0 / small;
+  if (rowcnd >= thresh && amax >= small && amax <= large) {
+    if (colcnd >= thresh) return 'N';
+    for (int j = 0; j < n; ++j)
+      for (int i = 0; i < n; ++i) a[i + n * j] = c[j] * a[i + n * j];
+    return 'C';
+  }
+  if (colcnd >= thresh) {
+    for (int j = 0; j < n; ++j)
+      for (int i = 0; i < n; ++i) a[i + n * j] = r[i] * a[i + n * j];
+    return 'R';
+  }
+  for (int j = 0; j < n; ++j)
+    for (int i = 0; i < n; ++i) a[i + n * j] = c[j] * r[i] * a[i + n * j];
+  return 'B';
+}
+// dgetrf: A = P L U in place (unit L below the diagonal); ipiv 0-based;
+// returns 0 or the 1-based column of the first zero pivot.
+inline int dgetrf(int n, double* a, int* ipiv) {
+  int info = 0;
+  for (int j = 0; j < n; ++j) {
+    const int jp = j + idamax(n - j, a + j + n * j);
+    ipiv[j] = jp;
+    if (a[jp + n * j] != 0.0) {
+      if (jp != j)
+        for (int k = 0; k < n; ++k) std::swap(a[j + n * k], a[jp + n * k]);
+      if (j < n - 1) {
+        if (std::fabs(a[j + n * j]) >= SFMIN) {
+          const double rp = 1.0 / a[j + n * j];
+          for (int i = j + 1; i < n; ++i) a[i + n * j] = rp * a[i + n * j];
+        } else {
+          for (int i = j + 1; i < n; ++i) a[i + n * j] = a[i + n * j] / a[j + n * j];
+        }
+      }
+    } else if (info == 0) {
+      info = j + 1;
+    }
+    for (int jj = j + 1; jj < n; ++jj) {  // dger: A22 += x * (-y)
+      if (a[j + n * jj] != 0.0) {
+        const double temp = -1.0 * a[j + n * jj];
+        for (int i = j + 1; i < n; ++i) a[i + n * jj] = a[i + n * jj] + a[i + n * j] * temp;
+      }
+    }
+  }
+  return info;
+}
+// dgetrs('N'): b <- A^-1 b with the factors of dgetrf.
+inline void dgetrs(int n, const double* af, const int* ipiv, double* b) {
+  for (int i = 0; i < n; ++i)
+    if (ipiv[i] != i) std::swap(b[i], b[ipiv[i]]);
+  for (int k = 0; k < n; ++k)
+    if (b[k] != 0.0)
+      for (int i = k + 1; i < n; ++i) b[i] = b[i] - b[k] * af[i + n * k];
+  for (int k = n - 1; k >= 0; --k)
+    if (b[k] != 0.0) {
+      b[k] = b[k] / af[k + n * k];
+      for (int i = 0; i < k; ++i) b[i] = b[i] - b[k] * af[i + n * k];
+    }
+}
+// dgerfs('N') refinement of x: at most 5 corrections while the componentwise
+// backward error exceeds eps and halves.  Returns the last backward error.
+inline double dgerfs(int n, const double* a, const double* af, const int* ipiv, const double* b, double* x) {
+  const int itmax = 5;
+  const double eps = EPS, safmin = SFMIN, safe1 = (n + 1) * safmin, safe2 = safe1 / eps;
+  double r[16], w[16], berr = 0.0, lstres = 3.0;
+  int count = 1;
+  for (;;) {
+    for (int i = 0; i < n; ++i) r[i] = b[i];
+    for (int j = 0; j < n; ++j) {  // dgemv: r = -A x + r
+      const double temp = -1.0 * x[j];
+      for (int i = 0; i < n; ++i) r[i] = r[i] + temp * a[i + n * j];
+    }
+    for (int i = 0; i < n; ++i) w[i] = std::fabs(b[i]);
+    for (int k = 0; k < n; ++k) {
+      const double xk = std::fabs(x[k]);
+      for (int i = 0; i < n; ++i) w[i] = w[i] + std::fabs(a[i + n * k]) * xk;
+    }
+    double sv = 0.0;
+    for (int i = 0; i < n; ++i) {
+      if (w[i] > safe2) sv = mx(sv, std::fabs(r[i]) / w[i]);
+      else sv = mx(sv, (std::fabs(r[i]) + safe1) / (w[i] + safe1));
+    }
+    berr = sv;
+    if (!(berr > eps && 2.0 * berr <= lstres && count <= itmax)) break;
+    dgetrs(n, af, ipiv, r);
+    for (int i = 0; i < n; ++i) x[i] = x[i] + r[i];  // daxpy, alpha = 1
+    lstres = berr;
+    count = count + 1;
+  }
+  return berr;
+}
+// dlange('1'): largest column sum of |A|.
+inline double dlange1(int n, const double* a) {
+  double value = 0.0;
+  for (int j = 0; j < n; ++j) {
+    double sum = 0.0;
+    for (int i = 0; i < n; ++i) sum = sum + std::fabs(a[i + n * j]);
+    if (value < sum || std::isnan(sum)) value = sum;
+  }
+  return value;
+}
+// dgecon('1'): reciprocal condition estimate from the factors; the solves
+// of kase 1 are inv(L) then inv(U), of kase 2 inv(U^T) then inv(L^T).
+inline void trs_kase(int n, const double* af, int kase, double* x) {
+  if (kase == 1) {
+    for (int j = 0; j < n; ++j)
+      if (x[j] != 0.0) {
+        const double temp = x[j];
+        for (int i = j + 1; i < n; ++i) x[i] = x[i] - temp * af[i + n * j];
+      }
+    for (int j = n - 1; j >= 0; --j)
+      if (x[j] != 0.0) {
+        x[j] = x[j] / af[j + n * j];
+        const double temp = x[j];
+        for (int i = j - 1; i >= 0; --i) x[i] = x[i] - temp * af[i + n * j];
+      }
+  } else {
+    for (int j = 0; j < n; ++j) {
+      double temp = x[j];
+      for (int i = 0; i < j; ++i) temp = temp - af[i + n * j] * x[i];
+      x[j] = temp / af[j + n * j];
+    }
+    for (int j = n - 1; j >= 0; --j) {
+      double temp = x[j];
+      for (int i = n - 1; i > j; --i) temp = temp - af[i + n * j] * x[i];
+      x[j] = temp;
+    }
+  }
+}
+inline double dgecon(int n, const double* af, double anorm) {
+  if (n == 0) return 1.0;
+  if (anorm == 0.0) return 0.0;
+  if (std::isnan(anorm)) return anorm;
+  // dlacn2 (itmax 5), its reverse communication unrolled
+  double x[16], v[16], est, estold;
+  int isgn[16];
+  for (int i = 0; i < n; ++i) x[i] = 1.0 / (double)n;
+  trs_kase(n, af, 1, x);
+  if (n == 1) {
+    v[0] = x[0];
+    est = std::fabs(v[0]);
+  } else {
+    est = dasum(n, x);
+    for (int i = 0; i < n; ++i) { x[i] = (x[i] >= 0.0) ? 1.0 : -1.0; isgn[i] = (int)std::lround(x[i]); }
+    trs_kase(n, af, 2, x);
+    int j = idamax(n, x), iter = 2;
+    for (;;) {
+      for (int i = 0; i < n; ++i) x[i] = 0.0;
+      x[j] = 1.0;
+      trs_kase(n, af, 1, x);
+      for (int i = 0; i < n; ++i) v[i] = x[i];
+      estold = est;
+      est = dasum(n, v);
+      bool same = true;
+      for (int i = 0; i < n; ++i)
+        if ((x[i] >= 0.0 ? 1 : -1) != isgn[i]) { same = false; break; }
+      if (same || est <= estold) break;
+      for (int i = 0; i < n; ++i) { x[i] = (x[i] >= 0.0) ? 1.0 : -1.0; isgn[i] = (int)std::lround(x[i]); }
+      trs_kase(n, af, 2, x);
+      const int jlast = j;
+      j = idamax(n, x);
+      if (x[jlast] != std::fabs(x[j]) && iter < 5) { iter = iter + 1; continue; }
+      break;
+    }
+    double altsgn = 1.0;
+    for (int i = 0; i < n; ++i) {
+      x[i] = altsgn * (1.0 + (double)i / (double)(n - 1));
+      altsgn = -altsgn;
+    }
+    trs_kase(n, af, 1, x);
+    const double temp = 2.0 * (dasum(n, x) / (double)(3 * n));
+    if (temp > est) est = temp;
+  }
+  if (est != 0.0) return (1.0 / est) / anorm;
+  return 0.0;
+}
+// dgesvx('E', 'N', n, 1): a (column-major) is overwritten by its equilibrated
+// form, b by diag(r) b when rows were scaled; x gets the solution.  Returns
+// info: 0, k (zero pivot in column k: x not computed) or n + 1 (rcond < eps).
+inline int dgesvx(int n, double* a, double* b, double* x, char* equed_out = nullptr, double* rcond_out = nullptr) {
+  double r[16], c[16], af[256], rowcnd = 0, colcnd = 0, amax = 0;
+  int ipiv[16];
+  char equed = 'N';
+  if (dgeequ(n, a, r, c, rowcnd, colcnd, amax) == 0) equed = dlaqge(n, a, r, c, rowcnd, colcnd, amax);
+  const bool rowequ = equed == 'R' || equed == 'B', colequ = equed == 'C' || equed == 'B';
+  if (rowequ)
+    for (int i = 0; i < n; ++i) b[i] = r[i] * b[i];
+  for (int k = 0; k < n * n; ++k) af[k] = a[k];
+  if (equed_out) *equed_out = equed;
+  const int info = dgetrf(n, af, ipiv);
+  if (info > 0) {
+    if (rcond_out) *rcond_out = 0.0;
+    return info;
+  }
+  const double anorm = dlange1(n, a);
+  const double rcond = dgecon(n, af, anorm);
+  if (rcond_out) *rcond_out = rcond;
+  for (int i = 0; i < n; ++i) x[i] = b[i];
+  dgetrs(n, af, ipiv, x);
+  dgerfs(n, a, af, ipiv, b, x);
+  if (colequ)
+    for (int i = 0; i < n; ++i) x[i] = c[i] * x[i];
+  return rcond < EPS ? n + 1 : 0;
+}
+}  // namespace lap
 
 struct Oracle {
   // ---- species (src/combustion_modeling/species.f90:4-12)
@@ -197,6 +466,8 @@ struct Oracle {
   FA1<int> KFace, Neigh, FProperty, NumNFace, Num_ghostcell, Hostcell, Hostface, BCtype_Ghostcell;
   FA2<double> COOR, VECX, SideOfs, CELLXY, reflen, XYH, WA, PA, hWA, GPA, wdis, CellXY_Ghostcell;
   FA1<double> VOL, alpaF, step, vol_Ghostcell;
+  FA2<double> WP, WP2, fixed;  // unsteady: WA of the last two physical steps, the BDF2 source term
+  double dt = 0;               // physical time step
   FA3<double> GradC, AMLS, Ofs, Coor_Ghostnode;
   long Nghostcell = 0;
 
@@ -391,9 +662,14 @@ struct Oracle {
       auto v = r.read(3);
       p_out_ratio = tod(v[0]); A_p = tod(v[1]); f_p = tod(v[2]);
     }
-    if (!IfSteady || IfExplicit || IfRightDomain || NPar != 1)
-      throw std::runtime_error("oracle covers the steady implicit single-partition path only");
-    InLoop = 1; InnerLoop = 1;  // initParam.f90:220-222
+    if (IfExplicit || IfRightDomain || NPar != 1 || (!IfSteady && implicit_time_method != 5))
+      throw std::runtime_error("oracle covers the steady implicit and the unsteady BDF2 single-partition paths only");
+    if (IfSteady) {
+      InLoop = 1; InnerLoop = 1;  // initParam.f90:220-222
+    } else {
+      dt = totaltime / (double)nstep_max;  // initParam.f90:72
+      InLoop = 1;                          // BDF2: one stage, cs(1) = 1 (initParam.f90:131-134)
+    }
   }
 
   // ============================================ thermochemistry (L3) =======
@@ -809,6 +1085,7 @@ struct Oracle {
     N.alloc(4, NE_Vir, 0); NeighF.alloc(4, NE_Vir, 0); KFace.alloc(NE_Vir, 0);
     COOR.alloc(2, NNT_vir, 0.0); VOL.alloc(NE_Vir, 0.0); CELLXY.alloc(2, NE_Vir, 0.0); reflen.alloc(2, NE_Vir, 0.0);
     WA.alloc(NVar, NE_Vir, 0.0); PA.alloc(NVar, NE_Vir, 0.0); GradC.alloc(MaxOrder, NVar, NE_Vir, 0.0);
+    if (!IfSteady) { WP.alloc(NVar, NE_Vir, 0.0); WP2.alloc(NVar, NE_Vir, 0.0); fixed.alloc(NVar, NE_Vir, 0.0); }
     hWA.alloc(NVar, NE_Vir, 0.0); XYH.alloc(MaxOrder, NE_Vir, 0.0); step.alloc(NE_Vir, 0.0);
     // allocate_face_arrary (allocate_arrary.f90:118-141)
     FNode.alloc(2, NF_vir, 0); Neighbor.alloc(2, NF_vir, 0); FProperty.alloc(NF_vir, 0);
@@ -1831,6 +2108,171 @@ struct Oracle {
     for (int k = 0; k < NVar; ++k) res[k] = s[k] / total_volume;
     *romax = rm;
   }
+  // ====================================== unsteady dual-time BDF2 (L5) ====
+  // Per-cell system matrix of BDF2_LU_SGS (Time_BDF2.f90:118-127, 216-224):
+  // dU/dP(PA_i) * dd_i, minus vol_i * d omega/dP in the species rows;
+  // column-major for the dgesvx restatement.
+  void bdf2_matrix(long i, double ddi, double* a) {
+    const int nv = NVar;
+    double pri[16], jaco[256], dw[256];
+    for (int k = 1; k <= nv; ++k) pri[k - 1] = PA(k, i);
+    Compute_Con_to_Pri_Jaco(pri, jaco);
+    for (int k = 0; k < nv * nv; ++k) jaco[k] = jaco[k] * ddi;
+    if (nv > NFlow) {
+      compute_derivative_production_rate(pri, dw);
+      for (int j = 0; j < nv - NFlow; ++j)
+        for (int c = 0; c < nv; ++c) jaco[(NFlow + j) * nv + c] = jaco[(NFlow + j) * nv + c] - VOL(i) * dw[j * nv + c];
+    }
+    for (int r = 0; r < nv; ++r)
+      for (int c = 0; c < nv; ++c) a[r + nv * c] = jaco[r * nv + c];
+  }
+  // One cell of the forward (NR < i) or backward (NR > i) sweep of
+  // BDF2_LU_SGS (Time_BDF2.f90:112-209, 217-305): hWA holds primitive
+  // increments dP; the neighbours' dP become conservative increments dU, the
+  // Rusanov-split flux differences are added in NeighF order, and the cell's
+  // system is solved by advanced_linear_solve_lapack.
+  void bdf2_cell(long i, bool fwd, const std::vector<double>& dd) {
+    const int nv = NVar, nY = NVar - NFlow;
+    double dflux[16], yy[16], entha[16], dyy[16], dry[16], ry[16], Cp, gama, Rcpcv;
+    for (int k = 0; k < nv; ++k) dflux[k] = 0.0;
+    for (int nei = 1; nei <= KFace(i); ++nei) {
+      int iface = NeighF(nei, i);
+      double dx = VECX(1, iface), dy = VECX(2, iface);
+      int NR = Neighbor(2, iface);
+      if (i == NR) { NR = Neighbor(1, iface); dx = -dx; dy = -dy; }
+      if (NR > 0 && (fwd ? NR < i : NR > i)) {
+        const double pp = PA(1, NR), uu = PA(2, NR), vv = PA(3, NR), tt = PA(4, NR);
+        cell_Y(PA, NR, yy);
+        ComputeGasParameter(yy, tt, Cp, gama, Rcpcv);
+        compute_enthalpy(tt, entha);
+        double hh = 0.0;
+        for (int k = 0; k < Nsp; ++k) hh = hh + yy[k] * entha[k];
+        const double rr = pp / (Rcpcv * tt);
+        const double rou = rr * uu, rov = rr * vv;
+        const double roe = rr * (hh + 0.5 * (powi(uu, 2) + powi(vv, 2))) - pp;
+        for (int k = 0; k < Nsp; ++k) ry[k] = rr * yy[k];
+        const double dpp = hWA(1, NR), duu = hWA(2, NR), dvv = hWA(3, NR), dtt = hWA(4, NR);
+        double s = 0.0;
+        for (int k = 1; k <= nY; ++k) { dyy[k - 1] = hWA(NFlow + k, NR); s = s + dyy[k - 1]; }
+        dyy[nY] = -s;
+        double s1 = 0.0, s2 = 0.0;
+        for (int k = 0; k < Nsp; ++k) s1 = s1 + R_species[k] * dyy[k];
+        const double drr = (dpp - rr * Rcpcv * dtt - rr * tt * s1) / (Rcpcv * tt);
+        const double dru = rr * duu + uu * drr;
+        const double drv = rr * dvv + vv * drr;
+        for (int k = 0; k < Nsp; ++k) s2 = s2 + entha[k] * dyy[k];
+        const double dre = rr * Cp * dtt + rr * s2 + hh * drr + rr * (uu * duu + vv * dvv) +
+                           0.5 * (powi(uu, 2) + powi(vv, 2)) * drr - dpp;
+        for (int k = 0; k < Nsp; ++k) dry[k] = rr * dyy[k] + yy[k] * drr;
+        const double unormal = uu * dx + vv * dy;
+        const double dunormal = duu * dx + dvv * dy;
+        const double aF = alpaF(iface);
+        dflux[0] = dflux[0] + 0.5 * (-aF * drr + dru * dx + drv * dy);
+        dflux[1] = dflux[1] + 0.5 * (-aF * dru + dru * unormal + rou * dunormal + dpp * dx);
+        dflux[2] = dflux[2] + 0.5 * (-aF * drv + drv * unormal + rov * dunormal + dpp * dy);
+        dflux[3] = dflux[3] + 0.5 * (-aF * dre + dunormal * (roe + pp) + unormal * (dre + dpp));
+        for (int k = 0; k < nY; ++k)
+          dflux[NFlow + k] = dflux[NFlow + k] + 0.5 * (-aF * dry[k] + dry[k] * unormal + ry[k] * dunormal);
+      }
+    }
+    double a[256], rhs[16], sol[16];
+    bdf2_matrix(i, dd[i], a);
+    for (int k = 1; k <= nv; ++k) rhs[k - 1] = fwd ? hWA(k, i) - dflux[k - 1] : dflux[k - 1];
+    if (lap::dgesvx(nv, a, rhs, sol) != 0) {
+      fail(E_LINSOLVE, "error in routine dgesvx");
+      for (int k = 0; k < nv; ++k) sol[k] = 0.0;
+    }
+    for (int k = 1; k <= nv; ++k) hWA(k, i) = fwd ? sol[k - 1] : hWA(k, i) - sol[k - 1];
+  }
+  // BDF2_LU_SGS (Time_BDF2.f90:73-337)
+  void BDF2_LU_SGS(int inner_rk, double phi) {
+    if (inner_rk == 1) {
+#pragma omp parallel for schedule(static) num_threads(nthreads) if (nthreads > 1)
+      for (long i = 1; i <= NE; ++i)
+        for (int k = 1; k <= NVar; ++k)
+          fixed(k, i) = VOL(i) / dt * ((1 + 2 * phi) * WP(k, i) - phi * WP2(k, i));
+    }
+    std::vector<double> dd(NE + 1, 0.0);
+#pragma omp parallel for schedule(static) num_threads(nthreads) if (nthreads > 1)
+    for (long i = 1; i <= NE; ++i) {
+      double d = 0.0;
+      for (int nei = 1; nei <= KFace(i); ++nei) d = d + 0.5 * alpaF(NeighF(nei, i));
+      dd[i] = d + VOL(i) * (1. / step(i) + (1 + phi) / dt);
+      for (int k = 1; k <= NVar; ++k) hWA(k, i) = hWA(k, i) - (1 + phi) * VOL(i) / dt * WA(k, i) + fixed(k, i);
+    }
+    if (nthreads <= 1) {
+      for (long i = 1; i <= NE; ++i) bdf2_cell(i, true, dd);
+      for (long i = NE; i >= 1; --i) bdf2_cell(i, false, dd);
+    } else {
+      for (size_t l = 0; l + 1 < fwd_off.size(); ++l) {
+#pragma omp parallel for schedule(static) num_threads(nthreads)
+        for (long q = fwd_off[l]; q < fwd_off[l + 1]; ++q) bdf2_cell(fwd_cells[q], true, dd);
+      }
+      for (size_t l = 0; l + 1 < bwd_off.size(); ++l) {
+#pragma omp parallel for schedule(static) num_threads(nthreads)
+        for (long q = bwd_off[l]; q < bwd_off[l + 1]; ++q) bdf2_cell(bwd_cells[q], false, dd);
+      }
+    }
+    for (long i = 1; i <= NE; ++i)
+      for (int k = 1; k <= NVar; ++k) PA(k, i) = PA(k, i) + hWA(k, i);
+    primitve_to_conserved_variables();
+  }
+  // inner_iteration_residual (residual.f90:23-59): RoRes = sum of the species
+  // rows of the normalised Residual of hWA (zero without species).
+  double inner_iteration_residual() {
+    double res[16], romax;
+    residual(res, &romax);
+    double r = 0.0;
+    for (int k = NFlow; k < NVar; ++k) r = r + res[k];
+    return r;
+  }
+  // BDF2_stage (Time_BDF2.f90:4-71); returns the inner iterations taken.
+  int BDF2_stage(long istep) {
+    double phi;
+    if (istep == 1) {
+      WP.d = WA.d; WP2.d = WP.d; phi = 0.;
+    } else {
+      WP2.d = WP.d; WP.d = WA.d; phi = 0.5;
+    }
+    double RoRes_tmp = 0.0;
+    int inner_rk = 1;
+    for (; inner_rk <= InnerLoop; ++inner_rk) {
+      timestep();
+      reconstruction();
+      flux_sourceterm();
+      BDF2_LU_SGS(inner_rk, phi);
+      const double RoRes = inner_iteration_residual();
+      if (inner_rk == 1) RoRes_tmp = RoRes;
+      if (RoRes < RoRes_tmp * relTol || inner_rk == InnerLoop) {
+        reconstruction();
+        flux_sourceterm();
+        break;
+      }
+      if (std::isnan(WA(1, 1))) { fail(E_NAN, "there is NAN"); break; }
+    }
+    return inner_rk;
+  }
+  // compute_p_out (fvm2d.f90:229-239)
+  void compute_p_out() {
+    const double pi = 4 * std::atan(1.0);
+    p_out = p_static * (1. + A_p * std::sin(2 * pi * f_p * ttime));
+  }
+  // One physical step of the unsteady implicit branch of the main loop
+  // (fvm2d.f90:48-104, InLoop = 1, cs(1) = 1): shortens the last step to end
+  // at totaltime (:52-56), advances ttime and p_out around BDF2_stage.
+  // Returns the inner iterations; *stop is set after the last step.
+  int unsteady_step(long istep, int* stop) {
+    const double totaltime_num = totaltime * (1. - 1.e-10);
+    *stop = 0;
+    if (ttime + dt > totaltime_num) { dt = totaltime - ttime; *stop = 1; }
+    const double ttime_n = ttime;
+    ttime = ttime_n + 1.0 * dt;
+    compute_p_out();
+    const int inner = BDF2_stage(istep);
+    ttime = ttime_n + dt;
+    compute_p_out();
+    return inner;
+  }
   // main (fvm2d.f90:7-47): start-up, mesh, initial field, LS matrices.
   void open(const std::string& dir) {
     startup(dir);
@@ -1911,7 +2353,7 @@ void* orc_array(void* h, const char* name, long* n) {
   ARR("N", N) ARR("KFace", KFace) ARR("NeighF", NeighF) ARR("NeighC", NeighC) ARR("Neigh", Neigh)
   ARR("FNode", FNode) ARR("Neighbor", Neighbor) ARR("FProperty", FProperty) ARR("Ghostcell", Ghostcell)
   ARR("Num_ghostcell", Num_ghostcell) ARR("Hostcell", Hostcell) ARR("Hostface", Hostface)
-  ARR("BCtype_Ghostcell", BCtype_Ghostcell)
+  ARR("BCtype_Ghostcell", BCtype_Ghostcell) ARR("WP", WP) ARR("WP2", WP2) ARR("fixed", fixed)
 #undef ARR
   *n = 0;
   return nullptr;
@@ -2002,5 +2444,36 @@ double orc_newton(void* h, double et, const double* Y, double t0) {
   double t, a, b, c;
   static_cast<Oracle*>(h)->Newton_temperature(et, Y, t, t0, a, b, c);
   return t;
+}
+// ---- unsteady dual-time BDF2 (implicit_time_method 5)
+// unsteady scalars: ttime, dt, p_out, p_static, relTol, InnerLoop, IfSteady, A_p, f_p, totaltime, nstep_max
+void orc_unsteady_scalars(void* h, double* s) {
+  auto* o = static_cast<Oracle*>(h);
+  s[0] = o->ttime; s[1] = o->dt; s[2] = o->p_out; s[3] = o->p_static; s[4] = o->relTol; s[5] = o->InnerLoop;
+  s[6] = o->IfSteady; s[7] = o->A_p; s[8] = o->f_p; s[9] = o->totaltime; s[10] = (double)o->nstep_max;
+}
+// BDF2_LU_SGS with the given inner iteration and phi (the caller sets WP,
+// WP2 through orc_array); returns the error bit mask.
+int orc_bdf2_lusgs(void* h, int inner_rk, double phi) {
+  auto* o = static_cast<Oracle*>(h);
+  if (o->IfSteady) { o->errmsg = "BDF2 needs an unsteady case"; return orc::E_SETUP; }
+  o->BDF2_LU_SGS(inner_rk, phi);
+  return o->err.load();
+}
+// One physical step (time advance, p_out, BDF2_stage); inner iterations and
+// the last-step flag are returned through the pointers.
+int orc_unsteady_step(void* h, long istep, int* inner, int* stop) {
+  auto* o = static_cast<Oracle*>(h);
+  if (o->IfSteady) { o->errmsg = "BDF2 needs an unsteady case"; return orc::E_SETUP; }
+  *inner = o->unsteady_step(istep, stop);
+  return o->err.load();
+}
+// The dgesvx restatement alone (column-major a, n <= 16): x, info, equed, rcond.
+int orc_dgesvx(int n, const double* a, const double* b, double* x, char* equed, double* rcond) {
+  if (n < 1 || n > 16) return -1;
+  double aa[256], bb[16];
+  for (int k = 0; k < n * n; ++k) aa[k] = a[k];
+  for (int k = 0; k < n; ++k) bb[k] = b[k];
+  return orc::lap::dgesvx(n, aa, bb, x, equed, rcond);
 }
 }  // extern "C"

@@ -13,6 +13,12 @@ reference subroutine of the steady iteration:
     Solver.lu_sgs_stage(i)     lu_sgs_stage        src/Time_LUSGS_steady.f90:74
     Solver.residual()          Residual/step_residual  src/residual.f90:4,61
 
+and, for the unsteady dual-time scheme (implicit_time_method 5):
+
+    Solver.bdf2_lusgs(k, phi, dt)     BDF2_LU_SGS     src/Time_BDF2.f90:73
+    Solver.bdf2_stage(i, dt, n, tol)  BDF2_stage      src/Time_BDF2.f90:4
+    Case.run_unsteady(n)              the unsteady branch of program main (src/fvm2d.f90:48-150)
+
 There is no CPU fallback: if the library is missing or no GPU is present the
 calls raise.
 """
@@ -29,7 +35,7 @@ from . import build as _build
 RC_OK = 0
 RC_ERR = {1: "thermo T out of range", 2: "transport T out of range", 4: "negative rho/p/T in TimeStep",
           8: "negative rho/p at a face", 16: "NaN in WA(1,1)", 32: "unknown boundary code",
-          64: "grid barrier timed out",
+          64: "grid barrier timed out", 128: "BDF2 cell system singular (dgesvx)",
           1024: "invalid argument", 2048: "CUDA error"}
 RC_PREC_FP64, RC_PREC_MIXED, RC_PREC_MIXED_DC = 0, 1, 2
 RC_CHEM_EXPLICIT, RC_CHEM_INTEGRATED, RC_CHEM_SURROGATE = 0, 1, 2
@@ -123,6 +129,11 @@ SIGNATURES = {
     "rc_mlp_last_error": (_cp, [_vp]),
     "rc_chem_substeps": (_i, [_vp, _IP]),
     "rc_chem_integrate": (_i, [_vp, _vp, _vp, _i, _vp, _vp, _d, _i]),
+    "rc_set_p_out": (_i, [_vp, _DP]),
+    "rc_bdf2_stage": (_i, [_vp, _i, _d, _i, _d, _IP]),
+    "rc_bdf2_lusgs": (_i, [_vp, _i, _d, _d]),
+    "rc_case_unsteady": (_i, [_vp, _DP]),
+    "rc_run_unsteady": (_i, [_vp, _i, _l, _l, _DP, _IP]),
 }
 
 _lib: Optional[ctypes.CDLL] = None
@@ -245,6 +256,26 @@ class Case:
         if st:
             raise RcError(st, load().rc_case_error(self._h).decode())
         return hist, int(sw.value)
+
+    @property
+    def unsteady(self) -> dict:
+        """Time scheme of the case (flow_solver_info.in and the backup's time)."""
+        o = np.zeros(10)
+        load().rc_case_unsteady(self._h, _dp(o))
+        return {"unsteady": bool(o[0]), "ttime": o[1], "dt": o[2], "totaltime": o[3], "nstep_max": int(o[4]),
+                "inner_loop": int(o[5]), "rel_tol": o[6], "p_static": o[7], "A_p": o[8], "f_p": o[9]}
+
+    def run_unsteady(self, nsteps: int, every: int = 1, device: int = 0):
+        """The unsteady BDF2 driver (rc_run_unsteady): up to nsteps physical
+        steps from the case's state and time, which it advances; returns
+        (residual history every `every` steps, inner iterations per step)."""
+        hist = np.zeros((nsteps // every, self.NVar + 1))
+        inner = np.zeros(nsteps, dtype=np.int32)
+        st = load().rc_run_unsteady(self._h, int(device), int(nsteps), int(every), _dp(hist),
+                                    inner.ctypes.data_as(_IP))
+        if st:
+            raise RcError(st, load().rc_case_error(self._h).decode())
+        return hist, inner
 
     def views(self, precision: int = RC_PREC_FP64, device: int = 0):
         m, t, g = RcMesh(), RcThermo(), RcConfig()
@@ -385,6 +416,23 @@ class Solver:
             self.lu_sgs_stage(it)
         return self.sync()
 
+    # -- unsteady dual-time BDF2
+    def set_p_out(self, p_out: float):
+        """Exit pressure for the following calls (compute_p_out's result)."""
+        p = np.array([float(p_out)])
+        self._check(load().rc_set_p_out(self._h, _dp(p)))
+
+    def bdf2_lusgs(self, inner_rk: int, phi: float, dt: float):
+        """BDF2_LU_SGS on the current residual (time levels from set_array("WP"/"WP2"))."""
+        return self._check(load().rc_bdf2_lusgs(self._h, int(inner_rk), float(phi), float(dt)))
+
+    def bdf2_stage(self, istep: int, dt: float, inner_loop: int, rel_tol: float) -> int:
+        """BDF2_stage; returns the inner iterations taken."""
+        n = ctypes.c_int()
+        self._check(load().rc_bdf2_stage(self._h, int(istep), float(dt), int(inner_loop), float(rel_tol),
+                                         ctypes.byref(n)))
+        return n.value
+
     def residual(self) -> Tuple[np.ndarray, float]:
         r = np.zeros(self.NVar)
         m = np.zeros(1)
@@ -412,7 +460,8 @@ class Solver:
 
     _SHAPES = {"PA": lambda s: (s.NE, s.NVar), "WA": lambda s: (s.NE, s.NVar), "hWA": lambda s: (s.NE, s.NVar),
                "GradC": lambda s: (s.NE, s.NVar, 2), "GPA": lambda s: (s.Nghost, s.NVar),
-               "alpaF": lambda s: (s.NF,), "step": lambda s: (s.NE,)}
+               "alpaF": lambda s: (s.NF,), "step": lambda s: (s.NE,), "WP": lambda s: (s.NE, s.NVar),
+               "WP2": lambda s: (s.NE, s.NVar)}
 
     def get_array(self, name: str) -> np.ndarray:
         out = np.zeros(self._SHAPES[name](self))

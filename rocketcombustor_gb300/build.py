@@ -26,6 +26,7 @@ UNITS = {
     "rc_core.cu": ["--fmad=false"],
     "rc_noalloc.cu": ["--fmad=false"],
     "rc_chem.cu": ["--fmad=false"],
+    "rc_bdf2.cu": ["--fmad=false"],
     "rc_mlp.cu": [],
     "rc_mixed.cu": ["--use_fast_math"],
 }

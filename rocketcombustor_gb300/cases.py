@@ -291,20 +291,25 @@ def write_inlet(path: str, Y: Sequence[float], T: float, p: float, mflow: float,
 
 
 def write_flow_info(d: str, combustion: bool, viscous: bool, cfl: float, nstep: int,
-                    limit_id: int, p_out_ratio: float) -> None:
+                    limit_id: int, p_out_ratio: float, unsteady: bool = False, totaltime: float = 1.0,
+                    inner_loop: int = 1, rel_tol: float = 1.0e-8, a_p: float = 0.0, f_p: float = 5000.0) -> None:
+    """flow/flow_solver_info.in (startup.f90:55-128).  Steady implicit LU-SGS,
+    or with `unsteady` the dual-time BDF2 scheme (implicit_time_method 5,
+    physical step totaltime/nstep, inner_loop inner iterations stopped at
+    rel_tol, exit pressure p_static (1 + a_p sin(2 pi f_p t)))."""
     L = lambda b: ".true." if b else ".false."  # noqa: E731
     with open(os.path.join(d, "flow", "flow_solver_info.in"), "w") as f:
         f.write(f"# If_turn_on_combustion, chemical model\n{L(combustion)}\n")
         f.write("# IfRightDomain\n.false.\n# NPreviousPar\n1\n# Npar, number of processors\n1\n")
         f.write("# unit\n1.0\n")
-        f.write(f"# IfSteady, IfViscous, IfReadBackup, IfExplicit\n.true., {L(viscous)}, .true., .false.\n")
+        f.write(f"# IfSteady, IfViscous, IfReadBackup, IfExplicit\n{L(not unsteady)}, {L(viscous)}, .true., .false.\n")
         f.write("# implicit_time_method: 1-> Implicit Runge-Kutta, 2-> Trapezoidal, 3-> Euler, 4-> Midpoint, 5-> BDF2\n5\n")
-        f.write(f"# cfl,totaltime,nstep_max,save_start_time, save_end_time\n{_fmt(cfl)}, 1.0, {nstep}, 0.0, 0.5\n")
-        f.write("# IfFixDt\n.false.\n# InLoop, InnerLoop, relTol\n1, 1, 1.0e-8\n")
+        f.write(f"# cfl,totaltime,nstep_max,save_start_time, save_end_time\n{_fmt(cfl)}, {_fmt(totaltime)}, {nstep}, 0.0, 0.5\n")
+        f.write(f"# IfFixDt\n.false.\n# InLoop, InnerLoop, relTol\n1, {inner_loop}, {_fmt(rel_tol)}\n")
         f.write("# NScreenOutput,NFileOutput,NFileBackup,NWriteMonitor\n100,100000,100000,100000\n")
         f.write(f"# rc_detector\n3.0\n# n_wbap,limit_ID: 0-> no limiter, 1-> WBAP, 2-> WBAP_Char\n10, {limit_id}\n")
         f.write("# number of monitor points\n1\n# x_monitor_point, y_monitor_point\n0,0\n")
-        f.write(f"# exit pressure ratio, A_p, f_p\n{_fmt(p_out_ratio)}, 0., 5000.0\n")
+        f.write(f"# exit pressure ratio, A_p, f_p\n{_fmt(p_out_ratio)}, {_fmt(a_p)}, {_fmt(f_p)}\n")
 
 
 def write_backup(path: str, mesh: Mesh, PA: np.ndarray) -> None:
@@ -346,6 +351,14 @@ class CaseConfig:
     h_exit: float = H_EXIT     # exit half-height (area ratio h_exit / 0.01)
     wall: int = 0              # wall BC code: 0 = no-slip (1) when viscous, else slip (6)
     x_exit: float = X_EXIT     # exit station (divergent length x_exit - 0.15)
+    # unsteady dual-time BDF2 (implicit_time_method 5) instead of steady LU-SGS:
+    # nstep physical steps of totaltime/nstep, inner_loop inner iterations
+    unsteady: bool = False
+    totaltime: float = 1.0
+    inner_loop: int = 1
+    rel_tol: float = 1.0e-8
+    a_p: float = 0.0           # exit-pressure oscillation amplitude (fraction of p_static)
+    f_p: float = 5000.0        # and frequency (Hz)
 
     @property
     def n_cells(self) -> int:
@@ -365,6 +378,15 @@ PRESETS: Dict[str, CaseConfig] = {
     "t1": CaseConfig("t1", nx=24, ny=6, seed=11),
     "t2": CaseConfig("t2", nx=24, ny=6, seed=12, nsp=4, viscous=True, combustion=True,
                      p0=5.0e6, T0=3500.0, perturb=0.02, init="isentropic"),
+    # the shipped configuration's time scheme (flow_solver_info.in: BDF2, CFL 10,
+    # dt = 5e-3 / 500000 = 1e-8 s, 10 inner iterations to 1e-3) on the tiny and
+    # the 120k-cell reacting nozzles
+    "t2u": CaseConfig("t2u", nx=24, ny=6, seed=12, nsp=4, viscous=True, combustion=True,
+                      p0=5.0e6, T0=3500.0, perturb=0.02, init="isentropic", unsteady=True, cfl=10.0,
+                      totaltime=5.0e-3, nstep=500000, inner_loop=10, rel_tol=1.0e-3),
+    "c2u": CaseConfig("c2u", nx=600, ny=100, seed=2, nsp=4, viscous=True, combustion=True,
+                      p0=5.0e6, T0=3500.0, perturb=0.02, init="isentropic", unsteady=True, cfl=10.0,
+                      totaltime=5.0e-3, nstep=500000, inner_loop=10, rel_tol=1.0e-3),
 }
 
 
@@ -451,7 +473,8 @@ def write_case(d: str, cfg: CaseConfig, mesh: Optional[Mesh] = None) -> Mesh:
                 mflux * 2.0 * H_CHAMBER, "oxidizer")
     write_inlet(os.path.join(d, "combustion", "fuel.in"), Yin, T_in, cfg.p0, 0.37, "fuel")
     pr = exit_pressure_ratio(gamma, cfg.h_exit) * cfg.p_out_factor
-    write_flow_info(d, cfg.combustion, cfg.viscous, cfg.cfl, cfg.nstep, cfg.limit_id, pr)
+    write_flow_info(d, cfg.combustion, cfg.viscous, cfg.cfl, cfg.nstep, cfg.limit_id, pr, cfg.unsteady,
+                    cfg.totaltime, cfg.inner_loop, cfg.rel_tol, cfg.a_p, cfg.f_p)
     # initial field: uniform inlet (chamber) state, or the quasi-1D isentropic
     # nozzle flow (subsonic up to the throat, supersonic after it) with the
     # velocity tilted along y/h * dh/dx; species optionally perturbed

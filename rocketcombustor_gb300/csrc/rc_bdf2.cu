@@ -1,0 +1,640 @@
+// Unsteady dual-time BDF2 stage of RocketCombustor on the device (FP64, built
+// with --fmad=false): the implicit_time_method 5 branch of the main loop,
+// BDF2_stage / BDF2_LU_SGS (Time_BDF2.f90:4-337).
+//
+// Per inner iteration, after the residual assembly that the steady path
+// shares (timestep, reconstruction, flux_sourceterm):
+//   k_bdf2_prep    every cell at once: the diagonal dd, the BDF2 right-hand
+//                  side hWA - (1+phi) vol/dt WA + fixed, the cell's system
+//                  matrix dU/dP dd - vol d omega/dP (Time_BDF2.f90:118-127),
+//                  its equilibration, LU factors and condition estimate (the
+//                  LAPACK dgesvx steps below), and the gas state the
+//                  neighbours' sweeps read;
+//   k_bdf2_sweep   one level of the forward or backward sweep: eight lanes
+//                  per cell, each face slot's flux difference of the
+//                  neighbour's increment split over two lanes, the terms added
+//                  in NeighF order, then the cell's 7x7 solve with one lane per
+//                  row (interchanges, triangular solves and the iterative
+//                  refinement of dgerfs through warp shuffles);
+//   k_bdf2_update  PA += dP, then primitve_to_conserved_variables.
+// The system matrix depends on PA, dd and vol only, so both sweeps share one
+// factorisation; the reference recomputes the same matrix in each sweep and
+// factors it the same way, so the results are the same bits.
+//
+// The per-cell solve restates reference LAPACK 3.12's dgesvx('E', 'N') as
+// called by advanced_linear_solve_lapack (la_math.f90:120-215): dgeequ +
+// dlaqge, dgetrf with partial pivoting, dgecon (dlacn2 over triangular
+// solves; only its comparison with eps matters: the reference stops there),
+// dgetrs and the refinement loop of dgerfs, in the operation order of the
+// netlib routines, which the CPU oracle restates too.
+#include "rc_chem.cuh"
+#include "rc_dev.cuh"
+
+namespace rc {
+
+namespace bdf2 {
+constexpr double EPS = 1.1102230246251565e-16;     // dlamch('E') = 2^-53
+constexpr double SFMIN = 2.2250738585072014e-308;  // dlamch('S') = 2^-1022
+constexpr double PREC = 2.220446049250313e-16;     // dlamch('P') = 2^-52
+constexpr unsigned FULL = 0xffffffffu;
+
+// gas state of a cell as a neighbour (bnb planes)
+enum : int { NB_RR = 0, NB_RRC, NB_RT, NB_RCT, NB_RCP, NB_HH, NB_EK, NB_ROU, NB_ROV, NB_ROEPP, NB_H };
+template <int NSP>
+__host__ __device__ constexpr int nbq() { return NB_H + NSP + (NSP - 1); }
+template <int NSP>
+__host__ __device__ constexpr int nb_ry() { return NB_H + NSP; }
+
+__device__ __forceinline__ double mx(double a, double b) { return (b > a) ? b : a; }
+__device__ __forceinline__ double mn(double a, double b) { return (b < a) ? b : a; }
+
+// ---- dgesvx steps on one row-major N x N matrix, a[r*N + c] = A(r, c)
+template <int N>
+__device__ __forceinline__ int dgeequ(const double* a, double* r, double* c, double& rowcnd, double& colcnd,
+                                      double& amax) {
+  const double smlnum = SFMIN, bignum = 1.0 / smlnum;
+#pragma unroll
+  for (int i = 0; i < N; ++i) r[i] = 0.0;
+#pragma unroll
+  for (int j = 0; j < N; ++j)
+#pragma unroll
+    for (int i = 0; i < N; ++i) r[i] = mx(r[i], fabs(a[i * N + j]));
+  double rcmin = bignum, rcmax = 0.0;
+#pragma unroll
+  for (int i = 0; i < N; ++i) { rcmax = mx(rcmax, r[i]); rcmin = mn(rcmin, r[i]); }
+  amax = rcmax;
+  if (rcmin == 0.0) return 1;
+#pragma unroll
+  for (int i = 0; i < N; ++i) r[i] = 1.0 / mn(mx(r[i], smlnum), bignum);
+  rowcnd = mx(rcmin, smlnum) / mn(rcmax, bignum);
+#pragma unroll
+  for (int j = 0; j < N; ++j) c[j] = 0.0;
+#pragma unroll
+  for (int j = 0; j < N; ++j)
+#pragma unroll
+    for (int i = 0; i < N; ++i) c[j] = mx(c[j], fabs(a[i * N + j]) * r[i]);
+  rcmin = bignum; rcmax = 0.0;
+#pragma unroll
+  for (int j = 0; j < N; ++j) { rcmin = mn(rcmin, c[j]); rcmax = mx(rcmax, c[j]); }
+  if (rcmin == 0.0) return 2;
+#pragma unroll
+  for (int j = 0; j < N; ++j) c[j] = 1.0 / mn(mx(c[j], smlnum), bignum);
+  colcnd = mx(rcmin, smlnum) / mn(rcmax, bignum);
+  return 0;
+}
+// dlaqge; returns bit 0 = rows scaled, bit 1 = columns scaled
+template <int N>
+__device__ __forceinline__ int dlaqge(double* a, const double* r, const double* c, double rowcnd, double colcnd,
+                                      double amax) {
+  const double thresh = 0.1, small = SFMIN / PREC, large = 1.0 / small;
+  if (rowcnd >= thresh && amax >= small && amax <= large) {
+    if (colcnd >= thresh) return 0;
+#pragma unroll
+    for (int j = 0; j < N; ++j)
+#pragma unroll
+      for (int i = 0; i < N; ++i) a[i * N + j] = c[j] * a[i * N + j];
+    return 2;
+  }
+  if (colcnd >= thresh) {
+#pragma unroll
+    for (int j = 0; j < N; ++j)
+#pragma unroll
+      for (int i = 0; i < N; ++i) a[i * N + j] = r[i] * a[i * N + j];
+    return 1;
+  }
+#pragma unroll
+  for (int j = 0; j < N; ++j)
+#pragma unroll
+    for (int i = 0; i < N; ++i) a[i * N + j] = c[j] * r[i] * a[i * N + j];
+  return 3;
+}
+// dgetrf (partial pivoting, unit L below the diagonal); returns 0 or the
+// 1-based column of the first zero pivot
+template <int N>
+__device__ __forceinline__ int dgetrf(double* a, int* ipiv) {
+  int info = 0;
+#pragma unroll
+  for (int j = 0; j < N; ++j) {
+    int jp = j;
+    double m = fabs(a[j * N + j]);
+#pragma unroll
+    for (int i = j + 1; i < N; ++i)
+      if (fabs(a[i * N + j]) > m) { jp = i; m = fabs(a[i * N + j]); }
+    ipiv[j] = jp;
+    if (a[jp * N + j] != 0.0) {
+      if (jp != j) {
+#pragma unroll
+        for (int k = 0; k < N; ++k) {
+          const double t = a[j * N + k];
+          a[j * N + k] = a[jp * N + k];
+          a[jp * N + k] = t;
+        }
+      }
+      if (j < N - 1) {
+        if (fabs(a[j * N + j]) >= SFMIN) {
+          const double rp = 1.0 / a[j * N + j];
+#pragma unroll
+          for (int i = j + 1; i < N; ++i) a[i * N + j] = rp * a[i * N + j];
+        } else {
+#pragma unroll
+          for (int i = j + 1; i < N; ++i) a[i * N + j] = a[i * N + j] / a[j * N + j];
+        }
+      }
+    } else if (info == 0) {
+      info = j + 1;
+    }
+#pragma unroll
+    for (int jj = j + 1; jj < N; ++jj) {
+      if (a[j * N + jj] != 0.0) {
+        const double temp = -1.0 * a[j * N + jj];
+#pragma unroll
+        for (int i = j + 1; i < N; ++i) a[i * N + jj] = a[i * N + jj] + a[i * N + j] * temp;
+      }
+    }
+  }
+  return info;
+}
+// the triangular solves of dgecon: kase 1 inv(L) then inv(U), kase 2 inv(U^T) then inv(L^T)
+template <int N>
+__device__ __forceinline__ void trs_kase(const double* af, int kase, double* x) {
+  if (kase == 1) {
+#pragma unroll
+    for (int j = 0; j < N; ++j)
+      if (x[j] != 0.0) {
+        const double temp = x[j];
+#pragma unroll
+        for (int i = j + 1; i < N; ++i) x[i] = x[i] - temp * af[i * N + j];
+      }
+#pragma unroll
+    for (int j = N - 1; j >= 0; --j)
+      if (x[j] != 0.0) {
+        x[j] = x[j] / af[j * N + j];
+        const double temp = x[j];
+#pragma unroll
+        for (int i = j - 1; i >= 0; --i) x[i] = x[i] - temp * af[i * N + j];
+      }
+  } else {
+#pragma unroll
+    for (int j = 0; j < N; ++j) {
+      double temp = x[j];
+#pragma unroll
+      for (int i = 0; i < j; ++i) temp = temp - af[i * N + j] * x[i];
+      x[j] = temp / af[j * N + j];
+    }
+#pragma unroll
+    for (int j = N - 1; j >= 0; --j) {
+      double temp = x[j];
+#pragma unroll
+      for (int i = N - 1; i > j; --i) temp = temp - af[i * N + j] * x[i];
+      x[j] = temp;
+    }
+  }
+}
+template <int N>
+__device__ __forceinline__ double dasum(const double* x) {
+  double t = 0.0;
+#pragma unroll
+  for (int i = 0; i < N; ++i) t = t + fabs(x[i]);
+  return t;
+}
+template <int N>
+__device__ __forceinline__ int idamax(const double* x) {
+  int k = 0;
+  double m = fabs(x[0]);
+#pragma unroll
+  for (int i = 1; i < N; ++i)
+    if (fabs(x[i]) > m) { k = i; m = fabs(x[i]); }
+  return k;
+}
+// dgecon('1') with dlacn2 (at most 5 iterations) unrolled
+template <int N>
+__device__ double dgecon(const double* af, double anorm) {
+  if (anorm == 0.0) return 0.0;
+  if (isnan(anorm)) return anorm;
+  double x[N], est, estold;
+  int isgn[N];
+#pragma unroll
+  for (int i = 0; i < N; ++i) x[i] = 1.0 / (double)N;
+  trs_kase<N>(af, 1, x);
+  if (N == 1) {
+    est = fabs(x[0]);
+  } else {
+    est = dasum<N>(x);
+#pragma unroll
+    for (int i = 0; i < N; ++i) { x[i] = (x[i] >= 0.0) ? 1.0 : -1.0; isgn[i] = x[i] >= 0.0 ? 1 : -1; }
+    trs_kase<N>(af, 2, x);
+    int j = idamax<N>(x), iter = 2;
+    for (int guard = 0; guard < 8; ++guard) {
+#pragma unroll
+      for (int i = 0; i < N; ++i) x[i] = (i == j) ? 1.0 : 0.0;
+      trs_kase<N>(af, 1, x);
+      estold = est;
+      est = dasum<N>(x);
+      bool same = true;
+#pragma unroll
+      for (int i = 0; i < N; ++i)
+        if ((x[i] >= 0.0 ? 1 : -1) != isgn[i]) same = false;
+      if (same || est <= estold) break;
+#pragma unroll
+      for (int i = 0; i < N; ++i) { x[i] = (x[i] >= 0.0) ? 1.0 : -1.0; isgn[i] = x[i] >= 0.0 ? 1 : -1; }
+      trs_kase<N>(af, 2, x);
+      const int jlast = j;
+      j = idamax<N>(x);
+      double xl = 0.0;
+#pragma unroll
+      for (int i = 0; i < N; ++i)
+        if (i == jlast) xl = x[i];
+      double xj = 0.0;
+#pragma unroll
+      for (int i = 0; i < N; ++i)
+        if (i == j) xj = x[i];
+      if (xl != fabs(xj) && iter < 5) { iter = iter + 1; continue; }
+      break;
+    }
+    double altsgn = 1.0;
+#pragma unroll
+    for (int i = 0; i < N; ++i) {
+      x[i] = altsgn * (1.0 + (double)i / (double)(N - 1));
+      altsgn = -altsgn;
+    }
+    trs_kase<N>(af, 1, x);
+    const double temp = 2.0 * (dasum<N>(x) / (double)(3 * N));
+    if (temp > est) est = temp;
+  }
+  if (est != 0.0) return (1.0 / est) / anorm;
+  return 0.0;
+}
+
+// ---- the per-row solve of one cell's system by its eight lanes
+// x: this row's right-hand side (already row-scaled); returns A^-1 x for this
+// row (dgetrs('N')): the composed interchanges, then the column-oriented unit
+// lower and upper solves of dtrsm, skipping zero entries as dtrsm does.
+template <int N>
+__device__ __forceinline__ double getrs_rows(double x, int src, const double* lu, const double* ukk, int r,
+                                             int base) {
+  x = __shfl_sync(FULL, x, base + src);
+#pragma unroll
+  for (int k = 0; k < N - 1; ++k) {
+    const double xk = __shfl_sync(FULL, x, base + k);
+    if (r > k && r < N && xk != 0.0) x = x - xk * lu[k];
+  }
+#pragma unroll
+  for (int k = N - 1; k >= 0; --k) {
+    double xk = __shfl_sync(FULL, x, base + k);
+    if (xk != 0.0) {
+      xk = xk / ukk[k];
+      if (r == k) x = xk;
+      else if (r < k) x = x - xk * lu[k];
+    }
+  }
+  return x;
+}
+}  // namespace bdf2
+
+// fixed = vol/dt ((1+2 phi) WP - phi WP2) (Time_BDF2.f90:100-105)
+template <int NSP>
+__global__ void __launch_bounds__(128) k_bdf2_fixed(const Dev d) {
+  constexpr int V = 3 + NSP;
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= d.NE) return;
+  const int NE = d.NE;
+  const double dt = d.bpar[0], phi = d.bpar[1];
+  const double vd = d.vol[i] / dt;
+#pragma unroll
+  for (int k = 0; k < V; ++k)
+    d.bfix[k * NE + i] = vd * ((1 + 2 * phi) * d.WP[k * NE + i] - phi * d.WP2[k * NE + i]);
+}
+
+// Everything of BDF2_LU_SGS that the sweeps do not change, one thread per cell.
+template <int NSP>
+__global__ void __launch_bounds__(128) k_bdf2_prep(const Dev d, const ThermoDev<NSP> th) {
+  using namespace bdf2;
+  constexpr int V = 3 + NSP, RW = 2 * V + 2;
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= d.NE) return;
+  const int NE = d.NE;
+  const double dt = d.bpar[0], phi = d.bpar[1], vol = d.vol[i];
+  unsigned err = 0;
+  // diagonal (Time_BDF2.f90:107-114) and right-hand side (:116-122)
+  double s = 0.0;
+  const int nf = d.nface[i];
+  for (int q = 0; q < nf; ++q) s = s + 0.5 * d.alpaF[d.cface[q * NE + i]];
+  const double ddi = s + vol * (1. / d.step[i] + (1 + phi) / dt);
+#pragma unroll
+  for (int k = 0; k < V; ++k)
+    d.hWA[k * NE + i] = d.hWA[k * NE + i] - (1 + phi) * vol / dt * d.WA[k * NE + i] + d.bfix[k * NE + i];
+  // system matrix (:124-132)
+  double pri[V];
+#pragma unroll
+  for (int k = 0; k < V; ++k) pri[k] = d.PA[k * NE + i];
+  double a[V * V], af[V * V];
+  con_to_pri_jaco<NSP>(th, pri, a, err);
+#pragma unroll
+  for (int k = 0; k < V * V; ++k) a[k] = a[k] * ddi;
+  if (NSP > 1) {
+    double dw[(NSP > 1 ? NSP - 1 : 1) * V];
+    dwdp<NSP>(th, pri, dw, err);
+#pragma unroll
+    for (int j = 0; j < NSP - 1; ++j)
+#pragma unroll
+      for (int c = 0; c < V; ++c) a[(4 + j) * V + c] = a[(4 + j) * V + c] - vol * dw[j * V + c];
+  }
+  // dgesvx('E'): equilibrate, factor, condition estimate
+  double rs[V], cs[V], rowcnd = 0, colcnd = 0, amax = 0;
+  int equ = 0;
+  if (dgeequ<V>(a, rs, cs, rowcnd, colcnd, amax) == 0) equ = dlaqge<V>(a, rs, cs, rowcnd, colcnd, amax);
+#pragma unroll
+  for (int k = 0; k < V * V; ++k) af[k] = a[k];
+  int ipiv[V];
+  const int info = dgetrf<V>(af, ipiv);
+  if (info > 0) {
+    err |= ERR_LINSOLVE;
+  } else {
+    double anorm = 0.0;  // dlange('1')
+#pragma unroll
+    for (int j = 0; j < V; ++j) {
+      double sum = 0.0;
+#pragma unroll
+      for (int r = 0; r < V; ++r) sum = sum + fabs(a[r * V + j]);
+      if (anorm < sum || isnan(sum)) anorm = sum;
+    }
+    if (dgecon<V>(af, anorm) < EPS) err |= ERR_LINSOLVE;
+  }
+  int src[V];
+#pragma unroll
+  for (int k = 0; k < V; ++k) src[k] = k;
+#pragma unroll
+  for (int k = 0; k < V; ++k) {
+    const int p = ipiv[k], t = src[k];
+    src[k] = src[p];
+    src[p] = t;
+  }
+  double* m = d.bmat + (size_t)i * V * RW;
+#pragma unroll
+  for (int r = 0; r < V; ++r) {
+#pragma unroll
+    for (int c = 0; c < V; ++c) { m[r * RW + c] = a[r * V + c]; m[r * RW + V + c] = af[r * V + c]; }
+    m[r * RW + 2 * V] = rs[r];
+    m[r * RW + 2 * V + 1] = cs[r];
+    d.bperm[i * 8 + r] = src[r];
+  }
+  d.bperm[i * 8 + 7] = equ;
+  // this cell's gas state for its neighbours' sweeps (Time_BDF2.f90:145-166)
+  double yy[NSP], entha[NSP], Cp, gama, Rcpcv;
+  double sy = 0.0;
+#pragma unroll
+  for (int k = 0; k < NSP - 1; ++k) { yy[k] = pri[4 + k]; sy = sy + yy[k]; }
+  yy[NSP - 1] = 1. - sy;
+  const double pp = pri[0], uu = pri[1], vv = pri[2], tt = pri[3];
+  gas<NSP>(th, yy, tt, Cp, gama, Rcpcv, err);
+  enthalpy<NSP>(th, tt, entha, err);
+  double hh = 0.0;
+#pragma unroll
+  for (int k = 0; k < NSP; ++k) hh = hh + yy[k] * entha[k];
+  const double rct = Rcpcv * tt, rr = pp / rct, ek = 0.5 * (uu * uu + vv * vv);
+  double* nb = d.bnb;
+  nb[NB_RR * NE + i] = rr;
+  nb[NB_RRC * NE + i] = rr * Rcpcv;
+  nb[NB_RT * NE + i] = rr * tt;
+  nb[NB_RCT * NE + i] = rct;
+  nb[NB_RCP * NE + i] = rr * Cp;
+  nb[NB_HH * NE + i] = hh;
+  nb[NB_EK * NE + i] = ek;
+  nb[NB_ROU * NE + i] = rr * uu;
+  nb[NB_ROV * NE + i] = rr * vv;
+  nb[NB_ROEPP * NE + i] = (rr * (hh + ek) - pp) + pp;
+#pragma unroll
+  for (int k = 0; k < NSP; ++k) nb[(NB_H + k) * NE + i] = entha[k];
+#pragma unroll
+  for (int k = 0; k < NSP - 1; ++k) nb[(nb_ry<NSP>() + k) * NE + i] = rr * yy[k];
+  flag(d, err);
+}
+
+// One level of the forward (FWD) or backward sweep, cells t0..t1-1 of the
+// level order; eight lanes per cell, four cells per warp (one warp per block).
+template <int NSP, bool FWD>
+__global__ void __launch_bounds__(32) k_bdf2_sweep(const Dev d, const ThermoDev<NSP> th, int t0, int t1) {
+  using namespace bdf2;
+  constexpr int V = 3 + NSP, RW = 2 * V + 2, DIR = FWD ? 0 : 1;
+  static_assert(V <= 7, "one lane per row and the flags in slot 7");
+  pdl_launch_dependents();
+  const int lane = threadIdx.x & 31, cell = lane >> 3, r = lane & 7, base = cell * 8;
+  const int q = r & 3;
+  const bool lo = r < 4;  // lanes 0-3: flux rows 1-3; lanes 4-7: rows 4.. (energy, species)
+  const int NE = d.NE, NF = d.NF;
+  const int t = t0 + blockIdx.x * 4 + cell;
+  const bool valid = t < t1;
+  const int i = valid ? d.swi[DIR][t] : 0;
+  // --- what the sweep does not change: the face of slot q and its neighbour's gas state
+  const int j = valid ? d.swj[DIR][q * NE + t] : -1;
+  const bool act = j >= 0;
+  double dx = 0, dy = 0, aF = 0, uu = 0, vv = 0, rr = 0, rrc = 0, rt = 0, rct = 0, unormal = 0;
+  double rou = 0, rov = 0, rcp = 0, hh = 0, ek = 0, roepp = 0, ent[NSP], yy[NSP], ry[NSP];
+#pragma unroll
+  for (int k = 0; k < NSP; ++k) { ent[k] = 0.0; yy[k] = 0.0; ry[k] = 0.0; }
+  if (act) {
+    const int fs = d.swf[DIR][q * NE + t], f = fs >= 0 ? fs : ~fs;
+    dx = d.fvec[f];
+    dy = d.fvec[NF + f];
+    if (fs < 0) { dx = -dx; dy = -dy; }
+    aF = d.alpaF[f];
+    uu = d.PA[1 * NE + j];
+    vv = d.PA[2 * NE + j];
+    const double* nb = d.bnb;
+    rr = nb[NB_RR * NE + j]; rrc = nb[NB_RRC * NE + j]; rt = nb[NB_RT * NE + j]; rct = nb[NB_RCT * NE + j];
+    unormal = uu * dx + vv * dy;
+    if (lo) {
+      rou = nb[NB_ROU * NE + j];
+      rov = nb[NB_ROV * NE + j];
+    } else {
+      rcp = nb[NB_RCP * NE + j]; hh = nb[NB_HH * NE + j]; ek = nb[NB_EK * NE + j]; roepp = nb[NB_ROEPP * NE + j];
+#pragma unroll
+      for (int k = 0; k < NSP; ++k) ent[k] = nb[(NB_H + k) * NE + j];
+#pragma unroll
+      for (int k = 0; k < NSP - 1; ++k) {
+        yy[k] = d.PA[(4 + k) * NE + j];
+        ry[k] = nb[(nb_ry<NSP>() + k) * NE + j];
+      }
+    }
+  }
+  // --- this lane's row of the cell's system
+  double arow[V], lrow[V], ukk[V], rsc = 1.0, csc = 1.0;
+  int src = 0, equ = 0;
+#pragma unroll
+  for (int k = 0; k < V; ++k) { arow[k] = 0.0; lrow[k] = 0.0; ukk[k] = 1.0; }
+  if (valid) {
+    const double* m = d.bmat + (size_t)i * V * RW;
+    if (r < V) {
+#pragma unroll
+      for (int k = 0; k < V; ++k) { arow[k] = m[r * RW + k]; lrow[k] = m[r * RW + V + k]; }
+      rsc = m[r * RW + 2 * V];
+      csc = m[r * RW + 2 * V + 1];
+      src = d.bperm[i * 8 + r];
+    }
+#pragma unroll
+    for (int k = 0; k < V; ++k) ukk[k] = m[k * RW + V + k];
+    equ = d.bperm[i * 8 + 7];
+  }
+  double hown = 0.0;
+  if (FWD && valid && r < V) hown = d.hWA[r * NE + i];  // written by k_bdf2_prep, complete before this grid
+  pdl_wait();
+  if (!FWD && valid && r < V) hown = d.hWA[r * NE + i];
+  // --- flux difference of the neighbour's increment (Time_BDF2.f90:168-197)
+  double c[V];
+#pragma unroll
+  for (int k = 0; k < V; ++k) c[k] = 0.0;
+  if (act) {
+    const double dpp = d.hWA[0 * NE + j], duu = d.hWA[1 * NE + j], dvv = d.hWA[2 * NE + j],
+                 dtt = d.hWA[3 * NE + j];
+    double dyy[NSP], s = 0.0;
+#pragma unroll
+    for (int k = 0; k < NSP - 1; ++k) { dyy[k] = d.hWA[(4 + k) * NE + j]; s = s + dyy[k]; }
+    dyy[NSP - 1] = -s;
+    double s1 = 0.0;
+#pragma unroll
+    for (int k = 0; k < NSP; ++k) s1 = s1 + th.R[k] * dyy[k];
+    const double drr = (dpp - rrc * dtt - rt * s1) / rct;
+    const double dunormal = duu * dx + dvv * dy;
+    if (lo) {
+      const double dru = rr * duu + uu * drr;
+      const double drv = rr * dvv + vv * drr;
+      c[0] = 0.5 * (-aF * drr + dru * dx + drv * dy);
+      c[1] = 0.5 * (-aF * dru + dru * unormal + rou * dunormal + dpp * dx);
+      c[2] = 0.5 * (-aF * drv + drv * unormal + rov * dunormal + dpp * dy);
+    } else {
+      double s2 = 0.0;
+#pragma unroll
+      for (int k = 0; k < NSP; ++k) s2 = s2 + ent[k] * dyy[k];
+      const double dre = rcp * dtt + rr * s2 + hh * drr + rr * (uu * duu + vv * dvv) + ek * drr - dpp;
+      c[3] = 0.5 * (-aF * dre + dunormal * roepp + unormal * (dre + dpp));
+#pragma unroll
+      for (int k = 0; k < NSP - 1; ++k) {
+        const double dry = rr * dyy[k] + yy[k] * drr;
+        c[4 + k] = 0.5 * (-aF * dry + dry * unormal + ry[k] * dunormal);
+      }
+    }
+  }
+  __shared__ double wsm[4 * V * 4];
+  double* w = wsm + cell * V * 4;  // [row][slot]
+  if (lo) {
+#pragma unroll
+    for (int k = 0; k < 3; ++k) w[k * 4 + q] = c[k];
+  } else {
+#pragma unroll
+    for (int k = 3; k < V; ++k) w[k * 4 + q] = c[k];
+  }
+  __syncwarp();
+  double dflux = 0.0;
+  if (r < V) {
+#pragma unroll
+    for (int sl = 0; sl < 4; ++sl) dflux = dflux + w[r * 4 + sl];
+  }
+  // --- the cell's system, one row per lane (dgesvx after the factorisation)
+  const bool rowequ = equ & 1, colequ = equ & 2;
+  double b = FWD ? hown - dflux : dflux;
+  if (rowequ) b = rsc * b;
+  if (!(valid && r < V)) b = 0.0;
+  double x = getrs_rows<V>(b, src, lrow, ukk, r, base);
+  // dgerfs refinement: residual, componentwise backward error, correction
+  const double safe1 = (V + 1) * SFMIN, safe2 = safe1 / EPS;
+  double lstres = 3.0;
+  int count = 1;
+  bool go = valid;
+  for (int it = 0; it < 6; ++it) {
+    double xs[V];
+#pragma unroll
+    for (int k = 0; k < V; ++k) xs[k] = __shfl_sync(FULL, x, base + k);
+    double y = b;
+#pragma unroll
+    for (int k = 0; k < V; ++k) y = y + (-1.0 * xs[k]) * arow[k];
+    double wk = fabs(b);
+#pragma unroll
+    for (int k = 0; k < V; ++k) wk = wk + fabs(arow[k]) * fabs(xs[k]);
+    double v = 0.0;
+    if (r < V) v = (wk > safe2) ? fabs(y) / wk : (fabs(y) + safe1) / (wk + safe1);
+    v = mx(v, __shfl_xor_sync(FULL, v, 1));
+    v = mx(v, __shfl_xor_sync(FULL, v, 2));
+    v = mx(v, __shfl_xor_sync(FULL, v, 4));
+    const bool cont = go && v > EPS && 2.0 * v <= lstres && count <= 5;
+    if (!__any_sync(FULL, cont)) break;
+    const double corr = getrs_rows<V>(y, src, lrow, ukk, r, base);
+    if (cont) {
+      x = x + corr;
+      lstres = v;
+      count = count + 1;
+    }
+    go = cont;
+  }
+  if (colequ) x = csc * x;
+  if (valid && r < V) d.hWA[r * NE + i] = FWD ? x : hown - x;
+}
+
+// PA += dP, then primitve_to_conserved_variables (update_flow_variables.f90:50-84)
+template <int NSP>
+__global__ void __launch_bounds__(128) k_bdf2_update(const Dev d, const ThermoDev<NSP> th) {
+  constexpr int V = 3 + NSP;
+  pdl_wait();
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= d.NE) return;
+  const int NE = d.NE;
+  unsigned err = 0;
+  double P[V];
+#pragma unroll
+  for (int k = 0; k < V; ++k) {
+    P[k] = d.PA[k * NE + i] + d.hWA[k * NE + i];
+    d.PA[k * NE + i] = P[k];
+  }
+  double yy[NSP], entha[NSP], Cp, gama, Rcpcv, s = 0.0;
+#pragma unroll
+  for (int k = 0; k < NSP - 1; ++k) { yy[k] = P[4 + k]; s = s + yy[k]; }
+  yy[NSP - 1] = 1.0 - s;
+  const double pp = P[0], uu = P[1], vv = P[2], tt = P[3];
+  gas<NSP>(th, yy, tt, Cp, gama, Rcpcv, err);
+  const double rr = pp / (Rcpcv * tt);
+  enthalpy<NSP>(th, tt, entha, err);
+  double hh = 0.0;
+#pragma unroll
+  for (int k = 0; k < NSP; ++k) hh = hh + yy[k] * entha[k];
+  d.WA[0 * NE + i] = rr;
+  d.WA[1 * NE + i] = rr * uu;
+  d.WA[2 * NE + i] = rr * vv;
+  d.WA[3 * NE + i] = rr * (hh + 0.5 * (uu * uu + vv * vv)) - pp;
+#pragma unroll
+  for (int k = 0; k < NSP - 1; ++k) d.WA[(4 + k) * NE + i] = rr * yy[k];
+  if (i == 0 && isnan(rr)) err |= ERR_NAN;
+  flag(d, err);
+}
+
+inline unsigned nblk(long n, int t) { return (unsigned)((n + t - 1) / t); }
+
+template <int NSP>
+void bdf2_fixed(const Dev& d, int bs, cudaStream_t s) {
+  k_bdf2_fixed<NSP><<<nblk(d.NE, bs), bs, 0, s>>>(d);
+}
+template <int NSP>
+void bdf2_prep(const Dev& d, const void* th, int bs, cudaStream_t s) {
+  k_bdf2_prep<NSP><<<nblk(d.NE, bs), bs, 0, s>>>(d, *static_cast<const ThermoDev<NSP>*>(th));
+}
+template <int NSP>
+void bdf2_sweep(const Dev& d, const void* th, bool fwd, int t0, int t1, cudaStream_t s) {
+  const auto& T = *static_cast<const ThermoDev<NSP>*>(th);
+  if (fwd) launch_pdl(k_bdf2_sweep<NSP, true>, nblk(t1 - t0, 4), 32, s, d, T, t0, t1);
+  else launch_pdl(k_bdf2_sweep<NSP, false>, nblk(t1 - t0, 4), 32, s, d, T, t0, t1);
+}
+template <int NSP>
+void bdf2_update(const Dev& d, const void* th, int bs, cudaStream_t s) {
+  launch_pdl(k_bdf2_update<NSP>, nblk(d.NE, bs), bs, s, d, *static_cast<const ThermoDev<NSP>*>(th));
+}
+template <int NSP>
+int bdf2_nbq() { return bdf2::nbq<NSP>(); }
+
+#define RC_BDF2_INST(N)                                                             \
+  template void bdf2_fixed<N>(const Dev&, int, cudaStream_t);                       \
+  template void bdf2_prep<N>(const Dev&, const void*, int, cudaStream_t);           \
+  template void bdf2_sweep<N>(const Dev&, const void*, bool, int, int, cudaStream_t); \
+  template void bdf2_update<N>(const Dev&, const void*, int, cudaStream_t);         \
+  template int bdf2_nbq<N>();
+RC_BDF2_INST(1)
+RC_BDF2_INST(4)
+
+}  // namespace rc

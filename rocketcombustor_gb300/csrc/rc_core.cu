@@ -892,6 +892,11 @@ void chem_batch(const void*, const double*, const double*, int, double*, int*, d
                 cudaStream_t);
 template <int NSP>
 void chem_list(const Dev&, const void*, double, int, int*, const int*, const unsigned*, unsigned*, cudaStream_t);
+template <int NSP> void bdf2_fixed(const Dev&, int, cudaStream_t);
+template <int NSP> void bdf2_prep(const Dev&, const void*, int, cudaStream_t);
+template <int NSP> void bdf2_sweep(const Dev&, const void*, bool, int, int, cudaStream_t);
+template <int NSP> void bdf2_update(const Dev&, const void*, int, cudaStream_t);
+template <int NSP> int bdf2_nbq();
 cudaError_t surrogate_source(const Dev&, const void*, const rc_mlp*, float, int*, unsigned*, unsigned*,
                              cudaStream_t);
 cudaError_t surrogate_prepare();
@@ -945,6 +950,12 @@ struct rc_ctx {
   unsigned* sur_counts = nullptr;     // [2]: fallback cells, surrogate cells
   cudaStream_t stream2 = nullptr;     // side stream: the integrated source runs beside the face fluxes
   cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
+
+  // unsteady dual-time BDF2 (allocated by the first BDF2 call)
+  bool bdf2_ready = false;
+  double* bpar_dev = nullptr;              // {dt, phi}
+  cudaGraphExec_t bdf2_graph = nullptr;    // one inner iteration and its norms
+  long long bdf2_graph_kernels = 0;
 
   double* norm_part = nullptr;
   double* norm_out = nullptr;
@@ -1072,20 +1083,6 @@ void q_persistent(rc_ctx* c) {
                      (int)c->fwd_off.size() - 1, (const int*)c->bwd_off_dev, (int)c->bwd_off.size() - 1,
                      c->lvl_count);
   c->launches++;
-}
-// launch as a programmatic dependent of the previous kernel of the stream
-template <class... Args, class... Act>
-void launch_pdl(void (*kernel)(Args...), unsigned grid, unsigned block, cudaStream_t s, Act&&... args) {
-  cudaLaunchConfig_t cfg = {};
-  cfg.gridDim = dim3(grid);
-  cfg.blockDim = dim3(block);
-  cfg.stream = s;
-  cudaLaunchAttribute attr[1];
-  attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
-  attr[0].val.programmaticStreamSerializationAllowed = 1;
-  cfg.attrs = attr;
-  cfg.numAttrs = 1;
-  cudaLaunchKernelEx(&cfg, kernel, std::forward<Act>(args)...);
 }
 template <int NSP>
 void q_sweeps(rc_ctx* c, int gather) {
@@ -1232,6 +1229,55 @@ void q_stage(rc_ctx* c) {
   }
   q_flux_mode<NSP>(c);
   q_sweeps32<NSP>(c);
+}
+
+// BDF2_LU_SGS after the residual assembly: per-cell set-up, the level-
+// scheduled sweeps, the primitive update.
+template <int NSP>
+void q_bdf2_lusgs(rc_ctx* c) {
+  bdf2_prep<NSP>(c->d, c->thermo.data(), c->d.bs, c->stream);
+  c->launches++;
+  for (size_t l = 0; l + 1 < c->fwd_off.size(); ++l) {
+    bdf2_sweep<NSP>(c->d, c->thermo.data(), true, c->fwd_off[l], c->fwd_off[l + 1], c->stream);
+    c->launches++;
+  }
+  for (size_t l = 0; l + 1 < c->bwd_off.size(); ++l) {
+    bdf2_sweep<NSP>(c->d, c->thermo.data(), false, c->bwd_off[l], c->bwd_off[l + 1], c->stream);
+    c->launches++;
+  }
+  bdf2_update<NSP>(c->d, c->thermo.data(), c->d.bs, c->stream);
+  c->launches++;
+}
+// Norms of every case into norm_out ([case][V+1]), enqueued.
+void q_norms(rc_ctx* c) {
+  const int nc = c->ncase;
+  k_norm_partial<<<dim3(NRM_BLOCKS, nc), NRM_THREADS, 0, c->stream>>>(c->d.hWA, c->d.WA, c->d.vol, c->NE, c->V,
+                                                                       nc > 1 ? c->case_off_dev : nullptr,
+                                                                       c->norm_part);
+  k_norm_final<<<nc, 32, 0, c->stream>>>(c->norm_part, c->V, c->case_vol_dev, c->norm_out);
+  c->launches += 2;
+}
+// One inner iteration of BDF2_stage (Time_BDF2.f90:25-46) and the norms of
+// inner_iteration_residual.
+template <int NSP>
+void q_bdf2_inner(rc_ctx* c) {
+  q_timestep_face<NSP>(c);
+  q_cell<NSP>(c, 1, 1);
+  q_chem_fork<NSP>(c);
+  q_face_flux<NSP>(c);
+  q_chem_join(c);
+  q_gather<NSP>(c);
+  q_bdf2_lusgs<NSP>(c);
+  q_norms(c);
+}
+// The residual assembly after the last inner iteration (Time_BDF2.f90:51-52).
+template <int NSP>
+void q_bdf2_final(rc_ctx* c) {
+  q_cell<NSP>(c, 0, 1);
+  q_chem_fork<NSP>(c);
+  q_face_flux<NSP>(c);
+  q_chem_join(c);
+  q_gather<NSP>(c);
 }
 
 #define RC_DISPATCH(c, fn, ...)                  \
@@ -1743,6 +1789,7 @@ int rc_finalize(rc_ctx* c) {
   if (!c) return RC_OK;
   for (auto& gx : c->graphs)
     if (gx) cudaGraphExecDestroy(gx);
+  if (c->bdf2_graph) cudaGraphExecDestroy(c->bdf2_graph);
   for (void* p : c->allocs) cudaFree(p);
   if (c->own_stream && c->stream) cudaStreamDestroy(c->stream);
   if (c->stream2) cudaStreamDestroy(c->stream2);
@@ -1793,6 +1840,7 @@ int rc_get_state(rc_ctx* c, double* PA, double* WA) {
   return st ? st : latch(c);
 }
 
+static int bdf2_setup(rc_ctx* c);
 static int array_desc(rc_ctx* c, const std::string& s, double** ptr, int* N, int* V, int* grad) {
   *grad = 0;
   if (s == "PA") { *ptr = c->d.PA; *N = c->NE; *V = c->V; }
@@ -1802,7 +1850,10 @@ static int array_desc(rc_ctx* c, const std::string& s, double** ptr, int* N, int
   else if (s == "GPA") { *ptr = c->d.GPA; *N = c->NG; *V = c->V; }
   else if (s == "alpaF") { *ptr = c->d.alpaF; *N = c->NF; *V = 1; }
   else if (s == "step") { *ptr = c->d.step; *N = c->NE; *V = 1; }
-  else return RC_ERR_ARG;
+  else if (s == "WP" || s == "WP2") {
+    if (int st = bdf2_setup(c)) return st;
+    *ptr = s == "WP" ? c->d.WP : c->d.WP2; *N = c->NE; *V = c->V;
+  } else return RC_ERR_ARG;
   return RC_OK;
 }
 int rc_get_array(rc_ctx* c, const char* name, double* out) {
@@ -1858,6 +1909,7 @@ static void drop_graphs(rc_ctx* c) {
   for (int k = 0; k < 3; ++k)
     if (c->graphs[k]) { cudaGraphExecDestroy(c->graphs[k]); c->graphs[k] = nullptr; }
   c->graph = nullptr;
+  if (c->bdf2_graph) { cudaGraphExecDestroy(c->bdf2_graph); c->bdf2_graph = nullptr; }
 }
 int rc_autotune(rc_ctx* c, int iters, char* report, int report_len) {
   if (!c || iters < 1) return RC_ERR_ARG;
@@ -2053,11 +2105,7 @@ int rc_sync(rc_ctx* c) {
 // Norms of every case into norm_out ([case][V+1]); synchronises.
 static int norms(rc_ctx* c, std::vector<double>& h) {
   const int nc = c->ncase;
-  k_norm_partial<<<dim3(NRM_BLOCKS, nc), NRM_THREADS, 0, c->stream>>>(c->d.hWA, c->d.WA, c->d.vol, c->NE, c->V,
-                                                                       nc > 1 ? c->case_off_dev : nullptr,
-                                                                       c->norm_part);
-  k_norm_final<<<nc, 32, 0, c->stream>>>(c->norm_part, c->V, c->case_vol_dev, c->norm_out);
-  c->launches += 2;
+  q_norms(c);
   h.resize((size_t)nc * (c->V + 1));
   RC_CU(cudaMemcpyAsync(h.data(), c->norm_out, sizeof(double) * h.size(), cudaMemcpyDeviceToHost, c->stream));
   RC_CU(cudaStreamSynchronize(c->stream));
@@ -2092,6 +2140,118 @@ int rc_batch_info(rc_ctx* c, int* ncase, int* cell_offsets) {
   if (cell_offsets)
     for (int b = 0; b <= c->ncase; ++b) cell_offsets[b] = c->case_off[b];
   return RC_OK;
+}
+
+// ------------------------------------------- unsteady dual-time BDF2 -----
+static int bdf2_setup(rc_ctx* c) {
+  if (c->ncase != 1) {
+    c->err = "the BDF2 stage takes one case per context";
+    return RC_ERR_ARG;
+  }
+  if (c->mode != RC_PREC_FP64 || c->chem != RC_CHEM_EXPLICIT) {
+    c->err = "the BDF2 stage runs the FP64 path with the explicit chemical source";
+    return RC_ERR_ARG;
+  }
+  if (c->bdf2_ready) return RC_OK;
+  const size_t NE = (size_t)c->NE, V = (size_t)c->V;
+  int nbq = 0;
+  RC_DISPATCH(c, nbq = bdf2_nbq);
+  int st = dev_zeros(c, V * NE, &c->d.WP);
+  st |= dev_zeros(c, V * NE, &c->d.WP2);
+  st |= dev_zeros(c, V * NE, &c->d.bfix);
+  st |= dev_zeros(c, NE * V * (2 * V + 2), &c->d.bmat);
+  st |= dev_zeros(c, 8 * NE, &c->d.bperm);
+  st |= dev_zeros(c, (size_t)nbq * NE, &c->d.bnb);
+  st |= dev_zeros(c, (size_t)2, &c->bpar_dev);
+  if (st) return st;
+  c->d.bpar = c->bpar_dev;
+  c->bdf2_ready = true;
+  drop_graphs(c);  // the captured kernels hold the old Dev
+  return RC_OK;
+}
+static int bdf2_params(rc_ctx* c, double dt, double phi) {
+  const double par[2] = {dt, phi};
+  RC_CU(cudaMemcpyAsync(c->bpar_dev, par, sizeof(par), cudaMemcpyHostToDevice, c->stream));
+  return RC_OK;
+}
+int rc_set_p_out(rc_ctx* c, const double* p_out) {
+  if (!c || !p_out) return RC_ERR_ARG;
+  for (int k = 0; k < c->ncase; ++k) {
+    const float p32 = (float)p_out[k];
+    RC_CU(cudaMemcpyAsync(const_cast<double*>(c->d.bctab) + (size_t)k * BCS + BC_POUT, &p_out[k], sizeof(double),
+                          cudaMemcpyHostToDevice, c->stream));
+    RC_CU(cudaMemcpyAsync(const_cast<float*>(c->d.bctab32) + (size_t)k * BCS + BC_POUT, &p32, sizeof(float),
+                          cudaMemcpyHostToDevice, c->stream));
+  }
+  return RC_OK;
+}
+int rc_bdf2_lusgs(rc_ctx* c, int inner_rk, double phi, double dt) {
+  if (!c || inner_rk < 1 || !(dt > 0.0)) return RC_ERR_ARG;
+  RC_NSP_OK(c);
+  if (int st = bdf2_setup(c)) return st;
+  if (int st = bdf2_params(c, dt, phi)) return st;
+  if (inner_rk == 1) {
+    RC_DISPATCH(c, bdf2_fixed, c->d, c->d.bs, c->stream);
+    c->launches++;
+  }
+  RC_DISPATCH(c, q_bdf2_lusgs, c);
+  return check_launch(c, "rc_bdf2_lusgs");
+}
+int rc_bdf2_stage(rc_ctx* c, int istep, double dt, int inner_loop, double rel_tol, int* inner_done) {
+  if (!c || istep < 1 || inner_loop < 1 || !(dt > 0.0)) return RC_ERR_ARG;
+  RC_NSP_OK(c);
+  if (int st = bdf2_setup(c)) return st;
+  const size_t bytes = sizeof(double) * (size_t)c->V * c->NE;
+  double phi;
+  if (istep == 1) {
+    RC_CU(cudaMemcpyAsync(c->d.WP, c->d.WA, bytes, cudaMemcpyDeviceToDevice, c->stream));
+    RC_CU(cudaMemcpyAsync(c->d.WP2, c->d.WP, bytes, cudaMemcpyDeviceToDevice, c->stream));
+    phi = 0.;
+  } else {
+    RC_CU(cudaMemcpyAsync(c->d.WP2, c->d.WP, bytes, cudaMemcpyDeviceToDevice, c->stream));
+    RC_CU(cudaMemcpyAsync(c->d.WP, c->d.WA, bytes, cudaMemcpyDeviceToDevice, c->stream));
+    phi = 0.5;
+  }
+  if (int st = bdf2_params(c, dt, phi)) return st;
+  RC_DISPATCH(c, bdf2_fixed, c->d, c->d.bs, c->stream);
+  c->launches++;
+  if (!c->bdf2_graph) {
+    cudaGraph_t gph;
+    const long long before = c->launches;
+    RC_CU(cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal));
+    RC_DISPATCH(c, q_bdf2_inner, c);
+    cudaError_t e = cudaStreamEndCapture(c->stream, &gph);
+    if (e != cudaSuccess) return cuda_fail(c, e, "capture of the BDF2 inner iteration");
+    c->bdf2_graph_kernels = c->launches - before;
+    c->launches = before;
+    e = cudaGraphInstantiate(&c->bdf2_graph, gph, 0);
+    cudaGraphDestroy(gph);
+    if (e != cudaSuccess) return cuda_fail(c, e, "cudaGraphInstantiate");
+  }
+  const int V = c->V;
+  std::vector<double> h((size_t)V + 1);
+  unsigned derr = 0;
+  double rores_tmp = 0.0;
+  int inner = 1;
+  for (; inner <= inner_loop; ++inner) {
+    RC_CU(cudaGraphLaunch(c->bdf2_graph, c->stream));
+    c->launches += c->bdf2_graph_kernels;
+    // inner_iteration_residual (residual.f90:23-59): sum of the species rows
+    RC_CU(cudaMemcpyAsync(h.data(), c->norm_out, sizeof(double) * h.size(), cudaMemcpyDeviceToHost, c->stream));
+    RC_CU(cudaMemcpyAsync(&derr, c->d.err, sizeof(unsigned), cudaMemcpyDeviceToHost, c->stream));
+    RC_CU(cudaStreamSynchronize(c->stream));
+    double rores = 0.0;
+    for (int k = 4; k < V; ++k) rores = rores + h[k];
+    if (inner == 1) rores_tmp = rores;
+    if (rores < rores_tmp * rel_tol || inner == inner_loop) {
+      RC_DISPATCH(c, q_bdf2_final, c);
+      break;
+    }
+    if (derr) break;  // the reference stops (NaN, thermo range, singular cell system)
+  }
+  if (inner_done) *inner_done = inner > inner_loop ? inner_loop : inner;
+  if (int st = check_launch(c, "rc_bdf2_stage")) return st;
+  return latch(c);
 }
 
 int rc_stats(rc_ctx* c, long long* launches, int* fwd, int* bwd) {

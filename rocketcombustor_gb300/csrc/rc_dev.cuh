@@ -1,6 +1,7 @@
 // Device layout shared by the FP64 and mixed-precision kernels.
 #pragma once
 #include <cstdint>
+#include <utility>
 
 #include "rc_thermo.cuh"
 
@@ -84,7 +85,31 @@ struct Dev {
   const float* bctab32;
   const int* fcase;
   const int* gcase;
+  // unsteady dual-time BDF2 (allocated on first use)
+  double* WP;                    // [V*NE] WA of the previous physical step
+  double* WP2;                   // [V*NE] WA of the step before
+  double* bfix;                  // [V*NE] vol/dt ((1+2 phi) WP - phi WP2)
+  double* bmat;                  // [NE*V*(2V+2)] per cell, per row: equilibrated row, LU row, r, c
+  int* bperm;                    // [8*NE] per cell: source row of each row after the interchanges; [7] flags
+  double* bnb;                   // [(9+2*NSP)*NE] gas state of each cell as seen by its neighbours' sweeps
+  const double* bpar;            // {dt, phi}
 };
+
+// launch as a programmatic dependent of the previous kernel of the stream
+// (cudaLaunchAttributeProgrammaticStreamSerialization)
+template <class... Args, class... Act>
+inline void launch_pdl(void (*kernel)(Args...), unsigned grid, unsigned block, cudaStream_t s, Act&&... args) {
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = dim3(grid);
+  cfg.blockDim = dim3(block);
+  cfg.stream = s;
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+  attr[0].val.programmaticStreamSerializationAllowed = 1;
+  cfg.attrs = attr;
+  cfg.numAttrs = 1;
+  cudaLaunchKernelEx(&cfg, kernel, std::forward<Act>(args)...);
+}
 
 constexpr int BCS = 13;                 // doubles per bctab row
 constexpr int BC_Y = 0, BC_T = 8, BC_MFLOW = 10, BC_POUT = 12;  // + w*NSPMAX (Y) or + w (T, mass flux)

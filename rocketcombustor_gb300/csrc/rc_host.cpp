@@ -159,6 +159,10 @@ struct rc_case {
   int limit = 0, nscreen = 1;
   long nstep = 0;
   double unit = 1, cfl = 0, p_out_ratio = 0, p_out = 0;
+  // unsteady dual-time BDF2 (implicit_time_method 5)
+  bool steady = true;
+  int inner_loop = 1;
+  double totaltime = 0, rel_tol = 0, A_p = 0, f_p = 0, p_static = 0, ttime = 0, dt = 0;
   // module arrays, Fortran layout, 1-based ids
   int NE = 0, NF = 0, NNT = 0, MaxNei = 0, Ng = 0;
   std::vector<int> KFace, N, Neighbor, FNode, FProperty, NeighF, Neigh, NeighC, Ghostcell, Num_ghostcell,
@@ -279,17 +283,21 @@ void rc_case::read_inputs() {
     r.skip(); unit = r.real();
     r.skip();
     auto f = r.take(4);
-    bool steady = Records::logical(f[0]);
+    steady = Records::logical(f[0]);
     viscous = Records::logical(f[1]);
     backup = Records::logical(f[2]);
     bool expl = Records::logical(f[3]);
-    r.skip(); r.integer();
+    r.skip(); const long method = r.integer();
     r.skip();
     auto g = r.take(5);
     cfl = num(g[0]);
+    totaltime = num(g[1]);
     nstep = inum(g[2]);
     r.skip(); r.take(1);
-    r.skip(); r.take(3);
+    r.skip();
+    auto il = r.take(3);
+    inner_loop = (int)inum(il[1]);
+    rel_tol = num(il[2]);
     r.skip(); nscreen = (int)inum(r.take(4)[0]);
     r.skip(); r.real();
     r.skip(); limit = (int)inum(r.take(2)[1]);
@@ -298,9 +306,14 @@ void rc_case::read_inputs() {
     r.skip();
     for (long i = 0; i < nmon; ++i) r.take(2);
     r.skip();
-    p_out_ratio = num(r.take(3)[0]);
-    if (!steady || expl || right || npar != 1)
-      throw std::runtime_error("the GPU path covers the steady implicit single-partition solver");
+    auto po = r.take(3);
+    p_out_ratio = num(po[0]);
+    A_p = num(po[1]);
+    f_p = num(po[2]);
+    if (expl || right || npar != 1 || (!steady && method != 5))
+      throw std::runtime_error("the GPU path covers the steady implicit and the unsteady BDF2 single-partition solver");
+    if (steady) inner_loop = 1;                    // initParam.f90:220-222
+    else dt = totaltime / (double)nstep;           // initParam.f90:72
   }
 }
 
@@ -446,9 +459,10 @@ void rc_case::initialise() {
   oxM = oxM / ox_d;
   fuM = 0.5 * fuM / fu_d;
   p_out = p_out_ratio * oxP;
+  p_static = p_out;
   if (!backup) throw std::runtime_error("the initial field is read from fvp1.sav (IfReadBackup=.true.)");
   Records r(dir + "/fvp1.sav");
-  r.real();
+  ttime = r.real();
   if (r.integer() != NE) throw std::runtime_error("Error in the number of cells when reading backup");
   std::vector<double> row;
   PA.assign((size_t)NVar * NE, 0);
@@ -845,6 +859,61 @@ int rc_run_steady(rc_case* c, int precision, int device, long nsteps, long every
       st = rc_residual(ctx, hist + (size_t)row * (c->NVar + 1), hist + (size_t)row * (c->NVar + 1) + c->NVar);
       ++row;
     }
+  }
+  if (!st) st = rc_get_state(ctx, c->PA.data(), c->WA.data());
+  if (st) c->err = rc_last_error(ctx);
+  rc_finalize(ctx);
+  return st;
+}
+
+int rc_case_unsteady(const rc_case* c, double* out) {
+  if (!c || !out) return RC_ERR_ARG;
+  out[0] = c->steady ? 0.0 : 1.0; out[1] = c->ttime; out[2] = c->dt; out[3] = c->totaltime;
+  out[4] = (double)c->nstep; out[5] = c->inner_loop; out[6] = c->rel_tol; out[7] = c->p_static;
+  out[8] = c->A_p; out[9] = c->f_p;
+  return RC_OK;
+}
+
+// compute_p_out (fvm2d.f90:229-239)
+static double case_p_out(const rc_case* c, double ttime) {
+  const double pi = 4 * std::atan(1.0);
+  return c->p_static * (1. + c->A_p * std::sin(2 * pi * c->f_p * ttime));
+}
+
+// The unsteady implicit branch of program main (fvm2d.f90:48-150) with the
+// BDF2 stage: per physical step the last step is shortened to end at
+// totaltime (:52-56), ttime and p_out advance around the stage, and the loop
+// ends after that last step.
+int rc_run_unsteady(rc_case* c, int device, long nsteps, long every, double* hist, int* inner) {
+  if (!c || nsteps < 0 || (hist && every < 1)) return RC_ERR_ARG;
+  if (c->steady) { c->err = "the case is steady (IfSteady = .true.)"; return RC_ERR_ARG; }
+  rc_mesh m;
+  rc_thermo t;
+  rc_config g;
+  rc_case_views(c, RC_PREC_FP64, device, &m, &t, &g);
+  rc_ctx* ctx = nullptr;
+  int st = rc_init(&m, &t, &g, &ctx);
+  if (st) { c->err = "rc_init failed"; return st; }
+  st = rc_set_state(ctx, c->PA.data(), c->WA.data());
+  const double totaltime_num = c->totaltime * (1. - 1.e-10);
+  long row = 0;
+  for (long istep = 1; istep <= nsteps && !st; ++istep) {
+    bool stop = false;
+    if (c->ttime + c->dt > totaltime_num) { c->dt = c->totaltime - c->ttime; stop = true; }
+    const double ttime_n = c->ttime;
+    c->ttime = ttime_n + 1.0 * c->dt;
+    c->p_out = case_p_out(c, c->ttime);
+    st = rc_set_p_out(ctx, &c->p_out);
+    int n_inner = 0;
+    if (!st) st = rc_bdf2_stage(ctx, (int)istep, c->dt, c->inner_loop, c->rel_tol, &n_inner);
+    if (inner) inner[istep - 1] = n_inner;
+    c->ttime = ttime_n + c->dt;
+    c->p_out = case_p_out(c, c->ttime);
+    if (!st && hist && istep % every == 0) {
+      st = rc_residual(ctx, hist + (size_t)row * (c->NVar + 1), hist + (size_t)row * (c->NVar + 1) + c->NVar);
+      ++row;
+    }
+    if (stop) break;
   }
   if (!st) st = rc_get_state(ctx, c->PA.data(), c->WA.data());
   if (st) c->err = rc_last_error(ctx);

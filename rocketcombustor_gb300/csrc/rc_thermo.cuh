@@ -15,7 +15,7 @@ namespace rc {
 
 enum : unsigned {
   ERR_THERMO_T = 1u, ERR_TRANSPORT_T = 2u, ERR_NEG_TIMESTEP = 4u, ERR_NEG_FACE = 8u,
-  ERR_NAN = 16u, ERR_BCTYPE = 32u, ERR_SYNC = 64u
+  ERR_NAN = 16u, ERR_BCTYPE = 32u, ERR_SYNC = 64u, ERR_LINSOLVE = 128u
 };
 
 template <int NSP>

@@ -1,0 +1,103 @@
+"""GPU parity of the unsteady dual-time BDF2 stage with the CPU oracle (needs a GB300).
+
+BDF2_LU_SGS (Time_BDF2.f90:73-337) keeps the reference's operation order on
+the device, including the per-cell dgesvx steps (equilibration, LU with
+partial pivoting, the triangular solves and dgerfs's refinement), with FMA
+contraction off; the results are expected to be bit-identical to the
+oracle's.  The inner-iteration stop compares norms whose GPU reduction order
+differs from the oracle's serial sum (rounding only), so the inner counts are
+compared too.
+"""
+import numpy as np
+import pytest
+
+import oracle
+import rocketcombustor_gb300 as rc
+from conftest import make_case
+
+pytestmark = pytest.mark.gpu
+
+T1U = {"unsteady": True, "inner_loop": 4, "rel_tol": 1e-3, "totaltime": 1e-3, "nstep": 100000}
+
+
+def _assemble(s, o):
+    s.timestep(); s.reconstruction(); s.flux_sourceterm()
+    o.call("timestep"); o.call("reconstruction"); o.call("flux_sourceterm")
+
+
+@pytest.mark.parametrize("name,over", [("t2u", {}), ("t1", T1U), ("t2u", {"order": "random"})])
+def test_bdf2_lusgs_bit_identical_to_oracle(case_root, name, over):
+    d = make_case(case_root, name, **over)
+    c = rc.Case(d)
+    s = rc.Solver(c)
+    o = oracle.Oracle(d, threads=4)
+    dt = o.unsteady()["dt"]
+    rng = np.random.default_rng(7)
+    WA = o.array("WA").copy()
+    WP = WA * (1 + 1e-3 * rng.standard_normal(WA.shape))
+    WP2 = WA * (1 + 2e-3 * rng.standard_normal(WA.shape))
+    o.array("WP")[:] = WP
+    o.array("WP2")[:] = WP2
+    s.set_array("WP", WP)
+    s.set_array("WP2", WP2)
+    for inner in (1, 2):
+        _assemble(s, o)
+        assert np.array_equal(s.get_array("hWA"), o.array("hWA"))
+        assert o.bdf2_lusgs(inner, 0.5) == 0
+        s.bdf2_lusgs(inner, 0.5, dt)
+        s.sync()
+        assert np.array_equal(s.get_array("hWA"), o.array("hWA")), inner
+        PA, WA = s.get_state()
+        assert np.array_equal(PA, o.array("PA")), inner
+        assert np.array_equal(WA, o.array("WA")), inner
+
+
+@pytest.mark.parametrize("name,over", [("t2u", {}), ("t1", T1U), ("t2u", {"order": "colored"}),
+                                       ("t2u", {"a_p": 0.05, "f_p": 2.0e6})])
+def test_unsteady_steps_bit_identical_to_oracle(case_root, name, over):
+    """Ten physical steps of the driver (time advance, compute_p_out,
+    BDF2_stage) against the oracle's; the last case has a moving exit
+    pressure."""
+    d = make_case(case_root, name, **over)
+    c = rc.Case(d)
+    _, inner_gpu = c.run_unsteady(10)
+    o = oracle.Oracle(d, threads=4)
+    inner_cpu = [o.unsteady_step(i)[0] for i in range(1, 11)]
+    assert list(inner_gpu) == inner_cpu
+    assert np.array_equal(c.array("PA"), o.array("PA"))
+    assert np.array_equal(c.array("WA"), o.array("WA"))
+    assert c.unsteady["ttime"] == o.unsteady()["ttime"]
+
+
+def test_stage_residual_and_history_levels(case_root):
+    """Solver.bdf2_stage: after the stage hWA is the residual of the final
+    flux_sourceterm, as in the oracle; the time levels WP / WP2 are WA of the
+    previous steps."""
+    d = make_case(case_root, "t2u")
+    c = rc.Case(d)
+    s = rc.Solver(c)
+    o = oracle.Oracle(d, threads=4)
+    u = o.unsteady()
+    s.set_p_out(u["p_out"])
+    WA_prev = []
+    for istep in (1, 2, 3):
+        WA_prev.append(s.get_state()[1])
+        n = s.bdf2_stage(istep, u["dt"], u["inner_loop"], u["rel_tol"])
+        m, _ = o.unsteady_step(istep)
+        assert n == m
+    assert np.array_equal(s.get_array("hWA"), o.array("hWA"))
+    assert np.array_equal(s.get_array("WP"), WA_prev[2])
+    assert np.array_equal(s.get_array("WP2"), WA_prev[1])
+    PA, WA = s.get_state()
+    assert np.array_equal(PA, o.array("PA")) and np.array_equal(WA, o.array("WA"))
+
+
+def test_bdf2_rejects_what_it_does_not_cover(case_root):
+    d = make_case(case_root, "t2u")
+    c = rc.Case(d)
+    s = rc.Solver(c, precision=rc.RC_PREC_MIXED)
+    with pytest.raises(rc.RcError):
+        s.bdf2_stage(1, 1e-8, 2, 1e-3)
+    steady = rc.Case(make_case(case_root, "t2"))
+    with pytest.raises(rc.RcError):
+        steady.run_unsteady(1)
