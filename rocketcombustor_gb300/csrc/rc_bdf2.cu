@@ -29,6 +29,7 @@
 // netlib routines, which the CPU oracle restates too.
 #include "rc_chem.cuh"
 #include "rc_dev.cuh"
+#include "rc_div.cuh"
 
 namespace rc {
 
@@ -41,9 +42,11 @@ constexpr unsigned FULL = 0xffffffffu;
 // gas state of a cell as a neighbour (bnb planes)
 enum : int { NB_RR = 0, NB_RRC, NB_RT, NB_RCT, NB_RCP, NB_HH, NB_EK, NB_ROU, NB_ROV, NB_ROEPP, NB_H };
 template <int NSP>
-__host__ __device__ constexpr int nbq() { return NB_H + NSP + (NSP - 1); }
-template <int NSP>
 __host__ __device__ constexpr int nb_ry() { return NB_H + NSP; }
+template <int NSP>
+__host__ __device__ constexpr int nb_rct() { return NB_H + NSP + (NSP - 1); }  // recip_of(Rcpcv T): 2 planes
+template <int NSP>
+__host__ __device__ constexpr int nbq() { return nb_rct<NSP>() + 2; }
 
 __device__ __forceinline__ double mx(double a, double b) { return (b > a) ? b : a; }
 __device__ __forceinline__ double mn(double a, double b) { return (b < a) ? b : a; }
@@ -268,21 +271,23 @@ __device__ double dgecon(const double* af, double anorm) {
 // ---- the per-row solve of one cell's system by its eight lanes
 // x: this row's right-hand side (already row-scaled); returns A^-1 x for this
 // row (dgetrs('N')): the composed interchanges, then the column-oriented unit
-// lower and upper solves of dtrsm, skipping zero entries as dtrsm does.
+// lower and upper solves of dtrsm, skipping zero entries as dtrsm does.  The
+// divisions by the diagonal of U use its reciprocal pairs urh, url (div_rn:
+// the same bits as the IEEE division).
 template <int N>
-__device__ __forceinline__ double getrs_rows(double x, int src, const double* lu, const double* ukk, int r,
-                                             int base) {
+__device__ __forceinline__ double getrs_rows(double x, int src, const double* lu, const double* ukk,
+                                             const double* urh, const double* url, int r, int base) {
   x = __shfl_sync(FULL, x, base + src);
 #pragma unroll
   for (int k = 0; k < N - 1; ++k) {
     const double xk = __shfl_sync(FULL, x, base + k);
-    if (r > k && r < N && xk != 0.0) x = x - xk * lu[k];
+    if (r > k && r < N && nonzero(xk)) x = x - xk * lu[k];
   }
 #pragma unroll
   for (int k = N - 1; k >= 0; --k) {
     double xk = __shfl_sync(FULL, x, base + k);
-    if (xk != 0.0) {
-      xk = xk / ukk[k];
+    if (nonzero(xk)) {
+      xk = div_rn(xk, ukk[k], urh[k], url[k]);
       if (r == k) x = xk;
       else if (r < k) x = x - xk * lu[k];
     }
@@ -309,7 +314,7 @@ __global__ void __launch_bounds__(128) k_bdf2_fixed(const Dev d) {
 template <int NSP>
 __global__ void __launch_bounds__(128) k_bdf2_prep(const Dev d, const ThermoDev<NSP> th) {
   using namespace bdf2;
-  constexpr int V = 3 + NSP, RW = 2 * V + 2;
+  constexpr int V = 3 + NSP, RW = 2 * V + 4;
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= d.NE) return;
   const int NE = d.NE;
@@ -376,6 +381,9 @@ __global__ void __launch_bounds__(128) k_bdf2_prep(const Dev d, const ThermoDev<
     for (int c = 0; c < V; ++c) { m[r * RW + c] = a[r * V + c]; m[r * RW + V + c] = af[r * V + c]; }
     m[r * RW + 2 * V] = rs[r];
     m[r * RW + 2 * V + 1] = cs[r];
+    const Recip ru = recip_of(af[r * V + r]);
+    m[r * RW + 2 * V + 2] = ru.h;
+    m[r * RW + 2 * V + 3] = ru.l;
     d.bperm[i * 8 + r] = src[r];
   }
   d.bperm[i * 8 + 7] = equ;
@@ -407,28 +415,32 @@ __global__ void __launch_bounds__(128) k_bdf2_prep(const Dev d, const ThermoDev<
   for (int k = 0; k < NSP; ++k) nb[(NB_H + k) * NE + i] = entha[k];
 #pragma unroll
   for (int k = 0; k < NSP - 1; ++k) nb[(nb_ry<NSP>() + k) * NE + i] = rr * yy[k];
+  const Recip rc = recip_of(rct);
+  nb[nb_rct<NSP>() * NE + i] = rc.h;
+  nb[(nb_rct<NSP>() + 1) * NE + i] = rc.l;
   flag(d, err);
 }
 
 // One level of the forward (FWD) or backward sweep, cells t0..t1-1 of the
-// level order; eight lanes per cell, four cells per warp (one warp per block).
-template <int NSP, bool FWD>
+// level order; eight lanes per cell, CPW cells per warp (one warp per block;
+// lanes of cell slots >= CPW only join the shuffles).
+template <int NSP, bool FWD, int CPW>
 __global__ void __launch_bounds__(32) k_bdf2_sweep(const Dev d, const ThermoDev<NSP> th, int t0, int t1) {
   using namespace bdf2;
-  constexpr int V = 3 + NSP, RW = 2 * V + 2, DIR = FWD ? 0 : 1;
+  constexpr int V = 3 + NSP, RW = 2 * V + 4, DIR = FWD ? 0 : 1;
   static_assert(V <= 7, "one lane per row and the flags in slot 7");
   pdl_launch_dependents();
   const int lane = threadIdx.x & 31, cell = lane >> 3, r = lane & 7, base = cell * 8;
   const int q = r & 3;
-  const bool lo = r < 4;  // lanes 0-3: flux rows 1-3; lanes 4-7: rows 4.. (energy, species)
+  const bool lo = r < 4;  // lanes 0-3 keep flux rows 1-3 of their slot, lanes 4-7 rows 4.. (energy, species)
   const int NE = d.NE, NF = d.NF;
-  const int t = t0 + blockIdx.x * 4 + cell;
-  const bool valid = t < t1;
+  const int t = t0 + blockIdx.x * CPW + cell;
+  const bool valid = cell < CPW && t < t1;
   const int i = valid ? d.swi[DIR][t] : 0;
   // --- what the sweep does not change: the face of slot q and its neighbour's gas state
   const int j = valid ? d.swj[DIR][q * NE + t] : -1;
   const bool act = j >= 0;
-  double dx = 0, dy = 0, aF = 0, uu = 0, vv = 0, rr = 0, rrc = 0, rt = 0, rct = 0, unormal = 0;
+  double dx = 0, dy = 0, aF = 0, uu = 0, vv = 0, rr = 0, rrc = 0, rt = 0, rct = 0, rcth = 1, rctl = 0, unormal = 0;
   double rou = 0, rov = 0, rcp = 0, hh = 0, ek = 0, roepp = 0, ent[NSP], yy[NSP], ry[NSP];
 #pragma unroll
   for (int k = 0; k < NSP; ++k) { ent[k] = 0.0; yy[k] = 0.0; ry[k] = 0.0; }
@@ -442,26 +454,24 @@ __global__ void __launch_bounds__(32) k_bdf2_sweep(const Dev d, const ThermoDev<
     vv = d.PA[2 * NE + j];
     const double* nb = d.bnb;
     rr = nb[NB_RR * NE + j]; rrc = nb[NB_RRC * NE + j]; rt = nb[NB_RT * NE + j]; rct = nb[NB_RCT * NE + j];
+    rcth = nb[nb_rct<NSP>() * NE + j]; rctl = nb[(nb_rct<NSP>() + 1) * NE + j];
     unormal = uu * dx + vv * dy;
-    if (lo) {
-      rou = nb[NB_ROU * NE + j];
-      rov = nb[NB_ROV * NE + j];
-    } else {
-      rcp = nb[NB_RCP * NE + j]; hh = nb[NB_HH * NE + j]; ek = nb[NB_EK * NE + j]; roepp = nb[NB_ROEPP * NE + j];
+    rou = nb[NB_ROU * NE + j];
+    rov = nb[NB_ROV * NE + j];
+    rcp = nb[NB_RCP * NE + j]; hh = nb[NB_HH * NE + j]; ek = nb[NB_EK * NE + j]; roepp = nb[NB_ROEPP * NE + j];
 #pragma unroll
-      for (int k = 0; k < NSP; ++k) ent[k] = nb[(NB_H + k) * NE + j];
+    for (int k = 0; k < NSP; ++k) ent[k] = nb[(NB_H + k) * NE + j];
 #pragma unroll
-      for (int k = 0; k < NSP - 1; ++k) {
-        yy[k] = d.PA[(4 + k) * NE + j];
-        ry[k] = nb[(nb_ry<NSP>() + k) * NE + j];
-      }
+    for (int k = 0; k < NSP - 1; ++k) {
+      yy[k] = d.PA[(4 + k) * NE + j];
+      ry[k] = nb[(nb_ry<NSP>() + k) * NE + j];
     }
   }
   // --- this lane's row of the cell's system
-  double arow[V], lrow[V], ukk[V], rsc = 1.0, csc = 1.0;
+  double arow[V], lrow[V], ukk[V], urh[V], url[V], rsc = 1.0, csc = 1.0;
   int src = 0, equ = 0;
 #pragma unroll
-  for (int k = 0; k < V; ++k) { arow[k] = 0.0; lrow[k] = 0.0; ukk[k] = 1.0; }
+  for (int k = 0; k < V; ++k) { arow[k] = 0.0; lrow[k] = 0.0; ukk[k] = 1.0; urh[k] = 1.0; url[k] = 0.0; }
   if (valid) {
     const double* m = d.bmat + (size_t)i * V * RW;
     if (r < V) {
@@ -472,7 +482,11 @@ __global__ void __launch_bounds__(32) k_bdf2_sweep(const Dev d, const ThermoDev<
       src = d.bperm[i * 8 + r];
     }
 #pragma unroll
-    for (int k = 0; k < V; ++k) ukk[k] = m[k * RW + V + k];
+    for (int k = 0; k < V; ++k) {
+      ukk[k] = m[k * RW + V + k];
+      urh[k] = m[k * RW + 2 * V + 2];
+      url[k] = m[k * RW + 2 * V + 3];
+    }
     equ = d.bperm[i * 8 + 7];
   }
   double hown = 0.0;
@@ -493,7 +507,7 @@ __global__ void __launch_bounds__(32) k_bdf2_sweep(const Dev d, const ThermoDev<
     double s1 = 0.0;
 #pragma unroll
     for (int k = 0; k < NSP; ++k) s1 = s1 + th.R[k] * dyy[k];
-    const double drr = (dpp - rrc * dtt - rt * s1) / rct;
+    const double drr = div_rn(dpp - rrc * dtt - rt * s1, rct, rcth, rctl);
     const double dunormal = duu * dx + dvv * dy;
     if (lo) {
       const double dru = rr * duu + uu * drr;
@@ -514,14 +528,16 @@ __global__ void __launch_bounds__(32) k_bdf2_sweep(const Dev d, const ThermoDev<
       }
     }
   }
-  __shared__ double wsm[4 * V * 4];
-  double* w = wsm + cell * V * 4;  // [row][slot]
-  if (lo) {
+  __shared__ double wsm[CPW * V * 4];
+  double* w = wsm + (cell < CPW ? cell : 0) * V * 4;  // [row][slot]
+  if (cell < CPW) {
+    if (lo) {
 #pragma unroll
-    for (int k = 0; k < 3; ++k) w[k * 4 + q] = c[k];
-  } else {
+      for (int k = 0; k < 3; ++k) w[k * 4 + q] = c[k];
+    } else {
 #pragma unroll
-    for (int k = 3; k < V; ++k) w[k * 4 + q] = c[k];
+      for (int k = 3; k < V; ++k) w[k * 4 + q] = c[k];
+    }
   }
   __syncwarp();
   double dflux = 0.0;
@@ -534,10 +550,12 @@ __global__ void __launch_bounds__(32) k_bdf2_sweep(const Dev d, const ThermoDev<
   double b = FWD ? hown - dflux : dflux;
   if (rowequ) b = rsc * b;
   if (!(valid && r < V)) b = 0.0;
-  double x = getrs_rows<V>(b, src, lrow, ukk, r, base);
-  // dgerfs refinement: residual, componentwise backward error, correction
+  double x = getrs_rows<V>(b, src, lrow, ukk, urh, url, r, base);
+  // dgerfs refinement: residual, componentwise backward error, correction.
+  // The backward error is non-negative: its maximum and the loop tests
+  // compare bit patterns; 2 berr <= lstres is berr <= lstres/2 (both exact).
   const double safe1 = (V + 1) * SFMIN, safe2 = safe1 / EPS;
-  double lstres = 3.0;
+  long long lstres_half = dbits(1.5);  // lstres = 3
   int count = 1;
   bool go = valid;
   for (int it = 0; it < 6; ++it) {
@@ -550,17 +568,17 @@ __global__ void __launch_bounds__(32) k_bdf2_sweep(const Dev d, const ThermoDev<
     double wk = fabs(b);
 #pragma unroll
     for (int k = 0; k < V; ++k) wk = wk + fabs(arow[k]) * fabs(xs[k]);
-    double v = 0.0;
-    if (r < V) v = (wk > safe2) ? fabs(y) / wk : (fabs(y) + safe1) / (wk + safe1);
-    v = mx(v, __shfl_xor_sync(FULL, v, 1));
-    v = mx(v, __shfl_xor_sync(FULL, v, 2));
-    v = mx(v, __shfl_xor_sync(FULL, v, 4));
-    const bool cont = go && v > EPS && 2.0 * v <= lstres && count <= 5;
+    long long vb = 0;
+    if (r < V) vb = dbits((dbits(wk) > dbits(safe2)) ? fabs(y) / wk : (fabs(y) + safe1) / (wk + safe1));
+    vb = max(vb, (long long)__shfl_xor_sync(FULL, (unsigned long long)vb, 1));
+    vb = max(vb, (long long)__shfl_xor_sync(FULL, (unsigned long long)vb, 2));
+    vb = max(vb, (long long)__shfl_xor_sync(FULL, (unsigned long long)vb, 4));
+    const bool cont = go && vb > dbits(EPS) && vb <= lstres_half && count <= 5;
     if (!__any_sync(FULL, cont)) break;
-    const double corr = getrs_rows<V>(y, src, lrow, ukk, r, base);
+    const double corr = getrs_rows<V>(y, src, lrow, ukk, urh, url, r, base);
     if (cont) {
       x = x + corr;
-      lstres = v;
+      lstres_half = vb - (1LL << 52);  // berr / 2: berr > eps is a normal number
       count = count + 1;
     }
     go = cont;
@@ -615,11 +633,17 @@ template <int NSP>
 void bdf2_prep(const Dev& d, const void* th, int bs, cudaStream_t s) {
   k_bdf2_prep<NSP><<<nblk(d.NE, bs), bs, 0, s>>>(d, *static_cast<const ThermoDev<NSP>*>(th));
 }
+template <int NSP, int CPW>
+void bdf2_sweep_cpw(const Dev& d, const ThermoDev<NSP>& T, bool fwd, int t0, int t1, cudaStream_t s) {
+  if (fwd) launch_pdl(k_bdf2_sweep<NSP, true, CPW>, nblk(t1 - t0, CPW), 32, s, d, T, t0, t1);
+  else launch_pdl(k_bdf2_sweep<NSP, false, CPW>, nblk(t1 - t0, CPW), 32, s, d, T, t0, t1);
+}
 template <int NSP>
-void bdf2_sweep(const Dev& d, const void* th, bool fwd, int t0, int t1, cudaStream_t s) {
+void bdf2_sweep(const Dev& d, const void* th, bool fwd, int t0, int t1, int cpw, cudaStream_t s) {
   const auto& T = *static_cast<const ThermoDev<NSP>*>(th);
-  if (fwd) launch_pdl(k_bdf2_sweep<NSP, true>, nblk(t1 - t0, 4), 32, s, d, T, t0, t1);
-  else launch_pdl(k_bdf2_sweep<NSP, false>, nblk(t1 - t0, 4), 32, s, d, T, t0, t1);
+  if (cpw >= 4) bdf2_sweep_cpw<NSP, 4>(d, T, fwd, t0, t1, s);
+  else if (cpw == 2) bdf2_sweep_cpw<NSP, 2>(d, T, fwd, t0, t1, s);
+  else bdf2_sweep_cpw<NSP, 1>(d, T, fwd, t0, t1, s);
 }
 template <int NSP>
 void bdf2_update(const Dev& d, const void* th, int bs, cudaStream_t s) {
@@ -631,7 +655,7 @@ int bdf2_nbq() { return bdf2::nbq<NSP>(); }
 #define RC_BDF2_INST(N)                                                             \
   template void bdf2_fixed<N>(const Dev&, int, cudaStream_t);                       \
   template void bdf2_prep<N>(const Dev&, const void*, int, cudaStream_t);           \
-  template void bdf2_sweep<N>(const Dev&, const void*, bool, int, int, cudaStream_t); \
+  template void bdf2_sweep<N>(const Dev&, const void*, bool, int, int, int, cudaStream_t); \
   template void bdf2_update<N>(const Dev&, const void*, int, cudaStream_t);         \
   template int bdf2_nbq<N>();
 RC_BDF2_INST(1)

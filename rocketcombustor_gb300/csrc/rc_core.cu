@@ -894,7 +894,7 @@ template <int NSP>
 void chem_list(const Dev&, const void*, double, int, int*, const int*, const unsigned*, unsigned*, cudaStream_t);
 template <int NSP> void bdf2_fixed(const Dev&, int, cudaStream_t);
 template <int NSP> void bdf2_prep(const Dev&, const void*, int, cudaStream_t);
-template <int NSP> void bdf2_sweep(const Dev&, const void*, bool, int, int, cudaStream_t);
+template <int NSP> void bdf2_sweep(const Dev&, const void*, bool, int, int, int, cudaStream_t);
 template <int NSP> void bdf2_update(const Dev&, const void*, int, cudaStream_t);
 template <int NSP> int bdf2_nbq();
 cudaError_t surrogate_source(const Dev&, const void*, const rc_mlp*, float, int*, unsigned*, unsigned*,
@@ -953,6 +953,7 @@ struct rc_ctx {
 
   // unsteady dual-time BDF2 (allocated by the first BDF2 call)
   bool bdf2_ready = false;
+  int bdf2_cpw = 4;                        // BDF2 sweep cells per warp (1, 2 or 4; RC_BDF2_CPW)
   double* bpar_dev = nullptr;              // {dt, phi}
   cudaGraphExec_t bdf2_graph = nullptr;    // one inner iteration and its norms
   long long bdf2_graph_kernels = 0;
@@ -1238,11 +1239,11 @@ void q_bdf2_lusgs(rc_ctx* c) {
   bdf2_prep<NSP>(c->d, c->thermo.data(), c->d.bs, c->stream);
   c->launches++;
   for (size_t l = 0; l + 1 < c->fwd_off.size(); ++l) {
-    bdf2_sweep<NSP>(c->d, c->thermo.data(), true, c->fwd_off[l], c->fwd_off[l + 1], c->stream);
+    bdf2_sweep<NSP>(c->d, c->thermo.data(), true, c->fwd_off[l], c->fwd_off[l + 1], c->bdf2_cpw, c->stream);
     c->launches++;
   }
   for (size_t l = 0; l + 1 < c->bwd_off.size(); ++l) {
-    bdf2_sweep<NSP>(c->d, c->thermo.data(), false, c->bwd_off[l], c->bwd_off[l + 1], c->stream);
+    bdf2_sweep<NSP>(c->d, c->thermo.data(), false, c->bwd_off[l], c->bwd_off[l + 1], c->bdf2_cpw, c->stream);
     c->launches++;
   }
   bdf2_update<NSP>(c->d, c->thermo.data(), c->d.bs, c->stream);
@@ -2159,12 +2160,13 @@ static int bdf2_setup(rc_ctx* c) {
   int st = dev_zeros(c, V * NE, &c->d.WP);
   st |= dev_zeros(c, V * NE, &c->d.WP2);
   st |= dev_zeros(c, V * NE, &c->d.bfix);
-  st |= dev_zeros(c, NE * V * (2 * V + 2), &c->d.bmat);
+  st |= dev_zeros(c, NE * V * (2 * V + 4), &c->d.bmat);
   st |= dev_zeros(c, 8 * NE, &c->d.bperm);
   st |= dev_zeros(c, (size_t)nbq * NE, &c->d.bnb);
   st |= dev_zeros(c, (size_t)2, &c->bpar_dev);
   if (st) return st;
   c->d.bpar = c->bpar_dev;
+  if (const char* e = std::getenv("RC_BDF2_CPW")) c->bdf2_cpw = std::atoi(e);
   c->bdf2_ready = true;
   drop_graphs(c);  // the captured kernels hold the old Dev
   return RC_OK;

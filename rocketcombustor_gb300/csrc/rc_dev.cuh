@@ -89,9 +89,9 @@ struct Dev {
   double* WP;                    // [V*NE] WA of the previous physical step
   double* WP2;                   // [V*NE] WA of the step before
   double* bfix;                  // [V*NE] vol/dt ((1+2 phi) WP - phi WP2)
-  double* bmat;                  // [NE*V*(2V+2)] per cell, per row: equilibrated row, LU row, r, c
+  double* bmat;                  // [NE*V*(2V+4)] per cell, per row: equilibrated row, LU row, r, c, 1/U_rr (2)
   int* bperm;                    // [8*NE] per cell: source row of each row after the interchanges; [7] flags
-  double* bnb;                   // [(9+2*NSP)*NE] gas state of each cell as seen by its neighbours' sweeps
+  double* bnb;                   // [(11+2*NSP)*NE] gas state of each cell as seen by its neighbours' sweeps
   const double* bpar;            // {dt, phi}
 };
 
