@@ -34,6 +34,7 @@
 #include "rc_gpu.h"
 #include "rc_mlp.h"
 #include "rc_dev.cuh"
+#include "rc_div.cuh"
 
 namespace rc {
 
@@ -122,7 +123,11 @@ __global__ void __launch_bounds__(128) k_cell(const Dev d, const ThermoDev<NSP> 
     double dsum = 0.0;
     for (int q = 0; q < nf; ++q) dsum = dsum + 0.5 * d.alpaF[d.cface[q * NE + i]];
     d.step[i] = st;
-    d.dd[i] = dsum + vol / st;
+    const double ddv = dsum + vol / st;
+    d.dd[i] = ddv;
+    const Recip rd = recip_of(ddv);
+    d.rcp[4 * NE + i] = rd.h;
+    d.rcp[5 * NE + i] = rd.l;
   }
   if (!do_recon) { flag(d, err); return; }
   double P[V], Y[NSP];
@@ -141,6 +146,10 @@ __global__ void __launch_bounds__(128) k_cell(const Dev d, const ThermoDev<NSP> 
   for (int k = 0; k < NSP; ++k) hh = hh + Y[k] * entha[k];
   d.cst[0 * NE + i] = rr;
   d.cst[1 * NE + i] = gama;
+  {
+    const Recip a = recip_of(rr), b = recip_of(gama - 1);
+    d.rcp[0 * NE + i] = a.h; d.rcp[1 * NE + i] = a.l; d.rcp[2 * NE + i] = b.h; d.rcp[3 * NE + i] = b.l;
+  }
   d.cst[2 * NE + i] = rr * (hh + 0.5 * (P[1] * P[1] + P[2] * P[2])) - P[0];
 #pragma unroll
   for (int k = 0; k < NSP; ++k) d.cst[(3 + k) * NE + i] = entha[k];
@@ -547,6 +556,9 @@ struct SweepPre {
   bool valid, act;
   int j;
   double dx, dy, pp, uu, vv, tt, rr, gama, roe, aF, ddi;
+  // reciprocal pairs (recip_of) of rr, gama - 1 and ddi: the divisions below
+  // by div_rn give the bits of the IEEE divisions
+  double rrh, rrl, gmh, gml, ddh, ddl;
   // products of the constants above, formed before the wait with the same
   // operations as the reference expressions use them
   double rou, rov, gm1, roepp, unormal;
@@ -563,6 +575,9 @@ __device__ __forceinline__ SweepPre<NSP> sweep_load(const Dev& d, int t, int ten
   p.j = p.valid ? d.swj[DIR][q * NE + t] : -1;
   const int fs = p.valid ? d.swf[DIR][q * NE + t] : 0;
   p.ddi = p.valid ? d.dd[p.i] : 1.0;
+  p.ddh = p.valid ? d.rcp[4 * NE + p.i] : 1.0;
+  p.ddl = p.valid ? d.rcp[5 * NE + p.i] : 0.0;
+  p.rrh = 1.0; p.rrl = 0.0; p.gmh = 1.0; p.gml = 0.0;
   p.act = p.j >= 0;
   if (p.act) {
     const int j = p.j, f = fs >= 0 ? fs : ~fs;
@@ -571,6 +586,7 @@ __device__ __forceinline__ SweepPre<NSP> sweep_load(const Dev& d, int t, int ten
     if (fs < 0) { p.dx = -p.dx; p.dy = -p.dy; }
     p.pp = d.PA[0 * NE + j]; p.uu = d.PA[1 * NE + j]; p.vv = d.PA[2 * NE + j]; p.tt = d.PA[3 * NE + j];
     p.rr = d.cst[0 * NE + j]; p.gama = d.cst[1 * NE + j]; p.roe = d.cst[2 * NE + j];
+    p.rrh = d.rcp[0 * NE + j]; p.rrl = d.rcp[1 * NE + j]; p.gmh = d.rcp[2 * NE + j]; p.gml = d.rcp[3 * NE + j];
     p.aF = d.alpaF[f];
 #pragma unroll
     for (int k = 0; k < NSP; ++k) p.cs[k] = d.cst[(3 + k) * NE + j];
@@ -607,15 +623,16 @@ __device__ __forceinline__ void sweep_compute(const Dev& d, const ThermoDev<NSP>
 #pragma unroll
     for (int k = 0; k < NSP - 1; ++k) { dry[k] = d.hWA[(4 + k) * NE + j]; s = s + dry[k]; }
     dry[NSP - 1] = drr - s;
-    const double duu = (dru - uu * drr) / rr;
-    const double dvv = (drv - vv * drr) / rr;
+    const double duu = div_rn(dru - uu * drr, rr, p.rrh, p.rrl);
+    const double dvv = div_rn(drv - vv * drr, rr, p.rrh, p.rrl);
     double s1 = 0.0, s2 = 0.0;
 #pragma unroll
     for (int k = 0; k < NSP; ++k) s1 = s1 + p.cs[k] * dry[k];
 #pragma unroll
     for (int k = 0; k < NSP; ++k) s2 = s2 + th.R[k] * dry[k];
     const double gm1 = p.gm1;
-    const double dpp = gm1 * (dre - s1 + tt * s2 * gama / gm1 - 0.5 * (dru * uu + duu * rou + drv * vv + dvv * rov));
+    const double dpp =
+        gm1 * (dre - s1 + div_rn(tt * s2 * gama, gm1, p.gmh, p.gml) - 0.5 * (dru * uu + duu * rou + drv * vv + dvv * rov));
     const double unormal = p.unormal;
     const double dunormal = duu * dx + dvv * dy;
     const double aF = p.aF;
@@ -643,8 +660,9 @@ __device__ __forceinline__ void sweep_compute(const Dev& d, const ThermoDev<NSP>
   }
   if (!p.valid) return;
   const double ddi = p.ddi;
-  d.hWA[q * NE + p.i] = FWD ? (R0 - df0) / ddi : R0 - df0 / ddi;
-  if (q + 4 < V) d.hWA[(q + 4) * NE + p.i] = FWD ? (R1 - df1) / ddi : R1 - df1 / ddi;
+  d.hWA[q * NE + p.i] = FWD ? div_rn(R0 - df0, ddi, p.ddh, p.ddl) : R0 - div_rn(df0, ddi, p.ddh, p.ddl);
+  if (q + 4 < V)
+    d.hWA[(q + 4) * NE + p.i] = FWD ? div_rn(R1 - df1, ddi, p.ddh, p.ddl) : R1 - div_rn(df1, ddi, p.ddh, p.ddl);
 }
 // The same cell step with 8 lanes per cell: lanes r = 0..3 (slot r) form the
 // terms that need dp (c1, c2, c3), lanes r = 4..7 (slot r-4) the others (c0,
@@ -671,8 +689,8 @@ __device__ __forceinline__ void sweep_compute8(const Dev& d, const ThermoDev<NSP
 #pragma unroll
     for (int k = 0; k < NSP - 1; ++k) { dry[k] = d.hWA[(4 + k) * NE + j]; s = s + dry[k]; }
     dry[NSP - 1] = drr - s;
-    const double duu = (dru - uu * drr) / rr;
-    const double dvv = (drv - vv * drr) / rr;
+    const double duu = div_rn(dru - uu * drr, rr, p.rrh, p.rrl);
+    const double dvv = div_rn(drv - vv * drr, rr, p.rrh, p.rrl);
     const double unormal = p.unormal;
     const double dunormal = duu * dx + dvv * dy;
     const double aF = p.aF;
@@ -684,8 +702,8 @@ __device__ __forceinline__ void sweep_compute8(const Dev& d, const ThermoDev<NSP
 #pragma unroll
       for (int k = 0; k < NSP; ++k) s2 = s2 + th.R[k] * dry[k];
       const double gm1 = p.gm1;
-      const double dpp =
-          gm1 * (dre - s1 + tt * s2 * gama / gm1 - 0.5 * (dru * uu + duu * rou + drv * vv + dvv * rov));
+      const double dpp = gm1 * (dre - s1 + div_rn(tt * s2 * gama, gm1, p.gmh, p.gml) -
+                                0.5 * (dru * uu + duu * rou + drv * vv + dvv * rov));
       c[1] = 0.5 * (-aF * dru + dru * unormal + rou * dunormal + dpp * dx);
       c[2] = 0.5 * (-aF * drv + drv * unormal + rov * dunormal + dpp * dy);
       c[3] = 0.5 * (-aF * dre + dunormal * p.roepp + unormal * (dre + dpp));
@@ -711,7 +729,7 @@ __device__ __forceinline__ void sweep_compute8(const Dev& d, const ThermoDev<NSP
 #pragma unroll
   for (int sl = 0; sl < 4; ++sl) df = df + w[r * 4 + sl];
   const double ddi = p.ddi;
-  d.hWA[r * NE + p.i] = FWD ? (R - df) / ddi : R - df / ddi;
+  d.hWA[r * NE + p.i] = FWD ? div_rn(R - df, ddi, p.ddh, p.ddl) : R - div_rn(df, ddi, p.ddh, p.ddl);
 }
 
 template <int NSP, bool FWD>
@@ -1657,6 +1675,7 @@ int init_impl(const rc_mesh* m, const rc_thermo* t, const rc_config* g, const Ba
   st |= dev_zeros(c, (size_t)NE, &d.step);
   st |= dev_zeros(c, (size_t)NE, &d.dd);
   st |= dev_zeros(c, (size_t)(3 + c->NSP) * NE, &d.cst);
+  st |= dev_zeros(c, (size_t)6 * NE, &d.rcp);
   st |= dev_zeros(c, (size_t)std::max(c->NSP - 1, 1) * NE, &d.src);
   st |= dev_zeros(c, (size_t)NF, &d.alpa);
   st |= dev_zeros(c, (size_t)NF, &d.visL);

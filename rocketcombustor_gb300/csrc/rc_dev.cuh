@@ -52,6 +52,7 @@ struct Dev {
   double* step;
   double* dd;
   double* cst;                   // [(3+NSP)*NE]: rho, gamma, rho*E, h_k
+  double* rcp;                   // [6*NE]: reciprocal pairs (h, l) of rho, gamma - 1 and dd
   double* src;                   // [(NSP-1)*NE]: vol*omega_k
   double* alpa;
   double* visL;
