@@ -242,6 +242,13 @@ int rc_surrogate_samples(rc_ctx* ctx, const double* d_P0, const double* d_P1, co
 int rc_set_p_out(rc_ctx* ctx, const double* p_out);
 int rc_bdf2_stage(rc_ctx* ctx, int istep, double dt, int inner_loop, double rel_tol, int* inner_done);
 int rc_bdf2_lusgs(rc_ctx* ctx, int inner_rk, double phi, double dt);
+/* Backward Euler (implicit_time_method 3): backwardEuler_stage and
+ * backwardEuler_LU_SGS (Time_BackwardEuler.f90:4-324).  The same sweeps,
+ * per-cell solves and inner-iteration stop as BDF2; the source term is
+ * vol/dt WA at the first inner iteration, the diagonal and right-hand side
+ * those of phi = 0, and there are no time levels. */
+int rc_euler_stage(rc_ctx* ctx, int istep, double dt, int inner_loop, double rel_tol, int* inner_done);
+int rc_euler_lusgs(rc_ctx* ctx, int inner_rk, double dt);
 
 /* Residual + step_residual norms (residual.f90:4-21, 61-79): res(k) =
  * sum(vol*|hWA(k,:)|)/total_volume, romax = max(WA(1,:)).  Synchronises. */

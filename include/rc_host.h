@@ -72,13 +72,15 @@ int rc_run_steady(rc_case* c, int precision, int device, long nsteps, long every
  * (0 if it never stalled).  No counterpart in the reference. */
 int rc_run_steady_dc(rc_case* c, int device, long nsteps, long every, int window, double* hist, long* switched_at);
 
-/* Time scheme of the case: out[0] 1 for the unsteady BDF2 scheme (0 steady),
- * ttime, dt, totaltime, nstep_max, InnerLoop, relTol, p_static, A_p, f_p
- * (10 values; startup.f90:87-120, initParam.f90:72, the backup's ttime). */
+/* Time scheme of the case: out[0] 1 for an unsteady scheme (0 steady),
+ * ttime, dt, totaltime, nstep_max, InnerLoop, relTol, p_static, A_p, f_p,
+ * implicit_time_method (11 values; startup.f90:87-120, initParam.f90:72, the
+ * backup's ttime). */
 int rc_case_unsteady(const rc_case* c, double* out);
 
-/* Unsteady driver for an unsteady BDF2 case: the implicit branch of program
- * main (src/fvm2d.f90:48-150) with BDF2_stage (src/Time_BDF2.f90:4): up to
+/* Unsteady driver: the implicit branch of program main (src/fvm2d.f90:48-150)
+ * with BDF2_stage (src/Time_BDF2.f90:4) or backwardEuler_stage
+ * (src/Time_BackwardEuler.f90:4), as the case's implicit_time_method says: up to
  * nsteps physical steps (fewer when totaltime is reached), each advancing
  * ttime, the exit pressure of compute_p_out (fvm2d.f90:229-239) and one
  * rc_bdf2_stage.  inner (may be NULL) gets the inner iterations of each step;

@@ -74,6 +74,7 @@ def lib() -> ctypes.CDLL:
         L.orc_chem_nsub.restype = ip; L.orc_chem_nsub.argtypes = [vp]
         L.orc_unsteady_scalars.argtypes = [vp, dp]
         L.orc_bdf2_lusgs.restype = i; L.orc_bdf2_lusgs.argtypes = [vp, i, d]
+        L.orc_euler_lusgs.restype = i; L.orc_euler_lusgs.argtypes = [vp, i]
         L.orc_unsteady_step.restype = i; L.orc_unsteady_step.argtypes = [vp, l, ip, ip]
         L.orc_dgesvx.restype = i; L.orc_dgesvx.argtypes = [i, dp, dp, dp, cp, dp]
         _lib = L
@@ -270,17 +271,21 @@ class Oracle:
 
     # unsteady dual-time BDF2
     def unsteady(self) -> dict:
-        s = np.zeros(11)
+        s = np.zeros(12)
         lib().orc_unsteady_scalars(self._h, _dp(s))
         return {"ttime": s[0], "dt": s[1], "p_out": s[2], "p_static": s[3], "rel_tol": s[4],
                 "inner_loop": int(s[5]), "steady": bool(s[6]), "A_p": s[7], "f_p": s[8],
-                "totaltime": s[9], "nstep_max": int(s[10])}
+                "totaltime": s[9], "nstep_max": int(s[10]), "method": int(s[11])}
 
     def bdf2_lusgs(self, inner_rk: int, phi: float) -> int:
         return lib().orc_bdf2_lusgs(self._h, int(inner_rk), float(phi))
 
+    def euler_lusgs(self, inner_rk: int) -> int:
+        return lib().orc_euler_lusgs(self._h, int(inner_rk))
+
     def unsteady_step(self, istep: int):
-        """One physical BDF2 step; returns (inner iterations, last step)."""
+        """One physical step of the case's implicit scheme (BDF2 or backward
+        Euler); returns (inner iterations, last step)."""
         inner = ctypes.c_int()
         stop = ctypes.c_int()
         e = lib().orc_unsteady_step(self._h, int(istep), ctypes.byref(inner), ctypes.byref(stop))

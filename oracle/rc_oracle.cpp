@@ -662,13 +662,15 @@ struct Oracle {
       auto v = r.read(3);
       p_out_ratio = tod(v[0]); A_p = tod(v[1]); f_p = tod(v[2]);
     }
-    if (IfExplicit || IfRightDomain || NPar != 1 || (!IfSteady && implicit_time_method != 5))
-      throw std::runtime_error("oracle covers the steady implicit and the unsteady BDF2 single-partition paths only");
+    if (IfExplicit || IfRightDomain || NPar != 1 ||
+        (!IfSteady && implicit_time_method != 5 && implicit_time_method != 3))
+      throw std::runtime_error(
+          "oracle covers the steady implicit, unsteady BDF2 and backward Euler single-partition paths only");
     if (IfSteady) {
       InLoop = 1; InnerLoop = 1;  // initParam.f90:220-222
     } else {
       dt = totaltime / (double)nstep_max;  // initParam.f90:72
-      InLoop = 1;                          // BDF2: one stage, cs(1) = 1 (initParam.f90:131-134)
+      InLoop = 1;                          // BDF2 / Euler: one stage, cs(1) = 1 (initParam.f90:119-134)
     }
   }
 
@@ -2184,21 +2186,27 @@ struct Oracle {
     }
     for (int k = 1; k <= nv; ++k) hWA(k, i) = fwd ? sol[k - 1] : hWA(k, i) - sol[k - 1];
   }
-  // BDF2_LU_SGS (Time_BDF2.f90:73-337)
-  void BDF2_LU_SGS(int inner_rk, double phi) {
+  // BDF2_LU_SGS (Time_BDF2.f90:73-337); with euler, backwardEuler_LU_SGS
+  // (Time_BackwardEuler.f90:58-324), whose sweeps and update are the same and
+  // whose source, diagonal and right-hand side are those of phi = 0 written
+  // without phi (:78-100).
+  void BDF2_LU_SGS(int inner_rk, double phi, bool euler = false) {
     if (inner_rk == 1) {
 #pragma omp parallel for schedule(static) num_threads(nthreads) if (nthreads > 1)
       for (long i = 1; i <= NE; ++i)
         for (int k = 1; k <= NVar; ++k)
-          fixed(k, i) = VOL(i) / dt * ((1 + 2 * phi) * WP(k, i) - phi * WP2(k, i));
+          fixed(k, i) = euler ? VOL(i) / dt * WA(k, i)
+                              : VOL(i) / dt * ((1 + 2 * phi) * WP(k, i) - phi * WP2(k, i));
     }
     std::vector<double> dd(NE + 1, 0.0);
 #pragma omp parallel for schedule(static) num_threads(nthreads) if (nthreads > 1)
     for (long i = 1; i <= NE; ++i) {
       double d = 0.0;
       for (int nei = 1; nei <= KFace(i); ++nei) d = d + 0.5 * alpaF(NeighF(nei, i));
-      dd[i] = d + VOL(i) * (1. / step(i) + (1 + phi) / dt);
-      for (int k = 1; k <= NVar; ++k) hWA(k, i) = hWA(k, i) - (1 + phi) * VOL(i) / dt * WA(k, i) + fixed(k, i);
+      dd[i] = euler ? d + VOL(i) * (1. / step(i) + 1. / dt) : d + VOL(i) * (1. / step(i) + (1 + phi) / dt);
+      for (int k = 1; k <= NVar; ++k)
+        hWA(k, i) = euler ? hWA(k, i) - VOL(i) / dt * WA(k, i) + fixed(k, i)
+                          : hWA(k, i) - (1 + phi) * VOL(i) / dt * WA(k, i) + fixed(k, i);
     }
     if (nthreads <= 1) {
       for (long i = 1; i <= NE; ++i) bdf2_cell(i, true, dd);
@@ -2226,10 +2234,13 @@ struct Oracle {
     for (int k = NFlow; k < NVar; ++k) r = r + res[k];
     return r;
   }
-  // BDF2_stage (Time_BDF2.f90:4-71); returns the inner iterations taken.
-  int BDF2_stage(long istep) {
-    double phi;
-    if (istep == 1) {
+  // BDF2_stage (Time_BDF2.f90:4-71), or with euler backwardEuler_stage
+  // (Time_BackwardEuler.f90:4-56: no time levels); returns the inner
+  // iterations taken.
+  int BDF2_stage(long istep, bool euler = false) {
+    double phi = 0.;
+    if (euler) {
+    } else if (istep == 1) {
       WP.d = WA.d; WP2.d = WP.d; phi = 0.;
     } else {
       WP2.d = WP.d; WP.d = WA.d; phi = 0.5;
@@ -2240,7 +2251,7 @@ struct Oracle {
       timestep();
       reconstruction();
       flux_sourceterm();
-      BDF2_LU_SGS(inner_rk, phi);
+      BDF2_LU_SGS(inner_rk, phi, euler);
       const double RoRes = inner_iteration_residual();
       if (inner_rk == 1) RoRes_tmp = RoRes;
       if (RoRes < RoRes_tmp * relTol || inner_rk == InnerLoop) {
@@ -2268,7 +2279,7 @@ struct Oracle {
     const double ttime_n = ttime;
     ttime = ttime_n + 1.0 * dt;
     compute_p_out();
-    const int inner = BDF2_stage(istep);
+    const int inner = BDF2_stage(istep, implicit_time_method == 3);
     ttime = ttime_n + dt;
     compute_p_out();
     return inner;
@@ -2446,11 +2457,13 @@ double orc_newton(void* h, double et, const double* Y, double t0) {
   return t;
 }
 // ---- unsteady dual-time BDF2 (implicit_time_method 5)
-// unsteady scalars: ttime, dt, p_out, p_static, relTol, InnerLoop, IfSteady, A_p, f_p, totaltime, nstep_max
+// unsteady scalars: ttime, dt, p_out, p_static, relTol, InnerLoop, IfSteady, A_p, f_p, totaltime, nstep_max,
+// implicit_time_method
 void orc_unsteady_scalars(void* h, double* s) {
   auto* o = static_cast<Oracle*>(h);
   s[0] = o->ttime; s[1] = o->dt; s[2] = o->p_out; s[3] = o->p_static; s[4] = o->relTol; s[5] = o->InnerLoop;
   s[6] = o->IfSteady; s[7] = o->A_p; s[8] = o->f_p; s[9] = o->totaltime; s[10] = (double)o->nstep_max;
+  s[11] = o->implicit_time_method;
 }
 // BDF2_LU_SGS with the given inner iteration and phi (the caller sets WP,
 // WP2 through orc_array); returns the error bit mask.
@@ -2458,6 +2471,13 @@ int orc_bdf2_lusgs(void* h, int inner_rk, double phi) {
   auto* o = static_cast<Oracle*>(h);
   if (o->IfSteady) { o->errmsg = "BDF2 needs an unsteady case"; return orc::E_SETUP; }
   o->BDF2_LU_SGS(inner_rk, phi);
+  return o->err.load();
+}
+// backwardEuler_LU_SGS (Time_BackwardEuler.f90:58-324)
+int orc_euler_lusgs(void* h, int inner_rk) {
+  auto* o = static_cast<Oracle*>(h);
+  if (o->IfSteady) { o->errmsg = "backward Euler needs an unsteady case"; return orc::E_SETUP; }
+  o->BDF2_LU_SGS(inner_rk, 0.0, true);
   return o->err.load();
 }
 // One physical step (time advance, p_out, BDF2_stage); inner iterations and

@@ -17,6 +17,7 @@ and, for the unsteady dual-time scheme (implicit_time_method 5):
 
     Solver.bdf2_lusgs(k, phi, dt)     BDF2_LU_SGS     src/Time_BDF2.f90:73
     Solver.bdf2_stage(i, dt, n, tol)  BDF2_stage      src/Time_BDF2.f90:4
+    Solver.euler_stage(i, dt, n, tol) backwardEuler_stage  src/Time_BackwardEuler.f90:4
     Case.run_unsteady(n)              the unsteady branch of program main (src/fvm2d.f90:48-150)
 
 There is no CPU fallback: if the library is missing or no GPU is present the
@@ -132,6 +133,8 @@ SIGNATURES = {
     "rc_set_p_out": (_i, [_vp, _DP]),
     "rc_bdf2_stage": (_i, [_vp, _i, _d, _i, _d, _IP]),
     "rc_bdf2_lusgs": (_i, [_vp, _i, _d, _d]),
+    "rc_euler_stage": (_i, [_vp, _i, _d, _i, _d, _IP]),
+    "rc_euler_lusgs": (_i, [_vp, _i, _d]),
     "rc_case_unsteady": (_i, [_vp, _DP]),
     "rc_run_unsteady": (_i, [_vp, _i, _l, _l, _DP, _IP]),
 }
@@ -260,10 +263,11 @@ class Case:
     @property
     def unsteady(self) -> dict:
         """Time scheme of the case (flow_solver_info.in and the backup's time)."""
-        o = np.zeros(10)
+        o = np.zeros(11)
         load().rc_case_unsteady(self._h, _dp(o))
         return {"unsteady": bool(o[0]), "ttime": o[1], "dt": o[2], "totaltime": o[3], "nstep_max": int(o[4]),
-                "inner_loop": int(o[5]), "rel_tol": o[6], "p_static": o[7], "A_p": o[8], "f_p": o[9]}
+                "inner_loop": int(o[5]), "rel_tol": o[6], "p_static": o[7], "A_p": o[8], "f_p": o[9],
+                "method": int(o[10])}
 
     def run_unsteady(self, nsteps: int, every: int = 1, device: int = 0):
         """The unsteady BDF2 driver (rc_run_unsteady): up to nsteps physical
@@ -431,6 +435,17 @@ class Solver:
         n = ctypes.c_int()
         self._check(load().rc_bdf2_stage(self._h, int(istep), float(dt), int(inner_loop), float(rel_tol),
                                          ctypes.byref(n)))
+        return n.value
+
+    def euler_lusgs(self, inner_rk: int, dt: float):
+        """backwardEuler_LU_SGS on the current residual."""
+        return self._check(load().rc_euler_lusgs(self._h, int(inner_rk), float(dt)))
+
+    def euler_stage(self, istep: int, dt: float, inner_loop: int, rel_tol: float) -> int:
+        """backwardEuler_stage; returns the inner iterations taken."""
+        n = ctypes.c_int()
+        self._check(load().rc_euler_stage(self._h, int(istep), float(dt), int(inner_loop), float(rel_tol),
+                                          ctypes.byref(n)))
         return n.value
 
     def residual(self) -> Tuple[np.ndarray, float]:

@@ -292,9 +292,11 @@ def write_inlet(path: str, Y: Sequence[float], T: float, p: float, mflow: float,
 
 def write_flow_info(d: str, combustion: bool, viscous: bool, cfl: float, nstep: int,
                     limit_id: int, p_out_ratio: float, unsteady: bool = False, totaltime: float = 1.0,
-                    inner_loop: int = 1, rel_tol: float = 1.0e-8, a_p: float = 0.0, f_p: float = 5000.0) -> None:
+                    inner_loop: int = 1, rel_tol: float = 1.0e-8, a_p: float = 0.0, f_p: float = 5000.0,
+                    time_method: int = 5) -> None:
     """flow/flow_solver_info.in (startup.f90:55-128).  Steady implicit LU-SGS,
-    or with `unsteady` the dual-time BDF2 scheme (implicit_time_method 5,
+    or with `unsteady` a dual-time scheme (implicit_time_method `time_method`:
+    5 BDF2, 3 backward Euler;
     physical step totaltime/nstep, inner_loop inner iterations stopped at
     rel_tol, exit pressure p_static (1 + a_p sin(2 pi f_p t)))."""
     L = lambda b: ".true." if b else ".false."  # noqa: E731
@@ -303,7 +305,8 @@ def write_flow_info(d: str, combustion: bool, viscous: bool, cfl: float, nstep: 
         f.write("# IfRightDomain\n.false.\n# NPreviousPar\n1\n# Npar, number of processors\n1\n")
         f.write("# unit\n1.0\n")
         f.write(f"# IfSteady, IfViscous, IfReadBackup, IfExplicit\n{L(not unsteady)}, {L(viscous)}, .true., .false.\n")
-        f.write("# implicit_time_method: 1-> Implicit Runge-Kutta, 2-> Trapezoidal, 3-> Euler, 4-> Midpoint, 5-> BDF2\n5\n")
+        f.write("# implicit_time_method: 1-> Implicit Runge-Kutta, 2-> Trapezoidal, 3-> Euler, 4-> Midpoint, 5-> BDF2\n"
+                f"{time_method}\n")
         f.write(f"# cfl,totaltime,nstep_max,save_start_time, save_end_time\n{_fmt(cfl)}, {_fmt(totaltime)}, {nstep}, 0.0, 0.5\n")
         f.write(f"# IfFixDt\n.false.\n# InLoop, InnerLoop, relTol\n1, {inner_loop}, {_fmt(rel_tol)}\n")
         f.write("# NScreenOutput,NFileOutput,NFileBackup,NWriteMonitor\n100,100000,100000,100000\n")
@@ -359,6 +362,7 @@ class CaseConfig:
     rel_tol: float = 1.0e-8
     a_p: float = 0.0           # exit-pressure oscillation amplitude (fraction of p_static)
     f_p: float = 5000.0        # and frequency (Hz)
+    time_method: int = 5       # implicit_time_method: 5 BDF2, 3 backward Euler
 
     @property
     def n_cells(self) -> int:
@@ -474,7 +478,7 @@ def write_case(d: str, cfg: CaseConfig, mesh: Optional[Mesh] = None) -> Mesh:
     write_inlet(os.path.join(d, "combustion", "fuel.in"), Yin, T_in, cfg.p0, 0.37, "fuel")
     pr = exit_pressure_ratio(gamma, cfg.h_exit) * cfg.p_out_factor
     write_flow_info(d, cfg.combustion, cfg.viscous, cfg.cfl, cfg.nstep, cfg.limit_id, pr, cfg.unsteady,
-                    cfg.totaltime, cfg.inner_loop, cfg.rel_tol, cfg.a_p, cfg.f_p)
+                    cfg.totaltime, cfg.inner_loop, cfg.rel_tol, cfg.a_p, cfg.f_p, cfg.time_method)
     # initial field: uniform inlet (chamber) state, or the quasi-1D isentropic
     # nozzle flow (subsonic up to the throat, supersonic after it) with the
     # velocity tilted along y/h * dh/dx; species optionally perturbed

@@ -1,6 +1,9 @@
 // Unsteady dual-time BDF2 stage of RocketCombustor on the device (FP64, built
 // with --fmad=false): the implicit_time_method 5 branch of the main loop,
-// BDF2_stage / BDF2_LU_SGS (Time_BDF2.f90:4-337).
+// BDF2_stage / BDF2_LU_SGS (Time_BDF2.f90:4-337).  The backward Euler stage
+// (implicit_time_method 3, Time_BackwardEuler.f90:4-324) runs the same
+// kernels: its source term is vol/dt WA, its diagonal and right-hand side
+// those of phi = 0.
 //
 // Per inner iteration, after the residual assembly that the steady path
 // shares (timestep, reconstruction, flux_sourceterm):
@@ -296,9 +299,10 @@ __device__ __forceinline__ double getrs_rows(double x, int src, const double* lu
 }
 }  // namespace bdf2
 
-// fixed = vol/dt ((1+2 phi) WP - phi WP2) (Time_BDF2.f90:100-105)
+// fixed = vol/dt ((1+2 phi) WP - phi WP2) (Time_BDF2.f90:100-105), or for
+// backward Euler vol/dt WA (Time_BackwardEuler.f90:78-82)
 template <int NSP>
-__global__ void __launch_bounds__(128) k_bdf2_fixed(const Dev d) {
+__global__ void __launch_bounds__(128) k_bdf2_fixed(const Dev d, int euler) {
   constexpr int V = 3 + NSP;
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= d.NE) return;
@@ -307,7 +311,8 @@ __global__ void __launch_bounds__(128) k_bdf2_fixed(const Dev d) {
   const double vd = d.vol[i] / dt;
 #pragma unroll
   for (int k = 0; k < V; ++k)
-    d.bfix[k * NE + i] = vd * ((1 + 2 * phi) * d.WP[k * NE + i] - phi * d.WP2[k * NE + i]);
+    d.bfix[k * NE + i] = euler ? vd * d.WA[k * NE + i]
+                               : vd * ((1 + 2 * phi) * d.WP[k * NE + i] - phi * d.WP2[k * NE + i]);
 }
 
 // Everything of BDF2_LU_SGS that the sweeps do not change, one thread per cell.
@@ -626,8 +631,8 @@ __global__ void __launch_bounds__(128) k_bdf2_update(const Dev d, const ThermoDe
 inline unsigned nblk(long n, int t) { return (unsigned)((n + t - 1) / t); }
 
 template <int NSP>
-void bdf2_fixed(const Dev& d, int bs, cudaStream_t s) {
-  k_bdf2_fixed<NSP><<<nblk(d.NE, bs), bs, 0, s>>>(d);
+void bdf2_fixed(const Dev& d, int bs, int euler, cudaStream_t s) {
+  k_bdf2_fixed<NSP><<<nblk(d.NE, bs), bs, 0, s>>>(d, euler);
 }
 template <int NSP>
 void bdf2_prep(const Dev& d, const void* th, int bs, cudaStream_t s) {
@@ -653,7 +658,7 @@ template <int NSP>
 int bdf2_nbq() { return bdf2::nbq<NSP>(); }
 
 #define RC_BDF2_INST(N)                                                             \
-  template void bdf2_fixed<N>(const Dev&, int, cudaStream_t);                       \
+  template void bdf2_fixed<N>(const Dev&, int, int, cudaStream_t);                  \
   template void bdf2_prep<N>(const Dev&, const void*, int, cudaStream_t);           \
   template void bdf2_sweep<N>(const Dev&, const void*, bool, int, int, int, cudaStream_t); \
   template void bdf2_update<N>(const Dev&, const void*, int, cudaStream_t);         \

@@ -910,7 +910,7 @@ void chem_batch(const void*, const double*, const double*, int, double*, int*, d
                 cudaStream_t);
 template <int NSP>
 void chem_list(const Dev&, const void*, double, int, int*, const int*, const unsigned*, unsigned*, cudaStream_t);
-template <int NSP> void bdf2_fixed(const Dev&, int, cudaStream_t);
+template <int NSP> void bdf2_fixed(const Dev&, int, int, cudaStream_t);
 template <int NSP> void bdf2_prep(const Dev&, const void*, int, cudaStream_t);
 template <int NSP> void bdf2_sweep(const Dev&, const void*, bool, int, int, int, cudaStream_t);
 template <int NSP> void bdf2_update(const Dev&, const void*, int, cudaStream_t);
@@ -1001,13 +1001,20 @@ int cuda_fail(rc_ctx* c, cudaError_t e, const char* what) {
     if (e_ != cudaSuccess) return cuda_fail(c, e_, #call);  \
   } while (0)
 
+// Allocations are filled on the context's stream and waited for: the stream
+// is non-blocking, so a fill on the legacy stream would not be ordered before
+// the context's kernels (and a pageable cudaMemcpy may return before its DMA
+// has landed).
 template <class T>
 int dev_upload(rc_ctx* c, const std::vector<T>& h, T** out) {
   void* p = nullptr;
   size_t bytes = std::max<size_t>(h.size(), 1) * sizeof(T);
   RC_CU(cudaMalloc(&p, bytes));
   c->allocs.push_back(p);
-  if (!h.empty()) RC_CU(cudaMemcpy(p, h.data(), h.size() * sizeof(T), cudaMemcpyHostToDevice));
+  if (!h.empty()) {
+    RC_CU(cudaMemcpyAsync(p, h.data(), h.size() * sizeof(T), cudaMemcpyHostToDevice, c->stream));
+    RC_CU(cudaStreamSynchronize(c->stream));
+  }
   *out = static_cast<T*>(p);
   return RC_OK;
 }
@@ -1016,7 +1023,8 @@ int dev_zeros(rc_ctx* c, size_t n, T** out) {
   void* p = nullptr;
   RC_CU(cudaMalloc(&p, std::max<size_t>(n, 1) * sizeof(T)));
   c->allocs.push_back(p);
-  RC_CU(cudaMemset(p, 0, std::max<size_t>(n, 1) * sizeof(T)));
+  RC_CU(cudaMemsetAsync(p, 0, std::max<size_t>(n, 1) * sizeof(T), c->stream));
+  RC_CU(cudaStreamSynchronize(c->stream));
   *out = static_cast<T*>(p);
   return RC_OK;
 }
@@ -2206,25 +2214,30 @@ int rc_set_p_out(rc_ctx* c, const double* p_out) {
   }
   return RC_OK;
 }
-int rc_bdf2_lusgs(rc_ctx* c, int inner_rk, double phi, double dt) {
+static int implicit_lusgs(rc_ctx* c, int inner_rk, double phi, double dt, int euler) {
   if (!c || inner_rk < 1 || !(dt > 0.0)) return RC_ERR_ARG;
   RC_NSP_OK(c);
   if (int st = bdf2_setup(c)) return st;
   if (int st = bdf2_params(c, dt, phi)) return st;
   if (inner_rk == 1) {
-    RC_DISPATCH(c, bdf2_fixed, c->d, c->d.bs, c->stream);
+    RC_DISPATCH(c, bdf2_fixed, c->d, c->d.bs, euler, c->stream);
     c->launches++;
   }
   RC_DISPATCH(c, q_bdf2_lusgs, c);
   return check_launch(c, "rc_bdf2_lusgs");
 }
-int rc_bdf2_stage(rc_ctx* c, int istep, double dt, int inner_loop, double rel_tol, int* inner_done) {
+int rc_bdf2_lusgs(rc_ctx* c, int inner_rk, double phi, double dt) { return implicit_lusgs(c, inner_rk, phi, dt, 0); }
+int rc_euler_lusgs(rc_ctx* c, int inner_rk, double dt) { return implicit_lusgs(c, inner_rk, 0.0, dt, 1); }
+// BDF2_stage, or with euler backwardEuler_stage (no time levels, phi = 0)
+static int implicit_stage(rc_ctx* c, int istep, double dt, int inner_loop, double rel_tol, int* inner_done,
+                          int euler) {
   if (!c || istep < 1 || inner_loop < 1 || !(dt > 0.0)) return RC_ERR_ARG;
   RC_NSP_OK(c);
   if (int st = bdf2_setup(c)) return st;
   const size_t bytes = sizeof(double) * (size_t)c->V * c->NE;
-  double phi;
-  if (istep == 1) {
+  double phi = 0.;
+  if (euler) {
+  } else if (istep == 1) {
     RC_CU(cudaMemcpyAsync(c->d.WP, c->d.WA, bytes, cudaMemcpyDeviceToDevice, c->stream));
     RC_CU(cudaMemcpyAsync(c->d.WP2, c->d.WP, bytes, cudaMemcpyDeviceToDevice, c->stream));
     phi = 0.;
@@ -2234,7 +2247,7 @@ int rc_bdf2_stage(rc_ctx* c, int istep, double dt, int inner_loop, double rel_to
     phi = 0.5;
   }
   if (int st = bdf2_params(c, dt, phi)) return st;
-  RC_DISPATCH(c, bdf2_fixed, c->d, c->d.bs, c->stream);
+  RC_DISPATCH(c, bdf2_fixed, c->d, c->d.bs, euler, c->stream);
   c->launches++;
   if (!c->bdf2_graph) {
     cudaGraph_t gph;
@@ -2273,6 +2286,12 @@ int rc_bdf2_stage(rc_ctx* c, int istep, double dt, int inner_loop, double rel_to
   if (inner_done) *inner_done = inner > inner_loop ? inner_loop : inner;
   if (int st = check_launch(c, "rc_bdf2_stage")) return st;
   return latch(c);
+}
+int rc_bdf2_stage(rc_ctx* c, int istep, double dt, int inner_loop, double rel_tol, int* inner_done) {
+  return implicit_stage(c, istep, dt, inner_loop, rel_tol, inner_done, 0);
+}
+int rc_euler_stage(rc_ctx* c, int istep, double dt, int inner_loop, double rel_tol, int* inner_done) {
+  return implicit_stage(c, istep, dt, inner_loop, rel_tol, inner_done, 1);
 }
 
 int rc_stats(rc_ctx* c, long long* launches, int* fwd, int* bwd) {

@@ -161,7 +161,7 @@ struct rc_case {
   double unit = 1, cfl = 0, p_out_ratio = 0, p_out = 0;
   // unsteady dual-time BDF2 (implicit_time_method 5)
   bool steady = true;
-  int inner_loop = 1;
+  int inner_loop = 1, method = 5;
   double totaltime = 0, rel_tol = 0, A_p = 0, f_p = 0, p_static = 0, ttime = 0, dt = 0;
   // module arrays, Fortran layout, 1-based ids
   int NE = 0, NF = 0, NNT = 0, MaxNei = 0, Ng = 0;
@@ -287,7 +287,7 @@ void rc_case::read_inputs() {
     viscous = Records::logical(f[1]);
     backup = Records::logical(f[2]);
     bool expl = Records::logical(f[3]);
-    r.skip(); const long method = r.integer();
+    r.skip(); method = (int)r.integer();
     r.skip();
     auto g = r.take(5);
     cfl = num(g[0]);
@@ -310,8 +310,9 @@ void rc_case::read_inputs() {
     p_out_ratio = num(po[0]);
     A_p = num(po[1]);
     f_p = num(po[2]);
-    if (expl || right || npar != 1 || (!steady && method != 5))
-      throw std::runtime_error("the GPU path covers the steady implicit and the unsteady BDF2 single-partition solver");
+    if (expl || right || npar != 1 || (!steady && method != 5 && method != 3))
+      throw std::runtime_error(
+          "the GPU path covers the steady implicit and the unsteady BDF2 / backward Euler single-partition solver");
     if (steady) inner_loop = 1;                    // initParam.f90:220-222
     else dt = totaltime / (double)nstep;           // initParam.f90:72
   }
@@ -870,7 +871,7 @@ int rc_case_unsteady(const rc_case* c, double* out) {
   if (!c || !out) return RC_ERR_ARG;
   out[0] = c->steady ? 0.0 : 1.0; out[1] = c->ttime; out[2] = c->dt; out[3] = c->totaltime;
   out[4] = (double)c->nstep; out[5] = c->inner_loop; out[6] = c->rel_tol; out[7] = c->p_static;
-  out[8] = c->A_p; out[9] = c->f_p;
+  out[8] = c->A_p; out[9] = c->f_p; out[10] = c->method;
   return RC_OK;
 }
 
@@ -881,7 +882,7 @@ static double case_p_out(const rc_case* c, double ttime) {
 }
 
 // The unsteady implicit branch of program main (fvm2d.f90:48-150) with the
-// BDF2 stage: per physical step the last step is shortened to end at
+// BDF2 or backward Euler stage (implicit_time_method 5 or 3): per physical step the last step is shortened to end at
 // totaltime (:52-56), ttime and p_out advance around the stage, and the loop
 // ends after that last step.
 int rc_run_unsteady(rc_case* c, int device, long nsteps, long every, double* hist, int* inner) {
@@ -905,7 +906,9 @@ int rc_run_unsteady(rc_case* c, int device, long nsteps, long every, double* his
     c->p_out = case_p_out(c, c->ttime);
     st = rc_set_p_out(ctx, &c->p_out);
     int n_inner = 0;
-    if (!st) st = rc_bdf2_stage(ctx, (int)istep, c->dt, c->inner_loop, c->rel_tol, &n_inner);
+    if (!st)
+      st = c->method == 3 ? rc_euler_stage(ctx, (int)istep, c->dt, c->inner_loop, c->rel_tol, &n_inner)
+                          : rc_bdf2_stage(ctx, (int)istep, c->dt, c->inner_loop, c->rel_tol, &n_inner);
     if (inner) inner[istep - 1] = n_inner;
     c->ttime = ttime_n + c->dt;
     c->p_out = case_p_out(c, c->ttime);

@@ -764,6 +764,9 @@ int rc_mlp_create(int device, rc_mlp** out) {
   cudaMemset(m->m1, 0, P * sizeof(float));
   cudaMemset(m->m2, 0, P * sizeof(float));
   cudaMemset(m->derr, 0, sizeof(unsigned));
+  // the fills run on the legacy stream; the network's kernels may run on
+  // non-blocking streams, which are not ordered after it
+  if (cudaDeviceSynchronize() != cudaSuccess) return bail(RC_ERR_CUDA);
   for (int i = 0; i < mlp::NIN; ++i) { m->norm.mean[i] = 0.f; m->norm.stdv[i] = 1.f; }
   const float dom[6] = {300.f, 6000.f, 1.0e2f, 2.0e7f, 1.0e-10f, 1.0e-4f};
   for (int i = 0; i < 6; ++i) m->norm.dom[i] = dom[i];

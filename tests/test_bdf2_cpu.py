@@ -1,4 +1,4 @@
-"""The unsteady dual-time BDF2 scheme on the CPU oracle (no GPU).
+"""The unsteady dual-time BDF2 and backward Euler schemes on the CPU oracle (no GPU).
 
 The reference solves each cell's system of its BDF2 sweeps with LAPACK's
 dgesvx (advanced_linear_solve_lapack, la_math.f90:120-215).  The oracle
@@ -79,11 +79,11 @@ def test_dgesvx_on_the_bdf2_cell_matrices(case_root):
         assert info == 0
 
 
-@pytest.mark.parametrize("name", ["t2u", "t1u"])
+@pytest.mark.parametrize("name", ["t2u", "t1u", "t2u_euler"])
 def test_serial_and_level_scheduled_bdf2_agree_bitwise(case_root, name):
-    over = {} if name == "t2u" else {"unsteady": True, "inner_loop": 4, "rel_tol": 1e-3, "totaltime": 1e-3,
-                                     "nstep": 100000}
-    d = make_case(case_root, "t2u" if name == "t2u" else "t1", **over)
+    over = {"t2u": {}, "t2u_euler": {"time_method": 3},
+            "t1u": {"unsteady": True, "inner_loop": 4, "rel_tol": 1e-3, "totaltime": 1e-3, "nstep": 100000}}[name]
+    d = make_case(case_root, "t1" if name == "t1u" else "t2u", **over)
     out = []
     for th in (1, 4):
         o = oracle.Oracle(d, threads=th)
@@ -105,14 +105,17 @@ def test_fluid_at_rest_stays_at_rest(case_root):
     assert dev[1] <= 1e-9 and dev[2] <= 1e-9  # m/s, from rest
 
 
-def test_tiny_step_moves_the_state_by_dt_times_the_residual(case_root):
-    """BDF2 with phi = 0 is implicit Euler in physical time: for dt much below
-    the pseudo time steps, (U1 - U0) vol / dt -> R(U0), the residual of
-    flux_sourceterm."""
+@pytest.mark.parametrize("method", [5, 3])
+def test_tiny_step_moves_the_state_by_dt_times_the_residual(case_root, method):
+    """The first BDF2 step (phi = 0) and every backward Euler step are implicit
+    Euler in physical time: for dt much below the pseudo time steps,
+    (U1 - U0) vol / dt -> R(U0), the residual of flux_sourceterm."""
     dt = 1e-12
-    d = make_case(case_root, "t2u", totaltime=dt * 1e5, nstep=100000, inner_loop=6, rel_tol=1e-12)
+    d = make_case(case_root, "t2u", totaltime=dt * 1e5, nstep=100000, inner_loop=6, rel_tol=1e-12,
+                  time_method=method)
     o = oracle.Oracle(d)
     assert o.unsteady()["dt"] == pytest.approx(dt, rel=1e-12)
+    assert o.unsteady()["method"] == method
     WA0 = o.array("WA").copy()
     o.call("timestep"); o.call("reconstruction"); o.call("flux_sourceterm")
     R0 = o.array("hWA").copy()
@@ -140,3 +143,17 @@ def test_last_step_ends_at_totaltime(case_root):
     stops = [o.unsteady_step(i)[1] for i in (1, 2, 3)]
     assert stops == [False, False, True]
     assert o.unsteady()["ttime"] == pytest.approx(3.0e-8, rel=1e-12)
+
+
+def test_euler_differs_from_bdf2_only_after_the_first_step(case_root):
+    """Step 1 of BDF2 has phi = 0 and WP = WA: the backward Euler step; from
+    step 2 on the schemes differ."""
+    runs = {}
+    for m in (5, 3):
+        o = oracle.Oracle(make_case(case_root, "t2u", time_method=m))
+        o.unsteady_step(1)
+        s1 = o.array("WA").copy()
+        o.unsteady_step(2)
+        runs[m] = (s1, o.array("WA").copy())
+    assert np.array_equal(runs[5][0], runs[3][0])
+    assert not np.array_equal(runs[5][1], runs[3][1])

@@ -1,4 +1,4 @@
-"""GPU parity of the unsteady dual-time BDF2 stage with the CPU oracle (needs a GB300).
+"""GPU parity of the unsteady dual-time BDF2 and backward Euler stages with the CPU oracle (needs a GB300).
 
 BDF2_LU_SGS (Time_BDF2.f90:73-337) keeps the reference's operation order on
 the device, including the per-cell dgesvx steps (equilibration, LU with
@@ -53,7 +53,8 @@ def test_bdf2_lusgs_bit_identical_to_oracle(case_root, name, over):
 
 
 @pytest.mark.parametrize("name,over", [("t2u", {}), ("t1", T1U), ("t2u", {"order": "colored"}),
-                                       ("t2u", {"a_p": 0.05, "f_p": 2.0e6})])
+                                       ("t2u", {"a_p": 0.05, "f_p": 2.0e6}), ("t2u", {"time_method": 3}),
+                                       ("t1", {**T1U, "time_method": 3})])
 def test_unsteady_steps_bit_identical_to_oracle(case_root, name, over):
     """Ten physical steps of the driver (time advance, compute_p_out,
     BDF2_stage) against the oracle's; the last case has a moving exit
@@ -101,3 +102,19 @@ def test_bdf2_rejects_what_it_does_not_cover(case_root):
     steady = rc.Case(make_case(case_root, "t2"))
     with pytest.raises(rc.RcError):
         steady.run_unsteady(1)
+
+
+def test_euler_lusgs_bit_identical_to_oracle(case_root):
+    d = make_case(case_root, "t2u", time_method=3)
+    c = rc.Case(d)
+    s = rc.Solver(c)
+    o = oracle.Oracle(d, threads=4)
+    dt = o.unsteady()["dt"]
+    for inner in (1, 2):
+        _assemble(s, o)
+        assert o.euler_lusgs(inner) == 0
+        s.euler_lusgs(inner, dt)
+        s.sync()
+        assert np.array_equal(s.get_array("hWA"), o.array("hWA")), inner
+        PA, WA = s.get_state()
+        assert np.array_equal(PA, o.array("PA")) and np.array_equal(WA, o.array("WA")), inner
