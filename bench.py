@@ -52,7 +52,10 @@ def algo_bytes_per_cell(V: int, nf_ne: float, viscous: bool, combustion: bool) -
 # DRAM bytes per cell of one launch of the dominant kernel of each subroutine
 # (dram__bytes_read.sum + dram__bytes_write.sum over the 30,000 cells of the
 # capture in profiles/kernels_c2_30k_full.md; the traffic grows with the cells)
-NCU_DRAM_PER_CELL = {"lu_sgs_steady": (10.29e6 + 0.48e6) / 30000, "flux_sourceterm": 10.61e6 / 30000}
+# DRAM bytes per cell of one FP64 iteration of the 120,000-cell nozzle (ncu,
+# --cache-control none: the caches as the live run leaves them; profiles/)
+NCU_DRAM_PER_CELL = {"lu_sgs_steady": (23588864 + 12020224 + 6755328 + 3684096) / 120000,
+                     "flux_sourceterm": (19888128 + 26114816 + 2120704 + 5835520) / 120000}
 
 
 def read_peaks():
@@ -292,7 +295,8 @@ def main():
                          "frac": achieved / peak, "peak_source": peak_kind,
                          "algorithmic_bytes_per_cell": ab[dom],
                          "traffic": NCU_DRAM_PER_CELL[dom] * NE if dom in NCU_DRAM_PER_CELL else None,
-                         "traffic_source": "ncu capture at 30,000 cells scaled by cells (profiles/)",
+                         "traffic_source": "ncu capture of one iteration at 120,000 cells, caches as in the "
+                                           "live run (profiles/c2_fp64_launches.md), scaled by cells",
                          "note": "LU-SGS is latency bound on its level barriers (natural cell order: 301+301 "
                                  "levels); the face and cell kernels are FP64-issue bound (FP64 pipe 85-88%, "
                                  "DRAM < 2%)"},
