@@ -664,12 +664,66 @@ __device__ __forceinline__ void sweep_compute(const Dev& d, const ThermoDev<NSP>
   if (q + 4 < V)
     d.hWA[(q + 4) * NE + p.i] = FWD ? div_rn(R1 - df1, ddi, p.ddh, p.ddl) : R1 - div_rn(df1, ddi, p.ddh, p.ddl);
 }
+// The terms of one face slot split in two parts: the terms that need dp (c1,
+// c2, c3; dpart) or the others (c0, c4..); both parts compute the velocity
+// increments they share.  The same expressions in the same order as
+// sweep_compute, so the same bits.
+template <int NSP>
+__device__ __forceinline__ void sweep_terms(const Dev& d, const ThermoDev<NSP>& th, const SweepPre<NSP>& p,
+                                            bool dpart, double* c) {
+  constexpr int V = 3 + NSP;
+  const int NE = d.NE;
+#pragma unroll
+  for (int k = 0; k < V; ++k) c[k] = 0.0;
+  if (!p.act) return;
+  const int j = p.j;
+  const double dx = p.dx, dy = p.dy, uu = p.uu, vv = p.vv, rr = p.rr;
+  const double drr = d.hWA[0 * NE + j], dru = d.hWA[1 * NE + j], drv = d.hWA[2 * NE + j];
+  double dry[NSP], s = 0.0;
+#pragma unroll
+  for (int k = 0; k < NSP - 1; ++k) { dry[k] = d.hWA[(4 + k) * NE + j]; s = s + dry[k]; }
+  dry[NSP - 1] = drr - s;
+  const double duu = div_rn(dru - uu * drr, rr, p.rrh, p.rrl);
+  const double dvv = div_rn(drv - vv * drr, rr, p.rrh, p.rrl);
+  const double unormal = p.unormal;
+  const double dunormal = duu * dx + dvv * dy;
+  const double aF = p.aF;
+  if (dpart) {
+    const double dre = d.hWA[3 * NE + j], tt = p.tt, gama = p.gama, rou = p.rou, rov = p.rov;
+    double s1 = 0.0, s2 = 0.0;
+#pragma unroll
+    for (int k = 0; k < NSP; ++k) s1 = s1 + p.cs[k] * dry[k];
+#pragma unroll
+    for (int k = 0; k < NSP; ++k) s2 = s2 + th.R[k] * dry[k];
+    const double gm1 = p.gm1;
+    const double dpp = gm1 * (dre - s1 + div_rn(tt * s2 * gama, gm1, p.gmh, p.gml) -
+                              0.5 * (dru * uu + duu * rou + drv * vv + dvv * rov));
+    c[1] = 0.5 * (-aF * dru + dru * unormal + rou * dunormal + dpp * dx);
+    c[2] = 0.5 * (-aF * drv + drv * unormal + rov * dunormal + dpp * dy);
+    c[3] = 0.5 * (-aF * dre + dunormal * p.roepp + unormal * (dre + dpp));
+  } else {
+    c[0] = 0.5 * (-aF * drr + dru * dx + drv * dy);
+#pragma unroll
+    for (int k = 0; k < NSP - 1; ++k) c[4 + k] = 0.5 * (-aF * dry[k] + dry[k] * unormal + p.ry[k] * dunormal);
+  }
+}
+// write a part's terms of slot q into the cell's [k][slot] scratch
+template <int NSP>
+__device__ __forceinline__ void sweep_put(double* w, bool dpart, int q, const double* c) {
+  constexpr int V = 3 + NSP;
+  if (dpart) {
+#pragma unroll
+    for (int k = 1; k < 4; ++k) w[k * 4 + q] = c[k];
+  } else {
+    w[q] = c[0];
+#pragma unroll
+    for (int k = 4; k < V; ++k) w[k * 4 + q] = c[k];
+  }
+}
 // The same cell step with 8 lanes per cell: lanes r = 0..3 (slot r) form the
-// terms that need dp (c1, c2, c3), lanes r = 4..7 (slot r-4) the others (c0,
-// c4..); both compute the velocity increments they share.  Then lane r adds
-// variable r over the 4 slots in slot order and divides.  The same
-// expressions in the same order as sweep_compute, so the same bits, with
-// about a third fewer FP64 instructions per lane.  wsm: 4 cells x V x 4 slots.
+// dp part, lanes r = 4..7 (slot r-4) the other part; then lane r adds
+// variable r over the 4 slots in slot order and divides.  wsm: 4 cells x V x
+// 4 slots.
 template <int NSP, bool FWD>
 __device__ __forceinline__ void sweep_compute8(const Dev& d, const ThermoDev<NSP>& th, const SweepPre<NSP>& p,
                                                int r, int cell, double* wsm) {
@@ -679,50 +733,10 @@ __device__ __forceinline__ void sweep_compute8(const Dev& d, const ThermoDev<NSP
   double R = 0.0;
   if (p.valid && r < V) R = d.hWA[r * NE + p.i];
   double c[V];
-#pragma unroll
-  for (int k = 0; k < V; ++k) c[k] = 0.0;
-  if (p.act) {
-    const int j = p.j;
-    const double dx = p.dx, dy = p.dy, uu = p.uu, vv = p.vv, rr = p.rr;
-    const double drr = d.hWA[0 * NE + j], dru = d.hWA[1 * NE + j], drv = d.hWA[2 * NE + j];
-    double dry[NSP], s = 0.0;
-#pragma unroll
-    for (int k = 0; k < NSP - 1; ++k) { dry[k] = d.hWA[(4 + k) * NE + j]; s = s + dry[k]; }
-    dry[NSP - 1] = drr - s;
-    const double duu = div_rn(dru - uu * drr, rr, p.rrh, p.rrl);
-    const double dvv = div_rn(drv - vv * drr, rr, p.rrh, p.rrl);
-    const double unormal = p.unormal;
-    const double dunormal = duu * dx + dvv * dy;
-    const double aF = p.aF;
-    if (dpart) {
-      const double dre = d.hWA[3 * NE + j], tt = p.tt, gama = p.gama, rou = p.rou, rov = p.rov;
-      double s1 = 0.0, s2 = 0.0;
-#pragma unroll
-      for (int k = 0; k < NSP; ++k) s1 = s1 + p.cs[k] * dry[k];
-#pragma unroll
-      for (int k = 0; k < NSP; ++k) s2 = s2 + th.R[k] * dry[k];
-      const double gm1 = p.gm1;
-      const double dpp = gm1 * (dre - s1 + div_rn(tt * s2 * gama, gm1, p.gmh, p.gml) -
-                                0.5 * (dru * uu + duu * rou + drv * vv + dvv * rov));
-      c[1] = 0.5 * (-aF * dru + dru * unormal + rou * dunormal + dpp * dx);
-      c[2] = 0.5 * (-aF * drv + drv * unormal + rov * dunormal + dpp * dy);
-      c[3] = 0.5 * (-aF * dre + dunormal * p.roepp + unormal * (dre + dpp));
-    } else {
-      c[0] = 0.5 * (-aF * drr + dru * dx + drv * dy);
-#pragma unroll
-      for (int k = 0; k < NSP - 1; ++k) c[4 + k] = 0.5 * (-aF * dry[k] + dry[k] * unormal + p.ry[k] * dunormal);
-    }
-  }
+  sweep_terms<NSP>(d, th, p, dpart, c);
   double* w = wsm + cell * V * 4;  // [k][slot]
   __syncwarp();
-  if (dpart) {
-#pragma unroll
-    for (int k = 1; k < 4; ++k) w[k * 4 + q] = c[k];
-  } else {
-    w[q] = c[0];
-#pragma unroll
-    for (int k = 4; k < V; ++k) w[k * 4 + q] = c[k];
-  }
+  sweep_put<NSP>(w, dpart, q, c);
   __syncwarp();
   if (!p.valid || r >= V) return;
   double df = 0.0;
@@ -752,6 +766,127 @@ __global__ void __launch_bounds__(32) k_sweep8(const Dev d, const ThermoDev<NSP>
   const SweepPre<NSP> p = sweep_load<NSP, FWD>(d, t0 + blockIdx.x * 4 + cell, t1, r & 3);
   pdl_wait();
   sweep_compute8<NSP, FWD>(d, th, p, r, cell, wsm);
+}
+// one level with the two parts of each slot in two warps (two SM sub-partitions,
+// each with its own FP64 pipe): block b (64 threads) takes cells t0 + 8b .. + 7;
+// warp 0 forms the dp part of every slot of the 8 cells (lane = 4 cell + slot),
+// warp 1 the other part; after a block barrier warp h finishes cells 4h .. 4h+3
+// (8 lanes per cell, lane r adds variable r over the slots and divides).  On
+// GB300 a warp's FP64 instruction occupies its sub-partition's FP64 pipe for
+// 64 cycles whatever its active lanes, so the per-warp instruction count sets
+// the level's time: the split cuts it by the other part's share.
+template <int NSP, bool FWD>
+__global__ void __launch_bounds__(64) k_sweep2w(const Dev d, const ThermoDev<NSP> th, int t0, int t1) {
+  constexpr int V = 3 + NSP, DIR = FWD ? 0 : 1;
+  pdl_launch_dependents();
+  const int NE = d.NE, role = threadIdx.x >> 5, lane = threadIdx.x & 31, cell = lane >> 2, q = lane & 3;
+  __shared__ double wsm[8 * V * 4];
+  const SweepPre<NSP> p = sweep_load<NSP, FWD>(d, t0 + blockIdx.x * 8 + cell, t1, q);
+  const int fcell = role * 4 + (lane >> 3), r = lane & 7, ft = t0 + blockIdx.x * 8 + fcell;
+  const bool fvalid = ft < t1 && r < V;
+  const int fi = fvalid ? d.swi[DIR][ft] : 0;
+  double fdd = 1.0, fddh = 1.0, fddl = 0.0;
+  if (fvalid) { fdd = d.dd[fi]; fddh = d.rcp[4 * NE + fi]; fddl = d.rcp[5 * NE + fi]; }
+  pdl_wait();
+  const double R = fvalid ? d.hWA[r * NE + fi] : 0.0;
+  double c[V];
+  sweep_terms<NSP>(d, th, p, role == 0, c);
+  sweep_put<NSP>(wsm + cell * V * 4, role == 0, q, c);
+  __syncthreads();
+  if (!fvalid) return;
+  const double* w = wsm + fcell * V * 4;
+  double df = 0.0;
+#pragma unroll
+  for (int sl = 0; sl < 4; ++sl) df = df + w[r * 4 + sl];
+  d.hWA[r * NE + fi] = FWD ? div_rn(R - df, fdd, fddh, fddl) : R - div_rn(df, fdd, fddh, fddl);
+}
+// named barrier over the first `count` threads of the block (warp multiples)
+__device__ __forceinline__ void bar_named(int id, int count) {
+  asm volatile("bar.sync %0, %1;" ::"r"(id), "r"(count) : "memory");
+}
+// one level with the work of each slot in four warps (the four SM
+// sub-partitions, each with its own FP64 pipe): block b (128 threads) takes
+// cells t0 + 8b .. + 7, lane = 4 cell + slot in every warp.
+//   warp 0: s1 = sum h_k dY_k              then c1
+//   warp 1: s2 = sum R_k dY_k, Q = T s2 gamma / (gamma-1)   then c2
+//   warp 2: X = du u + du rho u + dv v + dv rho v, dp = (gamma-1)((dE - s1 + Q) - X/2)   then c3
+//   warp 3: c0 and the species terms
+// with the velocity increments formed in every warp; warps 0 and 1 then
+// finish cells 0-3 and 4-7 (8 lanes per cell).  Every expression is the one
+// of sweep_terms in the same order, so the same bits; the longest warp chain
+// is about two thirds of k_sweep2w's.
+template <int NSP, bool FWD>
+__global__ void __launch_bounds__(128) k_sweep4w(const Dev d, const ThermoDev<NSP> th, int t0, int t1) {
+  constexpr int V = 3 + NSP, DIR = FWD ? 0 : 1;
+  pdl_launch_dependents();
+  const int NE = d.NE, role = threadIdx.x >> 5, lane = threadIdx.x & 31, cell = lane >> 2, q = lane & 3;
+  __shared__ double wsm[8 * V * 4];
+  __shared__ double xs1[32], xq[32], xdp[32];
+  const SweepPre<NSP> p = sweep_load<NSP, FWD>(d, t0 + blockIdx.x * 8 + cell, t1, q);
+  const int fcell = (role & 1) * 4 + (lane >> 3), r = lane & 7, ft = t0 + blockIdx.x * 8 + fcell;
+  const bool fvalid = role < 2 && ft < t1 && r < V;
+  const int fi = fvalid ? d.swi[DIR][ft] : 0;
+  double fdd = 1.0, fddh = 1.0, fddl = 0.0;
+  if (fvalid) { fdd = d.dd[fi]; fddh = d.rcp[4 * NE + fi]; fddl = d.rcp[5 * NE + fi]; }
+  pdl_wait();
+  const double R = fvalid ? d.hWA[r * NE + fi] : 0.0;
+  double* w = wsm + cell * V * 4;
+  double drr = 0, dru = 0, drv = 0, dre = 0, duu = 0, dvv = 0, dunormal = 0, X = 0, dry[NSP];
+#pragma unroll
+  for (int k = 0; k < NSP; ++k) dry[k] = 0.0;
+  const double aF = p.aF, unormal = p.unormal;
+  if (p.act) {
+    const int j = p.j;
+    drr = d.hWA[0 * NE + j]; dru = d.hWA[1 * NE + j]; drv = d.hWA[2 * NE + j]; dre = d.hWA[3 * NE + j];
+    double s = 0.0;
+#pragma unroll
+    for (int k = 0; k < NSP - 1; ++k) { dry[k] = d.hWA[(4 + k) * NE + j]; s = s + dry[k]; }
+    dry[NSP - 1] = drr - s;
+    duu = div_rn(dru - p.uu * drr, p.rr, p.rrh, p.rrl);
+    dvv = div_rn(drv - p.vv * drr, p.rr, p.rrh, p.rrl);
+    dunormal = duu * p.dx + dvv * p.dy;
+    if (role == 0) {
+      double s1 = 0.0;
+#pragma unroll
+      for (int k = 0; k < NSP; ++k) s1 = s1 + p.cs[k] * dry[k];
+      xs1[q + 4 * cell] = s1;
+    } else if (role == 1) {
+      double s2 = 0.0;
+#pragma unroll
+      for (int k = 0; k < NSP; ++k) s2 = s2 + th.R[k] * dry[k];
+      xq[q + 4 * cell] = div_rn(p.tt * s2 * p.gama, p.gm1, p.gmh, p.gml);
+    } else if (role == 2) {
+      X = dru * p.uu + duu * p.rou + drv * p.vv + dvv * p.rov;
+    } else {
+      w[q] = 0.5 * (-aF * drr + dru * p.dx + drv * p.dy);
+#pragma unroll
+      for (int k = 0; k < NSP - 1; ++k) w[(4 + k) * 4 + q] = 0.5 * (-aF * dry[k] + dry[k] * unormal + p.ry[k] * dunormal);
+    }
+  } else if (role == 3) {
+#pragma unroll
+    for (int k = 0; k < V; ++k)
+      if (k == 0 || k >= 4) w[k * 4 + q] = 0.0;
+  }
+  if (role < 3) {
+    bar_named(1, 96);
+    if (role == 2 && p.act) xdp[q + 4 * cell] = p.gm1 * (dre - xs1[q + 4 * cell] + xq[q + 4 * cell] - 0.5 * X);
+    bar_named(2, 96);
+    const double dpp = xdp[q + 4 * cell];
+    double ck = 0.0;
+    if (p.act) {
+      if (role == 0) ck = 0.5 * (-aF * dru + dru * unormal + p.rou * dunormal + dpp * p.dx);
+      else if (role == 1) ck = 0.5 * (-aF * drv + drv * unormal + p.rov * dunormal + dpp * p.dy);
+      else ck = 0.5 * (-aF * dre + dunormal * p.roepp + unormal * (dre + dpp));
+    }
+    w[(1 + role) * 4 + q] = ck;
+  }
+  __syncthreads();
+  if (!fvalid) return;
+  const double* wf = wsm + fcell * V * 4;
+  double df = 0.0;
+#pragma unroll
+  for (int sl = 0; sl < 4; ++sl) df = df + wf[r * 4 + sl];
+  d.hWA[r * NE + fi] = FWD ? div_rn(R - df, fdd, fddh, fddl) : R - div_rn(df, fdd, fddh, fddl);
 }
 template <int NSP, bool FWD>
 __global__ void __launch_bounds__(32) k_sweep4(const Dev d, const ThermoDev<NSP> th, int t0, int t1) {
@@ -942,7 +1077,8 @@ struct rc_ctx {
   std::vector<int> fwd_off, bwd_off;
   bool persistent = true;       // LU-SGS sweeps as one cooperative launch (else one launch per level)
   bool can_persistent = false;  // the device can co-schedule the persistent LU-SGS grid
-  bool wide = false;            // FP64 per-level sweeps with 8 lanes per cell (k_sweep8)
+  int wide = 0;                 // FP64 per-level sweeps: 4 lanes per cell (0), 8 lanes (1, k_sweep8),
+                                // the two parts of a slot in two warps (2, k_sweep2w) or four (3, k_sweep4w)
   int pers_grid = 0;             // blocks of the persistent launch (one per SM)
   unsigned* lvl_count = nullptr; // per-level completion counters of the persistent launch
   int nlevels = 0;
@@ -1120,16 +1256,24 @@ void q_sweeps(rc_ctx* c, int gather) {
   if (c->persistent) { q_persistent<NSP>(c); return; }
   for (size_t l = 0; l + 1 < c->fwd_off.size(); ++l) {
     const int n = c->fwd_off[l + 1] - c->fwd_off[l];
-    if (c->wide) launch_pdl(k_sweep8<NSP, true>, blocks(n, 4), 32, c->stream, c->d, TH<NSP>(c), c->fwd_off[l],
-                            c->fwd_off[l + 1]);
+    if (c->wide == 3) launch_pdl(k_sweep4w<NSP, true>, blocks(n, 8), 128, c->stream, c->d, TH<NSP>(c),
+                                 c->fwd_off[l], c->fwd_off[l + 1]);
+    else if (c->wide == 2) launch_pdl(k_sweep2w<NSP, true>, blocks(n, 8), 64, c->stream, c->d, TH<NSP>(c),
+                                      c->fwd_off[l], c->fwd_off[l + 1]);
+    else if (c->wide) launch_pdl(k_sweep8<NSP, true>, blocks(n, 4), 32, c->stream, c->d, TH<NSP>(c),
+                                 c->fwd_off[l], c->fwd_off[l + 1]);
     else launch_pdl(k_sweep4<NSP, true>, blocks(n, c->d.cpw), 32, c->stream, c->d, TH<NSP>(c), c->fwd_off[l],
                     c->fwd_off[l + 1]);
     c->launches++;
   }
   for (size_t l = 0; l + 1 < c->bwd_off.size(); ++l) {
     const int n = c->bwd_off[l + 1] - c->bwd_off[l];
-    if (c->wide) launch_pdl(k_sweep8<NSP, false>, blocks(n, 4), 32, c->stream, c->d, TH<NSP>(c), c->bwd_off[l],
-                            c->bwd_off[l + 1]);
+    if (c->wide == 3) launch_pdl(k_sweep4w<NSP, false>, blocks(n, 8), 128, c->stream, c->d, TH<NSP>(c),
+                                 c->bwd_off[l], c->bwd_off[l + 1]);
+    else if (c->wide == 2) launch_pdl(k_sweep2w<NSP, false>, blocks(n, 8), 64, c->stream, c->d, TH<NSP>(c),
+                                      c->bwd_off[l], c->bwd_off[l + 1]);
+    else if (c->wide) launch_pdl(k_sweep8<NSP, false>, blocks(n, 4), 32, c->stream, c->d, TH<NSP>(c),
+                                 c->bwd_off[l], c->bwd_off[l + 1]);
     else launch_pdl(k_sweep4<NSP, false>, blocks(n, c->d.cpw), 32, c->stream, c->d, TH<NSP>(c), c->bwd_off[l],
                     c->bwd_off[l + 1]);
     c->launches++;
@@ -1770,9 +1914,10 @@ int init_impl(const rc_mesh* m, const rc_thermo* t, const rc_config* g, const Ba
     const char* sched = std::getenv("RC_LUSGS_SCHEDULE");
     c->pers_grid = nsm;
     c->can_persistent = coop && nsm > 0 && occ64 >= 1 && occ32 >= 1;
-    const bool lv = sched && (std::string(sched) == "levels" || std::string(sched) == "levels8");
+    const std::string sc = sched ? sched : "";
+    const bool lv = sc == "levels" || sc == "levels8" || sc == "levels2w" || sc == "levels4w";
     c->persistent = c->can_persistent && !lv;
-    c->wide = sched && std::string(sched) == "levels8";
+    c->wide = sc == "levels4w" ? 3 : sc == "levels2w" ? 2 : sc == "levels8" ? 1 : 0;
   }
   *out = c;
   return RC_OK;
@@ -1950,12 +2095,13 @@ int rc_autotune(rc_ctx* c, int iters, char* report, int report_len) {
   };
   cudaMemcpyAsync(save, c->d.PA, n * sizeof(double), cudaMemcpyDeviceToDevice, c->stream);
   cudaMemcpyAsync(save + n, c->d.WA, n * sizeof(double), cudaMemcpyDeviceToDevice, c->stream);
-  struct Cand { bool pers; int bs; int cpw; bool wide; };
+  struct Cand { bool pers; int bs; int cpw; int wide; };
   std::vector<Cand> cands;
   for (int pers = c->can_persistent ? 1 : 0; pers >= 0; --pers)
     for (int cpw : {8, 4, 2})
-      for (int bs : {128, 64}) cands.push_back({pers != 0, bs, cpw, false});
-  for (int bs : {128, 64}) cands.push_back({false, bs, 8, true});
+      for (int bs : {128, 64}) cands.push_back({pers != 0, bs, cpw, 0});
+  for (int wide : {1, 2, 3})
+    for (int bs : {128, 64}) cands.push_back({false, bs, 8, wide});
   cudaEvent_t e0, e1;
   cudaEventCreate(&e0);
   cudaEventCreate(&e1);
@@ -1979,8 +2125,9 @@ int rc_autotune(rc_ctx* c, int iters, char* report, int report_len) {
     float ms = 0.f;
     cudaEventElapsedTime(&ms, e0, e1);
     const double per = ms / iters;
-    rep += std::string(k.pers ? "persistent" : k.wide ? "levels8" : "levels") + " bs=" + std::to_string(k.bs) +
-           " cpw=" + std::to_string(k.wide ? 4 : k.cpw) + ": " + std::to_string(per) + " ms; ";
+    rep += std::string(k.pers ? "persistent" : k.wide == 3 ? "levels4w" : k.wide == 2 ? "levels2w" : k.wide ? "levels8" : "levels") +
+           " bs=" + std::to_string(k.bs) + " cpw=" + std::to_string(k.wide >= 2 ? 8 : k.wide ? 4 : k.cpw) + ": " +
+           std::to_string(per) + " ms; ";
     if (per < best) { best = per; bc = k; }
   }
   c->persistent = bc.pers;
@@ -1993,8 +2140,9 @@ int rc_autotune(rc_ctx* c, int iters, char* report, int report_len) {
   cudaEventDestroy(e0);
   cudaEventDestroy(e1);
   cudaFree(save);
-  rep += std::string("chosen: ") + (bc.pers ? "persistent" : bc.wide ? "levels8" : "levels") + " bs=" +
-         std::to_string(bc.bs) + " cpw=" + std::to_string(bc.wide ? 4 : bc.cpw);
+  rep += std::string("chosen: ") +
+         (bc.pers ? "persistent" : bc.wide == 3 ? "levels4w" : bc.wide == 2 ? "levels2w" : bc.wide ? "levels8" : "levels") +
+         " bs=" + std::to_string(bc.bs) + " cpw=" + std::to_string(bc.wide >= 2 ? 8 : bc.wide ? 4 : bc.cpw);
   if (report && report_len > 0) {
     std::snprintf(report, (size_t)report_len, "%s", rep.c_str());
   }

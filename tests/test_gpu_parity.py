@@ -166,12 +166,13 @@ def test_device_stop_condition_is_reported(case_t1):
 @pytest.mark.parametrize("precision", [rc.RC_PREC_FP64, rc.RC_PREC_MIXED])
 def test_persistent_and_per_level_schedules_agree(case_root, precision, monkeypatch):
     """The cooperative one-launch LU-SGS and the one-launch-per-level LU-SGS
-    (4 lanes per cell with 8 or 1 cells per warp, or 8 lanes per cell) run the
+    (4 lanes per cell with 8 or 1 cells per warp, 8 lanes per cell, or the work
+    of each slot split over two or four warps) run the
     same recurrences: identical states after 30 iterations."""
     d = make_case(case_root, "c1", nx=40, ny=8)
     c = rc.Case(d)
     states = []
-    for sched in ("persistent", "levels", "levels8"):
+    for sched in ("persistent", "levels", "levels8", "levels2w", "levels4w"):
         for cpw in ("8", "1"):
             monkeypatch.setenv("RC_LUSGS_SCHEDULE", sched)
             monkeypatch.setenv("RC_LUSGS_CPW", cpw)
