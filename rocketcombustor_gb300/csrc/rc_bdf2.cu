@@ -426,124 +426,179 @@ __global__ void __launch_bounds__(128) k_bdf2_prep(const Dev d, const ThermoDev<
   flag(d, err);
 }
 
+// What a sweep does not change, loaded before the wait for the previous level:
+// the face of slot q of the cell at level position t and its neighbour's gas
+// state (BSlot), and row r of the cell's factorised system (BRow).
+template <int NSP>
+struct BSlot {
+  int j;
+  bool act;
+  double dx, dy, aF, uu, vv, rr, rrc, rt, rct, rcth, rctl, unormal, rou, rov, rcp, hh, ek, roepp;
+  double ent[NSP], yy[NSP], ry[NSP];
+};
+template <int NSP, bool FWD>
+__device__ __forceinline__ BSlot<NSP> bslot_load(const Dev& d, int t, bool valid, int q) {
+  using namespace bdf2;
+  constexpr int DIR = FWD ? 0 : 1;
+  const int NE = d.NE, NF = d.NF;
+  BSlot<NSP> b;
+  b.j = valid ? d.swj[DIR][q * NE + t] : -1;
+  b.act = b.j >= 0;
+  b.dx = b.dy = b.aF = b.uu = b.vv = b.rr = b.rrc = b.rt = b.rct = b.rctl = b.unormal = 0.0;
+  b.rou = b.rov = b.rcp = b.hh = b.ek = b.roepp = 0.0;
+  b.rcth = 1.0;
+#pragma unroll
+  for (int k = 0; k < NSP; ++k) { b.ent[k] = 0.0; b.yy[k] = 0.0; b.ry[k] = 0.0; }
+  if (b.act) {
+    const int j = b.j, fs = d.swf[DIR][q * NE + t], f = fs >= 0 ? fs : ~fs;
+    b.dx = d.fvec[f];
+    b.dy = d.fvec[NF + f];
+    if (fs < 0) { b.dx = -b.dx; b.dy = -b.dy; }
+    b.aF = d.alpaF[f];
+    b.uu = d.PA[1 * NE + j];
+    b.vv = d.PA[2 * NE + j];
+    const double* nb = d.bnb;
+    b.rr = nb[NB_RR * NE + j]; b.rrc = nb[NB_RRC * NE + j]; b.rt = nb[NB_RT * NE + j]; b.rct = nb[NB_RCT * NE + j];
+    b.rcth = nb[nb_rct<NSP>() * NE + j]; b.rctl = nb[(nb_rct<NSP>() + 1) * NE + j];
+    b.unormal = b.uu * b.dx + b.vv * b.dy;
+    b.rou = nb[NB_ROU * NE + j];
+    b.rov = nb[NB_ROV * NE + j];
+    b.rcp = nb[NB_RCP * NE + j]; b.hh = nb[NB_HH * NE + j]; b.ek = nb[NB_EK * NE + j];
+    b.roepp = nb[NB_ROEPP * NE + j];
+#pragma unroll
+    for (int k = 0; k < NSP; ++k) b.ent[k] = nb[(NB_H + k) * NE + j];
+#pragma unroll
+    for (int k = 0; k < NSP - 1; ++k) {
+      b.yy[k] = d.PA[(4 + k) * NE + j];
+      b.ry[k] = nb[(nb_ry<NSP>() + k) * NE + j];
+    }
+  }
+  return b;
+}
+template <int NSP>
+struct BRow {
+  double arow[3 + NSP], lrow[3 + NSP], ukk[3 + NSP], urh[3 + NSP], url[3 + NSP], rsc, csc;
+  int src, equ;
+};
+template <int NSP>
+__device__ __forceinline__ BRow<NSP> brow_load(const Dev& d, int i, bool valid, int r) {
+  constexpr int V = 3 + NSP, RW = 2 * V + 4;
+  BRow<NSP> w;
+  w.rsc = 1.0; w.csc = 1.0; w.src = 0; w.equ = 0;
+#pragma unroll
+  for (int k = 0; k < V; ++k) { w.arow[k] = 0.0; w.lrow[k] = 0.0; w.ukk[k] = 1.0; w.urh[k] = 1.0; w.url[k] = 0.0; }
+  if (valid) {
+    const double* m = d.bmat + (size_t)i * V * RW;
+    if (r < V) {
+#pragma unroll
+      for (int k = 0; k < V; ++k) { w.arow[k] = m[r * RW + k]; w.lrow[k] = m[r * RW + V + k]; }
+      w.rsc = m[r * RW + 2 * V];
+      w.csc = m[r * RW + 2 * V + 1];
+      w.src = d.bperm[i * 8 + r];
+    }
+#pragma unroll
+    for (int k = 0; k < V; ++k) {
+      w.ukk[k] = m[k * RW + V + k];
+      w.urh[k] = m[k * RW + 2 * V + 2];
+      w.url[k] = m[k * RW + 2 * V + 3];
+    }
+    w.equ = d.bperm[i * 8 + 7];
+  }
+  return w;
+}
+// The flux difference of slot b's neighbour increment dP (Time_BDF2.f90:168-197),
+// rows 1-3 (lo) or rows 4.. (energy and species) of the slot's terms.
+template <int NSP>
+__device__ __forceinline__ void bslot_terms(const Dev& d, const ThermoDev<NSP>& th, const BSlot<NSP>& b, bool lo,
+                                            double* c) {
+  constexpr int V = 3 + NSP;
+  const int NE = d.NE;
+#pragma unroll
+  for (int k = 0; k < V; ++k) c[k] = 0.0;
+  if (!b.act) return;
+  const int j = b.j;
+  const double dpp = d.hWA[0 * NE + j], duu = d.hWA[1 * NE + j], dvv = d.hWA[2 * NE + j], dtt = d.hWA[3 * NE + j];
+  double dyy[NSP], s = 0.0;
+#pragma unroll
+  for (int k = 0; k < NSP - 1; ++k) { dyy[k] = d.hWA[(4 + k) * NE + j]; s = s + dyy[k]; }
+  dyy[NSP - 1] = -s;
+  double s1 = 0.0;
+#pragma unroll
+  for (int k = 0; k < NSP; ++k) s1 = s1 + th.R[k] * dyy[k];
+  const double drr = div_rn(dpp - b.rrc * dtt - b.rt * s1, b.rct, b.rcth, b.rctl);
+  const double dunormal = duu * b.dx + dvv * b.dy;
+  const double aF = b.aF, unormal = b.unormal, rr = b.rr;
+  if (lo) {
+    const double dru = rr * duu + b.uu * drr;
+    const double drv = rr * dvv + b.vv * drr;
+    c[0] = 0.5 * (-aF * drr + dru * b.dx + drv * b.dy);
+    c[1] = 0.5 * (-aF * dru + dru * unormal + b.rou * dunormal + dpp * b.dx);
+    c[2] = 0.5 * (-aF * drv + drv * unormal + b.rov * dunormal + dpp * b.dy);
+  } else {
+    double s2 = 0.0;
+#pragma unroll
+    for (int k = 0; k < NSP; ++k) s2 = s2 + b.ent[k] * dyy[k];
+    const double dre = b.rcp * dtt + rr * s2 + b.hh * drr + rr * (b.uu * duu + b.vv * dvv) + b.ek * drr - dpp;
+    c[3] = 0.5 * (-aF * dre + dunormal * b.roepp + unormal * (dre + dpp));
+#pragma unroll
+    for (int k = 0; k < NSP - 1; ++k) {
+      const double dry = rr * dyy[k] + b.yy[k] * drr;
+      c[4 + k] = 0.5 * (-aF * dry + dry * unormal + b.ry[k] * dunormal);
+    }
+  }
+}
+template <int NSP>
+__device__ __forceinline__ void bslot_put(double* w, bool lo, int q, const double* c) {
+  constexpr int V = 3 + NSP;
+  if (lo) {
+#pragma unroll
+    for (int k = 0; k < 3; ++k) w[k * 4 + q] = c[k];
+  } else {
+#pragma unroll
+    for (int k = 3; k < V; ++k) w[k * 4 + q] = c[k];
+  }
+}
+// the backward error of one refinement pass over a cell's rows (8 lanes):
+// max over the rows of |y| / w (or the guarded form), as a bit pattern
+template <int V>
+__device__ __forceinline__ long long berr_bits(double y, double wk, int r) {
+  using namespace bdf2;
+  const double safe1 = (V + 1) * SFMIN, safe2 = safe1 / EPS;
+  long long vb = 0;
+  if (r < V) vb = dbits((dbits(wk) > dbits(safe2)) ? fabs(y) / wk : (fabs(y) + safe1) / (wk + safe1));
+  vb = max(vb, (long long)__shfl_xor_sync(FULL, (unsigned long long)vb, 1));
+  vb = max(vb, (long long)__shfl_xor_sync(FULL, (unsigned long long)vb, 2));
+  vb = max(vb, (long long)__shfl_xor_sync(FULL, (unsigned long long)vb, 4));
+  return vb;
+}
+
 // One level of the forward (FWD) or backward sweep, cells t0..t1-1 of the
 // level order; eight lanes per cell, CPW cells per warp (one warp per block;
 // lanes of cell slots >= CPW only join the shuffles).
 template <int NSP, bool FWD, int CPW>
 __global__ void __launch_bounds__(32) k_bdf2_sweep(const Dev d, const ThermoDev<NSP> th, int t0, int t1) {
   using namespace bdf2;
-  constexpr int V = 3 + NSP, RW = 2 * V + 4, DIR = FWD ? 0 : 1;
+  constexpr int V = 3 + NSP, DIR = FWD ? 0 : 1;
   static_assert(V <= 7, "one lane per row and the flags in slot 7");
   pdl_launch_dependents();
   const int lane = threadIdx.x & 31, cell = lane >> 3, r = lane & 7, base = cell * 8;
   const int q = r & 3;
   const bool lo = r < 4;  // lanes 0-3 keep flux rows 1-3 of their slot, lanes 4-7 rows 4.. (energy, species)
-  const int NE = d.NE, NF = d.NF;
+  const int NE = d.NE;
   const int t = t0 + blockIdx.x * CPW + cell;
   const bool valid = cell < CPW && t < t1;
   const int i = valid ? d.swi[DIR][t] : 0;
-  // --- what the sweep does not change: the face of slot q and its neighbour's gas state
-  const int j = valid ? d.swj[DIR][q * NE + t] : -1;
-  const bool act = j >= 0;
-  double dx = 0, dy = 0, aF = 0, uu = 0, vv = 0, rr = 0, rrc = 0, rt = 0, rct = 0, rcth = 1, rctl = 0, unormal = 0;
-  double rou = 0, rov = 0, rcp = 0, hh = 0, ek = 0, roepp = 0, ent[NSP], yy[NSP], ry[NSP];
-#pragma unroll
-  for (int k = 0; k < NSP; ++k) { ent[k] = 0.0; yy[k] = 0.0; ry[k] = 0.0; }
-  if (act) {
-    const int fs = d.swf[DIR][q * NE + t], f = fs >= 0 ? fs : ~fs;
-    dx = d.fvec[f];
-    dy = d.fvec[NF + f];
-    if (fs < 0) { dx = -dx; dy = -dy; }
-    aF = d.alpaF[f];
-    uu = d.PA[1 * NE + j];
-    vv = d.PA[2 * NE + j];
-    const double* nb = d.bnb;
-    rr = nb[NB_RR * NE + j]; rrc = nb[NB_RRC * NE + j]; rt = nb[NB_RT * NE + j]; rct = nb[NB_RCT * NE + j];
-    rcth = nb[nb_rct<NSP>() * NE + j]; rctl = nb[(nb_rct<NSP>() + 1) * NE + j];
-    unormal = uu * dx + vv * dy;
-    rou = nb[NB_ROU * NE + j];
-    rov = nb[NB_ROV * NE + j];
-    rcp = nb[NB_RCP * NE + j]; hh = nb[NB_HH * NE + j]; ek = nb[NB_EK * NE + j]; roepp = nb[NB_ROEPP * NE + j];
-#pragma unroll
-    for (int k = 0; k < NSP; ++k) ent[k] = nb[(NB_H + k) * NE + j];
-#pragma unroll
-    for (int k = 0; k < NSP - 1; ++k) {
-      yy[k] = d.PA[(4 + k) * NE + j];
-      ry[k] = nb[(nb_ry<NSP>() + k) * NE + j];
-    }
-  }
-  // --- this lane's row of the cell's system
-  double arow[V], lrow[V], ukk[V], urh[V], url[V], rsc = 1.0, csc = 1.0;
-  int src = 0, equ = 0;
-#pragma unroll
-  for (int k = 0; k < V; ++k) { arow[k] = 0.0; lrow[k] = 0.0; ukk[k] = 1.0; urh[k] = 1.0; url[k] = 0.0; }
-  if (valid) {
-    const double* m = d.bmat + (size_t)i * V * RW;
-    if (r < V) {
-#pragma unroll
-      for (int k = 0; k < V; ++k) { arow[k] = m[r * RW + k]; lrow[k] = m[r * RW + V + k]; }
-      rsc = m[r * RW + 2 * V];
-      csc = m[r * RW + 2 * V + 1];
-      src = d.bperm[i * 8 + r];
-    }
-#pragma unroll
-    for (int k = 0; k < V; ++k) {
-      ukk[k] = m[k * RW + V + k];
-      urh[k] = m[k * RW + 2 * V + 2];
-      url[k] = m[k * RW + 2 * V + 3];
-    }
-    equ = d.bperm[i * 8 + 7];
-  }
+  const BSlot<NSP> sp = bslot_load<NSP, FWD>(d, t, valid, q);
+  const BRow<NSP> rw = brow_load<NSP>(d, i, valid, r);
   double hown = 0.0;
   if (FWD && valid && r < V) hown = d.hWA[r * NE + i];  // written by k_bdf2_prep, complete before this grid
   pdl_wait();
   if (!FWD && valid && r < V) hown = d.hWA[r * NE + i];
-  // --- flux difference of the neighbour's increment (Time_BDF2.f90:168-197)
   double c[V];
-#pragma unroll
-  for (int k = 0; k < V; ++k) c[k] = 0.0;
-  if (act) {
-    const double dpp = d.hWA[0 * NE + j], duu = d.hWA[1 * NE + j], dvv = d.hWA[2 * NE + j],
-                 dtt = d.hWA[3 * NE + j];
-    double dyy[NSP], s = 0.0;
-#pragma unroll
-    for (int k = 0; k < NSP - 1; ++k) { dyy[k] = d.hWA[(4 + k) * NE + j]; s = s + dyy[k]; }
-    dyy[NSP - 1] = -s;
-    double s1 = 0.0;
-#pragma unroll
-    for (int k = 0; k < NSP; ++k) s1 = s1 + th.R[k] * dyy[k];
-    const double drr = div_rn(dpp - rrc * dtt - rt * s1, rct, rcth, rctl);
-    const double dunormal = duu * dx + dvv * dy;
-    if (lo) {
-      const double dru = rr * duu + uu * drr;
-      const double drv = rr * dvv + vv * drr;
-      c[0] = 0.5 * (-aF * drr + dru * dx + drv * dy);
-      c[1] = 0.5 * (-aF * dru + dru * unormal + rou * dunormal + dpp * dx);
-      c[2] = 0.5 * (-aF * drv + drv * unormal + rov * dunormal + dpp * dy);
-    } else {
-      double s2 = 0.0;
-#pragma unroll
-      for (int k = 0; k < NSP; ++k) s2 = s2 + ent[k] * dyy[k];
-      const double dre = rcp * dtt + rr * s2 + hh * drr + rr * (uu * duu + vv * dvv) + ek * drr - dpp;
-      c[3] = 0.5 * (-aF * dre + dunormal * roepp + unormal * (dre + dpp));
-#pragma unroll
-      for (int k = 0; k < NSP - 1; ++k) {
-        const double dry = rr * dyy[k] + yy[k] * drr;
-        c[4 + k] = 0.5 * (-aF * dry + dry * unormal + ry[k] * dunormal);
-      }
-    }
-  }
+  bslot_terms<NSP>(d, th, sp, lo, c);
   __shared__ double wsm[CPW * V * 4];
   double* w = wsm + (cell < CPW ? cell : 0) * V * 4;  // [row][slot]
-  if (cell < CPW) {
-    if (lo) {
-#pragma unroll
-      for (int k = 0; k < 3; ++k) w[k * 4 + q] = c[k];
-    } else {
-#pragma unroll
-      for (int k = 3; k < V; ++k) w[k * 4 + q] = c[k];
-    }
-  }
+  if (cell < CPW) bslot_put<NSP>(w, lo, q, c);
   __syncwarp();
   double dflux = 0.0;
   if (r < V) {
@@ -551,15 +606,14 @@ __global__ void __launch_bounds__(32) k_bdf2_sweep(const Dev d, const ThermoDev<
     for (int sl = 0; sl < 4; ++sl) dflux = dflux + w[r * 4 + sl];
   }
   // --- the cell's system, one row per lane (dgesvx after the factorisation)
-  const bool rowequ = equ & 1, colequ = equ & 2;
+  const bool rowequ = rw.equ & 1, colequ = rw.equ & 2;
   double b = FWD ? hown - dflux : dflux;
-  if (rowequ) b = rsc * b;
+  if (rowequ) b = rw.rsc * b;
   if (!(valid && r < V)) b = 0.0;
-  double x = getrs_rows<V>(b, src, lrow, ukk, urh, url, r, base);
+  double x = getrs_rows<V>(b, rw.src, rw.lrow, rw.ukk, rw.urh, rw.url, r, base);
   // dgerfs refinement: residual, componentwise backward error, correction.
   // The backward error is non-negative: its maximum and the loop tests
   // compare bit patterns; 2 berr <= lstres is berr <= lstres/2 (both exact).
-  const double safe1 = (V + 1) * SFMIN, safe2 = safe1 / EPS;
   long long lstres_half = dbits(1.5);  // lstres = 3
   int count = 1;
   bool go = valid;
@@ -569,18 +623,14 @@ __global__ void __launch_bounds__(32) k_bdf2_sweep(const Dev d, const ThermoDev<
     for (int k = 0; k < V; ++k) xs[k] = __shfl_sync(FULL, x, base + k);
     double y = b;
 #pragma unroll
-    for (int k = 0; k < V; ++k) y = y + (-1.0 * xs[k]) * arow[k];
+    for (int k = 0; k < V; ++k) y = y + (-1.0 * xs[k]) * rw.arow[k];
     double wk = fabs(b);
 #pragma unroll
-    for (int k = 0; k < V; ++k) wk = wk + fabs(arow[k]) * fabs(xs[k]);
-    long long vb = 0;
-    if (r < V) vb = dbits((dbits(wk) > dbits(safe2)) ? fabs(y) / wk : (fabs(y) + safe1) / (wk + safe1));
-    vb = max(vb, (long long)__shfl_xor_sync(FULL, (unsigned long long)vb, 1));
-    vb = max(vb, (long long)__shfl_xor_sync(FULL, (unsigned long long)vb, 2));
-    vb = max(vb, (long long)__shfl_xor_sync(FULL, (unsigned long long)vb, 4));
+    for (int k = 0; k < V; ++k) wk = wk + fabs(rw.arow[k]) * fabs(xs[k]);
+    const long long vb = berr_bits<V>(y, wk, r);
     const bool cont = go && vb > dbits(EPS) && vb <= lstres_half && count <= 5;
     if (!__any_sync(FULL, cont)) break;
-    const double corr = getrs_rows<V>(y, src, lrow, ukk, urh, url, r, base);
+    const double corr = getrs_rows<V>(y, rw.src, rw.lrow, rw.ukk, rw.urh, rw.url, r, base);
     if (cont) {
       x = x + corr;
       lstres_half = vb - (1LL << 52);  // berr / 2: berr > eps is a normal number
@@ -588,7 +638,7 @@ __global__ void __launch_bounds__(32) k_bdf2_sweep(const Dev d, const ThermoDev<
     }
     go = cont;
   }
-  if (colequ) x = csc * x;
+  if (colequ) x = rw.csc * x;
   if (valid && r < V) d.hWA[r * NE + i] = FWD ? x : hown - x;
 }
 
