@@ -76,10 +76,20 @@ constexpr double INV_LN2 = 1.4426950408889634074;
 // 2^k for integer k with a normal result
 RCM_HD double pow2i(int k) { return from_bits((int64_t)(k + 1023) << 52); }
 
+// Range and special-value tests compare bit patterns (integer operations):
+// for non-negative doubles the integer order of the patterns is the
+// floating-point order.
+constexpr int64_t ABS_MASK = 0x7fffffffffffffffLL;
+constexpr int64_t INF_BITS = 0x7ff0000000000000LL;
+constexpr int64_t EXP_HI_BITS = 0x40862e42fefa39efLL;  // 709.782712893384
+constexpr int64_t EXP_LO_BITS = 0x40874910d52d3052LL;  // 745.1332191019412
+constexpr int64_t SQRT2_BITS = 0x3ff6a09e667f3bcdLL;   // 1.4142135623730951
+
 RCM_HD double exp(double x) {
-  if (x != x) return x;
-  if (x > 709.782712893384) return HUGE_VAL;
-  if (x < -745.1332191019412) return 0.0;
+  const int64_t b = bits(x);
+  if ((b & ABS_MASK) > INF_BITS) return x;           // NaN
+  if (b > EXP_HI_BITS) return HUGE_VAL;              // x > 709.782712893384
+  if (b < 0 && (b & ABS_MASK) > EXP_LO_BITS) return 0.0;  // x < -745.1332191019412
   const double kd = rint_(x * INV_LN2);
   double r = fma_(-kd, LN2, x);
   r = fma_(-kd, LN2_TAIL, r);
@@ -104,10 +114,11 @@ RCM_HD double exp(double x) {
 }
 
 RCM_HD double log(double x) {
-  if (x != x) return x;
-  if (x <= 0.0) return x == 0.0 ? -HUGE_VAL : (x - x) / (x - x);
-  if (x == HUGE_VAL) return x;
   int64_t b = bits(x);
+  if ((b & ABS_MASK) > INF_BITS) return x;                                    // NaN
+  if (b <= 0)                                                                 // x <= 0 (incl. -0)
+    return (b & ABS_MASK) == 0 ? -HUGE_VAL : (x - x) / (x - x);
+  if (b == INF_BITS) return x;
   int e = (int)((b >> 52) & 0x7ff);
   if (e == 0) {  // subnormal: scale by 2^54 (exact)
     x = x * 18014398509481984.0;
@@ -115,8 +126,9 @@ RCM_HD double log(double x) {
     e = (int)((b >> 52) & 0x7ff) - 54;
   }
   e -= 1023;
-  double m = from_bits((b & 0x000fffffffffffffLL) | 0x3ff0000000000000LL);  // [1, 2)
-  if (m > 1.4142135623730951) {
+  const int64_t mb = (b & 0x000fffffffffffffLL) | 0x3ff0000000000000LL;
+  double m = from_bits(mb);  // [1, 2)
+  if (mb > SQRT2_BITS) {
     m = m * 0.5;
     e += 1;
   }
@@ -142,8 +154,9 @@ RCM_HD double log(double x) {
 
 // x > 0 (the reference only takes powers of positive quantities)
 RCM_HD double pow(double x, double y) {
-  if (x == 1.0 || y == 0.0) return 1.0;
-  if (x == 0.0) return y > 0.0 ? 0.0 : HUGE_VAL;
+  const int64_t bx = bits(x), by = bits(y);
+  if (bx == 0x3ff0000000000000LL || (by & ABS_MASK) == 0) return 1.0;  // x == 1 or y == 0
+  if ((bx & ABS_MASK) == 0) return (by > 0 && (by & ABS_MASK) <= INF_BITS) ? 0.0 : HUGE_VAL;  // x == 0
   const double L = log(x);
   const double t = y * L;
   const double terr = fma_(y, L, -t);
