@@ -118,3 +118,21 @@ def test_euler_lusgs_bit_identical_to_oracle(case_root):
         assert np.array_equal(s.get_array("hWA"), o.array("hWA")), inner
         PA, WA = s.get_state()
         assert np.array_equal(PA, o.array("PA")) and np.array_equal(WA, o.array("WA")), inner
+
+
+def test_driver_shortens_the_last_step_like_the_reference(case_root):
+    """fvm2d.f90:52-56: the step that would pass totaltime is shortened to end
+    on it and the loop stops; the driver does the same on the GPU."""
+    d = make_case(case_root, "t2u", totaltime=2.5e-8, nstep=2, inner_loop=3)
+    c = rc.Case(d)
+    _, inner = c.run_unsteady(10)
+    o = oracle.Oracle(d, threads=4)
+    ref = []
+    for i in range(1, 11):
+        n, stop = o.unsteady_step(i)
+        ref.append(n)
+        if stop:
+            break
+    assert len(ref) == 2 and list(inner[:2]) == ref and inner[2:].sum() == 0
+    assert c.unsteady["ttime"] == o.unsteady()["ttime"] == pytest.approx(2.5e-8, rel=1e-12)
+    assert np.array_equal(c.array("PA"), o.array("PA"))
