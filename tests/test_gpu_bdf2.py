@@ -136,3 +136,16 @@ def test_driver_shortens_the_last_step_like_the_reference(case_root):
     assert len(ref) == 2 and list(inner[:2]) == ref and inner[2:].sum() == 0
     assert c.unsteady["ttime"] == o.unsteady()["ttime"] == pytest.approx(2.5e-8, rel=1e-12)
     assert np.array_equal(c.array("PA"), o.array("PA"))
+
+
+def test_bdf2_step_bit_identical_at_full_size(case_root):
+    """One physical step of the shipped scheme on the 120,000-cell reacting
+    nozzle (301 + 301 levels, 3-4 inner iterations) against the oracle."""
+    d = make_case(case_root, "c2u")
+    c = rc.Case(d)
+    _, inner = c.run_unsteady(1)
+    o = oracle.Oracle(d, threads=oracle.Oracle.max_threads())
+    n, _ = o.unsteady_step(1)
+    assert int(inner[0]) == n
+    assert np.array_equal(c.array("PA"), o.array("PA"))
+    assert np.array_equal(c.array("WA"), o.array("WA"))
