@@ -136,17 +136,21 @@ def test_full_size_c1_100_iterations(case_root):
     PA, WA = s.get_state()
     assert rel_linf(PA, o.array("PA")).max() <= ITER_RTOL
     assert rel_linf(WA, o.array("WA")).max() <= ITER_RTOL
+    assert np.array_equal(PA, o.array("PA")) and np.array_equal(WA, o.array("WA"))
 
 
-def test_full_size_c2_few_iterations(case_root):
-    """The 120k-triangle reacting viscous nozzle at its full size, 3 iterations."""
+def test_full_size_c2_20_iterations(case_root):
+    """The 120k-triangle reacting viscous nozzle at its full size, 20
+    iterations (the autotuned schedule), bit for bit."""
     d = make_case(case_root, "c2")
     c, s, o = solver_and_oracle(d, threads=oracle.Oracle.max_threads())
-    s.run(3)
-    o.run(3)
+    s.autotune(2)
+    s.run(20)
+    o.run(20)
     PA, WA = s.get_state()
     assert rel_linf(PA, o.array("PA")).max() <= ITER_RTOL
     assert rel_linf(WA, o.array("WA")).max() <= ITER_RTOL
+    assert np.array_equal(PA, o.array("PA")) and np.array_equal(WA, o.array("WA"))
 
 
 def test_device_stop_condition_is_reported(case_t1):
