@@ -92,13 +92,13 @@ __device__ __forceinline__ void dwdp(const ThermoDev<NSP>& th, const double* pri
     for (int c = 0; c < V; ++c) dkf[c] = 0.;
   } else {
     double af = th.Af * rcm::exp(-th.E / (th.Rconstant * T));
-    const double r1 = y[0] * rho / th.mw1000[0];
-    const double dr1dr = y[0] / th.mw1000[0];
-    const double dr1dy1 = rho / th.mw1000[0];
+    const double r1 = div_rn(y[0] * rho, th.mw1000[0], th.mw1000r[0]);
+    const double dr1dr = div_rn(y[0], th.mw1000[0], th.mw1000r[0]);
+    const double dr1dy1 = div_rn(rho, th.mw1000[0], th.mw1000r[0]);
     const double y1 = NS1 > 1 ? y[NS1 > 1 ? 1 : 0] : 0.0;
-    const double r2 = y1 * rho / th.mw1000[1];
-    const double dr2dr = y1 / th.mw1000[1];
-    const double dr2dy2 = rho / th.mw1000[1];
+    const double r2 = div_rn(y1 * rho, th.mw1000[1], th.mw1000r[1]);
+    const double dr2dr = div_rn(y1, th.mw1000[1], th.mw1000r[1]);
+    const double dr2dy2 = div_rn(rho, th.mw1000[1], th.mw1000r[1]);
     const double drdp = rho / p, drdT = -rho / T;
 #pragma unroll
     for (int i = 0; i < NS1; ++i) drdy[i] = -(th.R[i] - th.R[NSP - 1]) * rho / Rcpcv;

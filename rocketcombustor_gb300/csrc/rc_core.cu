@@ -423,12 +423,13 @@ __global__ void __launch_bounds__(128) k_face_flux(const Dev d, const ThermoDev<
     }
     if (NR >= 0) {
       const double dxk = d.fdxk[f], y1 = d.fysn[f], y2 = d.fysn[NF + f];
+      const double rkh = d.fdxkr[f], rkl = d.fdxkr[NF + f];
       const double dxr = d.rinv[NR], dyr = d.rinv[NE + NR];
 #pragma unroll
       for (int k = 0; k < V; ++k) {
         const double du = uR[k] - uL[k];
-        t0[k] = 0.5 * (t0[k] + d.grad[(2 * k) * NE + NR] * dxr) + y1 * du / dxk;
-        t1[k] = 0.5 * (t1[k] + d.grad[(2 * k + 1) * NE + NR] * dyr) + y2 * du / dxk;
+        t0[k] = 0.5 * (t0[k] + d.grad[(2 * k) * NE + NR] * dxr) + div_rn(y1 * du, dxk, rkh, rkl);
+        t1[k] = 0.5 * (t1[k] + d.grad[(2 * k + 1) * NE + NR] * dyr) + div_rn(y2 * du, dxk, rkh, rkl);
       }
     }
     double dudx = t0[1], dudy = t1[1], dvdx = t0[2], dvdy = t1[2], dtdx = t0[3], dtdy = t1[3];
@@ -1204,6 +1205,20 @@ void fill_thermo(const rc_thermo* t, const rc_config* g, ThermoDev<NSP>& th) {
   th.mw1000[0] = t->mole_weight[0] * 1000;
   th.mw1000[1] = t->mole_weight[NSP > 1 ? 1 : 0] * 1000;
   th.cfl = g->cfl;
+  // the device's recip_of, on the host (IEEE division, a correctly rounded FMA)
+  auto rp = [](double x, double* r) {
+    r[0] = 1.0 / x;
+    r[1] = std::fma(-x, r[0], 1.0) * r[0];
+  };
+  for (int i = 0; i < NSP; ++i) {
+    rp(th.mw[i], th.mwr[i]);
+    for (int j = 0; j < NSP; ++j) {
+      rp(th.wd[i][j], th.wdr[i][j]);
+      rp(th.dlj[i][j], th.dljr[i][j]);
+    }
+  }
+  rp(th.mw1000[0], th.mw1000r[0]);
+  rp(th.mw1000[1], th.mw1000r[1]);
 }
 
 inline unsigned blocks(long n, int t) { return (unsigned)((n + t - 1) / t); }
@@ -1639,7 +1654,7 @@ int init_impl(const rc_mesh* m, const rc_thermo* t, const rc_config* g, const Ba
   // ---- faces
   std::vector<int> fNL(NF), fNR(NF);
   std::vector<double> fvec(2 * (size_t)NF), fsav(NF), fsn(2 * (size_t)NF), fss(NF), fs2(NF), fvL(2 * (size_t)NF),
-      fvR(2 * (size_t)NF), fdxk(NF), fysn(2 * (size_t)NF);
+      fvR(2 * (size_t)NF), fdxk(NF), fdxkr(2 * (size_t)NF), fysn(2 * (size_t)NF);
   for (int f = 1; f <= NF; ++f) {
     const int L = m->Neighbor[2 * (f - 1)], R = m->Neighbor[2 * (f - 1) + 1];
     if (m->FProperty[f - 1] == 100) return bail(RC_ERR_ARG, "periodic faces are not supported");
@@ -1666,6 +1681,8 @@ int init_impl(const rc_mesh* m, const rc_thermo* t, const rc_config* g, const Ba
       const double dlrx = C2(m->CELLXY, 1, L) - (C2(m->CELLXY, 1, R) - C2(m->SideOfs, 1, f));
       const double dlry = C2(m->CELLXY, 2, L) - (C2(m->CELLXY, 2, R) - C2(m->SideOfs, 2, f));
       fdxk[fi] = std::fabs(dlrx * fsn[fi] + dlry * fsn[NF + fi]);
+      fdxkr[fi] = 1.0 / fdxk[fi];
+      fdxkr[NF + fi] = std::fma(-fdxk[fi], fdxkr[fi], 1.0) * fdxkr[fi];
     }
     const double yita = 4. / 3;
     fysn[fi] = yita * fsn[fi];
@@ -1814,6 +1831,7 @@ int init_impl(const rc_mesh* m, const rc_thermo* t, const rc_config* g, const Ba
   st |= dev_upload(c, fvL, &p); d.fvL = p;
   st |= dev_upload(c, fvR, &p); d.fvR = p;
   st |= dev_upload(c, fdxk, &p); d.fdxk = p;
+  st |= dev_upload(c, fdxkr, &p); d.fdxkr = p;
   st |= dev_upload(c, fysn, &p); d.fysn = p;
   st |= dev_upload(c, gtype, &i32); d.gtype = i32;
   st |= dev_upload(c, gsn, &p); d.gsn = p;

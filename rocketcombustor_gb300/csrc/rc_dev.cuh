@@ -39,6 +39,7 @@ struct Dev {
   const double* fvL;             // [2*NF] fbaseAll at the Gauss point for NL
   const double* fvR;             // [2*NF] fbaseAll at the Gauss point for NR
   const double* fdxk;            // |(x_L - x_R).n|
+  const double* fdxkr;           // its reciprocal pair (2 planes), interior faces
   const double* fysn;            // [2*NF] yita*n
   // ghosts
   const int* gtype;

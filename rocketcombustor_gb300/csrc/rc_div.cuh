@@ -14,16 +14,20 @@
 // div_rn(a, b, yh, yl): q0 = RN(a yh + RN(a yl)) is within half an ulp plus
 // about 2^-104 relative of a/b, hence faithful; r = a - b q0 exactly;
 // q = RN(q0 + r yh) = RN(a/b).  Four dependent FP64 operations instead of a
-// division.  Operands whose exponents are outside [-400, 400] (where the
-// intermediate results could leave the normal range), and zeros, infinities
-// and NaNs, take the IEEE division.  The result equals a / b bit for bit.
+// division.  A zero numerator gives a zero through the same operations; its
+// sign, and the sign of every quotient, is set to sign(a) xor sign(b) on the
+// bit pattern (for a non-zero quotient that is its sign already).  Operands
+// whose exponents are outside [-400, 400] (where the intermediate results
+// could leave the normal range), zero divisors, infinities and NaNs take the
+// IEEE division.  The result equals a / b bit for bit.
 #pragma once
 
 namespace rc {
 
 __device__ __forceinline__ bool div_rn_safe(double a, double b) {
   const int ea = (__double2hiint(a) >> 20) & 0x7ff, eb = (__double2hiint(b) >> 20) & 0x7ff;
-  return ea >= 1023 - 400 && ea <= 1023 + 400 && eb >= 1023 - 400 && eb <= 1023 + 400;
+  const bool za = (__double_as_longlong(a) << 1) == 0;
+  return (za || (ea >= 1023 - 400 && ea <= 1023 + 400)) && eb >= 1023 - 400 && eb <= 1023 + 400;
 }
 struct Recip {
   double h, l;
@@ -38,8 +42,12 @@ __device__ __forceinline__ double div_rn(double a, double b, double yh, double y
   if (!div_rn_safe(a, b)) return a / b;
   const double q0 = fma(a, yh, a * yl);
   const double r = fma(-b, q0, a);
-  return fma(r, yh, q0);
+  const double q = fma(r, yh, q0);
+  const int hi = (__double2hiint(q) & 0x7fffffff) | ((__double2hiint(a) ^ __double2hiint(b)) & (int)0x80000000);
+  return __hiloint2double(hi, __double2loint(q));
 }
+// a / b for a divisor fixed in advance, its reciprocal pair given as r[0], r[1]
+__device__ __forceinline__ double div_rn(double a, double b, const double* r) { return div_rn(a, b, r[0], r[1]); }
 
 // x != 0.0 without an FP64 compare (NaN counts as non-zero, -0 as zero)
 __device__ __forceinline__ bool nonzero(double x) { return (__double_as_longlong(x) << 1) != 0; }

@@ -3,12 +3,17 @@
 // Each function keeps the operation order of the reference routine it cites,
 // so that with FMA contraction disabled (--fmad=false) +,-,*,/ and sqrt give
 // the reference's IEEE results; exp/log/pow come from include/rc_math.h, the
-// same code the CPU oracle runs, so the results are bit-identical.  Constants that depend on species data only (pair terms of the
-// Wilke and Chapman-Enskog sums) are evaluated once on the host with the
-// reference's expressions and passed in ThermoDev.
+// same code the CPU oracle runs, so the results are bit-identical.  Constants
+// that depend on species data only (pair terms of the Wilke and Chapman-Enskog
+// sums) are evaluated once on the host with the reference's expressions and
+// passed in ThermoDev, with reciprocal pairs of the fixed divisors; divisions
+// by those, and the transport fits' divisions by T and T^2, use the correctly
+// rounded division of rc_div.cuh (the IEEE quotient bit for bit, four FP64
+// operations instead of a division sequence).
 #pragma once
 #include <cstdint>
 
+#include "rc_div.cuh"
 #include "rc_math.h"
 
 namespace rc {
@@ -39,6 +44,11 @@ struct ThermoDev {
   double prodc[NSP];             // 1000*mole_weight(ks)*(coef_r-coef_f)
   double mw1000[2];              // mole_weight(1..2)*1000
   double cfl;
+  // reciprocal pairs {RN(1/x), RN((1 - x RN(1/x)) RN(1/x))} of fixed divisors
+  double mwr[NSP][2];            // of mw
+  double wdr[NSP][NSP][2];       // of wd
+  double dljr[NSP][NSP][2];      // of dlj
+  double mw1000r[2][2];          // of mw1000
 };
 
 __device__ __forceinline__ double fmin2(double a, double b) { return (b < a) ? b : a; }
@@ -116,20 +126,23 @@ __device__ __forceinline__ void transport(const ThermoDev<NSP>& th, double tem2,
   const double tem = fmax2(th.trlo, tem2);
   double s = 0.0;
 #pragma unroll
-  for (int i = 0; i < NSP; ++i) s = s + yy[i] / th.mw[i];
+  for (int i = 0; i < NSP; ++i) s = s + div_rn(yy[i], th.mw[i], th.mwr[i]);
   const double ww = 1.0 / s;
   double xx[NSP], mul[NSP], Kl[NSP];
 #pragma unroll
-  for (int i = 0; i < NSP; ++i) xx[i] = ww * yy[i] / th.mw[i];
+  for (int i = 0; i < NSP; ++i) xx[i] = div_rn(ww * yy[i], th.mw[i], th.mwr[i]);
   const bool low = (th.trlo <= tem && tem <= th.trcrit);
   if (!low && !(th.trcrit < tem && tem <= th.trhi)) err |= ERR_TRANSPORT_T;
   const int rg = low ? 0 : 1;
   const double lt = rcm::log(tem);
   const double t2 = tem * tem;
+  const Recip rt = recip_of(tem), rt2 = recip_of(t2);
 #pragma unroll
   for (int i = 0; i < NSP; ++i) {
-    mul[i] = rcm::exp(th.mu[rg][0][i] * lt + th.mu[rg][1][i] / tem + th.mu[rg][2][i] / t2 + th.mu[rg][3][i]);
-    Kl[i] = rcm::exp(th.kk[rg][0][i] * lt + th.kk[rg][1][i] / tem + th.kk[rg][2][i] / t2 + th.kk[rg][3][i]);
+    mul[i] = rcm::exp(th.mu[rg][0][i] * lt + div_rn(th.mu[rg][1][i], tem, rt.h, rt.l) +
+                      div_rn(th.mu[rg][2][i], t2, rt2.h, rt2.l) + th.mu[rg][3][i]);
+    Kl[i] = rcm::exp(th.kk[rg][0][i] * lt + div_rn(th.kk[rg][1][i], tem, rt.h, rt.l) +
+                     div_rn(th.kk[rg][2][i], t2, rt2.h, rt2.l) + th.kk[rg][3][i]);
   }
 #pragma unroll
   for (int i = 0; i < NSP; ++i) { mul[i] = mul[i] * 1.0e-7; Kl[i] = Kl[i] * 1.0e-4; }
@@ -142,7 +155,7 @@ __device__ __forceinline__ void transport(const ThermoDev<NSP>& th, double tem2,
       // sqrt(mul(i)/mul(i)) is exactly 1
       const double sq = (i == j) ? 1.0 : sqrt(mul[i] / mul[j]);
       const double q = 1.0 + sq * th.wc[i][j];
-      phil = phil + xx[j] * (q * q) / th.wd[i][j];
+      phil = phil + div_rn(xx[j] * (q * q), th.wd[i][j], th.wdr[i][j]);
     }
     phil = (0.25 * sqrt(2.0)) * phil;
     v = v + xx[i] * mul[i] / phil;
@@ -164,18 +177,18 @@ __device__ __forceinline__ void diffusion(const ThermoDev<NSP>& th, double pp, d
                                           double* Dk) {
   double s = 0.0;
 #pragma unroll
-  for (int i = 0; i < NSP; ++i) s = s + YY[i] / th.mw[i];
+  for (int i = 0; i < NSP; ++i) s = s + div_rn(YY[i], th.mw[i], th.mwr[i]);
   const double ww = 1.0 / s;
   double XX[NSP];
 #pragma unroll
-  for (int i = 0; i < NSP; ++i) XX[i] = ww * YY[i] / th.mw[i];
+  for (int i = 0; i < NSP; ++i) XX[i] = div_rn(ww * YY[i], th.mw[i], th.mwr[i]);
   const double num = 0.0266 * sqrt(tem * (tem * tem));
   double D[NSP][NSP];
 #pragma unroll
   for (int i = 0; i < NSP; ++i)
 #pragma unroll
     for (int j = i + 1; j < NSP; ++j) {
-      const double tstar = tem / th.dlj[i][j];
+      const double tstar = div_rn(tem, th.dlj[i][j], th.dljr[i][j]);
       const double om = 1.06036 * rcm::pow(tstar, -0.15610) + 0.19300 * rcm::exp(-0.47635 * tstar) +
                         1.03587 * rcm::exp(-1.52996 * tstar) + 1.76474 * rcm::exp(-3.89411 * tstar);
       const double d = num / (pp * th.dmw[i][j] * th.dcd[i][j] * om);
@@ -201,11 +214,11 @@ __device__ __forceinline__ void production(const ThermoDev<NSP>& th, double T, d
   if (th.model == 0) {
     const double y1 = fmin2(1.0, fmax2(0.0, Y2[NSP > 1 ? 1 : 0]));
     kf = th.Af * rcm::exp(-th.E / (th.Rconstant * T));
-    kf = kf * rcm::pow(y0 * rho / th.mw1000[0], 0.2);
-    kf = kf * rcm::pow(y1 * rho / th.mw1000[1], 1.3);
+    kf = kf * rcm::pow(div_rn(y0 * rho, th.mw1000[0], th.mw1000r[0]), 0.2);
+    kf = kf * rcm::pow(div_rn(y1 * rho, th.mw1000[1], th.mw1000r[1]), 1.3);
   } else {
     kf = (T > 710.0) ? 1e4 : 0.0;
-    kf = kf * (y0 * rho / th.mw1000[0]);
+    kf = kf * div_rn(y0 * rho, th.mw1000[0], th.mw1000r[0]);
   }
 #pragma unroll
   for (int k = 0; k < NSP; ++k) prod[k] = th.prodc[k] * kf;

@@ -2,7 +2,8 @@
 // pair) against the IEEE FP64 division on random operands: exponents in
 // [-450, 450] (so both the Markstein path and the IEEE fallback run), random
 // mantissas, every fourth divisor with an all-ones mantissa tail, every eighth
-// a power of two.  Prints the counts; exits 1 on any bit difference.
+// a power of two, every sixteenth numerator a signed zero.  Prints the counts;
+// exits 1 on any bit difference.
 #include <cstdint>
 #include <cstdio>
 #include <cstdlib>
@@ -24,7 +25,8 @@ __global__ void check(unsigned long long n, unsigned long long seed, unsigned lo
     uint64_t mb = h2 & ((1ULL << 52) - 1);
     if ((i & 3) == 0) mb |= ((1ULL << 52) - 1) & ~((1ULL << ((h1 >> 3) % 20)) - 1);
     if ((i & 7) == 1) mb = 0;
-    const double a = __longlong_as_double((long long)((ea << 52) | ma | ((h1 & 1) << 63)));
+    double a = __longlong_as_double((long long)((ea << 52) | ma | ((h1 & 1) << 63)));
+    if ((i & 15) == 5) a = (h1 & 1) ? -0.0 : 0.0;
     const double b = __longlong_as_double((long long)((eb << 52) | mb | ((h2 & 2) << 62)));
     const rc::Recip y = rc::recip_of(b);
     const double q = rc::div_rn(a, b, y.h, y.l);
