@@ -146,7 +146,12 @@ int rc_init_batch(int ncase, const rc_mesh* meshes, const rc_thermo* thermos, co
 /* Number of cases and the ncase+1 cell offsets of the numbering. */
 int rc_batch_info(rc_ctx* ctx, int* ncase, int* cell_offsets);
 
-/* PA(NVar,NE), WA(NVar,NE) in the Fortran layout (module.f90:54). */
+/* PA(NVar,NE), WA(NVar,NE) in the Fortran layout (module.f90:54).  Either
+ * pointer may be null.  rc_set_state queues the copies on the context's stream
+ * and returns: from page-locked host memory the copy may still be in flight,
+ * so the caller keeps such buffers unchanged until its next call that
+ * synchronises (rc_get_state, rc_residual, rc_sync).  rc_get_state returns
+ * when both arrays are on the host. */
 int rc_set_state(rc_ctx* ctx, const double* PA, const double* WA);
 int rc_get_state(rc_ctx* ctx, double* PA, double* WA);
 

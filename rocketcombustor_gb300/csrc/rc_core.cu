@@ -816,32 +816,58 @@ __device__ __forceinline__ void bar_named(int id, int count) {
 // finish cells 0-3 and 4-7 (8 lanes per cell).  Every expression is the one
 // of sweep_terms in the same order, so the same bits; the longest warp chain
 // is about two thirds of k_sweep2w's.
-template <int NSP, bool FWD>
-__global__ void __launch_bounds__(128) k_sweep4w(const Dev d, const ThermoDev<NSP> th, int t0, int t1) {
-  constexpr int V = 3 + NSP, DIR = FWD ? 0 : 1;
-  pdl_launch_dependents();
+// hWA as the sweeps read it: through L2 (ld.global.cg) where other SMs write
+// it during the launch (the dataflow schedule), else a plain load
+template <bool L2>
+__device__ __forceinline__ double ldh(const double* p) {
+  if (L2) return __ldcg(p);
+  return *p;
+}
+// What finishing a cell needs besides the terms: the cell (-1: no cell at
+// this position), dd and its reciprocal pair.
+struct Fin4w {
+  int i;
+  double dd, ddh, ddl;
+};
+template <bool FWD>
+__device__ __forceinline__ Fin4w fin_load(const Dev& d, int ft, int t1) {
+  Fin4w f = {-1, 1.0, 1.0, 0.0};
+  if (ft < t1) {
+    const int i = d.swi[FWD ? 0 : 1][ft];
+    f.i = i;
+    f.dd = d.dd[i];
+    f.ddh = d.rcp[4 * d.NE + i];
+    f.ddl = d.rcp[5 * d.NE + i];
+  }
+  return f;
+}
+// The sweep step of the 8 cells of one pass on threads 0..127 (four warps,
+// lane = 4 cell + slot): p is the thread's (cell, slot) data from sweep_load,
+// nbv the hWA of its neighbour (V values; unused when the slot is inactive),
+// fn the data of the cell it finishes (warps 0 and 1, 8 lanes per cell).
+// Barriers 1, 2 (warps 0-2) and 7 (warps 0-3) are used.
+template <int NSP, bool FWD, bool L2>
+__device__ __forceinline__ void sweep4w_compute(const Dev& d, const ThermoDev<NSP>& th, const SweepPre<NSP>& p,
+                                                const double* nbv, const Fin4w& fn) {
+  constexpr int V = 3 + NSP;
   const int NE = d.NE, role = threadIdx.x >> 5, lane = threadIdx.x & 31, cell = lane >> 2, q = lane & 3;
   __shared__ double wsm[8 * V * 4];
   __shared__ double xs1[32], xq[32], xdp[32];
-  const SweepPre<NSP> p = sweep_load<NSP, FWD>(d, t0 + blockIdx.x * 8 + cell, t1, q);
-  const int fcell = (role & 1) * 4 + (lane >> 3), r = lane & 7, ft = t0 + blockIdx.x * 8 + fcell;
-  const bool fvalid = role < 2 && ft < t1 && r < V;
-  const int fi = fvalid ? d.swi[DIR][ft] : 0;
-  double fdd = 1.0, fddh = 1.0, fddl = 0.0;
-  if (fvalid) { fdd = d.dd[fi]; fddh = d.rcp[4 * NE + fi]; fddl = d.rcp[5 * NE + fi]; }
-  pdl_wait();
-  const double R = fvalid ? d.hWA[r * NE + fi] : 0.0;
+  const int fcell = (role & 1) * 4 + (lane >> 3), r = lane & 7;
+  const bool fvalid = role < 2 && fn.i >= 0 && r < V;
+  const int fi = fvalid ? fn.i : 0;
+  const double fdd = fn.dd, fddh = fn.ddh, fddl = fn.ddl;
+  const double R = fvalid ? ldh<L2>(d.hWA + r * NE + fi) : 0.0;
   double* w = wsm + cell * V * 4;
   double drr = 0, dru = 0, drv = 0, dre = 0, duu = 0, dvv = 0, dunormal = 0, X = 0, dry[NSP];
 #pragma unroll
   for (int k = 0; k < NSP; ++k) dry[k] = 0.0;
   const double aF = p.aF, unormal = p.unormal;
   if (p.act) {
-    const int j = p.j;
-    drr = d.hWA[0 * NE + j]; dru = d.hWA[1 * NE + j]; drv = d.hWA[2 * NE + j]; dre = d.hWA[3 * NE + j];
+    drr = nbv[0]; dru = nbv[1]; drv = nbv[2]; dre = nbv[3];
     double s = 0.0;
 #pragma unroll
-    for (int k = 0; k < NSP - 1; ++k) { dry[k] = d.hWA[(4 + k) * NE + j]; s = s + dry[k]; }
+    for (int k = 0; k < NSP - 1; ++k) { dry[k] = nbv[4 + k]; s = s + dry[k]; }
     dry[NSP - 1] = drr - s;
     duu = div_rn(dru - p.uu * drr, p.rr, p.rrh, p.rrl);
     dvv = div_rn(drv - p.vv * drr, p.rr, p.rrh, p.rrl);
@@ -881,7 +907,7 @@ __global__ void __launch_bounds__(128) k_sweep4w(const Dev d, const ThermoDev<NS
     }
     w[(1 + role) * 4 + q] = ck;
   }
-  __syncthreads();
+  bar_named(7, 128);
   if (!fvalid) return;
   const double* wf = wsm + fcell * V * 4;
   double df = 0.0;
@@ -889,6 +915,146 @@ __global__ void __launch_bounds__(128) k_sweep4w(const Dev d, const ThermoDev<NS
   for (int sl = 0; sl < 4; ++sl) df = df + wf[r * 4 + sl];
   d.hWA[r * NE + fi] = FWD ? div_rn(R - df, fdd, fddh, fddl) : R - div_rn(df, fdd, fddh, fddl);
 }
+template <int NSP, bool FWD>
+__global__ void __launch_bounds__(128) k_sweep4w(const Dev d, const ThermoDev<NSP> th, int t0, int t1) {
+  pdl_launch_dependents();
+  const int lane = threadIdx.x & 31, role = threadIdx.x >> 5, tb = t0 + blockIdx.x * 8;
+  const SweepPre<NSP> p = sweep_load<NSP, FWD>(d, tb + (lane >> 2), t1, lane & 3);
+  const Fin4w fn = role < 2 ? fin_load<FWD>(d, tb + (role & 1) * 4 + (lane >> 3), t1) : Fin4w{-1, 1.0, 1.0, 0.0};
+  pdl_wait();
+  constexpr int V = 3 + NSP;
+  double nbv[V];
+#pragma unroll
+  for (int k = 0; k < V; ++k) nbv[k] = p.act ? d.hWA[k * d.NE + p.j] : 0.0;
+  sweep4w_compute<NSP, FWD, false>(d, th, p, nbv, fn);
+}
+// Both LU-SGS sweeps as a dataflow over one cooperative launch, one block per
+// SM.  Block b owns a contiguous range of cells; its cells of one level, in
+// runs of at most 8 consecutive sweep positions, form a pass, and the block
+// runs its forward passes, then its backward passes, in level order.  A pass
+// waits (bounded) only for the passes of other blocks that hold its lower
+// (forward) or upper (backward) neighbours; neighbours in the block itself
+// were done by an earlier pass.  Warps 0-3 compute the passes (the four-warp
+// step of k_sweep4w, hWA read through L2); warp 4 runs one pass ahead of them:
+// while they compute it stages the next pass's sweep_load data in shared
+// memory and looks once at the flags that pass waits for; when they are done
+// (barrier 4) it hands the next pass over (barrier 3) at once if those flags
+// were set, and publishes the finished pass's flag = this launch's epoch;
+// otherwise it publishes first and then waits for the flags, so that no
+// block waits while holding a finished pass that others may need.  The last block to finish advances the
+// epoch counter (ctr[0]; ctr[1] counts finished blocks), so the flags need no
+// reset between launches.  After a failed wait (ERR_SYNC latched) no flag is
+// published any more and every block runs to the end.  The Newton update
+// follows as its own launch.
+struct FlowDev {
+  const int* pstart;   // first sweep position of pass p
+  const int* pcount;   // its number of cells (1..8)
+  const int* boff[2];  // passes of block b: blist[d][boff[d][b] .. boff[d][b+1]), d = 0 forward, 1 backward
+  const int* blist[2];
+  const int* doff;     // passes that pass p waits for: deps[doff[p] .. doff[p+1])
+  const int* deps;
+  unsigned* pflag;     // per pass: epoch of the launch that finished it
+  unsigned* ctr;       // [0] epoch of the last finished launch, [1] finished blocks
+};
+constexpr int FLOW_THREADS = 160;
+// bar.arrive: count this warp in at barrier id without waiting
+__device__ __forceinline__ void bar_arrive(int id, int count) {
+  asm volatile("bar.arrive %0, %1;" ::"r"(id), "r"(count) : "memory");
+}
+template <int NSP>
+__global__ void __launch_bounds__(FLOW_THREADS) k_lusgs_flow(const Dev d, const ThermoDev<NSP> th, const FlowDev f) {
+  constexpr int V = 3 + NSP;
+  __shared__ SweepPre<NSP> s_pre[2][32];
+  __shared__ Fin4w s_fin[2][8];
+  __shared__ unsigned s_epoch;
+  __shared__ int s_bad;
+  if (threadIdx.x == 0) {
+    s_epoch = ld_acquire(f.ctr) + 1u;
+    s_bad = 0;
+  }
+  __syncthreads();
+  const unsigned epoch = s_epoch;
+  const int b = blockIdx.x, lane = threadIdx.x & 31;
+  const int f0 = f.boff[0][b], b0 = f.boff[1][b];
+  const int nf = f.boff[0][b + 1] - f0, n = nf + (f.boff[1][b + 1] - b0);
+  auto pass_of = [&](int k) { return k < nf ? f.blist[0][f0 + k] : f.blist[1][b0 + k - nf]; };
+  if (threadIdx.x >= 128) {
+    // the data of pass k that the sweep does not change
+    auto stage = [&](int k) {
+      const int pz = pass_of(k), t0 = f.pstart[pz], t1 = t0 + f.pcount[pz];
+      SweepPre<NSP> pl;
+      if (k < nf) {
+        pl = sweep_load<NSP, true>(d, t0 + (lane >> 2), t1, lane & 3);
+        if (lane < 8) s_fin[k & 1][lane] = fin_load<true>(d, t0 + lane, t1);
+      } else {
+        pl = sweep_load<NSP, false>(d, t0 + (lane >> 2), t1, lane & 3);
+        if (lane < 8) s_fin[k & 1][lane] = fin_load<false>(d, t0 + lane, t1);
+      }
+      s_pre[k & 1][lane] = pl;
+    };
+    auto poll = [&](int k) {
+      if (s_bad) return;
+      const int pz = pass_of(k), d0 = f.doff[pz], nd = f.doff[pz + 1] - d0;
+      bool ok = true;
+      for (int u = lane; u < nd; u += 32) ok = ok && wait_flag(f.pflag + f.deps[d0 + u], epoch, d.err, d.spin_limit);
+      if (__any_sync(0xffffffffu, !ok) && lane == 0) s_bad = 1;
+      __syncwarp();
+    };
+    // one look at the flags of pass k, without waiting
+    auto ready = [&](int k) -> bool {
+      if (s_bad) return true;
+      const int pz = pass_of(k), d0 = f.doff[pz], nd = f.doff[pz + 1] - d0;
+      bool ok = true;
+      for (int u = lane; u < nd; u += 32) ok = ok && ld_acquire(f.pflag + f.deps[d0 + u]) >= epoch;
+      return __all_sync(0xffffffffu, ok) != 0;
+    };
+    if (n > 0) {
+      stage(0);
+      poll(0);
+      bar_arrive(3, FLOW_THREADS);
+    }
+    // Never wait for other blocks while holding a finished, unpublished pass:
+    // if the next pass's flags are not all set yet, publish first.
+    for (int k = 0; k < n; ++k) {
+      const bool more = k + 1 < n;
+      bool go = false;
+      if (more) {
+        stage(k + 1);
+        go = ready(k + 1);
+      }
+      bar_named(4, FLOW_THREADS);
+      if (go) bar_arrive(3, FLOW_THREADS);
+      if (lane == 0 && !s_bad) st_release(f.pflag + pass_of(k), epoch);
+      if (more && !go) {
+        poll(k + 1);
+        bar_arrive(3, FLOW_THREADS);
+      }
+    }
+  } else {
+    const int role = threadIdx.x >> 5;
+    for (int k = 0; k < n; ++k) {
+      bar_named(3, FLOW_THREADS);
+      const SweepPre<NSP> p = s_pre[k & 1][lane];
+      const Fin4w fn = s_fin[k & 1][(role & 1) * 4 + (lane >> 3)];
+      double nbv[V];
+#pragma unroll
+      for (int v = 0; v < V; ++v) nbv[v] = p.act ? __ldcg(d.hWA + (size_t)v * d.NE + p.j) : 0.0;
+      if (k < nf) sweep4w_compute<NSP, true, true>(d, th, p, nbv, fn);
+      else sweep4w_compute<NSP, false, true>(d, th, p, nbv, fn);
+      bar_arrive(4, FLOW_THREADS);
+    }
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    __threadfence();
+    if (atomicAdd(f.ctr + 1, 1u) == gridDim.x - 1) {
+      f.ctr[1] = 0u;
+      __threadfence();
+      st_release(f.ctr, epoch);
+    }
+  }
+}
+
 template <int NSP, bool FWD>
 __global__ void __launch_bounds__(32) k_sweep4(const Dev d, const ThermoDev<NSP> th, int t0, int t1) {
   pdl_launch_dependents();
@@ -1079,7 +1245,11 @@ struct rc_ctx {
   bool persistent = true;       // LU-SGS sweeps as one cooperative launch (else one launch per level)
   bool can_persistent = false;  // the device can co-schedule the persistent LU-SGS grid
   int wide = 0;                 // FP64 per-level sweeps: 4 lanes per cell (0), 8 lanes (1, k_sweep8),
-                                // the two parts of a slot in two warps (2, k_sweep2w) or four (3, k_sweep4w)
+                                // the two parts of a slot in two warps (2, k_sweep2w) or four (3, k_sweep4w);
+                                // 4: the dataflow launch k_lusgs_flow (FP64; where it cannot run, as 3)
+  bool can_flow = false;        // the device can co-schedule the k_lusgs_flow grid
+  int flow_grid = 0;            // its blocks (one per SM)
+  FlowDev flow = {};            // its pass tables
   int pers_grid = 0;             // blocks of the persistent launch (one per SM)
   unsigned* lvl_count = nullptr; // per-level completion counters of the persistent launch
   int nlevels = 0;
@@ -1263,15 +1433,32 @@ void q_persistent(rc_ctx* c) {
   c->launches++;
 }
 template <int NSP>
+void q_flow(rc_ctx* c) {
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = dim3((unsigned)c->flow_grid);
+  cfg.blockDim = dim3(FLOW_THREADS);
+  cfg.stream = c->stream;
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeCooperative;
+  attr[0].val.cooperative = 1;
+  cfg.attrs = attr;
+  cfg.numAttrs = 1;
+  cudaLaunchKernelEx(&cfg, k_lusgs_flow<NSP>, c->d, TH<NSP>(c), c->flow);
+  c->launches++;
+  launch_pdl(k_update<NSP>, blocks(c->NE, c->d.bs), c->d.bs, c->stream, c->d, TH<NSP>(c));
+  c->launches++;
+}
+template <int NSP>
 void q_sweeps(rc_ctx* c, int gather) {
   if (gather) {
     k_gather<NSP><<<blocks(c->NE, c->d.bs), c->d.bs, 0, c->stream>>>(c->d, c->visc, c->comb);
     c->launches++;
   }
   if (c->persistent) { q_persistent<NSP>(c); return; }
+  if (c->wide == 4 && c->can_flow) { q_flow<NSP>(c); return; }
   for (size_t l = 0; l + 1 < c->fwd_off.size(); ++l) {
     const int n = c->fwd_off[l + 1] - c->fwd_off[l];
-    if (c->wide == 3) launch_pdl(k_sweep4w<NSP, true>, blocks(n, 8), 128, c->stream, c->d, TH<NSP>(c),
+    if (c->wide >= 3) launch_pdl(k_sweep4w<NSP, true>, blocks(n, 8), 128, c->stream, c->d, TH<NSP>(c),
                                  c->fwd_off[l], c->fwd_off[l + 1]);
     else if (c->wide == 2) launch_pdl(k_sweep2w<NSP, true>, blocks(n, 8), 64, c->stream, c->d, TH<NSP>(c),
                                       c->fwd_off[l], c->fwd_off[l + 1]);
@@ -1283,7 +1470,7 @@ void q_sweeps(rc_ctx* c, int gather) {
   }
   for (size_t l = 0; l + 1 < c->bwd_off.size(); ++l) {
     const int n = c->bwd_off[l + 1] - c->bwd_off[l];
-    if (c->wide == 3) launch_pdl(k_sweep4w<NSP, false>, blocks(n, 8), 128, c->stream, c->d, TH<NSP>(c),
+    if (c->wide >= 3) launch_pdl(k_sweep4w<NSP, false>, blocks(n, 8), 128, c->stream, c->d, TH<NSP>(c),
                                  c->bwd_off[l], c->bwd_off[l + 1]);
     else if (c->wide == 2) launch_pdl(k_sweep2w<NSP, false>, blocks(n, 8), 64, c->stream, c->d, TH<NSP>(c),
                                       c->bwd_off[l], c->bwd_off[l + 1]);
@@ -1899,6 +2086,66 @@ int init_impl(const rc_mesh* m, const rc_thermo* t, const rc_config* g, const Ba
       st |= dev_upload(c, tf, &p); d.swf[dir] = p;
     }
   }
+  {  // dataflow schedule of the sweeps (k_lusgs_flow): block b owns cells
+     // [b*C, (b+1)*C); a pass is a run of at most 8 consecutive positions of
+     // one level whose cells the same block owns
+    int nsm = 0;
+    cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, g->device);
+    const int G = std::max(nsm, 1), C = (NE + G - 1) / G;
+    std::vector<int> pstart, pcount, pdir, powner, doff(1, 0), deps;
+    std::vector<int> cellpass[2] = {std::vector<int>(NE, 0), std::vector<int>(NE, 0)};
+    std::vector<int> boff[2], blist[2];
+    for (int dir = 0; dir < 2; ++dir) {
+      const std::vector<int>& lst = dir == 0 ? fc : bc;
+      const std::vector<int>& off = dir == 0 ? c->fwd_off : c->bwd_off;
+      std::vector<std::vector<int>> per(G);
+      for (size_t l = 0; l + 1 < off.size(); ++l)
+        for (int t = off[l]; t < off[l + 1];) {
+          const int own = lst[t] / C;
+          int e = t + 1;
+          while (e < off[l + 1] && e - t < 8 && lst[e] / C == own) ++e;
+          const int pz = (int)pstart.size();
+          pstart.push_back(t); pcount.push_back(e - t); pdir.push_back(dir); powner.push_back(own);
+          per[own].push_back(pz);
+          for (int u = t; u < e; ++u) cellpass[dir][lst[u]] = pz;
+          t = e;
+        }
+      boff[dir].assign(1, 0);
+      for (int bb = 0; bb < G; ++bb) {
+        blist[dir].insert(blist[dir].end(), per[bb].begin(), per[bb].end());
+        boff[dir].push_back((int)blist[dir].size());
+      }
+    }
+    for (size_t pz = 0; pz < pstart.size(); ++pz) {
+      const int dir = pdir[pz];
+      const std::vector<int>& lst = dir == 0 ? fc : bc;
+      const size_t d0 = deps.size();
+      for (int u = pstart[pz]; u < pstart[pz] + pcount[pz]; ++u) {
+        const int i = lst[u];
+        for (int q = 0; q < nface[i]; ++q) {
+          const int j = cother[(size_t)q * NE + i];
+          if (j < 0 || (dir == 0 ? j >= i : j <= i) || j / C == powner[pz]) continue;
+          const int dp = cellpass[dir][j];
+          if (std::find(deps.begin() + (long)d0, deps.end(), dp) == deps.end()) deps.push_back(dp);
+        }
+      }
+      doff.push_back((int)deps.size());
+    }
+    FlowDev& f = c->flow;
+    int* ip;
+    st |= dev_upload(c, pstart, &ip); f.pstart = ip;
+    st |= dev_upload(c, pcount, &ip); f.pcount = ip;
+    for (int dir = 0; dir < 2; ++dir) {
+      st |= dev_upload(c, boff[dir], &ip); f.boff[dir] = ip;
+      st |= dev_upload(c, blist[dir], &ip); f.blist[dir] = ip;
+    }
+    st |= dev_upload(c, doff, &ip); f.doff = ip;
+    if (deps.empty()) deps.push_back(0);
+    st |= dev_upload(c, deps, &ip); f.deps = ip;
+    st |= dev_upload(c, std::vector<unsigned>(pstart.size() + 1, 0u), &f.pflag);
+    st |= dev_upload(c, std::vector<unsigned>(2, 0u), &f.ctr);
+    c->flow_grid = G;
+  }
   {  // boundary data per case, case layout
     std::vector<float> tab32(b.bctab.begin(), b.bctab.end());
     double* tp;
@@ -1933,9 +2180,12 @@ int init_impl(const rc_mesh* m, const rc_thermo* t, const rc_config* g, const Ba
     c->pers_grid = nsm;
     c->can_persistent = coop && nsm > 0 && occ64 >= 1 && occ32 >= 1;
     const std::string sc = sched ? sched : "";
-    const bool lv = sc == "levels" || sc == "levels8" || sc == "levels2w" || sc == "levels4w";
+    const bool lv = sc == "levels" || sc == "levels8" || sc == "levels2w" || sc == "levels4w" || sc == "flow";
     c->persistent = c->can_persistent && !lv;
-    c->wide = sc == "levels4w" ? 3 : sc == "levels2w" ? 2 : sc == "levels8" ? 1 : 0;
+    c->wide = sc == "flow" ? 4 : sc == "levels4w" ? 3 : sc == "levels2w" ? 2 : sc == "levels8" ? 1 : 0;
+    if (c->NSP == 1) cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ64, k_lusgs_flow<1>, FLOW_THREADS, 0);
+    else cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ64, k_lusgs_flow<4>, FLOW_THREADS, 0);
+    c->can_flow = coop && nsm > 0 && occ64 >= 1 && c->flow_grid == nsm;
   }
   *out = c;
   return RC_OK;
@@ -2016,18 +2266,29 @@ static int get_soa(rc_ctx* c, const double* src, double* host, int N, int V) {
   return check_launch(c, "k_soa_to_aos");
 }
 
+// The state moves through the two halves of the staging buffer (PA in the
+// first, WA in the second): both copies and both layout conversions are
+// queued back to back, and get_state synchronizes once.
 int rc_set_state(rc_ctx* c, const double* PA, const double* WA) {
   if (!c) return RC_ERR_ARG;
-  int st = 0;
-  if (PA) st |= put_soa(c, PA, c->d.PA, c->NE, c->V);
-  if (WA) st |= put_soa(c, WA, c->d.WA, c->NE, c->V);
-  return st;
+  const int N = c->NE, V = c->V;
+  const size_t n = (size_t)N * V;
+  if (PA) RC_CU(cudaMemcpyAsync(c->staging, PA, sizeof(double) * n, cudaMemcpyHostToDevice, c->stream));
+  if (WA) RC_CU(cudaMemcpyAsync(c->staging + n, WA, sizeof(double) * n, cudaMemcpyHostToDevice, c->stream));
+  if (PA) { k_aos_to_soa<<<blocks((long)n, 256), 256, 0, c->stream>>>(c->staging, c->d.PA, N, V); c->launches++; }
+  if (WA) { k_aos_to_soa<<<blocks((long)n, 256), 256, 0, c->stream>>>(c->staging + n, c->d.WA, N, V); c->launches++; }
+  return check_launch(c, "k_aos_to_soa");
 }
 int rc_get_state(rc_ctx* c, double* PA, double* WA) {
   if (!c) return RC_ERR_ARG;
-  int st = 0;
-  if (PA) st |= get_soa(c, c->d.PA, PA, c->NE, c->V);
-  if (WA) st |= get_soa(c, c->d.WA, WA, c->NE, c->V);
+  const int N = c->NE, V = c->V;
+  const size_t n = (size_t)N * V;
+  if (PA) { k_soa_to_aos<<<blocks((long)n, 256), 256, 0, c->stream>>>(c->d.PA, c->staging, N, V); c->launches++; }
+  if (WA) { k_soa_to_aos<<<blocks((long)n, 256), 256, 0, c->stream>>>(c->d.WA, c->staging + n, N, V); c->launches++; }
+  if (PA) RC_CU(cudaMemcpyAsync(PA, c->staging, sizeof(double) * n, cudaMemcpyDeviceToHost, c->stream));
+  if (WA) RC_CU(cudaMemcpyAsync(WA, c->staging + n, sizeof(double) * n, cudaMemcpyDeviceToHost, c->stream));
+  RC_CU(cudaStreamSynchronize(c->stream));
+  const int st = check_launch(c, "k_soa_to_aos");
   return st ? st : latch(c);
 }
 
@@ -2120,6 +2381,7 @@ int rc_autotune(rc_ctx* c, int iters, char* report, int report_len) {
       for (int bs : {128, 64}) cands.push_back({pers != 0, bs, cpw, 0});
   for (int wide : {1, 2, 3})
     for (int bs : {128, 64}) cands.push_back({false, bs, 8, wide});
+  if (c->can_flow && c->mode == RC_PREC_FP64) cands.push_back({false, 128, 8, 4});
   cudaEvent_t e0, e1;
   cudaEventCreate(&e0);
   cudaEventCreate(&e1);
@@ -2143,7 +2405,7 @@ int rc_autotune(rc_ctx* c, int iters, char* report, int report_len) {
     float ms = 0.f;
     cudaEventElapsedTime(&ms, e0, e1);
     const double per = ms / iters;
-    rep += std::string(k.pers ? "persistent" : k.wide == 3 ? "levels4w" : k.wide == 2 ? "levels2w" : k.wide ? "levels8" : "levels") +
+    rep += std::string(k.pers ? "persistent" : k.wide == 4 ? "flow" : k.wide == 3 ? "levels4w" : k.wide == 2 ? "levels2w" : k.wide ? "levels8" : "levels") +
            " bs=" + std::to_string(k.bs) + " cpw=" + std::to_string(k.wide >= 2 ? 8 : k.wide ? 4 : k.cpw) + ": " +
            std::to_string(per) + " ms; ";
     if (per < best) { best = per; bc = k; }
@@ -2159,7 +2421,7 @@ int rc_autotune(rc_ctx* c, int iters, char* report, int report_len) {
   cudaEventDestroy(e1);
   cudaFree(save);
   rep += std::string("chosen: ") +
-         (bc.pers ? "persistent" : bc.wide == 3 ? "levels4w" : bc.wide == 2 ? "levels2w" : bc.wide ? "levels8" : "levels") +
+         (bc.pers ? "persistent" : bc.wide == 4 ? "flow" : bc.wide == 3 ? "levels4w" : bc.wide == 2 ? "levels2w" : bc.wide ? "levels8" : "levels") +
          " bs=" + std::to_string(bc.bs) + " cpw=" + std::to_string(bc.wide >= 2 ? 8 : bc.wide ? 4 : bc.cpw);
   if (report && report_len > 0) {
     std::snprintf(report, (size_t)report_len, "%s", rep.c_str());

@@ -198,6 +198,22 @@ __device__ __forceinline__ bool wait_count(const unsigned* c, unsigned target, u
   __threadfence();
   return ok != 0;
 }
+// Dataflow LU-SGS: pass flags.  wait_flag: the calling thread waits until
+// the flag reaches `epoch` (acquire); bounded like wait_count.  set_flag
+// publishes a pass (release: the block's earlier stores, ordered before the
+// call by a block barrier, become visible with it).
+__device__ __forceinline__ void st_release(unsigned* p, unsigned v) {
+  asm volatile("st.release.gpu.global.u32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
+}
+__device__ __forceinline__ bool wait_flag(const unsigned* f, unsigned epoch, unsigned* err, unsigned limit) {
+  for (unsigned spin = 0; ld_acquire(f) < epoch; ++spin) {
+    if (spin >= limit || ((spin & 255u) == 255u && (ld_acquire(err) & ERR_SYNC))) {
+      atomicOr(err, ERR_SYNC);
+      return false;
+    }
+  }
+  return true;
+}
 // count_done: a warp's chunk of a level is done; every lane's stores are
 // made visible, then lane 0 counts the chunk.
 __device__ __forceinline__ void count_done(unsigned* c) {

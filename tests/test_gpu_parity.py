@@ -169,14 +169,15 @@ def test_device_stop_condition_is_reported(case_t1):
 
 @pytest.mark.parametrize("precision", [rc.RC_PREC_FP64, rc.RC_PREC_MIXED])
 def test_persistent_and_per_level_schedules_agree(case_root, precision, monkeypatch):
-    """The cooperative one-launch LU-SGS and the one-launch-per-level LU-SGS
+    """The cooperative one-launch LU-SGS, the one-launch-per-level LU-SGS
     (4 lanes per cell with 8 or 1 cells per warp, 8 lanes per cell, or the work
-    of each slot split over two or four warps) run the
-    same recurrences: identical states after 30 iterations."""
+    of each slot split over two or four warps) and the dataflow launch (FP64;
+    the mixed form runs its per-level sweeps under that name) run the same
+    recurrences: identical states after 30 iterations."""
     d = make_case(case_root, "c1", nx=40, ny=8)
     c = rc.Case(d)
     states = []
-    for sched in ("persistent", "levels", "levels8", "levels2w", "levels4w"):
+    for sched in ("persistent", "levels", "levels8", "levels2w", "levels4w", "flow"):
         for cpw in ("8", "1"):
             monkeypatch.setenv("RC_LUSGS_SCHEDULE", sched)
             monkeypatch.setenv("RC_LUSGS_CPW", cpw)
@@ -187,6 +188,47 @@ def test_persistent_and_per_level_schedules_agree(case_root, precision, monkeypa
     for st in states[1:]:
         assert np.array_equal(states[0][0], st[0])
         assert np.array_equal(states[0][1], st[1])
+
+
+def test_dataflow_schedule_bit_identical_to_oracle(case_root, monkeypatch):
+    """The dataflow LU-SGS (cells split into per-SM blocks, waits only on the
+    passes of other blocks that hold a neighbour) on the reacting viscous
+    case and on the colored order, 20 iterations against the oracle."""
+    monkeypatch.setenv("RC_LUSGS_SCHEDULE", "flow")
+    for name, over in (("t2", {}), ("c1", {"nx": 120, "ny": 20}), ("t2", {"order": "colored"})):
+        d = make_case(case_root, name, **over)
+        c = rc.Case(d)
+        s = rc.Solver(c)
+        s.run(20)
+        PA, WA = s.get_state()
+        o = oracle.Oracle(d, threads=4)
+        o.run(20)
+        assert np.array_equal(PA, o.array("PA")), (name, over)
+        assert np.array_equal(WA, o.array("WA")), (name, over)
+        s.close()
+
+
+def test_dataflow_wait_timeout_is_reported(case_root, monkeypatch):
+    """A poll limit of 1 makes the dataflow LU-SGS give up on a pass of
+    another block: RC_ERR_SYNC, every block still finishes the launch, and
+    after the error is cleared the next launches (a new epoch) are exact."""
+    monkeypatch.setenv("RC_LUSGS_SCHEDULE", "flow")
+    d = make_case(case_root, "c1", nx=60, ny=12)
+    c = rc.Case(d)
+    s = rc.Solver(c)
+    s.set_wait_limit(1)
+    s.lu_sgs_stage(1)
+    with pytest.raises(rc.RcError) as e:
+        s.sync()
+    assert e.value.code & 64
+    s.clear_error()
+    s.set_wait_limit(1 << 24)
+    s.set_state(c.array("PA"), c.array("WA"))
+    s.run(5)
+    o = oracle.Oracle(d, threads=4)
+    o.run(5)
+    PA, WA = s.get_state()
+    assert np.array_equal(PA, o.array("PA")) and np.array_equal(WA, o.array("WA"))
 
 
 def test_forced_level_wait_timeout_is_reported(case_root, monkeypatch):
