@@ -54,8 +54,8 @@ def algo_bytes_per_cell(V: int, nf_ne: float, viscous: bool, combustion: bool) -
 # capture in profiles/kernels_c2_30k_full.md; the traffic grows with the cells)
 # DRAM bytes per cell of one FP64 iteration of the 120,000-cell nozzle (ncu,
 # --cache-control none: the caches as the live run leaves them; profiles/)
-NCU_DRAM_PER_CELL = {"lu_sgs_steady": (23588864 + 12020224 + 6755328 + 3684096) / 120000,
-                     "flux_sourceterm": (19888128 + 26114816 + 2120704 + 5835520) / 120000}
+NCU_DRAM_PER_CELL = {"lu_sgs_steady": (25643776 + 13218816 + 6815488 + 3588096) / 120000,
+                     "flux_sourceterm": (22433024 + 25496320 + 2027776 + 6353152) / 120000}
 
 
 def read_peaks():
@@ -295,11 +295,12 @@ def main():
                          "frac": achieved / peak, "peak_source": peak_kind,
                          "algorithmic_bytes_per_cell": ab[dom],
                          "traffic": NCU_DRAM_PER_CELL[dom] * NE if dom in NCU_DRAM_PER_CELL else None,
-                         "traffic_source": "ncu capture of one iteration at 120,000 cells, caches as in the "
-                                           "live run (profiles/c2_fp64_launches.md), scaled by cells",
-                         "note": "LU-SGS is latency bound on its level barriers (natural cell order: 301+301 "
-                                 "levels); the face and cell kernels are FP64-issue bound (FP64 pipe 85-88%, "
-                                 "DRAM < 2%)"},
+                         "traffic_source": "ncu capture of one iteration at 120,000 cells with the dataflow "
+                                           "LU-SGS, caches as in the live run (profiles/c2_fp64_flow_launches.md), "
+                                           "scaled by cells",
+                         "note": "LU-SGS is latency bound: the dependent instruction chain of one pass of 8 "
+                                 "cells along 301+301 levels (natural cell order); the face and cell kernels "
+                                 "are FP64-issue bound (FP64 pipe 85-88%, DRAM < 2%)"},
             "subroutine_ms": sub_ms,
             "stage_algorithmic_gbs": ab["stage"] * NE / (t_max / args.steps) / 1e9,
             "levels": head["levels"],

@@ -19,9 +19,13 @@
  * Threading: one host thread per context; each context owns one CUDA stream.
  *
  * LU-SGS schedule: by default both sweeps of an iteration run as one
- * cooperative kernel with a grid barrier between levels; setting the
- * environment variable RC_LUSGS_SCHEDULE=levels before rc_init launches one
- * kernel per level instead.  Both compute the same recurrences bit for bit.
+ * cooperative kernel with a grid barrier between levels; rc_autotune picks the
+ * fastest of the schedules, and the environment variable RC_LUSGS_SCHEDULE,
+ * read by rc_init, fixes one: "levels", "levels8", "levels2w", "levels4w" (one
+ * kernel per level, with 4 or 8 lanes per cell or each slot's work over two
+ * or four warps) or "flow" (one cooperative dataflow kernel: per-SM blocks of
+ * cells, each pass waiting only for the passes of other blocks that hold its
+ * neighbours; FP64 form).  All compute the same recurrences bit for bit.
  */
 #ifndef RC_GPU_H
 #define RC_GPU_H
@@ -37,7 +41,7 @@ extern "C" {
 #define RC_ERR_NEG_FACE 8      /* rho or p < 0 at a face in flux_lax (flux_lax.f90:239-242) */
 #define RC_ERR_NAN 16          /* NaN in WA(1,1) after a stage (Time_LUSGS_steady.f90:94-97) */
 #define RC_ERR_BCTYPE 32       /* unknown boundary code (flux_lax.f90:232-235, update_flow_variables.f90:364-367) */
-#define RC_ERR_SYNC 64         /* a grid barrier of the persistent LU-SGS kernel gave up waiting (bounded spin) */
+#define RC_ERR_SYNC 64         /* a bounded wait of the cooperative LU-SGS kernels gave up (level counter or pass flag) */
 #define RC_ERR_LINSOLVE 128    /* a BDF2 cell system is singular to working precision (dgesvx info /= 0, la_math.f90:176-211) */
 #define RC_ERR_ARG 1024        /* invalid argument or unsupported configuration */
 #define RC_ERR_CUDA 2048       /* CUDA runtime failure */
@@ -176,8 +180,9 @@ int rc_set_wait_limit(rc_ctx* ctx, unsigned polls);
 int rc_clear_error(rc_ctx* ctx);
 
 /* Autotuner: times `iters` iterations of every launch configuration (LU-SGS
- * as one cooperative kernel or one kernel per level; 32, 64 or 128 threads
- * per block for the cell and face kernels) on the current state, keeps the
+ * as one cooperative kernel, one kernel per level or, in the FP64 form, the
+ * dataflow kernel; 64 or 128 threads per block for the cell and face kernels)
+ * on the current state, keeps the
  * fastest and restores the state.  The configurations compute the same bits.
  * report (may be null) gets one line of timings.  Synchronises. */
 int rc_autotune(rc_ctx* ctx, int iters, char* report, int report_len);

@@ -36,7 +36,7 @@ from . import build as _build
 RC_OK = 0
 RC_ERR = {1: "thermo T out of range", 2: "transport T out of range", 4: "negative rho/p/T in TimeStep",
           8: "negative rho/p at a face", 16: "NaN in WA(1,1)", 32: "unknown boundary code",
-          64: "grid barrier timed out", 128: "BDF2 cell system singular (dgesvx)",
+          64: "LU-SGS wait timed out", 128: "BDF2 cell system singular (dgesvx)",
           1024: "invalid argument", 2048: "CUDA error"}
 RC_PREC_FP64, RC_PREC_MIXED, RC_PREC_MIXED_DC = 0, 1, 2
 RC_CHEM_EXPLICIT, RC_CHEM_INTEGRATED, RC_CHEM_SURROGATE = 0, 1, 2
