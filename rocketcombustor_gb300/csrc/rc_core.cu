@@ -801,10 +801,6 @@ __global__ void __launch_bounds__(64) k_sweep2w(const Dev d, const ThermoDev<NSP
   for (int sl = 0; sl < 4; ++sl) df = df + w[r * 4 + sl];
   d.hWA[r * NE + fi] = FWD ? div_rn(R - df, fdd, fddh, fddl) : R - div_rn(df, fdd, fddh, fddl);
 }
-// named barrier over the first `count` threads of the block (warp multiples)
-__device__ __forceinline__ void bar_named(int id, int count) {
-  asm volatile("bar.sync %0, %1;" ::"r"(id), "r"(count) : "memory");
-}
 // one level with the work of each slot in four warps (the four SM
 // sub-partitions, each with its own FP64 pipe): block b (128 threads) takes
 // cells t0 + 8b .. + 7, lane = 4 cell + slot in every warp.
@@ -946,21 +942,7 @@ __global__ void __launch_bounds__(128) k_sweep4w(const Dev d, const ThermoDev<NS
 // reset between launches.  After a failed wait (ERR_SYNC latched) no flag is
 // published any more and every block runs to the end.  The Newton update
 // follows as its own launch.
-struct FlowDev {
-  const int* pstart;   // first sweep position of pass p
-  const int* pcount;   // its number of cells (1..8)
-  const int* boff[2];  // passes of block b: blist[d][boff[d][b] .. boff[d][b+1]), d = 0 forward, 1 backward
-  const int* blist[2];
-  const int* doff;     // passes that pass p waits for: deps[doff[p] .. doff[p+1])
-  const int* deps;
-  unsigned* pflag;     // per pass: epoch of the launch that finished it
-  unsigned* ctr;       // [0] epoch of the last finished launch, [1] finished blocks
-};
 constexpr int FLOW_THREADS = 160;
-// bar.arrive: count this warp in at barrier id without waiting
-__device__ __forceinline__ void bar_arrive(int id, int count) {
-  asm volatile("bar.arrive %0, %1;" ::"r"(id), "r"(count) : "memory");
-}
 template <int NSP>
 __global__ void __launch_bounds__(FLOW_THREADS) k_lusgs_flow(const Dev d, const ThermoDev<NSP> th, const FlowDev f) {
   constexpr int V = 3 + NSP;

@@ -198,6 +198,28 @@ __device__ __forceinline__ bool wait_count(const unsigned* c, unsigned target, u
   __threadfence();
   return ok != 0;
 }
+// named barrier over the first `count` threads of the block (warp multiples)
+__device__ __forceinline__ void bar_named(int id, int count) {
+  asm volatile("bar.sync %0, %1;" ::"r"(id), "r"(count) : "memory");
+}
+// bar.arrive: count this warp in at barrier id without waiting
+__device__ __forceinline__ void bar_arrive(int id, int count) {
+  asm volatile("bar.arrive %0, %1;" ::"r"(id), "r"(count) : "memory");
+}
+// Tables of the dataflow LU-SGS (k_lusgs_flow): cells are
+// split into per-SM blocks, a pass is a run of at most 8 consecutive sweep
+// positions of one level whose cells one block owns.
+struct FlowDev {
+  const int* pstart;   // first sweep position of pass p
+  const int* pcount;   // its number of cells (1..8)
+  const int* boff[2];  // passes of block b: blist[d][boff[d][b] .. boff[d][b+1]), d = 0 forward, 1 backward
+  const int* blist[2];
+  const int* doff;     // passes that pass p waits for: deps[doff[p] .. doff[p+1])
+  const int* deps;
+  unsigned* pflag;     // per pass: epoch of the launch that finished it
+  unsigned* ctr;       // [0] epoch of the last finished launch, [1] finished blocks
+};
+
 // Dataflow LU-SGS: pass flags.  wait_flag: the calling thread waits until
 // the flag reaches `epoch` (acquire); bounded like wait_count.  set_flag
 // publishes a pass (release: the block's earlier stores, ordered before the
