@@ -151,11 +151,13 @@ int rc_init_batch(int ncase, const rc_mesh* meshes, const rc_thermo* thermos, co
 int rc_batch_info(rc_ctx* ctx, int* ncase, int* cell_offsets);
 
 /* PA(NVar,NE), WA(NVar,NE) in the Fortran layout (module.f90:54).  Either
- * pointer may be null.  rc_set_state queues the copies on the context's stream
- * and returns: from page-locked host memory the copy may still be in flight,
- * so the caller keeps such buffers unchanged until its next call that
- * synchronises (rc_get_state, rc_residual, rc_sync).  rc_get_state returns
- * when both arrays are on the host. */
+ * pointer may be null.  Page-locked host buffers (cudaHostAlloc,
+ * cudaHostRegister) are read and written in place by the device's layout
+ * kernel; pageable ones go through one copy.  rc_set_state queues its work on
+ * the context's stream and returns: from page-locked memory the device may
+ * still be reading, so the caller keeps such buffers unchanged until its next
+ * call that synchronises (rc_get_state, rc_residual, rc_sync).  rc_get_state
+ * returns when both arrays are on the host. */
 int rc_set_state(rc_ctx* ctx, const double* PA, const double* WA);
 int rc_get_state(rc_ctx* ctx, double* PA, double* WA);
 

@@ -2248,27 +2248,51 @@ static int get_soa(rc_ctx* c, const double* src, double* host, int N, int V) {
   return check_launch(c, "k_soa_to_aos");
 }
 
-// The state moves through the two halves of the staging buffer (PA in the
-// first, WA in the second): both copies and both layout conversions are
-// queued back to back, and get_state synchronizes once.
+// The device address of a page-locked host buffer, which kernels can read and
+// write in place (over the CPU-GPU link); null for pageable memory.
+static double* mapped_host(const void* p) {
+  cudaPointerAttributes at;
+  if (cudaPointerGetAttributes(&at, p) != cudaSuccess) {
+    cudaGetLastError();
+    return nullptr;
+  }
+  return at.type == cudaMemoryTypeHost ? static_cast<double*>(at.devicePointer) : nullptr;
+}
+// The state (PA, WA): a page-locked host array is converted in place by the
+// layout kernel; a pageable one goes through its half of the staging buffer
+// (PA the first, WA the second) with one copy.  get_state synchronizes once.
 int rc_set_state(rc_ctx* c, const double* PA, const double* WA) {
   if (!c) return RC_ERR_ARG;
   const int N = c->NE, V = c->V;
   const size_t n = (size_t)N * V;
-  if (PA) RC_CU(cudaMemcpyAsync(c->staging, PA, sizeof(double) * n, cudaMemcpyHostToDevice, c->stream));
-  if (WA) RC_CU(cudaMemcpyAsync(c->staging + n, WA, sizeof(double) * n, cudaMemcpyHostToDevice, c->stream));
-  if (PA) { k_aos_to_soa<<<blocks((long)n, 256), 256, 0, c->stream>>>(c->staging, c->d.PA, N, V); c->launches++; }
-  if (WA) { k_aos_to_soa<<<blocks((long)n, 256), 256, 0, c->stream>>>(c->staging + n, c->d.WA, N, V); c->launches++; }
+  const double* src[2] = {PA, WA};
+  double* dst[2] = {c->d.PA, c->d.WA};
+  for (int a = 0; a < 2; ++a) {
+    if (!src[a]) continue;
+    const double* m = mapped_host(src[a]);
+    if (!m) {
+      RC_CU(cudaMemcpyAsync(c->staging + a * n, src[a], sizeof(double) * n, cudaMemcpyHostToDevice, c->stream));
+      m = c->staging + a * n;
+    }
+    k_aos_to_soa<<<blocks((long)n, 256), 256, 0, c->stream>>>(m, dst[a], N, V);
+    c->launches++;
+  }
   return check_launch(c, "k_aos_to_soa");
 }
 int rc_get_state(rc_ctx* c, double* PA, double* WA) {
   if (!c) return RC_ERR_ARG;
   const int N = c->NE, V = c->V;
   const size_t n = (size_t)N * V;
-  if (PA) { k_soa_to_aos<<<blocks((long)n, 256), 256, 0, c->stream>>>(c->d.PA, c->staging, N, V); c->launches++; }
-  if (WA) { k_soa_to_aos<<<blocks((long)n, 256), 256, 0, c->stream>>>(c->d.WA, c->staging + n, N, V); c->launches++; }
-  if (PA) RC_CU(cudaMemcpyAsync(PA, c->staging, sizeof(double) * n, cudaMemcpyDeviceToHost, c->stream));
-  if (WA) RC_CU(cudaMemcpyAsync(WA, c->staging + n, sizeof(double) * n, cudaMemcpyDeviceToHost, c->stream));
+  const double* src[2] = {c->d.PA, c->d.WA};
+  double* dst[2] = {PA, WA};
+  for (int a = 0; a < 2; ++a) {
+    if (!dst[a]) continue;
+    double* m = mapped_host(dst[a]);
+    k_soa_to_aos<<<blocks((long)n, 256), 256, 0, c->stream>>>(src[a], m ? m : c->staging + a * n, N, V);
+    c->launches++;
+    if (!m)
+      RC_CU(cudaMemcpyAsync(dst[a], c->staging + a * n, sizeof(double) * n, cudaMemcpyDeviceToHost, c->stream));
+  }
   RC_CU(cudaStreamSynchronize(c->stream));
   const int st = check_launch(c, "k_soa_to_aos");
   return st ? st : latch(c);
