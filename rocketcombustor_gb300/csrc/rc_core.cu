@@ -801,17 +801,21 @@ __global__ void __launch_bounds__(64) k_sweep2w(const Dev d, const ThermoDev<NSP
   for (int sl = 0; sl < 4; ++sl) df = df + w[r * 4 + sl];
   d.hWA[r * NE + fi] = FWD ? div_rn(R - df, fdd, fddh, fddl) : R - div_rn(df, fdd, fddh, fddl);
 }
-// one level with the work of each slot in four warps (the four SM
-// sub-partitions, each with its own FP64 pipe): block b (128 threads) takes
-// cells t0 + 8b .. + 7, lane = 4 cell + slot in every warp.
-//   warp 0: s1 = sum h_k dY_k              then c1
-//   warp 1: s2 = sum R_k dY_k, Q = T s2 gamma / (gamma-1)   then c2
-//   warp 2: X = du u + du rho u + dv v + dv rho v, dp = (gamma-1)((dE - s1 + Q) - X/2)   then c3
-//   warp 3: c0 and the species terms
-// with the velocity increments formed in every warp; warps 0 and 1 then
-// finish cells 0-3 and 4-7 (8 lanes per cell).  Every expression is the one
-// of sweep_terms in the same order, so the same bits; the longest warp chain
-// is about two thirds of k_sweep2w's.
+// one level with the work of each slot in four warps: block b (128 threads)
+// takes cells t0 + 8b .. + 7, lane = 4 cell + slot in every warp, in three
+// phases between named barriers 5 (all warps), 6 and 7:
+//   A  warp 0: s1 = sum h_k dY_k and c0     warp 1: s2 = sum R_k dY_k and
+//      Q = T s2 gamma / (gamma-1)           warp 2: du      warp 3: dv
+//   B  warp 2: X = du u + du rho u + dv v + dv rho v,
+//      dp = (gamma-1)((dE - s1 + Q) - X/2)
+//      warp 3: dun = du nx + dv ny (published before barrier 6), then the
+//      species terms
+//   C  warps 0-2: c1, c2, c3
+// then warps 0 and 1 finish cells 0-3 and 4-7 (8 lanes per cell).  The SM's
+// FP64 pipe is shared by the four warps (an FP64 instruction of a full warp
+// holds it for 16 cycles on GB300), so each quantity is formed once, in one
+// warp, and exchanged through shared memory.  Every expression is the one of
+// sweep_terms in the same order, so the same bits.
 // hWA as the sweeps read it: through L2 (ld.global.cg) where other SMs write
 // it during the launch (the dataflow schedule), else a plain load
 template <bool L2>
@@ -841,62 +845,75 @@ __device__ __forceinline__ Fin4w fin_load(const Dev& d, int ft, int t1) {
 // lane = 4 cell + slot): p is the thread's (cell, slot) data from sweep_load,
 // nbv the hWA of its neighbour (V values; unused when the slot is inactive),
 // fn the data of the cell it finishes (warps 0 and 1, 8 lanes per cell).
-// Barriers 1, 2 (warps 0-2) and 7 (warps 0-3) are used.
+// Named barriers 5, 6 and 7 (warps 0-3) are used.
 template <int NSP, bool FWD, bool L2>
 __device__ __forceinline__ void sweep4w_compute(const Dev& d, const ThermoDev<NSP>& th, const SweepPre<NSP>& p,
                                                 const double* nbv, const Fin4w& fn) {
   constexpr int V = 3 + NSP;
   const int NE = d.NE, role = threadIdx.x >> 5, lane = threadIdx.x & 31, cell = lane >> 2, q = lane & 3;
   __shared__ double wsm[8 * V * 4];
-  __shared__ double xs1[32], xq[32], xdp[32];
+  __shared__ double xs1[32], xq[32], xdp[32], xdu[32], xdv[32], xdn[32];
   const int fcell = (role & 1) * 4 + (lane >> 3), r = lane & 7;
   const bool fvalid = role < 2 && fn.i >= 0 && r < V;
   const int fi = fvalid ? fn.i : 0;
   const double fdd = fn.dd, fddh = fn.ddh, fddl = fn.ddl;
   const double R = fvalid ? ldh<L2>(d.hWA + r * NE + fi) : 0.0;
   double* w = wsm + cell * V * 4;
-  double drr = 0, dru = 0, drv = 0, dre = 0, duu = 0, dvv = 0, dunormal = 0, X = 0, dry[NSP];
+  const double aF = p.aF, unormal = p.unormal;
+  const double drr = nbv[0], dru = nbv[1], drv = nbv[2], dre = nbv[3];
+  double dry[NSP];
 #pragma unroll
   for (int k = 0; k < NSP; ++k) dry[k] = 0.0;
-  const double aF = p.aF, unormal = p.unormal;
-  if (p.act) {
-    drr = nbv[0]; dru = nbv[1]; drv = nbv[2]; dre = nbv[3];
+  if (role != 2) {  // the species increments: warps 0, 1 and 3
     double s = 0.0;
 #pragma unroll
     for (int k = 0; k < NSP - 1; ++k) { dry[k] = nbv[4 + k]; s = s + dry[k]; }
     dry[NSP - 1] = drr - s;
-    duu = div_rn(dru - p.uu * drr, p.rr, p.rrh, p.rrl);
-    dvv = div_rn(drv - p.vv * drr, p.rr, p.rrh, p.rrl);
-    dunormal = duu * p.dx + dvv * p.dy;
-    if (role == 0) {
+  }
+  // A
+  if (role == 0) {
+    if (p.act) {
       double s1 = 0.0;
 #pragma unroll
       for (int k = 0; k < NSP; ++k) s1 = s1 + p.cs[k] * dry[k];
-      xs1[q + 4 * cell] = s1;
-    } else if (role == 1) {
+      xs1[lane] = s1;
+    }
+    w[q] = p.act ? 0.5 * (-aF * drr + dru * p.dx + drv * p.dy) : 0.0;
+  } else if (role == 1) {
+    if (p.act) {
       double s2 = 0.0;
 #pragma unroll
       for (int k = 0; k < NSP; ++k) s2 = s2 + th.R[k] * dry[k];
-      xq[q + 4 * cell] = div_rn(p.tt * s2 * p.gama, p.gm1, p.gmh, p.gml);
-    } else if (role == 2) {
-      X = dru * p.uu + duu * p.rou + drv * p.vv + dvv * p.rov;
-    } else {
-      w[q] = 0.5 * (-aF * drr + dru * p.dx + drv * p.dy);
-#pragma unroll
-      for (int k = 0; k < NSP - 1; ++k) w[(4 + k) * 4 + q] = 0.5 * (-aF * dry[k] + dry[k] * unormal + p.ry[k] * dunormal);
+      xq[lane] = div_rn(p.tt * s2 * p.gama, p.gm1, p.gmh, p.gml);
     }
-  } else if (role == 3) {
-#pragma unroll
-    for (int k = 0; k < V; ++k)
-      if (k == 0 || k >= 4) w[k * 4 + q] = 0.0;
+  } else if (role == 2) {
+    if (p.act) xdu[lane] = div_rn(dru - p.uu * drr, p.rr, p.rrh, p.rrl);
+  } else {
+    if (p.act) xdv[lane] = div_rn(drv - p.vv * drr, p.rr, p.rrh, p.rrl);
   }
-  if (role < 3) {
-    bar_named(1, 96);
-    if (role == 2 && p.act) xdp[q + 4 * cell] = p.gm1 * (dre - xs1[q + 4 * cell] + xq[q + 4 * cell] - 0.5 * X);
-    bar_named(2, 96);
-    const double dpp = xdp[q + 4 * cell];
+  bar_named(5, 128);
+  // B
+  if (role == 3) {
+    double dunormal = 0.0;
+    if (p.act) {
+      dunormal = xdu[lane] * p.dx + xdv[lane] * p.dy;
+      xdn[lane] = dunormal;
+    }
+    bar_arrive(6, 128);
+#pragma unroll
+    for (int k = 0; k < NSP - 1; ++k)
+      w[(4 + k) * 4 + q] = p.act ? 0.5 * (-aF * dry[k] + dry[k] * unormal + p.ry[k] * dunormal) : 0.0;
+  } else {
+    if (role == 2 && p.act) {
+      const double duu = xdu[lane], dvv = xdv[lane];
+      const double X = dru * p.uu + duu * p.rou + drv * p.vv + dvv * p.rov;
+      xdp[lane] = p.gm1 * (dre - xs1[lane] + xq[lane] - 0.5 * X);
+    }
+    bar_named(6, 128);
+    // C
     double ck = 0.0;
     if (p.act) {
+      const double dpp = xdp[lane], dunormal = xdn[lane];
       if (role == 0) ck = 0.5 * (-aF * dru + dru * unormal + p.rou * dunormal + dpp * p.dx);
       else if (role == 1) ck = 0.5 * (-aF * drv + drv * unormal + p.rov * dunormal + dpp * p.dy);
       else ck = 0.5 * (-aF * dre + dunormal * p.roepp + unormal * (dre + dpp));
