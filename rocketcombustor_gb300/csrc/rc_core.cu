@@ -1241,7 +1241,7 @@ struct rc_ctx {
   int* fwd_cells = nullptr;
   int* bwd_cells = nullptr;
   std::vector<int> fwd_off, bwd_off;
-  bool persistent = true;       // LU-SGS sweeps as one cooperative launch (else one launch per level)
+  bool persistent = false;      // LU-SGS sweeps as one cooperative launch with level counters
   bool can_persistent = false;  // the device can co-schedule the persistent LU-SGS grid
   int wide = 0;                 // FP64 per-level sweeps: 4 lanes per cell (0), 8 lanes (1, k_sweep8),
                                 // the two parts of a slot in two warps (2, k_sweep2w) or four (3, k_sweep4w);
@@ -2161,9 +2161,8 @@ int init_impl(const rc_mesh* m, const rc_thermo* t, const rc_config* g, const Ba
     if (!b.gcase.empty()) { st |= dev_upload(c, b.gcase, &ip); d.gcase = ip; }
   }
   if (st) return bail(st, c->err);
-  // LU-SGS schedule: one cooperative launch per iteration when every SM can
-  // hold a block of the persistent kernels; RC_LUSGS_SCHEDULE=levels selects
-  // one launch per level instead.
+  // LU-SGS schedule: which cooperative kernels every SM can hold a block of,
+  // and the schedule RC_LUSGS_SCHEDULE names (rc_autotune may change it).
   {
     int nsm = 0, occ64 = 0, occ32 = 0, coop = 0;
     cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, g->device);
@@ -2178,10 +2177,12 @@ int init_impl(const rc_mesh* m, const rc_thermo* t, const rc_config* g, const Ba
     const char* sched = std::getenv("RC_LUSGS_SCHEDULE");
     c->pers_grid = nsm;
     c->can_persistent = coop && nsm > 0 && occ64 >= 1 && occ32 >= 1;
+    // default (no or another value): the dataflow launch for FP64 (the four-warp
+    // per-level sweeps where it cannot run) and the per-level sweeps for the
+    // mixed forms
     const std::string sc = sched ? sched : "";
-    const bool lv = sc == "levels" || sc == "levels8" || sc == "levels2w" || sc == "levels4w" || sc == "flow";
-    c->persistent = c->can_persistent && !lv;
-    c->wide = sc == "flow" ? 4 : sc == "levels4w" ? 3 : sc == "levels2w" ? 2 : sc == "levels8" ? 1 : 0;
+    c->persistent = c->can_persistent && sc == "persistent";
+    c->wide = sc == "levels" ? 0 : sc == "levels8" ? 1 : sc == "levels2w" ? 2 : sc == "levels4w" ? 3 : 4;
     if (c->NSP == 1) cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ64, k_lusgs_flow<1>, FLOW_THREADS, 0);
     else cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ64, k_lusgs_flow<4>, FLOW_THREADS, 0);
     c->can_flow = coop && nsm > 0 && occ64 >= 1 && c->flow_grid == nsm;
