@@ -182,6 +182,19 @@ int rc_set_wait_limit(rc_ctx* ctx, unsigned polls);
 /* Clear the latched stop conditions (after the caller has dealt with them). */
 int rc_clear_error(rc_ctx* ctx);
 
+/* Host-only check of the dataflow LU-SGS plan that rc_init builds for the
+ * cell graph (no device work; callable without a GPU).  nface[i] <= 4 faces of
+ * cell i, cother[q*ne + i] the cell across face q (-1 at a boundary), nblocks
+ * blocks.  Checks that every cell is in exactly one pass of each sweep, that a
+ * pass's dependencies are passes of other blocks at lower levels and cover
+ * every neighbour it reads from another block, and runs the blocks' protocol
+ * in rounds (each block finishes its next pass once its dependencies are
+ * done) to the end.  stats[8]: forward passes, backward passes, dependencies,
+ * most dependencies of one pass, rounds, forward levels, backward levels,
+ * cells per block.  Returns RC_OK, RC_ERR_ARG (bad input) or RC_ERR_SYNC (a
+ * check failed or the rounds stalled). */
+int rc_flow_plan_check(int ne, int nblocks, const int* nface, const int* cother, long long* stats);
+
 /* Autotuner: times `iters` iterations of every launch configuration (LU-SGS
  * as one cooperative kernel, one kernel per level or, in the FP64 form, the
  * dataflow kernel; 64 or 128 threads per block for the cell and face kernels)

@@ -137,6 +137,7 @@ SIGNATURES = {
     "rc_euler_lusgs": (_i, [_vp, _i, _d]),
     "rc_case_unsteady": (_i, [_vp, _DP]),
     "rc_run_unsteady": (_i, [_vp, _i, _l, _l, _DP, _IP]),
+    "rc_flow_plan_check": (_i, [_i, _i, _IP, _IP, ctypes.POINTER(ctypes.c_longlong)]),
 }
 
 _lib: Optional[ctypes.CDLL] = None
@@ -190,6 +191,22 @@ _CASE_ARRAYS = {  # name -> (dtype, shape from dims NE,NF,NNT,NVar,Nsp,MaxNei,Ng
     "XYH": (np.float64, lambda d: (d[0], 2)), "PA": (np.float64, lambda d: (d[0], d[3])),
     "WA": (np.float64, lambda d: (d[0], d[3])),
 }
+
+
+def flow_plan_check(nface: np.ndarray, cother: np.ndarray, nblocks: int) -> dict:
+    """The host-side check of the dataflow LU-SGS plan (rc_flow_plan_check; no
+    GPU needed).  nface (NE,) faces per cell; cother (NE, 4) the cell across
+    each face, -1 at a boundary.  Raises RcError when a check fails."""
+    nface = np.ascontiguousarray(nface, dtype=np.int32)
+    ne = nface.shape[0]
+    co = np.ascontiguousarray(np.asarray(cother, dtype=np.int32).reshape(ne, 4).T)  # [q * NE + i]
+    stats = np.zeros(8, np.int64)
+    st = load().rc_flow_plan_check(ne, int(nblocks), nface.ctypes.data_as(_IP), co.ctypes.data_as(_IP),
+                                   stats.ctypes.data_as(ctypes.POINTER(ctypes.c_longlong)))
+    if st:
+        raise RcError(st, "dataflow plan check failed" if st == 64 else "bad arguments")
+    keys = ("passes_fwd", "passes_bwd", "deps", "max_deps", "rounds", "levels_fwd", "levels_bwd", "cells_per_block")
+    return dict(zip(keys, (int(v) for v in stats)))
 
 
 class Case:

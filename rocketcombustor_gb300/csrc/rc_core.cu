@@ -1337,6 +1337,105 @@ int dev_zeros(rc_ctx* c, size_t n, T** out) {
 
 double hmax(double a, double b) { return (b > a) ? b : a; }
 
+// ---- LU-SGS planning (host only)
+// The level order of both sweeps over the reference cell order: forward, the
+// level of cell i is 1 + the largest level of its neighbours j < i; backward,
+// of its neighbours j > i.  cells[d] lists the cells level by level (ascending
+// index inside a level), off[d] the level boundaries.  nface[i] faces,
+// cother[q*NE + i] the cell across face q (-1 at a boundary).
+struct SweepOrder {
+  std::vector<int> cells[2], off[2];
+};
+template <class NF>
+SweepOrder sweep_order(int NE, const NF& nface, const std::vector<int>& cother) {
+  std::vector<int> lev[2] = {std::vector<int>(NE, 0), std::vector<int>(NE, 0)};
+  int mx[2] = {0, 0};
+  for (int i = 0; i < NE; ++i) {
+    int l = 0;
+    for (int q = 0; q < nface[i]; ++q) {
+      const int j = cother[(size_t)q * NE + i];
+      if (j >= 0 && j < i) l = std::max(l, lev[0][j] + 1);
+    }
+    lev[0][i] = l; mx[0] = std::max(mx[0], l);
+  }
+  for (int i = NE - 1; i >= 0; --i) {
+    int l = 0;
+    for (int q = 0; q < nface[i]; ++q) {
+      const int j = cother[(size_t)q * NE + i];
+      if (j > i) l = std::max(l, lev[1][j] + 1);
+    }
+    lev[1][i] = l; mx[1] = std::max(mx[1], l);
+  }
+  SweepOrder so;
+  for (int d = 0; d < 2; ++d) {
+    std::vector<int>& off = so.off[d];
+    off.assign(mx[d] + 2, 0);
+    for (int i = 0; i < NE; ++i) off[lev[d][i] + 1]++;
+    for (int l = 0; l <= mx[d]; ++l) off[l + 1] += off[l];
+    so.cells[d].assign(NE, 0);
+    std::vector<int> pos(off.begin(), off.end() - 1);
+    for (int i = 0; i < NE; ++i) so.cells[d][pos[lev[d][i]]++] = i;
+  }
+  return so;
+}
+// The dataflow schedule (k_lusgs_flow) over G blocks: block b owns the cells
+// [b*C, (b+1)*C), C = ceil(NE/G); a pass is a run of at most 8 consecutive
+// positions of one level whose cells one block owns; a block's passes are
+// listed forward then backward in level order; a pass depends on the passes
+// (same sweep) of the neighbours it reads that other blocks own.
+struct FlowPlan {
+  int C = 1;
+  std::vector<int> pstart, pcount, pdir, powner, plevel, doff, deps;
+  std::vector<int> boff[2], blist[2];
+  std::vector<int> cellpass[2];
+};
+template <class NF>
+FlowPlan flow_plan(int NE, int G, const NF& nface, const std::vector<int>& cother, const SweepOrder& so) {
+  FlowPlan fp;
+  fp.C = (NE + G - 1) / G;
+  const int C = fp.C;
+  fp.doff.assign(1, 0);
+  for (int dir = 0; dir < 2; ++dir) {
+    const std::vector<int>& lst = so.cells[dir];
+    const std::vector<int>& off = so.off[dir];
+    fp.cellpass[dir].assign(NE, 0);
+    std::vector<std::vector<int>> per(G);
+    for (size_t l = 0; l + 1 < off.size(); ++l)
+      for (int t = off[l]; t < off[l + 1];) {
+        const int own = lst[t] / C;
+        int e = t + 1;
+        while (e < off[l + 1] && e - t < 8 && lst[e] / C == own) ++e;
+        const int pz = (int)fp.pstart.size();
+        fp.pstart.push_back(t); fp.pcount.push_back(e - t); fp.pdir.push_back(dir); fp.powner.push_back(own);
+        fp.plevel.push_back((int)l);
+        per[own].push_back(pz);
+        for (int u = t; u < e; ++u) fp.cellpass[dir][lst[u]] = pz;
+        t = e;
+      }
+    fp.boff[dir].assign(1, 0);
+    for (int bb = 0; bb < G; ++bb) {
+      fp.blist[dir].insert(fp.blist[dir].end(), per[bb].begin(), per[bb].end());
+      fp.boff[dir].push_back((int)fp.blist[dir].size());
+    }
+  }
+  for (size_t pz = 0; pz < fp.pstart.size(); ++pz) {
+    const int dir = fp.pdir[pz];
+    const std::vector<int>& lst = so.cells[dir];
+    const size_t d0 = fp.deps.size();
+    for (int u = fp.pstart[pz]; u < fp.pstart[pz] + fp.pcount[pz]; ++u) {
+      const int i = lst[u];
+      for (int q = 0; q < nface[i]; ++q) {
+        const int j = cother[(size_t)q * NE + i];
+        if (j < 0 || (dir == 0 ? j >= i : j <= i) || j / C == fp.powner[pz]) continue;
+        const int dp = fp.cellpass[dir][j];
+        if (std::find(fp.deps.begin() + (long)d0, fp.deps.end(), dp) == fp.deps.end()) fp.deps.push_back(dp);
+      }
+    }
+    fp.doff.push_back((int)fp.deps.size());
+  }
+  return fp;
+}
+
 template <int NSP>
 void fill_thermo(const rc_thermo* t, const rc_config* g, ThermoDev<NSP>& th) {
   std::memset(&th, 0, sizeof(th));
@@ -1936,35 +2035,11 @@ int init_impl(const rc_mesh* m, const rc_thermo* t, const rc_config* g, const Ba
     gsn[NG + j] = sav2 / sav;
   }
   // ---- LU-SGS levels over the reference cell order
-  std::vector<int> lf(NE, 0), lbk(NE, 0);
-  int mf = 0, mb = 0;
-  for (int i = 0; i < NE; ++i) {
-    int l = 0;
-    for (int q = 0; q < nface[i]; ++q) {
-      const int j = cother[(size_t)q * NE + i];
-      if (j >= 0 && j < i) l = std::max(l, lf[j] + 1);
-    }
-    lf[i] = l; mf = std::max(mf, l);
-  }
-  for (int i = NE - 1; i >= 0; --i) {
-    int l = 0;
-    for (int q = 0; q < nface[i]; ++q) {
-      const int j = cother[(size_t)q * NE + i];
-      if (j > i) l = std::max(l, lbk[j] + 1);
-    }
-    lbk[i] = l; mb = std::max(mb, l);
-  }
-  auto group = [&](const std::vector<int>& lev, int mx, std::vector<int>& cells, std::vector<int>& off) {
-    off.assign(mx + 2, 0);
-    for (int i = 0; i < NE; ++i) off[lev[i] + 1]++;
-    for (int l = 0; l <= mx; ++l) off[l + 1] += off[l];
-    cells.assign(NE, 0);
-    std::vector<int> p(off.begin(), off.end() - 1);
-    for (int i = 0; i < NE; ++i) cells[p[lev[i]]++] = i;
-  };
-  std::vector<int> fc, bc;
-  group(lf, mf, fc, c->fwd_off);
-  group(lbk, mb, bc, c->bwd_off);
+  const SweepOrder so = sweep_order(NE, nface, cother);
+  const std::vector<int>& fc = so.cells[0];
+  const std::vector<int>& bc = so.cells[1];
+  c->fwd_off = so.off[0];
+  c->bwd_off = so.off[1];
 
   // ---- thermo tables
   if (c->NSP == 1) {
@@ -2085,51 +2160,17 @@ int init_impl(const rc_mesh* m, const rc_thermo* t, const rc_config* g, const Ba
       st |= dev_upload(c, tf, &p); d.swf[dir] = p;
     }
   }
-  {  // dataflow schedule of the sweeps (k_lusgs_flow): block b owns cells
-     // [b*C, (b+1)*C); a pass is a run of at most 8 consecutive positions of
-     // one level whose cells the same block owns
+  {  // dataflow schedule of the sweeps (k_lusgs_flow), one block per SM
     int nsm = 0;
     cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, g->device);
-    const int G = std::max(nsm, 1), C = (NE + G - 1) / G;
-    std::vector<int> pstart, pcount, pdir, powner, doff(1, 0), deps;
-    std::vector<int> cellpass[2] = {std::vector<int>(NE, 0), std::vector<int>(NE, 0)};
-    std::vector<int> boff[2], blist[2];
-    for (int dir = 0; dir < 2; ++dir) {
-      const std::vector<int>& lst = dir == 0 ? fc : bc;
-      const std::vector<int>& off = dir == 0 ? c->fwd_off : c->bwd_off;
-      std::vector<std::vector<int>> per(G);
-      for (size_t l = 0; l + 1 < off.size(); ++l)
-        for (int t = off[l]; t < off[l + 1];) {
-          const int own = lst[t] / C;
-          int e = t + 1;
-          while (e < off[l + 1] && e - t < 8 && lst[e] / C == own) ++e;
-          const int pz = (int)pstart.size();
-          pstart.push_back(t); pcount.push_back(e - t); pdir.push_back(dir); powner.push_back(own);
-          per[own].push_back(pz);
-          for (int u = t; u < e; ++u) cellpass[dir][lst[u]] = pz;
-          t = e;
-        }
-      boff[dir].assign(1, 0);
-      for (int bb = 0; bb < G; ++bb) {
-        blist[dir].insert(blist[dir].end(), per[bb].begin(), per[bb].end());
-        boff[dir].push_back((int)blist[dir].size());
-      }
-    }
-    for (size_t pz = 0; pz < pstart.size(); ++pz) {
-      const int dir = pdir[pz];
-      const std::vector<int>& lst = dir == 0 ? fc : bc;
-      const size_t d0 = deps.size();
-      for (int u = pstart[pz]; u < pstart[pz] + pcount[pz]; ++u) {
-        const int i = lst[u];
-        for (int q = 0; q < nface[i]; ++q) {
-          const int j = cother[(size_t)q * NE + i];
-          if (j < 0 || (dir == 0 ? j >= i : j <= i) || j / C == powner[pz]) continue;
-          const int dp = cellpass[dir][j];
-          if (std::find(deps.begin() + (long)d0, deps.end(), dp) == deps.end()) deps.push_back(dp);
-        }
-      }
-      doff.push_back((int)deps.size());
-    }
+    const int G = std::max(nsm, 1);
+    FlowPlan fp = flow_plan(NE, G, nface, cother, so);
+    std::vector<int>& pstart = fp.pstart;
+    std::vector<int>& pcount = fp.pcount;
+    std::vector<int>& doff = fp.doff;
+    std::vector<int>& deps = fp.deps;
+    std::vector<int>* boff = fp.boff;
+    std::vector<int>* blist = fp.blist;
     FlowDev& f = c->flow;
     int* ip;
     st |= dev_upload(c, pstart, &ip); f.pstart = ip;
@@ -2194,6 +2235,109 @@ int init_impl(const rc_mesh* m, const rc_thermo* t, const rc_config* g, const Ba
 }  // namespace
 
 extern "C" {
+
+int rc_flow_plan_check(int ne, int nblocks, const int* nface, const int* cother, long long* stats) {
+  if (ne < 1 || nblocks < 1 || !nface || !cother || !stats) return RC_ERR_ARG;
+  std::vector<int> nf(nface, nface + ne);
+  std::vector<int> co(cother, cother + 4 * (size_t)ne);
+  for (int i = 0; i < ne; ++i) {
+    if (nf[i] < 0 || nf[i] > 4) return RC_ERR_ARG;
+    for (int q = 0; q < nf[i]; ++q) {
+      const int j = co[(size_t)q * ne + i];
+      if (j < -1 || j >= ne || j == i) return RC_ERR_ARG;
+    }
+  }
+  const SweepOrder so = sweep_order(ne, nf, co);
+  const FlowPlan fp = flow_plan(ne, nblocks, nf, co, so);
+  const int P = (int)fp.pstart.size(), C = fp.C;
+  bool ok = true;
+  long long npass[2] = {0, 0}, maxdep = 0;
+  // every cell in exactly one pass per sweep; a pass is 1..8 positions of one
+  // level, all owned by its block
+  for (int dir = 0; dir < 2 && ok; ++dir) {
+    std::vector<int> seen(ne, 0);
+    for (int pz = 0; pz < P; ++pz) {
+      if (fp.pdir[pz] != dir) continue;
+      ++npass[dir];
+      const int l = fp.plevel[pz], t0 = fp.pstart[pz], n = fp.pcount[pz];
+      if (n < 1 || n > 8 || t0 < so.off[dir][l] || t0 + n > so.off[dir][l + 1]) ok = false;
+      for (int u = t0; u < t0 + n && ok; ++u) {
+        const int i = so.cells[dir][u];
+        if (i / C != fp.powner[pz] || fp.cellpass[dir][i] != pz) ok = false;
+        ++seen[i];
+      }
+    }
+    for (int i = 0; i < ne && ok; ++i) ok = seen[i] == 1;
+  }
+  // dependencies: passes of the same sweep, other blocks, lower levels, and
+  // every neighbour the pass reads from another block
+  for (int pz = 0; pz < P && ok; ++pz) {
+    const int dir = fp.pdir[pz];
+    maxdep = std::max<long long>(maxdep, fp.doff[pz + 1] - fp.doff[pz]);
+    for (int k = fp.doff[pz]; k < fp.doff[pz + 1]; ++k) {
+      const int dp = fp.deps[k];
+      if (dp < 0 || dp >= P || fp.pdir[dp] != dir || fp.powner[dp] == fp.powner[pz] || fp.plevel[dp] >= fp.plevel[pz])
+        ok = false;
+    }
+    for (int u = fp.pstart[pz]; u < fp.pstart[pz] + fp.pcount[pz] && ok; ++u) {
+      const int i = so.cells[dir][u];
+      for (int q = 0; q < nf[i]; ++q) {
+        const int j = co[(size_t)q * ne + i];
+        if (j < 0 || (dir == 0 ? j >= i : j <= i)) continue;
+        const int jp = fp.cellpass[dir][j];
+        if (j / C == i / C) {
+          if (fp.plevel[jp] >= fp.plevel[pz]) ok = false;  // done earlier by the same block
+        } else if (std::find(fp.deps.begin() + fp.doff[pz], fp.deps.begin() + fp.doff[pz + 1], jp) ==
+                   fp.deps.begin() + fp.doff[pz + 1]) {
+          ok = false;
+        }
+      }
+    }
+  }
+  // the blocks' sequences (forward then backward, each in level order); run
+  // the protocol in rounds: every block finishes its next pass once the
+  // passes it depends on are done.  A round without progress is a deadlock.
+  std::vector<std::vector<int>> seq(nblocks);
+  for (int b = 0; b < nblocks && ok; ++b) {
+    for (int dir = 0; dir < 2; ++dir)
+      for (int k = fp.boff[dir][b]; k < fp.boff[dir][b + 1]; ++k) {
+        const int pz = fp.blist[dir][k];
+        if (fp.powner[pz] != b || fp.pdir[pz] != dir ||
+            (k > fp.boff[dir][b] && fp.plevel[fp.blist[dir][k - 1]] > fp.plevel[pz]))
+          ok = false;
+        seq[b].push_back(pz);
+      }
+  }
+  long long rounds = 0;
+  if (ok) {
+    std::vector<char> done(P, 0);
+    std::vector<size_t> at(nblocks, 0);
+    long long left = P;
+    std::vector<int> fin;
+    while (left > 0) {
+      fin.clear();
+      for (int b = 0; b < nblocks; ++b) {
+        if (at[b] >= seq[b].size()) continue;
+        const int pz = seq[b][at[b]];
+        bool ready = true;
+        for (int k = fp.doff[pz]; k < fp.doff[pz + 1] && ready; ++k) ready = done[fp.deps[k]] != 0;
+        if (ready) fin.push_back(b);
+      }
+      if (fin.empty()) { ok = false; break; }
+      for (int b : fin) { done[seq[b][at[b]]] = 1; ++at[b]; --left; }
+      ++rounds;
+    }
+  }
+  stats[0] = npass[0];
+  stats[1] = npass[1];
+  stats[2] = (long long)fp.deps.size();
+  stats[3] = maxdep;
+  stats[4] = rounds;
+  stats[5] = (long long)so.off[0].size() - 1;
+  stats[6] = (long long)so.off[1].size() - 1;
+  stats[7] = C;
+  return ok ? RC_OK : RC_ERR_SYNC;
+}
 
 int rc_init(const rc_mesh* m, const rc_thermo* t, const rc_config* g, rc_ctx** out) {
   if (!m || !t || !g || !out) return RC_ERR_ARG;

@@ -1,0 +1,65 @@
+"""The dataflow LU-SGS plan (host side, no GPU): the level order of both
+sweeps, the per-block passes and their cross-block dependencies that rc_init
+builds for k_lusgs_flow, checked by rc_flow_plan_check on nozzle meshes in the
+natural, colored and random cell orders, and the blocks' protocol run in
+rounds to its end (no deadlock; at least as many rounds as levels)."""
+import numpy as np
+import pytest
+
+import rocketcombustor_gb300 as rc
+from rocketcombustor_gb300.cases import nozzle_mesh
+
+
+def _graph(nx, ny, order, seed=3):
+    cells = nozzle_mesh(nx, ny, seed, order).cells
+    ne = cells.shape[0]
+    cother = -np.ones((ne, 4), np.int32)
+    first = {}
+    for c, tri in enumerate(cells):
+        for q, (a, b) in enumerate(((tri[0], tri[1]), (tri[1], tri[2]), (tri[2], tri[0]))):
+            k = (min(a, b), max(a, b))
+            if k in first:
+                o, oq = first.pop(k)
+                cother[c, q] = o
+                cother[o, oq] = c
+            else:
+                first[k] = (c, q)
+    return np.full(ne, 3, np.int32), cother
+
+
+@pytest.mark.parametrize("nx,ny,order,nblocks", [(24, 6, "natural", 152), (24, 6, "natural", 4),
+                                                 (100, 20, "natural", 152), (100, 20, "colored", 152),
+                                                 (100, 20, "random", 152), (100, 20, "natural", 1)])
+def test_plan_is_consistent_and_runs_to_the_end(nx, ny, order, nblocks):
+    nface, cother = _graph(nx, ny, order)
+    ne = nface.shape[0]
+    st = rc.flow_plan_check(nface, cother, nblocks)
+    assert st["passes_fwd"] >= st["levels_fwd"] and st["passes_bwd"] >= st["levels_bwd"]
+    assert st["passes_fwd"] <= ne and st["passes_bwd"] <= ne
+    # the rounds are at least the longest dependency chain through both sweeps
+    # and at most one pass per round
+    assert st["levels_fwd"] + st["levels_bwd"] <= st["rounds"] <= st["passes_fwd"] + st["passes_bwd"]
+    assert st["cells_per_block"] == -(-ne // nblocks)
+    if nblocks == 1:
+        assert st["deps"] == 0  # one block: every dependency is inside it
+
+
+def test_natural_order_nozzle_levels():
+    """The natural order of a 100 x 20 nozzle: 2 cells per quad, the sweeps run
+    up each column with a shift per column; the plan for 152 blocks needs no
+    more rounds than the levels plus the block crossings."""
+    nface, cother = _graph(100, 20, "natural")
+    st = rc.flow_plan_check(nface, cother, 152)
+    assert st["levels_fwd"] == st["levels_bwd"]
+    assert st["max_deps"] <= 32
+    assert st["rounds"] <= 2 * (st["levels_fwd"] + st["levels_bwd"])
+
+
+def test_bad_arguments_are_refused():
+    nface, cother = _graph(24, 6, "natural")
+    bad = cother.copy()
+    bad[0, 0] = nface.shape[0] + 5  # out of range
+    with pytest.raises(rc.RcError):
+        rc.flow_plan_check(nface, bad, 8)
+    with pytest.raises(rc.RcError):
+        rc.flow_plan_check(nface, cother, 0)
