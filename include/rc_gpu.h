@@ -188,11 +188,11 @@ int rc_clear_error(rc_ctx* ctx);
  * blocks.  Checks that every cell is in exactly one pass of each sweep, that a
  * pass's dependencies are passes of other blocks at lower levels and cover
  * every neighbour it reads from another block, and runs the blocks' protocol
- * in rounds (each block finishes its next pass once its dependencies are
- * done) to the end.  stats[8]: forward passes, backward passes, dependencies,
- * most dependencies of one pass, rounds, forward levels, backward levels,
- * cells per block.  Returns RC_OK, RC_ERR_ARG (bad input) or RC_ERR_SYNC (a
- * check failed or the rounds stalled). */
+ * in synchronous steps (each block finishes its next pass once its
+ * dependencies are done) to the end.  stats[8]: forward passes, backward
+ * passes, dependencies, most dependencies of one pass, steps, forward levels,
+ * backward levels, cells per block.  Returns RC_OK, RC_ERR_ARG (bad input) or
+ * RC_ERR_SYNC (a check failed or the steps stalled). */
 int rc_flow_plan_check(int ne, int nblocks, const int* nface, const int* cother, long long* stats);
 
 /* Autotuner: times `iters` iterations of every launch configuration (LU-SGS

@@ -205,7 +205,7 @@ def flow_plan_check(nface: np.ndarray, cother: np.ndarray, nblocks: int) -> dict
                                    stats.ctypes.data_as(ctypes.POINTER(ctypes.c_longlong)))
     if st:
         raise RcError(st, "dataflow plan check failed" if st == 64 else "bad arguments")
-    keys = ("passes_fwd", "passes_bwd", "deps", "max_deps", "rounds", "levels_fwd", "levels_bwd", "cells_per_block")
+    keys = ("passes_fwd", "passes_bwd", "deps", "max_deps", "steps", "levels_fwd", "levels_bwd", "cells_per_block")
     return dict(zip(keys, (int(v) for v in stats)))
 
 

@@ -2295,8 +2295,9 @@ int rc_flow_plan_check(int ne, int nblocks, const int* nface, const int* cother,
     }
   }
   // the blocks' sequences (forward then backward, each in level order); run
-  // the protocol in rounds: every block finishes its next pass once the
-  // passes it depends on are done.  A round without progress is a deadlock.
+  // the protocol in synchronous steps: every block finishes its next pass
+  // once the passes it depends on are done.  A step without progress is a
+  // deadlock.
   std::vector<std::vector<int>> seq(nblocks);
   for (int b = 0; b < nblocks && ok; ++b) {
     for (int dir = 0; dir < 2; ++dir)
@@ -2308,7 +2309,7 @@ int rc_flow_plan_check(int ne, int nblocks, const int* nface, const int* cother,
         seq[b].push_back(pz);
       }
   }
-  long long rounds = 0;
+  long long steps = 0;
   if (ok) {
     std::vector<char> done(P, 0);
     std::vector<size_t> at(nblocks, 0);
@@ -2325,14 +2326,14 @@ int rc_flow_plan_check(int ne, int nblocks, const int* nface, const int* cother,
       }
       if (fin.empty()) { ok = false; break; }
       for (int b : fin) { done[seq[b][at[b]]] = 1; ++at[b]; --left; }
-      ++rounds;
+      ++steps;
     }
   }
   stats[0] = npass[0];
   stats[1] = npass[1];
   stats[2] = (long long)fp.deps.size();
   stats[3] = maxdep;
-  stats[4] = rounds;
+  stats[4] = steps;
   stats[5] = (long long)so.off[0].size() - 1;
   stats[6] = (long long)so.off[1].size() - 1;
   stats[7] = C;

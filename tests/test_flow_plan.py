@@ -2,7 +2,7 @@
 sweeps, the per-block passes and their cross-block dependencies that rc_init
 builds for k_lusgs_flow, checked by rc_flow_plan_check on nozzle meshes in the
 natural, colored and random cell orders, and the blocks' protocol run in
-rounds to its end (no deadlock; at least as many rounds as levels)."""
+synchronous steps to its end (no deadlock; at least as many steps as levels)."""
 import numpy as np
 import pytest
 
@@ -36,23 +36,25 @@ def test_plan_is_consistent_and_runs_to_the_end(nx, ny, order, nblocks):
     st = rc.flow_plan_check(nface, cother, nblocks)
     assert st["passes_fwd"] >= st["levels_fwd"] and st["passes_bwd"] >= st["levels_bwd"]
     assert st["passes_fwd"] <= ne and st["passes_bwd"] <= ne
-    # the rounds are at least the longest dependency chain through both sweeps
-    # and at most one pass per round
-    assert st["levels_fwd"] + st["levels_bwd"] <= st["rounds"] <= st["passes_fwd"] + st["passes_bwd"]
+    # the steps are at least the longest dependency chain through both sweeps
+    # and at most one pass per step
+    assert st["levels_fwd"] + st["levels_bwd"] <= st["steps"] <= st["passes_fwd"] + st["passes_bwd"]
     assert st["cells_per_block"] == -(-ne // nblocks)
     if nblocks == 1:
         assert st["deps"] == 0  # one block: every dependency is inside it
 
 
-def test_natural_order_nozzle_levels():
-    """The natural order of a 100 x 20 nozzle: 2 cells per quad, the sweeps run
-    up each column with a shift per column; the plan for 152 blocks needs no
-    more rounds than the levels plus the block crossings."""
-    nface, cother = _graph(100, 20, "natural")
+@pytest.mark.parametrize("nx,ny", [(100, 20), (300, 50)])
+def test_natural_order_plan_adds_nothing_to_the_critical_path(nx, ny):
+    """The natural order of a nozzle (columns downstream, bottom to top inside a
+    column) split over 152 blocks: with equal pass times the blocks' protocol
+    ends in exactly as many steps as there are levels in the two sweeps, and a
+    pass waits for at most two passes of other blocks."""
+    nface, cother = _graph(nx, ny, "natural")
     st = rc.flow_plan_check(nface, cother, 152)
     assert st["levels_fwd"] == st["levels_bwd"]
-    assert st["max_deps"] <= 32
-    assert st["rounds"] <= 2 * (st["levels_fwd"] + st["levels_bwd"])
+    assert st["max_deps"] <= 2
+    assert st["steps"] == st["levels_fwd"] + st["levels_bwd"]
 
 
 def test_bad_arguments_are_refused():
