@@ -18,15 +18,15 @@
  *
  * Threading: one host thread per context; each context owns one CUDA stream.
  *
- * LU-SGS schedule: by default the FP64 form runs both sweeps of an iteration
- * as one cooperative dataflow kernel (per-SM blocks of cells, each pass
- * waiting only for the passes of other blocks that hold its neighbours) and
- * the mixed forms one kernel per level; rc_autotune picks the fastest of the
- * schedules, and the environment variable RC_LUSGS_SCHEDULE, read by rc_init,
- * fixes one: "flow", "levels", "levels8", "levels2w", "levels4w" (one kernel
- * per level, with 4 or 8 lanes per cell or each slot's work over two or four
- * warps) or "persistent" (one cooperative kernel with a grid-wide level
- * counter).  All compute the same recurrences bit for bit.
+ * LU-SGS schedule: by default both sweeps of an iteration run as one
+ * cooperative dataflow kernel (per-SM blocks of cells, each pass waiting only
+ * for the passes of other blocks that hold its neighbours; FP64 and mixed
+ * forms each have theirs); rc_autotune picks the fastest of the schedules,
+ * and the environment variable RC_LUSGS_SCHEDULE, read by rc_init, fixes one:
+ * "flow", "levels", "levels8", "levels2w", "levels4w" (one kernel per level,
+ * with 4 or 8 lanes per cell or, in the FP64 form, each slot's work over two
+ * or four warps) or "persistent" (one cooperative kernel with a grid-wide
+ * level counter).  All compute the same recurrences bit for bit.
  */
 #ifndef RC_GPU_H
 #define RC_GPU_H

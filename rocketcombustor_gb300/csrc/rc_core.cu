@@ -1205,6 +1205,9 @@ cudaError_t mixed_lusgs_persistent(const Dev&, const void*, const int*, int, con
                                    cudaStream_t);
 template <int NSP> int mixed_persistent_occupancy();
 template <int NSP>
+cudaError_t mixed_lusgs_flow(const Dev&, const void*, const FlowDev&, int, cudaStream_t);
+template <int NSP> int mixed_flow_occupancy();
+template <int NSP>
 void chem_source(const Dev&, const void*, double, int, int*, int*, unsigned*, unsigned*, cudaStream_t);
 template <int NSP>
 void chem_batch(const void*, const double*, const double*, int, double*, int*, double, int, unsigned*, unsigned*,
@@ -1245,8 +1248,10 @@ struct rc_ctx {
   bool can_persistent = false;  // the device can co-schedule the persistent LU-SGS grid
   int wide = 0;                 // FP64 per-level sweeps: 4 lanes per cell (0), 8 lanes (1, k_sweep8),
                                 // the two parts of a slot in two warps (2, k_sweep2w) or four (3, k_sweep4w);
-                                // 4: the dataflow launch k_lusgs_flow (FP64; where it cannot run, as 3)
+                                // 4: the dataflow launches k_lusgs_flow / k_lusgs_flow32 (where they
+                                // cannot run: as 3 for FP64, the per-level sweeps for the mixed forms)
   bool can_flow = false;        // the device can co-schedule the k_lusgs_flow grid
+  bool can_flow32 = false;      // ... and the k_lusgs_flow32 grid (mixed forms)
   int flow_grid = 0;            // its blocks (one per SM)
   FlowDev flow = {};            // its pass tables
   int pers_grid = 0;             // blocks of the persistent launch (one per SM)
@@ -1616,6 +1621,12 @@ void q_gather(rc_ctx* c) {
 // Sweeps of the mixed-precision modes: FP32 off-diagonal terms, FP64 division.
 template <int NSP>
 void q_sweeps32(rc_ctx* c) {
+  if (!c->persistent && c->wide == 4 && c->can_flow32) {
+    mixed_lusgs_flow<NSP>(c->d, c->thermo32.data(), c->flow, c->flow_grid, c->stream);
+    launch_pdl(k_update<NSP>, blocks(c->NE, c->d.bs), c->d.bs, c->stream, c->d, TH<NSP>(c));
+    c->launches += 2;
+    return;
+  }
   if (c->persistent) {
     cudaMemsetAsync(c->lvl_count, 0, sizeof(unsigned) * c->nlevels, c->stream);
     mixed_lusgs_persistent<NSP>(c->d, c->thermo32.data(), c->fwd_off_dev, (int)c->fwd_off.size() - 1, c->bwd_off_dev,
@@ -2218,15 +2229,17 @@ int init_impl(const rc_mesh* m, const rc_thermo* t, const rc_config* g, const Ba
     const char* sched = std::getenv("RC_LUSGS_SCHEDULE");
     c->pers_grid = nsm;
     c->can_persistent = coop && nsm > 0 && occ64 >= 1 && occ32 >= 1;
-    // default (no or another value): the dataflow launch for FP64 (the four-warp
-    // per-level sweeps where it cannot run) and the per-level sweeps for the
-    // mixed forms
+    // default (no or another value): the dataflow launches (where they cannot
+    // run: the four-warp per-level sweeps for FP64, the per-level sweeps for
+    // the mixed forms)
     const std::string sc = sched ? sched : "";
     c->persistent = c->can_persistent && sc == "persistent";
     c->wide = sc == "levels" ? 0 : sc == "levels8" ? 1 : sc == "levels2w" ? 2 : sc == "levels4w" ? 3 : 4;
     if (c->NSP == 1) cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ64, k_lusgs_flow<1>, FLOW_THREADS, 0);
     else cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ64, k_lusgs_flow<4>, FLOW_THREADS, 0);
     c->can_flow = coop && nsm > 0 && occ64 >= 1 && c->flow_grid == nsm;
+    occ32 = c->NSP == 1 ? mixed_flow_occupancy<1>() : mixed_flow_occupancy<4>();
+    c->can_flow32 = coop && nsm > 0 && occ32 >= 1 && c->flow_grid == nsm;
   }
   *out = c;
   return RC_OK;
@@ -2550,7 +2563,7 @@ int rc_autotune(rc_ctx* c, int iters, char* report, int report_len) {
       for (int bs : {128, 64}) cands.push_back({pers != 0, bs, cpw, 0});
   for (int wide : {1, 2, 3})
     for (int bs : {128, 64}) cands.push_back({false, bs, 8, wide});
-  if (c->can_flow && c->mode == RC_PREC_FP64) cands.push_back({false, 128, 8, 4});
+  if (c->mode == RC_PREC_FP64 ? c->can_flow : c->can_flow32) cands.push_back({false, 128, 8, 4});
   cudaEvent_t e0, e1;
   cudaEventCreate(&e0);
   cudaEventCreate(&e1);

@@ -551,15 +551,19 @@ __device__ __forceinline__ SweepPre32<NSP> sweep_load32(const Dev& d, int t, int
   }
   return p;
 }
-template <int NSP, bool FWD>
+// L2: read the sweep's values (own residual, the neighbour's FP32 increment)
+// through L2, as the dataflow launch needs (other SMs write them during it)
+template <int NSP, bool FWD, bool L2 = false>
 __device__ __forceinline__ void sweep_compute32(const Dev& d, const ThermoDev32<NSP>& th, const SweepPre32<NSP>& p,
                                                 int q, float* wsm) {
   constexpr int V = 3 + NSP;
   const int NE = d.NE;
+  auto ldd = [](const double* a) { return L2 ? __ldcg(a) : *a; };
+  auto ldf = [](const float* a) { return L2 ? __ldcg(a) : *a; };
   double R0 = 0.0, R1 = 0.0;
   if (p.valid) {
-    R0 = d.hWA[q * NE + p.i];
-    if (q + 4 < V) R1 = d.hWA[(q + 4) * NE + p.i];
+    R0 = ldd(d.hWA + q * NE + p.i);
+    if (q + 4 < V) R1 = ldd(d.hWA + (q + 4) * NE + p.i);
   }
   float c[V];
 #pragma unroll
@@ -569,11 +573,11 @@ __device__ __forceinline__ void sweep_compute32(const Dev& d, const ThermoDev32<
     const float dx = p.dx, dy = p.dy, pp = p.pp, uu = p.uu, vv = p.vv, tt = p.tt, rr = p.rr, gama = p.gama,
                 roe = p.roe;
     const float rou = rr * uu, rov = rr * vv;
-    const float drr = d.dU32[0 * NE + j], dru = d.dU32[1 * NE + j], drv = d.dU32[2 * NE + j],
-                dre = d.dU32[3 * NE + j];
+    const float drr = ldf(d.dU32 + 0 * NE + j), dru = ldf(d.dU32 + 1 * NE + j), drv = ldf(d.dU32 + 2 * NE + j),
+                dre = ldf(d.dU32 + 3 * NE + j);
     float dry[NSP], s = 0.f;
 #pragma unroll
-    for (int k = 0; k < NSP - 1; ++k) { dry[k] = d.dU32[(4 + k) * NE + j]; s += dry[k]; }
+    for (int k = 0; k < NSP - 1; ++k) { dry[k] = ldf(d.dU32 + (4 + k) * NE + j); s += dry[k]; }
     dry[NSP - 1] = drr - s;
     const float rinv = 1.f / rr;
     const float duu = (dru - uu * drr) * rinv;
@@ -698,6 +702,123 @@ __global__ void __launch_bounds__(PERS32_THREADS) k_lusgs_persistent32(const Dev
   }
 }
 
+// Both FP32 sweeps as a dataflow on the pass tables of k_lusgs_flow (one block
+// per SM, its cells' passes in level order, each pass waiting only for the
+// passes of other blocks that hold its neighbours).  An FP32 pass is short, so
+// the work around it is split over two warps: warp 1 stages the passes'
+// sweep_load32 data up to NBUF passes ahead into a ring of shared buffers
+// (s_staged counts the staged passes, s_consumed the passes warp 0 has taken);
+// warp 2 looks at the next pass's flags, hands each pass to warp 0 (barrier 3)
+// once it is staged and its flags are set, and publishes each finished pass
+// (barrier 4 from warp 0, then the flag = this launch's epoch), before any
+// blocking wait, so that no block waits while holding a finished pass.  Warp 0
+// runs the step of k_sweep32 (8 cells, 4 lanes each) with the sweep's values
+// read through L2.  Every wait is bounded (ERR_SYNC); the FP64 update follows
+// as its own kernel.
+constexpr int FLOW32_THREADS = 96, FLOW32_NBUF = 4;
+template <int NSP>
+__global__ void __launch_bounds__(FLOW32_THREADS) k_lusgs_flow32(const Dev d, const ThermoDev32<NSP> th,
+                                                                 const FlowDev f) {
+  __shared__ SweepPre32<NSP> s_pre[FLOW32_NBUF][32];
+  __shared__ float wsm[32 * (3 + NSP)];
+  __shared__ unsigned s_epoch;
+  __shared__ volatile int s_bad, s_staged, s_consumed;
+  if (threadIdx.x == 0) {
+    s_epoch = ld_acquire(f.ctr) + 1u;
+    s_bad = 0;
+    s_staged = 0;
+    s_consumed = 0;
+  }
+  __syncthreads();
+  const unsigned epoch = s_epoch;
+  const int b = blockIdx.x, lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const int f0 = f.boff[0][b], b0 = f.boff[1][b];
+  const int nf = f.boff[0][b + 1] - f0, n = nf + (f.boff[1][b + 1] - b0);
+  auto pass_of = [&](int k) { return k < nf ? f.blist[0][f0 + k] : f.blist[1][b0 + k - nf]; };
+  auto give_up = [&]() {
+    if (lane == 0) {
+      s_bad = 1;
+      atomicOr(d.err, ERR_SYNC);
+    }
+    __syncwarp();
+  };
+  if (warp == 1) {
+    for (int k = 0; k < n && !s_bad; ++k) {
+      // pass k reuses the buffer of pass k - NBUF once warp 0 has taken it
+      for (unsigned spin = 0; s_consumed < k - FLOW32_NBUF + 1 && !s_bad; ++spin)
+        if (spin >= d.spin_limit) give_up();
+      if (s_bad) break;
+      const int pz = pass_of(k), t0 = f.pstart[pz], t1 = t0 + f.pcount[pz];
+      if (k < nf) s_pre[k % FLOW32_NBUF][lane] = sweep_load32<NSP, true>(d, t0 + (lane >> 2), t1, lane & 3);
+      else s_pre[k % FLOW32_NBUF][lane] = sweep_load32<NSP, false>(d, t0 + (lane >> 2), t1, lane & 3);
+      __syncwarp();
+      __threadfence_block();
+      if (lane == 0) s_staged = k + 1;
+      __syncwarp();
+    }
+  } else if (warp == 2) {
+    auto staged = [&](int k) {  // wait (bounded) until pass k is staged
+      for (unsigned spin = 0; s_staged <= k && !s_bad; ++spin)
+        if (spin >= d.spin_limit) give_up();
+      __threadfence_block();
+    };
+    auto poll = [&](int k) {
+      if (s_bad) return;
+      const int pz = pass_of(k), d0 = f.doff[pz], nd = f.doff[pz + 1] - d0;
+      bool ok = true;
+      for (int u = lane; u < nd; u += 32) ok = ok && wait_flag(f.pflag + f.deps[d0 + u], epoch, d.err, d.spin_limit);
+      if (__any_sync(0xffffffffu, !ok)) give_up();
+    };
+    auto ready = [&](int k) -> bool {
+      if (s_bad) return true;
+      if (s_staged <= k) return false;
+      const int pz = pass_of(k), d0 = f.doff[pz], nd = f.doff[pz + 1] - d0;
+      bool ok = true;
+      for (int u = lane; u < nd; u += 32) ok = ok && ld_acquire(f.pflag + f.deps[d0 + u]) >= epoch;
+      return __all_sync(0xffffffffu, ok) != 0;
+    };
+    if (n > 0) {
+      staged(0);
+      poll(0);
+      bar_arrive(3, 64);
+    }
+    for (int k = 0; k < n; ++k) {
+      const bool more = k + 1 < n;
+      const bool go = more && ready(k + 1);
+      if (go) __threadfence_block();
+      bar_named(4, 64);
+      if (go) bar_arrive(3, 64);
+      if (lane == 0 && !s_bad) st_release(f.pflag + pass_of(k), epoch);
+      if (more && !go) {
+        poll(k + 1);
+        staged(k + 1);
+        bar_arrive(3, 64);
+      }
+    }
+  } else {
+    for (int k = 0; k < n; ++k) {
+      bar_named(3, 64);
+      const SweepPre32<NSP> p = s_pre[k % FLOW32_NBUF][lane];
+      __syncwarp();
+      __threadfence_block();
+      if (lane == 0) s_consumed = k + 1;
+      if (k < nf) sweep_compute32<NSP, true, true>(d, th, p, lane & 3, wsm);
+      else sweep_compute32<NSP, false, true>(d, th, p, lane & 3, wsm);
+      __syncwarp();
+      bar_arrive(4, 64);
+    }
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    __threadfence();
+    if (atomicAdd(f.ctr + 1, 1u) == gridDim.x - 1) {
+      f.ctr[1] = 0u;
+      __threadfence();
+      st_release(f.ctr, epoch);
+    }
+  }
+}
+
 // ------------------------------------------------------- host launchers ----
 inline unsigned nblk(long n, int t) { return (unsigned)((n + t - 1) / t); }
 
@@ -758,6 +879,26 @@ cudaError_t mixed_lusgs_persistent(const Dev& d, const void* th32, const int* fo
   return cudaLaunchKernelEx(&cfg, k_lusgs_persistent32<NSP>, d, *static_cast<const ThermoDev32<NSP>*>(th32), foff, nf,
                             boff, nb, count);
 }
+// Cooperative launch of the dataflow FP32 sweeps, one block per SM.
+template <int NSP>
+cudaError_t mixed_lusgs_flow(const Dev& d, const void* th32, const FlowDev& f, int grid, cudaStream_t s) {
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = dim3((unsigned)grid);
+  cfg.blockDim = dim3(FLOW32_THREADS);
+  cfg.stream = s;
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeCooperative;
+  attr[0].val.cooperative = 1;
+  cfg.attrs = attr;
+  cfg.numAttrs = 1;
+  return cudaLaunchKernelEx(&cfg, k_lusgs_flow32<NSP>, d, *static_cast<const ThermoDev32<NSP>*>(th32), f);
+}
+template <int NSP>
+int mixed_flow_occupancy() {
+  int nb = 0;
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_lusgs_flow32<NSP>, FLOW32_THREADS, 0);
+  return nb;
+}
 template <int NSP>
 int mixed_persistent_occupancy() {
   int nb = 0;
@@ -780,7 +921,9 @@ size_t mixed_thermo(const void* th64, void* out) {
   template size_t mixed_thermo<N>(const void*, void*);                                                       \
   template cudaError_t mixed_lusgs_persistent<N>(const Dev&, const void*, const int*, int, const int*, int,       \
                                                  unsigned*, int, cudaStream_t);                                 \
-  template int mixed_persistent_occupancy<N>();
+  template int mixed_persistent_occupancy<N>();                                                                 \
+  template cudaError_t mixed_lusgs_flow<N>(const Dev&, const void*, const FlowDev&, int, cudaStream_t);         \
+  template int mixed_flow_occupancy<N>();
 RC_MIXED_INST(1)
 RC_MIXED_INST(4)
 

@@ -171,9 +171,8 @@ def test_device_stop_condition_is_reported(case_t1):
 def test_persistent_and_per_level_schedules_agree(case_root, precision, monkeypatch):
     """The cooperative one-launch LU-SGS, the one-launch-per-level LU-SGS
     (4 lanes per cell with 8 or 1 cells per warp, 8 lanes per cell, or the work
-    of each slot split over two or four warps) and the dataflow launch (FP64;
-    the mixed form runs its per-level sweeps under that name) run the same
-    recurrences: identical states after 30 iterations."""
+    of each slot split over two or four warps) and the dataflow launches run
+    the same recurrences: identical states after 30 iterations."""
     d = make_case(case_root, "c1", nx=40, ny=8)
     c = rc.Case(d)
     states = []
