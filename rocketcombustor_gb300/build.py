@@ -28,7 +28,9 @@ UNITS = {
     "rc_chem.cu": ["--fmad=false"],
     "rc_bdf2.cu": ["--fmad=false"],
     "rc_mlp.cu": [],
-    "rc_mixed.cu": ["--use_fast_math"],
+    # approximate FP32 division/sqrt and FTZ, but no FMA contraction: the FP64
+    # Newton update fused into the mixed sweeps must round like rc_core.cu's
+    "rc_mixed.cu": ["--ftz=true", "--prec-div=false", "--prec-sqrt=false", "--fmad=false"],
 }
 HOST_UNITS = ["rc_host.cpp"]
 

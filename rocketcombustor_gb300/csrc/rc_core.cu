@@ -1205,7 +1205,7 @@ cudaError_t mixed_lusgs_persistent(const Dev&, const void*, const int*, int, con
                                    cudaStream_t);
 template <int NSP> int mixed_persistent_occupancy();
 template <int NSP>
-cudaError_t mixed_lusgs_flow(const Dev&, const void*, const FlowDev&, int, cudaStream_t);
+cudaError_t mixed_lusgs_flow(const Dev&, const void*, const void*, const FlowDev&, int, cudaStream_t);
 template <int NSP> int mixed_flow_occupancy();
 template <int NSP>
 void chem_source(const Dev&, const void*, double, int, int*, int*, unsigned*, unsigned*, cudaStream_t);
@@ -1622,9 +1622,9 @@ void q_gather(rc_ctx* c) {
 template <int NSP>
 void q_sweeps32(rc_ctx* c) {
   if (!c->persistent && c->wide == 4 && c->can_flow32) {
-    mixed_lusgs_flow<NSP>(c->d, c->thermo32.data(), c->flow, c->flow_grid, c->stream);
-    launch_pdl(k_update<NSP>, blocks(c->NE, c->d.bs), c->d.bs, c->stream, c->d, TH<NSP>(c));
-    c->launches += 2;
+    // the Newton update runs inside the dataflow launch
+    mixed_lusgs_flow<NSP>(c->d, c->thermo32.data(), c->thermo.data(), c->flow, c->flow_grid, c->stream);
+    c->launches += 1;
     return;
   }
   if (c->persistent) {

@@ -10,8 +10,11 @@
 // FP64 kernels of rc_core.cu while the LU-SGS sweeps stay in FP32, so the fixed
 // point is the FP64 one.
 //
-// Built with --use_fast_math (FP32 SFU math, FMA contraction); double
-// arithmetic is unaffected by that flag apart from contraction.
+// Built with approximate FP32 division and square root and FP32 denormals
+// flushed (--prec-div=false --prec-sqrt=false --ftz=true; the FP32 SFU math is
+// called by name in rc_thermo32.cuh), and without FMA contraction
+// (--fmad=false), so that the FP64 code here (the Newton update fused into
+// k_lusgs_flow32, the chemical source) gives the bits of rc_core.cu's.
 #include <cuda_runtime.h>
 
 #include "rc_dev.cuh"
@@ -713,21 +716,32 @@ __global__ void __launch_bounds__(PERS32_THREADS) k_lusgs_persistent32(const Dev
 // (barrier 4 from warp 0, then the flag = this launch's epoch), before any
 // blocking wait, so that no block waits while holding a finished pass.  Warp 0
 // runs the step of k_sweep32 (8 cells, 4 lanes each) with the sweep's values
-// read through L2.  Every wait is bounded (ERR_SYNC); the FP64 update follows
-// as its own kernel.
-constexpr int FLOW32_THREADS = 96, FLOW32_NBUF = 4;
+// read through L2.  Every wait is bounded (ERR_SYNC).
+// The FP64 Newton update (update_primitve_variables) of a cell needs only
+// its own final increment, which its backward pass writes; the sweeps read
+// neither WA nor PA (their FP32 copies PA32, cst32 stay as the iteration
+// began), so warps 3 and 6 update the cells of each finished backward pass
+// during the sweep, on the FP64 units of sub-partitions 3 and 2 that the
+// FP32 passes leave idle (warps 4 and 5 only keep them there).  Warp 0
+// counts its finished passes in s_done; update warp u takes the backward
+// passes nf + u, nf + u + 2, ..., as many finished ones at a time as fill
+// its 32 lanes with one cell each.  The update is the function k_update
+// runs, compiled with the same flags, so the bits are the same.
+constexpr int FLOW32_THREADS = 224, FLOW32_NBUF = 4;
 template <int NSP>
-__global__ void __launch_bounds__(FLOW32_THREADS) k_lusgs_flow32(const Dev d, const ThermoDev32<NSP> th,
-                                                                 const FlowDev f) {
+__global__ void __launch_bounds__(FLOW32_THREADS, 1) k_lusgs_flow32(const Dev d, const ThermoDev32<NSP> th,
+                                                                 const ThermoDev<NSP> th64, const FlowDev f) {
   __shared__ SweepPre32<NSP> s_pre[FLOW32_NBUF][32];
   __shared__ float wsm[32 * (3 + NSP)];
+  __shared__ int s_cells[2][32];
   __shared__ unsigned s_epoch;
-  __shared__ volatile int s_bad, s_staged, s_consumed;
+  __shared__ volatile int s_bad, s_staged, s_consumed, s_done;
   if (threadIdx.x == 0) {
     s_epoch = ld_acquire(f.ctr) + 1u;
     s_bad = 0;
     s_staged = 0;
     s_consumed = 0;
+    s_done = 0;
   }
   __syncthreads();
   const unsigned epoch = s_epoch;
@@ -795,7 +809,7 @@ __global__ void __launch_bounds__(FLOW32_THREADS) k_lusgs_flow32(const Dev d, co
         bar_arrive(3, 64);
       }
     }
-  } else {
+  } else if (warp == 0) {
     for (int k = 0; k < n; ++k) {
       bar_named(3, 64);
       const SweepPre32<NSP> p = s_pre[k % FLOW32_NBUF][lane];
@@ -805,8 +819,52 @@ __global__ void __launch_bounds__(FLOW32_THREADS) k_lusgs_flow32(const Dev d, co
       if (k < nf) sweep_compute32<NSP, true, true>(d, th, p, lane & 3, wsm);
       else sweep_compute32<NSP, false, true>(d, th, p, lane & 3, wsm);
       __syncwarp();
+      __threadfence_block();
+      if (lane == 0) s_done = k + 1;
       bar_arrive(4, 64);
     }
+  } else if (warp == 3 || warp == 6) {
+    const int u = warp == 3 ? 0 : 1;
+    int* cells = s_cells[u];
+    unsigned err = 0;
+    for (int k = nf + u; k < n;) {
+      // bounded wait for pass k; the polls are spaced out, as these warps
+      // wait through the whole forward sweep and must not take issue slots
+      // from warp 2 on their sub-partition
+      for (unsigned spin = 0; s_done <= k && !s_bad; ++spin) {
+        if (spin >= d.spin_limit) give_up();
+        __nanosleep(256);
+      }
+      if (s_bad) break;
+      __threadfence_block();
+      const int avail = s_done;
+      // lane l looks at this warp's pass k + 2l; the finished ones whose
+      // cells fit in 32 lanes (a prefix of the lanes: at least pass k) are
+      // taken, their sweep positions listed in order in cells[]
+      const int kl = k + 2 * lane;
+      int cnt = 0, t0 = 0;
+      if (kl < avail) {
+        const int pz = pass_of(kl);
+        cnt = f.pcount[pz];
+        t0 = f.pstart[pz];
+      }
+      int incl = cnt;
+#pragma unroll
+      for (int o = 1; o < 32; o <<= 1) {
+        const int x = __shfl_up_sync(0xffffffffu, incl, o);
+        if (lane >= o) incl += x;
+      }
+      const bool take = kl < avail && incl <= 32;
+      const int ntake = __popc(__ballot_sync(0xffffffffu, take));
+      if (take)
+        for (int c = 0; c < cnt; ++c) cells[incl - cnt + c] = t0 + c;
+      const int ncell = __shfl_sync(0xffffffffu, incl, ntake - 1);
+      __syncwarp();
+      if (lane < ncell) update_cell<NSP>(d, th64, d.swi[1][cells[lane]], err);
+      __syncwarp();
+      k += 2 * ntake;
+    }
+    flag(d, err);
   }
   __syncthreads();
   if (threadIdx.x == 0) {
@@ -879,9 +937,11 @@ cudaError_t mixed_lusgs_persistent(const Dev& d, const void* th32, const int* fo
   return cudaLaunchKernelEx(&cfg, k_lusgs_persistent32<NSP>, d, *static_cast<const ThermoDev32<NSP>*>(th32), foff, nf,
                             boff, nb, count);
 }
-// Cooperative launch of the dataflow FP32 sweeps, one block per SM.
+// Cooperative launch of the dataflow FP32 sweeps with the fused FP64 Newton
+// update, one block per SM (th32, th64: ThermoDev32<NSP>, ThermoDev<NSP>).
 template <int NSP>
-cudaError_t mixed_lusgs_flow(const Dev& d, const void* th32, const FlowDev& f, int grid, cudaStream_t s) {
+cudaError_t mixed_lusgs_flow(const Dev& d, const void* th32, const void* th64, const FlowDev& f, int grid,
+                             cudaStream_t s) {
   cudaLaunchConfig_t cfg = {};
   cfg.gridDim = dim3((unsigned)grid);
   cfg.blockDim = dim3(FLOW32_THREADS);
@@ -891,7 +951,8 @@ cudaError_t mixed_lusgs_flow(const Dev& d, const void* th32, const FlowDev& f, i
   attr[0].val.cooperative = 1;
   cfg.attrs = attr;
   cfg.numAttrs = 1;
-  return cudaLaunchKernelEx(&cfg, k_lusgs_flow32<NSP>, d, *static_cast<const ThermoDev32<NSP>*>(th32), f);
+  return cudaLaunchKernelEx(&cfg, k_lusgs_flow32<NSP>, d, *static_cast<const ThermoDev32<NSP>*>(th32),
+                            *static_cast<const ThermoDev<NSP>*>(th64), f);
 }
 template <int NSP>
 int mixed_flow_occupancy() {
@@ -922,7 +983,8 @@ size_t mixed_thermo(const void* th64, void* out) {
   template cudaError_t mixed_lusgs_persistent<N>(const Dev&, const void*, const int*, int, const int*, int,       \
                                                  unsigned*, int, cudaStream_t);                                 \
   template int mixed_persistent_occupancy<N>();                                                                 \
-  template cudaError_t mixed_lusgs_flow<N>(const Dev&, const void*, const FlowDev&, int, cudaStream_t);         \
+  template cudaError_t mixed_lusgs_flow<N>(const Dev&, const void*, const void*, const FlowDev&, int,           \
+                                           cudaStream_t);                                                       \
   template int mixed_flow_occupancy<N>();
 RC_MIXED_INST(1)
 RC_MIXED_INST(4)

@@ -1,8 +1,9 @@
 // Single-precision thermochemistry for the mixed-precision form: the same
 // point functions as rc_thermo.cuh (ComputeGasParameter, compute_enthalpy,
 // compute_transport_property, compute_diffusion_velocity of the reference's
-// src/combustion_modeling) evaluated in FP32 with the fast SFU math of
-// --use_fast_math.  Used for the spectral radius, reconstruction, limiter and
+// src/combustion_modeling) evaluated in FP32 with the fast SFU math
+// (__logf, __expf, __powf; the unit is built with approximate FP32 division
+// and square root).  Used for the spectral radius, reconstruction, limiter and
 // face fluxes; chemistry, the LU-SGS diagonal, Newton and norms stay FP64.
 #pragma once
 #include "rc_thermo.cuh"
@@ -69,7 +70,7 @@ __device__ __forceinline__ void gas32(const ThermoDev32<NSP>& th, const float* Y
 template <int NSP>
 __device__ __forceinline__ void enthalpy32(const ThermoDev32<NSP>& th, float tem, float* entha, unsigned& err) {
   const float t2 = tem * tem, r1 = 1.0f / tem;
-  const float e[7] = {-(r1 * r1), logf(tem) * r1, 1.0f, 0.5f * tem, t2 * (1.f / 3.f), 0.25f * tem * t2, 0.2f * t2 * t2};
+  const float e[7] = {-(r1 * r1), __logf(tem) * r1, 1.0f, 0.5f * tem, t2 * (1.f / 3.f), 0.25f * tem * t2, 0.2f * t2 * t2};
   const bool low = (th.tlo <= tem && tem <= th.tcrit);
   if (!low && !(th.tcrit < tem && tem <= th.thi)) err |= ERR_THERMO_T;
 #pragma unroll
@@ -95,11 +96,11 @@ __device__ __forceinline__ void transport32(const ThermoDev32<NSP>& th, float te
   const bool low = (th.trlo <= tem && tem <= th.trcrit);
   if (!low && !(th.trcrit < tem && tem <= th.trhi)) err |= ERR_TRANSPORT_T;
   const int rg = low ? 0 : 1;
-  const float lt = logf(tem), r1 = 1.f / tem, r2 = r1 * r1;
+  const float lt = __logf(tem), r1 = 1.f / tem, r2 = r1 * r1;
 #pragma unroll
   for (int i = 0; i < NSP; ++i) {
-    mul[i] = 1.0e-7f * expf(th.mu[rg][0][i] * lt + th.mu[rg][1][i] * r1 + th.mu[rg][2][i] * r2 + th.mu[rg][3][i]);
-    Kl[i] = 1.0e-4f * expf(th.kk[rg][0][i] * lt + th.kk[rg][1][i] * r1 + th.kk[rg][2][i] * r2 + th.kk[rg][3][i]);
+    mul[i] = 1.0e-7f * __expf(th.mu[rg][0][i] * lt + th.mu[rg][1][i] * r1 + th.mu[rg][2][i] * r2 + th.mu[rg][3][i]);
+    Kl[i] = 1.0e-4f * __expf(th.kk[rg][0][i] * lt + th.kk[rg][1][i] * r1 + th.kk[rg][2][i] * r2 + th.kk[rg][3][i]);
   }
   float v = 0.f, s1 = 0.f, s2 = 0.f;
 #pragma unroll
@@ -137,8 +138,8 @@ __device__ __forceinline__ void diffusion32(const ThermoDev32<NSP>& th, float pp
 #pragma unroll
     for (int j = i + 1; j < NSP; ++j) {
       const float tstar = tem / th.dlj[i][j];
-      const float om = 1.06036f * powf(tstar, -0.15610f) + 0.19300f * expf(-0.47635f * tstar) +
-                       1.03587f * expf(-1.52996f * tstar) + 1.76474f * expf(-3.89411f * tstar);
+      const float om = 1.06036f * __powf(tstar, -0.15610f) + 0.19300f * __expf(-0.47635f * tstar) +
+                       1.03587f * __expf(-1.52996f * tstar) + 1.76474f * __expf(-3.89411f * tstar);
       const float dv = num / (pp * th.dmw[i][j] * th.dcd[i][j] * om);
       D[i][j] = dv;
       D[j][i] = dv;
