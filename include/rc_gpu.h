@@ -177,7 +177,11 @@ int rc_set_precision(rc_ctx* ctx, int precision);
 
 /* Polls after which a level wait of the persistent LU-SGS kernels gives up
  * (default 2^24): the kernel then latches RC_ERR_SYNC and returns, leaving the
- * context usable.  A small limit forces the timeout path (fault tests). */
+ * context usable.  A small limit forces the timeout path (fault tests).  The
+ * Newton-update warps of the mixed forms' dataflow launch wait through the
+ * whole forward sweep with polls at least 256 ns apart and count them against
+ * the same limit, so a limit set by hand must cover the forward sweep's
+ * duration divided by 256 ns (the default covers over 4 s). */
 int rc_set_wait_limit(rc_ctx* ctx, unsigned polls);
 /* Clear the latched stop conditions (after the caller has dealt with them). */
 int rc_clear_error(rc_ctx* ctx);
