@@ -307,6 +307,13 @@ int rc_stats(rc_ctx* ctx, long long* kernel_launches, int* fwd_levels, int* bwd_
 
 const char* rc_last_error(rc_ctx* ctx);
 
+/* The same message copied into a caller buffer of len bytes, the form a
+ * Fortran host binds (character(kind=c_char) :: buf(len)) to print it before
+ * MPI_STOP (src/parallel.f90:56-62 stops with a message).  At most len-1
+ * bytes of the message are copied and a NUL always follows them.  Returns
+ * RC_OK, or RC_ERR_ARG when buf is NULL or len < 1 (nothing written). */
+int rc_last_error_buf(rc_ctx* ctx, char* buf, int len);
+
 /*
  * Residual norms of device arrays that the caller owns, computed without any
  * device allocation.  No counterpart in the reference: it serves hosts that
@@ -323,9 +330,11 @@ const char* rc_last_error(rc_ctx* ctx);
  * Scratch: a fixed array compiled into the library, sized for NVar up to
  * RC_NOALLOC_MAX_NVAR (about 41 KB, held by every GPU that loads the library
  * until the process exits); a larger NVar is rejected with RC_ERR_ARG and a
- * message on stderr.  The first call on a device looks up the array's device
- * address (cudaGetSymbolAddress) with that device current; make that first call
- * before any stream capture.  Every value read from the scratch is written
+ * message on stderr.  Every call looks up the array's device address
+ * (cudaGetSymbolAddress) in the device and context current on the calling
+ * thread, so the address stays right after cudaDeviceReset and under a
+ * non-primary context; the first call on a device may load the module, so make
+ * it before any stream capture.  Every value read from the scratch is written
  * earlier in the same call, so nothing has to be cleared between calls, but all
  * calls share the one array: calls whose work overlaps on the GPU (other
  * streams, other host threads) race and must be serialised by the caller.

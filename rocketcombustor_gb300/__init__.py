@@ -34,6 +34,7 @@ import numpy as np
 from . import build as _build
 
 RC_OK = 0
+RC_ERR_ARG = 1024
 RC_ERR = {1: "thermo T out of range", 2: "transport T out of range", 4: "negative rho/p/T in TimeStep",
           8: "negative rho/p at a face", 16: "NaN in WA(1,1)", 32: "unknown boundary code",
           64: "LU-SGS wait timed out", 128: "BDF2 cell system singular (dgesvx)",
@@ -91,6 +92,7 @@ SIGNATURES = {
     "rc_get_stream": (_vp, [_vp]),
     "rc_stats": (_i, [_vp, ctypes.POINTER(ctypes.c_longlong), _IP, _IP]),
     "rc_last_error": (_cp, [_vp]),
+    "rc_last_error_buf": (_i, [_vp, _cp, _i]),
     "rc_case_open": (_i, [_cp, ctypes.POINTER(_vp)]),
     "rc_case_error": (_cp, [_vp]),
     "rc_case_close": (None, [_vp]),

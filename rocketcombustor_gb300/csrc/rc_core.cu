@@ -2914,4 +2914,13 @@ int rc_stats(rc_ctx* c, long long* launches, int* fwd, int* bwd) {
 
 const char* rc_last_error(rc_ctx* c) { return c ? c->err.c_str() : "no context"; }
 
+int rc_last_error_buf(rc_ctx* c, char* buf, int len) {
+  if (!buf || len < 1) return RC_ERR_ARG;
+  const char* m = rc_last_error(c);
+  const size_t n = std::min(std::strlen(m), (size_t)(len - 1));
+  std::memcpy(buf, m, n);
+  buf[n] = '\0';
+  return RC_OK;
+}
+
 }  // extern "C"

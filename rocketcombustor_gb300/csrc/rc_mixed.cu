@@ -812,6 +812,13 @@ __global__ void __launch_bounds__(FLOW32_THREADS, 1) k_lusgs_flow32(const Dev d,
   } else if (warp == 0) {
     for (int k = 0; k < n; ++k) {
       bar_named(3, 64);
+      // after a give-up warp 2 still hands every pass over (the barrier
+      // counts must match) but warp 1 has stopped staging: the buffer may
+      // hold no pass at all, so nothing of it is read
+      if (s_bad) {
+        bar_arrive(4, 64);
+        continue;
+      }
       const SweepPre32<NSP> p = s_pre[k % FLOW32_NBUF][lane];
       __syncwarp();
       __threadfence_block();

@@ -10,16 +10,18 @@
 //
 // The scratch is one file-scope __device__ array.  Every GPU that loads the
 // library holds it (about 41 KB) until the process exits.  Host code may not
-// use the array's name as a device address, so its address is looked up with
-// cudaGetSymbolAddress once per device, on the first call made on that device
-// (the device that is current at the call).
+// use the array's name as a device address, so every call looks the address
+// up with cudaGetSymbolAddress, with the caller's device and context current.
+// The lookup is cheap next to the call's own stream synchronisation, and a
+// per-call lookup stays right where a cached one would not: after
+// cudaDeviceReset (the module is loaded again, possibly elsewhere) and under a
+// driver-API context that is not the device's primary one.
 //
 // Sums use the same fixed-shape block decomposition as rc_residual, so the
 // results are deterministic run to run.
 #include <cuda_runtime.h>
 
 #include <cstdio>
-#include <mutex>
 #include <string>
 
 #include "rc_gpu.h"
@@ -69,29 +71,17 @@ __global__ void k_na_final(int V, double total_volume, double* scratch) {
   scratch[NA_SLOTS * NA_BLOCKS + k] = (k == V) ? a : a / total_volume;
 }
 
-constexpr int NA_MAX_DEVICES = 64;
-std::mutex g_mu;
-double* g_scratch_ptr[NA_MAX_DEVICES] = {};
-
 int fail(int code, const std::string& msg) {
   std::fprintf(stderr, "rc_residual_noalloc: %s\n", msg.c_str());
   return code;
 }
 
-// Device address of the scratch array on the current device (looked up once per device).
-int scratch_on_current_device(double** out) {
-  int dev = 0;
-  cudaError_t e = cudaGetDevice(&dev);
-  if (e != cudaSuccess) return fail(RC_ERR_CUDA, std::string("cudaGetDevice: ") + cudaGetErrorString(e));
-  if (dev < 0 || dev >= NA_MAX_DEVICES) return fail(RC_ERR_ARG, "device ordinal beyond 63");
-  std::lock_guard<std::mutex> lock(g_mu);
-  if (!g_scratch_ptr[dev]) {
-    void* p = nullptr;
-    e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
-    if (e != cudaSuccess || !p) return fail(RC_ERR_CUDA, std::string("cudaGetSymbolAddress: ") + cudaGetErrorString(e));
-    g_scratch_ptr[dev] = static_cast<double*>(p);
-  }
-  *out = g_scratch_ptr[dev];
+// Device address of the scratch array in the context current on this thread.
+int scratch_in_current_context(double** out) {
+  void* p = nullptr;
+  const cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+  if (e != cudaSuccess || !p) return fail(RC_ERR_CUDA, std::string("cudaGetSymbolAddress: ") + cudaGetErrorString(e));
+  *out = static_cast<double*>(p);
   return RC_OK;
 }
 
@@ -107,7 +97,7 @@ int rc_residual_noalloc(const double* d_hWA, const double* d_WA, const double* d
     return fail(RC_ERR_ARG, "NVar " + std::to_string(NVar) + " is outside 1.." + std::to_string(RC_NOALLOC_MAX_NVAR) +
                                 " (RC_NOALLOC_MAX_NVAR, the size of the built-in scratch)");
   double* scratch = nullptr;
-  int st = scratch_on_current_device(&scratch);
+  int st = scratch_in_current_context(&scratch);
   if (st) return st;
   cudaStream_t s = static_cast<cudaStream_t>(cuda_stream);
   k_na_partial<<<NA_BLOCKS, NA_THREADS, 0, s>>>(d_hWA, d_WA, d_VOL, NE, NVar, scratch);

@@ -168,12 +168,17 @@ def test_device_stop_condition_is_reported(case_t1):
 
 
 @pytest.mark.parametrize("precision", [rc.RC_PREC_FP64, rc.RC_PREC_MIXED])
-def test_persistent_and_per_level_schedules_agree(case_root, precision, monkeypatch):
+@pytest.mark.parametrize("name,over", [("c1", {"nx": 40, "ny": 8}), ("t2", {})])
+def test_persistent_and_per_level_schedules_agree(case_root, precision, name, over, monkeypatch):
     """The cooperative one-launch LU-SGS, the one-launch-per-level LU-SGS
     (4 lanes per cell with 8 or 1 cells per warp, 8 lanes per cell, or the work
     of each slot split over two or four warps) and the dataflow launches run
-    the same recurrences: identical states after 30 iterations."""
-    d = make_case(case_root, "c1", nx=40, ny=8)
+    the same recurrences: identical states after 30 iterations.  In mixed
+    precision the dataflow launch does the FP64 Newton update inside the sweep
+    launch and the other schedules in a separate k_update: the one-species
+    inviscid nozzle and the four-species reacting viscous case check both
+    builds of that update."""
+    d = make_case(case_root, name, **over)
     c = rc.Case(d)
     states = []
     for sched in ("persistent", "levels", "levels8", "levels2w", "levels4w", "flow"):
@@ -228,6 +233,36 @@ def test_dataflow_wait_timeout_is_reported(case_root, monkeypatch):
     o.run(5)
     PA, WA = s.get_state()
     assert np.array_equal(PA, o.array("PA")) and np.array_equal(WA, o.array("WA"))
+
+
+@pytest.mark.parametrize("sched", ["flow", "persistent"])
+def test_mixed_wait_timeout_is_reported(case_root, sched, monkeypatch):
+    """The mixed-precision LU-SGS launches give up the same way: a poll limit
+    of 1 ends the staging, hand-over and update-warp waits of the FP32 dataflow
+    launch (or the level waits of the FP32 persistent launch) with RC_ERR_SYNC;
+    after the error is cleared and the state set again, five iterations give
+    the bits of a clean mixed run from the same state."""
+    monkeypatch.setenv("RC_LUSGS_SCHEDULE", sched)
+    d = make_case(case_root, "t2")
+    c = rc.Case(d)
+    s = rc.Solver(c, precision=rc.RC_PREC_MIXED)
+    s.set_wait_limit(1)
+    s.lu_sgs_stage(1)
+    with pytest.raises(rc.RcError) as e:
+        s.sync()
+    assert e.value.code & 64
+    s.clear_error()
+    s.set_wait_limit(1 << 24)
+    s.set_state(c.array("PA"), c.array("WA"))
+    s.run(5)
+    clean = rc.Solver(c, precision=rc.RC_PREC_MIXED)
+    clean.set_state(c.array("PA"), c.array("WA"))
+    clean.run(5)
+    PA, WA = s.get_state()
+    PA0, WA0 = clean.get_state()
+    assert np.array_equal(PA, PA0) and np.array_equal(WA, WA0)
+    s.close()
+    clean.close()
 
 
 def test_forced_level_wait_timeout_is_reported(case_root, monkeypatch):

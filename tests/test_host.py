@@ -39,6 +39,25 @@ def test_library_exports_every_declared_symbol():
     assert set(names) == set(rc.SIGNATURES), set(names) ^ set(rc.SIGNATURES)
 
 
+def test_last_error_buffer_form():
+    """rc_last_error_buf copies the message a Fortran host prints before it
+    stops: at most len-1 bytes, always NUL-terminated; a NULL buffer or a
+    length below 1 is rejected without writing.  (No context: the message is
+    the fixed "no context", so no GPU is needed.)"""
+    L = rc.load()
+    full = L.rc_last_error(None).decode()
+    for n in (1, 2, 4, len(full), len(full) + 1, 64):
+        buf = ctypes.create_string_buffer(b"\xff" * n, n)
+        assert L.rc_last_error_buf(None, buf, n) == rc.RC_OK
+        raw = buf.raw
+        k = min(len(full), n - 1)
+        assert raw[:k].decode() == full[:k] and raw[k] == 0, (n, raw)
+    buf = ctypes.create_string_buffer(b"\xff" * 4, 4)
+    assert L.rc_last_error_buf(None, buf, 0) == rc.RC_ERR_ARG
+    assert buf.raw == b"\xff" * 4
+    assert L.rc_last_error_buf(None, None, 16) == rc.RC_ERR_ARG
+
+
 @pytest.mark.parametrize("name,over", [("t1", {}), ("t2", {}), ("t1", {"order": "random"}),
                                        ("c1", {"nx": 60, "ny": 12})])
 def test_setup_matches_oracle_bitwise(case_root, name, over):
