@@ -3,15 +3,19 @@
 
 One step = one lu_sgs_stage (TimeStep, reconstruction, flux_sourceterm,
 LU_SGS_steady with the Newton update) over the whole mesh, launched as one
-captured CUDA graph.  Default workload: the reacting viscous nozzle of about
-120k triangles (4 species, T-dependent cp, global H2/O2 reaction), plain FP64.
+captured CUDA graph.  Default workload: the large single case of the
+roofline configuration, the reacting viscous nozzle at 2,000,000 triangles
+(4 species, T-dependent cp, global H2/O2 reaction), plain FP64, with the mixed
+form timed beside it.
 
   value   cell-iters/s = NE * K / (sum of device-timed steps), state resident in
           HBM, L2 flushed (256 MB write) between timed steps;
   e2e     the same metric through the C ABI with the state in pinned host
           memory: each step copies PA, WA host->device, runs the stage, reads the
           residual norms and copies PA, WA device->host;
-  roofline  the dominant subroutine timed live with CUDA events;
+  roofline  the dominant subroutine timed live with CUDA events, and per
+          subroutine its fraction of the measured HBM bandwidth and of the
+          FP64 rate measured on this GPU by rc_fp64_rate;
   cpu_baseline  the FP64 CPU oracle on all host threads, bounded sample.
 
 --impl reference times the CPU restatement of the reference (the oracle) on
@@ -56,6 +60,8 @@ def algo_bytes_per_cell(V: int, nf_ne: float, viscous: bool, combustion: bool) -
 # --cache-control none: the caches as the live run leaves them; profiles/)
 NCU_DRAM_PER_CELL = {"lu_sgs_steady": (25643776 + 13218816 + 6815488 + 3588096) / 120000,
                      "flux_sourceterm": (22433024 + 25496320 + 2027776 + 6353152) / 120000}
+NCU_TRAFFIC_SOURCE = ("ncu capture of one iteration at 120,000 cells with the dataflow LU-SGS, caches as in the "
+                      "live run (profiles/c2_fp64_flow_launches.md), scaled by cells")
 
 
 def read_peaks():
@@ -65,6 +71,64 @@ def read_peaks():
             d = json.load(f)
         return float(d["hbm_gbs"]), "measured"
     return 6800.0, "fallback"
+
+
+# FP64-pipe warp instructions per cell of each subroutine's kernels in one FP64
+# iteration of the reacting viscous nozzle (ncu sm__inst_executed_pipe_fp64.sum
+# over the launches of each subroutine, divided by the cells; the count grows
+# with the cells).  Filled from the capture in profiles/.
+NCU_FP64_INST_PER_CELL: dict = {}
+
+
+def fp64_rate(rc, stream, torch, iters: int = 4000, repeats: int = 3) -> dict:
+    """The FP64 rate of this GPU (rc_fp64_rate: DADD/DMUL chains on every SM),
+    best of `repeats` CUDA-event-timed launches, SM clock sampled meanwhile."""
+    import ctypes
+    L = rc.load()
+    best, secs = 0.0, []
+    with ClockSampler(gpu_id(torch)) as clk:
+        for _ in range(repeats):
+            ops, sec = ctypes.c_double(0.0), ctypes.c_double(0.0)
+            st = L.rc_fp64_rate(ctypes.c_void_p(stream.cuda_stream), iters, ctypes.byref(ops), ctypes.byref(sec))
+            if st != 0:
+                raise RuntimeError(f"rc_fp64_rate failed with status {st}")
+            best = max(best, ops.value)
+            secs.append(sec.value)
+    return {"ops_per_s": best, "warp_inst_per_s": best / 32.0, "unit": "FP64 ops/s (DADD, DMUL)",
+            "seconds_per_launch": secs, "clocks": clk.summary(),
+            "source": "measured here: rc_fp64_rate, 8 blocks x 256 threads per SM, 8 independent DADD/DMUL "
+                      "chains per thread, best of 3 launches (CUDA events)"}
+
+
+def roofline(dom, sub_ms, ab, NE, peak, peak_kind, fp64) -> dict:
+    """The dominant subroutine against the HBM roofline, and every subroutine
+    against both the HBM bandwidth and the measured FP64 rate, with the one
+    that binds."""
+    per = {}
+    for name, ms in sub_ms.items():
+        t = ms * 1e-3
+        hbm = ab[name] * NE / t / 1e9
+        e = {"ms": ms, "algorithmic_bytes_per_cell": ab[name], "hbm_gbs": hbm, "hbm_frac": hbm / peak}
+        c = NCU_FP64_INST_PER_CELL.get(name)
+        if c is not None and fp64:
+            rate = c * NE / t
+            e.update({"fp64_warp_inst_per_cell": c, "fp64_warp_inst_per_s": rate,
+                      "fp64_frac": rate / fp64["warp_inst_per_s"]})
+        if name == "lu_sgs_steady":
+            e["binds"] = "latency: the dependent chain of one pass per level, level after level"
+        elif e.get("fp64_frac", 0.0) > e["hbm_frac"]:
+            e["binds"] = "fp64"
+        else:
+            e["binds"] = "hbm"
+        per[name] = e
+    d = per[dom]
+    return {"bound": "hbm", "kernel": dom, "achieved": d["hbm_gbs"], "peak": peak, "unit": "GB/s",
+            "frac": d["hbm_frac"], "peak_source": peak_kind, "algorithmic_bytes_per_cell": ab[dom],
+            "traffic": NCU_DRAM_PER_CELL[dom] * NE if dom in NCU_DRAM_PER_CELL else None,
+            "traffic_source": NCU_TRAFFIC_SOURCE,
+            "fp64_peak": fp64, "per_subroutine": per,
+            "note": "LU-SGS is latency bound (a pass of a few cells per level, level after level along the "
+                    "reference cell order); the face and cell kernels are bound by the FP64 pipe"}
 
 
 class ClockSampler:
@@ -167,12 +231,17 @@ def run_reference(args, rank, world):
                 "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
                 "ms_per_step": 1e3 * dt / args.steps, "higher_is_better": True, "scaling": "weak",
                 "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-                "config": workload_config(cfg, o.NE, o.NF, "replicas" if world > 1 else "single"),
+                "config": workload_config(cfg, o.NE, o.NF, par_label(world)),
                 "cpu_baseline": {"value": v, "unit": "cell-iters/s", "cores": threads, "kind": "port",
                                  "sample": f"{args.steps} whole iterations after {args.warmup} warm-up"},
                 "e2e": {"value": v, "unit": "cell-iters/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
         print(json.dumps(line), flush=True)
     return 0
+
+
+def par_label(world: int) -> str:
+    """The `parallelism` entry, the same for both arms: one case per process."""
+    return "single" if world == 1 else f"replicas x{world}"
 
 
 def workload_config(cfg, ne, nf, par):
@@ -190,7 +259,7 @@ def main():
     ap.add_argument("--steps", type=int, default=50)
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--case", default="c2")
+    ap.add_argument("--case", default="c4")
     ap.add_argument("--order", default=None)
     ap.add_argument("--nx", type=int, default=None, help="override the preset's cells along the axis")
     ap.add_argument("--ny", type=int, default=None, help="override the preset's cells across")
@@ -241,6 +310,7 @@ def main():
     stream = torch.cuda.Stream(device=local)
     flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=f"cuda:{local}")
     forms_req = ["fp64", "mixed"] if args.precision == "both" else [args.precision]
+    fp64 = fp64_rate(rc, stream, torch)
     with tempfile.TemporaryDirectory() as tmp:
         d, cfg = make_workload(args.case, tmp, **case_overrides(args))
         case = rc.Case(d)
@@ -282,25 +352,15 @@ def main():
         ab = algo_bytes_per_cell(V, NF / NE, cfg.viscous, cfg.combustion)
         sub_ms = head["subroutine_ms"]
         dom = max(sub_ms, key=sub_ms.get)
-        achieved = ab[dom] * NE / (sub_ms[dom] * 1e-3) / 1e9
         line = {
             "metric": "cell-iters/s", "value": value, "unit": "cell-iters/s", "n_gpus": world,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * t_max / args.steps,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
             "dtype": "f64" if forms_req[0] == "fp64" else "f32+f64", "data": "synthetic",
-            "config": workload_config(cfg, NE, NF, f"replicas x{world}" if world > 1 else "single GPU"),
+            "config": workload_config(cfg, NE, NF, par_label(world)),
             "e2e": head["e2e"],
             "gpu_launches": head["launches"],
-            "roofline": {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": peak, "unit": "GB/s",
-                         "frac": achieved / peak, "peak_source": peak_kind,
-                         "algorithmic_bytes_per_cell": ab[dom],
-                         "traffic": NCU_DRAM_PER_CELL[dom] * NE if dom in NCU_DRAM_PER_CELL else None,
-                         "traffic_source": "ncu capture of one iteration at 120,000 cells with the dataflow "
-                                           "LU-SGS, caches as in the live run (profiles/c2_fp64_flow_launches.md), "
-                                           "scaled by cells",
-                         "note": "LU-SGS is latency bound: the dependent instruction chain of one pass of 8 "
-                                 "cells along 301+301 levels (natural cell order); the face and cell kernels "
-                                 "are FP64-issue bound (FP64 pipe 85-88%, DRAM < 2%)"},
+            "roofline": roofline(dom, sub_ms, ab, NE, peak, peak_kind, fp64),
             "subroutine_ms": sub_ms,
             "stage_algorithmic_gbs": ab["stage"] * NE / (t_max / args.steps) / 1e9,
             "levels": head["levels"],
@@ -331,8 +391,16 @@ def main():
             bat = batched_form(args, stream, flush, torch, rc, tmp)
             line.setdefault("forms", {})["batched"] = bat[0]
         if not args.no_surrogate and world == 1 and cfg.combustion and cfg.nsp == 4:
+            # trained and compared on the 120k-cell reacting nozzle (and the
+            # batched cases' states): the trajectories the surrogate is made for
+            if cfg.name == "c2":
+                case_s = case
+            else:
+                d_s, _ = make_workload("c2", tmp)
+                case_s = rc.Case(d_s)
             extra = torch.tensor(bat[2].T.copy(), device="cuda") if bat else None
-            sur, net = surrogate_form(args, stream, flush, torch, rc, case, extra)
+            sur, net = surrogate_form(args, stream, flush, torch, rc, case_s, extra)
+            sur["workload"] = f"c2: {case_s.NE} triangles, reacting viscous"
             line.setdefault("forms", {})["surrogate"] = sur
             if bat:
                 bat[0]["surrogate"] = batched_surrogate(args, stream, flush, torch, rc, bat[1], bat[2], net)
@@ -521,7 +589,7 @@ def converge(args, rc, torch):
     out = {"mode": "converge", "iterations": args.converge, "every": args.every, "levels": list(LEVELS)}
     with tempfile.TemporaryDirectory() as tmp:
         d, cfg = make_workload(args.case, tmp, **case_overrides(args))
-        out["config"] = workload_config(cfg, 0, 0, "single GPU")
+        out["config"] = workload_config(cfg, 0, 0, par_label(1))
         finals = {}
         for form in ("fp64", "mixed", "mixed_dc"):
             case = rc.Case(d)

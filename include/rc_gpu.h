@@ -305,6 +305,13 @@ void* rc_get_stream(rc_ctx* ctx);
  * captured kernel node) and the number of LU-SGS levels of each sweep. */
 int rc_stats(rc_ctx* ctx, long long* kernel_launches, int* fwd_levels, int* bwd_levels);
 
+/* Measured FP64 rate of the current device (no counterpart in the reference:
+ * a measurement aid).  A kernel of 8 independent DADD/DMUL chains per thread,
+ * 8 blocks of 256 threads per SM, `iters` steps of each chain, timed with CUDA
+ * events on cuda_stream after one shorter warm-up launch.  ops_per_s =
+ * thread-level FP64 operations per second; seconds = the timed launch. */
+int rc_fp64_rate(void* cuda_stream, int iters, double* ops_per_s, double* seconds);
+
 const char* rc_last_error(rc_ctx* ctx);
 
 /* The same message copied into a caller buffer of len bytes, the form a

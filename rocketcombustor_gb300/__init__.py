@@ -93,6 +93,7 @@ SIGNATURES = {
     "rc_stats": (_i, [_vp, ctypes.POINTER(ctypes.c_longlong), _IP, _IP]),
     "rc_last_error": (_cp, [_vp]),
     "rc_last_error_buf": (_i, [_vp, _cp, _i]),
+    "rc_fp64_rate": (_i, [_vp, _i, _DP, _DP]),
     "rc_case_open": (_i, [_cp, ctypes.POINTER(_vp)]),
     "rc_case_error": (_cp, [_vp]),
     "rc_case_close": (None, [_vp]),

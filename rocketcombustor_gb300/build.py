@@ -25,6 +25,7 @@ NVCC_COMMON = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC,-ffp-contr
 UNITS = {
     "rc_core.cu": ["--fmad=false"],
     "rc_noalloc.cu": ["--fmad=false"],
+    "rc_peak.cu": ["--fmad=false"],
     "rc_chem.cu": ["--fmad=false"],
     "rc_bdf2.cu": ["--fmad=false"],
     "rc_mlp.cu": [],

@@ -68,8 +68,13 @@ def area_ratio_mach(ratio, gamma: float, supersonic):
         mid = 0.5 * (lo + hi)
         f = (1.0 / mid) * ((2.0 / (gamma + 1.0)) * (1.0 + 0.5 * (gamma - 1.0) * mid * mid)) ** g1 - ratio
         go_up = (f > 0) == (~sup)
-        lo = np.where(go_up, mid, lo)
-        hi = np.where(go_up, hi, mid)
+        lo2 = np.where(go_up, mid, lo)
+        hi2 = np.where(go_up, hi, mid)
+        # once every bracket is two adjacent doubles, further steps change nothing
+        done = np.array_equal(lo2, lo) and np.array_equal(hi2, hi)
+        lo, hi = lo2, hi2
+        if done:
+            break
     m = 0.5 * (lo + hi)
     return float(m) if m.ndim == 0 else m
 
@@ -93,10 +98,10 @@ class Mesh:
     @property
     def nf(self) -> int:
         """Number of distinct cell edges."""
-        c = self.cells
+        c = self.cells.astype(np.int64)
         e = np.concatenate([c[:, [0, 1]], c[:, [1, 2]], c[:, [2, 0]]])
-        e.sort(axis=1)
-        return int(np.unique(e, axis=0).shape[0])
+        key = np.minimum(e[:, 0], e[:, 1]) * (self.nnt + 1) + np.maximum(e[:, 0], e[:, 1])
+        return int(np.unique(key).shape[0])
 
 
 def _color_order(cells: np.ndarray, nnt: int) -> np.ndarray:
@@ -168,21 +173,35 @@ def nozzle_mesh(nx: int, ny: int, seed: int, order: str = "natural", wall_type: 
     return Mesh(coor=coor, cells=cells, boundaries=boundaries, nx=nx, ny=ny)
 
 
+def _write_rows(f, arr, fmt) -> None:
+    """The text np.savetxt(f, arr, fmt) writes (space-separated, one line per
+    row, each field through `%`), formatted a chunk of rows at a time."""
+    arr = np.asarray(arr)
+    if arr.ndim == 1:
+        arr = arr[:, None]
+    ncol = arr.shape[1]
+    row = (" ".join(fmt) if isinstance(fmt, (list, tuple)) else " ".join([fmt] * ncol)) + "\n"
+    step = 65536
+    for a in range(0, arr.shape[0], step):
+        blk = arr[a:a + step]
+        f.write((row * blk.shape[0]) % tuple(blk.ravel().tolist()))
+
+
 def write_grid(path: str, mesh: Mesh) -> None:
     """grid1.in in the layout read by ReadMesh (src/mesh.f90:10-65)."""
     ne, nnt, nf = mesh.ne, mesh.nnt, mesh.nf
     with open(path, "w") as f:
         f.write(f"{ne} {ne} {nnt} {nnt} {nf} {nf}\n")
         cells = np.concatenate([np.full((ne, 1), 3, dtype=np.int64), mesh.cells], axis=1)
-        np.savetxt(f, cells, fmt="%d")
+        _write_rows(f, cells, "%d")
         cz = np.concatenate([mesh.coor, np.zeros((nnt, 2))], axis=1)
-        np.savetxt(f, cz, fmt=["%.17g", "%.17g", "%d", "%d"])
+        _write_rows(f, cz, ["%.17g", "%.17g", "%d", "%d"])
         f.write("0\n")  # NConE
         nbmax = max(len(p) for _, p in mesh.boundaries)
         f.write(f"{len(mesh.boundaries)} {nbmax}\n")
         for itype, pairs in mesh.boundaries:
             f.write(f"{itype} {len(pairs)}\n")
-            np.savetxt(f, pairs, fmt="%d")
+            _write_rows(f, pairs, "%d")
         f.write("0\n")  # NCon
 
 
@@ -321,7 +340,7 @@ def write_backup(path: str, mesh: Mesh, PA: np.ndarray) -> None:
     with open(path, "w") as f:
         f.write("0.0\n")
         f.write(f"{mesh.ne}\n")
-        np.savetxt(f, np.concatenate([cxy, PA], axis=1), fmt="%.17g")
+        _write_rows(f, np.concatenate([cxy, PA], axis=1), "%.17g")
 
 
 # --------------------------------------------------------------- configs ---

@@ -153,6 +153,32 @@ def test_full_size_c2_20_iterations(case_root):
     assert np.array_equal(PA, o.array("PA")) and np.array_equal(WA, o.array("WA"))
 
 
+@pytest.mark.parametrize("precision", [rc.RC_PREC_FP64, rc.RC_PREC_MIXED])
+def test_full_size_c4_3_iterations(case_root, precision):
+    """The 2,000,000-triangle reacting viscous nozzle (the benchmark workload)
+    at its full size: 3 iterations with the autotuned schedule.  FP64 is bit
+    for bit the oracle's (run on all host threads); the mixed form stays
+    within its stated bound of the oracle (p, T 1e-4, Y_k 1e-3 relative
+    L-infinity after 3 iterations from the same state)."""
+    d = make_case(case_root, "c4")
+    c = rc.Case(d)
+    s = rc.Solver(c, precision=precision)
+    s.autotune(2)
+    s.set_state(c.array("PA"), c.array("WA"))
+    s.run(3)
+    o = oracle.Oracle(d, threads=oracle.Oracle.max_threads())
+    o.run(3)
+    PA, WA = s.get_state()
+    if precision == rc.RC_PREC_FP64:
+        assert np.array_equal(PA, o.array("PA")), rel_linf(PA, o.array("PA"))
+        assert np.array_equal(WA, o.array("WA")), rel_linf(WA, o.array("WA"))
+    else:
+        e = rel_linf(PA, o.array("PA"))
+        assert e[0] <= 1e-4 and e[3] <= 1e-4 and e[4:].max() <= 1e-3, e
+    s.close()
+    o.close()
+
+
 def test_device_stop_condition_is_reported(case_t1):
     """A negative pressure planted in the host state is caught by TimeStep's
     check (TimeStep.f90:66-70) and reported at the next synchronising call."""
