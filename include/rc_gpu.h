@@ -36,12 +36,12 @@ extern "C" {
 #endif
 
 #define RC_OK 0
-#define RC_ERR_THERMO_T 1      /* ComputeGasParameter/compute_enthalpy T out of range (thermo_property.f90:174-177,214-217) */
+#define RC_ERR_THERMO_T 1      /* ComputeGasParameter/compute_enthalpy T out of range (thermo_property.f90:97-101,137-141) */
 #define RC_ERR_TRANSPORT_T 2   /* compute_transport_property T out of range (transport_property.f90:101-105) */
 #define RC_ERR_NEG_TIMESTEP 4  /* rho, p or T < 0 in TimeStep (TimeStep.f90:66-70) */
 #define RC_ERR_NEG_FACE 8      /* rho or p < 0 at a face in flux_lax (flux_lax.f90:239-242) */
-#define RC_ERR_NAN 16          /* NaN in WA(1,1) after a stage (Time_LUSGS_steady.f90:94-97) */
-#define RC_ERR_BCTYPE 32       /* unknown boundary code (flux_lax.f90:232-235, update_flow_variables.f90:364-367) */
+#define RC_ERR_NAN 16          /* NaN in WA(1,1) after a stage (Time_LUSGS_steady.f90:24-27) */
+#define RC_ERR_BCTYPE 32       /* unknown boundary code (flux_lax.f90:232-235, update_flow_variables.f90:256-259) */
 #define RC_ERR_SYNC 64         /* a bounded wait of the cooperative LU-SGS kernels gave up (level counter or pass flag) */
 #define RC_ERR_LINSOLVE 128    /* a BDF2 cell system is singular to working precision (dgesvx info /= 0, la_math.f90:176-211) */
 #define RC_ERR_ARG 1024        /* invalid argument or unsupported configuration */
@@ -108,15 +108,15 @@ typedef struct rc_thermo {
   const double* high_enthalpy_b1;       /* (Nsp) */
   double transport_lowest_tem, transport_critical_tem, transport_highest_tem;
   const double* mu_K[16];               /* low_mu_A..D, high_mu_A..D, low_K_A..D, high_K_A..D, each (Nsp) */
-  const double* collision_diameter;     /* (Nsp) diffusion_velocity.f90:132 */
+  const double* collision_diameter;     /* (Nsp) diffusion_velocity.f90:7 */
   const double* LJ_energy;              /* (Nsp) */
   int code_chemical_model;              /* chemical_kinetics.f90:6 */
   const double* coef_f_react;           /* (Nsp) of reaction 1 */
   const double* coef_r_react;           /* (Nsp) of reaction 1 */
   double Af_react, E_react;             /* reaction 1 */
-  const double* oxidizer_mass_fraction; /* (Nsp) oxidizer.f90:323 */
+  const double* oxidizer_mass_fraction; /* (Nsp) oxidizer.f90:9 */
   double oxidizer_temp_in, oxidizer_mass_flow;
-  const double* fuel_mass_fraction;     /* (Nsp) fuel.f90:392 */
+  const double* fuel_mass_fraction;     /* (Nsp) fuel.f90:9 */
   double fuel_temp_in, fuel_mass_flow;
 } rc_thermo;
 
@@ -166,8 +166,8 @@ int rc_get_state(rc_ctx* ctx, double* PA, double* WA);
 int rc_timestep(rc_ctx* ctx);          /* TimeStep            TimeStep.f90:4 */
 int rc_reconstruction(rc_ctx* ctx);    /* reconstruction      fvm2d.f90:183 (gradient + Limiter_Barth) */
 int rc_flux_sourceterm(rc_ctx* ctx);   /* flux_sourceterm     fvm2d.f90:196 (flux_lax + flux_viscous + sourceterm) */
-int rc_lusgs_steady(rc_ctx* ctx);      /* LU_SGS_steady       Time_LUSGS_steady.f90:102 (incl. update_primitve_variables) */
-int rc_lusgs_stage(rc_ctx* ctx, int istep); /* lu_sgs_stage   Time_LUSGS_steady.f90:74, one captured graph */
+int rc_lusgs_steady(rc_ctx* ctx);      /* LU_SGS_steady       Time_LUSGS_steady.f90:32 (incl. update_primitve_variables) */
+int rc_lusgs_stage(rc_ctx* ctx, int istep); /* lu_sgs_stage   Time_LUSGS_steady.f90:4, one captured graph */
 
 /* Switch the precision of the following calls: RC_PREC_FP64 on any context,
  * RC_PREC_MIXED / RC_PREC_MIXED_DC on contexts created with a mixed mode.  A
@@ -250,7 +250,7 @@ int rc_surrogate_samples(rc_ctx* ctx, const double* d_P0, const double* d_P1, co
  * following calls: the host's compute_p_out (fvm2d.f90:229-239) result at the
  * current time.
  *
- * rc_bdf2_stage = BDF2_stage (Time_BDF2.f90:4-71): shifts the time levels
+ * rc_bdf2_stage = BDF2_stage (Time_BDF2.f90:4-69): shifts the time levels
  * (istep 1: WP = WP2 = WA, phi = 0; later WP2 = WP, WP = WA, phi = 1/2), then
  * up to inner_loop inner iterations of timestep, reconstruction,
  * flux_sourceterm and BDF2_LU_SGS, each one CUDA graph launch, stopped when
@@ -261,11 +261,11 @@ int rc_surrogate_samples(rc_ctx* ctx, const double* d_P0, const double* d_P1, co
  * driver shortens the last one, fvm2d.f90:52-56).  *inner_done gets the inner
  * iterations taken.  Synchronises once per inner iteration.
  *
- * rc_bdf2_lusgs = BDF2_LU_SGS (Time_BDF2.f90:73-337) alone, for per-subroutine
+ * rc_bdf2_lusgs = BDF2_LU_SGS (Time_BDF2.f90:71-337) alone, for per-subroutine
  * checks: on inner_rk 1 the source term vol/dt ((1+2 phi) WP - phi WP2) is
  * formed from the time levels "WP" and "WP2" (rc_set_array), then the
  * primitive-variable LU-SGS sweeps with the per-cell 7x7 solves of
- * advanced_linear_solve_lapack (la_math.f90:120-215) and the update of PA and
+ * advanced_linear_solve_lapack (la_math.f90:120-213) and the update of PA and
  * WA.  A cell system singular to working precision latches RC_ERR_LINSOLVE
  * (the reference stops).
  */

@@ -55,7 +55,7 @@ int rc_case_set_state(rc_case* c, const double* PA, const double* WA);
 /* BackupData (src/output.f90:256): fvp-format restart file of the case's state,
  * readable by Read_Backup (and by rc_case_open); 17 significant digits. */
 int rc_case_write_backup(rc_case* c, const char* path, double ttime);
-/* output_vtk (src/output.f90:4): legacy ASCII VTK of the cell-centred rho, u,
+/* output_vtk (src/output.f90:5): legacy ASCII VTK of the cell-centred rho, u,
  * v, p, T, Ma, Y_k and production rates of the case's state. */
 int rc_case_write_vtk(rc_case* c, const char* path);
 

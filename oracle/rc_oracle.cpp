@@ -149,7 +149,7 @@ enum Err { E_OK = 0, E_THERMO_T = 1, E_TRANSPORT_T = 2, E_NEG_TIMESTEP = 4, E_NE
            E_NAN = 16, E_BCTYPE = 32, E_SETUP = 64, E_LINSOLVE = 128 };
 
 // ------------------------------------------ LAPACK dgesvx restatement -----
-// advanced_linear_solve_lapack (la_math.f90:120-215) solves the per-cell
+// advanced_linear_solve_lapack (la_math.f90:120-213) solves the per-cell
 // system of the BDF2 sweeps with LAPACK's expert driver
 //   dgesvx('E', 'N', n, 1, A, n, AF, n, ipiv, equed, r, c, b, n, x, n, rcond, ferr, berr, ...)
 // and stops unless info == 0.  LAPACK is linked as -llapack (src/Makefile:43)
@@ -422,7 +422,7 @@ struct Oracle {
   int Nsp = 0;
   double Rconstant = 0;
   std::vector<double> mole_weight, R_species;
-  // ---- thermo (thermo_property.f90:81-93)
+  // ---- thermo (thermo_property.f90:4-16)
   double Tref = 0;
   int order_of_cp_polynomial = 0;
   double thermo_lowest_tem = 0, thermo_critical_tem = 0, thermo_highest_tem = 0;
@@ -432,7 +432,7 @@ struct Oracle {
   double transport_lowest_tem = 0, transport_critical_tem = 0, transport_highest_tem = 0;
   std::vector<double> low_mu_A, low_mu_B, low_mu_C, low_mu_D, high_mu_A, high_mu_B, high_mu_C, high_mu_D;
   std::vector<double> low_K_A, low_K_B, low_K_C, low_K_D, high_K_A, high_K_B, high_K_C, high_K_D;
-  // ---- diffusion (diffusion_velocity.f90:129-138)
+  // ---- diffusion (diffusion_velocity.f90:4-13)
   double k_B = 0;
   std::vector<double> collision_diameter, LJ_energy;
   // ---- kinetics (chemical_kinetics.f90:4-13)
@@ -440,7 +440,7 @@ struct Oracle {
   FA2<double> coef_f_react, coef_r_react;
   std::vector<double> Af_react, beta_react, E_react, dentropy_react, denthalpy_react;
   double p_a = 0;
-  // ---- inlets (oxidizer.f90:318-325, fuel.f90:387-394)
+  // ---- inlets (oxidizer.f90:4-11, fuel.f90:4-11)
   std::vector<double> oxidizer_mass_fraction, fuel_mass_fraction;
   double oxidizer_temp_in = 0, oxidizer_pre_in = 0, oxidizer_mass_flow = 0;
   double fuel_temp_in = 0, fuel_pre_in = 0, fuel_mass_flow = 0;
@@ -459,7 +459,7 @@ struct Oracle {
   double unit = 1, cfl = 0, totaltime = 0, save_start_time = 0, save_end_time = 0, relTol = 0;
   double rc_detector = 0, p_out_ratio = 0, A_p = 0, f_p = 0, p_out = 0, p_static = 0, ttime = 0;
   long nstep_max = 0;
-  double wxx = 0.5, wgg = 1.0;  // InitParam (initParam.f90:168-169), NG=1
+  double wxx = 0.5, wgg = 1.0;  // InitParam (initParam.f90:12-13), NG=1
   double total_volume = 0;
 
   FA2<int> N, NeighF, NeighC, FNode, Neighbor, NodeFace, Ghostcell;
@@ -503,7 +503,7 @@ struct Oracle {
     Rconstant = r.d();
     for (int i = 0; i < Nsp; ++i) R_species[i] = Rconstant / mole_weight[i];
   }
-  // setup_thermo_property (thermo_property.f90:95-136)
+  // setup_thermo_property (thermo_property.f90:18-59)
   void setup_thermo_property(const std::string& dir) {
     LDReader r(dir + "/combustion/thermo.in");
     r.skip();
@@ -547,7 +547,7 @@ struct Oracle {
         for (int c = 0; c < 4; ++c) (*arrs[row * 4 + c])[i] = tod(v[c]);
       }
   }
-  // setup_diffusion_velocity (diffusion_velocity.f90:140-166)
+  // setup_diffusion_velocity (diffusion_velocity.f90:15-41)
   void setup_diffusion_velocity(const std::string& dir) {
     LDReader r(dir + "/combustion/diffusion.in");
     r.skip();
@@ -592,7 +592,7 @@ struct Oracle {
     r.skip();
     p_a = r.d();
   }
-  // setup_oxidizer_info / setup_fuel_info (oxidizer.f90:327-355, fuel.f90:396-424)
+  // setup_oxidizer_info / setup_fuel_info (oxidizer.f90:13-41, fuel.f90:13-41)
   void setup_inlet(const std::string& path, std::vector<double>& Y, double& T, double& p, double& mflow) {
     LDReader r(path);
     r.skip();
@@ -605,7 +605,7 @@ struct Oracle {
     r.skip();
     mflow = r.d();
   }
-  // startup (startup.f90:1-136) and InitParam (initParam.f90:158-303, steady branch)
+  // startup (startup.f90:1-136) and InitParam (initParam.f90:2-147, steady branch)
   void startup(const std::string& dir) {
     setup_species_info(dir);
     setup_thermo_property(dir);
@@ -667,7 +667,7 @@ struct Oracle {
       throw std::runtime_error(
           "oracle covers the steady implicit, unsteady BDF2 and backward Euler single-partition paths only");
     if (IfSteady) {
-      InLoop = 1; InnerLoop = 1;  // initParam.f90:220-222
+      InLoop = 1; InnerLoop = 1;  // initParam.f90:64-66
     } else {
       dt = totaltime / (double)nstep_max;  // initParam.f90:72
       InLoop = 1;                          // BDF2 / Euler: one stage, cs(1) = 1 (initParam.f90:119-134)
@@ -675,7 +675,7 @@ struct Oracle {
   }
 
   // ============================================ thermochemistry (L3) =======
-  // ComputeGasParameter (thermo_property.f90:155-189)
+  // ComputeGasParameter (thermo_property.f90:78-112)
   void ComputeGasParameter(const double* Y, double tem, double& Cp, double& gama, double& Rcpcv) {
     const int P = order_of_cp_polynomial;
     double cp_basis[16];
@@ -696,7 +696,7 @@ struct Oracle {
     for (int i = 0; i < Nsp; ++i) Rcpcv = Rcpcv + R_species[i] * Y[i];
     gama = Cp / (Cp - Rcpcv);
   }
-  // compute_enthalpy (thermo_property.f90:191-221)
+  // compute_enthalpy (thermo_property.f90:114-144)
   void compute_enthalpy(double tem, double* entha) {
     const int P = order_of_cp_polynomial;
     double basis[16];
@@ -714,7 +714,7 @@ struct Oracle {
       entha[i - 1] = R_species[i - 1] * (tem * s + (*b1)[i - 1]);
     }
   }
-  // Newton_temperature (thermo_property.f90:223-257)
+  // Newton_temperature (thermo_property.f90:146-180)
   void Newton_temperature(double et, const double* Y, double& t, double t0, double& Cp, double& gama, double& Rcpcv) {
     const double epsilon = 1.0e-5;
     double entha[16];
@@ -773,7 +773,7 @@ struct Oracle {
     for (int i = 0; i < Nsp; ++i) s2 = s2 + xx[i] / Kl[i];
     akmu = 0.5 * (s1 + 1.0 / s2);
   }
-  // compute_diffusion_velocity (diffusion_velocity.f90:180-243)
+  // compute_diffusion_velocity (diffusion_velocity.f90:55-118)
   void compute_diffusion_velocity(double pp, double tem, const double* YY, double* Dk) {
     const double A = 1.06036, B = 0.15610, C = 0.19300, D = 0.47635, E = 1.03587, F = 1.52996, G = 1.76474,
                  H = 3.89411;
@@ -861,7 +861,7 @@ struct Oracle {
   }
   // compute_derivative_production_rate (chemical_kinetics.f90:167-265):
   // dwdp[i*NVar+c] = d omega_i / dP_c for the Nsp-1 transported species.
-  // Model 1 leaves dkfdy(3:) unset in the reference (:231-246); it is taken
+  // Model 1 leaves dkfdy(3:) unset in the reference (:228-243); it is taken
   // here as dkfdr*drdy(3:), the expression of model 0.
   void compute_derivative_production_rate(const double* pri, double* dwdp) {
     const int nv = NVar, ns1 = Nsp - 1;
@@ -1023,7 +1023,7 @@ struct Oracle {
   double chem_tol = 0.05;
   std::vector<int> chem_nsub;
 
-  // oxidizer_inlet_bc / fuel_inlet_bc (oxidizer.f90:367-382, fuel.f90:437-452)
+  // oxidizer_inlet_bc / fuel_inlet_bc (oxidizer.f90:53-68, fuel.f90:54-69)
   void inlet_bc(bool oxid, double pl, double& pr, double& ur, double& vr, double& tr, double& rr, double* Yr,
                 double& Cpr, double& gamar, double& Rcpcvr) {
     const std::vector<double>& Yin = oxid ? oxidizer_mass_fraction : fuel_mass_fraction;
@@ -1142,7 +1142,7 @@ struct Oracle {
     long NCon = toi(r.read(1)[0]);
     if (NCon != 0) throw std::runtime_error("oracle covers NCon=0 (no periodic pairs) only");
     change();
-    // CreatePeriodConnect (period.f90:65-156): with NCon=0 it only locates the
+    // CreatePeriodConnect (period.f90:15-106): with NCon=0 it only locates the
     // boundary faces, which this restatement does not need afterwards.
     // Face property / boundary type (mesh.f90:75-93): first matching boundary wins.
     for (long i = 1; i <= NF; ++i) {
@@ -1274,7 +1274,7 @@ struct Oracle {
     }
     primitve_to_conserved_variables();
   }
-  // primitve_to_conserved_variables (update_flow_variables.f90:158-192)
+  // primitve_to_conserved_variables (update_flow_variables.f90:50-84)
   void primitve_to_conserved_variables() {
     for (long i = 1; i <= NE; ++i) {
       double YY[16], entha[16], Cp, gama, Rcpcv;
@@ -1294,7 +1294,7 @@ struct Oracle {
       for (int k = 1; k <= Nsp - 1; ++k) WA(NFlow + k, i) = rr * YY[k - 1];
     }
   }
-  // construct_ghostcells (ghostcell.f90:19-195)
+  // construct_ghostcells (ghostcell.f90:19-181)
   void construct_ghostcells() {
     Nghostcell = 0;
     for (long i = 1; i <= NE; ++i) Nghostcell += KFace(i) - Neigh(i);
@@ -1376,7 +1376,7 @@ struct Oracle {
       B[2 * k + 1] = (g11 * A1[m + k] - g12 * A1[k]) / det;
     }
   }
-  // compute_reconstruction_matrix (reconstruction_initialization.f90:1-327)
+  // compute_reconstruction_matrix (reconstruction_initialization.f90:1-167)
   void compute_reconstruction_matrix() {
     std::vector<int> Ntemp(NE_Vir + 1, 0);
     for (long i = 1; i <= NF_vir; ++i) {
@@ -1581,7 +1581,7 @@ struct Oracle {
     }
   }
 
-  // update_ghostcell_variables (update_flow_variables.f90:195-377), one ghost.
+  // update_ghostcell_variables (update_flow_variables.f90:90-269), one ghost.
   void ghost_one(long j) {
     long i = Hostcell(j);
     double Yl[16], Yr[16], Cp, gama, Rcpcv;
@@ -1692,7 +1692,7 @@ struct Oracle {
 #pragma omp parallel for schedule(static) num_threads(nthreads) if (nthreads > 1)
     for (long i = 1; i <= NE; ++i) limiter_one(i);
   }
-  // reconstruction (fvm2d.f90:183-192)
+  // reconstruction (fvm2d.f90:183-191)
   void reconstruction() {
     gradient();
     if (limit_ID > 0) limiter_Barth();
@@ -1997,7 +1997,7 @@ struct Oracle {
     if (IfViscous) flux_viscous();
     sourceterm();
   }
-  // One LU-SGS sweep step for cell i (Time_LUSGS_steady.f90:126-190).
+  // One LU-SGS sweep step for cell i (Time_LUSGS_steady.f90:56-120, 127-190).
   // fwd: neighbours j<i, hWA(i) = (hWA(i)-dflux)/dd(i);
   // bwd: neighbours j>i, hWA(i) = hWA(i) - dflux/dd(i).
   void lusgs_cell(long i, bool fwd, const std::vector<double>& dd) {
@@ -2046,7 +2046,7 @@ struct Oracle {
       else hWA(k, i) = hWA(k, i) - dflux[k - 1] / dd[i];
     }
   }
-  // update_primitve_variables (update_flow_variables.f90:112-156), one cell.
+  // update_primitve_variables (update_flow_variables.f90:4-48), one cell.
   void update_prim_one(long i) {
     double Y[16], t, Cp, gama, Rcpcv;
     double rho = WA(1, i);
@@ -2063,7 +2063,7 @@ struct Oracle {
 #pragma omp parallel for schedule(static) num_threads(nthreads) if (nthreads > 1)
     for (long i = 1; i <= NE; ++i) update_prim_one(i);
   }
-  // LU_SGS_steady (Time_LUSGS_steady.f90:102-274)
+  // LU_SGS_steady (Time_LUSGS_steady.f90:32-204)
   void LU_SGS_steady() {
     std::vector<double> dd(NE + 1, 0.0);
 #pragma omp parallel for schedule(static) num_threads(nthreads) if (nthreads > 1)
@@ -2186,10 +2186,10 @@ struct Oracle {
     }
     for (int k = 1; k <= nv; ++k) hWA(k, i) = fwd ? sol[k - 1] : hWA(k, i) - sol[k - 1];
   }
-  // BDF2_LU_SGS (Time_BDF2.f90:73-337); with euler, backwardEuler_LU_SGS
+  // BDF2_LU_SGS (Time_BDF2.f90:71-337); with euler, backwardEuler_LU_SGS
   // (Time_BackwardEuler.f90:58-324), whose sweeps and update are the same and
   // whose source, diagonal and right-hand side are those of phi = 0 written
-  // without phi (:78-100).
+  // without phi (:75-98).
   void BDF2_LU_SGS(int inner_rk, double phi, bool euler = false) {
     if (inner_rk == 1) {
 #pragma omp parallel for schedule(static) num_threads(nthreads) if (nthreads > 1)
@@ -2234,7 +2234,7 @@ struct Oracle {
     for (int k = NFlow; k < NVar; ++k) r = r + res[k];
     return r;
   }
-  // BDF2_stage (Time_BDF2.f90:4-71), or with euler backwardEuler_stage
+  // BDF2_stage (Time_BDF2.f90:4-69), or with euler backwardEuler_stage
   // (Time_BackwardEuler.f90:4-56: no time levels); returns the inner
   // iterations taken.
   int BDF2_stage(long istep, bool euler = false) {

@@ -9,13 +9,13 @@ reference subroutine of the steady iteration:
     Solver.timestep()          TimeStep            src/TimeStep.f90:4
     Solver.reconstruction()    reconstruction      src/fvm2d.f90:183
     Solver.flux_sourceterm()   flux_sourceterm     src/fvm2d.f90:196
-    Solver.lu_sgs_steady()     LU_SGS_steady       src/Time_LUSGS_steady.f90:102
-    Solver.lu_sgs_stage(i)     lu_sgs_stage        src/Time_LUSGS_steady.f90:74
+    Solver.lu_sgs_steady()     LU_SGS_steady       src/Time_LUSGS_steady.f90:32
+    Solver.lu_sgs_stage(i)     lu_sgs_stage        src/Time_LUSGS_steady.f90:4
     Solver.residual()          Residual/step_residual  src/residual.f90:4,61
 
 and, for the unsteady dual-time scheme (implicit_time_method 5):
 
-    Solver.bdf2_lusgs(k, phi, dt)     BDF2_LU_SGS     src/Time_BDF2.f90:73
+    Solver.bdf2_lusgs(k, phi, dt)     BDF2_LU_SGS     src/Time_BDF2.f90:71
     Solver.bdf2_stage(i, dt, n, tol)  BDF2_stage      src/Time_BDF2.f90:4
     Solver.euler_stage(i, dt, n, tol) backwardEuler_stage  src/Time_BackwardEuler.f90:4
     Case.run_unsteady(n)              the unsteady branch of program main (src/fvm2d.f90:48-150)
@@ -514,7 +514,7 @@ class Solver:
         self.case.write_backup(path, ttime)
 
     def write_vtk(self, path: str):
-        """The device state as a VTK file (output_vtk, output.f90:4-227)."""
+        """The device state as a VTK file (output_vtk, output.f90:5-227)."""
         PA, WA = self.get_state()
         self.case.set_state(PA, WA)
         self.case.write_vtk(path)

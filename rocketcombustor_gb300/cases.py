@@ -17,7 +17,7 @@ half-height 0.01 at x = 0.15, cosine expansion to 0.03 at x = 0.25.  A mapped
 nx-by-ny quad grid is split into triangles with alternating diagonals and the
 interior nodes are jittered by a seeded uniform +-10 % of the local spacing.
 
-Boundary codes follow src/update_flow_variables.f90:240-368: 2 symmetry (axis),
+Boundary codes follow src/update_flow_variables.f90:132-260: 2 symmetry (axis),
 3 mass-flux inlet (x = 0), 5 outlet (x = 0.25), 6 slip wall or 1 no-slip wall.
 
 Cell order — the order in ``grid1.in`` fixes the Gauss-Seidel recurrence of the
@@ -229,7 +229,7 @@ def write_species(d: str, sp: Species) -> None:
 
 def write_thermo(d: str, low: np.ndarray, high: np.ndarray, b1: Sequence[float],
                  trange=(200.0, 1000.0, 60000.0)) -> None:
-    """thermo.in (thermo_property.f90:95-136); coefficient arrays are (Nsp, 7)."""
+    """thermo.in (thermo_property.f90:18-59); coefficient arrays are (Nsp, 7)."""
     nsp = low.shape[0]
     with open(os.path.join(d, "combustion", "thermo.in"), "w") as f:
         f.write("# reference temperature\n298.15\n# order of Cp polynomial\n7\n")
@@ -416,7 +416,7 @@ PRESETS: Dict[str, CaseConfig] = {
 def synthetic_cp(nsp: int, seed: int) -> np.ndarray:
     """Seeded smooth cp/R = a3 + a4 T + a5 T^2, rising from a3 in [3.5, 3.7] at
     T -> 0 to a maximum in [4.2, 4.5] at 4000 K (coefficient slots 3..5 of the
-    7-term polynomial, thermo_property.f90:162-172)."""
+    7-term polynomial, thermo_property.f90:84-96)."""
     rng = np.random.default_rng(seed)
     coef = np.zeros((nsp, 7))
     for i in range(nsp):

@@ -9,7 +9,7 @@
 // shares (timestep, reconstruction, flux_sourceterm):
 //   k_bdf2_prep    every cell at once: the diagonal dd, the BDF2 right-hand
 //                  side hWA - (1+phi) vol/dt WA + fixed, the cell's system
-//                  matrix dU/dP dd - vol d omega/dP (Time_BDF2.f90:118-127),
+//                  matrix dU/dP dd - vol d omega/dP (Time_BDF2.f90:121-129),
 //                  its equilibration, LU factors and condition estimate (the
 //                  LAPACK dgesvx steps below), and the gas state the
 //                  neighbours' sweeps read;
@@ -25,7 +25,7 @@
 // factors it the same way, so the results are the same bits.
 //
 // The per-cell solve restates reference LAPACK 3.12's dgesvx('E', 'N') as
-// called by advanced_linear_solve_lapack (la_math.f90:120-215): dgeequ +
+// called by advanced_linear_solve_lapack (la_math.f90:120-213): dgeequ +
 // dlaqge, dgetrf with partial pivoting, dgecon (dlacn2 over triangular
 // solves; only its comparison with eps matters: the reference stops there),
 // dgetrs and the refinement loop of dgerfs, in the operation order of the
@@ -299,8 +299,8 @@ __device__ __forceinline__ double getrs_rows(double x, int src, const double* lu
 }
 }  // namespace bdf2
 
-// fixed = vol/dt ((1+2 phi) WP - phi WP2) (Time_BDF2.f90:100-105), or for
-// backward Euler vol/dt WA (Time_BackwardEuler.f90:78-82)
+// fixed = vol/dt ((1+2 phi) WP - phi WP2) (Time_BDF2.f90:88-92), or for
+// backward Euler vol/dt WA (Time_BackwardEuler.f90:75-79)
 template <int NSP>
 __global__ void __launch_bounds__(128) k_bdf2_fixed(const Dev d, int euler) {
   constexpr int V = 3 + NSP;
@@ -325,7 +325,7 @@ __global__ void __launch_bounds__(128) k_bdf2_prep(const Dev d, const ThermoDev<
   const int NE = d.NE;
   const double dt = d.bpar[0], phi = d.bpar[1], vol = d.vol[i];
   unsigned err = 0;
-  // diagonal (Time_BDF2.f90:107-114) and right-hand side (:116-122)
+  // diagonal (Time_BDF2.f90:94-102) and right-hand side (:104-111)
   double s = 0.0;
   const int nf = d.nface[i];
   for (int q = 0; q < nf; ++q) s = s + 0.5 * d.alpaF[d.cface[q * NE + i]];
@@ -333,7 +333,7 @@ __global__ void __launch_bounds__(128) k_bdf2_prep(const Dev d, const ThermoDev<
 #pragma unroll
   for (int k = 0; k < V; ++k)
     d.hWA[k * NE + i] = d.hWA[k * NE + i] - (1 + phi) * vol / dt * d.WA[k * NE + i] + d.bfix[k * NE + i];
-  // system matrix (:124-132)
+  // system matrix (:121-129)
   double pri[V];
 #pragma unroll
   for (int k = 0; k < V; ++k) pri[k] = d.PA[k * NE + i];

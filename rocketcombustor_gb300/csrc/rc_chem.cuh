@@ -73,7 +73,7 @@ __device__ __forceinline__ void con_to_pri_jaco(const ThermoDev<NSP>& th, const 
 }
 
 // d omega_i / dP, row-major [NSP-1][V].  Model 1 leaves dkfdy(3:) unset in
-// the reference (chemical_kinetics.f90:231-246); it is taken as dkfdr*drdy(3:).
+// the reference (chemical_kinetics.f90:228-243); it is taken as dkfdr*drdy(3:).
 template <int NSP>
 __device__ __forceinline__ void dwdp(const ThermoDev<NSP>& th, const double* pri, double* D, unsigned& err) {
   constexpr int V = 3 + NSP, NS1 = NSP - 1;

@@ -1,5 +1,5 @@
 // GB300 (sm_103a) kernels and C ABI for the steady LU-SGS iteration of
-// RocketCombustor (lu_sgs_stage, src/Time_LUSGS_steady.f90:74-100).
+// RocketCombustor (lu_sgs_stage, src/Time_LUSGS_steady.f90:4-30).
 //
 // Device layout (structure of arrays, reference cell/face order, 0-based):
 //   cell arrays  X[k*NE + i]  (PA, WA, hWA, cell gas state, sources)
@@ -38,7 +38,7 @@
 
 namespace rc {
 
-// oxidizer_inlet_bc / fuel_inlet_bc (oxidizer.f90:367-382, fuel.f90:437-452)
+// oxidizer_inlet_bc / fuel_inlet_bc (oxidizer.f90:53-68, fuel.f90:54-69)
 // with the inlet data of row bc of the case table (w = 0 oxidizer, 1 fuel).
 template <int NSP>
 __device__ __forceinline__ void inlet_bc(const ThermoDev<NSP>& th, const double* bc, int w, double pl, double& pr,
@@ -98,8 +98,8 @@ __global__ void __launch_bounds__(128) k_ts_face(const Dev d, const ThermoDev<NS
 }
 
 // --------------------------------------------------------- cell kernel -----
-// step/dd (TimeStep.f90:94-96, Time_LUSGS_steady.f90:116-123), ghost states
-// (update_flow_variables.f90:195-377), gradient (gradient.f90:4-45), Barth
+// step/dd (TimeStep.f90:94-96, Time_LUSGS_steady.f90:46-53), ghost states
+// (update_flow_variables.f90:90-269), gradient (gradient.f90:4-45), Barth
 // limiter (limiter.f90:5-107), cell gas state and source (sourceterm.f90:2-70).
 template <int NSP>
 __global__ void __launch_bounds__(128) k_cell(const Dev d, const ThermoDev<NSP> th, int do_step, int do_recon,
@@ -540,7 +540,7 @@ __global__ void __launch_bounds__(128) k_gather(const Dev d, int visc, int comb)
 }
 
 // ---------------------------------------------------------------- LU-SGS ---
-// LU-SGS forward / backward sweeps (Time_LUSGS_steady.f90:125-260).
+// LU-SGS forward / backward sweeps (Time_LUSGS_steady.f90:55-190).
 // A quad of 4 lanes handles one cell: lane q evaluates the dflux term of the
 // neighbour in face slot q, the terms are added in slot order (the NeighF
 // order of the reference) and the lanes share the final divisions.  The
@@ -1966,7 +1966,7 @@ int init_impl(const rc_mesh* m, const rc_thermo* t, const rc_config* g, const Ba
     fss[fi] = std::sqrt(dx * dx + dy * dy);
     fs2[fi] = dx * dx + dy * dy;
     const int n1 = m->FNode[2 * (f - 1)], n2 = m->FNode[2 * (f - 1) + 1];
-    // Gauss point xy = Coor(n1) + wxx*(Coor(n2)-Coor(n1)), wxx = 0.5 (initParam.f90:169)
+    // Gauss point xy = Coor(n1) + wxx*(Coor(n2)-Coor(n1)), wxx = 0.5 (initParam.f90:13)
     const double x = C2(m->COOR, 1, n1) + 0.5 * (C2(m->COOR, 1, n2) - C2(m->COOR, 1, n1));
     const double y = C2(m->COOR, 2, n1) + 0.5 * (C2(m->COOR, 2, n2) - C2(m->COOR, 2, n1));
     fvL[fi] = (x - C2(m->CELLXY, 1, L)) / C2(m->reflen, 1, L);
@@ -2033,7 +2033,7 @@ int init_impl(const rc_mesh* m, const rc_thermo* t, const rc_config* g, const Ba
       am[(size_t)(2 * q + 1) * NE + ii] = m->AMLS[(size_t)2 * M * ii + 2 * q + 1];
     }
   }
-  // ---- ghosts: unit normal of the ghost face (update_flow_variables.f90:222-236)
+  // ---- ghosts: unit normal of the ghost face (update_flow_variables.f90:114-128)
   std::vector<int> gtype(NG);
   std::vector<double> gsn(2 * (size_t)NG);
   for (int j = 0; j < NG; ++j) {

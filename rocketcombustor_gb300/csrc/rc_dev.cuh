@@ -150,7 +150,7 @@ __device__ __forceinline__ unsigned ld_acquire(const unsigned* p) {
   return v;
 }
 
-// WA += hWA and update_primitve_variables (update_flow_variables.f90:112-156).
+// WA += hWA and update_primitve_variables (update_flow_variables.f90:4-48).
 template <int NSP>
 __device__ __forceinline__ void update_cell(const Dev& d, const ThermoDev<NSP>& th, int i, unsigned& err) {
   constexpr int V = 3 + NSP;

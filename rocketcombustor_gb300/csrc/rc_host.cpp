@@ -199,7 +199,7 @@ void rc_case::read_inputs() {
     for (int i = 0; i < Nsp; ++i) Rsp[i] = Rconstant / mw[i];
     NVar = 4 + Nsp - 1;  // setup_number_of_variables (species.f90:53-65)
   }
-  {  // setup_thermo_property (thermo_property.f90:95-136)
+  {  // setup_thermo_property (thermo_property.f90:18-59)
     Records r(c + "thermo.in");
     r.skip(); r.real();
     r.skip();
@@ -231,7 +231,7 @@ void rc_case::read_inputs() {
         for (int k = 0; k < 4; ++k) muK[row * 4 + k][i] = num(v[k]);
       }
   }
-  {  // setup_diffusion_velocity (diffusion_velocity.f90:140-166)
+  {  // setup_diffusion_velocity (diffusion_velocity.f90:15-41)
     Records r(c + "diffusion.in");
     r.skip(); r.real(); r.skip();
     sigma.resize(Nsp); eps.resize(Nsp);
@@ -262,7 +262,7 @@ void rc_case::read_inputs() {
     }
   }
   auto inlet = [&](const char* f, std::vector<double>& Y, double& T, double& p, double& m) {
-    Records r(c + f);  // oxidizer.f90:327-355, fuel.f90:396-424
+    Records r(c + f);  // oxidizer.f90:13-41, fuel.f90:13-41
     r.skip();
     Y.resize(Nsp);
     for (int i = 0; i < Nsp; ++i) Y[i] = r.real();
@@ -313,7 +313,7 @@ void rc_case::read_inputs() {
     if (expl || right || npar != 1 || (!steady && method != 5 && method != 3))
       throw std::runtime_error(
           "the GPU path covers the steady implicit and the unsteady BDF2 / backward Euler single-partition solver");
-    if (steady) inner_loop = 1;                    // initParam.f90:220-222
+    if (steady) inner_loop = 1;                    // initParam.f90:64-66
     else dt = totaltime / (double)nstep;           // initParam.f90:72
   }
 }
@@ -411,7 +411,7 @@ void rc_case::read_mesh() {
   total_volume = s;
 }
 
-// ComputeGasParameter (thermo_property.f90:155-189), host copy.
+// ComputeGasParameter (thermo_property.f90:78-112), host copy.
 void rc_case::gas(const double* Y, double T, double& Cp, double& gama, double& R) const {
   const double t2 = T * T;
   const double b[7] = {1.0 / t2, 1.0 / T, 1.0, T, t2, T * t2, t2 * t2};
@@ -429,7 +429,7 @@ void rc_case::gas(const double* Y, double T, double& Cp, double& gama, double& R
   for (int i = 0; i < Nsp; ++i) r = r + Rsp[i] * Y[i];
   Cp = cp; R = r; gama = cp / (cp - r);
 }
-// compute_enthalpy (thermo_property.f90:191-221), host copy.
+// compute_enthalpy (thermo_property.f90:114-144), host copy.
 void rc_case::enthalpy(double T, double* h) const {
   const double t2 = T * T;
   const double e[7] = {-(1.0 / t2), rcm::log(T) / T, 1.0, T / 2.0, t2 / 3.0, (T * t2) / 4.0, (t2 * t2) / 5.0};
@@ -445,7 +445,7 @@ void rc_case::enthalpy(double T, double* h) const {
 
 // initialization (initialization.f90:17-35 + 156-201) and Read_Backup
 // (output.f90:276-338) followed by primitve_to_conserved_variables
-// (update_flow_variables.f90:158-192).  The reference fills hard-coded
+// (update_flow_variables.f90:50-84).  The reference fills hard-coded
 // combustor zones first (:70-146), which the backup then overwrites; those
 // zones assume four species and are left out.
 void rc_case::initialise() {
@@ -493,8 +493,8 @@ void rc_case::initialise() {
   }
 }
 
-// compute_reconstruction_matrix (reconstruction_initialization.f90:1-327) with
-// construct_ghostcells (ghostcell.f90:19-195).  The LAPACK pseudo-inverse
+// compute_reconstruction_matrix (reconstruction_initialization.f90:1-167) with
+// construct_ghostcells (ghostcell.f90:19-181).  The LAPACK pseudo-inverse
 // (la_math.f90:1-62) of the full-rank kface x 2 matrix is taken in closed
 // form, (A^T A)^-1 A^T.
 void rc_case::stencils() {
@@ -751,11 +751,11 @@ std::string ltrim(const std::string& s) {
 }
 }  // namespace
 
-// output_vtk (output.f90:4-227): legacy ASCII VTK of the cell-centred rho, u,
+// output_vtk (output.f90:5-227): legacy ASCII VTK of the cell-centred rho, u,
 // v, p, T, Ma, Y_1..Y_Nsp and the production rates of the transported species
 // (compute_production_rate, chemical_kinetics.f90:109-165, at the state; the
 // reference writes its module copy from the last sourceterm).  Values below
-// 1e-15 are written as 0 as in the reference (:52-56).
+// 1e-15 are written as 0 as in the reference (output.f90:51-54).
 int rc_case_write_vtk(rc_case* c, const char* path) {
   if (!c || !path) return RC_ERR_ARG;
   const int NE = c->NE, Nsp = c->Nsp, NVar = c->NVar;

@@ -54,7 +54,7 @@ struct ThermoDev {
 __device__ __forceinline__ double fmin2(double a, double b) { return (b < a) ? b : a; }
 __device__ __forceinline__ double fmax2(double a, double b) { return (b > a) ? b : a; }
 
-// ComputeGasParameter (thermo_property.f90:155-189)
+// ComputeGasParameter (thermo_property.f90:78-112)
 template <int NSP>
 __device__ __forceinline__ void gas(const ThermoDev<NSP>& th, const double* Y, double tem, double& Cp,
                                     double& gama, double& Rcpcv, unsigned& err) {
@@ -80,7 +80,7 @@ __device__ __forceinline__ void gas(const ThermoDev<NSP>& th, const double* Y, d
   gama = c / (c - r);
 }
 
-// compute_enthalpy (thermo_property.f90:191-221)
+// compute_enthalpy (thermo_property.f90:114-144)
 template <int NSP>
 __device__ __forceinline__ void enthalpy(const ThermoDev<NSP>& th, double tem, double* entha, unsigned& err) {
   const double t2 = tem * tem;
@@ -96,7 +96,7 @@ __device__ __forceinline__ void enthalpy(const ThermoDev<NSP>& th, double tem, d
   }
 }
 
-// Newton_temperature (thermo_property.f90:223-257); returns T, sets Rcpcv.
+// Newton_temperature (thermo_property.f90:146-180); returns T, sets Rcpcv.
 template <int NSP>
 __device__ __forceinline__ double newton_T(const ThermoDev<NSP>& th, double et, const double* Y, double t0,
                                            double& Rcpcv, unsigned& err) {
@@ -169,7 +169,7 @@ __device__ __forceinline__ void transport(const ThermoDev<NSP>& th, double tem2,
   akmu = 0.5 * (s1 + 1.0 / s2);
 }
 
-// compute_diffusion_velocity (diffusion_velocity.f90:180-243).  D_ij is
+// compute_diffusion_velocity (diffusion_velocity.f90:55-118).  D_ij is
 // symmetric bit for bit (every pair term is), so each pair is evaluated once;
 // the diagonal D_ii is never used.
 template <int NSP>

@@ -11,9 +11,9 @@ line.  They fix both sides of the parity tests to committed numbers:
 
 Cases (all 24 x 6 cells along x/y, 288 triangles):
   t1   inviscid perfect gas (NVar 4), 50 steady LU-SGS iterations
-       (lu_sgs_stage, src/Time_LUSGS_steady.f90:74-100);
+       (lu_sgs_stage, src/Time_LUSGS_steady.f90:4-30);
   t2   reacting viscous, 4 species (NVar 7), 50 steady iterations;
-  t2u  t2 under the shipped dual-time BDF2 scheme (src/Time_BDF2.f90:4-71,
+  t2u  t2 under the shipped dual-time BDF2 scheme (src/Time_BDF2.f90:4-69,
        driver src/fvm2d.f90:80-99), 3 physical steps.
 
 Each <case>.npz holds PA, WA and hWA (the oracle's arrays, [cell, var]),

@@ -1,7 +1,7 @@
 """The unsteady dual-time BDF2 and backward Euler schemes on the CPU oracle (no GPU).
 
 The reference solves each cell's system of its BDF2 sweeps with LAPACK's
-dgesvx (advanced_linear_solve_lapack, la_math.f90:120-215).  The oracle
+dgesvx (advanced_linear_solve_lapack, la_math.f90:120-213).  The oracle
 restates dgesvx; that restatement is pinned here against SciPy's LAPACK on
 badly scaled random systems and on the BDF2 cell matrices themselves, then
 the scheme is checked by its own properties: serial (reference loop order)

@@ -1,6 +1,6 @@
 """GPU parity of the unsteady dual-time BDF2 and backward Euler stages with the CPU oracle (needs a GB300).
 
-BDF2_LU_SGS (Time_BDF2.f90:73-337) keeps the reference's operation order on
+BDF2_LU_SGS (Time_BDF2.f90:71-337) keeps the reference's operation order on
 the device, including the per-cell dgesvx steps (equilibration, LU with
 partial pivoting, the triangular solves and dgerfs's refinement), with FMA
 contraction off; the results are expected to be bit-identical to the

@@ -315,7 +315,7 @@ def test_forced_level_wait_timeout_is_reported(case_root, monkeypatch):
 
 def test_out_of_range_temperature_is_reported(case_t1):
     """T beyond the thermo fit in one cell stops at the next synchronising call
-    (ComputeGasParameter, thermo_property.f90:174-177)."""
+    (ComputeGasParameter, thermo_property.f90:97-101)."""
     c = rc.Case(case_t1)
     s = rc.Solver(c)
     PA = c.array("PA").copy()

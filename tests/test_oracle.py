@@ -20,7 +20,7 @@ def test_invariants_of_setup(case_t1):
     o = oracle.Oracle(case_t1)
     vol = o.array("VOL")
     assert (vol > 0).all()
-    assert np.abs(o.array("XYH")).sum(axis=1).max() < 1e-8            # reconstruction_initialization.f90:241
+    assert np.abs(o.array("XYH")).sum(axis=1).max() < 1e-8            # reconstruction_initialization.f90:83-86
     # every cell: neighbours + ghosts = faces (ghostcell.f90:163)
     assert (o.array("Neigh") + o.array("Num_ghostcell") == o.array("KFace")).all()
     # polygonal area of the nozzle section
