@@ -272,20 +272,31 @@ def main():
                     help="chemical source: the reference's explicit rate or the per-cell integrator")
     ap.add_argument("--no-batch", action="store_true",
                     help="skip the batched form (64 uneven reacting cases in one context)")
-    ap.add_argument("--batch-cases", type=int, default=64)
+    ap.add_argument("--batch-cases", type=int, default=None,
+                    help="cases of the batched form (64 for the throughput line, 16 for --converge)")
     ap.add_argument("--no-surrogate", action="store_true",
                     help="skip the surrogate form (network trained here on integrator pairs)")
-    ap.add_argument("--sur-samples", type=int, default=10_000_000)
-    ap.add_argument("--sur-steps", type=int, default=8000)
+    ap.add_argument("--sur-samples", type=int, default=None,
+                    help="integrator pairs for the surrogate (10M for the throughput line, 2M for --converge)")
+    ap.add_argument("--sur-steps", type=int, default=None,
+                    help="training steps of the surrogate (8000 for the throughput line, 4000 for --converge)")
     ap.add_argument("--no-bdf2", action="store_true",
                     help="skip the unsteady form (dual-time BDF2, the reference's shipped time scheme)")
     ap.add_argument("--bdf2-steps", type=int, default=10)
-    ap.add_argument("--converge", type=int, default=0,
-                    help="instead of the throughput line: N iterations per form with the residual history, "
-                         "iterations and wall time to each residual level")
+    ap.add_argument("--converge", action="store_true",
+                    help="instead of the throughput line: wall time to the steady state (--tol) of the plain FP64 "
+                         "path and each form on a steady-state preset (default s2), errors against the FP64 "
+                         "converged state, and the oracle to the same criterion")
+    ap.add_argument("--tol", type=float, default=1e-8)
+    ap.add_argument("--max-iters", type=int, default=40000)
     ap.add_argument("--every", type=int, default=10)
+    ap.add_argument("--dc-window", type=int, default=20,
+                    help="norm reads without a 1%% improvement before the mixed form switches to defect correction")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
+    for k, thr, conv in (("batch_cases", 64, 16), ("sur_samples", 10_000_000, 2_000_000), ("sur_steps", 8000, 4000)):
+        if getattr(args, k) is None:
+            setattr(args, k, conv if args.converge else thr)
 
     rank = int(os.environ.get("RANK", "0"))
     world = int(os.environ.get("WORLD_SIZE", "1"))
@@ -567,79 +578,168 @@ def batched_surrogate(args, stream, flush, torch, rc, cs, ref_state, net):
     return out
 
 
-LEVELS = (1e-1, 5e-2, 3e-2, 1e-2, 1e-3, 1e-8)
+def rel_err(st, ref) -> dict:
+    """Relative L-infinity difference per field (p, T, Y_k) of a state against
+    a reference state, each field relative to the reference field's maximum."""
+    den = np.maximum(np.abs(ref).max(axis=0), 1e-300)
+    e = np.abs(st - ref).max(axis=0) / den
+    return {"p": float(e[0]), "T": float(e[3]), "Y": [float(x) for x in e[4:]]}
 
 
-def reach(hist, every, levels=LEVELS):
-    """Iteration at which max_k Res_k / Res_k(first check) first falls to each level."""
-    r0 = np.where(hist[0, :-1] > 0, hist[0, :-1], 1.0)
-    rel = np.where(hist[0, :-1] > 0, hist[:, :-1] / r0, 0.0).max(axis=1)
-    out = {}
-    for lv in levels:
-        hit = np.nonzero(rel <= lv)[0]
-        out[f"{lv:g}"] = int((hit[0] + 1) * every) if hit.size else None
-    return out, float(rel.min()), float(rel[-1])
+def steady_run(s, args, dc_window=0):
+    """run_to_steady with wall time (set-up excluded: the solver exists and its
+    state is set; the timed loop includes the graph launches and the host reads
+    of the norms)."""
+    s.sync()
+    t0 = time.perf_counter()
+    r = s.run_to_steady(args.tol, args.max_iters, args.every, dc_window=dc_window)
+    wall = time.perf_counter() - t0
+    reached = r["reached"]
+    out = {"iterations": r["iterations"], "wall_s": wall,
+           "reached_tol_at": reached[0] if len(reached) == 1 else reached,
+           "final_level": float(np.max(r["levels"])),
+           "lowest_level": float(min(float(np.max(lv)) for _, lv in r["history"])),
+           "ms_per_iteration": 1e3 * wall / r["iterations"]}
+    if dc_window:
+        out["switched_to_dc_at"] = r["switched_at"]
+    return out, r
 
 
 def converge(args, rc, torch):
-    """Residual histories of the forms on the same case: iterations and wall
-    time to each level of max_k Res_k/Res_k(first), the lowest level reached
-    (the reference's Barth limiter stalls the steady residual), and the final
-    state against the FP64 one."""
-    out = {"mode": "converge", "iterations": args.converge, "every": args.every, "levels": list(LEVELS)}
+    """Wall time to the steady state, max_k Res_k(n)/Res_k(1) <= tol (the
+    step_residual columns), for the plain FP64 path and each form, with each
+    form's final state against the FP64 converged state, and the oracle's
+    time to the same criterion on all host threads."""
+    out = {"mode": "converge", "metric": "wall time to steady", "tol": args.tol, "every": args.every,
+           "criterion": "max_k Res_k(n)/Res_k(1) <= tol, Res_k = sum(vol*|dU_k|)/V_tot after LU-SGS "
+                        "(the step_residual columns), Res_k(1) after the first iteration"}
+    case_name = args.case if args.case not in ("c4", "c2") else "s2"
     with tempfile.TemporaryDirectory() as tmp:
-        d, cfg = make_workload(args.case, tmp, **case_overrides(args))
-        out["config"] = workload_config(cfg, 0, 0, par_label(1))
-        finals = {}
-        for form in ("fp64", "mixed", "mixed_dc"):
-            case = rc.Case(d)
-            t0 = time.perf_counter()
-            sw = None
-            if form == "mixed_dc":
-                hist, sw = case.run_steady_dc(args.converge, args.every, window=5)
-            else:
-                hist = case.run_steady(args.converge, args.every,
-                                       rc.RC_PREC_FP64 if form == "fp64" else rc.RC_PREC_MIXED)
-            wall = time.perf_counter() - t0
-            lv, best, last = reach(hist, args.every)
-            per_it = wall / args.converge
-            finals[form] = case.array("PA").copy()
-            out[form] = {"wall_s": wall, "iterations_to": lv,
-                         "seconds_to": {k: (v * per_it if v else None) for k, v in lv.items()},
-                         "lowest_level": best, "final_level": last}
-            if sw is not None:
-                out[form]["switched_to_dc_at"] = sw
-            case.close()
-        ref = finals["fp64"]
-        den = np.maximum(np.abs(ref).max(axis=0), 1e-300)
-        for form in ("mixed", "mixed_dc"):
-            e = np.abs(finals[form] - ref).max(axis=0) / den
-            out[form]["final_rel_linf_vs_fp64"] = {"p": float(e[0]), "T": float(e[3]),
-                                                  "Y": [float(x) for x in e[4:]]}
+        d, cfg = make_workload(case_name, tmp, **case_overrides(args))
+        case = rc.Case(d)
+        out["config"] = workload_config(cfg, case.NE, case.NF, par_label(1))
+        forms = {}
+        # plain FP64 (the reference's operation order, explicit chemical source)
+        s = rc.Solver(case)
+        f, r64 = steady_run(s, args)
+        P64 = s.get_state()[0]
+        it64 = r64["iterations"]
+        s.close()
+        forms["fp64"] = f
+        # mixed precision alone: FP32 residual, stalls at its rounding level
+        s = rc.Solver(case, precision=rc.RC_PREC_MIXED)
+        a2 = argparse.Namespace(**{**vars(args), "max_iters": it64})
+        f, _ = steady_run(s, a2)
+        f["rel_linf_vs_fp64_converged"] = rel_err(s.get_state()[0], P64)
+        s.close()
+        forms["mixed"] = f
+        # mixed precision switching to defect correction when it stalls
+        s = rc.Solver(case, precision=rc.RC_PREC_MIXED)
+        f, _ = steady_run(s, args, dc_window=args.dc_window)
+        f["rel_linf_vs_fp64_converged"] = rel_err(s.get_state()[0], P64)
+        s.close()
+        forms["mixed_dc"] = f
         if not args.no_batch:
-            from rocketcombustor_gb300 import cases
-            dirs = cases.make_batch(os.path.join(tmp, "batch"), args.batch_cases, 5)
-            cs = [rc.Case(x) for x in dirs]
-            b = rc.BatchSolver(cs)
-            b.set_chemistry(rc.RC_CHEM_INTEGRATED)
-            n_it = min(args.converge, 1000)
-            hists = []
+            forms["batched"] = converge_batched(args, rc, tmp)
+        if not args.no_surrogate and cfg.combustion and cfg.nsp == 4:
+            forms["surrogate"] = converge_surrogate(args, rc, torch, case)
+        out["forms"] = forms
+        if not args.no_cpu:
+            import oracle
+            th = oracle.Oracle.max_threads()
+            o = oracle.Oracle(d, threads=th)
             t0 = time.perf_counter()
-            for it in range(1, n_it + 1):
-                b.lu_sgs_stage(it)
-                if it % args.every == 0:
-                    hists.append(np.concatenate([b.residual()[0], np.zeros((len(cs), 1))], axis=1))
+            h = o.run(it64, history=True)
             wall = time.perf_counter() - t0
-            H = np.stack(hists, axis=1)  # case, check, V+1
-            per = []
-            for k in range(len(cs)):
-                lv, best, _ = reach(H[k], args.every, (1e-1, 5e-2))
-                per.append({"cells": cs[k].NE, "iterations_to": lv, "lowest_level": best})
-            out["batched"] = {"cases": len(cs), "iterations": n_it, "wall_s": wall,
-                              "ms_per_iteration": 1e3 * wall / n_it, "per_case": per,
-                              "reached_1e-1": sum(1 for p in per if p["iterations_to"]["0.1"])}
+            res = h[:, :-1]
+            m = res[0] > 0
+            lv = np.where(m, res / np.where(m, res[0], 1.0), 0.0).max(axis=1)
+            hit = np.nonzero(lv <= args.tol)[0]
+            out["cpu_baseline"] = {"kind": "port", "cores": th, "iterations": it64, "wall_s": wall,
+                                   "reached_tol_at": int(hit[0] + 1) if hit.size else None,
+                                   "final_level": float(lv[-1]),
+                                   "state_equals_gpu_fp64": bool(np.array_equal(o.array("PA"), P64)),
+                                   "sample": f"the oracle's {it64} iterations (as many as the FP64 GPU run took)"}
+            o.close()
+        case.close()
     print(json.dumps(out), flush=True)
     return 0
+
+
+def converge_batched(args, rc, tmp):
+    """The batched form to steady: `--batch-cases` uneven cases of the steady
+    spread (500-5000 cells each) in one context, FP64 and mixed with the
+    defect-correction switch; each case's iteration to tol, and the mixed
+    batch's states against the FP64 batch's."""
+    from rocketcombustor_gb300 import cases
+    cfgs = cases.steady_batch_configs(args.batch_cases)
+    dirs = []
+    for c in cfgs:
+        dd = os.path.join(tmp, "steady_batch", c.name)
+        cases.write_case(dd, c)
+        dirs.append(dd)
+    cs = [rc.Case(x) for x in dirs]
+    res = {"cases": len(cs), "cells": int(sum(c.NE for c in cs)),
+           "cells_per_case": [int(c.NE) for c in cs]}
+    b = rc.BatchSolver(cs)
+    f, _ = steady_run(b, args)
+    ref = b.get_state()[0]
+    b.close()
+    res["fp64"] = f
+    b = rc.BatchSolver(cs, precision=rc.RC_PREC_MIXED)
+    f, _ = steady_run(b, args, dc_window=args.dc_window)
+    st = b.get_state()[0]
+    off = b.offsets
+    f["rel_linf_vs_fp64_converged"] = [rel_err(st[off[k]:off[k + 1]], ref[off[k]:off[k + 1]])
+                                       for k in range(len(cs))]
+    b.close()
+    res["mixed_dc"] = f
+    for c in cs:
+        c.close()
+    return res
+
+
+def converge_surrogate(args, rc, torch, case):
+    """The surrogate form to steady on the same case: the network trained here
+    on integrator pairs from this case's states, then the steady runs with the
+    integrated source (FP64) and with the surrogate source (FP64, cells the
+    error indicator rejects sent to the integrator), and the surrogate's
+    converged state against the integrated one."""
+    from rocketcombustor_gb300 import surrogate
+    s = rc.Solver(case)
+    s.set_chemistry(rc.RC_CHEM_INTEGRATED)
+    t0 = time.perf_counter()
+    pool = surrogate.collect_pool(s, iters=200, every=20)
+    x, t, nsub = surrogate.build_dataset(s, pool, args.sur_samples, seed=7)
+    torch.cuda.synchronize()
+    t_data = time.perf_counter() - t0
+    s.close()
+    ntr = x.shape[0] - min(1 << 18, x.shape[0] // 10)
+    net = surrogate.MLP(seed=7)
+    net.fit_norm(x[:ntr])
+    t0 = time.perf_counter()
+    net.train(x[:ntr], t[:ntr], steps=args.sur_steps, batch=8192, lr=2e-3, lr_end=3e-5)
+    torch.cuda.synchronize()
+    t_train = time.perf_counter() - t0
+    out = {"training": {"samples": int(x.shape[0]), "data_s": t_data, "steps": args.sur_steps, "train_s": t_train,
+                        "validation_vs_integrator": surrogate.validate(net, x[ntr:], t[ntr:])}}
+    s = rc.Solver(case)
+    s.set_chemistry(rc.RC_CHEM_INTEGRATED)
+    f, _ = steady_run(s, args)
+    ref = s.get_state()[0]
+    s.close()
+    out["integrated_fp64"] = f
+    s = rc.Solver(case)
+    s.set_surrogate(net)
+    s.set_chemistry(rc.RC_CHEM_SURROGATE)
+    f, _ = steady_run(s, args)
+    f["rel_linf_vs_integrated_converged"] = rel_err(s.get_state()[0], ref)
+    a, b_ = s.surrogate_stats()
+    f["cells_network"], f["cells_integrator"] = a, b_
+    s.close()
+    out["surrogate_fp64"] = f
+    net.close()
+    return out
 
 
 def surrogate_form(args, stream, flush, torch, rc, case, extra_pool=None):

@@ -440,6 +440,57 @@ class Solver:
             self.lu_sgs_stage(it)
         return self.sync()
 
+    def run_to_steady(self, tol: float = 1e-8, max_iters: int = 100000, every: int = 10, dc_window: int = 0,
+                      start: int = 1) -> dict:
+        """The steady loop (fvm2d.f90:48-76) with the stopping test the
+        reference does not have: iterate lu_sgs_stage until, for every case,
+        max_k Res_k(n) / Res_k(1) <= tol, Res_k being the step_residual
+        columns (residual.f90:61-97, sum of vol*|dU_k| over the total volume)
+        and Res_k(1) their values after the first iteration.  The norms are
+        read after the first iteration and then every `every` iterations.
+
+        dc_window > 0 (mixed precision): once the level has not fallen below
+        0.99 of its best for dc_window reads, switch to defect correction
+        (RC_PREC_MIXED_DC, the FP64 residual driving the FP32 sweeps), whose
+        fixed point is the FP64 one.
+
+        Returns {"iterations": last iteration run, "levels": per-case level at
+        the end, "reached": per-case first iteration at or below tol (None if
+        not), "history": [(iteration, per-case levels)], "switched_at":
+        iteration of the switch or 0}."""
+        res0 = mask = None
+        hist, reached = [], None
+        best, since, switched = np.inf, 0, 0
+        it = start - 1
+        for it in range(start, start + max_iters):
+            self.lu_sgs_stage(it)
+            if it != start and (it - start + 1) % every:
+                continue
+            r = np.atleast_2d(self.residual()[0])
+            if res0 is None:
+                mask = r > 0.0
+                res0 = np.where(mask, r, 1.0)
+                reached = [None] * r.shape[0]
+            lv = np.where(mask, r / res0, 0.0).max(axis=1)
+            hist.append((it, lv))
+            for k in range(lv.shape[0]):
+                if reached[k] is None and lv[k] <= tol:
+                    reached[k] = it
+            if all(x is not None for x in reached):
+                break
+            if dc_window > 0 and not switched:
+                top = float(lv.max())
+                if top < 0.99 * best:
+                    best, since = top, 0
+                else:
+                    since += 1
+                    if since >= dc_window:
+                        self.set_precision(RC_PREC_MIXED_DC)
+                        switched = it
+        self.sync()
+        return {"iterations": it - start + 1, "levels": hist[-1][1] if hist else None, "reached": reached,
+                "history": hist, "switched_at": switched}
+
     # -- unsteady dual-time BDF2
     def set_p_out(self, p_out: float):
         """Exit pressure for the following calls (compute_p_out's result)."""

@@ -82,7 +82,7 @@ def area_ratio_mach(ratio, gamma: float, supersonic):
 @dataclass
 class Mesh:
     coor: np.ndarray          # (NNT, 2) float64
-    cells: np.ndarray         # (NE, 3) int64, 1-based node ids, counter-clockwise
+    cells: np.ndarray         # (NE, 3) or (NE, 4) int64, 1-based node ids, counter-clockwise
     boundaries: List[tuple]   # [(itype, (nb,2) int64 1-based node pairs)]
     nx: int
     ny: int
@@ -99,7 +99,8 @@ class Mesh:
     def nf(self) -> int:
         """Number of distinct cell edges."""
         c = self.cells.astype(np.int64)
-        e = np.concatenate([c[:, [0, 1]], c[:, [1, 2]], c[:, [2, 0]]])
+        k = c.shape[1]
+        e = np.concatenate([c[:, [q, (q + 1) % k]] for q in range(k)])
         key = np.minimum(e[:, 0], e[:, 1]) * (self.nnt + 1) + np.maximum(e[:, 0], e[:, 1])
         return int(np.unique(key).shape[0])
 
@@ -129,8 +130,10 @@ def _color_order(cells: np.ndarray, nnt: int) -> np.ndarray:
 
 
 def nozzle_mesh(nx: int, ny: int, seed: int, order: str = "natural", wall_type: int = 6,
-                jitter: float = 0.10, h_exit: float = H_EXIT, x_exit: float = X_EXIT) -> Mesh:
-    """Seeded triangulated nozzle: (nx*ny*2) triangles, ordering per `order`."""
+                jitter: float = 0.10, h_exit: float = H_EXIT, x_exit: float = X_EXIT,
+                quads: bool = False) -> Mesh:
+    """Seeded nozzle mesh: (nx*ny*2) triangles, or with `quads` the nx*ny
+    quadrilaterals of the mapped grid; ordering per `order`."""
     rng = np.random.default_rng(seed)
     xs = np.linspace(0.0, x_exit, nx + 1)
     hx = half_height(xs, h_exit, x_exit)
@@ -151,10 +154,13 @@ def nozzle_mesh(nx: int, ny: int, seed: int, order: str = "natural", wall_type: 
     I, J = np.meshgrid(np.arange(nx), np.arange(ny), indexing="ij")
     I, J = I.ravel(), J.ravel()
     a, b, c, d = nid(I, J), nid(I + 1, J), nid(I + 1, J + 1), nid(I, J + 1)
-    diag_ac = ((I + J) % 2) == 0
-    t1 = np.where(diag_ac[:, None], np.stack([a, b, c], 1), np.stack([a, b, d], 1))
-    t2 = np.where(diag_ac[:, None], np.stack([a, c, d], 1), np.stack([b, c, d], 1))
-    cells = np.stack([t1, t2], axis=1).reshape(-1, 3).astype(np.int64)
+    if quads:
+        cells = np.stack([a, b, c, d], 1).astype(np.int64)
+    else:
+        diag_ac = ((I + J) % 2) == 0
+        t1 = np.where(diag_ac[:, None], np.stack([a, b, c], 1), np.stack([a, b, d], 1))
+        t2 = np.where(diag_ac[:, None], np.stack([a, c, d], 1), np.stack([b, c, d], 1))
+        cells = np.stack([t1, t2], axis=1).reshape(-1, 3).astype(np.int64)
     if order == "natural":
         pass
     elif order == "colored":
@@ -192,7 +198,7 @@ def write_grid(path: str, mesh: Mesh) -> None:
     ne, nnt, nf = mesh.ne, mesh.nnt, mesh.nf
     with open(path, "w") as f:
         f.write(f"{ne} {ne} {nnt} {nnt} {nf} {nf}\n")
-        cells = np.concatenate([np.full((ne, 1), 3, dtype=np.int64), mesh.cells], axis=1)
+        cells = np.concatenate([np.full((ne, 1), mesh.cells.shape[1], dtype=np.int64), mesh.cells], axis=1)
         _write_rows(f, cells, "%d")
         cz = np.concatenate([mesh.coor, np.zeros((nnt, 2))], axis=1)
         _write_rows(f, cz, ["%.17g", "%.17g", "%d", "%d"])
@@ -382,10 +388,16 @@ class CaseConfig:
     a_p: float = 0.0           # exit-pressure oscillation amplitude (fraction of p_static)
     f_p: float = 5000.0        # and frequency (Hz)
     time_method: int = 5       # implicit_time_method: 5 BDF2, 3 backward Euler
+    # subsonic nozzle: the throat Mach number of a nozzle flow that stays
+    # subsonic (inlet mass flux, initial field and exit pressure from the
+    # subsonic isentropic branch through the throat at this Mach number);
+    # 0 = the choked design (sonic throat, supersonic divergent section)
+    throat_mach: float = 0.0
+    quads: bool = False        # quadrilateral cells of the mapped grid instead of its triangles
 
     @property
     def n_cells(self) -> int:
-        return 2 * self.nx * self.ny
+        return (1 if self.quads else 2) * self.nx * self.ny
 
 
 PRESETS: Dict[str, CaseConfig] = {
@@ -407,6 +419,16 @@ PRESETS: Dict[str, CaseConfig] = {
     "t2u": CaseConfig("t2u", nx=24, ny=6, seed=12, nsp=4, viscous=True, combustion=True,
                       p0=5.0e6, T0=3500.0, perturb=0.02, init="isentropic", unsteady=True, cfl=10.0,
                       totaltime=5.0e-3, nstep=500000, inner_loop=10, rel_tol=1.0e-3),
+    # steady-state cases: the reacting viscous nozzle on quadrilaterals with a
+    # 1500 K chamber (same mechanism, 99 % burnt inlet).  On triangles the
+    # reference's face-neighbour least-squares reconstruction makes entropy
+    # modes grow (the Barth limiter then holds the residual in a limit cycle)
+    # and the explicit rate at 3500 K with O2 nearly used up cycles at the
+    # Y = 0 clip; these converge to 1e-8 and below
+    "s2": CaseConfig("s2", nx=120, ny=24, seed=21, nsp=4, viscous=True, combustion=True,
+                     p0=5.0e6, T0=1500.0, perturb=0.02, init="isentropic", quads=True, nstep=12000),
+    "s2t": CaseConfig("s2t", nx=60, ny=12, seed=22, nsp=4, viscous=True, combustion=True,
+                      p0=5.0e6, T0=1500.0, perturb=0.02, init="isentropic", quads=True, nstep=8000),
     "c2u": CaseConfig("c2u", nx=600, ny=100, seed=2, nsp=4, viscous=True, combustion=True,
                       p0=5.0e6, T0=3500.0, perturb=0.02, init="isentropic", unsteady=True, cfl=10.0,
                       totaltime=5.0e-3, nstep=500000, inner_loop=10, rel_tol=1.0e-3),
@@ -429,10 +451,22 @@ def synthetic_cp(nsp: int, seed: int) -> np.ndarray:
     return coef
 
 
+def sonic_height(cfg: CaseConfig, gamma: float) -> float:
+    """Half-height of the isentropic flow's sonic section: the throat for the
+    choked design, below it (A* = A_throat / (A/A*)(M_throat)) for a subsonic
+    nozzle."""
+    if cfg.throat_mach <= 0.0:
+        return H_THROAT
+    m = cfg.throat_mach
+    g1 = (gamma + 1.0) / (2.0 * (gamma - 1.0))
+    ar = (1.0 / m) * ((2.0 / (gamma + 1.0)) * (1.0 + 0.5 * (gamma - 1.0) * m * m)) ** g1
+    return H_THROAT / ar
+
+
 def inlet_state(cfg: CaseConfig, R: float, gamma: float):
     """Static inlet state of the subsonic chamber for total (p0, T0) at the
-    chamber-to-throat area ratio: returns (p, T, u, mass flux)."""
-    M = area_ratio_mach(H_CHAMBER / H_THROAT, gamma, supersonic=False)
+    chamber-to-sonic area ratio: returns (p, T, u, mass flux)."""
+    M = area_ratio_mach(H_CHAMBER / sonic_height(cfg, gamma), gamma, supersonic=False)
     T = cfg.T0 / (1.0 + 0.5 * (gamma - 1.0) * M * M)
     p = cfg.p0 * (T / cfg.T0) ** (gamma / (gamma - 1.0))
     rho = p / (R * T)
@@ -452,7 +486,7 @@ def write_case(d: str, cfg: CaseConfig, mesh: Optional[Mesh] = None) -> Mesh:
     if mesh is None:
         wall = cfg.wall or (1 if cfg.viscous else 6)
         mesh = nozzle_mesh(cfg.nx, cfg.ny, cfg.seed, cfg.order, wall_type=wall, jitter=cfg.jitter,
-                           h_exit=cfg.h_exit, x_exit=cfg.x_exit)
+                           h_exit=cfg.h_exit, x_exit=cfg.x_exit, quads=cfg.quads)
     if cfg.closed:
         wall = cfg.wall or (1 if cfg.viscous else 6)
         mesh.boundaries = [(wall, pairs) for _, pairs in mesh.boundaries]
@@ -495,7 +529,11 @@ def write_case(d: str, cfg: CaseConfig, mesh: Optional[Mesh] = None) -> Mesh:
     write_inlet(os.path.join(d, "combustion", "oxidizer.in"), Yin, T_in, cfg.p0,
                 mflux * 2.0 * H_CHAMBER, "oxidizer")
     write_inlet(os.path.join(d, "combustion", "fuel.in"), Yin, T_in, cfg.p0, 0.37, "fuel")
-    pr = exit_pressure_ratio(gamma, cfg.h_exit) * cfg.p_out_factor
+    if cfg.throat_mach > 0.0:
+        m_e = area_ratio_mach(cfg.h_exit / sonic_height(cfg, gamma), gamma, supersonic=False)
+        pr = (1.0 + 0.5 * (gamma - 1.0) * m_e * m_e) ** (-gamma / (gamma - 1.0)) * cfg.p_out_factor
+    else:
+        pr = exit_pressure_ratio(gamma, cfg.h_exit) * cfg.p_out_factor
     write_flow_info(d, cfg.combustion, cfg.viscous, cfg.cfl, cfg.nstep, cfg.limit_id, pr, cfg.unsteady,
                     cfg.totaltime, cfg.inner_loop, cfg.rel_tol, cfg.a_p, cfg.f_p, cfg.time_method)
     # initial field: uniform inlet (chamber) state, or the quasi-1D isentropic
@@ -510,7 +548,9 @@ def write_case(d: str, cfg: CaseConfig, mesh: Optional[Mesh] = None) -> Mesh:
         h = half_height(x, cfg.h_exit, cfg.x_exit)
         eps = 1e-6
         dh = (half_height(x + eps, cfg.h_exit, cfg.x_exit) - half_height(x - eps, cfg.h_exit, cfg.x_exit)) / (2 * eps)
-        M = area_ratio_mach(np.maximum(h / H_THROAT, 1.0 + 1e-9), gamma, supersonic=(x > X_THROAT))
+        hs = sonic_height(cfg, gamma)
+        M = area_ratio_mach(np.maximum(h / hs, 1.0 + 1e-9), gamma,
+                            supersonic=(x > X_THROAT) & (cfg.throat_mach <= 0.0))
         T = cfg.T0 / (1.0 + 0.5 * (gamma - 1.0) * M * M)
         p = cfg.p0 * (T / cfg.T0) ** (gamma / (gamma - 1.0))
         q = M * np.sqrt(gamma * Rmix * T)
@@ -541,8 +581,15 @@ def make_case(d: str, name: str, **over) -> CaseConfig:
     return cfg
 
 
+def _area_ratio(u: float, lo: float, hi: float) -> float:
+    """A draw u from [4, 25] mapped onto [lo, hi] (u itself for the default range)."""
+    if (lo, hi) == (4.0, 25.0):
+        return u
+    return lo + (u - 4.0) / 21.0 * (hi - lo)
+
+
 def batch_configs(n: int = 64, seed: int = 5, ne_min: int = 2000, ne_max: int = 60000,
-                  **over) -> List[CaseConfig]:
+                  ar_min: float = 4.0, ar_max: float = 25.0, **over) -> List[CaseConfig]:
     """n independent reacting viscous nozzle cases of uneven size (the batched
     workload): cells log-uniform in [ne_min, ne_max] (nx = 6 ny), chamber
     pressure uniform in 1-10 MPa, O/F uniform in 4-8 and area ratio uniform in
@@ -551,17 +598,27 @@ def batch_configs(n: int = 64, seed: int = 5, ne_min: int = 2000, ne_max: int = 
     physics of preset c2 otherwise."""
     rng = np.random.default_rng(seed)
     base = asdict(PRESETS["c2"])
+    per_quad = 1 if over.get("quads") else 2  # cells per quadrilateral of the mapped grid
     out = []
     for c in range(n):
         ne = math.exp(rng.uniform(math.log(ne_min), math.log(ne_max)))
-        ny = max(4, int(round(math.sqrt(ne / 12.0))))
+        ny = max(4, int(round(math.sqrt(ne / (6.0 * per_quad)))))
         cfg = {**base, "name": f"b{c:02d}", "nx": 6 * ny, "ny": ny, "seed": seed * 1000 + c,
                "p0": float(rng.uniform(1.0e6, 1.0e7)), "of_ratio": float(rng.uniform(4.0, 8.0)),
-               "h_exit": float(rng.uniform(4.0, 25.0)) * H_THROAT, "perturb_seed": seed * 1000 + 500 + c}
+               "h_exit": _area_ratio(float(rng.uniform(4.0, 25.0)), ar_min, ar_max) * H_THROAT,
+               "perturb_seed": seed * 1000 + 500 + c}
         cfg["x_exit"] = X_THROAT + (X_EXIT - X_THROAT) * (cfg["h_exit"] - H_THROAT) / (H_EXIT - H_THROAT)
         cfg.update(over)
         out.append(CaseConfig(**cfg))
     return out
+
+
+def steady_batch_configs(n: int = 16, seed: int = 8) -> List[CaseConfig]:
+    """The batched steady-state workload: n cases of the batch_configs spread
+    (1-10 MPa, O/F 4-8) with area ratios 4-12 at 500-5000 cells each, on
+    quadrilaterals with the 1500 K chamber of preset s2."""
+    return batch_configs(n, seed, ne_min=500, ne_max=5000, ar_min=4.0, ar_max=12.0, quads=True, T0=1500.0,
+                         nstep=12000)
 
 
 def make_batch(d: str, n: int = 64, seed: int = 5, **over) -> List[str]:

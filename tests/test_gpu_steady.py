@@ -1,0 +1,98 @@
+"""The converged steady state (needs a GB300).
+
+The steady criterion is max_k Res_k(n)/Res_k(1) <= 1e-8 over the
+step_residual columns (residual.f90:61-97).  The 720-cell reacting viscous
+nozzle on quadrilaterals (preset s2t) reaches it; the plain FP64 path must
+then match the oracle to 1e-9 relative L-infinity per field (it matches bit
+for bit), defect correction must land within 1e-6 of the FP64 converged
+state on p, T and Y_k, and every case of a batch must converge as it does
+alone.
+"""
+import numpy as np
+import pytest
+
+import oracle
+import rocketcombustor_gb300 as rc
+from conftest import make_case
+
+pytestmark = pytest.mark.gpu
+
+TOL = 1e-8
+FORM_TOL = 1e-6   # a form's state against the FP64 converged state, per field
+
+
+def rel_linf(a, b):
+    den = np.maximum(np.abs(b).max(axis=0), 1e-300)
+    return np.abs(a - b).max(axis=0) / den
+
+
+def level(hist):
+    r = hist[:, :-1]
+    m = r[0] > 0
+    return np.where(m, r / np.where(m, r[0], 1.0), 0.0).max(axis=1)
+
+
+def test_fp64_steady_state_matches_oracle(case_root):
+    d = make_case(case_root, "s2t")
+    c = rc.Case(d)
+    s = rc.Solver(c)
+    r = s.run_to_steady(TOL, max_iters=20000, every=10)
+    n = r["iterations"]
+    assert r["reached"][0] is not None and r["reached"][0] == n, r["levels"]
+    PA, WA = s.get_state()
+    o = oracle.Oracle(d, threads=oracle.Oracle.max_threads())
+    lv = level(o.run(n, history=True))
+    assert lv[-1] <= TOL and lv[n - 11] > TOL  # the oracle crosses on the same 10-iteration read
+    assert rel_linf(PA, o.array("PA")).max() <= 1e-9
+    assert np.array_equal(PA, o.array("PA")) and np.array_equal(WA, o.array("WA"))
+    s.close()
+
+
+def test_defect_correction_reaches_the_fp64_fixed_point(case_root):
+    d = make_case(case_root, "s2t")
+    c = rc.Case(d)
+    s = rc.Solver(c)
+    r64 = s.run_to_steady(TOL, max_iters=20000, every=10)
+    P64 = s.get_state()[0]
+    s.close()
+    m = rc.Solver(c, precision=rc.RC_PREC_MIXED)
+    r = m.run_to_steady(TOL, max_iters=40000, every=10, dc_window=20)
+    assert r["reached"][0] is not None, r["levels"]
+    assert r["switched_at"] > 0
+    e = rel_linf(m.get_state()[0], P64)
+    assert e[0] <= FORM_TOL and e[3] <= FORM_TOL and e[4:].max() <= FORM_TOL, (e, r64["iterations"], r["iterations"])
+    m.close()
+
+
+def test_mixed_alone_stalls_above_the_fp64_level(case_root):
+    """The FP32 residual alone cannot reach 1e-8 on this case: its level stops
+    at the rounding of the FP32 flux (the reason for defect correction)."""
+    d = make_case(case_root, "s2t")
+    c = rc.Case(d)
+    m = rc.Solver(c, precision=rc.RC_PREC_MIXED)
+    r = m.run_to_steady(TOL, max_iters=8000, every=10)
+    assert r["reached"][0] is None and min(float(lv.max()) for _, lv in r["history"]) > TOL
+    m.close()
+
+
+def test_batched_cases_each_reach_steady_as_alone(tmp_path):
+    from rocketcombustor_gb300 import cases
+
+    cfgs = cases.steady_batch_configs(16)[:4]
+    dirs = []
+    for cfg in cfgs:
+        dd = str(tmp_path / cfg.name)
+        cases.write_case(dd, cfg)
+        dirs.append(dd)
+    cs = [rc.Case(x) for x in dirs]
+    b = rc.BatchSolver(cs)
+    r = b.run_to_steady(TOL, max_iters=30000, every=10)
+    assert all(x is not None for x in r["reached"]), r["levels"]
+    n = r["iterations"]
+    st = b.get_state()[0]
+    for k, c in enumerate(cs):
+        s = rc.Solver(c)
+        s.run(n)
+        assert np.array_equal(st[b.case_slice(k)], s.get_state()[0]), k
+        s.close()
+    b.close()
