@@ -53,15 +53,18 @@ def algo_bytes_per_cell(V: int, nf_ne: float, viscous: bool, combustion: bool) -
     return b
 
 
-# DRAM bytes per cell of one launch of the dominant kernel of each subroutine
-# (dram__bytes_read.sum + dram__bytes_write.sum over the 30,000 cells of the
-# capture in profiles/kernels_c2_30k_full.md; the traffic grows with the cells)
-# DRAM bytes per cell of one FP64 iteration of the 120,000-cell nozzle (ncu,
-# --cache-control none: the caches as the live run leaves them; profiles/)
-NCU_DRAM_PER_CELL = {"lu_sgs_steady": (25643776 + 13218816 + 6815488 + 3588096) / 120000,
-                     "flux_sourceterm": (22433024 + 25496320 + 2027776 + 6353152) / 120000}
-NCU_TRAFFIC_SOURCE = ("ncu capture of one iteration at 120,000 cells with the dataflow LU-SGS, caches as in the "
-                      "live run (profiles/c2_fp64_flow_launches.md), scaled by cells")
+# DRAM bytes and FP64-pipe warp instructions per cell of each subroutine's
+# kernels in one FP64 iteration of the reacting viscous nozzle at 500,000 cells
+# (a working set above the 129 MB L2; ncu dram__bytes_read.sum +
+# dram__bytes_write.sum and sm__inst_executed_pipe_fp64.sum over the
+# subroutine's launches, divided by the cells: profiles/c4_500k_fp64_counters.md).
+# Both grow with the cells.
+NCU_DRAM_PER_CELL = {"timestep": 198.05, "reconstruction": 334.50, "flux_sourceterm": 672.79,
+                     "lu_sgs_steady": 651.65}
+NCU_FP64_INST_PER_CELL = {"timestep": 46.713, "reconstruction": 46.004, "flux_sourceterm": 128.919,
+                          "lu_sgs_steady": 74.476}
+NCU_TRAFFIC_SOURCE = ("ncu capture of one FP64 iteration of the same physics at 500,000 cells (dataflow LU-SGS; "
+                      "profiles/c4_500k_fp64_counters.md), scaled by cells")
 
 
 def read_peaks():
@@ -71,13 +74,6 @@ def read_peaks():
             d = json.load(f)
         return float(d["hbm_gbs"]), "measured"
     return 6800.0, "fallback"
-
-
-# FP64-pipe warp instructions per cell of each subroutine's kernels in one FP64
-# iteration of the reacting viscous nozzle (ncu sm__inst_executed_pipe_fp64.sum
-# over the launches of each subroutine, divided by the cells; the count grows
-# with the cells).  Filled from the capture in profiles/.
-NCU_FP64_INST_PER_CELL: dict = {}
 
 
 def fp64_rate(rc, stream, torch, iters: int = 4000, repeats: int = 3) -> dict:
