@@ -21,6 +21,7 @@
 // Every reduction has a fixed order, so gradients are reproducible run to run.
 #include <cuda_runtime.h>
 #include <cuda_bf16.h>
+#include <cuda_fp16.h>
 
 #include <cmath>
 #include <cstdio>
@@ -214,6 +215,157 @@ __global__ void __launch_bounds__(128 * FG, 1) k_mlp_fused(const float* __restri
     if (!ok) break;
 #pragma unroll
     for (int m = 0; m < NOUT; ++m) out[m] += b4[m];
+    io.store(s, s < n, out, loc);
+  }
+  if (!ok && t == 0) atomicOr(err, ERR_SYNC);
+  umma::tc_fence_before();
+  __syncthreads();
+  if (threadIdx.x < 32) {
+    umma::tc_fence_after();
+    umma::tmem_dealloc(tmem, FUSED_TMEM_COLS);
+  }
+}
+
+// ------------------------------------------------ fused forward, all tcgen05
+// Every layer on the tensor cores with F16 operands and FP32 accumulators in
+// TMEM: layer 0 as one K = 16 step (the 7 features padded with zeros), the
+// three hidden layers as 8 K-steps, the output layer as N = 16 (4 outputs
+// padded).  The epilogue of each layer adds the FP32 bias, converts pairs to
+// f16x2 and evaluates the tanh form of GELU on packed halves (2 values per
+// instruction, hardware tanh on f16x2), writing the next layer's A operand
+// directly.  F16 keeps 11 significant bits where BF16 keeps 8, so the
+// activations are closer to FP32 than the training forward's BF16 ones.
+// The weights come pre-swizzled in F16 (k_pack16), in the shared-memory order
+// of the kernel: hidden tiles 1..3, the layer-0 tile (128 rows, K columns 0-15
+// used), the output tile (16 rows); the CTA copies them once.  FG groups of
+// four warps, each with its activation tile, 128 TMEM columns and mbarrier,
+// work on different tiles of 128 samples, so one group's epilogue overlaps
+// another's MMAs.
+constexpr int W0_TILE_BYTES = 128 * 128, W4_TILE_BYTES = 16 * 128 * 2;
+constexpr int WH_BYTES = 3 * TILE_BYTES + W0_TILE_BYTES + W4_TILE_BYTES;  // 118784
+constexpr int F2_W0 = 3 * TILE_BYTES, F2_W4 = F2_W0 + W0_TILE_BYTES, F2_ACT = F2_W4 + W4_TILE_BYTES;
+constexpr int F2_BIAS = F2_ACT + FG * TILE_BYTES;  // b0..b3 then b4 (16 floats)
+constexpr int F2_BAR = F2_BIAS + (4 * H + 16) * 4;
+constexpr int F2_SLOT = F2_BAR + 8 * FG, F2_OK = F2_SLOT + 4;
+constexpr int F2_SMEM = F2_OK + 4 * FG + 1024;
+constexpr uint32_t IDESC_H = umma::idesc_f16(128, 128), IDESC_H16 = umma::idesc_f16(128, 16);
+static_assert(F2_ACT % 1024 == 0 && F2_W0 % 1024 == 0 && F2_W4 % 1024 == 0, "tile alignment");
+static_assert(F2_BAR % 8 == 0, "mbarrier alignment");
+static_assert(F2_SMEM <= 227 * 1024, "shared memory");
+
+__device__ __forceinline__ uint32_t h2_bits(float v) {
+  const __half2 h = __float2half2_rn(v);
+  return *reinterpret_cast<const uint32_t*>(&h);
+}
+// pack (a, b) to f16x2, a in the low half
+__device__ __forceinline__ uint32_t pack_h2(float a, float b) {
+  uint32_t x;
+  asm("cvt.rn.f16x2.f32 %0, %1, %2;" : "=r"(x) : "f"(b), "f"(a));
+  return x;
+}
+// GELU (tanh form) of two FP32 pre-activations on packed halves:
+// 0.5 x (1 + tanh(x (k0 + k0 k1 x^2)))
+__device__ __forceinline__ uint32_t gelu_h2(float a, float b) {
+  const uint32_t c0 = h2_bits(GK0), c1 = h2_bits(GK0 * GK1), half = h2_bits(0.5f);
+  uint32_t x, x2, p, u, t, hx, g;
+  asm("cvt.rn.satfinite.f16x2.f32 %0, %1, %2;" : "=r"(x) : "f"(b), "f"(a));
+  asm("mul.rn.f16x2 %0, %1, %1;" : "=r"(x2) : "r"(x));
+  asm("fma.rn.f16x2 %0, %1, %2, %3;" : "=r"(p) : "r"(x2), "r"(c1), "r"(c0));
+  asm("mul.rn.f16x2 %0, %1, %2;" : "=r"(u) : "r"(x), "r"(p));
+  asm("tanh.approx.f16x2 %0, %1;" : "=r"(t) : "r"(u));
+  asm("mul.rn.f16x2 %0, %1, %2;" : "=r"(hx) : "r"(x), "r"(half));
+  asm("fma.rn.f16x2 %0, %1, %2, %2;" : "=r"(g) : "r"(t), "r"(hx));
+  return g;
+}
+
+template <class Io>
+__global__ void __launch_bounds__(128 * FG, 1) k_mlp_fwd16(const uint4* __restrict__ Wh, const float* __restrict__ params,
+                                                           Norm nr, Io io, int n, unsigned* err) {
+  extern __shared__ uint8_t smem_raw[];
+  uint8_t* base = smem_raw + ((1024u - (umma::smem_u32(smem_raw) & 1023u)) & 1023u);
+  const uint32_t sbase = umma::smem_u32(base);
+  float* bias = reinterpret_cast<float*>(base + F2_BIAS);
+  uint32_t* slot = reinterpret_cast<uint32_t*>(base + F2_SLOT);
+  const int g = threadIdx.x >> 7, t = threadIdx.x & 127, warp = t >> 5;
+  uint64_t* bar = reinterpret_cast<uint64_t*>(base + F2_BAR) + g;
+  int* s_ok = reinterpret_cast<int*>(base + F2_OK) + g;
+  for (int q = threadIdx.x; q < WH_BYTES / 16; q += 128 * FG) reinterpret_cast<uint4*>(base)[q] = Wh[q];
+  for (int q = threadIdx.x; q < H; q += 128 * FG) {
+    bias[q] = params[OFF_B0 + q];
+    for (int l = 1; l <= 3; ++l) bias[l * H + q] = params[off_b(l) + q];
+  }
+  if (threadIdx.x < 16) bias[4 * H + threadIdx.x] = threadIdx.x < NOUT ? params[OFF_B4 + threadIdx.x] : 0.f;
+  if (t == 0) umma::mbar_init(bar, 1);
+  if (threadIdx.x < 32) {
+    umma::tmem_alloc(slot, FUSED_TMEM_COLS);
+    umma::tmem_relinquish();
+  }
+  umma::tc_fence_before();
+  __syncthreads();
+  umma::tc_fence_after();
+  const uint32_t tmem = *slot, tmem_g = tmem + (uint32_t)(g * 128);
+  const uint32_t act = sbase + F2_ACT + g * TILE_BYTES;
+  uint8_t* actp = base + F2_ACT + g * TILE_BYTES;
+  const uint32_t trow = tmem_g + ((uint32_t)(warp * 32) << 16);
+  uint32_t phase = 0;
+  bool ok = true;
+  // issue nk K-steps of A (this group's tile) x B (tile at bsh, rb rows) into
+  // the group's accumulator and wait for them (bounded)
+  auto mma = [&](int nk, uint32_t bsh, int rb, uint32_t idesc) {
+    umma::fence_async_smem();
+    umma::tc_fence_before();
+    group_sync(g);
+    if (t == 0) {
+      umma::tc_fence_after();
+      for (int kk = 0; kk < nk; ++kk)
+        umma::mma_bf16(tmem_g, umma::sdesc_k(act, 128, kk), umma::sdesc_k(bsh, rb, kk), idesc, kk > 0 ? 1u : 0u);
+      umma::mma_commit(bar);
+      *s_ok = umma::mbar_wait(bar, phase) ? 1 : 0;
+    }
+    group_sync(g);
+    phase ^= 1u;
+    umma::tc_fence_after();
+    return *s_ok != 0;
+  };
+  // bias + GELU of the accumulator row t -> row t of the activation tile
+  auto epilogue = [&](const float* bl) {
+    for (int c = 0; c < 4; ++c) {
+      float v[32];
+      umma::tmem_ld32(trow + (uint32_t)(c * 32), v);
+#pragma unroll
+      for (int c8 = 0; c8 < 4; ++c8) {
+        uint32_t h[4];
+#pragma unroll
+        for (int e = 0; e < 4; ++e) {
+          const int j = c8 * 8 + 2 * e;
+          h[e] = gelu_h2(v[j] + bl[c * 32 + j], v[j + 1] + bl[c * 32 + j + 1]);
+        }
+        *reinterpret_cast<uint4*>(actp + umma::sw128_offset(t, c * 32 + c8 * 8, 128)) =
+            make_uint4(h[0], h[1], h[2], h[3]);
+      }
+    }
+  };
+  const int ntiles = (n + 127) / 128;
+  for (int tile = blockIdx.x * FG + g; tile < ntiles && ok; tile += gridDim.x * FG) {
+    const int s = tile * 128 + t;
+    float xn[NIN];
+    typename Io::Local loc;
+    io.load(s, s < n, nr, xn, loc);
+    // the features as K columns 0-15 of row t (7 values, then zeros)
+    *reinterpret_cast<uint4*>(actp + umma::sw128_offset(t, 0, 128)) =
+        make_uint4(pack_h2(xn[0], xn[1]), pack_h2(xn[2], xn[3]), pack_h2(xn[4], xn[5]), pack_h2(xn[6], 0.f));
+    *reinterpret_cast<uint4*>(actp + umma::sw128_offset(t, 8, 128)) = make_uint4(0u, 0u, 0u, 0u);
+    if (!(ok = mma(1, sbase + F2_W0, 128, IDESC_H))) break;
+    epilogue(bias);
+    for (int l = 1; l <= 3 && ok; ++l) {
+      if (!(ok = mma(8, sbase + (l - 1) * TILE_BYTES, 128, IDESC_H))) break;
+      epilogue(bias + l * H);
+    }
+    if (!ok || !(ok = mma(8, sbase + F2_W4, 16, IDESC_H16))) break;
+    float v[32], out[NOUT];
+    umma::tmem_ld32(trow, v);
+#pragma unroll
+    for (int m = 0; m < NOUT; ++m) out[m] = v[m] + bias[4 * H + m];
     io.store(s, s < n, out, loc);
   }
   if (!ok && t == 0) atomicOr(err, ERR_SYNC);
@@ -602,6 +754,34 @@ __global__ void k_pack(const float* __restrict__ p, __nv_bfloat16* Wb, __nv_bflo
   WbT[(size_t)l * H * H + i * H + o] = w;
 }
 
+// F16 weights of the inference kernel, swizzled in its shared-memory order
+// (k_mlp_fwd16): hidden tiles, the layer-0 tile (K padded 7 -> 16 with zeros),
+// the output tile (N padded 4 -> 16 with zeros).  Bytes of the tiles that the
+// MMAs never read stay as the creation left them (zero).
+__global__ void k_pack16(const float* __restrict__ p, uint8_t* Wh) {
+  const int q = blockIdx.x * blockDim.x + threadIdx.x;
+  constexpr int NH = 3 * H * H, N0 = H * 16, N4 = 16 * H;
+  float v;
+  uint32_t off;
+  if (q < NH) {
+    const int l = q / (H * H), o = (q % (H * H)) / H, i = q % H;
+    v = p[off_w(l + 1) + o * H + i];
+    off = (uint32_t)(l * TILE_BYTES) + umma::sw128_offset(o, i, 128);
+  } else if (q < NH + N0) {
+    const int o = (q - NH) / 16, i = (q - NH) % 16;
+    v = i < NIN ? p[OFF_W0 + o * NIN + i] : 0.f;
+    off = (uint32_t)F2_W0 + umma::sw128_offset(o, i, 128);
+  } else if (q < NH + N0 + N4) {
+    const int m = (q - NH - N0) / H, i = (q - NH - N0) % H;
+    v = m < NOUT ? p[OFF_W4 + m * H + i] : 0.f;
+    off = (uint32_t)F2_W4 + umma::sw128_offset(m, i, 16);
+  } else {
+    return;
+  }
+  *reinterpret_cast<__half*>(Wh + off) = __float2half_rn(v);
+}
+constexpr int PACK16_N = 3 * H * H + H * 16 + 16 * H;
+
 }  // namespace mlp
 
 // samples for training: raw features (T, p, Y1..Y4, dt) and targets
@@ -650,6 +830,7 @@ struct rc_mlp {
   float* m2 = nullptr;
   __nv_bfloat16* Wb = nullptr;
   __nv_bfloat16* WbT = nullptr;
+  uint8_t* Wh = nullptr;  // F16 weights of the inference kernel (k_pack16)
   unsigned* derr = nullptr;
   mlp::Norm norm{};
   int step = 0;
@@ -725,14 +906,14 @@ namespace rc {
 cudaError_t surrogate_source(const Dev& d, const void* th, const rc_mlp* net, float spread_tol, int* list,
                              unsigned* nlist, unsigned* nsurr, cudaStream_t s) {
   mlp::IoSolver io{d, *static_cast<const ThermoDev<4>*>(th), spread_tol, list, nlist, nsurr};
-  mlp::k_mlp_fused<mlp::IoSolver><<<fused_grid(net->device, d.NE), 128 * mlp::FG, mlp::FUSED_SMEM, s>>>(
-      net->params, net->Wb, net->norm, io, d.NE, d.err);
+  mlp::k_mlp_fwd16<mlp::IoSolver><<<fused_grid(net->device, d.NE), 128 * mlp::FG, mlp::F2_SMEM, s>>>(
+      reinterpret_cast<const uint4*>(net->Wh), net->params, net->norm, io, d.NE, d.err);
   return cudaGetLastError();
 }
 // outside stream capture, once per context
 cudaError_t surrogate_prepare() {
-  return cudaFuncSetAttribute(mlp::k_mlp_fused<mlp::IoSolver>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                              mlp::FUSED_SMEM);
+  return cudaFuncSetAttribute(mlp::k_mlp_fwd16<mlp::IoSolver>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                              mlp::F2_SMEM);
 }
 cudaError_t surrogate_samples(const void* th, const double* P0, const double* P1, const double* dt, int n, float* x,
                               float* t, cudaStream_t s) {
@@ -758,8 +939,9 @@ int rc_mlp_create(int device, rc_mlp** out) {
       cudaMalloc(&m->m2, P * sizeof(float)) != cudaSuccess || cudaMalloc(&m->grad, P * sizeof(float)) != cudaSuccess ||
       cudaMalloc(&m->Wb, 3 * mlp::H * mlp::H * sizeof(__nv_bfloat16)) != cudaSuccess ||
       cudaMalloc(&m->WbT, 3 * mlp::H * mlp::H * sizeof(__nv_bfloat16)) != cudaSuccess ||
-      cudaMalloc(&m->derr, sizeof(unsigned)) != cudaSuccess)
+      cudaMalloc(&m->Wh, mlp::WH_BYTES) != cudaSuccess || cudaMalloc(&m->derr, sizeof(unsigned)) != cudaSuccess)
     return bail(RC_ERR_CUDA);
+  cudaMemset(m->Wh, 0, mlp::WH_BYTES);
   cudaMemset(m->params, 0, P * sizeof(float));
   cudaMemset(m->m1, 0, P * sizeof(float));
   cudaMemset(m->m2, 0, P * sizeof(float));
@@ -770,8 +952,8 @@ int rc_mlp_create(int device, rc_mlp** out) {
   for (int i = 0; i < mlp::NIN; ++i) { m->norm.mean[i] = 0.f; m->norm.stdv[i] = 1.f; }
   const float dom[6] = {300.f, 6000.f, 1.0e2f, 2.0e7f, 1.0e-10f, 1.0e-4f};
   for (int i = 0; i < 6; ++i) m->norm.dom[i] = dom[i];
-  if (cudaFuncSetAttribute(mlp::k_mlp_fused<mlp::IoRaw>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                           mlp::FUSED_SMEM) != cudaSuccess ||
+  if (cudaFuncSetAttribute(mlp::k_mlp_fwd16<mlp::IoRaw>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                           mlp::F2_SMEM) != cudaSuccess ||
       cudaFuncSetAttribute(mlp::k_gemm<mlp::EPI_FWD>, cudaFuncAttributeMaxDynamicSharedMemorySize, mlp::GEMM_SMEM) !=
           cudaSuccess ||
       cudaFuncSetAttribute(mlp::k_gemm<mlp::EPI_BWD>, cudaFuncAttributeMaxDynamicSharedMemorySize, mlp::GEMM_SMEM) !=
@@ -787,7 +969,7 @@ int rc_mlp_destroy(rc_mlp* m) {
   if (!m) return RC_OK;
   for (void* p : m->work) cudaFree(p);
   cudaFree(m->params); cudaFree(m->m1); cudaFree(m->m2); cudaFree(m->grad);
-  cudaFree(m->Wb); cudaFree(m->WbT); cudaFree(m->derr);
+  cudaFree(m->Wb); cudaFree(m->WbT); cudaFree(m->Wh); cudaFree(m->derr);
   delete m;
   return RC_OK;
 }
@@ -801,6 +983,7 @@ int rc_mlp_set_params(rc_mlp* m, const float* params) {
   MLP_CU(cudaMemset(m->m2, 0, sizeof(float) * mlp::NPARAM));
   m->step = 0;
   mlp::k_pack<<<(3 * mlp::H * mlp::H + 255) / 256, 256>>>(m->params, m->Wb, m->WbT);
+  mlp::k_pack16<<<(mlp::PACK16_N + 255) / 256, 256>>>(m->params, m->Wh);
   MLP_CU(cudaGetLastError());
   MLP_CU(cudaDeviceSynchronize());
   return RC_OK;
@@ -829,8 +1012,8 @@ int rc_mlp_forward(rc_mlp* m, const float* d_x, int n, float* d_y, void* stream)
   if (n == 0) return RC_OK;
   cudaStream_t s = static_cast<cudaStream_t>(stream);
   mlp::IoRaw io{d_x, d_y};
-  mlp::k_mlp_fused<mlp::IoRaw><<<fused_grid(m->device, n), 128 * mlp::FG, mlp::FUSED_SMEM, s>>>(m->params, m->Wb,
-                                                                                                m->norm, io, n, m->derr);
+  mlp::k_mlp_fwd16<mlp::IoRaw><<<fused_grid(m->device, n), 128 * mlp::FG, mlp::F2_SMEM, s>>>(
+      reinterpret_cast<const uint4*>(m->Wh), m->params, m->norm, io, n, m->derr);
   MLP_CU(cudaGetLastError());
   return RC_OK;
 }
@@ -910,6 +1093,7 @@ int rc_mlp_adam(rc_mlp* m, const float* d_grad, float lr, float beta1, float bet
   mlp::k_adam<<<(mlp::NPARAM + 255) / 256, 256, 0, s>>>(m->params, m->m1, m->m2, d_grad, lr, beta1, beta2, eps, bc1,
                                                        bc2);
   mlp::k_pack<<<(3 * mlp::H * mlp::H + 255) / 256, 256, 0, s>>>(m->params, m->Wb, m->WbT);
+  mlp::k_pack16<<<(mlp::PACK16_N + 255) / 256, 256, 0, s>>>(m->params, m->Wh);
   MLP_CU(cudaGetLastError());
   return RC_OK;
 }

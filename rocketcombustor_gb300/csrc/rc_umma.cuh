@@ -1,10 +1,10 @@
 // Blackwell (sm_100 family) tensor-core building blocks as inline PTX:
-// TMEM allocation, tcgen05.mma kind::f16 (BF16 x BF16 -> FP32 in TMEM),
-// tcgen05.commit to an mbarrier, tcgen05.ld of the accumulator, and the
-// shared-memory operand layout the MMA reads.
+// TMEM allocation, tcgen05.mma kind::f16 (BF16 x BF16 or F16 x F16 -> FP32
+// in TMEM), tcgen05.commit to an mbarrier, tcgen05.ld of the accumulator, and
+// the shared-memory operand layout the MMA reads.
 //
 // Operand layout (both A and B "K-major", 128-byte swizzle).  An operand tile
-// of R rows (R a multiple of 8) and 128 K-elements (bf16) is stored as two
+// of R rows (R a multiple of 8) and 128 K-elements (16-bit) is stored as two
 // swizzle atoms of 64 K-elements each; atom a holds rows at a 128-byte pitch
 // starting at a * R * 128, and inside a row the 16-byte chunk c (elements
 // 8c..8c+7 of the atom) sits at chunk position c ^ (row % 8).  Tiles start on
@@ -52,6 +52,11 @@ __device__ __forceinline__ uint64_t sdesc_k(uint32_t base, int R, int kk) {
 // M>>4 at bits 24-28.
 __host__ __device__ constexpr uint32_t idesc_bf16(int M, int N) {
   return (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(N >> 3) << 17) | ((uint32_t)(M >> 4) << 24);
+}
+
+// the same with A = B = F16 (bits 7-9, 10-12 = 0)
+__host__ __device__ constexpr uint32_t idesc_f16(int M, int N) {
+  return (1u << 4) | ((uint32_t)(N >> 3) << 17) | ((uint32_t)(M >> 4) << 24);
 }
 
 // ---- TMEM allocation (one warp) ------------------------------------------

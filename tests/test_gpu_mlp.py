@@ -1,9 +1,12 @@
 """Surrogate MLP kernels (tcgen05) against the CPU FP64 reference (needs a GB300).
 
-The reference (oracle/mlp_ref.py) rounds to BF16 where the GPU keeps BF16, so
-what remains is FP32 accumulation order and the hardware tanh; outputs are
-compared at 1e-2 absolute on O(1) values and gradients per tensor at 3e-2
-relative L2 norm with cosine similarity >= 0.999.
+Training (the gradient) keeps BF16 activations and weights; the reference
+(oracle/mlp_ref.py) rounds to BF16 at the same points, so what remains is FP32
+accumulation order and the hardware tanh: gradients per tensor within 3e-2
+relative L2 norm with cosine similarity >= 0.999.  Inference runs every layer
+with F16 operands and the GELU on packed halves: its outputs are compared with
+the unrounded FP64 reference at 5e-3 of max(1, |y|) (F16 keeps 11 significant
+bits), and with the training forward at the BF16 level.
 """
 import numpy as np
 import pytest
@@ -35,8 +38,10 @@ def test_fused_forward_matches_reference(net):
     import torch
     x = raw_samples(1000, 1)  # not a multiple of 128: a partial last tile
     y = net.forward(torch.tensor(x, device="cuda")).cpu().numpy()
-    yr, _ = mlp_ref.forward(net.get_params(), x, MEAN, STD, bf=True)
-    assert np.abs(y - yr).max() <= 1e-2 * max(1.0, np.abs(yr).max()), np.abs(y - yr).max()
+    yr, _ = mlp_ref.forward(net.get_params(), x, MEAN, STD, bf=False)
+    assert np.abs(y - yr).max() <= 5e-3 * max(1.0, np.abs(yr).max()), np.abs(y - yr).max()
+    yb, _ = mlp_ref.forward(net.get_params(), x, MEAN, STD, bf=True)
+    assert np.abs(y - yb).max() <= 1e-2 * max(1.0, np.abs(yb).max()), np.abs(y - yb).max()
 
 
 def test_gradient_matches_reference(net):
@@ -62,7 +67,8 @@ def test_training_and_inference_paths_agree(net):
     x = torch.tensor(raw_samples(n, 4), device="cuda")
     y = net.forward(x)
     _, loss = net.gradient(x, torch.zeros((n, 4), device="cuda"))
-    assert loss == pytest.approx(float((y.double() ** 2).mean()), rel=1e-4)
+    # the training forward's BF16 activations against the inference's F16 ones
+    assert loss == pytest.approx(float((y.double() ** 2).mean()), rel=2e-2)
 
 
 def test_gradient_is_reproducible(net):
