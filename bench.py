@@ -582,13 +582,13 @@ def rel_err(st, ref) -> dict:
     return {"p": float(e[0]), "T": float(e[3]), "Y": [float(x) for x in e[4:]]}
 
 
-def steady_run(s, args, dc_window=0):
+def steady_run(s, args, dc_window=0, freeze_window=0):
     """run_to_steady with wall time (set-up excluded: the solver exists and its
     state is set; the timed loop includes the graph launches and the host reads
     of the norms)."""
     s.sync()
     t0 = time.perf_counter()
-    r = s.run_to_steady(args.tol, args.max_iters, args.every, dc_window=dc_window)
+    r = s.run_to_steady(args.tol, args.max_iters, args.every, dc_window=dc_window, freeze_window=freeze_window)
     wall = time.perf_counter() - t0
     reached = r["reached"]
     out = {"iterations": r["iterations"], "wall_s": wall,
@@ -598,6 +598,8 @@ def steady_run(s, args, dc_window=0):
            "ms_per_iteration": 1e3 * wall / r["iterations"]}
     if dc_window:
         out["switched_to_dc_at"] = r["switched_at"]
+    if freeze_window:
+        out["surrogate_choice_frozen_at"] = r["frozen_at"]
     return out, r
 
 
@@ -728,7 +730,7 @@ def converge_surrogate(args, rc, torch, case):
     s = rc.Solver(case)
     s.set_surrogate(net)
     s.set_chemistry(rc.RC_CHEM_SURROGATE)
-    f, _ = steady_run(s, args)
+    f, _ = steady_run(s, args, freeze_window=args.dc_window)
     f["rel_linf_vs_integrated_converged"] = rel_err(s.get_state()[0], ref)
     a, b_ = s.surrogate_stats()
     f["cells_network"], f["cells_integrator"] = a, b_

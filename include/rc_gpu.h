@@ -235,6 +235,14 @@ struct rc_mlp;
 int rc_set_surrogate(rc_ctx* ctx, struct rc_mlp* net, double spread_tol);
 /* Cells of the last surrogate source served by the network / by the integrator. */
 int rc_surrogate_stats(rc_ctx* ctx, unsigned* n_surrogate, unsigned* n_fallback);
+/* Freeze (on != 0) or free (on = 0) the surrogate's per-cell choice between
+ * the network and the integrator.  With on, the next rc_lusgs_stage records
+ * every cell's choice and the stages after it keep it (a network cell whose
+ * source is not finite still goes to the integrator): the source is then a
+ * smooth function of the state, which a steady iteration needs to converge
+ * (the choice itself switches as the state moves near a threshold).  No
+ * counterpart in the reference.  Returns RC_ERR_ARG before rc_set_surrogate. */
+int rc_surrogate_freeze(rc_ctx* ctx, int on);
 /* Training pairs from integrated states: d_P0, d_P1 (NVar x n SoA, before and
  * after d_dt) -> raw features d_x (n x 7: T, p, Y_1..Y_4, dt) and targets d_t
  * (n x 4: the normalised changes z_k of rc_mlp.h).  Device pointers; on the

@@ -120,6 +120,7 @@ SIGNATURES = {
     "rc_clear_error": (_i, [_vp]),
     "rc_set_surrogate": (_i, [_vp, _vp, _d]),
     "rc_surrogate_stats": (_i, [_vp, ctypes.POINTER(ctypes.c_uint), ctypes.POINTER(ctypes.c_uint)]),
+    "rc_surrogate_freeze": (_i, [_vp, _i]),
     "rc_surrogate_samples": (_i, [_vp, _vp, _vp, _vp, _i, _vp, _vp]),
     "rc_mlp_create": (_i, [_i, ctypes.POINTER(_vp)]),
     "rc_mlp_destroy": (_i, [_vp]),
@@ -397,6 +398,11 @@ class Solver:
         self._check(load().rc_surrogate_stats(self._h, ctypes.byref(a), ctypes.byref(b)))
         return a.value, b.value
 
+    def surrogate_freeze(self, on: bool = True):
+        """Freeze (record at the next stage, then keep) or free the surrogate's
+        per-cell choice between the network and the integrator."""
+        self._check(load().rc_surrogate_freeze(self._h, int(bool(on))))
+
     def surrogate_samples(self, P0, P1, dt):
         """Training pairs from states before (P0) and after (P1) dt: CUDA float64
         tensors (NVar, n) and (n,) -> raw features (n, 7) and targets (n, 4)."""
@@ -441,7 +447,7 @@ class Solver:
         return self.sync()
 
     def run_to_steady(self, tol: float = 1e-8, max_iters: int = 100000, every: int = 10, dc_window: int = 0,
-                      start: int = 1) -> dict:
+                      start: int = 1, freeze_window: int = 0) -> dict:
         """The steady loop (fvm2d.f90:48-76) with the stopping test the
         reference does not have: iterate lu_sgs_stage until, for every case,
         max_k Res_k(n) / Res_k(1) <= tol, Res_k being the step_residual
@@ -452,15 +458,20 @@ class Solver:
         dc_window > 0 (mixed precision): once the level has not fallen below
         0.99 of its best for dc_window reads, switch to defect correction
         (RC_PREC_MIXED_DC, the FP64 residual driving the FP32 sweeps), whose
-        fixed point is the FP64 one.
+        fixed point is the FP64 one.  freeze_window > 0 (surrogate chemistry):
+        the same stall test freezes the surrogate's per-cell choice between
+        network and integrator (surrogate_freeze), whose switching otherwise
+        keeps the source from settling.
 
         Returns {"iterations": last iteration run, "levels": per-case level at
         the end, "reached": per-case first iteration at or below tol (None if
         not), "history": [(iteration, per-case levels)], "switched_at":
-        iteration of the switch or 0}."""
+        iteration of the switch or 0, "frozen_at": iteration of the freeze or
+        0}."""
         res0 = mask = None
         hist, reached = [], None
-        best, since, switched = np.inf, 0, 0
+        best, since, switched, frozen = np.inf, 0, 0, 0
+        fbest, fsince = np.inf, 0
         it = start - 1
         for it in range(start, start + max_iters):
             self.lu_sgs_stage(it)
@@ -478,8 +489,8 @@ class Solver:
                     reached[k] = it
             if all(x is not None for x in reached):
                 break
+            top = float(lv.max())
             if dc_window > 0 and not switched:
-                top = float(lv.max())
                 if top < 0.99 * best:
                     best, since = top, 0
                 else:
@@ -487,9 +498,17 @@ class Solver:
                     if since >= dc_window:
                         self.set_precision(RC_PREC_MIXED_DC)
                         switched = it
+            if freeze_window > 0 and not frozen:
+                if top < 0.99 * fbest:
+                    fbest, fsince = top, 0
+                else:
+                    fsince += 1
+                    if fsince >= freeze_window:
+                        self.surrogate_freeze(True)
+                        frozen = it
         self.sync()
         return {"iterations": it - start + 1, "levels": hist[-1][1] if hist else None, "reached": reached,
-                "history": hist, "switched_at": switched}
+                "history": hist, "switched_at": switched, "frozen_at": frozen}
 
     # -- unsteady dual-time BDF2
     def set_p_out(self, p_out: float):

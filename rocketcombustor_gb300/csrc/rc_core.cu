@@ -1219,8 +1219,8 @@ template <int NSP> void bdf2_prep(const Dev&, const void*, int, cudaStream_t);
 template <int NSP> void bdf2_sweep(const Dev&, const void*, bool, int, int, int, cudaStream_t);
 template <int NSP> void bdf2_update(const Dev&, const void*, int, cudaStream_t);
 template <int NSP> int bdf2_nbq();
-cudaError_t surrogate_source(const Dev&, const void*, const rc_mlp*, float, int*, unsigned*, unsigned*,
-                             cudaStream_t);
+cudaError_t surrogate_source(const Dev&, const void*, const rc_mlp*, float, int*, unsigned*, unsigned*, const int*,
+                             unsigned char*, cudaStream_t);
 cudaError_t surrogate_prepare();
 cudaError_t surrogate_samples(const void*, const double*, const double*, const double*, int, float*, float*,
                               cudaStream_t);
@@ -1277,6 +1277,9 @@ struct rc_ctx {
   float spread_tol = 0.02f;
   int* sur_list = nullptr;            // [NE] cells handed back to the integrator
   unsigned* sur_counts = nullptr;     // [2]: fallback cells, surrogate cells
+  int* sur_mode = nullptr;            // [1]: 0 each cell decided per call, 1 decide and record, 2 recorded
+  unsigned char* sur_dec = nullptr;   // [NE]: recorded decision, 1 = integrator
+  bool sur_freeze_pending = false;    // switch sur_mode to 2 after the next stage
   cudaStream_t stream2 = nullptr;     // side stream: the integrated source runs beside the face fluxes
   cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
 
@@ -1598,7 +1601,7 @@ void q_chem_fork(rc_ctx* c) {
   if (c->chem == RC_CHEM_SURROGATE) {
     cudaMemsetAsync(c->sur_counts, 0, 2 * sizeof(unsigned), c->stream2);
     surrogate_source(c->d, c->thermo.data(), c->net, c->spread_tol, c->sur_list, c->sur_counts, c->sur_counts + 1,
-                     c->stream2);
+                     c->sur_mode, c->sur_dec, c->stream2);
     chem_list<NSP>(c->d, c->thermo.data(), c->chem_tol, c->chem_maxsub, c->chem_nsub, c->sur_list, c->sur_counts,
                    c->chem_counter, c->stream2);
     c->launches += 2;
@@ -2620,11 +2623,21 @@ int rc_set_surrogate(rc_ctx* c, rc_mlp* net, double spread_tol) {
   if (!c->sur_list) {
     if (int st = dev_zeros(c, (size_t)c->NE, &c->sur_list)) return st;
     if (int st = dev_zeros(c, (size_t)2, &c->sur_counts)) return st;
+    if (int st = dev_zeros(c, (size_t)1, &c->sur_mode)) return st;
+    if (int st = dev_zeros(c, (size_t)c->NE, &c->sur_dec)) return st;
   }
   RC_CU(surrogate_prepare());
   c->net = net;
   c->spread_tol = (float)spread_tol;
   drop_graphs(c);
+  return RC_OK;
+}
+int rc_surrogate_freeze(rc_ctx* c, int on) {
+  if (!c || !c->sur_mode) return RC_ERR_ARG;
+  const int m = on ? 1 : 0;
+  RC_CU(cudaMemcpyAsync(c->sur_mode, &m, sizeof(int), cudaMemcpyHostToDevice, c->stream));
+  RC_CU(cudaStreamSynchronize(c->stream));
+  c->sur_freeze_pending = on != 0;
   return RC_OK;
 }
 int rc_surrogate_stats(rc_ctx* c, unsigned* n_surrogate, unsigned* n_fallback) {
@@ -2731,6 +2744,11 @@ int rc_lusgs_stage(rc_ctx* c, int istep) {
   }
   RC_CU(cudaGraphLaunch(c->graph, c->stream));
   c->launches += c->graph_kernels;
+  if (c->sur_freeze_pending) {  // this stage recorded the surrogate's decisions: keep them from now on
+    static const int recorded = 2;
+    RC_CU(cudaMemcpyAsync(c->sur_mode, &recorded, sizeof(int), cudaMemcpyHostToDevice, c->stream));
+    c->sur_freeze_pending = false;
+  }
   return RC_OK;
 }
 

@@ -427,7 +427,10 @@ __device__ __forceinline__ double progress_scale(const ThermoDev<4>& th, const d
 // domain, when the z_k of the reacting species disagree by more than
 // spread_tol (one global reaction: they are equal for the exact integrator),
 // when their mean is outside [-0.01, 3], or when Y + dY leaves [0, 1] by more
-// than 1e-6.
+// than 1e-6.  Once the decisions are frozen (rc_surrogate_freeze: one call
+// records them, later calls reuse them) a cell keeps its side, the network
+// unless its source is not finite, so that the source is a smooth function of
+// the state and a steady iteration can converge.
 struct IoSolver {
   Dev d;
   ThermoDev<4> th;
@@ -435,6 +438,8 @@ struct IoSolver {
   int* list;
   unsigned* nlist;
   unsigned* nsurr;
+  const int* mode;     // 0 decide per call, 1 decide and record in dec, 2 use dec
+  unsigned char* dec;  // per cell: 1 = integrator
   struct Local {
     double Y[4], dt, rho, vol, xs;
     bool dom;
@@ -491,6 +496,14 @@ struct IoSolver {
       const double Yn = L.Y[k] + dY;
       fall = fall || !(Yn >= -1e-6 && Yn <= 1.0 + 1e-6);
       src[k] = L.vol * (L.rho * (dY / L.dt));
+    }
+    const int md = *mode;
+    if (md == 2) {
+      fall = dec[i] != 0;
+#pragma unroll
+      for (int k = 0; k < 3; ++k) fall = fall || !isfinite(src[k]);
+    } else if (md == 1) {
+      dec[i] = fall ? 1 : 0;
     }
     if (fall) {
       const unsigned slot = atomicAdd(nlist, 1u);
@@ -904,8 +917,8 @@ int ensure_work(rc_mlp* m, int n) {
 namespace rc {
 // inference over the cells of a solver context (NSP must be 4)
 cudaError_t surrogate_source(const Dev& d, const void* th, const rc_mlp* net, float spread_tol, int* list,
-                             unsigned* nlist, unsigned* nsurr, cudaStream_t s) {
-  mlp::IoSolver io{d, *static_cast<const ThermoDev<4>*>(th), spread_tol, list, nlist, nsurr};
+                             unsigned* nlist, unsigned* nsurr, const int* mode, unsigned char* dec, cudaStream_t s) {
+  mlp::IoSolver io{d, *static_cast<const ThermoDev<4>*>(th), spread_tol, list, nlist, nsurr, mode, dec};
   mlp::k_mlp_fwd16<mlp::IoSolver><<<fused_grid(net->device, d.NE), 128 * mlp::FG, mlp::F2_SMEM, s>>>(
       reinterpret_cast<const uint4*>(net->Wh), net->params, net->norm, io, d.NE, d.err);
   return cudaGetLastError();

@@ -5,9 +5,11 @@ off-diagonal terms in FP32 (compensated FP32 gather into an FP64 residual) and
 keeps the step, diagonal division, chemistry, Newton update and norms in FP64.
 RC_PREC_MIXED_DC (defect correction) drives the FP32 sweeps with the FP64
 residual, so its fixed point is the FP64 one.  The error against the FP64
-path is measured and bounded here; the bound is loose on purpose (FP32 noise
-is amplified by the non-smooth Barth limiter), the measured values are what
-the benchmark reports.
+path is measured and bounded here: after 20 iterations the measured
+differences are at most 2.3e-6 (t1) and 1.0e-6 (t2) relative L-infinity per
+field, bounded at 1e-5 (a margin of 4-10 for other boxes and builds).  That
+defect correction lands on the FP64 fixed point is tested at the converged
+steady state (tests/test_gpu_steady.py).
 """
 import numpy as np
 import pytest
@@ -35,8 +37,7 @@ def test_mixed_tracks_fp64(case_root, name):
     pm, _ = mix.get_state()
     e = rel_linf(pm, pr)
     assert np.isfinite(pm).all()
-    assert e[[0, 3]].max() < 1e-3, e          # p, T
-    assert e.max() < 5e-2, e
+    assert e.max() < 1e-5, e
 
 
 def test_defect_correction_uses_fp64_residual(case_t2):

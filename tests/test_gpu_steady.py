@@ -96,3 +96,40 @@ def test_batched_cases_each_reach_steady_as_alone(tmp_path):
         assert np.array_equal(st[b.case_slice(k)], s.get_state()[0]), k
         s.close()
     b.close()
+
+
+def test_surrogate_reaches_steady_once_its_choice_is_frozen(case_root):
+    """The surrogate chemistry (network, integrator where its error indicator
+    rejects a cell), trained here on integrator pairs of this case: with the
+    per-cell choice frozen once the residual stalls, the source is smooth and
+    the iteration reaches 1e-8; its state is compared with the integrated
+    chemistry's converged state (a learned model: within 1e-2 on p and T and
+    5e-2 on Y_k of each field's maximum)."""
+    from rocketcombustor_gb300 import surrogate
+    d = make_case(case_root, "s2t")
+    c = rc.Case(d)
+    s = rc.Solver(c)
+    s.set_chemistry(rc.RC_CHEM_INTEGRATED)
+    pool = surrogate.collect_pool(s, iters=200, every=20)
+    x, t, _ = surrogate.build_dataset(s, pool, 400_000, seed=7)
+    s.close()
+    net = surrogate.MLP(seed=7)
+    net.fit_norm(x)
+    net.train(x, t, steps=3000, batch=8192, lr=2e-3, lr_end=3e-5)
+    ref = rc.Solver(c)
+    ref.set_chemistry(rc.RC_CHEM_INTEGRATED)
+    r0 = ref.run_to_steady(TOL, max_iters=20000, every=10)
+    assert r0["reached"][0] is not None, r0["levels"]
+    P_int = ref.get_state()[0]
+    ref.close()
+    m = rc.Solver(c)
+    m.set_surrogate(net)
+    m.set_chemistry(rc.RC_CHEM_SURROGATE)
+    r = m.run_to_steady(TOL, max_iters=30000, every=10, freeze_window=20)
+    print("surrogate: frozen at", r["frozen_at"], "reached", r["reached"], "cells", m.surrogate_stats())
+    assert r["frozen_at"] > 0 and r["reached"][0] is not None, r["levels"]
+    e = rel_linf(m.get_state()[0], P_int)
+    print("surrogate steady state vs integrated", e)
+    assert e[0] <= 1e-2 and e[3] <= 1e-2 and e[4:].max() <= 5e-2, e
+    m.close()
+    net.close()
