@@ -2,22 +2,24 @@
 //
 // Network: 7 raw inputs (T, p, Y_1..Y_4, dt) -> features (1000/T, log10 p,
 // log10(Y + 1e-10), log10 dt) normalised -> layer 0 (7 -> 128, GELU) -> three 128 -> 128 GELU layers -> 4
-// outputs.  Layer 0 and the output layer are thin and run on the CUDA cores in
-// FP32; the three 128 x 128 layers run on the tcgen05 tensor cores with BF16
-// operands staged in shared memory (128-byte swizzle) and FP32 accumulators in
-// TMEM.  GELU is the tanh form of Hendrycks & Gimpel evaluated with the
-// tanh.approx.f32 instruction.
+// outputs.  GELU is the tanh form of Hendrycks & Gimpel on the hardware tanh.
+// Training keeps FP32 master weights and BF16 operands: the three 128 x 128
+// layers on the tcgen05 tensor cores (operands staged in shared memory with
+// the 128-byte swizzle, FP32 accumulators in TMEM), layer 0 and the output
+// layer on the CUDA cores in FP32.  Inference runs all five layers on tcgen05
+// with F16 operands.
 //
 // Kernels:
-//   k_mlp_fused<Io>   inference, persistent over tiles of 128 samples: the 3
-//                     hidden weight tiles stay in shared memory, activations
-//                     never leave the SM (inputs and outputs through Io);
+//   k_mlp_fwd16<Io>   inference, persistent over tiles of 128 samples: all
+//                     weights stay in shared memory, activations never leave
+//                     the SM (inputs and outputs through Io);
 //   k_gemm<EPI>       training GEMMs, one 128 x 128 output tile per CTA, K in
 //                     chunks of 128, optional split-K: forward layers (bias +
 //                     GELU epilogue), backward data (x GELU' epilogue) and
 //                     weight gradients (FP32 partials);
-//   k_layer0, k_head, k_small_grads, k_reduce_dw, k_adam, k_pack: the thin
-//                     layers, the loss, the small reductions and Adam.
+//   k_layer0, k_head, k_small_grads, k_reduce_dw, k_adam, k_pack, k_pack16: the thin
+//                     layers, the loss, the small reductions, Adam and the
+//                     BF16 / F16 weight copies.
 // Every reduction has a fixed order, so gradients are reproducible run to run.
 #include <cuda_runtime.h>
 #include <cuda_bf16.h>
@@ -87,143 +89,14 @@ __device__ __forceinline__ void features(const float* raw, const Norm& nr, float
   }
 }
 
-// ------------------------------------------------------------ fused forward
-// FG warp groups of 4 warps per CTA, each with its own activation tile, TMEM
-// accumulator (128 columns) and mbarrier, work on different tiles of 128
-// samples: one group's CUDA-core epilogue overlaps another group's MMAs.  The
-// three hidden weight tiles are shared.
+// FG warp groups of 4 warps per CTA in the fused forward (k_mlp_fwd16), each
+// with its own activation tile, TMEM accumulator (128 columns) and mbarrier.
 constexpr int FG = 3;
-constexpr int FS_ACT = 3 * TILE_BYTES;                // + g * TILE_BYTES
-constexpr int FS_W0 = FS_ACT + FG * TILE_BYTES;
-constexpr int FS_BIAS = FS_W0 + H * NIN * 4;          // b0..b3
-constexpr int FS_W4 = FS_BIAS + 4 * H * 4;
-constexpr int FS_B4 = FS_W4 + NOUT * H * 4;
-constexpr int FS_BAR = FS_B4 + 16;                    // FG mbarriers
-constexpr int FS_SLOT = FS_BAR + 8 * FG;
-constexpr int FS_OK = FS_SLOT + 4;                    // FG flags
-constexpr int FUSED_SMEM = FS_OK + 4 * FG + 1024;     // + alignment slack
 constexpr uint32_t FUSED_TMEM_COLS = FG * 128 <= 256 ? 256 : 512;
-static_assert(FS_BAR % 8 == 0, "mbarrier alignment");
-static_assert(FUSED_SMEM <= 227 * 1024, "shared memory");
 
 // barrier of the 128 threads of group g (named barrier 1 + g; 0 is __syncthreads)
 __device__ __forceinline__ void group_sync(int g) {
   asm volatile("bar.sync %0, 128;" ::"r"(1 + g) : "memory");
-}
-
-template <class Io>
-__global__ void __launch_bounds__(128 * FG, 1) k_mlp_fused(const float* __restrict__ params,
-                                                           const __nv_bfloat16* __restrict__ Wb, Norm nr, Io io,
-                                                           int n, unsigned* err) {
-  extern __shared__ uint8_t smem_raw[];
-  uint8_t* base = smem_raw + ((1024u - (umma::smem_u32(smem_raw) & 1023u)) & 1023u);
-  const uint32_t sbase = umma::smem_u32(base);
-  float* W0 = reinterpret_cast<float*>(base + FS_W0);
-  float* bias = reinterpret_cast<float*>(base + FS_BIAS);
-  float* W4 = reinterpret_cast<float*>(base + FS_W4);
-  float* b4 = reinterpret_cast<float*>(base + FS_B4);
-  uint32_t* slot = reinterpret_cast<uint32_t*>(base + FS_SLOT);
-  const int g = threadIdx.x >> 7, t = threadIdx.x & 127, warp = t >> 5;
-  uint64_t* bar = reinterpret_cast<uint64_t*>(base + FS_BAR) + g;
-  int* s_ok = reinterpret_cast<int*>(base + FS_OK) + g;
-
-  // the three hidden-layer weight tiles (B operands: row = output, K = input)
-  for (int q = threadIdx.x; q < 3 * 2048; q += 128 * FG) {
-    const int l = q >> 11, r = (q >> 4) & 127, c = q & 15;
-    const uint4 v = reinterpret_cast<const uint4*>(Wb)[q];
-    *reinterpret_cast<uint4*>(base + l * TILE_BYTES + umma::sw128_offset(r, c * 8, 128)) = v;
-  }
-  for (int q = threadIdx.x; q < H * NIN; q += 128 * FG) W0[q] = params[OFF_W0 + q];
-  for (int q = threadIdx.x; q < H; q += 128 * FG) {
-    bias[q] = params[OFF_B0 + q];
-    for (int l = 1; l <= 3; ++l) bias[l * H + q] = params[off_b(l) + q];
-  }
-  for (int q = threadIdx.x; q < NOUT * H; q += 128 * FG) W4[q] = params[OFF_W4 + q];
-  if (threadIdx.x < NOUT) b4[threadIdx.x] = params[OFF_B4 + threadIdx.x];
-  if (t == 0) umma::mbar_init(bar, 1);
-  if (threadIdx.x < 32) {
-    umma::tmem_alloc(slot, FUSED_TMEM_COLS);
-    umma::tmem_relinquish();
-  }
-  umma::tc_fence_before();
-  __syncthreads();
-  umma::tc_fence_after();
-  const uint32_t tmem = *slot, tmem_g = tmem + (uint32_t)(g * 128);
-  const uint32_t act = sbase + FS_ACT + g * TILE_BYTES;
-  uint8_t* actp = base + FS_ACT + g * TILE_BYTES;
-  uint32_t phase = 0;
-  bool ok = true;
-  const int ntiles = (n + 127) / 128;
-  for (int tile = blockIdx.x * FG + g; tile < ntiles && ok; tile += gridDim.x * FG) {
-    const int s = tile * 128 + t;
-    float xn[NIN];
-    typename Io::Local loc;
-    io.load(s, s < n, nr, xn, loc);
-    // layer 0 on the CUDA cores -> row t of the group's activation tile
-    for (int c8 = 0; c8 < 16; ++c8) {
-      float a[8];
-#pragma unroll
-      for (int e = 0; e < 8; ++e) {
-        const int o = c8 * 8 + e;
-        float h = bias[o];
-#pragma unroll
-        for (int i = 0; i < NIN; ++i) h = fmaf(W0[o * NIN + i], xn[i], h);
-        a[e] = gelu(h);
-      }
-      *reinterpret_cast<uint4*>(actp + umma::sw128_offset(t, c8 * 8, 128)) = pack8(a);
-    }
-    float out[NOUT] = {0.f, 0.f, 0.f, 0.f};
-    for (int l = 1; l <= 3; ++l) {
-      umma::fence_async_smem();
-      umma::tc_fence_before();
-      group_sync(g);
-      if (t == 0) {
-        umma::tc_fence_after();
-#pragma unroll
-        for (int kk = 0; kk < 8; ++kk)
-          umma::mma_bf16(tmem_g, umma::sdesc_k(act, 128, kk), umma::sdesc_k(sbase + (l - 1) * TILE_BYTES, 128, kk),
-                         IDESC, kk > 0 ? 1u : 0u);
-        umma::mma_commit(bar);
-        *s_ok = umma::mbar_wait(bar, phase) ? 1 : 0;
-      }
-      group_sync(g);
-      phase ^= 1u;
-      umma::tc_fence_after();
-      if (!*s_ok) { ok = false; break; }
-      const float* bl = bias + l * H;
-      for (int c = 0; c < 4; ++c) {
-        float v[32];
-        umma::tmem_ld32(tmem_g + ((uint32_t)(warp * 32) << 16) + (uint32_t)(c * 32), v);
-        if (l < 3) {
-#pragma unroll
-          for (int c8 = 0; c8 < 4; ++c8) {
-            float a[8];
-#pragma unroll
-            for (int e = 0; e < 8; ++e) a[e] = gelu(v[c8 * 8 + e] + bl[c * 32 + c8 * 8 + e]);
-            *reinterpret_cast<uint4*>(actp + umma::sw128_offset(t, c * 32 + c8 * 8, 128)) = pack8(a);
-          }
-        } else {
-#pragma unroll
-          for (int j = 0; j < 32; ++j) {
-            const float a = gelu(v[j] + bl[c * 32 + j]);
-#pragma unroll
-            for (int m = 0; m < NOUT; ++m) out[m] = fmaf(a, W4[m * H + c * 32 + j], out[m]);
-          }
-        }
-      }
-    }
-    if (!ok) break;
-#pragma unroll
-    for (int m = 0; m < NOUT; ++m) out[m] += b4[m];
-    io.store(s, s < n, out, loc);
-  }
-  if (!ok && t == 0) atomicOr(err, ERR_SYNC);
-  umma::tc_fence_before();
-  __syncthreads();
-  if (threadIdx.x < 32) {
-    umma::tc_fence_after();
-    umma::tmem_dealloc(tmem, FUSED_TMEM_COLS);
-  }
 }
 
 // ------------------------------------------------ fused forward, all tcgen05
