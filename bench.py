@@ -286,6 +286,9 @@ def main():
     ap.add_argument("--tol", type=float, default=1e-8)
     ap.add_argument("--max-iters", type=int, default=40000)
     ap.add_argument("--every", type=int, default=10)
+    ap.add_argument("--mlp-infer", type=int, default=0,
+                    help="instead of the throughput line: the surrogate network's inference kernel alone on this "
+                         "many synthetic samples (10 timed calls), with its error against the FP64 reference")
     ap.add_argument("--dc-window", type=int, default=20,
                     help="norm reads without a 1%% improvement before the mixed form switches to defect correction")
     args = ap.parse_args()
@@ -313,6 +316,8 @@ def main():
 
     if args.converge:
         return converge(args, rc, torch)
+    if args.mlp_infer:
+        return mlp_infer(args, torch)
     torch.cuda.set_device(local)
     stream = torch.cuda.Stream(device=local)
     flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=f"cuda:{local}")
@@ -816,6 +821,44 @@ def surrogate_form(args, stream, flush, torch, rc, case, extra_pool=None):
     out["steady"] = forms
     ref.close()
     return out, net
+
+
+def mlp_infer(args, torch):
+    """Inference of the surrogate network (random weights, seed 3) on
+    `--mlp-infer` samples of a fixed synthetic spread of states: samples/s and
+    TFLOP/s over 10 CUDA-event-timed calls, and the largest output difference
+    from the FP64 reference forward (oracle/mlp_ref.py, no rounding) on 1,000
+    of them."""
+    from oracle import mlp_ref
+    from rocketcombustor_gb300 import surrogate
+    mean = np.array([0.6, 6.0, -1.8, -1.8, -0.05, -2.3, -7.0], dtype=np.float32)
+    std = np.array([0.5, 0.7, 0.5, 0.5, 0.02, 0.8, 1.2], dtype=np.float32)
+    rng = np.random.default_rng(9)
+    n = args.mlp_infer
+    x = np.stack([rng.uniform(300, 3800, n), 10 ** rng.uniform(4.7, 7, n), rng.uniform(0, .05, n),
+                  rng.uniform(0, .05, n), rng.uniform(.85, .95, n), rng.uniform(0, .02, n),
+                  10 ** rng.uniform(-9, -5, n)], 1).astype(np.float32)
+    net = surrogate.MLP(seed=3)
+    net.set_norm(mean, std)
+    xd = torch.tensor(x, device="cuda")
+    y = net.forward(xd[:1000]).cpu().numpy()
+    yr, _ = mlp_ref.forward(net.get_params(), x[:1000], mean, std, bf=False)
+    net.forward(xd)
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record()
+    for _ in range(10):
+        net.forward(xd)
+    e1.record()
+    torch.cuda.synchronize()
+    t = e0.elapsed_time(e1) / 1e3 / 10
+    flops = 2 * (7 * 128 + 3 * 128 * 128 + 128 * 4)
+    print(json.dumps({"mode": "mlp_infer", "samples": n, "samples_per_s": n / t,
+                      "tflops": flops * n / t / 1e12, "peak_bf16_tflops": read_peaks_tensor(),
+                      "max_abs_err_vs_fp64": float(np.abs(y - yr).max()), "output_scale": float(np.abs(yr).max())}),
+          flush=True)
+    net.close()
+    return 0
 
 
 def read_peaks_tensor():

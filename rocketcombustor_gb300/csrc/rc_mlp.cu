@@ -100,13 +100,14 @@ __device__ __forceinline__ void group_sync(int g) {
 }
 
 // ------------------------------------------------ fused forward, all tcgen05
-// Every layer on the tensor cores with F16 operands and FP32 accumulators in
-// TMEM: layer 0 as one K = 16 step (the 7 features padded with zeros), the
-// three hidden layers as 8 K-steps, the output layer as N = 16 (4 outputs
-// padded).  The epilogue of each layer adds the FP32 bias, converts pairs to
-// f16x2 and evaluates the tanh form of GELU on packed halves (2 values per
+// Every layer on the tensor cores with F16 operands: layer 0 as one K = 16
+// step (the 7 features padded with zeros), the three hidden layers as 8
+// K-steps, the output layer as N = 16 (4 outputs padded).  Layers 0-3
+// accumulate in F16 in TMEM, read back two columns per register
+// (tcgen05.ld .pack::16b), so the epilogue needs no conversion: it adds the
+// bias and evaluates the tanh form of GELU on packed halves (2 values per
 // instruction, hardware tanh on f16x2), writing the next layer's A operand
-// directly.  F16 keeps 11 significant bits where BF16 keeps 8, so the
+// directly; the output layer accumulates in FP32.  F16 keeps 11 significant bits where BF16 keeps 8, so the
 // activations are closer to FP32 than the training forward's BF16 ones.
 // The weights come pre-swizzled in F16 (k_pack16), in the shared-memory order
 // of the kernel: hidden tiles 1..3, the layer-0 tile (128 rows, K columns 0-15
@@ -117,11 +118,13 @@ __device__ __forceinline__ void group_sync(int g) {
 constexpr int W0_TILE_BYTES = 128 * 128, W4_TILE_BYTES = 16 * 128 * 2;
 constexpr int WH_BYTES = 3 * TILE_BYTES + W0_TILE_BYTES + W4_TILE_BYTES;  // 118784
 constexpr int F2_W0 = 3 * TILE_BYTES, F2_W4 = F2_W0 + W0_TILE_BYTES, F2_ACT = F2_W4 + W4_TILE_BYTES;
-constexpr int F2_BIAS = F2_ACT + FG * TILE_BYTES;  // b0..b3 then b4 (16 floats)
-constexpr int F2_BAR = F2_BIAS + (4 * H + 16) * 4;
+constexpr int F2_BIAS = F2_ACT + FG * TILE_BYTES;  // b0..b3 as f16x2 pairs (4 x 64), then b4 (16 floats)
+constexpr int F2_BAR = F2_BIAS + (4 * H / 2 + 16) * 4;
 constexpr int F2_SLOT = F2_BAR + 8 * FG, F2_OK = F2_SLOT + 4;
 constexpr int F2_SMEM = F2_OK + 4 * FG + 1024;
-constexpr uint32_t IDESC_H = umma::idesc_f16(128, 128), IDESC_H16 = umma::idesc_f16(128, 16);
+// layers 0-3 accumulate in F16 (read back two columns per register, no
+// conversion), the output layer in FP32
+constexpr uint32_t IDESC_H = umma::idesc_f16_acc16(128, 128), IDESC_H16 = umma::idesc_f16(128, 16);
 static_assert(F2_ACT % 1024 == 0 && F2_W0 % 1024 == 0 && F2_W4 % 1024 == 0, "tile alignment");
 static_assert(F2_BAR % 8 == 0, "mbarrier alignment");
 static_assert(F2_SMEM <= 227 * 1024, "shared memory");
@@ -136,12 +139,12 @@ __device__ __forceinline__ uint32_t pack_h2(float a, float b) {
   asm("cvt.rn.f16x2.f32 %0, %1, %2;" : "=r"(x) : "f"(b), "f"(a));
   return x;
 }
-// GELU (tanh form) of two FP32 pre-activations on packed halves:
+// GELU (tanh form) of a packed pair of pre-activations acc + bias:
 // 0.5 x (1 + tanh(x (k0 + k0 k1 x^2)))
-__device__ __forceinline__ uint32_t gelu_h2(float a, float b) {
+__device__ __forceinline__ uint32_t gelu_h2(uint32_t acc, uint32_t bias) {
   const uint32_t c0 = h2_bits(GK0), c1 = h2_bits(GK0 * GK1), half = h2_bits(0.5f);
   uint32_t x, x2, p, u, t, hx, g;
-  asm("cvt.rn.satfinite.f16x2.f32 %0, %1, %2;" : "=r"(x) : "f"(b), "f"(a));
+  asm("add.rn.f16x2 %0, %1, %2;" : "=r"(x) : "r"(acc), "r"(bias));
   asm("mul.rn.f16x2 %0, %1, %1;" : "=r"(x2) : "r"(x));
   asm("fma.rn.f16x2 %0, %1, %2, %3;" : "=r"(p) : "r"(x2), "r"(c1), "r"(c0));
   asm("mul.rn.f16x2 %0, %1, %2;" : "=r"(u) : "r"(x), "r"(p));
@@ -157,17 +160,18 @@ __global__ void __launch_bounds__(128 * FG, 1) k_mlp_fwd16(const uint4* __restri
   extern __shared__ uint8_t smem_raw[];
   uint8_t* base = smem_raw + ((1024u - (umma::smem_u32(smem_raw) & 1023u)) & 1023u);
   const uint32_t sbase = umma::smem_u32(base);
-  float* bias = reinterpret_cast<float*>(base + F2_BIAS);
+  uint32_t* bias2 = reinterpret_cast<uint32_t*>(base + F2_BIAS);  // [4][64] f16x2
+  float* bias4 = reinterpret_cast<float*>(base + F2_BIAS) + 4 * H / 2;
   uint32_t* slot = reinterpret_cast<uint32_t*>(base + F2_SLOT);
   const int g = threadIdx.x >> 7, t = threadIdx.x & 127, warp = t >> 5;
   uint64_t* bar = reinterpret_cast<uint64_t*>(base + F2_BAR) + g;
   int* s_ok = reinterpret_cast<int*>(base + F2_OK) + g;
   for (int q = threadIdx.x; q < WH_BYTES / 16; q += 128 * FG) reinterpret_cast<uint4*>(base)[q] = Wh[q];
-  for (int q = threadIdx.x; q < H; q += 128 * FG) {
-    bias[q] = params[OFF_B0 + q];
-    for (int l = 1; l <= 3; ++l) bias[l * H + q] = params[off_b(l) + q];
+  for (int q = threadIdx.x; q < H / 2; q += 128 * FG) {
+    bias2[q] = pack_h2(params[OFF_B0 + 2 * q], params[OFF_B0 + 2 * q + 1]);
+    for (int l = 1; l <= 3; ++l) bias2[l * H / 2 + q] = pack_h2(params[off_b(l) + 2 * q], params[off_b(l) + 2 * q + 1]);
   }
-  if (threadIdx.x < 16) bias[4 * H + threadIdx.x] = threadIdx.x < NOUT ? params[OFF_B4 + threadIdx.x] : 0.f;
+  if (threadIdx.x < 16) bias4[threadIdx.x] = threadIdx.x < NOUT ? params[OFF_B4 + threadIdx.x] : 0.f;
   if (t == 0) umma::mbar_init(bar, 1);
   if (threadIdx.x < 32) {
     umma::tmem_alloc(slot, FUSED_TMEM_COLS);
@@ -201,18 +205,15 @@ __global__ void __launch_bounds__(128 * FG, 1) k_mlp_fwd16(const uint4* __restri
     return *s_ok != 0;
   };
   // bias + GELU of the accumulator row t -> row t of the activation tile
-  auto epilogue = [&](const float* bl) {
+  auto epilogue = [&](const uint32_t* bl) {
     for (int c = 0; c < 4; ++c) {
-      float v[32];
-      umma::tmem_ld32(trow + (uint32_t)(c * 32), v);
+      uint32_t v[16];
+      umma::tmem_ld32_pack16(trow + (uint32_t)(c * 32), v);
 #pragma unroll
       for (int c8 = 0; c8 < 4; ++c8) {
         uint32_t h[4];
 #pragma unroll
-        for (int e = 0; e < 4; ++e) {
-          const int j = c8 * 8 + 2 * e;
-          h[e] = gelu_h2(v[j] + bl[c * 32 + j], v[j + 1] + bl[c * 32 + j + 1]);
-        }
+        for (int e = 0; e < 4; ++e) h[e] = gelu_h2(v[c8 * 4 + e], bl[c * 16 + c8 * 4 + e]);
         *reinterpret_cast<uint4*>(actp + umma::sw128_offset(t, c * 32 + c8 * 8, 128)) =
             make_uint4(h[0], h[1], h[2], h[3]);
       }
@@ -229,16 +230,16 @@ __global__ void __launch_bounds__(128 * FG, 1) k_mlp_fwd16(const uint4* __restri
         make_uint4(pack_h2(xn[0], xn[1]), pack_h2(xn[2], xn[3]), pack_h2(xn[4], xn[5]), pack_h2(xn[6], 0.f));
     *reinterpret_cast<uint4*>(actp + umma::sw128_offset(t, 8, 128)) = make_uint4(0u, 0u, 0u, 0u);
     if (!(ok = mma(1, sbase + F2_W0, 128, IDESC_H))) break;
-    epilogue(bias);
+    epilogue(bias2);
     for (int l = 1; l <= 3 && ok; ++l) {
       if (!(ok = mma(8, sbase + (l - 1) * TILE_BYTES, 128, IDESC_H))) break;
-      epilogue(bias + l * H);
+      epilogue(bias2 + l * H / 2);
     }
     if (!ok || !(ok = mma(8, sbase + F2_W4, 16, IDESC_H16))) break;
     float v[32], out[NOUT];
     umma::tmem_ld32(trow, v);
 #pragma unroll
-    for (int m = 0; m < NOUT; ++m) out[m] = v[m] + bias[4 * H + m];
+    for (int m = 0; m < NOUT; ++m) out[m] = v[m] + bias4[m];
     io.store(s, s < n, out, loc);
   }
   if (!ok && t == 0) atomicOr(err, ERR_SYNC);
