@@ -845,14 +845,20 @@ __device__ __forceinline__ Fin4w fin_load(const Dev& d, int ft, int t1) {
 // lane = 4 cell + slot): p is the thread's (cell, slot) data from sweep_load,
 // nbv the hWA of its neighbour (V values; unused when the slot is inactive),
 // fn the data of the cell it finishes (warps 0 and 1, 8 lanes per cell).
-// Named barriers 5, 6 and 7 (warps 0-3) are used.
-template <int NSP, bool FWD, bool L2>
+// A block may hold NG such groups of four warps (threads 128 g .. 128 g +
+// 127), each with its own shared scratch and named barriers 5 + 3g, 6 + 3g
+// and 7 + 3g.
+template <int NSP, bool FWD, bool L2, int NG = 1>
 __device__ __forceinline__ void sweep4w_compute(const Dev& d, const ThermoDev<NSP>& th, const SweepPre<NSP>& p,
                                                 const double* nbv, const Fin4w& fn) {
   constexpr int V = 3 + NSP;
-  const int NE = d.NE, role = threadIdx.x >> 5, lane = threadIdx.x & 31, cell = lane >> 2, q = lane & 3;
-  __shared__ double wsm[8 * V * 4];
-  __shared__ double xs1[32], xq[32], xdp[32], xdu[32], xdv[32], xdn[32];
+  const int NE = d.NE, gi = NG > 1 ? (int)(threadIdx.x >> 7) : 0, role = (threadIdx.x >> 5) & 3,
+            lane = threadIdx.x & 31, cell = lane >> 2, q = lane & 3;
+  __shared__ double wsm_g[NG][8 * V * 4];
+  __shared__ double xs1_g[NG][32], xq_g[NG][32], xdp_g[NG][32], xdu_g[NG][32], xdv_g[NG][32], xdn_g[NG][32];
+  double* wsm = wsm_g[gi];
+  double *xs1 = xs1_g[gi], *xq = xq_g[gi], *xdp = xdp_g[gi], *xdu = xdu_g[gi], *xdv = xdv_g[gi], *xdn = xdn_g[gi];
+  const int b5 = 5 + 3 * gi, b6 = 6 + 3 * gi, b7 = 7 + 3 * gi;
   const int fcell = (role & 1) * 4 + (lane >> 3), r = lane & 7;
   const bool fvalid = role < 2 && fn.i >= 0 && r < V;
   const int fi = fvalid ? fn.i : 0;
@@ -891,7 +897,7 @@ __device__ __forceinline__ void sweep4w_compute(const Dev& d, const ThermoDev<NS
   } else {
     if (p.act) xdv[lane] = div_rn(drv - p.vv * drr, p.rr, p.rrh, p.rrl);
   }
-  bar_named(5, 128);
+  bar_named(b5, 128);
   // B
   if (role == 3) {
     double dunormal = 0.0;
@@ -899,7 +905,7 @@ __device__ __forceinline__ void sweep4w_compute(const Dev& d, const ThermoDev<NS
       dunormal = xdu[lane] * p.dx + xdv[lane] * p.dy;
       xdn[lane] = dunormal;
     }
-    bar_arrive(6, 128);
+    bar_arrive(b6, 128);
 #pragma unroll
     for (int k = 0; k < NSP - 1; ++k)
       w[(4 + k) * 4 + q] = p.act ? 0.5 * (-aF * dry[k] + dry[k] * unormal + p.ry[k] * dunormal) : 0.0;
@@ -909,7 +915,7 @@ __device__ __forceinline__ void sweep4w_compute(const Dev& d, const ThermoDev<NS
       const double X = dru * p.uu + duu * p.rou + drv * p.vv + dvv * p.rov;
       xdp[lane] = p.gm1 * (dre - xs1[lane] + xq[lane] - 0.5 * X);
     }
-    bar_named(6, 128);
+    bar_named(b6, 128);
     // C
     double ck = 0.0;
     if (p.act) {
@@ -920,7 +926,7 @@ __device__ __forceinline__ void sweep4w_compute(const Dev& d, const ThermoDev<NS
     }
     w[(1 + role) * 4 + q] = ck;
   }
-  bar_named(7, 128);
+  bar_named(b7, 128);
   if (!fvalid) return;
   const double* wf = wsm + fcell * V * 4;
   double df = 0.0;
@@ -947,8 +953,9 @@ __global__ void __launch_bounds__(128) k_sweep4w(const Dev d, const ThermoDev<NS
 // runs its forward passes, then its backward passes, in level order.  A pass
 // waits (bounded) only for the passes of other blocks that hold its lower
 // (forward) or upper (backward) neighbours; neighbours in the block itself
-// were done by an earlier pass.  Warps 0-3 compute the passes (the four-warp
-// step of k_sweep4w, hWA read through L2); warp 4 runs one pass ahead of them:
+// were done by an earlier pass.  Warps 0-3 of each compute group compute the
+// passes (the four-warp step of k_sweep4w, hWA read through L2); the last warp
+// runs one pass ahead of them:
 // while they compute it stages the next pass's sweep_load data in shared
 // memory and looks once at the flags that pass waits for; when they are done
 // (barrier 4) it hands the next pass over (barrier 3) at once if those flags
@@ -959,12 +966,24 @@ __global__ void __launch_bounds__(128) k_sweep4w(const Dev d, const ThermoDev<NS
 // reset between launches.  After a failed wait (ERR_SYNC latched) no flag is
 // published any more and every block runs to the end.  The Newton update
 // follows as its own launch.
-constexpr int FLOW_THREADS = 160;
-template <int NSP>
-__global__ void __launch_bounds__(FLOW_THREADS) k_lusgs_flow(const Dev d, const ThermoDev<NSP> th, const FlowDev f) {
-  constexpr int V = 3 + NSP;
-  __shared__ SweepPre<NSP> s_pre[2][32];
-  __shared__ Fin4w s_fin[2][8];
+// With G groups a pass holds up to 8 G consecutive positions: G groups of
+// four compute warps each take 8 of them (a group without cells in the pass
+// only joins the hand-over), and the last warp stages all of them.  On a wide
+// mesh a block's cells of one level then form one pass instead of several
+// (the 2,000,000-cell nozzle: 6,689 protocol steps with G = 1, 4,420 with 2,
+// 2,402 = its levels with 3).  G = 3 has 13 warps, 4 of them on one SM
+// sub-partition, which caps a thread at 128 registers (the kernel spills);
+// rc_autotune picks G.
+constexpr int FLOW_GMAX = 3;
+__host__ __device__ constexpr int flow_threads(int G) { return 128 * G + 32; }
+template <int NSP, int G>
+constexpr int flow_dsmem() { return (int)(2 * 32 * G * sizeof(SweepPre<NSP>)); }
+template <int NSP, int G>
+__global__ void __launch_bounds__(flow_threads(G), 1) k_lusgs_flow(const Dev d, const ThermoDev<NSP> th, const FlowDev f) {
+  constexpr int V = 3 + NSP, FLOW_G = G, FLOW_THREADS = flow_threads(G);
+  extern __shared__ __align__(16) uint8_t flow_smem[];
+  SweepPre<NSP>(*s_pre)[32 * FLOW_G] = reinterpret_cast<SweepPre<NSP>(*)[32 * FLOW_G]>(flow_smem);
+  __shared__ Fin4w s_fin[2][8 * FLOW_G];
   __shared__ unsigned s_epoch;
   __shared__ int s_bad;
   if (threadIdx.x == 0) {
@@ -977,19 +996,23 @@ __global__ void __launch_bounds__(FLOW_THREADS) k_lusgs_flow(const Dev d, const 
   const int f0 = f.boff[0][b], b0 = f.boff[1][b];
   const int nf = f.boff[0][b + 1] - f0, n = nf + (f.boff[1][b + 1] - b0);
   auto pass_of = [&](int k) { return k < nf ? f.blist[0][f0 + k] : f.blist[1][b0 + k - nf]; };
-  if (threadIdx.x >= 128) {
+  if (threadIdx.x >= 128 * FLOW_G) {
     // the data of pass k that the sweep does not change
     auto stage = [&](int k) {
       const int pz = pass_of(k), t0 = f.pstart[pz], t1 = t0 + f.pcount[pz];
-      SweepPre<NSP> pl;
-      if (k < nf) {
-        pl = sweep_load<NSP, true>(d, t0 + (lane >> 2), t1, lane & 3);
-        if (lane < 8) s_fin[k & 1][lane] = fin_load<true>(d, t0 + lane, t1);
-      } else {
-        pl = sweep_load<NSP, false>(d, t0 + (lane >> 2), t1, lane & 3);
-        if (lane < 8) s_fin[k & 1][lane] = fin_load<false>(d, t0 + lane, t1);
+#pragma unroll
+      for (int g = 0; g < FLOW_G; ++g) {
+        const int tg = t0 + 8 * g;
+        SweepPre<NSP> pl;
+        if (k < nf) {
+          pl = sweep_load<NSP, true>(d, tg + (lane >> 2), t1, lane & 3);
+          if (lane < 8) s_fin[k & 1][8 * g + lane] = fin_load<true>(d, tg + lane, t1);
+        } else {
+          pl = sweep_load<NSP, false>(d, tg + (lane >> 2), t1, lane & 3);
+          if (lane < 8) s_fin[k & 1][8 * g + lane] = fin_load<false>(d, tg + lane, t1);
+        }
+        s_pre[k & 1][32 * g + lane] = pl;
       }
-      s_pre[k & 1][lane] = pl;
     };
     auto poll = [&](int k) {
       if (s_bad) return;
@@ -1030,16 +1053,20 @@ __global__ void __launch_bounds__(FLOW_THREADS) k_lusgs_flow(const Dev d, const 
       }
     }
   } else {
-    const int role = threadIdx.x >> 5;
+    const int gi = threadIdx.x >> 7, role = (threadIdx.x >> 5) & 3;
     for (int k = 0; k < n; ++k) {
       bar_named(3, FLOW_THREADS);
-      const SweepPre<NSP> p = s_pre[k & 1][lane];
-      const Fin4w fn = s_fin[k & 1][(role & 1) * 4 + (lane >> 3)];
-      double nbv[V];
+      // the group's first position holds a cell iff the group has work in
+      // this pass; all 128 threads of the group read the same entry
+      if (s_fin[k & 1][8 * gi].i >= 0) {
+        const SweepPre<NSP> p = s_pre[k & 1][32 * gi + lane];
+        const Fin4w fn = s_fin[k & 1][8 * gi + (role & 1) * 4 + (lane >> 3)];
+        double nbv[V];
 #pragma unroll
-      for (int v = 0; v < V; ++v) nbv[v] = p.act ? __ldcg(d.hWA + (size_t)v * d.NE + p.j) : 0.0;
-      if (k < nf) sweep4w_compute<NSP, true, true>(d, th, p, nbv, fn);
-      else sweep4w_compute<NSP, false, true>(d, th, p, nbv, fn);
+        for (int v = 0; v < V; ++v) nbv[v] = p.act ? __ldcg(d.hWA + (size_t)v * d.NE + p.j) : 0.0;
+        if (k < nf) sweep4w_compute<NSP, true, true, FLOW_G>(d, th, p, nbv, fn);
+        else sweep4w_compute<NSP, false, true, FLOW_G>(d, th, p, nbv, fn);
+      }
       bar_arrive(4, FLOW_THREADS);
     }
   }
@@ -1250,10 +1277,12 @@ struct rc_ctx {
                                 // the two parts of a slot in two warps (2, k_sweep2w) or four (3, k_sweep4w);
                                 // 4: the dataflow launches k_lusgs_flow / k_lusgs_flow32 (where they
                                 // cannot run: as 3 for FP64, the per-level sweeps for the mixed forms)
-  bool can_flow = false;        // the device can co-schedule the k_lusgs_flow grid
+  bool can_flow[FLOW_GMAX] = {};  // the device can co-schedule the k_lusgs_flow grid (per G)
   bool can_flow32 = false;      // ... and the k_lusgs_flow32 grid (mixed forms)
   int flow_grid = 0;            // its blocks (one per SM)
-  FlowDev flow = {};            // its pass tables
+  FlowDev flows[FLOW_GMAX] = {};  // its pass tables for G = 1..3 groups (passes of up to 8 G cells;
+                                  // G = 1 is also the mixed forms' k_lusgs_flow32)
+  int flow_g = 1;                 // the groups of the FP64 dataflow launch
   int pers_grid = 0;             // blocks of the persistent launch (one per SM)
   unsigned* lvl_count = nullptr; // per-level completion counters of the persistent launch
   int nlevels = 0;
@@ -1387,8 +1416,9 @@ SweepOrder sweep_order(int NE, const NF& nface, const std::vector<int>& cother) 
   return so;
 }
 // The dataflow schedule (k_lusgs_flow) over G blocks: block b owns the cells
-// [b*C, (b+1)*C), C = ceil(NE/G); a pass is a run of at most 8 consecutive
-// positions of one level whose cells one block owns; a block's passes are
+// [b*C, (b+1)*C), C = ceil(NE/G); a pass is a run of at most `width`
+// consecutive positions of one level whose cells one block owns (24 for the
+// FP64 launch, three groups of 8; 8 for the mixed forms'); a block's passes are
 // listed forward then backward in level order; a pass depends on the passes
 // (same sweep) of the neighbours it reads that other blocks own.
 struct FlowPlan {
@@ -1398,7 +1428,8 @@ struct FlowPlan {
   std::vector<int> cellpass[2];
 };
 template <class NF>
-FlowPlan flow_plan(int NE, int G, const NF& nface, const std::vector<int>& cother, const SweepOrder& so) {
+FlowPlan flow_plan(int NE, int G, const NF& nface, const std::vector<int>& cother, const SweepOrder& so,
+                   int width = 8) {
   FlowPlan fp;
   fp.C = (NE + G - 1) / G;
   const int C = fp.C;
@@ -1412,7 +1443,7 @@ FlowPlan flow_plan(int NE, int G, const NF& nface, const std::vector<int>& cothe
       for (int t = off[l]; t < off[l + 1];) {
         const int own = lst[t] / C;
         int e = t + 1;
-        while (e < off[l + 1] && e - t < 8 && lst[e] / C == own) ++e;
+        while (e < off[l + 1] && e - t < width && lst[e] / C == own) ++e;
         const int pz = (int)fp.pstart.size();
         fp.pstart.push_back(t); fp.pcount.push_back(e - t); fp.pdir.push_back(dir); fp.powner.push_back(own);
         fp.plevel.push_back((int)l);
@@ -1538,18 +1569,25 @@ void q_persistent(rc_ctx* c) {
                      c->lvl_count);
   c->launches++;
 }
-template <int NSP>
-void q_flow(rc_ctx* c) {
+template <int NSP, int G>
+void q_flow_g(rc_ctx* c) {
   cudaLaunchConfig_t cfg = {};
   cfg.gridDim = dim3((unsigned)c->flow_grid);
-  cfg.blockDim = dim3(FLOW_THREADS);
+  cfg.blockDim = dim3(flow_threads(G));
+  cfg.dynamicSmemBytes = (size_t)flow_dsmem<NSP, G>();
   cfg.stream = c->stream;
   cudaLaunchAttribute attr[1];
   attr[0].id = cudaLaunchAttributeCooperative;
   attr[0].val.cooperative = 1;
   cfg.attrs = attr;
   cfg.numAttrs = 1;
-  cudaLaunchKernelEx(&cfg, k_lusgs_flow<NSP>, c->d, TH<NSP>(c), c->flow);
+  cudaLaunchKernelEx(&cfg, k_lusgs_flow<NSP, G>, c->d, TH<NSP>(c), c->flows[G - 1]);
+}
+template <int NSP>
+void q_flow(rc_ctx* c) {
+  if (c->flow_g == 3) q_flow_g<NSP, 3>(c);
+  else if (c->flow_g == 2) q_flow_g<NSP, 2>(c);
+  else q_flow_g<NSP, 1>(c);
   c->launches++;
   launch_pdl(k_update<NSP>, blocks(c->NE, c->d.bs), c->d.bs, c->stream, c->d, TH<NSP>(c));
   c->launches++;
@@ -1561,7 +1599,7 @@ void q_sweeps(rc_ctx* c, int gather) {
     c->launches++;
   }
   if (c->persistent) { q_persistent<NSP>(c); return; }
-  if (c->wide == 4 && c->can_flow) { q_flow<NSP>(c); return; }
+  if (c->wide == 4 && c->can_flow[c->flow_g - 1]) { q_flow<NSP>(c); return; }
   for (size_t l = 0; l + 1 < c->fwd_off.size(); ++l) {
     const int n = c->fwd_off[l + 1] - c->fwd_off[l];
     if (c->wide >= 3) launch_pdl(k_sweep4w<NSP, true>, blocks(n, 8), 128, c->stream, c->d, TH<NSP>(c),
@@ -1626,7 +1664,7 @@ template <int NSP>
 void q_sweeps32(rc_ctx* c) {
   if (!c->persistent && c->wide == 4 && c->can_flow32) {
     // the Newton update runs inside the dataflow launch
-    mixed_lusgs_flow<NSP>(c->d, c->thermo32.data(), c->thermo.data(), c->flow, c->flow_grid, c->stream);
+    mixed_lusgs_flow<NSP>(c->d, c->thermo32.data(), c->thermo.data(), c->flows[0], c->flow_grid, c->stream);
     c->launches += 1;
     return;
   }
@@ -2178,26 +2216,28 @@ int init_impl(const rc_mesh* m, const rc_thermo* t, const rc_config* g, const Ba
     int nsm = 0;
     cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, g->device);
     const int G = std::max(nsm, 1);
-    FlowPlan fp = flow_plan(NE, G, nface, cother, so);
-    std::vector<int>& pstart = fp.pstart;
-    std::vector<int>& pcount = fp.pcount;
-    std::vector<int>& doff = fp.doff;
-    std::vector<int>& deps = fp.deps;
-    std::vector<int>* boff = fp.boff;
-    std::vector<int>* blist = fp.blist;
-    FlowDev& f = c->flow;
-    int* ip;
-    st |= dev_upload(c, pstart, &ip); f.pstart = ip;
-    st |= dev_upload(c, pcount, &ip); f.pcount = ip;
-    for (int dir = 0; dir < 2; ++dir) {
-      st |= dev_upload(c, boff[dir], &ip); f.boff[dir] = ip;
-      st |= dev_upload(c, blist[dir], &ip); f.blist[dir] = ip;
+    for (int gr = 1; gr <= FLOW_GMAX; ++gr) {
+      FlowPlan fp = flow_plan(NE, G, nface, cother, so, 8 * gr);
+      std::vector<int>& pstart = fp.pstart;
+      std::vector<int>& pcount = fp.pcount;
+      std::vector<int>& doff = fp.doff;
+      std::vector<int>& deps = fp.deps;
+      std::vector<int>* boff = fp.boff;
+      std::vector<int>* blist = fp.blist;
+      FlowDev& f = c->flows[gr - 1];
+      int* ip;
+      st |= dev_upload(c, pstart, &ip); f.pstart = ip;
+      st |= dev_upload(c, pcount, &ip); f.pcount = ip;
+      for (int dir = 0; dir < 2; ++dir) {
+        st |= dev_upload(c, boff[dir], &ip); f.boff[dir] = ip;
+        st |= dev_upload(c, blist[dir], &ip); f.blist[dir] = ip;
+      }
+      st |= dev_upload(c, doff, &ip); f.doff = ip;
+      if (deps.empty()) deps.push_back(0);
+      st |= dev_upload(c, deps, &ip); f.deps = ip;
+      st |= dev_upload(c, std::vector<unsigned>(pstart.size() + 1, 0u), &f.pflag);
+      st |= dev_upload(c, std::vector<unsigned>(2, 0u), &f.ctr);
     }
-    st |= dev_upload(c, doff, &ip); f.doff = ip;
-    if (deps.empty()) deps.push_back(0);
-    st |= dev_upload(c, deps, &ip); f.deps = ip;
-    st |= dev_upload(c, std::vector<unsigned>(pstart.size() + 1, 0u), &f.pflag);
-    st |= dev_upload(c, std::vector<unsigned>(2, 0u), &f.ctr);
     c->flow_grid = G;
   }
   {  // boundary data per case, case layout
@@ -2238,9 +2278,23 @@ int init_impl(const rc_mesh* m, const rc_thermo* t, const rc_config* g, const Ba
     const std::string sc = sched ? sched : "";
     c->persistent = c->can_persistent && sc == "persistent";
     c->wide = sc == "levels" ? 0 : sc == "levels8" ? 1 : sc == "levels2w" ? 2 : sc == "levels4w" ? 3 : 4;
-    if (c->NSP == 1) cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ64, k_lusgs_flow<1>, FLOW_THREADS, 0);
-    else cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ64, k_lusgs_flow<4>, FLOW_THREADS, 0);
-    c->can_flow = coop && nsm > 0 && occ64 >= 1 && c->flow_grid == nsm;
+    c->flow_g = sc == "flow3" ? 3 : sc == "flow2" ? 2 : 1;
+    auto occ_flow = [&](auto kern, int threads, int dsmem) {
+      int o = 0;
+      cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, dsmem);
+      cudaOccupancyMaxActiveBlocksPerMultiprocessor(&o, kern, threads, dsmem);
+      return coop && nsm > 0 && o >= 1 && c->flow_grid == nsm;
+    };
+    if (c->NSP == 1) {
+      c->can_flow[0] = occ_flow(k_lusgs_flow<1, 1>, flow_threads(1), flow_dsmem<1, 1>());
+      c->can_flow[1] = occ_flow(k_lusgs_flow<1, 2>, flow_threads(2), flow_dsmem<1, 2>());
+      c->can_flow[2] = occ_flow(k_lusgs_flow<1, 3>, flow_threads(3), flow_dsmem<1, 3>());
+    } else {
+      c->can_flow[0] = occ_flow(k_lusgs_flow<4, 1>, flow_threads(1), flow_dsmem<4, 1>());
+      c->can_flow[1] = occ_flow(k_lusgs_flow<4, 2>, flow_threads(2), flow_dsmem<4, 2>());
+      c->can_flow[2] = occ_flow(k_lusgs_flow<4, 3>, flow_threads(3), flow_dsmem<4, 3>());
+    }
+    cudaGetLastError();  // an attribute or occupancy query that failed leaves can_flow false
     occ32 = c->NSP == 1 ? mixed_flow_occupancy<1>() : mixed_flow_occupancy<4>();
     c->can_flow32 = coop && nsm > 0 && occ32 >= 1 && c->flow_grid == nsm;
   }
@@ -2250,21 +2304,10 @@ int init_impl(const rc_mesh* m, const rc_thermo* t, const rc_config* g, const Ba
 
 }  // namespace
 
-extern "C" {
-
-int rc_flow_plan_check(int ne, int nblocks, const int* nface, const int* cother, long long* stats) {
-  if (ne < 1 || nblocks < 1 || !nface || !cother || !stats) return RC_ERR_ARG;
-  std::vector<int> nf(nface, nface + ne);
-  std::vector<int> co(cother, cother + 4 * (size_t)ne);
-  for (int i = 0; i < ne; ++i) {
-    if (nf[i] < 0 || nf[i] > 4) return RC_ERR_ARG;
-    for (int q = 0; q < nf[i]; ++q) {
-      const int j = co[(size_t)q * ne + i];
-      if (j < -1 || j >= ne || j == i) return RC_ERR_ARG;
-    }
-  }
-  const SweepOrder so = sweep_order(ne, nf, co);
-  const FlowPlan fp = flow_plan(ne, nblocks, nf, co, so);
+// The plan with passes of up to `width` positions; stats as rc_flow_plan_check.
+int flow_plan_check_width(int ne, int nblocks, const std::vector<int>& nf, const std::vector<int>& co,
+                          const SweepOrder& so, int width, long long* stats) {
+  const FlowPlan fp = flow_plan(ne, nblocks, nf, co, so, width);
   const int P = (int)fp.pstart.size(), C = fp.C;
   bool ok = true;
   long long npass[2] = {0, 0}, maxdep = 0;
@@ -2276,7 +2319,7 @@ int rc_flow_plan_check(int ne, int nblocks, const int* nface, const int* cother,
       if (fp.pdir[pz] != dir) continue;
       ++npass[dir];
       const int l = fp.plevel[pz], t0 = fp.pstart[pz], n = fp.pcount[pz];
-      if (n < 1 || n > 8 || t0 < so.off[dir][l] || t0 + n > so.off[dir][l + 1]) ok = false;
+      if (n < 1 || n > width || t0 < so.off[dir][l] || t0 + n > so.off[dir][l + 1]) ok = false;
       for (int u = t0; u < t0 + n && ok; ++u) {
         const int i = so.cells[dir][u];
         if (i / C != fp.powner[pz] || fp.cellpass[dir][i] != pz) ok = false;
@@ -2354,6 +2397,25 @@ int rc_flow_plan_check(int ne, int nblocks, const int* nface, const int* cother,
   stats[6] = (long long)so.off[1].size() - 1;
   stats[7] = C;
   return ok ? RC_OK : RC_ERR_SYNC;
+}
+
+extern "C" {
+
+int rc_flow_plan_check(int ne, int nblocks, const int* nface, const int* cother, long long* stats) {
+  if (ne < 1 || nblocks < 1 || !nface || !cother || !stats) return RC_ERR_ARG;
+  std::vector<int> nf(nface, nface + ne);
+  std::vector<int> co(cother, cother + 4 * (size_t)ne);
+  for (int i = 0; i < ne; ++i) {
+    if (nf[i] < 0 || nf[i] > 4) return RC_ERR_ARG;
+    for (int q = 0; q < nf[i]; ++q) {
+      const int j = co[(size_t)q * ne + i];
+      if (j < -1 || j >= ne || j == i) return RC_ERR_ARG;
+    }
+  }
+  const SweepOrder so = sweep_order(ne, nf, co);
+  int st = RC_OK;
+  for (int gr = FLOW_GMAX; gr >= 1 && st == RC_OK; --gr) st = flow_plan_check_width(ne, nblocks, nf, co, so, 8 * gr, stats);
+  return st;
 }
 
 int rc_init(const rc_mesh* m, const rc_thermo* t, const rc_config* g, rc_ctx** out) {
@@ -2559,26 +2621,37 @@ int rc_autotune(rc_ctx* c, int iters, char* report, int report_len) {
   };
   cudaMemcpyAsync(save, c->d.PA, n * sizeof(double), cudaMemcpyDeviceToDevice, c->stream);
   cudaMemcpyAsync(save + n, c->d.WA, n * sizeof(double), cudaMemcpyDeviceToDevice, c->stream);
-  struct Cand { bool pers; int bs; int cpw; int wide; };
+  struct Cand { bool pers; int bs; int cpw; int wide; int fg; };
   std::vector<Cand> cands;
   for (int pers = c->can_persistent ? 1 : 0; pers >= 0; --pers)
     for (int cpw : {8, 4, 2})
-      for (int bs : {128, 64}) cands.push_back({pers != 0, bs, cpw, 0});
+      for (int bs : {128, 64}) cands.push_back({pers != 0, bs, cpw, 0, 1});
   for (int wide : {1, 2, 3})
-    for (int bs : {128, 64}) cands.push_back({false, bs, 8, wide});
-  if (c->mode == RC_PREC_FP64 ? c->can_flow : c->can_flow32) cands.push_back({false, 128, 8, 4});
+    for (int bs : {128, 64}) cands.push_back({false, bs, 8, wide, 1});
+  if (c->mode == RC_PREC_FP64) {
+    for (int g = 1; g <= FLOW_GMAX; ++g)
+      if (c->can_flow[g - 1]) cands.push_back({false, 128, 8, 4, g});
+  } else if (c->can_flow32) {
+    cands.push_back({false, 128, 8, 4, 1});
+  }
+  auto name = [](const Cand& k) {
+    return std::string(k.pers ? "persistent"
+                              : k.wide == 4 ? (k.fg == 1 ? "flow" : "flow" + std::to_string(k.fg))
+                              : k.wide == 3 ? "levels4w" : k.wide == 2 ? "levels2w" : k.wide ? "levels8" : "levels");
+  };
   cudaEvent_t e0, e1;
   cudaEventCreate(&e0);
   cudaEventCreate(&e1);
   std::string rep;
   double best = 1e300;
-  Cand bc = {c->persistent, c->d.bs, c->d.cpw, c->wide};
+  Cand bc = {c->persistent, c->d.bs, c->d.cpw, c->wide, c->flow_g};
   int st = RC_OK;
   for (const Cand& k : cands) {
     c->persistent = k.pers;
     c->d.bs = k.bs;
     c->d.cpw = k.cpw;
     c->wide = k.wide;
+    c->flow_g = k.fg;
     drop_graphs(c);
     restore();
     for (int w = 0; w < 2 && !st; ++w) st = rc_lusgs_stage(c, 1);
@@ -2590,8 +2663,7 @@ int rc_autotune(rc_ctx* c, int iters, char* report, int report_len) {
     float ms = 0.f;
     cudaEventElapsedTime(&ms, e0, e1);
     const double per = ms / iters;
-    rep += std::string(k.pers ? "persistent" : k.wide == 4 ? "flow" : k.wide == 3 ? "levels4w" : k.wide == 2 ? "levels2w" : k.wide ? "levels8" : "levels") +
-           " bs=" + std::to_string(k.bs) + " cpw=" + std::to_string(k.wide >= 2 ? 8 : k.wide ? 4 : k.cpw) + ": " +
+    rep += name(k) + " bs=" + std::to_string(k.bs) + " cpw=" + std::to_string(k.wide >= 2 ? 8 : k.wide ? 4 : k.cpw) + ": " +
            std::to_string(per) + " ms; ";
     if (per < best) { best = per; bc = k; }
   }
@@ -2599,15 +2671,14 @@ int rc_autotune(rc_ctx* c, int iters, char* report, int report_len) {
   c->d.bs = bc.bs;
   c->d.cpw = bc.cpw;
   c->wide = bc.wide;
+  c->flow_g = bc.fg;
   drop_graphs(c);
   restore();
   cudaStreamSynchronize(c->stream);
   cudaEventDestroy(e0);
   cudaEventDestroy(e1);
   cudaFree(save);
-  rep += std::string("chosen: ") +
-         (bc.pers ? "persistent" : bc.wide == 4 ? "flow" : bc.wide == 3 ? "levels4w" : bc.wide == 2 ? "levels2w" : bc.wide ? "levels8" : "levels") +
-         " bs=" + std::to_string(bc.bs) + " cpw=" + std::to_string(bc.wide >= 2 ? 8 : bc.wide ? 4 : bc.cpw);
+  rep += std::string("chosen: ") + name(bc) + " bs=" + std::to_string(bc.bs) + " cpw=" + std::to_string(bc.wide >= 2 ? 8 : bc.wide ? 4 : bc.cpw);
   if (report && report_len > 0) {
     std::snprintf(report, (size_t)report_len, "%s", rep.c_str());
   }

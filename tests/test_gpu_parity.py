@@ -207,7 +207,7 @@ def test_persistent_and_per_level_schedules_agree(case_root, precision, name, ov
     d = make_case(case_root, name, **over)
     c = rc.Case(d)
     states = []
-    for sched in ("persistent", "levels", "levels8", "levels2w", "levels4w", "flow"):
+    for sched in ("persistent", "levels", "levels8", "levels2w", "levels4w", "flow", "flow2", "flow3"):
         for cpw in ("8", "1"):
             monkeypatch.setenv("RC_LUSGS_SCHEDULE", sched)
             monkeypatch.setenv("RC_LUSGS_CPW", cpw)
@@ -220,11 +220,13 @@ def test_persistent_and_per_level_schedules_agree(case_root, precision, name, ov
         assert np.array_equal(states[0][1], st[1])
 
 
-def test_dataflow_schedule_bit_identical_to_oracle(case_root, monkeypatch):
+@pytest.mark.parametrize("sched", ["flow", "flow2", "flow3"])
+def test_dataflow_schedule_bit_identical_to_oracle(case_root, sched, monkeypatch):
     """The dataflow LU-SGS (cells split into per-SM blocks, waits only on the
-    passes of other blocks that hold a neighbour) on the reacting viscous
+    passes of other blocks that hold a neighbour; passes of up to 8, 16 or 24
+    cells over 1, 2 or 3 groups of compute warps) on the reacting viscous
     case and on the colored order, 20 iterations against the oracle."""
-    monkeypatch.setenv("RC_LUSGS_SCHEDULE", "flow")
+    monkeypatch.setenv("RC_LUSGS_SCHEDULE", sched)
     for name, over in (("t2", {}), ("c1", {"nx": 120, "ny": 20}), ("t2", {"order": "colored"})):
         d = make_case(case_root, name, **over)
         c = rc.Case(d)
@@ -238,11 +240,12 @@ def test_dataflow_schedule_bit_identical_to_oracle(case_root, monkeypatch):
         s.close()
 
 
-def test_dataflow_wait_timeout_is_reported(case_root, monkeypatch):
+@pytest.mark.parametrize("sched", ["flow", "flow3"])
+def test_dataflow_wait_timeout_is_reported(case_root, sched, monkeypatch):
     """A poll limit of 1 makes the dataflow LU-SGS give up on a pass of
     another block: RC_ERR_SYNC, every block still finishes the launch, and
     after the error is cleared the next launches (a new epoch) are exact."""
-    monkeypatch.setenv("RC_LUSGS_SCHEDULE", "flow")
+    monkeypatch.setenv("RC_LUSGS_SCHEDULE", sched)
     d = make_case(case_root, "c1", nx=60, ny=12)
     c = rc.Case(d)
     s = rc.Solver(c)
