@@ -1081,6 +1081,340 @@ __global__ void __launch_bounds__(flow_threads(G), 1) k_lusgs_flow(const Dev d, 
   }
 }
 
+// ---- compact dataflow LU-SGS (k_lusgs_flowc) ----
+// In a sweep only the faces to lower (forward) or upper (backward) neighbours
+// carry a term: on a triangulation about 1.5 of a cell's 3 slots.  The
+// per-slot lanes of k_lusgs_flow spend the other lanes' FP64 issue on terms
+// that are zero.  Here a group of four warps takes up to 32 ACTIVE (cell,
+// slot) pairs of up to 16 consecutive cells, one pair per lane, so one
+// group holds about twice the cells of a k_lusgs_flow group on the same
+// FP64 instruction count.  The finishing sums add only the active slots, in
+// slot order: a sum that starts at +0.0 is never -0.0, so leaving out the
+// +0.0 terms of the inactive slots leaves its bits unchanged.
+constexpr int FLOWC_CELLS = 16, FLOWC_PAIRS = 32, FLOWC_GMAX = 2;
+constexpr int FLOWC_STAGERS = 2, FLOWC_NBUF = 4;
+// compute groups, the coordinator warp, the staging warps
+__host__ __device__ constexpr int flowc_threads(int G) { return 128 * G + 32 + 32 * FLOWC_STAGERS; }
+// What the sweep step of one active pair needs (the neighbour j's gas state
+// and its products, the face), staged before the pass may start: the fields
+// of SweepPre that the step reads, formed with the same expressions.
+template <int NSP>
+struct PairPre {
+  int j;   // the neighbour (-1: no pair in this lane)
+  int cs;  // the pair's cell within its group << 2 | its slot
+  double dx, dy, uu, vv, tt, rr, gama, aF;
+  double rrh, rrl, gmh, gml;
+  double rou, rov, gm1, roepp, unormal;
+  double cs_h[NSP];
+  double ry[NSP > 1 ? NSP - 1 : 1];
+};
+template <int NSP, bool FWD>
+__device__ __forceinline__ PairPre<NSP> pair_load(const Dev& d, int t, int q, int tg) {
+  constexpr int DIR = FWD ? 0 : 1;
+  const int NE = d.NE, NF = d.NF;
+  PairPre<NSP> p;
+  const int j = d.swj[DIR][q * NE + t], fs = d.swf[DIR][q * NE + t], f = fs >= 0 ? fs : ~fs;
+  p.j = j;
+  p.cs = ((t - tg) << 2) | q;
+  p.dx = d.fvec[f];
+  p.dy = d.fvec[NF + f];
+  if (fs < 0) { p.dx = -p.dx; p.dy = -p.dy; }
+  const double pp = d.PA[0 * NE + j];
+  p.uu = d.PA[1 * NE + j]; p.vv = d.PA[2 * NE + j]; p.tt = d.PA[3 * NE + j];
+  p.rr = d.cst[0 * NE + j]; p.gama = d.cst[1 * NE + j];
+  const double roe = d.cst[2 * NE + j];
+  p.rrh = d.rcp[0 * NE + j]; p.rrl = d.rcp[1 * NE + j]; p.gmh = d.rcp[2 * NE + j]; p.gml = d.rcp[3 * NE + j];
+  p.aF = d.alpaF[f];
+#pragma unroll
+  for (int k = 0; k < NSP; ++k) p.cs_h[k] = d.cst[(3 + k) * NE + j];
+#pragma unroll
+  for (int k = 0; k < NSP - 1; ++k) p.ry[k] = p.rr * d.PA[(4 + k) * NE + j];
+  p.rou = p.rr * p.uu;
+  p.rov = p.rr * p.vv;
+  p.gm1 = p.gama - 1;
+  p.roepp = roe + pp;
+  p.unormal = p.uu * p.dx + p.vv * p.dy;
+  return p;
+}
+// one ring slot: G groups of 32 pairs and 16 cells
+template <int NSP, int G>
+__host__ __device__ constexpr int flowc_slot_bytes() { return (int)(32 * G * sizeof(PairPre<NSP>) + FLOWC_CELLS * G * 32); }
+template <int NSP, int G>
+__host__ __device__ constexpr int flowc_dsmem() { return FLOWC_NBUF * flowc_slot_bytes<NSP, G>(); }
+// The cell a finishing lane needs: its index, dd and dd's reciprocal pair,
+// and its active slots (bit q: slot q has a neighbour in this sweep).
+struct FinC {
+  int i, mask;
+  double dd, ddh, ddl;
+};
+template <bool FWD>
+__device__ __forceinline__ FinC finc_load(const Dev& d, int t) {
+  constexpr int DIR = FWD ? 0 : 1;
+  FinC f;
+  const int NE = d.NE;
+  f.i = d.swi[DIR][t];
+  f.dd = d.dd[f.i];
+  f.ddh = d.rcp[4 * NE + f.i];
+  f.ddl = d.rcp[5 * NE + f.i];
+  f.mask = 0;
+#pragma unroll
+  for (int q = 0; q < 4; ++q) f.mask |= (d.swj[DIR][q * NE + t] >= 0 ? 1 : 0) << q;
+  return f;
+}
+// One group's step (threads 128 g .. 128 g + 127): in the term phases lane l
+// holds the group's l-th active pair (p; p.j < 0 past the last pair) and nbv
+// its neighbour's hWA; in the finishing phase warp `role` finishes local
+// cells 4 role .. 4 role + 3 (8 lanes per cell, lane r variable r; fn the
+// lane's cell, fn.i < 0 past the last cell).  The phases, barriers and
+// expressions are sweep4w_compute's.
+template <int NSP, bool FWD, int G>
+__device__ __forceinline__ void sweepc_compute(const Dev& d, const ThermoDev<NSP>& th, const PairPre<NSP>& p,
+                                               const double* nbv, const FinC& fn) {
+  constexpr int V = 3 + NSP;
+  const int NE = d.NE, gi = G > 1 ? (int)(threadIdx.x >> 7) : 0, role = (threadIdx.x >> 5) & 3,
+            lane = threadIdx.x & 31, q = p.cs & 3;
+  const bool act = p.j >= 0;
+  __shared__ double wsc_g[G][FLOWC_CELLS * V * 4];
+  __shared__ double cs1_g[G][32], cq_g[G][32], cdp_g[G][32], cdu_g[G][32], cdv_g[G][32], cdn_g[G][32];
+  double* wsm = wsc_g[gi];
+  double *xs1 = cs1_g[gi], *xq = cq_g[gi], *xdp = cdp_g[gi], *xdu = cdu_g[gi], *xdv = cdv_g[gi], *xdn = cdn_g[gi];
+  const int b5 = 5 + 3 * gi, b6 = 6 + 3 * gi, b7 = 7 + 3 * gi;
+  const int r = lane & 7;
+  const bool fvalid = fn.i >= 0 && r < V;
+  const int fi = fvalid ? fn.i : 0;
+  const double R = fvalid ? __ldcg(d.hWA + r * NE + fi) : 0.0;
+  double* w = wsm + ((p.cs >> 2) & (FLOWC_CELLS - 1)) * V * 4;
+  const double aF = p.aF, unormal = p.unormal;
+  const double drr = nbv[0], dru = nbv[1], drv = nbv[2], dre = nbv[3];
+  double dry[NSP];
+#pragma unroll
+  for (int k = 0; k < NSP; ++k) dry[k] = 0.0;
+  if (role != 2 && act) {  // the species increments: warps 0, 1 and 3
+    double s = 0.0;
+#pragma unroll
+    for (int k = 0; k < NSP - 1; ++k) { dry[k] = nbv[4 + k]; s = s + dry[k]; }
+    dry[NSP - 1] = drr - s;
+  }
+  // A
+  if (act) {
+    if (role == 0) {
+      double s1 = 0.0;
+#pragma unroll
+      for (int k = 0; k < NSP; ++k) s1 = s1 + p.cs_h[k] * dry[k];
+      xs1[lane] = s1;
+      w[q] = 0.5 * (-aF * drr + dru * p.dx + drv * p.dy);
+    } else if (role == 1) {
+      double s2 = 0.0;
+#pragma unroll
+      for (int k = 0; k < NSP; ++k) s2 = s2 + th.R[k] * dry[k];
+      xq[lane] = div_rn(p.tt * s2 * p.gama, p.gm1, p.gmh, p.gml);
+    } else if (role == 2) {
+      xdu[lane] = div_rn(dru - p.uu * drr, p.rr, p.rrh, p.rrl);
+    } else {
+      xdv[lane] = div_rn(drv - p.vv * drr, p.rr, p.rrh, p.rrl);
+    }
+  }
+  bar_named(b5, 128);
+  // B
+  if (role == 3) {
+    double dunormal = 0.0;
+    if (act) {
+      dunormal = xdu[lane] * p.dx + xdv[lane] * p.dy;
+      xdn[lane] = dunormal;
+    }
+    bar_arrive(b6, 128);
+    if (act) {
+#pragma unroll
+      for (int k = 0; k < NSP - 1; ++k) w[(4 + k) * 4 + q] = 0.5 * (-aF * dry[k] + dry[k] * unormal + p.ry[k] * dunormal);
+    }
+  } else {
+    if (role == 2 && act) {
+      const double duu = xdu[lane], dvv = xdv[lane];
+      const double X = dru * p.uu + duu * p.rou + drv * p.vv + dvv * p.rov;
+      xdp[lane] = p.gm1 * (dre - xs1[lane] + xq[lane] - 0.5 * X);
+    }
+    bar_named(b6, 128);
+    // C
+    if (act) {
+      const double dpp = xdp[lane], dunormal = xdn[lane];
+      double ck;
+      if (role == 0) ck = 0.5 * (-aF * dru + dru * unormal + p.rou * dunormal + dpp * p.dx);
+      else if (role == 1) ck = 0.5 * (-aF * drv + drv * unormal + p.rov * dunormal + dpp * p.dy);
+      else ck = 0.5 * (-aF * dre + dunormal * p.roepp + unormal * (dre + dpp));
+      w[(1 + role) * 4 + q] = ck;
+    }
+  }
+  bar_named(b7, 128);
+  if (!fvalid) return;
+  const double* wf = wsm + (role * 4 + (lane >> 3)) * V * 4;
+  double df = 0.0;
+#pragma unroll
+  for (int sl = 0; sl < 4; ++sl)
+    if ((fn.mask >> sl) & 1) df = df + wf[r * 4 + sl];
+  d.hWA[r * NE + fi] = FWD ? div_rn(R - df, fn.dd, fn.ddh, fn.ddl) : R - div_rn(df, fn.dd, fn.ddh, fn.ddl);
+}
+// Both LU-SGS sweeps as a dataflow over one cooperative launch with compact
+// passes: block b owns cells [bC, (b+1)C); a pass is a run of consecutive
+// positions of one level owned by the block, split into G groups of at most
+// 16 cells and 32 active pairs, group g on warps 4g .. 4g+3.  The work
+// around a pass is spread over more warps than k_lusgs_flow's single staging
+// warp, whose gathers, polls and publishing took longer than a pass:
+//  - FLOWC_STAGERS staging warps: warp s stages passes s, s + STAGERS, ...
+//    (pair_load / finc_load) into a ring of FLOWC_NBUF shared slots, once
+//    the pass that held the slot before is finished (s_consumed); s_slot[b]
+//    = k + 1 marks pass k staged in slot b;
+//  - the coordinator warp (4G): looks at the flags of the next pass, hands
+//    it to the compute warps (barrier 3) once it is staged, its flags are
+//    set and the current pass is done (barrier 4), and publishes the
+//    finished pass (flag = this launch's epoch), before any blocking wait, so
+//    no block waits while holding a finished pass.
+// With each hand-over the coordinator writes s_go[slot]: 0 after any wait
+// gave up (ERR_SYNC), when the staging may have stopped; all warps of a group
+// read the same s_go and skip the pass together, so the group's barriers
+// stay matched.  Every wait is bounded.  A group without cells in the pass
+// only joins the hand-over.
+template <int NSP, int G>
+__global__ void __launch_bounds__(flowc_threads(G), 1) k_lusgs_flowc(const Dev d, const ThermoDev<NSP> th, const FlowDev f) {
+  constexpr int V = 3 + NSP, T34 = 128 * G + 32, SLOT = flowc_slot_bytes<NSP, G>();
+  extern __shared__ __align__(16) uint8_t flowc_smem[];
+  auto slot_pre = [&](int s) { return reinterpret_cast<PairPre<NSP>*>(flowc_smem + s * SLOT); };
+  auto slot_fin = [&](int s) {
+    return reinterpret_cast<FinC*>(flowc_smem + s * SLOT + 32 * G * sizeof(PairPre<NSP>));
+  };
+  __shared__ unsigned s_epoch;
+  __shared__ volatile int s_bad, s_consumed;
+  __shared__ volatile int s_slot[FLOWC_NBUF], s_go[FLOWC_NBUF];
+  if (threadIdx.x == 0) {
+    s_epoch = ld_acquire(f.ctr) + 1u;
+    s_bad = 0;
+    s_consumed = 0;
+    for (int s = 0; s < FLOWC_NBUF; ++s) { s_slot[s] = 0; s_go[s] = 0; }
+  }
+  __syncthreads();
+  const unsigned epoch = s_epoch;
+  const int b = blockIdx.x, lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const int f0 = f.boff[0][b], b0 = f.boff[1][b];
+  const int nf = f.boff[0][b + 1] - f0, n = nf + (f.boff[1][b + 1] - b0);
+  auto pass_of = [&](int k) { return k < nf ? f.blist[0][f0 + k] : f.blist[1][b0 + k - nf]; };
+  auto give_up = [&]() {
+    if (lane == 0) {
+      s_bad = 1;
+      atomicOr(d.err, ERR_SYNC);
+    }
+    __syncwarp();
+  };
+  if (warp > 4 * G) {
+    // staging warp s: the data of its passes that the sweep does not change
+    const int s = warp - 4 * G - 1;
+    for (int k = s; k < n && !s_bad; k += FLOWC_STAGERS) {
+      for (unsigned spin = 0; s_consumed < k - FLOWC_NBUF + 1 && !s_bad; ++spin)
+        if (spin >= d.spin_limit) give_up();
+      if (s_bad) break;
+      const int pz = pass_of(k), sl = k % FLOWC_NBUF;
+      PairPre<NSP>* pre = slot_pre(sl);
+      FinC* fin = slot_fin(sl);
+      int tg = f.pstart[pz];
+#pragma unroll
+      for (int g = 0; g < G; ++g) {
+        const int nc = f.gcell[pz * G + g], e0 = f.poff[pz * G + g], np = f.poff[pz * G + g + 1] - e0;
+        PairPre<NSP> pl;
+        pl.j = -1;
+        pl.cs = 0;
+        if (lane < np) {
+          const int e = f.plist[e0 + lane];
+          pl = k < nf ? pair_load<NSP, true>(d, e >> 2, e & 3, tg) : pair_load<NSP, false>(d, e >> 2, e & 3, tg);
+        }
+        pre[32 * g + lane] = pl;
+        if (lane < FLOWC_CELLS) {
+          FinC fc = {-1, 0, 1.0, 1.0, 0.0};
+          if (lane < nc) fc = k < nf ? finc_load<true>(d, tg + lane) : finc_load<false>(d, tg + lane);
+          fin[FLOWC_CELLS * g + lane] = fc;
+        }
+        tg += nc;
+      }
+      __syncwarp();
+      __threadfence_block();
+      if (lane == 0) s_slot[sl] = k + 1;
+      __syncwarp();
+    }
+  } else if (warp == 4 * G) {
+    // the coordinator
+    auto staged = [&](int k) {  // wait (bounded) until pass k is staged
+      for (unsigned spin = 0; s_slot[k % FLOWC_NBUF] != k + 1 && !s_bad; ++spin)
+        if (spin >= d.spin_limit) give_up();
+      __threadfence_block();
+    };
+    auto poll = [&](int k) {
+      if (s_bad) return;
+      const int pz = pass_of(k), d0 = f.doff[pz], nd = f.doff[pz + 1] - d0;
+      bool ok = true;
+      for (int u = lane; u < nd; u += 32) ok = ok && wait_flag(f.pflag + f.deps[d0 + u], epoch, d.err, d.spin_limit);
+      if (__any_sync(0xffffffffu, !ok)) give_up();
+    };
+    auto ready = [&](int k) -> bool {
+      if (s_bad) return true;
+      if (s_slot[k % FLOWC_NBUF] != k + 1) return false;
+      const int pz = pass_of(k), d0 = f.doff[pz], nd = f.doff[pz + 1] - d0;
+      bool ok = true;
+      for (int u = lane; u < nd; u += 32) ok = ok && ld_acquire(f.pflag + f.deps[d0 + u]) >= epoch;
+      return __all_sync(0xffffffffu, ok) != 0;
+    };
+    // hand pass k over: the compute warps run it iff nothing gave up
+    auto hand_over = [&](int k) {
+      if (lane == 0) s_go[k % FLOWC_NBUF] = s_bad ? 0 : 1;
+      __syncwarp();
+      __threadfence_block();
+      bar_arrive(3, T34);
+    };
+    if (n > 0) {
+      staged(0);
+      poll(0);
+      hand_over(0);
+    }
+    for (int k = 0; k < n; ++k) {
+      const bool more = k + 1 < n;
+      const bool go = more && ready(k + 1);
+      if (go) __threadfence_block();
+      bar_named(4, T34);
+      __threadfence_block();
+      if (lane == 0) s_consumed = k + 1;  // pass k's slot is free
+      if (go) hand_over(k + 1);
+      if (lane == 0 && !s_bad) st_release(f.pflag + pass_of(k), epoch);
+      if (more && !go) {
+        poll(k + 1);
+        staged(k + 1);
+        hand_over(k + 1);
+      }
+    }
+  } else {
+    const int gi = threadIdx.x >> 7, role = (threadIdx.x >> 5) & 3;
+    for (int k = 0; k < n; ++k) {
+      bar_named(3, T34);
+      const int sl = k % FLOWC_NBUF;
+      // the group's first cell exists iff the group has work in this pass
+      if (s_go[sl] && slot_fin(sl)[FLOWC_CELLS * gi].i >= 0) {
+        const PairPre<NSP> p = slot_pre(sl)[32 * gi + lane];
+        const FinC fn = slot_fin(sl)[FLOWC_CELLS * gi + role * 4 + (lane >> 3)];
+        double nbv[V];
+#pragma unroll
+        for (int v = 0; v < V; ++v) nbv[v] = p.j >= 0 ? __ldcg(d.hWA + (size_t)v * d.NE + p.j) : 0.0;
+        if (k < nf) sweepc_compute<NSP, true, G>(d, th, p, nbv, fn);
+        else sweepc_compute<NSP, false, G>(d, th, p, nbv, fn);
+      }
+      bar_arrive(4, T34);
+    }
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    __threadfence();
+    if (atomicAdd(f.ctr + 1, 1u) == gridDim.x - 1) {
+      f.ctr[1] = 0u;
+      __threadfence();
+      st_release(f.ctr, epoch);
+    }
+  }
+}
+
 template <int NSP, bool FWD>
 __global__ void __launch_bounds__(32) k_sweep4(const Dev d, const ThermoDev<NSP> th, int t0, int t1) {
   pdl_launch_dependents();
@@ -1283,6 +1617,9 @@ struct rc_ctx {
   FlowDev flows[FLOW_GMAX] = {};  // its pass tables for G = 1..3 groups (passes of up to 8 G cells;
                                   // G = 1 is also the mixed forms' k_lusgs_flow32)
   int flow_g = 1;                 // the groups of the FP64 dataflow launch
+  bool can_flowc[FLOWC_GMAX] = {};  // the device can co-schedule the k_lusgs_flowc grid (per G)
+  FlowDev flowc[FLOWC_GMAX] = {};   // compact pass tables for G = 1, 2 groups
+  bool flow_c = false;              // the FP64 dataflow launch is k_lusgs_flowc (flow_g groups)
   int pers_grid = 0;             // blocks of the persistent launch (one per SM)
   unsigned* lvl_count = nullptr; // per-level completion counters of the persistent launch
   int nlevels = 0;
@@ -1421,19 +1758,35 @@ SweepOrder sweep_order(int NE, const NF& nface, const std::vector<int>& cother) 
 // FP64 launch, three groups of 8; 8 for the mixed forms'); a block's passes are
 // listed forward then backward in level order; a pass depends on the passes
 // (same sweep) of the neighbours it reads that other blocks own.
+//
+// Compact passes (groups > 0, k_lusgs_flowc): the run is cut into up to
+// `groups` groups of consecutive positions, each of at most FLOWC_CELLS cells
+// and FLOWC_PAIRS active (position, slot) pairs, filled greedily; plist
+// lists each group's pairs in (position, slot) order.
 struct FlowPlan {
   int C = 1;
   std::vector<int> pstart, pcount, pdir, powner, plevel, doff, deps;
   std::vector<int> boff[2], blist[2];
   std::vector<int> cellpass[2];
+  int groups = 0;
+  std::vector<int> gcell, poff, plist;
 };
+// the slot q of cell i has a neighbour in sweep dir (0 forward: a lower one)
+template <class NF>
+inline bool sweep_slot(int NE, const NF& nface, const std::vector<int>& cother, int dir, int i, int q) {
+  if (q >= nface[i]) return false;
+  const int j = cother[(size_t)q * NE + i];
+  return j >= 0 && (dir == 0 ? j < i : j > i);
+}
 template <class NF>
 FlowPlan flow_plan(int NE, int G, const NF& nface, const std::vector<int>& cother, const SweepOrder& so,
-                   int width = 8) {
+                   int width = 8, int groups = 0) {
   FlowPlan fp;
   fp.C = (NE + G - 1) / G;
   const int C = fp.C;
   fp.doff.assign(1, 0);
+  fp.groups = groups;
+  if (groups > 0) fp.poff.assign(1, 0);
   for (int dir = 0; dir < 2; ++dir) {
     const std::vector<int>& lst = so.cells[dir];
     const std::vector<int>& off = so.off[dir];
@@ -1443,7 +1796,26 @@ FlowPlan flow_plan(int NE, int G, const NF& nface, const std::vector<int>& cothe
       for (int t = off[l]; t < off[l + 1];) {
         const int own = lst[t] / C;
         int e = t + 1;
-        while (e < off[l + 1] && e - t < width && lst[e] / C == own) ++e;
+        if (groups > 0) {
+          e = t;
+          for (int g = 0; g < groups; ++g) {
+            int nc = 0, np = 0;
+            while (e < off[l + 1] && lst[e] / C == own && nc < FLOWC_CELLS) {
+              int a = 0;
+              for (int q = 0; q < 4; ++q) a += sweep_slot(NE, nface, cother, dir, lst[e], q) ? 1 : 0;
+              if (np + a > FLOWC_PAIRS) break;
+              for (int q = 0; q < 4; ++q)
+                if (sweep_slot(NE, nface, cother, dir, lst[e], q)) fp.plist.push_back(e << 2 | q);
+              np += a;
+              ++nc;
+              ++e;
+            }
+            fp.gcell.push_back(nc);
+            fp.poff.push_back((int)fp.plist.size());
+          }
+        } else {
+          while (e < off[l + 1] && e - t < width && lst[e] / C == own) ++e;
+        }
         const int pz = (int)fp.pstart.size();
         fp.pstart.push_back(t); fp.pcount.push_back(e - t); fp.pdir.push_back(dir); fp.powner.push_back(own);
         fp.plevel.push_back((int)l);
@@ -1583,9 +1955,30 @@ void q_flow_g(rc_ctx* c) {
   cfg.numAttrs = 1;
   cudaLaunchKernelEx(&cfg, k_lusgs_flow<NSP, G>, c->d, TH<NSP>(c), c->flows[G - 1]);
 }
+template <int NSP, int G>
+void q_flowc_g(rc_ctx* c) {
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = dim3((unsigned)c->flow_grid);
+  cfg.blockDim = dim3(flowc_threads(G));
+  cfg.dynamicSmemBytes = (size_t)flowc_dsmem<NSP, G>();
+  cfg.stream = c->stream;
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeCooperative;
+  attr[0].val.cooperative = 1;
+  cfg.attrs = attr;
+  cfg.numAttrs = 1;
+  cudaLaunchKernelEx(&cfg, k_lusgs_flowc<NSP, G>, c->d, TH<NSP>(c), c->flowc[G - 1]);
+}
+// the FP64 dataflow launch the context runs, if the device can hold its grid
+bool flow_runs(const rc_ctx* c) {
+  return c->wide == 4 && (c->flow_c ? c->flow_g <= FLOWC_GMAX && c->can_flowc[c->flow_g - 1] : c->can_flow[c->flow_g - 1]);
+}
 template <int NSP>
 void q_flow(rc_ctx* c) {
-  if (c->flow_g == 3) q_flow_g<NSP, 3>(c);
+  if (c->flow_c) {
+    if (c->flow_g == 2) q_flowc_g<NSP, 2>(c);
+    else q_flowc_g<NSP, 1>(c);
+  } else if (c->flow_g == 3) q_flow_g<NSP, 3>(c);
   else if (c->flow_g == 2) q_flow_g<NSP, 2>(c);
   else q_flow_g<NSP, 1>(c);
   c->launches++;
@@ -1599,7 +1992,7 @@ void q_sweeps(rc_ctx* c, int gather) {
     c->launches++;
   }
   if (c->persistent) { q_persistent<NSP>(c); return; }
-  if (c->wide == 4 && c->can_flow[c->flow_g - 1]) { q_flow<NSP>(c); return; }
+  if (flow_runs(c)) { q_flow<NSP>(c); return; }
   for (size_t l = 0; l + 1 < c->fwd_off.size(); ++l) {
     const int n = c->fwd_off[l + 1] - c->fwd_off[l];
     if (c->wide >= 3) launch_pdl(k_sweep4w<NSP, true>, blocks(n, 8), 128, c->stream, c->d, TH<NSP>(c),
@@ -2216,16 +2609,24 @@ int init_impl(const rc_mesh* m, const rc_thermo* t, const rc_config* g, const Ba
     int nsm = 0;
     cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, g->device);
     const int G = std::max(nsm, 1);
-    for (int gr = 1; gr <= FLOW_GMAX; ++gr) {
-      FlowPlan fp = flow_plan(NE, G, nface, cother, so, 8 * gr);
+    for (int gr = 1; gr <= FLOW_GMAX + FLOWC_GMAX; ++gr) {
+      // G = 1..3 groups of 8 positions, then the compact plans of 1..2 groups
+      const int cg = gr > FLOW_GMAX ? gr - FLOW_GMAX : 0;
+      FlowPlan fp = cg ? flow_plan(NE, G, nface, cother, so, FLOWC_CELLS * cg, cg) : flow_plan(NE, G, nface, cother, so, 8 * gr);
       std::vector<int>& pstart = fp.pstart;
       std::vector<int>& pcount = fp.pcount;
       std::vector<int>& doff = fp.doff;
       std::vector<int>& deps = fp.deps;
       std::vector<int>* boff = fp.boff;
       std::vector<int>* blist = fp.blist;
-      FlowDev& f = c->flows[gr - 1];
+      FlowDev& f = cg ? c->flowc[cg - 1] : c->flows[gr - 1];
       int* ip;
+      if (cg) {
+        st |= dev_upload(c, fp.gcell, &ip); f.gcell = ip;
+        st |= dev_upload(c, fp.poff, &ip); f.poff = ip;
+        if (fp.plist.empty()) fp.plist.push_back(0);
+        st |= dev_upload(c, fp.plist, &ip); f.plist = ip;
+      }
       st |= dev_upload(c, pstart, &ip); f.pstart = ip;
       st |= dev_upload(c, pcount, &ip); f.pcount = ip;
       for (int dir = 0; dir < 2; ++dir) {
@@ -2278,7 +2679,8 @@ int init_impl(const rc_mesh* m, const rc_thermo* t, const rc_config* g, const Ba
     const std::string sc = sched ? sched : "";
     c->persistent = c->can_persistent && sc == "persistent";
     c->wide = sc == "levels" ? 0 : sc == "levels8" ? 1 : sc == "levels2w" ? 2 : sc == "levels4w" ? 3 : 4;
-    c->flow_g = sc == "flow3" ? 3 : sc == "flow2" ? 2 : 1;
+    c->flow_g = sc == "flow3" ? 3 : sc == "flow2" || sc == "flowc2" ? 2 : 1;
+    c->flow_c = sc == "flowc" || sc == "flowc2";
     auto occ_flow = [&](auto kern, int threads, int dsmem) {
       int o = 0;
       cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, dsmem);
@@ -2289,10 +2691,14 @@ int init_impl(const rc_mesh* m, const rc_thermo* t, const rc_config* g, const Ba
       c->can_flow[0] = occ_flow(k_lusgs_flow<1, 1>, flow_threads(1), flow_dsmem<1, 1>());
       c->can_flow[1] = occ_flow(k_lusgs_flow<1, 2>, flow_threads(2), flow_dsmem<1, 2>());
       c->can_flow[2] = occ_flow(k_lusgs_flow<1, 3>, flow_threads(3), flow_dsmem<1, 3>());
+      c->can_flowc[0] = occ_flow(k_lusgs_flowc<1, 1>, flowc_threads(1), flowc_dsmem<1, 1>());
+      c->can_flowc[1] = occ_flow(k_lusgs_flowc<1, 2>, flowc_threads(2), flowc_dsmem<1, 2>());
     } else {
       c->can_flow[0] = occ_flow(k_lusgs_flow<4, 1>, flow_threads(1), flow_dsmem<4, 1>());
       c->can_flow[1] = occ_flow(k_lusgs_flow<4, 2>, flow_threads(2), flow_dsmem<4, 2>());
       c->can_flow[2] = occ_flow(k_lusgs_flow<4, 3>, flow_threads(3), flow_dsmem<4, 3>());
+      c->can_flowc[0] = occ_flow(k_lusgs_flowc<4, 1>, flowc_threads(1), flowc_dsmem<4, 1>());
+      c->can_flowc[1] = occ_flow(k_lusgs_flowc<4, 2>, flowc_threads(2), flowc_dsmem<4, 2>());
     }
     cudaGetLastError();  // an attribute or occupancy query that failed leaves can_flow false
     occ32 = c->NSP == 1 ? mixed_flow_occupancy<1>() : mixed_flow_occupancy<4>();
@@ -2305,12 +2711,37 @@ int init_impl(const rc_mesh* m, const rc_thermo* t, const rc_config* g, const Ba
 }  // namespace
 
 // The plan with passes of up to `width` positions; stats as rc_flow_plan_check.
+// groups > 0: the compact plan of that many groups of FLOWC_CELLS cells.
 int flow_plan_check_width(int ne, int nblocks, const std::vector<int>& nf, const std::vector<int>& co,
-                          const SweepOrder& so, int width, long long* stats) {
-  const FlowPlan fp = flow_plan(ne, nblocks, nf, co, so, width);
+                          const SweepOrder& so, int width, long long* stats, int groups = 0) {
+  const FlowPlan fp = groups > 0 ? flow_plan(ne, nblocks, nf, co, so, FLOWC_CELLS * groups, groups)
+                                 : flow_plan(ne, nblocks, nf, co, so, width);
+  if (groups > 0) width = FLOWC_CELLS * groups;
   const int P = (int)fp.pstart.size(), C = fp.C;
   bool ok = true;
   long long npass[2] = {0, 0}, maxdep = 0;
+  // compact plans: the groups of a pass split its positions in order; a
+  // group holds at most FLOWC_CELLS cells and lists exactly their active
+  // (position, slot) pairs, at most FLOWC_PAIRS, in (position, slot) order
+  if (groups > 0) {
+    if ((int)fp.gcell.size() != P * groups || (int)fp.poff.size() != P * groups + 1 || fp.poff[0] != 0) ok = false;
+    for (int pz = 0; pz < P && ok; ++pz) {
+      const int dir = fp.pdir[pz];
+      int t = fp.pstart[pz], tot = 0;
+      for (int g = 0; g < groups && ok; ++g) {
+        const int nc = fp.gcell[pz * groups + g], e0 = fp.poff[pz * groups + g], e1 = fp.poff[pz * groups + g + 1];
+        if (nc < 0 || nc > FLOWC_CELLS || e1 - e0 < 0 || e1 - e0 > FLOWC_PAIRS) { ok = false; break; }
+        int e = e0;
+        for (int u = t; u < t + nc && ok; ++u)
+          for (int q = 0; q < 4 && ok; ++q)
+            if (sweep_slot(ne, nf, co, dir, so.cells[dir][u], q)) ok = e < e1 && fp.plist[e++] == (u << 2 | q);
+        if (e != e1) ok = false;
+        t += nc;
+        tot += nc;
+      }
+      if (tot != fp.pcount[pz]) ok = false;
+    }
+  }
   // every cell in exactly one pass per sweep; a pass is 1..8 positions of one
   // level, all owned by its block
   for (int dir = 0; dir < 2 && ok; ++dir) {
@@ -2414,8 +2845,27 @@ int rc_flow_plan_check(int ne, int nblocks, const int* nface, const int* cother,
   }
   const SweepOrder so = sweep_order(ne, nf, co);
   int st = RC_OK;
+  for (int gr = FLOWC_GMAX; gr >= 1 && st == RC_OK; --gr) st = flow_plan_check_width(ne, nblocks, nf, co, so, 0, stats, gr);
   for (int gr = FLOW_GMAX; gr >= 1 && st == RC_OK; --gr) st = flow_plan_check_width(ne, nblocks, nf, co, so, 8 * gr, stats);
   return st;
+}
+
+int rc_flow_plan_stats(int ne, int nblocks, const int* nface, const int* cother, int groups, int compact,
+                       long long* stats) {
+  if (ne < 1 || nblocks < 1 || !nface || !cother || !stats) return RC_ERR_ARG;
+  if (compact ? (groups < 1 || groups > FLOWC_GMAX) : (groups < 1 || groups > FLOW_GMAX)) return RC_ERR_ARG;
+  std::vector<int> nf(nface, nface + ne);
+  std::vector<int> co(cother, cother + 4 * (size_t)ne);
+  for (int i = 0; i < ne; ++i) {
+    if (nf[i] < 0 || nf[i] > 4) return RC_ERR_ARG;
+    for (int q = 0; q < nf[i]; ++q) {
+      const int j = co[(size_t)q * ne + i];
+      if (j < -1 || j >= ne || j == i) return RC_ERR_ARG;
+    }
+  }
+  const SweepOrder so = sweep_order(ne, nf, co);
+  return compact ? flow_plan_check_width(ne, nblocks, nf, co, so, 0, stats, groups)
+                 : flow_plan_check_width(ne, nblocks, nf, co, so, 8 * groups, stats);
 }
 
 int rc_init(const rc_mesh* m, const rc_thermo* t, const rc_config* g, rc_ctx** out) {
@@ -2621,22 +3071,25 @@ int rc_autotune(rc_ctx* c, int iters, char* report, int report_len) {
   };
   cudaMemcpyAsync(save, c->d.PA, n * sizeof(double), cudaMemcpyDeviceToDevice, c->stream);
   cudaMemcpyAsync(save + n, c->d.WA, n * sizeof(double), cudaMemcpyDeviceToDevice, c->stream);
-  struct Cand { bool pers; int bs; int cpw; int wide; int fg; };
+  struct Cand { bool pers; int bs; int cpw; int wide; int fg; bool fc; };
   std::vector<Cand> cands;
   for (int pers = c->can_persistent ? 1 : 0; pers >= 0; --pers)
     for (int cpw : {8, 4, 2})
-      for (int bs : {128, 64}) cands.push_back({pers != 0, bs, cpw, 0, 1});
+      for (int bs : {128, 64}) cands.push_back({pers != 0, bs, cpw, 0, 1, false});
   for (int wide : {1, 2, 3})
-    for (int bs : {128, 64}) cands.push_back({false, bs, 8, wide, 1});
+    for (int bs : {128, 64}) cands.push_back({false, bs, 8, wide, 1, false});
   if (c->mode == RC_PREC_FP64) {
     for (int g = 1; g <= FLOW_GMAX; ++g)
-      if (c->can_flow[g - 1]) cands.push_back({false, 128, 8, 4, g});
+      if (c->can_flow[g - 1]) cands.push_back({false, 128, 8, 4, g, false});
+    for (int g = 1; g <= FLOWC_GMAX; ++g)
+      if (c->can_flowc[g - 1]) cands.push_back({false, 128, 8, 4, g, true});
   } else if (c->can_flow32) {
-    cands.push_back({false, 128, 8, 4, 1});
+    cands.push_back({false, 128, 8, 4, 1, false});
   }
   auto name = [](const Cand& k) {
+    const std::string fl = k.fc ? "flowc" : "flow";
     return std::string(k.pers ? "persistent"
-                              : k.wide == 4 ? (k.fg == 1 ? "flow" : "flow" + std::to_string(k.fg))
+                              : k.wide == 4 ? (k.fg == 1 ? fl : fl + std::to_string(k.fg))
                               : k.wide == 3 ? "levels4w" : k.wide == 2 ? "levels2w" : k.wide ? "levels8" : "levels");
   };
   cudaEvent_t e0, e1;
@@ -2644,7 +3097,7 @@ int rc_autotune(rc_ctx* c, int iters, char* report, int report_len) {
   cudaEventCreate(&e1);
   std::string rep;
   double best = 1e300;
-  Cand bc = {c->persistent, c->d.bs, c->d.cpw, c->wide, c->flow_g};
+  Cand bc = {c->persistent, c->d.bs, c->d.cpw, c->wide, c->flow_g, c->flow_c};
   int st = RC_OK;
   for (const Cand& k : cands) {
     c->persistent = k.pers;
@@ -2652,6 +3105,7 @@ int rc_autotune(rc_ctx* c, int iters, char* report, int report_len) {
     c->d.cpw = k.cpw;
     c->wide = k.wide;
     c->flow_g = k.fg;
+    c->flow_c = k.fc;
     drop_graphs(c);
     restore();
     for (int w = 0; w < 2 && !st; ++w) st = rc_lusgs_stage(c, 1);
@@ -2672,6 +3126,7 @@ int rc_autotune(rc_ctx* c, int iters, char* report, int report_len) {
   c->d.cpw = bc.cpw;
   c->wide = bc.wide;
   c->flow_g = bc.fg;
+  c->flow_c = bc.fc;
   drop_graphs(c);
   restore();
   cudaStreamSynchronize(c->stream);

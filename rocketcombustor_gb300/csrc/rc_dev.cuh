@@ -218,6 +218,13 @@ struct FlowDev {
   const int* deps;
   unsigned* pflag;     // per pass: epoch of the launch that finished it
   unsigned* ctr;       // [0] epoch of the last finished launch, [1] finished blocks
+  // compact passes only (k_lusgs_flowc; null otherwise): a pass is split into
+  // G groups of consecutive cells; group g of pass p holds gcell[p*G + g]
+  // cells (0..16) and the active (position, slot) pairs
+  // plist[poff[p*G + g] .. poff[p*G + g + 1]) (0..32), each position << 2 | slot
+  const int* gcell;
+  const int* poff;
+  const int* plist;
 };
 
 // Dataflow LU-SGS: pass flags.  wait_flag: the calling thread waits until

@@ -57,6 +57,24 @@ def test_natural_order_plan_adds_nothing_to_the_critical_path(nx, ny):
     assert st["steps"] == st["levels_fwd"] + st["levels_bwd"]
 
 
+@pytest.mark.parametrize("nx,ny,order", [(24, 6, "natural"), (100, 20, "colored"), (100, 20, "random"),
+                                         (3000, 8, "natural")])
+@pytest.mark.parametrize("groups", [1, 2])
+def test_compact_plan_is_consistent(nx, ny, order, groups):
+    """The compact plans of k_lusgs_flowc (groups of at most 16 cells and 32
+    active pairs, each group listing exactly its cells' active pairs) pass
+    every check and need no more passes than the 8-position plan of as many
+    groups; on the long, thin nozzle (about 13 cells of a level per block)
+    two compact groups end in as many steps as there are levels."""
+    nface, cother = _graph(nx, ny, order)
+    st = rc.flow_plan_check(nface, cother, 152, groups=groups, compact=True)
+    old = rc.flow_plan_check(nface, cother, 152, groups=groups)
+    assert st["passes_fwd"] <= old["passes_fwd"] and st["passes_bwd"] <= old["passes_bwd"]
+    assert st["levels_fwd"] + st["levels_bwd"] <= st["steps"] <= st["passes_fwd"] + st["passes_bwd"]
+    if (nx, ny, groups) == (3000, 8, 2):
+        assert st["steps"] == st["levels_fwd"] + st["levels_bwd"]
+
+
 def test_bad_arguments_are_refused():
     nface, cother = _graph(24, 6, "natural")
     bad = cother.copy()
@@ -65,3 +83,5 @@ def test_bad_arguments_are_refused():
         rc.flow_plan_check(nface, bad, 8)
     with pytest.raises(rc.RcError):
         rc.flow_plan_check(nface, cother, 0)
+    with pytest.raises(rc.RcError):
+        rc.flow_plan_check(nface, cother, 8, groups=3, compact=True)

@@ -207,7 +207,8 @@ def test_persistent_and_per_level_schedules_agree(case_root, precision, name, ov
     d = make_case(case_root, name, **over)
     c = rc.Case(d)
     states = []
-    for sched in ("persistent", "levels", "levels8", "levels2w", "levels4w", "flow", "flow2", "flow3"):
+    for sched in ("persistent", "levels", "levels8", "levels2w", "levels4w", "flow", "flow2", "flow3", "flowc",
+                  "flowc2"):
         for cpw in ("8", "1"):
             monkeypatch.setenv("RC_LUSGS_SCHEDULE", sched)
             monkeypatch.setenv("RC_LUSGS_CPW", cpw)
@@ -220,12 +221,13 @@ def test_persistent_and_per_level_schedules_agree(case_root, precision, name, ov
         assert np.array_equal(states[0][1], st[1])
 
 
-@pytest.mark.parametrize("sched", ["flow", "flow2", "flow3"])
+@pytest.mark.parametrize("sched", ["flow", "flow2", "flow3", "flowc", "flowc2"])
 def test_dataflow_schedule_bit_identical_to_oracle(case_root, sched, monkeypatch):
     """The dataflow LU-SGS (cells split into per-SM blocks, waits only on the
     passes of other blocks that hold a neighbour; passes of up to 8, 16 or 24
-    cells over 1, 2 or 3 groups of compute warps) on the reacting viscous
-    case and on the colored order, 20 iterations against the oracle."""
+    cells over 1, 2 or 3 groups of compute warps, or compact passes of one
+    or two groups of up to 16 cells and 32 active pairs) on the reacting
+    viscous case and on the colored order, 20 iterations against the oracle."""
     monkeypatch.setenv("RC_LUSGS_SCHEDULE", sched)
     for name, over in (("t2", {}), ("c1", {"nx": 120, "ny": 20}), ("t2", {"order": "colored"})):
         d = make_case(case_root, name, **over)
@@ -240,7 +242,35 @@ def test_dataflow_schedule_bit_identical_to_oracle(case_root, sched, monkeypatch
         s.close()
 
 
-@pytest.mark.parametrize("sched", ["flow", "flow3"])
+@pytest.mark.parametrize("name,over", [("c1", {"nx": 3000, "ny": 8}), ("c2", {"nx": 3000, "ny": 8})])
+@pytest.mark.parametrize("sched", ["flowc", "flowc2"])
+def test_compact_dataflow_wide_levels_bit_identical_to_oracle(case_root, sched, name, over, monkeypatch):
+    """A long, thin nozzle (3000 x 8 columns of triangles, 48,000 cells) puts
+    about 13 cells of every level in each of the 152 blocks: the compact
+    passes hold up to 16 cells and 32 active (cell, face) pairs per group,
+    so some passes fill two groups (fewer passes with two groups than with
+    one).  The one-species inviscid and the four-species reacting viscous
+    physics, 20 iterations against the oracle, bit for bit."""
+    from test_flow_plan import _graph
+
+    nface, cother = _graph(over["nx"], over["ny"], "natural")
+    one = rc.flow_plan_check(nface, cother, 152, groups=1, compact=True)
+    two = rc.flow_plan_check(nface, cother, 152, groups=2, compact=True)
+    assert two["passes_fwd"] < one["passes_fwd"] and two["passes_bwd"] < one["passes_bwd"]
+    monkeypatch.setenv("RC_LUSGS_SCHEDULE", sched)
+    d = make_case(case_root, name, **over)
+    c = rc.Case(d)
+    s = rc.Solver(c)
+    s.run(20)
+    PA, WA = s.get_state()
+    o = oracle.Oracle(d, threads=oracle.Oracle.max_threads())
+    o.run(20)
+    assert np.array_equal(PA, o.array("PA")), rel_linf(PA, o.array("PA"))
+    assert np.array_equal(WA, o.array("WA")), rel_linf(WA, o.array("WA"))
+    s.close()
+
+
+@pytest.mark.parametrize("sched", ["flow", "flow3", "flowc2"])
 def test_dataflow_wait_timeout_is_reported(case_root, sched, monkeypatch):
     """A poll limit of 1 makes the dataflow LU-SGS give up on a pass of
     another block: RC_ERR_SYNC, every block still finishes the launch, and
