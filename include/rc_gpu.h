@@ -200,10 +200,10 @@ int rc_clear_error(rc_ctx* ctx);
 int rc_flow_plan_check(int ne, int nblocks, const int* nface, const int* cother, long long* stats);
 /* The same checks and stats for one plan: passes of `groups` groups of 8
  * positions (compact = 0; groups 1..3) or the compact plan of `groups` groups
- * of at most 16 cells and 32 active (cell, face) pairs each (compact = 1;
- * groups 1..2), for which it also checks that each group lists exactly its
- * cells' active pairs.  Host only, like rc_flow_plan_check. */
-int rc_flow_plan_stats(int ne, int nblocks, const int* nface, const int* cother, int groups, int compact,
+ * (compact = 1; groups 1..2) of at most min(128 / nvar, 32) cells and 32
+ * active (cell, face) pairs each, for which it also checks that each group
+ * lists exactly its cells' active pairs.  Host only, like rc_flow_plan_check. */
+int rc_flow_plan_stats(int ne, int nblocks, const int* nface, const int* cother, int groups, int compact, int nvar,
                        long long* stats);
 
 /* Autotuner: times `iters` iterations of every launch configuration (LU-SGS

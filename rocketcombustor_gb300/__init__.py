@@ -142,7 +142,7 @@ SIGNATURES = {
     "rc_case_unsteady": (_i, [_vp, _DP]),
     "rc_run_unsteady": (_i, [_vp, _i, _l, _l, _DP, _IP]),
     "rc_flow_plan_check": (_i, [_i, _i, _IP, _IP, ctypes.POINTER(ctypes.c_longlong)]),
-    "rc_flow_plan_stats": (_i, [_i, _i, _IP, _IP, _i, _i, ctypes.POINTER(ctypes.c_longlong)]),
+    "rc_flow_plan_stats": (_i, [_i, _i, _IP, _IP, _i, _i, _i, ctypes.POINTER(ctypes.c_longlong)]),
 }
 
 _lib: Optional[ctypes.CDLL] = None
@@ -199,13 +199,13 @@ _CASE_ARRAYS = {  # name -> (dtype, shape from dims NE,NF,NNT,NVar,Nsp,MaxNei,Ng
 
 
 def flow_plan_check(nface: np.ndarray, cother: np.ndarray, nblocks: int, groups: Optional[int] = None,
-                    compact: bool = False) -> dict:
+                    compact: bool = False, nvar: int = 7) -> dict:
     """The host-side check of the dataflow LU-SGS plan (rc_flow_plan_check; no
     GPU needed).  nface (NE,) faces per cell; cother (NE, 4) the cell across
     each face, -1 at a boundary.  Without `groups`: every plan rc_init builds,
     with the stats of the 8-position passes; with it: that one plan
-    (rc_flow_plan_stats; compact for k_lusgs_flowc's).  Raises RcError when a
-    check fails."""
+    (rc_flow_plan_stats; compact for k_lusgs_flowc's, whose groups hold up to
+    min(128 // nvar, 32) cells).  Raises RcError when a check fails."""
     nface = np.ascontiguousarray(nface, dtype=np.int32)
     ne = nface.shape[0]
     co = np.ascontiguousarray(np.asarray(cother, dtype=np.int32).reshape(ne, 4).T)  # [q * NE + i]
@@ -215,7 +215,7 @@ def flow_plan_check(nface: np.ndarray, cother: np.ndarray, nblocks: int, groups:
         st = load().rc_flow_plan_check(ne, int(nblocks), nface.ctypes.data_as(_IP), co.ctypes.data_as(_IP), sp)
     else:
         st = load().rc_flow_plan_stats(ne, int(nblocks), nface.ctypes.data_as(_IP), co.ctypes.data_as(_IP),
-                                       int(groups), int(bool(compact)), sp)
+                                       int(groups), int(bool(compact)), int(nvar), sp)
     if st:
         raise RcError(st, "dataflow plan check failed" if st == 64 else "bad arguments")
     keys = ("passes_fwd", "passes_bwd", "deps", "max_deps", "steps", "levels_fwd", "levels_bwd", "cells_per_block")

@@ -1091,7 +1091,7 @@ __global__ void __launch_bounds__(flow_threads(G), 1) k_lusgs_flow(const Dev d, 
 // FP64 instruction count.  The finishing sums add only the active slots, in
 // slot order: a sum that starts at +0.0 is never -0.0, so leaving out the
 // +0.0 terms of the inactive slots leaves its bits unchanged.
-constexpr int FLOWC_CELLS = 16, FLOWC_PAIRS = 32, FLOWC_GMAX = 2;
+constexpr int FLOWC_GMAX = 2;
 constexpr int FLOWC_STAGERS = 2, FLOWC_NBUF = 4;
 // compute groups, the coordinator warp, the staging warps
 __host__ __device__ constexpr int flowc_threads(int G) { return 128 * G + 32 + 32 * FLOWC_STAGERS; }
@@ -1138,7 +1138,9 @@ __device__ __forceinline__ PairPre<NSP> pair_load(const Dev& d, int t, int q, in
 }
 // one ring slot: G groups of 32 pairs and 16 cells
 template <int NSP, int G>
-__host__ __device__ constexpr int flowc_slot_bytes() { return (int)(32 * G * sizeof(PairPre<NSP>) + FLOWC_CELLS * G * 32); }
+__host__ __device__ constexpr int flowc_slot_bytes() {
+  return (int)(32 * G * sizeof(PairPre<NSP>) + flowc_cells(3 + NSP) * G * 32);
+}
 template <int NSP, int G>
 __host__ __device__ constexpr int flowc_dsmem() { return FLOWC_NBUF * flowc_slot_bytes<NSP, G>(); }
 // The cell a finishing lane needs: its index, dd and dd's reciprocal pair,
@@ -1163,10 +1165,10 @@ __device__ __forceinline__ FinC finc_load(const Dev& d, int t) {
 }
 // One group's step (threads 128 g .. 128 g + 127): in the term phases lane l
 // holds the group's l-th active pair (p; p.j < 0 past the last pair) and nbv
-// its neighbour's hWA; in the finishing phase warp `role` finishes local
-// cells 4 role .. 4 role + 3 (8 lanes per cell, lane r variable r; fn the
-// lane's cell, fn.i < 0 past the last cell).  The phases, barriers and
-// expressions are sweep4w_compute's.
+// its neighbour's hWA; in the finishing phase the group's thread x = 32 role
+// + lane finishes variable x % V of local cell x / V (fn: that cell, fn.i < 0
+// past the last cell).  The phases, barriers and expressions are
+// sweep4w_compute's.
 template <int NSP, bool FWD, int G>
 __device__ __forceinline__ void sweepc_compute(const Dev& d, const ThermoDev<NSP>& th, const PairPre<NSP>& p,
                                                const double* nbv, const FinC& fn) {
@@ -1174,16 +1176,17 @@ __device__ __forceinline__ void sweepc_compute(const Dev& d, const ThermoDev<NSP
   const int NE = d.NE, gi = G > 1 ? (int)(threadIdx.x >> 7) : 0, role = (threadIdx.x >> 5) & 3,
             lane = threadIdx.x & 31, q = p.cs & 3;
   const bool act = p.j >= 0;
-  __shared__ double wsc_g[G][FLOWC_CELLS * V * 4];
+  constexpr int CAP = flowc_cells(V);
+  __shared__ double wsc_g[G][CAP * V * 4];
   __shared__ double cs1_g[G][32], cq_g[G][32], cdp_g[G][32], cdu_g[G][32], cdv_g[G][32], cdn_g[G][32];
   double* wsm = wsc_g[gi];
   double *xs1 = cs1_g[gi], *xq = cq_g[gi], *xdp = cdp_g[gi], *xdu = cdu_g[gi], *xdv = cdv_g[gi], *xdn = cdn_g[gi];
   const int b5 = 5 + 3 * gi, b6 = 6 + 3 * gi, b7 = 7 + 3 * gi;
-  const int r = lane & 7;
-  const bool fvalid = fn.i >= 0 && r < V;
+  const int x = role * 32 + lane, fc = x / V, r = x - fc * V;
+  const bool fvalid = fc < CAP && fn.i >= 0;
   const int fi = fvalid ? fn.i : 0;
   const double R = fvalid ? __ldcg(d.hWA + r * NE + fi) : 0.0;
-  double* w = wsm + ((p.cs >> 2) & (FLOWC_CELLS - 1)) * V * 4;
+  double* w = wsm + min(p.cs >> 2, CAP - 1) * V * 4;
   const double aF = p.aF, unormal = p.unormal;
   const double drr = nbv[0], dru = nbv[1], drv = nbv[2], dre = nbv[3];
   double dry[NSP];
@@ -1246,7 +1249,7 @@ __device__ __forceinline__ void sweepc_compute(const Dev& d, const ThermoDev<NSP
   }
   bar_named(b7, 128);
   if (!fvalid) return;
-  const double* wf = wsm + (role * 4 + (lane >> 3)) * V * 4;
+  const double* wf = wsm + fc * V * 4;
   double df = 0.0;
 #pragma unroll
   for (int sl = 0; sl < 4; ++sl)
@@ -1275,7 +1278,7 @@ __device__ __forceinline__ void sweepc_compute(const Dev& d, const ThermoDev<NSP
 // only joins the hand-over.
 template <int NSP, int G>
 __global__ void __launch_bounds__(flowc_threads(G), 1) k_lusgs_flowc(const Dev d, const ThermoDev<NSP> th, const FlowDev f) {
-  constexpr int V = 3 + NSP, T34 = 128 * G + 32, SLOT = flowc_slot_bytes<NSP, G>();
+  constexpr int V = 3 + NSP, T34 = 128 * G + 32, SLOT = flowc_slot_bytes<NSP, G>(), CAP = flowc_cells(V);
   extern __shared__ __align__(16) uint8_t flowc_smem[];
   auto slot_pre = [&](int s) { return reinterpret_cast<PairPre<NSP>*>(flowc_smem + s * SLOT); };
   auto slot_fin = [&](int s) {
@@ -1325,10 +1328,10 @@ __global__ void __launch_bounds__(flowc_threads(G), 1) k_lusgs_flowc(const Dev d
           pl = k < nf ? pair_load<NSP, true>(d, e >> 2, e & 3, tg) : pair_load<NSP, false>(d, e >> 2, e & 3, tg);
         }
         pre[32 * g + lane] = pl;
-        if (lane < FLOWC_CELLS) {
+        if (lane < CAP) {
           FinC fc = {-1, 0, 1.0, 1.0, 0.0};
           if (lane < nc) fc = k < nf ? finc_load<true>(d, tg + lane) : finc_load<false>(d, tg + lane);
-          fin[FLOWC_CELLS * g + lane] = fc;
+          fin[CAP * g + lane] = fc;
         }
         tg += nc;
       }
@@ -1392,9 +1395,9 @@ __global__ void __launch_bounds__(flowc_threads(G), 1) k_lusgs_flowc(const Dev d
       bar_named(3, T34);
       const int sl = k % FLOWC_NBUF;
       // the group's first cell exists iff the group has work in this pass
-      if (s_go[sl] && slot_fin(sl)[FLOWC_CELLS * gi].i >= 0) {
+      if (s_go[sl] && slot_fin(sl)[CAP * gi].i >= 0) {
         const PairPre<NSP> p = slot_pre(sl)[32 * gi + lane];
-        const FinC fn = slot_fin(sl)[FLOWC_CELLS * gi + role * 4 + (lane >> 3)];
+        const FinC fn = slot_fin(sl)[CAP * gi + min((role * 32 + lane) / V, CAP - 1)];
         double nbv[V];
 #pragma unroll
         for (int v = 0; v < V; ++v) nbv[v] = p.j >= 0 ? __ldcg(d.hWA + (size_t)v * d.NE + p.j) : 0.0;
@@ -1569,6 +1572,9 @@ template <int NSP>
 cudaError_t mixed_lusgs_flow(const Dev&, const void*, const void*, const FlowDev&, int, cudaStream_t);
 template <int NSP> int mixed_flow_occupancy();
 template <int NSP>
+cudaError_t mixed_lusgs_flowc(const Dev&, const void*, const void*, const FlowDev&, int, int, cudaStream_t);
+template <int NSP> int mixed_flowc_occupancy(int);
+template <int NSP>
 void chem_source(const Dev&, const void*, double, int, int*, int*, unsigned*, unsigned*, cudaStream_t);
 template <int NSP>
 void chem_batch(const void*, const double*, const double*, int, double*, int*, double, int, unsigned*, unsigned*,
@@ -1619,7 +1625,8 @@ struct rc_ctx {
   int flow_g = 1;                 // the groups of the FP64 dataflow launch
   bool can_flowc[FLOWC_GMAX] = {};  // the device can co-schedule the k_lusgs_flowc grid (per G)
   FlowDev flowc[FLOWC_GMAX] = {};   // compact pass tables for G = 1, 2 groups
-  bool flow_c = false;              // the FP64 dataflow launch is k_lusgs_flowc (flow_g groups)
+  bool flow_c = false;              // the dataflow launch is k_lusgs_flowc / k_lusgs_flowc32 (flow_g groups)
+  bool can_flowc32[FLOWC_GMAX] = {};  // the device can co-schedule the k_lusgs_flowc32 grid (per G)
   int pers_grid = 0;             // blocks of the persistent launch (one per SM)
   unsigned* lvl_count = nullptr; // per-level completion counters of the persistent launch
   int nlevels = 0;
@@ -1760,7 +1767,7 @@ SweepOrder sweep_order(int NE, const NF& nface, const std::vector<int>& cother) 
 // (same sweep) of the neighbours it reads that other blocks own.
 //
 // Compact passes (groups > 0, k_lusgs_flowc): the run is cut into up to
-// `groups` groups of consecutive positions, each of at most FLOWC_CELLS cells
+// `groups` groups of consecutive positions, each of at most `cap` cells
 // and FLOWC_PAIRS active (position, slot) pairs, filled greedily; plist
 // lists each group's pairs in (position, slot) order.
 struct FlowPlan {
@@ -1780,7 +1787,7 @@ inline bool sweep_slot(int NE, const NF& nface, const std::vector<int>& cother, 
 }
 template <class NF>
 FlowPlan flow_plan(int NE, int G, const NF& nface, const std::vector<int>& cother, const SweepOrder& so,
-                   int width = 8, int groups = 0) {
+                   int width = 8, int groups = 0, int cap = 0) {
   FlowPlan fp;
   fp.C = (NE + G - 1) / G;
   const int C = fp.C;
@@ -1800,7 +1807,7 @@ FlowPlan flow_plan(int NE, int G, const NF& nface, const std::vector<int>& cothe
           e = t;
           for (int g = 0; g < groups; ++g) {
             int nc = 0, np = 0;
-            while (e < off[l + 1] && lst[e] / C == own && nc < FLOWC_CELLS) {
+            while (e < off[l + 1] && lst[e] / C == own && nc < cap) {
               int a = 0;
               for (int q = 0; q < 4; ++q) a += sweep_slot(NE, nface, cother, dir, lst[e], q) ? 1 : 0;
               if (np + a > FLOWC_PAIRS) break;
@@ -2055,6 +2062,13 @@ void q_gather(rc_ctx* c) {
 // Sweeps of the mixed-precision modes: FP32 off-diagonal terms, FP64 division.
 template <int NSP>
 void q_sweeps32(rc_ctx* c) {
+  if (!c->persistent && c->wide == 4 && c->flow_c && c->flow_g <= FLOWC_GMAX && c->can_flowc32[c->flow_g - 1]) {
+    // compact passes; the Newton update runs inside the dataflow launch
+    mixed_lusgs_flowc<NSP>(c->d, c->thermo32.data(), c->thermo.data(), c->flowc[c->flow_g - 1], c->flow_g,
+                           c->flow_grid, c->stream);
+    c->launches += 1;
+    return;
+  }
   if (!c->persistent && c->wide == 4 && c->can_flow32) {
     // the Newton update runs inside the dataflow launch
     mixed_lusgs_flow<NSP>(c->d, c->thermo32.data(), c->thermo.data(), c->flows[0], c->flow_grid, c->stream);
@@ -2612,7 +2626,8 @@ int init_impl(const rc_mesh* m, const rc_thermo* t, const rc_config* g, const Ba
     for (int gr = 1; gr <= FLOW_GMAX + FLOWC_GMAX; ++gr) {
       // G = 1..3 groups of 8 positions, then the compact plans of 1..2 groups
       const int cg = gr > FLOW_GMAX ? gr - FLOW_GMAX : 0;
-      FlowPlan fp = cg ? flow_plan(NE, G, nface, cother, so, FLOWC_CELLS * cg, cg) : flow_plan(NE, G, nface, cother, so, 8 * gr);
+      const int cap = flowc_cells(c->V);
+      FlowPlan fp = cg ? flow_plan(NE, G, nface, cother, so, cap * cg, cg, cap) : flow_plan(NE, G, nface, cother, so, 8 * gr);
       std::vector<int>& pstart = fp.pstart;
       std::vector<int>& pcount = fp.pcount;
       std::vector<int>& doff = fp.doff;
@@ -2703,6 +2718,11 @@ int init_impl(const rc_mesh* m, const rc_thermo* t, const rc_config* g, const Ba
     cudaGetLastError();  // an attribute or occupancy query that failed leaves can_flow false
     occ32 = c->NSP == 1 ? mixed_flow_occupancy<1>() : mixed_flow_occupancy<4>();
     c->can_flow32 = coop && nsm > 0 && occ32 >= 1 && c->flow_grid == nsm;
+    for (int g = 1; g <= FLOWC_GMAX; ++g) {
+      const int o = c->NSP == 1 ? mixed_flowc_occupancy<1>(g) : mixed_flowc_occupancy<4>(g);
+      c->can_flowc32[g - 1] = coop && nsm > 0 && o >= 1 && c->flow_grid == nsm;
+    }
+    cudaGetLastError();
   }
   *out = c;
   return RC_OK;
@@ -2711,17 +2731,17 @@ int init_impl(const rc_mesh* m, const rc_thermo* t, const rc_config* g, const Ba
 }  // namespace
 
 // The plan with passes of up to `width` positions; stats as rc_flow_plan_check.
-// groups > 0: the compact plan of that many groups of FLOWC_CELLS cells.
+// groups > 0: the compact plan of that many groups of at most `cap` cells.
 int flow_plan_check_width(int ne, int nblocks, const std::vector<int>& nf, const std::vector<int>& co,
-                          const SweepOrder& so, int width, long long* stats, int groups = 0) {
-  const FlowPlan fp = groups > 0 ? flow_plan(ne, nblocks, nf, co, so, FLOWC_CELLS * groups, groups)
+                          const SweepOrder& so, int width, long long* stats, int groups = 0, int cap = 0) {
+  const FlowPlan fp = groups > 0 ? flow_plan(ne, nblocks, nf, co, so, cap * groups, groups, cap)
                                  : flow_plan(ne, nblocks, nf, co, so, width);
-  if (groups > 0) width = FLOWC_CELLS * groups;
+  if (groups > 0) width = cap * groups;
   const int P = (int)fp.pstart.size(), C = fp.C;
   bool ok = true;
   long long npass[2] = {0, 0}, maxdep = 0;
   // compact plans: the groups of a pass split its positions in order; a
-  // group holds at most FLOWC_CELLS cells and lists exactly their active
+  // group holds at most `cap` cells and lists exactly their active
   // (position, slot) pairs, at most FLOWC_PAIRS, in (position, slot) order
   if (groups > 0) {
     if ((int)fp.gcell.size() != P * groups || (int)fp.poff.size() != P * groups + 1 || fp.poff[0] != 0) ok = false;
@@ -2730,7 +2750,7 @@ int flow_plan_check_width(int ne, int nblocks, const std::vector<int>& nf, const
       int t = fp.pstart[pz], tot = 0;
       for (int g = 0; g < groups && ok; ++g) {
         const int nc = fp.gcell[pz * groups + g], e0 = fp.poff[pz * groups + g], e1 = fp.poff[pz * groups + g + 1];
-        if (nc < 0 || nc > FLOWC_CELLS || e1 - e0 < 0 || e1 - e0 > FLOWC_PAIRS) { ok = false; break; }
+        if (nc < 0 || nc > cap || e1 - e0 < 0 || e1 - e0 > FLOWC_PAIRS) { ok = false; break; }
         int e = e0;
         for (int u = t; u < t + nc && ok; ++u)
           for (int q = 0; q < 4 && ok; ++q)
@@ -2845,14 +2865,17 @@ int rc_flow_plan_check(int ne, int nblocks, const int* nface, const int* cother,
   }
   const SweepOrder so = sweep_order(ne, nf, co);
   int st = RC_OK;
-  for (int gr = FLOWC_GMAX; gr >= 1 && st == RC_OK; --gr) st = flow_plan_check_width(ne, nblocks, nf, co, so, 0, stats, gr);
+  for (int nv : {4, 7})  // the compact plans of the one- and four-species builds
+    for (int gr = FLOWC_GMAX; gr >= 1 && st == RC_OK; --gr)
+      st = flow_plan_check_width(ne, nblocks, nf, co, so, 0, stats, gr, flowc_cells(nv));
   for (int gr = FLOW_GMAX; gr >= 1 && st == RC_OK; --gr) st = flow_plan_check_width(ne, nblocks, nf, co, so, 8 * gr, stats);
   return st;
 }
 
-int rc_flow_plan_stats(int ne, int nblocks, const int* nface, const int* cother, int groups, int compact,
+int rc_flow_plan_stats(int ne, int nblocks, const int* nface, const int* cother, int groups, int compact, int nvar,
                        long long* stats) {
   if (ne < 1 || nblocks < 1 || !nface || !cother || !stats) return RC_ERR_ARG;
+  if (compact && (nvar < 3 || nvar > 16)) return RC_ERR_ARG;
   if (compact ? (groups < 1 || groups > FLOWC_GMAX) : (groups < 1 || groups > FLOW_GMAX)) return RC_ERR_ARG;
   std::vector<int> nf(nface, nface + ne);
   std::vector<int> co(cother, cother + 4 * (size_t)ne);
@@ -2864,7 +2887,7 @@ int rc_flow_plan_stats(int ne, int nblocks, const int* nface, const int* cother,
     }
   }
   const SweepOrder so = sweep_order(ne, nf, co);
-  return compact ? flow_plan_check_width(ne, nblocks, nf, co, so, 0, stats, groups)
+  return compact ? flow_plan_check_width(ne, nblocks, nf, co, so, 0, stats, groups, flowc_cells(nvar))
                  : flow_plan_check_width(ne, nblocks, nf, co, so, 8 * groups, stats);
 }
 
@@ -3083,8 +3106,10 @@ int rc_autotune(rc_ctx* c, int iters, char* report, int report_len) {
       if (c->can_flow[g - 1]) cands.push_back({false, 128, 8, 4, g, false});
     for (int g = 1; g <= FLOWC_GMAX; ++g)
       if (c->can_flowc[g - 1]) cands.push_back({false, 128, 8, 4, g, true});
-  } else if (c->can_flow32) {
-    cands.push_back({false, 128, 8, 4, 1, false});
+  } else {
+    if (c->can_flow32) cands.push_back({false, 128, 8, 4, 1, false});
+    for (int g = 1; g <= FLOWC_GMAX; ++g)
+      if (c->can_flowc32[g - 1]) cands.push_back({false, 128, 8, 4, g, true});
   }
   auto name = [](const Cand& k) {
     const std::string fl = k.fc ? "flowc" : "flow";

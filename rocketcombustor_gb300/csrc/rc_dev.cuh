@@ -226,6 +226,11 @@ struct FlowDev {
   const int* poff;
   const int* plist;
 };
+// Compact passes: at most FLOWC_PAIRS active pairs per group (one per lane
+// of a warp) and flowc_cells(V) cells, the cells that 128 finishing lanes
+// hold at V lanes per cell (18 for four species, 32 for one).
+constexpr int FLOWC_PAIRS = 32;
+__host__ __device__ constexpr int flowc_cells(int V) { return 128 / V < 32 ? 128 / V : 32; }
 
 // Dataflow LU-SGS: pass flags.  wait_flag: the calling thread waits until
 // the flag reaches `epoch` (acquire); bounded like wait_count.  set_flag

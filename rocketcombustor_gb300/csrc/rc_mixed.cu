@@ -554,6 +554,38 @@ __device__ __forceinline__ SweepPre32<NSP> sweep_load32(const Dev& d, int t, int
   }
   return p;
 }
+// The FP32 off-diagonal terms of one face slot (P: SweepPre32 or PairPre32;
+// nb: the neighbour's FP32 increment dU32, V values) into c[V].
+template <int NSP, class P>
+__device__ __forceinline__ void terms32(const ThermoDev32<NSP>& th, const P& p, const float* nb, float* c) {
+  const float dx = p.dx, dy = p.dy, pp = p.pp, uu = p.uu, vv = p.vv, tt = p.tt, rr = p.rr, gama = p.gama,
+              roe = p.roe;
+  const float rou = rr * uu, rov = rr * vv;
+  const float drr = nb[0], dru = nb[1], drv = nb[2], dre = nb[3];
+  float dry[NSP], s = 0.f;
+#pragma unroll
+  for (int k = 0; k < NSP - 1; ++k) { dry[k] = nb[4 + k]; s += dry[k]; }
+  dry[NSP - 1] = drr - s;
+  const float rinv = 1.f / rr;
+  const float duu = (dru - uu * drr) * rinv;
+  const float dvv = (drv - vv * drr) * rinv;
+  float s1 = 0.f, s2 = 0.f;
+#pragma unroll
+  for (int k = 0; k < NSP; ++k) {
+    s1 += p.cs[k] * dry[k];
+    s2 += th.R[k] * dry[k];
+  }
+  const float gm1 = gama - 1.f;
+  const float dpp = gm1 * (dre - s1 + tt * s2 * gama / gm1 - 0.5f * (dru * uu + duu * rou + drv * vv + dvv * rov));
+  const float un = uu * dx + vv * dy, dun = duu * dx + dvv * dy;
+  const float aF = p.aF;
+  c[0] = 0.5f * (-aF * drr + dru * dx + drv * dy);
+  c[1] = 0.5f * (-aF * dru + dru * un + rou * dun + dpp * dx);
+  c[2] = 0.5f * (-aF * drv + drv * un + rov * dun + dpp * dy);
+  c[3] = 0.5f * (-aF * dre + dun * (roe + pp) + un * (dre + dpp));
+#pragma unroll
+  for (int k = 0; k < NSP - 1; ++k) c[4 + k] = 0.5f * (-aF * dry[k] + dry[k] * un + rr * p.Yk[k] * dun);
+}
 // L2: read the sweep's values (own residual, the neighbour's FP32 increment)
 // through L2, as the dataflow launch needs (other SMs write them during it)
 template <int NSP, bool FWD, bool L2 = false>
@@ -572,35 +604,10 @@ __device__ __forceinline__ void sweep_compute32(const Dev& d, const ThermoDev32<
 #pragma unroll
   for (int k = 0; k < V; ++k) c[k] = 0.f;
   if (p.act) {
-    const int j = p.j;
-    const float dx = p.dx, dy = p.dy, pp = p.pp, uu = p.uu, vv = p.vv, tt = p.tt, rr = p.rr, gama = p.gama,
-                roe = p.roe;
-    const float rou = rr * uu, rov = rr * vv;
-    const float drr = ldf(d.dU32 + 0 * NE + j), dru = ldf(d.dU32 + 1 * NE + j), drv = ldf(d.dU32 + 2 * NE + j),
-                dre = ldf(d.dU32 + 3 * NE + j);
-    float dry[NSP], s = 0.f;
+    float nb[V];
 #pragma unroll
-    for (int k = 0; k < NSP - 1; ++k) { dry[k] = ldf(d.dU32 + (4 + k) * NE + j); s += dry[k]; }
-    dry[NSP - 1] = drr - s;
-    const float rinv = 1.f / rr;
-    const float duu = (dru - uu * drr) * rinv;
-    const float dvv = (drv - vv * drr) * rinv;
-    float s1 = 0.f, s2 = 0.f;
-#pragma unroll
-    for (int k = 0; k < NSP; ++k) {
-      s1 += p.cs[k] * dry[k];
-      s2 += th.R[k] * dry[k];
-    }
-    const float gm1 = gama - 1.f;
-    const float dpp = gm1 * (dre - s1 + tt * s2 * gama / gm1 - 0.5f * (dru * uu + duu * rou + drv * vv + dvv * rov));
-    const float un = uu * dx + vv * dy, dun = duu * dx + dvv * dy;
-    const float aF = p.aF;
-    c[0] = 0.5f * (-aF * drr + dru * dx + drv * dy);
-    c[1] = 0.5f * (-aF * dru + dru * un + rou * dun + dpp * dx);
-    c[2] = 0.5f * (-aF * drv + drv * un + rov * dun + dpp * dy);
-    c[3] = 0.5f * (-aF * dre + dun * (roe + pp) + un * (dre + dpp));
-#pragma unroll
-    for (int k = 0; k < NSP - 1; ++k) c[4 + k] = 0.5f * (-aF * dry[k] + dry[k] * un + rr * p.Yk[k] * dun);
+    for (int k = 0; k < V; ++k) nb[k] = ldf(d.dU32 + k * NE + p.j);
+    terms32<NSP>(th, p, nb, c);
   }
   // terms in slot order through the warp's shared scratch (see sweep_compute)
   const int lane = threadIdx.x & 31, base = lane & ~3;
@@ -884,6 +891,299 @@ __global__ void __launch_bounds__(FLOW32_THREADS, 1) k_lusgs_flow32(const Dev d,
   }
 }
 
+// Both FP32 sweeps as a dataflow on the compact pass tables of k_lusgs_flowc
+// (rc_core.cu): a pass is split into G groups of at most flowc_cells(V)
+// cells and 32 active (cell, slot) pairs.  Group g is two warps (2g, 2g+1):
+// warp 2g forms the FP32 terms of its 32 pairs (terms32, one pair per lane)
+// into the group's [cell][variable][slot] scratch, then both warps finish the
+// group's cells in two rounds, thread x = 64 round + 32 h + lane taking
+// variable x % V of cell x / V:
+// the terms of the active slots added in slot order from +0 (the inactive
+// slots' +0 terms of k_lusgs_flow32 leave such a sum unchanged: with FP32
+// denormals flushed every partial sum is normal or +0), then the FP64
+// division by the diagonal and the FP32 copy.  The work around a pass is
+// k_lusgs_flowc's: two staging warps fill a ring of FLOWC32_NBUF shared
+// slots ahead of the compute warps, and a coordinator warp looks at the next
+// pass's flags, hands it over (barrier 3) once it is staged and the current
+// pass is done (barrier 4), then publishes the finished pass; s_go[slot]
+// (0 after a give-up) keeps both warps of a group on the same path.  Two
+// more warps run the FP64 Newton update of each finished backward pass
+// during the sweep, as in k_lusgs_flow32 (the sweeps read only the FP32
+// copies PA32, cst32 of the state).  Every wait is bounded (ERR_SYNC).
+constexpr int FLOWC32_NBUF = 4;
+__host__ __device__ constexpr int flowc32_threads(int G) { return 32 * (2 * G + 5); }
+template <int NSP>
+struct PairPre32 {
+  int j;   // the neighbour (-1: no pair in this lane)
+  int cq;  // the pair's cell within its group << 2 | its slot
+  float dx, dy, pp, uu, vv, tt, rr, gama, roe, aF;
+  float cs[NSP];  // h_k of the neighbour
+  float Yk[NSP > 1 ? NSP - 1 : 1];
+};
+// sweep_load32's reads for one active pair (position t, slot q)
+template <int NSP, bool FWD>
+__device__ __forceinline__ PairPre32<NSP> pair_load32(const Dev& d, int t, int q, int tg) {
+  constexpr int DIR = FWD ? 0 : 1;
+  const int NE = d.NE, NF = d.NF;
+  PairPre32<NSP> p;
+  const int j = d.swj[DIR][q * NE + t], fs = d.swf[DIR][q * NE + t], f = fs >= 0 ? fs : ~fs;
+  p.j = j;
+  p.cq = ((t - tg) << 2) | q;
+  p.dx = d.fvec32[f];
+  p.dy = d.fvec32[NF + f];
+  if (fs < 0) { p.dx = -p.dx; p.dy = -p.dy; }
+  p.pp = d.PA32[0 * NE + j]; p.uu = d.PA32[1 * NE + j]; p.vv = d.PA32[2 * NE + j]; p.tt = d.PA32[3 * NE + j];
+  p.rr = d.cst32[0 * NE + j]; p.gama = d.cst32[1 * NE + j]; p.roe = d.cst32[2 * NE + j];
+  p.aF = d.alpaF32[f];
+#pragma unroll
+  for (int k = 0; k < NSP; ++k) p.cs[k] = d.cst32[(3 + k) * NE + j];
+#pragma unroll
+  for (int k = 0; k < NSP - 1; ++k) p.Yk[k] = d.PA32[(4 + k) * NE + j];
+  return p;
+}
+struct FinC32 {
+  int i, mask;
+  double rdd;  // 1 / dd of the cell
+};
+template <bool FWD>
+__device__ __forceinline__ FinC32 finc_load32(const Dev& d, int t) {
+  constexpr int DIR = FWD ? 0 : 1;
+  FinC32 f;
+  const int NE = d.NE;
+  f.i = d.swi[DIR][t];
+  f.rdd = 1.0 / d.dd[f.i];
+  f.mask = 0;
+#pragma unroll
+  for (int q = 0; q < 4; ++q) f.mask |= (d.swj[DIR][q * NE + t] >= 0 ? 1 : 0) << q;
+  return f;
+}
+template <int NSP, int G>
+__global__ void __launch_bounds__(flowc32_threads(G), 1) k_lusgs_flowc32(const Dev d, const ThermoDev32<NSP> th,
+                                                                        const ThermoDev<NSP> th64, const FlowDev f) {
+  constexpr int V = 3 + NSP, T34 = 64 * G + 32, CW = 2 * G;  // compute warps 0 .. CW-1
+  constexpr int CAP = flowc_cells(V);
+  __shared__ PairPre32<NSP> s_pre[FLOWC32_NBUF][32 * G];
+  __shared__ FinC32 s_fin[FLOWC32_NBUF][CAP * G];
+  __shared__ float wsc[G][CAP * V * 4];
+  __shared__ int s_cells[2][32];
+  __shared__ unsigned s_epoch;
+  __shared__ volatile int s_bad, s_consumed, s_done;
+  __shared__ volatile int s_slot[FLOWC32_NBUF], s_go[FLOWC32_NBUF];
+  if (threadIdx.x == 0) {
+    s_epoch = ld_acquire(f.ctr) + 1u;
+    s_bad = 0;
+    s_consumed = 0;
+    s_done = 0;
+    for (int s = 0; s < FLOWC32_NBUF; ++s) { s_slot[s] = 0; s_go[s] = 0; }
+  }
+  __syncthreads();
+  const unsigned epoch = s_epoch;
+  const int b = blockIdx.x, lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const int f0 = f.boff[0][b], b0 = f.boff[1][b];
+  const int nf = f.boff[0][b + 1] - f0, n = nf + (f.boff[1][b + 1] - b0);
+  auto pass_of = [&](int k) { return k < nf ? f.blist[0][f0 + k] : f.blist[1][b0 + k - nf]; };
+  auto give_up = [&]() {
+    if (lane == 0) {
+      s_bad = 1;
+      atomicOr(d.err, ERR_SYNC);
+    }
+    __syncwarp();
+  };
+  if (warp == CW + 1 || warp == CW + 2) {
+    // staging warp s: its passes s, s + 2, ... into the ring
+    const int s = warp - CW - 1;
+    for (int k = s; k < n && !s_bad; k += 2) {
+      for (unsigned spin = 0; s_consumed < k - FLOWC32_NBUF + 1 && !s_bad; ++spin)
+        if (spin >= d.spin_limit) give_up();
+      if (s_bad) break;
+      const int pz = pass_of(k), sl = k % FLOWC32_NBUF;
+      int tg = f.pstart[pz];
+#pragma unroll
+      for (int g = 0; g < G; ++g) {
+        const int nc = f.gcell[pz * G + g], e0 = f.poff[pz * G + g], np = f.poff[pz * G + g + 1] - e0;
+        PairPre32<NSP> pl;
+        pl.j = -1;
+        pl.cq = 0;
+        if (lane < np) {
+          const int e = f.plist[e0 + lane];
+          pl = k < nf ? pair_load32<NSP, true>(d, e >> 2, e & 3, tg) : pair_load32<NSP, false>(d, e >> 2, e & 3, tg);
+        }
+        s_pre[sl][32 * g + lane] = pl;
+        if (lane < CAP) {
+          FinC32 fc = {-1, 0, 0.0};
+          if (lane < nc) fc = k < nf ? finc_load32<true>(d, tg + lane) : finc_load32<false>(d, tg + lane);
+          s_fin[sl][CAP * g + lane] = fc;
+        }
+        tg += nc;
+      }
+      __syncwarp();
+      __threadfence_block();
+      if (lane == 0) s_slot[sl] = k + 1;
+      __syncwarp();
+    }
+  } else if (warp == CW) {
+    // the coordinator
+    auto staged = [&](int k) {
+      for (unsigned spin = 0; s_slot[k % FLOWC32_NBUF] != k + 1 && !s_bad; ++spin)
+        if (spin >= d.spin_limit) give_up();
+      __threadfence_block();
+    };
+    auto poll = [&](int k) {
+      if (s_bad) return;
+      const int pz = pass_of(k), d0 = f.doff[pz], nd = f.doff[pz + 1] - d0;
+      bool ok = true;
+      for (int u = lane; u < nd; u += 32) ok = ok && wait_flag(f.pflag + f.deps[d0 + u], epoch, d.err, d.spin_limit);
+      if (__any_sync(0xffffffffu, !ok)) give_up();
+    };
+    auto ready = [&](int k) -> bool {
+      if (s_bad) return true;
+      if (s_slot[k % FLOWC32_NBUF] != k + 1) return false;
+      const int pz = pass_of(k), d0 = f.doff[pz], nd = f.doff[pz + 1] - d0;
+      bool ok = true;
+      for (int u = lane; u < nd; u += 32) ok = ok && ld_acquire(f.pflag + f.deps[d0 + u]) >= epoch;
+      return __all_sync(0xffffffffu, ok) != 0;
+    };
+    auto hand_over = [&](int k) {
+      if (lane == 0) s_go[k % FLOWC32_NBUF] = s_bad ? 0 : 1;
+      __syncwarp();
+      __threadfence_block();
+      bar_arrive(3, T34);
+    };
+    if (n > 0) {
+      staged(0);
+      poll(0);
+      hand_over(0);
+    }
+    for (int k = 0; k < n; ++k) {
+      const bool more = k + 1 < n;
+      const bool go = more && ready(k + 1);
+      if (go) __threadfence_block();
+      bar_named(4, T34);
+      __threadfence_block();
+      if (lane == 0) {
+        s_consumed = k + 1;  // pass k's slot is free
+        s_done = k + 1;      // and its increments are final
+      }
+      if (go) hand_over(k + 1);
+      if (lane == 0 && !s_bad) st_release(f.pflag + pass_of(k), epoch);
+      if (more && !go) {
+        poll(k + 1);
+        staged(k + 1);
+        hand_over(k + 1);
+      }
+    }
+  } else if (warp < CW) {
+    const int gi = warp >> 1, h = warp & 1;
+    float* wsm = wsc[gi];
+    for (int k = 0; k < n; ++k) {
+      bar_named(3, T34);
+      const int sl = k % FLOWC32_NBUF;
+      if (s_go[sl] && s_fin[sl][CAP * gi].i >= 0) {
+        const bool fwd = k < nf;
+        // the own residuals of this warp's two rounds of (cell, variable)
+        int fc[2], r[2];
+        FinC32 fn[2];
+        double R[2];
+#pragma unroll
+        for (int u = 0; u < 2; ++u) {
+          const int x = 64 * u + 32 * h + lane;
+          fc[u] = x / V;
+          r[u] = x - fc[u] * V;
+          fn[u] = s_fin[sl][CAP * gi + min(fc[u], CAP - 1)];
+          if (fc[u] >= CAP) fn[u].i = -1;
+          R[u] = fn[u].i >= 0 ? __ldcg(d.hWA + r[u] * d.NE + fn[u].i) : 0.0;
+        }
+        if (h == 0) {
+          const PairPre32<NSP> p = s_pre[sl][32 * gi + lane];
+          if (p.j >= 0) {
+            float nb[V], c[V];
+#pragma unroll
+            for (int v = 0; v < V; ++v) nb[v] = __ldcg(d.dU32 + v * d.NE + p.j);
+            terms32<NSP>(th, p, nb, c);
+            float* w = wsm + min(p.cq >> 2, CAP - 1) * V * 4 + (p.cq & 3);
+#pragma unroll
+            for (int v = 0; v < V; ++v) w[v * 4] = c[v];
+          }
+        }
+        bar_named(5 + gi, 64);
+#pragma unroll
+        for (int u = 0; u < 2; ++u) {
+          if (fn[u].i < 0) continue;
+          const float* wf = wsm + fc[u] * V * 4 + r[u] * 4;
+          float df = 0.f;
+#pragma unroll
+          for (int q = 0; q < 4; ++q)
+            if ((fn[u].mask >> q) & 1) df += wf[q];
+          const double rdd = fn[u].rdd;
+          const double uo = fwd ? (R[u] - (double)df) * rdd : R[u] - (double)df * rdd;
+          d.hWA[r[u] * d.NE + fn[u].i] = uo;
+          d.dU32[r[u] * d.NE + fn[u].i] = (float)uo;
+        }
+        // the scratch is written again by the next pass only after barrier 3,
+        // which follows every warp's barrier 4 below
+      }
+      bar_arrive(4, T34);
+    }
+  } else {
+    // the Newton update warps (CW + 3, CW + 4): update warp u takes the
+    // backward passes nf + u, nf + u + 2, ... once finished, as many at a
+    // time as fill its 32 lanes with one cell each
+    const int u = warp - CW - 3;
+    int* cells = s_cells[u];
+    unsigned err = 0;
+    for (int k = nf + u; k < n;) {
+      for (unsigned spin = 0; s_done <= k && !s_bad; ++spin) {
+        if (spin >= d.spin_limit) give_up();
+        __nanosleep(256);
+      }
+      if (s_bad) break;
+      __threadfence_block();
+      const int avail = s_done;
+      const int kl = k + 2 * lane;
+      int cnt = 0, t0 = 0;
+      if (kl < avail) {
+        const int pz = pass_of(kl);
+        cnt = f.pcount[pz];
+        t0 = f.pstart[pz];
+      }
+      int incl = cnt;
+#pragma unroll
+      for (int o = 1; o < 32; o <<= 1) {
+        const int x = __shfl_up_sync(0xffffffffu, incl, o);
+        if (lane >= o) incl += x;
+      }
+      const bool take = kl < avail && incl <= 32;
+      const int ntake = __popc(__ballot_sync(0xffffffffu, take));
+      if (ntake == 0) {
+        // pass k alone holds more than 32 cells: 32 of them at a time
+        const int pz = pass_of(k), ts = f.pstart[pz], nc = f.pcount[pz];
+        for (int c0 = 0; c0 < nc; c0 += 32)
+          if (c0 + lane < nc) update_cell<NSP>(d, th64, d.swi[1][ts + c0 + lane], err);
+        __syncwarp();
+        k += 2;
+        continue;
+      }
+      if (take)
+        for (int c = 0; c < cnt; ++c) cells[incl - cnt + c] = t0 + c;
+      const int ncell = __shfl_sync(0xffffffffu, incl, ntake - 1);
+      __syncwarp();
+      if (lane < ncell) update_cell<NSP>(d, th64, d.swi[1][cells[lane]], err);
+      __syncwarp();
+      k += 2 * ntake;
+    }
+    flag(d, err);
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    __threadfence();
+    if (atomicAdd(f.ctr + 1, 1u) == gridDim.x - 1) {
+      f.ctr[1] = 0u;
+      __threadfence();
+      st_release(f.ctr, epoch);
+    }
+  }
+}
+
 // ------------------------------------------------------- host launchers ----
 inline unsigned nblk(long n, int t) { return (unsigned)((n + t - 1) / t); }
 
@@ -961,6 +1261,32 @@ cudaError_t mixed_lusgs_flow(const Dev& d, const void* th32, const void* th64, c
   return cudaLaunchKernelEx(&cfg, k_lusgs_flow32<NSP>, d, *static_cast<const ThermoDev32<NSP>*>(th32),
                             *static_cast<const ThermoDev<NSP>*>(th64), f);
 }
+// Cooperative launch of the compact dataflow FP32 sweeps (G groups) with the
+// fused FP64 Newton update, one block per SM.
+template <int NSP>
+cudaError_t mixed_lusgs_flowc(const Dev& d, const void* th32, const void* th64, const FlowDev& f, int G, int grid,
+                              cudaStream_t s) {
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = dim3((unsigned)grid);
+  cfg.blockDim = dim3(flowc32_threads(G));
+  cfg.stream = s;
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeCooperative;
+  attr[0].val.cooperative = 1;
+  cfg.attrs = attr;
+  cfg.numAttrs = 1;
+  const auto& t32 = *static_cast<const ThermoDev32<NSP>*>(th32);
+  const auto& t64 = *static_cast<const ThermoDev<NSP>*>(th64);
+  if (G == 2) return cudaLaunchKernelEx(&cfg, k_lusgs_flowc32<NSP, 2>, d, t32, t64, f);
+  return cudaLaunchKernelEx(&cfg, k_lusgs_flowc32<NSP, 1>, d, t32, t64, f);
+}
+template <int NSP>
+int mixed_flowc_occupancy(int G) {
+  int nb = 0;
+  if (G == 2) cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_lusgs_flowc32<NSP, 2>, flowc32_threads(2), 0);
+  else cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_lusgs_flowc32<NSP, 1>, flowc32_threads(1), 0);
+  return nb;
+}
 template <int NSP>
 int mixed_flow_occupancy() {
   int nb = 0;
@@ -992,7 +1318,10 @@ size_t mixed_thermo(const void* th64, void* out) {
   template int mixed_persistent_occupancy<N>();                                                                 \
   template cudaError_t mixed_lusgs_flow<N>(const Dev&, const void*, const void*, const FlowDev&, int,           \
                                            cudaStream_t);                                                       \
-  template int mixed_flow_occupancy<N>();
+  template int mixed_flow_occupancy<N>();                                                                       \
+  template cudaError_t mixed_lusgs_flowc<N>(const Dev&, const void*, const void*, const FlowDev&, int, int,      \
+                                            cudaStream_t);                                                      \
+  template int mixed_flowc_occupancy<N>(int);
 RC_MIXED_INST(1)
 RC_MIXED_INST(4)
 

@@ -58,21 +58,36 @@ def test_natural_order_plan_adds_nothing_to_the_critical_path(nx, ny):
 
 
 @pytest.mark.parametrize("nx,ny,order", [(24, 6, "natural"), (100, 20, "colored"), (100, 20, "random"),
-                                         (3000, 8, "natural")])
+                                         (3000, 8, "natural"), (9000, 4, "natural")])
 @pytest.mark.parametrize("groups", [1, 2])
-def test_compact_plan_is_consistent(nx, ny, order, groups):
-    """The compact plans of k_lusgs_flowc (groups of at most 16 cells and 32
-    active pairs, each group listing exactly its cells' active pairs) pass
-    every check and need no more passes than the 8-position plan of as many
-    groups; on the long, thin nozzle (about 13 cells of a level per block)
-    two compact groups end in as many steps as there are levels."""
+@pytest.mark.parametrize("nvar", [4, 7])
+def test_compact_plan_is_consistent(nx, ny, order, groups, nvar):
+    """The compact plans of k_lusgs_flowc (groups of at most 128 / nvar cells
+    and 32 active pairs, each group listing exactly its cells' active pairs)
+    pass every check and need no more passes than the 8-position plan of as
+    many groups; on the long, thin nozzle with about 13 cells of a level per
+    block two compact groups end in as many steps as there are levels, and
+    with about 39 they need more passes with one group than with two."""
     nface, cother = _graph(nx, ny, order)
-    st = rc.flow_plan_check(nface, cother, 152, groups=groups, compact=True)
+    st = rc.flow_plan_check(nface, cother, 152, groups=groups, compact=True, nvar=nvar)
     old = rc.flow_plan_check(nface, cother, 152, groups=groups)
     assert st["passes_fwd"] <= old["passes_fwd"] and st["passes_bwd"] <= old["passes_bwd"]
     assert st["levels_fwd"] + st["levels_bwd"] <= st["steps"] <= st["passes_fwd"] + st["passes_bwd"]
     if (nx, ny, groups) == (3000, 8, 2):
         assert st["steps"] == st["levels_fwd"] + st["levels_bwd"]
+    if (nx, ny) == (9000, 4) and groups == 2:
+        one = rc.flow_plan_check(nface, cother, 152, groups=1, compact=True, nvar=nvar)
+        assert st["passes_fwd"] < one["passes_fwd"]
+
+
+def test_compact_plan_of_the_benchmark_mesh_has_one_group_per_level():
+    """The 2,000,000-cell benchmark nozzle (2500 x 400): a block holds at most
+    17 cells (26 active pairs) of a level, within one group of the
+    four-species build (18 cells), so the compact plan with one group ends
+    in as many steps as there are levels."""
+    nface, cother = _graph(2500, 400, "natural")
+    st = rc.flow_plan_check(nface, cother, 152, groups=1, compact=True, nvar=7)
+    assert st["steps"] == st["levels_fwd"] + st["levels_bwd"] == 2402
 
 
 def test_bad_arguments_are_refused():
@@ -85,3 +100,5 @@ def test_bad_arguments_are_refused():
         rc.flow_plan_check(nface, cother, 0)
     with pytest.raises(rc.RcError):
         rc.flow_plan_check(nface, cother, 8, groups=3, compact=True)
+    with pytest.raises(rc.RcError):
+        rc.flow_plan_check(nface, cother, 8, groups=1, compact=True, nvar=2)

@@ -242,20 +242,24 @@ def test_dataflow_schedule_bit_identical_to_oracle(case_root, sched, monkeypatch
         s.close()
 
 
-@pytest.mark.parametrize("name,over", [("c1", {"nx": 3000, "ny": 8}), ("c2", {"nx": 3000, "ny": 8})])
+THIN = {"nx": 9000, "ny": 4}
+
+
+@pytest.mark.parametrize("name,over", [("c1", THIN), ("c2", THIN)])
 @pytest.mark.parametrize("sched", ["flowc", "flowc2"])
 def test_compact_dataflow_wide_levels_bit_identical_to_oracle(case_root, sched, name, over, monkeypatch):
-    """A long, thin nozzle (3000 x 8 columns of triangles, 48,000 cells) puts
-    about 13 cells of every level in each of the 152 blocks: the compact
-    passes hold up to 16 cells and 32 active (cell, face) pairs per group,
-    so some passes fill two groups (fewer passes with two groups than with
-    one).  The one-species inviscid and the four-species reacting viscous
-    physics, 20 iterations against the oracle, bit for bit."""
+    """A long, thin nozzle (9000 x 4 columns of triangles, 72,000 cells) puts
+    about 39 cells of every level in each of the 152 blocks: a compact group
+    holds up to 32 active (cell, face) pairs and 128 / V cells (32 for one
+    species, 18 for four), so passes fill two groups (fewer passes with two
+    groups than with one).  The one-species inviscid and the four-species
+    reacting viscous physics, 20 iterations against the oracle, bit for bit."""
     from test_flow_plan import _graph
 
+    nv = 4 if name == "c1" else 7
     nface, cother = _graph(over["nx"], over["ny"], "natural")
-    one = rc.flow_plan_check(nface, cother, 152, groups=1, compact=True)
-    two = rc.flow_plan_check(nface, cother, 152, groups=2, compact=True)
+    one = rc.flow_plan_check(nface, cother, 152, groups=1, compact=True, nvar=nv)
+    two = rc.flow_plan_check(nface, cother, 152, groups=2, compact=True, nvar=nv)
     assert two["passes_fwd"] < one["passes_fwd"] and two["passes_bwd"] < one["passes_bwd"]
     monkeypatch.setenv("RC_LUSGS_SCHEDULE", sched)
     d = make_case(case_root, name, **over)
@@ -268,6 +272,27 @@ def test_compact_dataflow_wide_levels_bit_identical_to_oracle(case_root, sched, 
     assert np.array_equal(PA, o.array("PA")), rel_linf(PA, o.array("PA"))
     assert np.array_equal(WA, o.array("WA")), rel_linf(WA, o.array("WA"))
     s.close()
+
+
+@pytest.mark.parametrize("name,over", [("c1", THIN), ("c2", THIN)])
+def test_compact_mixed_dataflow_equals_per_level_sweeps(case_root, name, over, monkeypatch):
+    """The mixed-precision compact dataflow launch (FP32 terms of the active
+    pairs only, groups of up to 16 cells, the FP64 Newton update inside the
+    launch) on the long, thin nozzle whose passes fill two groups: after 20
+    iterations its state is bit for bit that of the per-level FP32 sweeps
+    followed by k_update, with one group and with two."""
+    d = make_case(case_root, name, **over)
+    c = rc.Case(d)
+    states = {}
+    for sched in ("levels", "flowc", "flowc2"):
+        monkeypatch.setenv("RC_LUSGS_SCHEDULE", sched)
+        s = rc.Solver(c, precision=rc.RC_PREC_MIXED)
+        s.run(20)
+        states[sched] = s.get_state()
+        s.close()
+    for sched in ("flowc", "flowc2"):
+        assert np.array_equal(states["levels"][0], states[sched][0]), sched
+        assert np.array_equal(states["levels"][1], states[sched][1]), sched
 
 
 @pytest.mark.parametrize("sched", ["flow", "flow3", "flowc2"])
@@ -294,11 +319,12 @@ def test_dataflow_wait_timeout_is_reported(case_root, sched, monkeypatch):
     assert np.array_equal(PA, o.array("PA")) and np.array_equal(WA, o.array("WA"))
 
 
-@pytest.mark.parametrize("sched", ["flow", "persistent"])
+@pytest.mark.parametrize("sched", ["flow", "flowc2", "persistent"])
 def test_mixed_wait_timeout_is_reported(case_root, sched, monkeypatch):
     """The mixed-precision LU-SGS launches give up the same way: a poll limit
     of 1 ends the staging, hand-over and update-warp waits of the FP32 dataflow
-    launch (or the level waits of the FP32 persistent launch) with RC_ERR_SYNC;
+    launches (8-position or compact passes) or the level waits of the FP32
+    persistent launch with RC_ERR_SYNC;
     after the error is cleared and the state set again, five iterations give
     the bits of a clean mixed run from the same state."""
     monkeypatch.setenv("RC_LUSGS_SCHEDULE", sched)
