@@ -906,12 +906,16 @@ __global__ void __launch_bounds__(FLOW32_THREADS, 1) k_lusgs_flow32(const Dev d,
 // slots ahead of the compute warps, and a coordinator warp looks at the next
 // pass's flags, hands it over (barrier 3) once it is staged and the current
 // pass is done (barrier 4), then publishes the finished pass; s_go[slot]
-// (0 after a give-up) keeps both warps of a group on the same path.  Two
-// more warps run the FP64 Newton update of each finished backward pass
-// during the sweep, as in k_lusgs_flow32 (the sweeps read only the FP32
-// copies PA32, cst32 of the state).  Every wait is bounded (ERR_SYNC).
-constexpr int FLOWC32_NBUF = 4;
-__host__ __device__ constexpr int flowc32_threads(int G) { return 32 * (2 * G + 5); }
+// (0 after a give-up) keeps both warps of a group on the same path.
+// FLOWC32_UPD more warps run the FP64 Newton update of each finished
+// backward pass during the sweep, as in k_lusgs_flow32 (the sweeps read only
+// the FP32 copies PA32, cst32 of the state).  The update is FP64 work of
+// about a quarter of a plain FP64 iteration's face flux: two warps per SM
+// (k_lusgs_flow32) fall behind the compact sweep on a large mesh and finish
+// long after its last pass, so there are enough update warps to keep each
+// sub-partition's FP64 unit busy.  Every wait is bounded (ERR_SYNC).
+constexpr int FLOWC32_NBUF = 4, FLOWC32_UPD = 6;
+__host__ __device__ constexpr int flowc32_threads(int G) { return 32 * (2 * G + 3 + FLOWC32_UPD); }
 template <int NSP>
 struct PairPre32 {
   int j;   // the neighbour (-1: no pair in this lane)
@@ -965,7 +969,7 @@ __global__ void __launch_bounds__(flowc32_threads(G), 1) k_lusgs_flowc32(const D
   __shared__ PairPre32<NSP> s_pre[FLOWC32_NBUF][32 * G];
   __shared__ FinC32 s_fin[FLOWC32_NBUF][CAP * G];
   __shared__ float wsc[G][CAP * V * 4];
-  __shared__ int s_cells[2][32];
+  __shared__ int s_cells[FLOWC32_UPD][32];
   __shared__ unsigned s_epoch;
   __shared__ volatile int s_bad, s_consumed, s_done;
   __shared__ volatile int s_slot[FLOWC32_NBUF], s_go[FLOWC32_NBUF];
@@ -1125,9 +1129,10 @@ __global__ void __launch_bounds__(flowc32_threads(G), 1) k_lusgs_flowc32(const D
       bar_arrive(4, T34);
     }
   } else {
-    // the Newton update warps (CW + 3, CW + 4): update warp u takes the
-    // backward passes nf + u, nf + u + 2, ... once finished, as many at a
-    // time as fill its 32 lanes with one cell each
+    // the Newton update warps (CW + 3 ..): update warp u takes the backward
+    // passes nf + u, nf + u + UPD, ... once finished, as many at a time as
+    // fill its 32 lanes with one cell each
+    constexpr int UPD = FLOWC32_UPD;
     const int u = warp - CW - 3;
     int* cells = s_cells[u];
     unsigned err = 0;
@@ -1139,7 +1144,7 @@ __global__ void __launch_bounds__(flowc32_threads(G), 1) k_lusgs_flowc32(const D
       if (s_bad) break;
       __threadfence_block();
       const int avail = s_done;
-      const int kl = k + 2 * lane;
+      const int kl = k + UPD * lane;
       int cnt = 0, t0 = 0;
       if (kl < avail) {
         const int pz = pass_of(kl);
@@ -1160,7 +1165,7 @@ __global__ void __launch_bounds__(flowc32_threads(G), 1) k_lusgs_flowc32(const D
         for (int c0 = 0; c0 < nc; c0 += 32)
           if (c0 + lane < nc) update_cell<NSP>(d, th64, d.swi[1][ts + c0 + lane], err);
         __syncwarp();
-        k += 2;
+        k += UPD;
         continue;
       }
       if (take)
@@ -1169,7 +1174,7 @@ __global__ void __launch_bounds__(flowc32_threads(G), 1) k_lusgs_flowc32(const D
       __syncwarp();
       if (lane < ncell) update_cell<NSP>(d, th64, d.swi[1][cells[lane]], err);
       __syncwarp();
-      k += 2 * ntake;
+      k += UPD * ntake;
     }
     flag(d, err);
   }
