@@ -59,12 +59,12 @@ def algo_bytes_per_cell(V: int, nf_ne: float, viscous: bool, combustion: bool) -
 # dram__bytes_write.sum and sm__inst_executed_pipe_fp64.sum over the
 # subroutine's launches, divided by the cells: profiles/c4_500k_fp64_counters.md).
 # Both grow with the cells.
-NCU_DRAM_PER_CELL = {"timestep": 198.05, "reconstruction": 334.50, "flux_sourceterm": 672.79,
-                     "lu_sgs_steady": 651.65}
-NCU_FP64_INST_PER_CELL = {"timestep": 46.713, "reconstruction": 46.004, "flux_sourceterm": 128.919,
-                          "lu_sgs_steady": 74.476}
-NCU_TRAFFIC_SOURCE = ("ncu capture of one FP64 iteration of the same physics at 500,000 cells (dataflow LU-SGS; "
-                      "profiles/c4_500k_fp64_counters.md), scaled by cells")
+NCU_DRAM_PER_CELL = {"timestep": 199.5, "reconstruction": 339.2, "flux_sourceterm": 685.7,
+                     "lu_sgs_steady": 640.3}
+NCU_FP64_INST_PER_CELL = {"timestep": 46.72, "reconstruction": 46.00, "flux_sourceterm": 128.92,
+                          "lu_sgs_steady": 76.62}
+NCU_TRAFFIC_SOURCE = ("ncu capture of one FP64 iteration of the same physics at 500,000 cells (compact dataflow "
+                      "LU-SGS; profiles/c4_500k_fp64_counters.md), scaled by cells")
 
 
 def read_peaks():
@@ -122,9 +122,11 @@ def roofline(dom, sub_ms, ab, NE, peak, peak_kind, fp64) -> dict:
             "frac": d["hbm_frac"], "peak_source": peak_kind, "algorithmic_bytes_per_cell": ab[dom],
             "traffic": NCU_DRAM_PER_CELL[dom] * NE if dom in NCU_DRAM_PER_CELL else None,
             "traffic_source": NCU_TRAFFIC_SOURCE,
+            "binds": d["binds"], "fp64_frac": d.get("fp64_frac"),
             "fp64_peak": fp64, "per_subroutine": per,
-            "note": "LU-SGS is latency bound (a pass of a few cells per level, level after level along the "
-                    "reference cell order); the face and cell kernels are bound by the FP64 pipe"}
+            "note": "the face and cell kernels are bound by the FP64 pipe (fp64_frac of the FP64 rate measured "
+                    "here), not by HBM; LU-SGS is latency bound (a pass of a few cells per level, level after "
+                    "level along the reference cell order)"}
 
 
 class ClockSampler:
@@ -792,8 +794,8 @@ def surrogate_form(args, stream, flush, torch, rc, case, extra_pool=None):
     peak = read_peaks_tensor()
     out["inference"] = {"samples": int(xi.shape[0]), "samples_per_s": xi.shape[0] / t_inf,
                         "tflops": flops_sample * xi.shape[0] / t_inf / 1e12, "peak_bf16_tflops": peak,
-                        "note": "fused kernel: layer 0 and the output layer on the CUDA cores, the three 128x128 "
-                                "layers on tcgen05; FLOP counted for the whole network"}
+                        "note": "k_mlp_fwd16: all five layers on tcgen05 (F16 operands, FP32 accumulation in "
+                                "TMEM, packed-half GELU epilogue); FLOP counted for the whole network"}
     # steady iterations: integrated source vs surrogate source, same start
     forms = {}
     states = {}
