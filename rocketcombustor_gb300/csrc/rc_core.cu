@@ -1167,93 +1167,151 @@ __device__ __forceinline__ FinC finc_load(const Dev& d, int t) {
 // holds the group's l-th active pair (p; p.j < 0 past the last pair) and nbv
 // its neighbour's hWA; in the finishing phase the group's thread x = 32 role
 // + lane finishes variable x % V of local cell x / V (fn: that cell, fn.i < 0
-// past the last cell).  The phases, barriers and expressions are
-// sweep4w_compute's.
+// past the last cell).  The expressions are sweep4w_compute's, each rounded
+// operation the same in the same order, but the parts of every term that do
+// not wait for du, dv, dp or dun are formed in phase A, where the four warps
+// have room, so that fewer dependent FP64 operations follow (on GB300 a
+// warp's FP64 instruction holds its sub-partition's FP64 unit for 64
+// cycles, so the count per warp on the critical path sets the step's time):
+//   A  warp 0: s = 0 + dY_0 + dY_1 + dY_2, dY_3 = drho - s; s1 = 0 + sum h_k dY_k;
+//      es1 = dE - s1; S_k = -aF dY_k + dY_k un for k = 0, 1
+//      warp 1: dY; s2 = 0 + sum R_k dY_k; Q = (T s2) gamma / (gamma - 1)
+//      warp 2: du = (drho u - u drho) / rho; c0; a1 = drho u * u, a3 = drho v * v;
+//      P1 = -aF drho u + drho u un
+//      warp 3: dY; dv; P2 = -aF drho v + drho v un; A3 = -aF dE; S_2
+//   B  warp 3: dun = du nx + dv ny (barrier B6 to warps 0, 1), then the species
+//      terms half(S_k + ry_k dun)
+//      warp 2: X = ((a1 + du rho u) + a3) + dv rho v, dp = gm1 ((es1 + Q) - X / 2)
+//      (barrier B8 to warps 0, 1)
+//      warp 0: c1p = P1 + rho u dun; warp 1: c2p = P2 + rho v dun, c3p = A3 + dun (rho E + p)
+//   C  warp 0: c1 = half(c1p + dp nx); warp 1: c2 = half(c2p + dp ny);
+//      warp 2: c3 = half(c3p + un (dE + dp))
+// with 0 + x and 0.5 x on the integer pipe (plus_zero, half_of: the same bits).
 template <int NSP, bool FWD, int G>
 __device__ __forceinline__ void sweepc_compute(const Dev& d, const ThermoDev<NSP>& th, const PairPre<NSP>& p,
                                                const double* nbv, const FinC& fn) {
-  constexpr int V = 3 + NSP;
+  constexpr int V = 3 + NSP, NS = NSP > 1 ? NSP - 1 : 1;
   const int NE = d.NE, gi = G > 1 ? (int)(threadIdx.x >> 7) : 0, role = (threadIdx.x >> 5) & 3,
             lane = threadIdx.x & 31, q = p.cs & 3;
   const bool act = p.j >= 0;
   constexpr int CAP = flowc_cells(V);
   __shared__ double wsc_g[G][CAP * V * 4];
-  __shared__ double cs1_g[G][32], cq_g[G][32], cdp_g[G][32], cdu_g[G][32], cdv_g[G][32], cdn_g[G][32];
+  // per pair: es1, Q, du, dv, dun, dp, P1, P2, A3, c3p, S_0, S_1
+  __shared__ double xc_g[G][12][32];
   double* wsm = wsc_g[gi];
-  double *xs1 = cs1_g[gi], *xq = cq_g[gi], *xdp = cdp_g[gi], *xdu = cdu_g[gi], *xdv = cdv_g[gi], *xdn = cdn_g[gi];
-  const int b5 = 5 + 3 * gi, b6 = 6 + 3 * gi, b7 = 7 + 3 * gi;
+  double(*xc)[32] = xc_g[gi];
+  enum { ES1, XQ, XDU, XDV, XDN, XDP, XP1, XP2, XA3, XC3, XS0, XS1 };
+  const int B5 = 5 + 4 * gi, B6 = B5 + 1, B7 = B5 + 2, B8 = B5 + 3;
   const int x = role * 32 + lane, fc = x / V, r = x - fc * V;
   const bool fvalid = fc < CAP && fn.i >= 0;
   const int fi = fvalid ? fn.i : 0;
   const double R = fvalid ? __ldcg(d.hWA + r * NE + fi) : 0.0;
   double* w = wsm + min(p.cs >> 2, CAP - 1) * V * 4;
-  const double aF = p.aF, unormal = p.unormal;
+  const double aF = p.aF, un = p.unormal;
   const double drr = nbv[0], dru = nbv[1], drv = nbv[2], dre = nbv[3];
+  // the species increments dY_k (warps 0, 1 and 3)
   double dry[NSP];
 #pragma unroll
   for (int k = 0; k < NSP; ++k) dry[k] = 0.0;
-  if (role != 2 && act) {  // the species increments: warps 0, 1 and 3
+  if (role != 2 && act) {
     double s = 0.0;
+    if (NSP > 1) {
+      dry[0] = nbv[4];
+      s = plus_zero(dry[0]);
 #pragma unroll
-    for (int k = 0; k < NSP - 1; ++k) { dry[k] = nbv[4 + k]; s = s + dry[k]; }
+      for (int k = 1; k < NSP - 1; ++k) { dry[k] = nbv[4 + k]; s = s + dry[k]; }
+    }
     dry[NSP - 1] = drr - s;
   }
   // A
+  double S2 = 0.0;  // warp 3: S_{NSP-2}
   if (act) {
     if (role == 0) {
-      double s1 = 0.0;
+      double s1 = plus_zero(p.cs_h[0] * dry[0]);
 #pragma unroll
-      for (int k = 0; k < NSP; ++k) s1 = s1 + p.cs_h[k] * dry[k];
-      xs1[lane] = s1;
-      w[q] = 0.5 * (-aF * drr + dru * p.dx + drv * p.dy);
+      for (int k = 1; k < NSP; ++k) s1 = s1 + p.cs_h[k] * dry[k];
+      xc[ES1][lane] = dre - s1;
+      if (NSP > 1) xc[XS0][lane] = -aF * dry[0] + dry[0] * un;
+      if (NSP > 2) xc[XS1][lane] = -aF * dry[1] + dry[1] * un;
     } else if (role == 1) {
-      double s2 = 0.0;
+      double s2 = plus_zero(th.R[0] * dry[0]);
 #pragma unroll
-      for (int k = 0; k < NSP; ++k) s2 = s2 + th.R[k] * dry[k];
-      xq[lane] = div_rn(p.tt * s2 * p.gama, p.gm1, p.gmh, p.gml);
+      for (int k = 1; k < NSP; ++k) s2 = s2 + th.R[k] * dry[k];
+      xc[XQ][lane] = div_rn(p.tt * s2 * p.gama, p.gm1, p.gmh, p.gml);
     } else if (role == 2) {
-      xdu[lane] = div_rn(dru - p.uu * drr, p.rr, p.rrh, p.rrl);
+      xc[XDU][lane] = div_rn(dru - p.uu * drr, p.rr, p.rrh, p.rrl);
+      w[q] = half_of(-aF * drr + dru * p.dx + drv * p.dy);
+      xc[XP1][lane] = -aF * dru + dru * un;
     } else {
-      xdv[lane] = div_rn(drv - p.vv * drr, p.rr, p.rrh, p.rrl);
+      xc[XDV][lane] = div_rn(drv - p.vv * drr, p.rr, p.rrh, p.rrl);
+      xc[XP2][lane] = -aF * drv + drv * un;
+      xc[XA3][lane] = -aF * dre;
+      if (NSP > 3) S2 = -aF * dry[2] + dry[2] * un;
     }
   }
-  bar_named(b5, 128);
-  // B
+  // the X partials of warp 2, formed while the others finish phase A
+  double a1 = 0.0, a3 = 0.0;
+  if (role == 2 && act) {
+    a1 = dru * p.uu;
+    a3 = drv * p.vv;
+  }
+  bar_named(B5, 128);
+  // B, C
   if (role == 3) {
-    double dunormal = 0.0;
+    double dun = 0.0;
     if (act) {
-      dunormal = xdu[lane] * p.dx + xdv[lane] * p.dy;
-      xdn[lane] = dunormal;
+      dun = xc[XDU][lane] * p.dx + xc[XDV][lane] * p.dy;
+      xc[XDN][lane] = dun;
     }
-    bar_arrive(b6, 128);
+    bar_arrive(B6, 96);
     if (act) {
 #pragma unroll
-      for (int k = 0; k < NSP - 1; ++k) w[(4 + k) * 4 + q] = 0.5 * (-aF * dry[k] + dry[k] * unormal + p.ry[k] * dunormal);
+      for (int k = 0; k < NSP - 1; ++k) {
+        const double Sk = k == 0 ? xc[XS0][lane] : k == 1 ? xc[XS1][lane] : S2;
+        w[(4 + k) * 4 + q] = half_of(Sk + p.ry[k] * dun);
+      }
     }
-  } else {
-    if (role == 2 && act) {
-      const double duu = xdu[lane], dvv = xdv[lane];
-      const double X = dru * p.uu + duu * p.rou + drv * p.vv + dvv * p.rov;
-      xdp[lane] = p.gm1 * (dre - xs1[lane] + xq[lane] - 0.5 * X);
-    }
-    bar_named(b6, 128);
-    // C
+  } else if (role == 2) {
+    double dpp = 0.0;
     if (act) {
-      const double dpp = xdp[lane], dunormal = xdn[lane];
-      double ck;
-      if (role == 0) ck = 0.5 * (-aF * dru + dru * unormal + p.rou * dunormal + dpp * p.dx);
-      else if (role == 1) ck = 0.5 * (-aF * drv + drv * unormal + p.rov * dunormal + dpp * p.dy);
-      else ck = 0.5 * (-aF * dre + dunormal * p.roepp + unormal * (dre + dpp));
-      w[(1 + role) * 4 + q] = ck;
+      const double duu = xc[XDU][lane], dvv = xc[XDV][lane];
+      const double X = a1 + duu * p.rou + a3 + dvv * p.rov;
+      dpp = p.gm1 * (xc[ES1][lane] + xc[XQ][lane] - half_of(X));
+      xc[XDP][lane] = dpp;
+    }
+    bar_named(B8, 96);
+    if (act) w[3 * 4 + q] = half_of(xc[XC3][lane] + un * (dre + dpp));
+  } else {
+    bar_named(B6, 96);
+    double cp = 0.0;
+    if (act) {
+      const double dun = xc[XDN][lane];
+      if (role == 0) {
+        cp = xc[XP1][lane] + p.rou * dun;
+      } else {
+        cp = xc[XP2][lane] + p.rov * dun;
+        xc[XC3][lane] = xc[XA3][lane] + dun * p.roepp;
+      }
+    }
+    bar_named(B8, 96);
+    if (act) {
+      const double dpp = xc[XDP][lane];
+      if (role == 0) w[1 * 4 + q] = half_of(cp + dpp * p.dx);
+      else w[2 * 4 + q] = half_of(cp + dpp * p.dy);
     }
   }
-  bar_named(b7, 128);
+  (void)NS;
+  bar_named(B7, 128);
   if (!fvalid) return;
   const double* wf = wsm + fc * V * 4;
   double df = 0.0;
+  bool first = true;
 #pragma unroll
   for (int sl = 0; sl < 4; ++sl)
-    if ((fn.mask >> sl) & 1) df = df + wf[r * 4 + sl];
+    if ((fn.mask >> sl) & 1) {
+      df = first ? plus_zero(wf[r * 4 + sl]) : df + wf[r * 4 + sl];
+      first = false;
+    }
   d.hWA[r * NE + fi] = FWD ? div_rn(R - df, fn.dd, fn.ddh, fn.ddl) : R - div_rn(df, fn.dd, fn.ddh, fn.ddl);
 }
 // Both LU-SGS sweeps as a dataflow over one cooperative launch with compact

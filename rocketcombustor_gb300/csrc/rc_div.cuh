@@ -55,4 +55,19 @@ __device__ __forceinline__ bool nonzero(double x) { return (__double_as_longlong
 // the floating-point order
 __device__ __forceinline__ long long dbits(double x) { return __double_as_longlong(x); }
 
+// 0.0 + x on the integer pipe: x, except that -0 becomes +0 (every other
+// value, NaN included, is unchanged by adding +0 in round-to-nearest)
+__device__ __forceinline__ double plus_zero(double x) {
+  return __double_as_longlong(x) == (long long)0x8000000000000000ULL ? 0.0 : x;
+}
+// 0.5 * x: for a normal x whose exponent field is at least 2 the product is
+// x with that field less one, exactly; zeros, subnormals, the smallest
+// normals, infinities and NaNs take the FP64 multiply
+__device__ __forceinline__ double half_of(double x) {
+  const long long b = __double_as_longlong(x);
+  const unsigned e = (unsigned)(b >> 52) & 0x7ffu;
+  if (e - 2u < 0x7fdu) return __longlong_as_double(b - (1LL << 52));
+  return 0.5 * x;
+}
+
 }  // namespace rc
