@@ -92,7 +92,7 @@ __device__ __forceinline__ void features(const float* raw, const Norm& nr, float
 // FG warp groups of 4 warps per CTA in the fused forward (k_mlp_fwd16), each
 // with its own activation tile, TMEM accumulator (128 columns) and mbarrier.
 constexpr int FG = 3;
-constexpr uint32_t FUSED_TMEM_COLS = FG * 128 <= 256 ? 256 : 512;
+constexpr uint32_t FUSED_TMEM_COLS = 512;
 
 // barrier of the 128 threads of group g (named barrier 1 + g; 0 is __syncthreads)
 __device__ __forceinline__ void group_sync(int g) {
@@ -101,29 +101,36 @@ __device__ __forceinline__ void group_sync(int g) {
 
 // ------------------------------------------------ fused forward, all tcgen05
 // Every layer on the tensor cores with F16 operands: layer 0 as one K = 16
-// step (the 7 features padded with zeros), the three hidden layers as 8
-// K-steps, the output layer as N = 16 (4 outputs padded).  Layers 0-3
-// accumulate in F16 in TMEM, read back two columns per register
-// (tcgen05.ld .pack::16b), so the epilogue needs no conversion: it adds the
-// bias and evaluates the tanh form of GELU on packed halves (2 values per
-// instruction, hardware tanh on f16x2), writing the next layer's A operand
-// directly; the output layer accumulates in FP32.  F16 keeps 11 significant bits where BF16 keeps 8, so the
-// activations are closer to FP32 than the training forward's BF16 ones.
-// The weights come pre-swizzled in F16 (k_pack16), in the shared-memory order
-// of the kernel: hidden tiles 1..3, the layer-0 tile (128 rows, K columns 0-15
-// used), the output tile (16 rows); the CTA copies them once.  FG groups of
-// four warps, each with its activation tile, 128 TMEM columns and mbarrier,
-// work on different tiles of 128 samples, so one group's epilogue overlaps
-// another's MMAs.
+// step (the 7 features, a constant 1 in column 7 that takes b0 from column 7
+// of the layer-0 weights, zeros), the three hidden layers as 8 K-steps, the
+// output layer as N = 16 (4 outputs padded).  Layers 0-3 accumulate in F16
+// in TMEM, read back two columns per register (tcgen05.ld .pack::16b), so
+// the epilogue needs no conversion; the output layer accumulates in FP32.
+// F16 keeps 11 significant bits where BF16 keeps 8, so the activations are
+// closer to FP32 than the training forward's BF16 ones.  The epilogue loads
+// the whole 128-column row of its accumulator (four tcgen05.ld, one wait),
+// then forms 2 GELU(h) = h (1 + tanh(h (k0 + k0 k1 h^2))), h = acc + bias, in
+// six packed-half operations per pair, the hardware tanh on f16x2; the F16
+// weights of layers 1-4 carry the factor 1/2 (halving an F16 is exact above
+// the subnormal range, |w| >= 2^-13), so the products are those of GELU(h)
+// with the trained weights.  The weights come pre-scaled and pre-swizzled in
+// F16 (k_pack16), in the shared-memory order of the kernel: hidden tiles
+// 1..3, the layer-0 tile (128 rows, K columns 0-15 used), the output tile (16
+// rows); the CTA copies them once.  FG groups of four warps, each with its
+// activation tile, 128 TMEM columns and mbarrier, work on different tiles of
+// 128 samples, so one group's epilogue overlaps another's MMAs (a tile's
+// layers depend on one another, so the overlap is between tiles).  Issuing a
+// layer's K-steps as the previous epilogue writes each 32 columns, with a
+// group barrier per 32 columns, measured slower (5.0e9 against 5.4e9 samples/s
+// on 4M samples), and so did two groups with two accumulators each (4.0e9).
 constexpr int W0_TILE_BYTES = 128 * 128, W4_TILE_BYTES = 16 * 128 * 2;
 constexpr int WH_BYTES = 3 * TILE_BYTES + W0_TILE_BYTES + W4_TILE_BYTES;  // 118784
 constexpr int F2_W0 = 3 * TILE_BYTES, F2_W4 = F2_W0 + W0_TILE_BYTES, F2_ACT = F2_W4 + W4_TILE_BYTES;
-constexpr int F2_BIAS = F2_ACT + FG * TILE_BYTES;  // b0..b3 as f16x2 pairs (4 x 64), then b4 (16 floats)
-constexpr int F2_BAR = F2_BIAS + (4 * H / 2 + 16) * 4;
+constexpr int F2_BIAS = F2_ACT + FG * TILE_BYTES;  // b1..b3 as f16x2 pairs (3 x 64), then b4 (16 floats)
+constexpr int F2_BAR = F2_BIAS + (3 * H / 2 + 16) * 4;
 constexpr int F2_SLOT = F2_BAR + 8 * FG, F2_OK = F2_SLOT + 4;
 constexpr int F2_SMEM = F2_OK + 4 * FG + 1024;
-// layers 0-3 accumulate in F16 (read back two columns per register, no
-// conversion), the output layer in FP32
+// layers 0-3 accumulate in F16, the output layer in FP32
 constexpr uint32_t IDESC_H = umma::idesc_f16_acc16(128, 128), IDESC_H16 = umma::idesc_f16(128, 16);
 static_assert(F2_ACT % 1024 == 0 && F2_W0 % 1024 == 0 && F2_W4 % 1024 == 0, "tile alignment");
 static_assert(F2_BAR % 8 == 0, "mbarrier alignment");
@@ -139,18 +146,28 @@ __device__ __forceinline__ uint32_t pack_h2(float a, float b) {
   asm("cvt.rn.f16x2.f32 %0, %1, %2;" : "=r"(x) : "f"(b), "f"(a));
   return x;
 }
-// GELU (tanh form) of a packed pair of pre-activations acc + bias:
-// 0.5 x (1 + tanh(x (k0 + k0 k1 x^2)))
-__device__ __forceinline__ uint32_t gelu_h2(uint32_t acc, uint32_t bias) {
-  const uint32_t c0 = h2_bits(GK0), c1 = h2_bits(GK0 * GK1), half = h2_bits(0.5f);
-  uint32_t x, x2, p, u, t, hx, g;
-  asm("add.rn.f16x2 %0, %1, %2;" : "=r"(x) : "r"(acc), "r"(bias));
-  asm("mul.rn.f16x2 %0, %1, %1;" : "=r"(x2) : "r"(x));
-  asm("fma.rn.f16x2 %0, %1, %2, %3;" : "=r"(p) : "r"(x2), "r"(c1), "r"(c0));
-  asm("mul.rn.f16x2 %0, %1, %2;" : "=r"(u) : "r"(x), "r"(p));
+// twice the GELU (tanh form) of a packed pair of pre-activations acc + bias:
+// h (1 + tanh(h (k0 + k0 k1 h^2)))
+__device__ __forceinline__ uint32_t gelu2_h2(uint32_t acc, uint32_t bias) {
+  const uint32_t c0 = h2_bits(GK0), c1 = h2_bits(GK0 * GK1);
+  uint32_t h, h2, p, u, t, g;
+  asm("add.rn.f16x2 %0, %1, %2;" : "=r"(h) : "r"(acc), "r"(bias));
+  asm("mul.rn.f16x2 %0, %1, %1;" : "=r"(h2) : "r"(h));
+  asm("fma.rn.f16x2 %0, %1, %2, %3;" : "=r"(p) : "r"(h2), "r"(c1), "r"(c0));
+  asm("mul.rn.f16x2 %0, %1, %2;" : "=r"(u) : "r"(h), "r"(p));
   asm("tanh.approx.f16x2 %0, %1;" : "=r"(t) : "r"(u));
-  asm("mul.rn.f16x2 %0, %1, %2;" : "=r"(hx) : "r"(x), "r"(half));
-  asm("fma.rn.f16x2 %0, %1, %2, %2;" : "=r"(g) : "r"(t), "r"(hx));
+  asm("fma.rn.f16x2 %0, %1, %2, %2;" : "=r"(g) : "r"(t), "r"(h));
+  return g;
+}
+// the same without a bias (layer 0 has it in the accumulator)
+__device__ __forceinline__ uint32_t gelu2_h2(uint32_t h) {
+  const uint32_t c0 = h2_bits(GK0), c1 = h2_bits(GK0 * GK1);
+  uint32_t h2, p, u, t, g;
+  asm("mul.rn.f16x2 %0, %1, %1;" : "=r"(h2) : "r"(h));
+  asm("fma.rn.f16x2 %0, %1, %2, %3;" : "=r"(p) : "r"(h2), "r"(c1), "r"(c0));
+  asm("mul.rn.f16x2 %0, %1, %2;" : "=r"(u) : "r"(h), "r"(p));
+  asm("tanh.approx.f16x2 %0, %1;" : "=r"(t) : "r"(u));
+  asm("fma.rn.f16x2 %0, %1, %2, %2;" : "=r"(g) : "r"(t), "r"(h));
   return g;
 }
 
@@ -160,17 +177,15 @@ __global__ void __launch_bounds__(128 * FG, 1) k_mlp_fwd16(const uint4* __restri
   extern __shared__ uint8_t smem_raw[];
   uint8_t* base = smem_raw + ((1024u - (umma::smem_u32(smem_raw) & 1023u)) & 1023u);
   const uint32_t sbase = umma::smem_u32(base);
-  uint32_t* bias2 = reinterpret_cast<uint32_t*>(base + F2_BIAS);  // [4][64] f16x2
-  float* bias4 = reinterpret_cast<float*>(base + F2_BIAS) + 4 * H / 2;
+  uint32_t* bias2 = reinterpret_cast<uint32_t*>(base + F2_BIAS);  // [3][64] f16x2, layers 1..3
+  float* bias4 = reinterpret_cast<float*>(base + F2_BIAS) + 3 * H / 2;
   uint32_t* slot = reinterpret_cast<uint32_t*>(base + F2_SLOT);
   const int g = threadIdx.x >> 7, t = threadIdx.x & 127, warp = t >> 5;
   uint64_t* bar = reinterpret_cast<uint64_t*>(base + F2_BAR) + g;
   int* s_ok = reinterpret_cast<int*>(base + F2_OK) + g;
   for (int q = threadIdx.x; q < WH_BYTES / 16; q += 128 * FG) reinterpret_cast<uint4*>(base)[q] = Wh[q];
-  for (int q = threadIdx.x; q < H / 2; q += 128 * FG) {
-    bias2[q] = pack_h2(params[OFF_B0 + 2 * q], params[OFF_B0 + 2 * q + 1]);
-    for (int l = 1; l <= 3; ++l) bias2[l * H / 2 + q] = pack_h2(params[off_b(l) + 2 * q], params[off_b(l) + 2 * q + 1]);
-  }
+  for (int q = threadIdx.x; q < H / 2; q += 128 * FG)
+    for (int l = 1; l <= 3; ++l) bias2[(l - 1) * H / 2 + q] = pack_h2(params[off_b(l) + 2 * q], params[off_b(l) + 2 * q + 1]);
   if (threadIdx.x < 16) bias4[threadIdx.x] = threadIdx.x < NOUT ? params[OFF_B4 + threadIdx.x] : 0.f;
   if (t == 0) umma::mbar_init(bar, 1);
   if (threadIdx.x < 32) {
@@ -204,19 +219,18 @@ __global__ void __launch_bounds__(128 * FG, 1) k_mlp_fwd16(const uint4* __restri
     umma::tc_fence_after();
     return *s_ok != 0;
   };
-  // bias + GELU of the accumulator row t -> row t of the activation tile
+  // (bias +) 2 GELU of the accumulator row t -> row t of the activation tile
   auto epilogue = [&](const uint32_t* bl) {
-    for (int c = 0; c < 4; ++c) {
-      uint32_t v[16];
-      umma::tmem_ld32_pack16(trow + (uint32_t)(c * 32), v);
+    uint32_t v[64];
 #pragma unroll
-      for (int c8 = 0; c8 < 4; ++c8) {
-        uint32_t h[4];
+    for (int c = 0; c < 4; ++c) umma::tmem_ld32_pack16_nowait(trow + (uint32_t)(c * 32), v + 16 * c);
+    umma::tmem_wait_ld();
 #pragma unroll
-        for (int e = 0; e < 4; ++e) h[e] = gelu_h2(v[c8 * 4 + e], bl[c * 16 + c8 * 4 + e]);
-        *reinterpret_cast<uint4*>(actp + umma::sw128_offset(t, c * 32 + c8 * 8, 128)) =
-            make_uint4(h[0], h[1], h[2], h[3]);
-      }
+    for (int c = 0; c < 16; ++c) {
+      uint32_t h[4];
+#pragma unroll
+      for (int e = 0; e < 4; ++e) h[e] = bl ? gelu2_h2(v[4 * c + e], bl[4 * c + e]) : gelu2_h2(v[4 * c + e]);
+      *reinterpret_cast<uint4*>(actp + umma::sw128_offset(t, c * 8, 128)) = make_uint4(h[0], h[1], h[2], h[3]);
     }
   };
   const int ntiles = (n + 127) / 128;
@@ -225,15 +239,15 @@ __global__ void __launch_bounds__(128 * FG, 1) k_mlp_fwd16(const uint4* __restri
     float xn[NIN];
     typename Io::Local loc;
     io.load(s, s < n, nr, xn, loc);
-    // the features as K columns 0-15 of row t (7 values, then zeros)
+    // the features as K columns 0-6 of row t, 1 in column 7 (the bias), zeros to 15
     *reinterpret_cast<uint4*>(actp + umma::sw128_offset(t, 0, 128)) =
-        make_uint4(pack_h2(xn[0], xn[1]), pack_h2(xn[2], xn[3]), pack_h2(xn[4], xn[5]), pack_h2(xn[6], 0.f));
+        make_uint4(pack_h2(xn[0], xn[1]), pack_h2(xn[2], xn[3]), pack_h2(xn[4], xn[5]), pack_h2(xn[6], 1.f));
     *reinterpret_cast<uint4*>(actp + umma::sw128_offset(t, 8, 128)) = make_uint4(0u, 0u, 0u, 0u);
     if (!(ok = mma(1, sbase + F2_W0, 128, IDESC_H))) break;
-    epilogue(bias2);
+    epilogue(nullptr);
     for (int l = 1; l <= 3 && ok; ++l) {
       if (!(ok = mma(8, sbase + (l - 1) * TILE_BYTES, 128, IDESC_H))) break;
-      epilogue(bias2 + l * H / 2);
+      epilogue(bias2 + (l - 1) * H / 2);
     }
     if (!ok || !(ok = mma(8, sbase + F2_W4, 16, IDESC_H16))) break;
     float v[32], out[NOUT];
@@ -645,6 +659,8 @@ __global__ void k_pack(const float* __restrict__ p, __nv_bfloat16* Wb, __nv_bflo
 // (k_mlp_fwd16): hidden tiles, the layer-0 tile (K padded 7 -> 16 with zeros),
 // the output tile (N padded 4 -> 16 with zeros).  Bytes of the tiles that the
 // MMAs never read stay as the creation left them (zero).
+// the F16 weights of k_mlp_fwd16: layers 1-4 times 1/2 (the epilogue forms
+// 2 GELU), the layer-0 tile with b0 in K column 7 (the features' constant 1)
 __global__ void k_pack16(const float* __restrict__ p, uint8_t* Wh) {
   const int q = blockIdx.x * blockDim.x + threadIdx.x;
   constexpr int NH = 3 * H * H, N0 = H * 16, N4 = 16 * H;
@@ -652,15 +668,15 @@ __global__ void k_pack16(const float* __restrict__ p, uint8_t* Wh) {
   uint32_t off;
   if (q < NH) {
     const int l = q / (H * H), o = (q % (H * H)) / H, i = q % H;
-    v = p[off_w(l + 1) + o * H + i];
+    v = 0.5f * p[off_w(l + 1) + o * H + i];
     off = (uint32_t)(l * TILE_BYTES) + umma::sw128_offset(o, i, 128);
   } else if (q < NH + N0) {
     const int o = (q - NH) / 16, i = (q - NH) % 16;
-    v = i < NIN ? p[OFF_W0 + o * NIN + i] : 0.f;
+    v = i < NIN ? p[OFF_W0 + o * NIN + i] : i == NIN ? p[OFF_B0 + o] : 0.f;
     off = (uint32_t)F2_W0 + umma::sw128_offset(o, i, 128);
   } else if (q < NH + N0 + N4) {
     const int m = (q - NH - N0) / H, i = (q - NH - N0) % H;
-    v = m < NOUT ? p[OFF_W4 + m * H + i] : 0.f;
+    v = m < NOUT ? 0.5f * p[OFF_W4 + m * H + i] : 0.f;
     off = (uint32_t)F2_W4 + umma::sw128_offset(m, i, 16);
   } else {
     return;

@@ -1,7 +1,7 @@
 // Blackwell (sm_100 family) tensor-core building blocks as inline PTX:
 // TMEM allocation, tcgen05.mma kind::f16 (BF16 x BF16 or F16 x F16 -> FP32
-// in TMEM), tcgen05.commit to an mbarrier, tcgen05.ld of the accumulator, and
-// the shared-memory operand layout the MMA reads.
+// or F16 in TMEM), tcgen05.commit to an mbarrier, tcgen05.ld of the
+// accumulator, and the shared-memory operand layout the MMA reads.
 //
 // Operand layout (both A and B "K-major", 128-byte swizzle).  An operand tile
 // of R rows (R a multiple of 8) and 128 K-elements (16-bit) is stored as two
@@ -154,6 +154,18 @@ __device__ __forceinline__ void tmem_ld32_pack16(uint32_t taddr, uint32_t* r) {
       : "memory");
   asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
 }
+
+// the same without the wait: several loads in flight, then tmem_wait_ld
+__device__ __forceinline__ void tmem_ld32_pack16_nowait(uint32_t taddr, uint32_t* r) {
+  asm volatile(
+      "tcgen05.ld.sync.aligned.32x32b.x16.pack::16b.b32 "
+      "{%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, %12, %13, %14, %15}, [%16];"
+      : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
+        "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
+      : "r"(taddr)
+      : "memory");
+}
+__device__ __forceinline__ void tmem_wait_ld() { asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory"); }
 
 }  // namespace umma
 }  // namespace rc
