@@ -337,7 +337,7 @@ __global__ void __launch_bounds__(128) k_bdf2_prep(const Dev d, const ThermoDev<
   double pri[V];
 #pragma unroll
   for (int k = 0; k < V; ++k) pri[k] = d.PA[k * NE + i];
-  double a[V * V], af[V * V];
+  double a[V * V];
   con_to_pri_jaco<NSP>(th, pri, a, err);
 #pragma unroll
   for (int k = 0; k < V * V; ++k) a[k] = a[k] * ddi;
@@ -349,25 +349,32 @@ __global__ void __launch_bounds__(128) k_bdf2_prep(const Dev d, const ThermoDev<
 #pragma unroll
       for (int c = 0; c < V; ++c) a[(4 + j) * V + c] = a[(4 + j) * V + c] - vol * dw[j * V + c];
   }
-  // dgesvx('E'): equilibrate, factor, condition estimate
+  // dgesvx('E'): equilibrate, factor, condition estimate.  The equilibrated
+  // matrix goes to the cell's record and gives its 1-norm (dlange('1')) before
+  // the factorisation overwrites it in registers, so one V x V array is live
+  // instead of two (the same operations as factoring a copy).
   double rs[V], cs[V], rowcnd = 0, colcnd = 0, amax = 0;
   int equ = 0;
   if (dgeequ<V>(a, rs, cs, rowcnd, colcnd, amax) == 0) equ = dlaqge<V>(a, rs, cs, rowcnd, colcnd, amax);
+  double* m = d.bmat + (size_t)i * V * RW;
+  double anorm = 0.0;
 #pragma unroll
-  for (int k = 0; k < V * V; ++k) af[k] = a[k];
+  for (int j = 0; j < V; ++j) {
+    double sum = 0.0;
+#pragma unroll
+    for (int r = 0; r < V; ++r) sum = sum + fabs(a[r * V + j]);
+    if (anorm < sum || isnan(sum)) anorm = sum;
+  }
+#pragma unroll
+  for (int r = 0; r < V; ++r)
+#pragma unroll
+    for (int c = 0; c < V; ++c) m[r * RW + c] = a[r * V + c];
+  double* af = a;
   int ipiv[V];
   const int info = dgetrf<V>(af, ipiv);
   if (info > 0) {
     err |= ERR_LINSOLVE;
   } else {
-    double anorm = 0.0;  // dlange('1')
-#pragma unroll
-    for (int j = 0; j < V; ++j) {
-      double sum = 0.0;
-#pragma unroll
-      for (int r = 0; r < V; ++r) sum = sum + fabs(a[r * V + j]);
-      if (anorm < sum || isnan(sum)) anorm = sum;
-    }
     if (dgecon<V>(af, anorm) < EPS) err |= ERR_LINSOLVE;
   }
   int src[V];
@@ -379,11 +386,10 @@ __global__ void __launch_bounds__(128) k_bdf2_prep(const Dev d, const ThermoDev<
     src[k] = src[p];
     src[p] = t;
   }
-  double* m = d.bmat + (size_t)i * V * RW;
 #pragma unroll
   for (int r = 0; r < V; ++r) {
 #pragma unroll
-    for (int c = 0; c < V; ++c) { m[r * RW + c] = a[r * V + c]; m[r * RW + V + c] = af[r * V + c]; }
+    for (int c = 0; c < V; ++c) m[r * RW + V + c] = af[r * V + c];
     m[r * RW + 2 * V] = rs[r];
     m[r * RW + 2 * V + 1] = cs[r];
     const Recip ru = recip_of(af[r * V + r]);
