@@ -514,19 +514,23 @@ __device__ __forceinline__ BRow<NSP> brow_load(const Dev& d, int i, bool valid, 
 }
 // The flux difference of slot b's neighbour increment dP (Time_BDF2.f90:168-197),
 // rows 1-3 (lo) or rows 4.. (energy and species) of the slot's terms.
-template <int NSP>
+// L2: the neighbour's increment read through L2 (ld.global.cg), as the
+// dataflow launch needs (other SMs write it during the launch).
+template <int NSP, bool L2 = false>
 __device__ __forceinline__ void bslot_terms(const Dev& d, const ThermoDev<NSP>& th, const BSlot<NSP>& b, bool lo,
                                             double* c) {
   constexpr int V = 3 + NSP;
   const int NE = d.NE;
+  auto ld = [](const double* p) { return L2 ? __ldcg(p) : *p; };
 #pragma unroll
   for (int k = 0; k < V; ++k) c[k] = 0.0;
   if (!b.act) return;
   const int j = b.j;
-  const double dpp = d.hWA[0 * NE + j], duu = d.hWA[1 * NE + j], dvv = d.hWA[2 * NE + j], dtt = d.hWA[3 * NE + j];
+  const double dpp = ld(d.hWA + 0 * NE + j), duu = ld(d.hWA + 1 * NE + j), dvv = ld(d.hWA + 2 * NE + j),
+               dtt = ld(d.hWA + 3 * NE + j);
   double dyy[NSP], s = 0.0;
 #pragma unroll
-  for (int k = 0; k < NSP - 1; ++k) { dyy[k] = d.hWA[(4 + k) * NE + j]; s = s + dyy[k]; }
+  for (int k = 0; k < NSP - 1; ++k) { dyy[k] = ld(d.hWA + (4 + k) * NE + j); s = s + dyy[k]; }
   dyy[NSP - 1] = -s;
   double s1 = 0.0;
 #pragma unroll
@@ -578,31 +582,24 @@ __device__ __forceinline__ long long berr_bits(double y, double wk, int r) {
   return vb;
 }
 
-// One level of the forward (FWD) or backward sweep, cells t0..t1-1 of the
-// level order; eight lanes per cell, CPW cells per warp (one warp per block;
-// lanes of cell slots >= CPW only join the shuffles).
-template <int NSP, bool FWD, int CPW>
-__global__ void __launch_bounds__(32) k_bdf2_sweep(const Dev d, const ThermoDev<NSP> th, int t0, int t1) {
+// The sweep step of up to four cells on one warp, eight lanes per cell (lane
+// = 8 cell + r; lanes of cell slots >= CPW only join the shuffles): the flux
+// differences of the neighbours' increments (sp: this lane's slot, q = r % 4,
+// rows 1-3 on lanes r < 4, rows 4.. on the others), added in NeighF order
+// through w (this warp's [cell][row][slot] scratch), then the cell's system
+// (rw: row r of its factorisation) solved with one lane per row and refined
+// as dgerfs does; hown is the cell's own increment (row r), i its index.
+template <int NSP, bool FWD, int CPW, bool L2>
+__device__ __forceinline__ void bdf2_cell_step(const Dev& d, const ThermoDev<NSP>& th, const BSlot<NSP>& sp,
+                                               const BRow<NSP>& rw, double hown, int i, bool valid, double* wsm) {
   using namespace bdf2;
-  constexpr int V = 3 + NSP, DIR = FWD ? 0 : 1;
-  static_assert(V <= 7, "one lane per row and the flags in slot 7");
-  pdl_launch_dependents();
+  constexpr int V = 3 + NSP;
   const int lane = threadIdx.x & 31, cell = lane >> 3, r = lane & 7, base = cell * 8;
   const int q = r & 3;
   const bool lo = r < 4;  // lanes 0-3 keep flux rows 1-3 of their slot, lanes 4-7 rows 4.. (energy, species)
   const int NE = d.NE;
-  const int t = t0 + blockIdx.x * CPW + cell;
-  const bool valid = cell < CPW && t < t1;
-  const int i = valid ? d.swi[DIR][t] : 0;
-  const BSlot<NSP> sp = bslot_load<NSP, FWD>(d, t, valid, q);
-  const BRow<NSP> rw = brow_load<NSP>(d, i, valid, r);
-  double hown = 0.0;
-  if (FWD && valid && r < V) hown = d.hWA[r * NE + i];  // written by k_bdf2_prep, complete before this grid
-  pdl_wait();
-  if (!FWD && valid && r < V) hown = d.hWA[r * NE + i];
   double c[V];
-  bslot_terms<NSP>(d, th, sp, lo, c);
-  __shared__ double wsm[CPW * V * 4];
+  bslot_terms<NSP, L2>(d, th, sp, lo, c);
   double* w = wsm + (cell < CPW ? cell : 0) * V * 4;  // [row][slot]
   if (cell < CPW) bslot_put<NSP>(w, lo, q, c);
   __syncwarp();
@@ -646,6 +643,140 @@ __global__ void __launch_bounds__(32) k_bdf2_sweep(const Dev d, const ThermoDev<
   }
   if (colequ) x = rw.csc * x;
   if (valid && r < V) d.hWA[r * NE + i] = FWD ? x : hown - x;
+}
+
+// One level of the forward (FWD) or backward sweep, cells t0..t1-1 of the
+// level order; eight lanes per cell, CPW cells per warp (one warp per block;
+// lanes of cell slots >= CPW only join the shuffles).
+template <int NSP, bool FWD, int CPW>
+__global__ void __launch_bounds__(32) k_bdf2_sweep(const Dev d, const ThermoDev<NSP> th, int t0, int t1) {
+  using namespace bdf2;
+  constexpr int V = 3 + NSP, DIR = FWD ? 0 : 1;
+  static_assert(V <= 7, "one lane per row and the flags in slot 7");
+  pdl_launch_dependents();
+  const int lane = threadIdx.x & 31, cell = lane >> 3, r = lane & 7;
+  const int q = r & 3;
+  const int NE = d.NE;
+  const int t = t0 + blockIdx.x * CPW + cell;
+  const bool valid = cell < CPW && t < t1;
+  const int i = valid ? d.swi[DIR][t] : 0;
+  const BSlot<NSP> sp = bslot_load<NSP, FWD>(d, t, valid, q);
+  const BRow<NSP> rw = brow_load<NSP>(d, i, valid, r);
+  double hown = 0.0;
+  if (FWD && valid && r < V) hown = d.hWA[r * NE + i];  // written by k_bdf2_prep, complete before this grid
+  pdl_wait();
+  if (!FWD && valid && r < V) hown = d.hWA[r * NE + i];
+  __shared__ double wsm[CPW * V * 4];
+  bdf2_cell_step<NSP, FWD, CPW, false>(d, th, sp, rw, hown, i, valid, wsm);
+}
+
+// Both BDF2 sweeps as one cooperative dataflow launch on the pass tables of
+// k_lusgs_flow (FlowDev with passes of up to 8 consecutive positions of one
+// level owned by one block; one block per SM).  A cell's step is long (two
+// 7 x 7 solves and up to five refinement passes, about 12 us of dependent
+// FP64) and uneven: with one launch per level every level lasts as long as
+// its slowest cell, here a slow cell holds up only the passes that read it.
+// Warps 0 and 1 take four cells of each pass each and load what the sweep
+// does not change (the neighbours' gas state, the cell's factorisation)
+// before the pass is handed over; warp 2 looks at the flags of the next pass,
+// hands it over (barrier 3) once the current one is done (barrier 4) and its
+// flags are set, and publishes the finished pass (flag = this launch's epoch),
+// before any blocking wait.  s_go[k % 2] = 0 after a bounded wait gave up
+// (ERR_SYNC): the compute warps then skip the pass.  The last block to finish
+// advances the epoch counter; the primitive update follows as its own launch.
+constexpr int BFLOW_THREADS = 96;
+template <int NSP>
+__global__ void __launch_bounds__(BFLOW_THREADS, 1) k_bdf2_flow(const Dev d, const ThermoDev<NSP> th, const FlowDev f) {
+  using namespace bdf2;
+  constexpr int V = 3 + NSP;
+  static_assert(V <= 7, "one lane per row and the flags in slot 7");
+  __shared__ double wsm[2][4 * V * 4];
+  __shared__ unsigned s_epoch;
+  __shared__ volatile int s_bad, s_go[2];
+  if (threadIdx.x == 0) {
+    s_epoch = ld_acquire(f.ctr) + 1u;
+    s_bad = 0;
+    s_go[0] = 0;
+    s_go[1] = 0;
+  }
+  __syncthreads();
+  const unsigned epoch = s_epoch;
+  const int b = blockIdx.x, lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const int f0 = f.boff[0][b], b0 = f.boff[1][b];
+  const int nf = f.boff[0][b + 1] - f0, n = nf + (f.boff[1][b + 1] - b0);
+  auto pass_of = [&](int k) { return k < nf ? f.blist[0][f0 + k] : f.blist[1][b0 + k - nf]; };
+  if (warp == 2) {
+    auto poll = [&](int k) {
+      if (s_bad) return;
+      const int pz = pass_of(k), d0 = f.doff[pz], nd = f.doff[pz + 1] - d0;
+      bool ok = true;
+      for (int u = lane; u < nd; u += 32) ok = ok && wait_flag(f.pflag + f.deps[d0 + u], epoch, d.err, d.spin_limit);
+      if (__any_sync(FULL, !ok) && lane == 0) s_bad = 1;
+      __syncwarp();
+    };
+    auto ready = [&](int k) -> bool {
+      if (s_bad) return true;
+      const int pz = pass_of(k), d0 = f.doff[pz], nd = f.doff[pz + 1] - d0;
+      bool ok = true;
+      for (int u = lane; u < nd; u += 32) ok = ok && ld_acquire(f.pflag + f.deps[d0 + u]) >= epoch;
+      return __all_sync(FULL, ok) != 0;
+    };
+    auto hand_over = [&](int k) {
+      if (lane == 0) s_go[k & 1] = s_bad ? 0 : 1;
+      __syncwarp();
+      __threadfence_block();
+      bar_arrive(3, BFLOW_THREADS);
+    };
+    if (n > 0) {
+      poll(0);
+      hand_over(0);
+    }
+    for (int k = 0; k < n; ++k) {
+      const bool more = k + 1 < n;
+      const bool go = more && ready(k + 1);
+      bar_named(4, BFLOW_THREADS);
+      if (go) hand_over(k + 1);
+      if (lane == 0 && !s_bad) st_release(f.pflag + pass_of(k), epoch);
+      if (more && !go) {
+        poll(k + 1);
+        hand_over(k + 1);
+      }
+    }
+  } else {
+    const int cell = lane >> 3, r = lane & 7, q = r & 3;
+    for (int k = 0; k < n; ++k) {
+      const bool fwd = k < nf;
+      const int pz = pass_of(k), t0 = f.pstart[pz], t1 = t0 + f.pcount[pz];
+      const int t = t0 + 4 * warp + cell;
+      const bool valid = t < t1;
+      const int i = valid ? d.swi[fwd ? 0 : 1][t] : 0;
+      // what the sweep does not change: before the hand-over
+      const BSlot<NSP> sp = fwd ? bslot_load<NSP, true>(d, t, valid, q) : bslot_load<NSP, false>(d, t, valid, q);
+      const BRow<NSP> rw = brow_load<NSP>(d, i, valid, r);
+      // the cell's own increment: the set-up's right-hand side (forward), or
+      // what this block's forward pass of the cell wrote (backward; read after
+      // the hand-over, as the other warp may still be finishing the forward
+      // pass that holds the cell)
+      double hown = fwd && valid && r < V ? __ldcg(d.hWA + r * d.NE + i) : 0.0;
+      bar_named(3, BFLOW_THREADS);
+      if (!fwd && valid && r < V) hown = __ldcg(d.hWA + r * d.NE + i);
+      if (s_go[k & 1]) {
+        if (fwd) bdf2_cell_step<NSP, true, 4, true>(d, th, sp, rw, hown, i, valid, wsm[warp]);
+        else bdf2_cell_step<NSP, false, 4, true>(d, th, sp, rw, hown, i, valid, wsm[warp]);
+      }
+      __syncwarp();
+      bar_arrive(4, BFLOW_THREADS);
+    }
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    __threadfence();
+    if (atomicAdd(f.ctr + 1, 1u) == gridDim.x - 1) {
+      f.ctr[1] = 0u;
+      __threadfence();
+      st_release(f.ctr, epoch);
+    }
+  }
 }
 
 // PA += dP, then primitve_to_conserved_variables (update_flow_variables.f90:50-84)
@@ -706,6 +837,26 @@ void bdf2_sweep(const Dev& d, const void* th, bool fwd, int t0, int t1, int cpw,
   else if (cpw == 2) bdf2_sweep_cpw<NSP, 2>(d, T, fwd, t0, t1, s);
   else bdf2_sweep_cpw<NSP, 1>(d, T, fwd, t0, t1, s);
 }
+// the cooperative dataflow launch of both sweeps (grid: one block per SM)
+template <int NSP>
+cudaError_t bdf2_flow(const Dev& d, const void* th, const FlowDev& f, int grid, cudaStream_t s) {
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = dim3((unsigned)grid);
+  cfg.blockDim = dim3(BFLOW_THREADS);
+  cfg.stream = s;
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeCooperative;
+  attr[0].val.cooperative = 1;
+  cfg.attrs = attr;
+  cfg.numAttrs = 1;
+  return cudaLaunchKernelEx(&cfg, k_bdf2_flow<NSP>, d, *static_cast<const ThermoDev<NSP>*>(th), f);
+}
+template <int NSP>
+int bdf2_flow_occupancy() {
+  int nb = 0;
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_bdf2_flow<NSP>, BFLOW_THREADS, 0);
+  return nb;
+}
 template <int NSP>
 void bdf2_update(const Dev& d, const void* th, int bs, cudaStream_t s) {
   launch_pdl(k_bdf2_update<NSP>, nblk(d.NE, bs), bs, s, d, *static_cast<const ThermoDev<NSP>*>(th));
@@ -718,6 +869,8 @@ int bdf2_nbq() { return bdf2::nbq<NSP>(); }
   template void bdf2_prep<N>(const Dev&, const void*, int, cudaStream_t);           \
   template void bdf2_sweep<N>(const Dev&, const void*, bool, int, int, int, cudaStream_t); \
   template void bdf2_update<N>(const Dev&, const void*, int, cudaStream_t);         \
+  template cudaError_t bdf2_flow<N>(const Dev&, const void*, const FlowDev&, int, cudaStream_t); \
+  template int bdf2_flow_occupancy<N>();                                           \
   template int bdf2_nbq<N>();
 RC_BDF2_INST(1)
 RC_BDF2_INST(4)

@@ -1644,6 +1644,8 @@ template <int NSP> void bdf2_prep(const Dev&, const void*, int, cudaStream_t);
 template <int NSP> void bdf2_sweep(const Dev&, const void*, bool, int, int, int, cudaStream_t);
 template <int NSP> void bdf2_update(const Dev&, const void*, int, cudaStream_t);
 template <int NSP> int bdf2_nbq();
+template <int NSP> cudaError_t bdf2_flow(const Dev&, const void*, const FlowDev&, int, cudaStream_t);
+template <int NSP> int bdf2_flow_occupancy();
 cudaError_t surrogate_source(const Dev&, const void*, const rc_mlp*, float, int*, unsigned*, unsigned*, const int*,
                              unsigned char*, cudaStream_t);
 cudaError_t surrogate_prepare();
@@ -1717,6 +1719,8 @@ struct rc_ctx {
   // unsteady dual-time BDF2 (allocated by the first BDF2 call)
   bool bdf2_ready = false;
   int bdf2_cpw = 4;                        // BDF2 sweep cells per warp (1, 2 or 4; RC_BDF2_CPW)
+  bool bdf2_flow = false;                  // BDF2 sweeps as one dataflow launch on flows[0]
+                                           // (RC_BDF2_SCHEDULE=levels: one launch per level)
   double* bpar_dev = nullptr;              // {dt, phi}
   cudaGraphExec_t bdf2_graph = nullptr;    // one inner iteration and its norms
   long long bdf2_graph_kernels = 0;
@@ -2219,17 +2223,21 @@ void q_stage(rc_ctx* c) {
   q_sweeps32<NSP>(c);
 }
 
-// BDF2_LU_SGS after the residual assembly: per-cell set-up, the level-
-// scheduled sweeps, the primitive update.
+// BDF2_LU_SGS after the residual assembly: per-cell set-up, the sweeps (one
+// dataflow launch, or one launch per level), the primitive update.
 template <int NSP>
 void q_bdf2_lusgs(rc_ctx* c) {
   bdf2_prep<NSP>(c->d, c->thermo.data(), c->d.bs, c->stream);
   c->launches++;
-  for (size_t l = 0; l + 1 < c->fwd_off.size(); ++l) {
+  if (c->bdf2_flow) {
+    bdf2_flow<NSP>(c->d, c->thermo.data(), c->flows[0], c->flow_grid, c->stream);
+    c->launches++;
+  }
+  for (size_t l = 0; !c->bdf2_flow && l + 1 < c->fwd_off.size(); ++l) {
     bdf2_sweep<NSP>(c->d, c->thermo.data(), true, c->fwd_off[l], c->fwd_off[l + 1], c->bdf2_cpw, c->stream);
     c->launches++;
   }
-  for (size_t l = 0; l + 1 < c->bwd_off.size(); ++l) {
+  for (size_t l = 0; !c->bdf2_flow && l + 1 < c->bwd_off.size(); ++l) {
     bdf2_sweep<NSP>(c->d, c->thermo.data(), false, c->bwd_off[l], c->bwd_off[l + 1], c->bdf2_cpw, c->stream);
     c->launches++;
   }
@@ -3431,6 +3439,15 @@ static int bdf2_setup(rc_ctx* c) {
   if (st) return st;
   c->d.bpar = c->bpar_dev;
   if (const char* e = std::getenv("RC_BDF2_CPW")) c->bdf2_cpw = std::atoi(e);
+  {  // the dataflow sweeps: a cooperative grid of one block per SM
+    int nsm = 0, coop = 0, occ = 0;
+    cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, c->device);
+    cudaDeviceGetAttribute(&coop, cudaDevAttrCooperativeLaunch, c->device);
+    RC_DISPATCH(c, occ = bdf2_flow_occupancy);
+    cudaGetLastError();
+    const char* e = std::getenv("RC_BDF2_SCHEDULE");
+    c->bdf2_flow = coop && nsm > 0 && occ >= 1 && c->flow_grid == nsm && !(e && std::string(e) == "levels");
+  }
   c->bdf2_ready = true;
   drop_graphs(c);  // the captured kernels hold the old Dev
   return RC_OK;

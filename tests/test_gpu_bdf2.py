@@ -70,6 +70,70 @@ def test_unsteady_steps_bit_identical_to_oracle(case_root, name, over):
     assert c.unsteady["ttime"] == o.unsteady()["ttime"]
 
 
+@pytest.mark.parametrize("name,over", [("t2u", {}), ("t2u", {"nx": 300, "ny": 20}), ("t1", T1U),
+                                       ("t2u", {"order": "random"})])
+def test_bdf2_dataflow_sweeps_equal_level_sweeps(case_root, name, over, monkeypatch):
+    """Both BDF2 sweeps as one cooperative dataflow launch (passes of up to 8
+    positions of one level, per-pass flags between the SMs) against one
+    launch per level: the same inner counts and bits after five physical
+    steps; BDF2_LU_SGS is then three launches (set-up, sweeps, update)."""
+    d = make_case(case_root, name, **over)
+    got = {}
+    for sched in ("levels", "dataflow"):
+        monkeypatch.setenv("RC_BDF2_SCHEDULE", sched)
+        c = rc.Case(d)
+        _, inner = c.run_unsteady(5)
+        got[sched] = (list(inner), c.array("PA").copy(), c.array("WA").copy())
+        c.close()
+    assert got["levels"][0] == got["dataflow"][0]
+    assert np.array_equal(got["levels"][1], got["dataflow"][1])
+    assert np.array_equal(got["levels"][2], got["dataflow"][2])
+    c = rc.Case(d)
+    s = rc.Solver(c)
+    dt = oracle.Oracle(d).unsteady()["dt"]
+    s.timestep(); s.reconstruction(); s.flux_sourceterm()
+    n0 = s.stats()["kernel_launches"]
+    s.bdf2_lusgs(2, 0.5, dt)
+    s.sync()
+    assert s.stats()["kernel_launches"] - n0 == 3
+    s.close()
+
+
+def test_bdf2_dataflow_wait_timeout_is_reported(case_root, monkeypatch):
+    """A poll limit of 1 makes the BDF2 dataflow sweeps give up on a pass of
+    another block: RC_ERR_SYNC, every block still finishes the launch, and
+    after the error is cleared and the state set again the next call (a new
+    epoch of the pass flags) gives the oracle's bits."""
+    monkeypatch.setenv("RC_BDF2_SCHEDULE", "dataflow")
+    d = make_case(case_root, "t2u")
+    c = rc.Case(d)
+    s = rc.Solver(c)
+    o = oracle.Oracle(d, threads=4)
+    dt = o.unsteady()["dt"]
+    PA0, WA0 = c.array("PA").copy(), c.array("WA").copy()
+    s.set_array("WP", WA0)
+    s.set_array("WP2", WA0)
+    s.set_wait_limit(1)
+    s.timestep(); s.reconstruction(); s.flux_sourceterm()
+    s.bdf2_lusgs(1, 0.5, dt)
+    with pytest.raises(rc.RcError) as e:
+        s.sync()
+    assert e.value.code & 64
+    s.clear_error()
+    s.set_wait_limit(1 << 24)
+    s.set_state(PA0, WA0)
+    o.array("WP")[:] = WA0
+    o.array("WP2")[:] = WA0
+    _assemble(s, o)
+    assert o.bdf2_lusgs(1, 0.5) == 0
+    s.bdf2_lusgs(1, 0.5, dt)
+    s.sync()
+    PA, WA = s.get_state()
+    assert np.array_equal(s.get_array("hWA"), o.array("hWA"))
+    assert np.array_equal(PA, o.array("PA")) and np.array_equal(WA, o.array("WA"))
+    s.close()
+
+
 def test_stage_residual_and_history_levels(case_root):
     """Solver.bdf2_stage: after the stage hWA is the residual of the final
     flux_sourceterm, as in the oracle; the time levels WP / WP2 are WA of the
