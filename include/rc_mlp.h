@@ -51,6 +51,15 @@ int rc_mlp_gradient(rc_mlp* net, const float* d_x, const float* d_t, int n, floa
                     void* stream);
 /* one Adam step (bias-corrected, step counted from 1) with the given gradient */
 int rc_mlp_adam(rc_mlp* net, const float* d_grad, float lr, float beta1, float beta2, float eps, void* stream);
+/* `steps` Adam steps on batches of `batch` (a multiple of 128) pairs drawn
+ * with replacement on the device from the n pairs (d_x: n x 7 raw features,
+ * d_t: n x 4 targets, row-major; seed selects the draws), learning rate
+ * decaying from lr to lr_end on a cosine; d_loss (device, steps floats, may be
+ * null) receives each step's loss.  One CUDA graph per step; returns when the
+ * steps are done. */
+int rc_mlp_train(rc_mlp* net, const float* d_x, const float* d_t, long long n, int steps, int batch, float lr,
+                 float lr_end, float beta1, float beta2, float eps, unsigned long long seed, float* d_loss,
+                 void* stream);
 const char* rc_mlp_last_error(rc_mlp* net);
 
 #ifdef __cplusplus

@@ -131,6 +131,8 @@ SIGNATURES = {
     "rc_mlp_forward": (_i, [_vp, _vp, _i, _vp, _vp]),
     "rc_mlp_gradient": (_i, [_vp, _vp, _vp, _i, _vp, ctypes.POINTER(ctypes.c_float), _vp]),
     "rc_mlp_adam": (_i, [_vp, _vp, ctypes.c_float, ctypes.c_float, ctypes.c_float, ctypes.c_float, _vp]),
+    "rc_mlp_train": (_i, [_vp, _vp, _vp, ctypes.c_longlong, _i, _i, ctypes.c_float, ctypes.c_float, ctypes.c_float,
+                          ctypes.c_float, ctypes.c_float, ctypes.c_ulonglong, _vp, _vp]),
     "rc_mlp_last_error": (_cp, [_vp]),
     "rc_chem_substeps": (_i, [_vp, _IP]),
     "rc_chem_integrate": (_i, [_vp, _vp, _vp, _i, _vp, _vp, _d, _i]),

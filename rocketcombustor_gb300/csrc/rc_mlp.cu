@@ -13,11 +13,11 @@
 //   k_mlp_fwd16<Io>   inference, persistent over tiles of 128 samples: all
 //                     weights stay in shared memory, activations never leave
 //                     the SM (inputs and outputs through Io);
-//   k_gemm<EPI>       training GEMMs, one 128 x 128 output tile per CTA, K in
+//   k_gemm<EPI, BN>   training GEMMs, one 128 x BN output tile per CTA, K in
 //                     chunks of 128, optional split-K: forward layers (bias +
 //                     GELU epilogue), backward data (x GELU' epilogue) and
 //                     weight gradients (FP32 partials);
-//   k_layer0, k_head, k_small_grads, k_reduce_dw, k_adam, k_pack, k_pack16: the thin
+//   k_layer0, k_head, k_small_part, k_reduce_grads, k_adam, k_pack, k_pack16: the thin
 //                     layers, the loss, the small reductions, Adam and the
 //                     BF16 / F16 weight copies.
 // Every reduction has a fixed order, so gradients are reproducible run to run.
@@ -44,7 +44,6 @@ __host__ __device__ constexpr int off_w(int l) { return H * NIN + H + (l - 1) * 
 __host__ __device__ constexpr int off_b(int l) { return off_w(l) + H * H; }
 constexpr int OFF_W4 = off_w(4), OFF_B4 = OFF_W4 + NOUT * H, NPARAM = OFF_B4 + NOUT;
 static_assert(NPARAM == RC_MLP_NPARAM, "parameter layout");
-constexpr uint32_t IDESC = umma::idesc_bf16(128, 128);
 constexpr int TILE_BYTES = 128 * 128 * 2;
 
 struct Norm {
@@ -420,8 +419,20 @@ struct GemmArgs {
 enum { EPI_FWD = 0, EPI_BWD = 1, EPI_F32 = 2 };
 constexpr int GS_BAR = 2 * TILE_BYTES, GS_SLOT = GS_BAR + 8, GS_OK = GS_SLOT + 4, GEMM_SMEM = GS_OK + 4 + 1024;
 
-template <int EPI>
+// 16-byte copy global -> shared (cp.async, L2 only); cp_async_wait_all: this
+// thread's copies are complete
+__device__ __forceinline__ void cp_async16(uint32_t dst, const void* src) {
+  asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(dst), "l"(src) : "memory");
+}
+__device__ __forceinline__ void cp_async_wait_all() {
+  asm volatile("cp.async.commit_group;\n\tcp.async.wait_group 0;" ::: "memory");
+}
+
+// BN: output columns per CTA (128 or 64; the B tile holds BN rows); grid
+// (N / BN, M / 128, split-K)
+template <int EPI, int BN>
 __global__ void __launch_bounds__(128) k_gemm(GemmArgs g) {
+  static_assert(BN == 128 || BN == 64, "the tile widths of the epilogue and the TMEM allocation");
   extern __shared__ uint8_t smem_raw[];
   uint8_t* base = smem_raw + ((1024u - (umma::smem_u32(smem_raw) & 1023u)) & 1023u);
   const uint32_t sA = umma::smem_u32(base), sB = sA + TILE_BYTES;
@@ -429,11 +440,11 @@ __global__ void __launch_bounds__(128) k_gemm(GemmArgs g) {
   uint32_t* slot = reinterpret_cast<uint32_t*>(base + GS_SLOT);
   int* s_ok = reinterpret_cast<int*>(base + GS_OK);
   const int t = threadIdx.x, warp = t >> 5;
-  const int m0 = blockIdx.y * 128, n0 = blockIdx.x * 128;
+  const int m0 = blockIdx.y * 128, n0 = blockIdx.x * BN;
   const int kper = g.K / gridDim.z, kb = blockIdx.z * kper;
   if (t == 0) umma::mbar_init(bar, 1);
   if (warp == 0) {
-    umma::tmem_alloc(slot, 128);
+    umma::tmem_alloc(slot, BN);
     umma::tmem_relinquish();
   }
   umma::tc_fence_before();
@@ -443,13 +454,14 @@ __global__ void __launch_bounds__(128) k_gemm(GemmArgs g) {
   uint32_t phase = 0;
   bool ok = true;
   for (int k0 = kb; k0 < kb + kper; k0 += 128) {
+    // both 128 x 128 operand tiles as 16-byte asynchronous copies, all in
+    // flight at once, into the swizzled layout
     for (int q = t; q < 2048; q += 128) {
       const int r = q >> 4, c = q & 15;
-      const uint4 va = *reinterpret_cast<const uint4*>(g.A + (size_t)(m0 + r) * g.lda + k0 + c * 8);
-      const uint4 vb = *reinterpret_cast<const uint4*>(g.B + (size_t)(n0 + r) * g.ldb + k0 + c * 8);
-      *reinterpret_cast<uint4*>(base + umma::sw128_offset(r, c * 8, 128)) = va;
-      *reinterpret_cast<uint4*>(base + TILE_BYTES + umma::sw128_offset(r, c * 8, 128)) = vb;
+      cp_async16(sA + umma::sw128_offset(r, c * 8, 128), g.A + (size_t)(m0 + r) * g.lda + k0 + c * 8);
+      if (r < BN) cp_async16(sB + umma::sw128_offset(r, c * 8, BN), g.B + (size_t)(n0 + r) * g.ldb + k0 + c * 8);
     }
+    cp_async_wait_all();
     umma::fence_async_smem();
     umma::tc_fence_before();
     __syncthreads();
@@ -457,7 +469,7 @@ __global__ void __launch_bounds__(128) k_gemm(GemmArgs g) {
       umma::tc_fence_after();
 #pragma unroll
       for (int kk = 0; kk < 8; ++kk)
-        umma::mma_bf16(tmem, umma::sdesc_k(sA, 128, kk), umma::sdesc_k(sB, 128, kk), IDESC,
+        umma::mma_bf16(tmem, umma::sdesc_k(sA, 128, kk), umma::sdesc_k(sB, BN, kk), umma::idesc_bf16(128, BN),
                        (k0 > kb || kk > 0) ? 1u : 0u);
       umma::mma_commit(bar);
       *s_ok = umma::mbar_wait(bar, phase) ? 1 : 0;
@@ -469,7 +481,7 @@ __global__ void __launch_bounds__(128) k_gemm(GemmArgs g) {
   }
   if (ok) {
     const int m = m0 + warp * 32 + (t & 31);
-    for (int c = 0; c < 4; ++c) {
+    for (int c = 0; c < BN / 32; ++c) {
       float v[32];
       umma::tmem_ld32(tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)(c * 32), v);
       const int nc = n0 + c * 32;
@@ -480,17 +492,29 @@ __global__ void __launch_bounds__(128) k_gemm(GemmArgs g) {
       } else {
         float o[32];
         if (EPI == EPI_FWD) {
-          float* hd = g.Hout + (size_t)m * g.N + nc;
+          float4* hd = reinterpret_cast<float4*>(g.Hout + (size_t)m * g.N + nc);
+          const float4* bz = reinterpret_cast<const float4*>(g.bias + nc);
 #pragma unroll
-          for (int j = 0; j < 32; ++j) {
-            const float h = v[j] + g.bias[nc + j];
+          for (int j = 0; j < 8; ++j) {
+            const float4 b4 = bz[j];
+            const float4 h = make_float4(v[4 * j] + b4.x, v[4 * j + 1] + b4.y, v[4 * j + 2] + b4.z,
+                                         v[4 * j + 3] + b4.w);
             hd[j] = h;
-            o[j] = gelu(h);
+            o[4 * j] = gelu(h.x);
+            o[4 * j + 1] = gelu(h.y);
+            o[4 * j + 2] = gelu(h.z);
+            o[4 * j + 3] = gelu(h.w);
           }
         } else {
-          const float* hs = g.Hin + (size_t)m * g.N + nc;
+          const float4* hs = reinterpret_cast<const float4*>(g.Hin + (size_t)m * g.N + nc);
 #pragma unroll
-          for (int j = 0; j < 32; ++j) o[j] = v[j] * gelu_d(hs[j]);
+          for (int j = 0; j < 8; ++j) {
+            const float4 h = hs[j];
+            o[4 * j] = v[4 * j] * gelu_d(h.x);
+            o[4 * j + 1] = v[4 * j + 1] * gelu_d(h.y);
+            o[4 * j + 2] = v[4 * j + 2] * gelu_d(h.z);
+            o[4 * j + 3] = v[4 * j + 3] * gelu_d(h.w);
+          }
         }
         uint4* rd = reinterpret_cast<uint4*>(g.Orow + (size_t)m * g.N + nc);
 #pragma unroll
@@ -506,76 +530,113 @@ __global__ void __launch_bounds__(128) k_gemm(GemmArgs g) {
   __syncthreads();
   if (warp == 0) {
     umma::tc_fence_after();
-    umma::tmem_dealloc(tmem, 128);
+    umma::tmem_dealloc(tmem, BN);
   }
 }
 
-// layer 0 for a training batch: xn (n x 7), H0 (n x 128 FP32), A0 row / column (BF16)
-__global__ void k_layer0(const float* __restrict__ x, Norm nr, const float* __restrict__ P, int n, float* xn,
-                         float* H0, __nv_bfloat16* Arow, __nv_bfloat16* Acol) {
-  const int s = blockIdx.x * blockDim.x + threadIdx.x;
+// layer 0 for a training batch: xn (n x 7), H0 (n x 128 FP32), A0 row / column
+// (BF16).  A block takes 32 samples (the lanes) and its 16 warps 8 outputs each;
+// warp 0 forms the samples' features.
+constexpr int L0_THREADS = 512;
+__global__ void __launch_bounds__(L0_THREADS) k_layer0(const float* __restrict__ x, Norm nr,
+                                                       const float* __restrict__ P, int n, float* xn, float* H0,
+                                                       __nv_bfloat16* Arow, __nv_bfloat16* Acol) {
+  __shared__ float sf[32][NIN + 1];
+  const int lane = threadIdx.x & 31, c8 = threadIdx.x >> 5;
+  const int s = blockIdx.x * 32 + lane;
+  if (c8 == 0 && s < n) {
+    float f[NIN];
+    features(x + (size_t)s * NIN, nr, f);
+#pragma unroll
+    for (int i = 0; i < NIN; ++i) {
+      xn[(size_t)s * NIN + i] = f[i];
+      sf[lane][i] = f[i];
+    }
+  }
+  __syncthreads();
   if (s >= n) return;
   float f[NIN];
-  features(x + (size_t)s * NIN, nr, f);
 #pragma unroll
-  for (int i = 0; i < NIN; ++i) xn[(size_t)s * NIN + i] = f[i];
-  for (int c8 = 0; c8 < 16; ++c8) {
-    float a[8];
-    for (int e = 0; e < 8; ++e) {
-      const int o = c8 * 8 + e;
-      float h = P[OFF_B0 + o];
+  for (int i = 0; i < NIN; ++i) f[i] = sf[lane][i];
+  float h[8], a[8];
 #pragma unroll
-      for (int i = 0; i < NIN; ++i) h = fmaf(P[OFF_W0 + o * NIN + i], f[i], h);
-      H0[(size_t)s * H + o] = h;
-      a[e] = gelu(h);
-      Acol[(size_t)o * n + s] = __float2bfloat16_rn(a[e]);
-    }
-    reinterpret_cast<uint4*>(Arow + (size_t)s * H)[c8] = pack8(a);
+  for (int e = 0; e < 8; ++e) {
+    const int o = c8 * 8 + e;
+    h[e] = P[OFF_B0 + o];
+#pragma unroll
+    for (int i = 0; i < NIN; ++i) h[e] = fmaf(P[OFF_W0 + o * NIN + i], f[i], h[e]);
+    a[e] = gelu(h[e]);
+    Acol[(size_t)o * n + s] = __float2bfloat16_rn(a[e]);
   }
+  float4* hd = reinterpret_cast<float4*>(H0 + (size_t)s * H + c8 * 8);
+  hd[0] = make_float4(h[0], h[1], h[2], h[3]);
+  hd[1] = make_float4(h[4], h[5], h[6], h[7]);
+  reinterpret_cast<uint4*>(Arow + (size_t)s * H)[c8] = pack8(a);
 }
 
 // output layer, loss and its gradient down to dH3: y = W4 gelu(H3) + b4,
-// L = mean((y - t)^2) over n x 4, dy = 2 (y - t) / (4 n)
-constexpr int HEAD_THREADS = 128;
+// L = mean((y - t)^2) over n x 4, dy = 2 (y - t) / (4 n).  Four threads per
+// sample (lane = 4 sample + quarter), each over 32 of the 128 inputs; the
+// quarters' partial outputs are added by a butterfly (every thread of the
+// sample gets the same sum).  loss_part: one partial per block of 32 samples.
+constexpr int HEAD_THREADS = 128, HEAD_SAMPLES = HEAD_THREADS / 4;
 __global__ void __launch_bounds__(HEAD_THREADS) k_head(const float* __restrict__ H3, const float* __restrict__ tgt,
                                                        const float* __restrict__ P, int n, float* dy,
                                                        __nv_bfloat16* dHrow, __nv_bfloat16* dHcol, float* loss_part) {
   __shared__ float red[HEAD_THREADS];
-  const int s = blockIdx.x * blockDim.x + threadIdx.x;
+  const int qd = threadIdx.x & 3, s = blockIdx.x * HEAD_SAMPLES + (threadIdx.x >> 2);
+  const bool valid = s < n;
+  const int sc_ = valid ? s : 0;
+  float h[32];
+#pragma unroll
+  for (int j = 0; j < 8; ++j) {
+    const float4 v = reinterpret_cast<const float4*>(H3 + (size_t)sc_ * H + qd * 32)[j];
+    h[4 * j] = v.x;
+    h[4 * j + 1] = v.y;
+    h[4 * j + 2] = v.z;
+    h[4 * j + 3] = v.w;
+  }
+  float y[NOUT];
+#pragma unroll
+  for (int m = 0; m < NOUT; ++m) y[m] = 0.f;
+#pragma unroll
+  for (int i = 0; i < 32; ++i) {
+    const float a = gelu(h[i]);
+#pragma unroll
+    for (int m = 0; m < NOUT; ++m) y[m] = fmaf(a, P[OFF_W4 + m * H + qd * 32 + i], y[m]);
+  }
+#pragma unroll
+  for (int m = 0; m < NOUT; ++m) {
+    y[m] += __shfl_xor_sync(0xffffffffu, y[m], 1);
+    y[m] += __shfl_xor_sync(0xffffffffu, y[m], 2);
+  }
   float l2 = 0.f;
-  if (s < n) {
-    const float* h = H3 + (size_t)s * H;
-    float y[NOUT];
+  float g[NOUT];
+  const float sc = 2.f / (4.f * (float)n);
 #pragma unroll
-    for (int m = 0; m < NOUT; ++m) y[m] = 0.f;
-    for (int i = 0; i < H; ++i) {
-      const float a = gelu(h[i]);
+  for (int m = 0; m < NOUT; ++m) {
+    const float e = valid ? y[m] + P[OFF_B4 + m] - tgt[(size_t)s * NOUT + m] : 0.f;
+    l2 = fmaf(e, e, l2);
+    g[m] = sc * e;
+    if (valid && qd == 0) dy[(size_t)s * NOUT + m] = g[m];
+  }
+  if (valid) {
 #pragma unroll
-      for (int m = 0; m < NOUT; ++m) y[m] = fmaf(a, P[OFF_W4 + m * H + i], y[m]);
-    }
-    float g[NOUT];
-    const float sc = 2.f / (4.f * (float)n);
-#pragma unroll
-    for (int m = 0; m < NOUT; ++m) {
-      const float e = y[m] + P[OFF_B4 + m] - tgt[(size_t)s * NOUT + m];
-      l2 = fmaf(e, e, l2);
-      g[m] = sc * e;
-      dy[(size_t)s * NOUT + m] = g[m];
-    }
-    for (int c8 = 0; c8 < 16; ++c8) {
+    for (int c8 = 0; c8 < 4; ++c8) {
       float o[8];
+#pragma unroll
       for (int e = 0; e < 8; ++e) {
-        const int i = c8 * 8 + e;
+        const int i = qd * 32 + c8 * 8 + e;
         float da = 0.f;
 #pragma unroll
         for (int m = 0; m < NOUT; ++m) da = fmaf(P[OFF_W4 + m * H + i], g[m], da);
-        o[e] = da * gelu_d(h[i]);
+        o[e] = da * gelu_d(h[c8 * 8 + e]);
         dHcol[(size_t)i * n + s] = __float2bfloat16_rn(o[e]);
       }
-      reinterpret_cast<uint4*>(dHrow + (size_t)s * H)[c8] = pack8(o);
+      reinterpret_cast<uint4*>(dHrow + (size_t)s * H + qd * 32)[c8] = pack8(o);
     }
   }
-  red[threadIdx.x] = l2;
+  red[threadIdx.x] = qd == 0 ? l2 : 0.f;
   __syncthreads();
   for (int w = HEAD_THREADS / 2; w > 0; w >>= 1) {
     if (threadIdx.x < w) red[threadIdx.x] += red[threadIdx.x + w];
@@ -584,59 +645,181 @@ __global__ void __launch_bounds__(HEAD_THREADS) k_head(const float* __restrict__
   if (threadIdx.x == 0) loss_part[blockIdx.x] = red[0];
 }
 
-// gradients of W0, b0..b3, W4, b4 (one thread per parameter, samples in order)
-__global__ void k_small_grads(const float* __restrict__ xn, const __nv_bfloat16* __restrict__ dH0,
-                              const __nv_bfloat16* __restrict__ dH1, const __nv_bfloat16* __restrict__ dH2,
-                              const __nv_bfloat16* __restrict__ dH3, const float* __restrict__ H3,
-                              const float* __restrict__ dy, int n, float* grad) {
-  const int q = blockIdx.x * blockDim.x + threadIdx.x;
-  constexpr int NW0 = H * NIN, NB = 4 * H, NW4 = NOUT * H;
-  if (q < NW0) {
-    const int o = q / NIN, i = q % NIN;
-    float a = 0.f;
-    for (int s = 0; s < n; ++s) a = fmaf(__bfloat162float(dH0[(size_t)s * H + o]), xn[(size_t)s * NIN + i], a);
-    grad[OFF_W0 + q] = a;
-  } else if (q < NW0 + NB) {
-    const int l = (q - NW0) / H, o = (q - NW0) % H;
-    const __nv_bfloat16* d = l == 0 ? dH0 : l == 1 ? dH1 : l == 2 ? dH2 : dH3;
-    float a = 0.f;
-    for (int s = 0; s < n; ++s) a += __bfloat162float(d[(size_t)s * H + o]);
-    grad[(l == 0 ? OFF_B0 : off_b(l)) + o] = a;
-  } else if (q < NW0 + NB + NW4) {
-    const int m = (q - NW0 - NB) / H, i = (q - NW0 - NB) % H;
-    float a = 0.f;
-    for (int s = 0; s < n; ++s) a = fmaf(dy[(size_t)s * NOUT + m], gelu(H3[(size_t)s * H + i]), a);
-    grad[OFF_W4 + m * H + i] = a;
-  } else if (q < NW0 + NB + NW4 + NOUT) {
-    const int m = q - NW0 - NB - NW4;
-    float a = 0.f;
-    for (int s = 0; s < n; ++s) a += dy[(size_t)s * NOUT + m];
-    grad[OFF_B4 + m] = a;
+// Gradients of the thin parameters (W0, b0..b3, W4, b4) in two passes of
+// fixed order.  k_small_part: block c sums samples [c chunk, (c + 1) chunk),
+// thread o its column: W0[o][0..6], b0..b3[o], W4[0..3][o] (SMALL_PER
+// values at part[c][o SMALL_PER ..]) and, for o < 4, b4[o] (at H SMALL_PER + o).
+// The samples come through shared memory in tiles of SMALL_TILE (dH0..dH3,
+// H3, xn, dy rows), the next tile's asynchronous copies in flight while the
+// current one is summed.  chunk: a multiple of SMALL_TILE.
+constexpr int SMALL_PER = NIN + 4 + NOUT, SMALL_N = H * SMALL_PER + NOUT, SMALL_ZMAX = 512, SMALL_TILE = 16;
+// one tile's buffer: dH0..dH3 (BF16), H3 (FP32), xn, dy
+constexpr int ST_DH = 0, ST_H3 = ST_DH + 4 * SMALL_TILE * H * 2, ST_XN = ST_H3 + SMALL_TILE * H * 4,
+              ST_DY = ST_XN + SMALL_TILE * NIN * 4, ST_BYTES = ST_DY + SMALL_TILE * NOUT * 4,
+              SMALL_SMEM = 2 * ST_BYTES;
+static_assert(ST_XN % 16 == 0 && ST_DY % 16 == 0 && ST_BYTES % 16 == 0 && (SMALL_TILE * NIN * 4) % 16 == 0,
+              "16-byte copies");
+__global__ void __launch_bounds__(H) k_small_part(const float* __restrict__ xn, const __nv_bfloat16* __restrict__ dH0,
+                                                  const __nv_bfloat16* __restrict__ dH1,
+                                                  const __nv_bfloat16* __restrict__ dH2,
+                                                  const __nv_bfloat16* __restrict__ dH3, const float* __restrict__ H3,
+                                                  const float* __restrict__ dy, int n, int chunk, float* part) {
+  extern __shared__ __align__(16) uint8_t st_smem[];
+  const int o = threadIdx.x, s0 = blockIdx.x * chunk, s1 = min(n, s0 + chunk);
+  const int ntile = (s1 - s0) / SMALL_TILE;
+  const uint32_t sbase = umma::smem_u32(st_smem);
+  auto stage = [&](int k) {
+    const int t0 = s0 + k * SMALL_TILE;
+    const uint32_t b = sbase + (uint32_t)((k & 1) * ST_BYTES);
+    const __nv_bfloat16* dh[4] = {dH0, dH1, dH2, dH3};
+    constexpr int DH16 = SMALL_TILE * H * 2 / 16;  // 16-byte pieces of one dH tile
+#pragma unroll
+    for (int l = 0; l < 4; ++l)
+      for (int q = o; q < DH16; q += H)
+        cp_async16(b + ST_DH + (uint32_t)(l * DH16 + q) * 16u, reinterpret_cast<const uint8_t*>(dh[l] + (size_t)t0 * H) + q * 16);
+    for (int q = o; q < SMALL_TILE * H * 4 / 16; q += H)
+      cp_async16(b + ST_H3 + (uint32_t)q * 16u, reinterpret_cast<const uint8_t*>(H3 + (size_t)t0 * H) + q * 16);
+    if (o < SMALL_TILE * NIN * 4 / 16)
+      cp_async16(b + ST_XN + (uint32_t)o * 16u, reinterpret_cast<const uint8_t*>(xn + (size_t)t0 * NIN) + o * 16);
+    if (o < SMALL_TILE * NOUT * 4 / 16)
+      cp_async16(b + ST_DY + (uint32_t)o * 16u, reinterpret_cast<const uint8_t*>(dy + (size_t)t0 * NOUT) + o * 16);
+    asm volatile("cp.async.commit_group;" ::: "memory");
+  };
+  float w0[NIN], b[4], w4[NOUT], b4 = 0.f;
+#pragma unroll
+  for (int i = 0; i < NIN; ++i) w0[i] = 0.f;
+#pragma unroll
+  for (int l = 0; l < 4; ++l) b[l] = 0.f;
+#pragma unroll
+  for (int m = 0; m < NOUT; ++m) w4[m] = 0.f;
+  if (ntile > 0) stage(0);
+  for (int k = 0; k < ntile; ++k) {
+    if (k + 1 < ntile) {
+      stage(k + 1);
+      asm volatile("cp.async.wait_group 1;" ::: "memory");
+    } else {
+      asm volatile("cp.async.wait_group 0;" ::: "memory");
+    }
+    __syncthreads();
+    const uint8_t* tb = st_smem + (k & 1) * ST_BYTES;
+    const __nv_bfloat16* sdh = reinterpret_cast<const __nv_bfloat16*>(tb + ST_DH);
+    const float* sh3 = reinterpret_cast<const float*>(tb + ST_H3);
+    const float* sxn = reinterpret_cast<const float*>(tb + ST_XN);
+    const float* sdy = reinterpret_cast<const float*>(tb + ST_DY);
+#pragma unroll 4
+    for (int s = 0; s < SMALL_TILE; ++s) {
+      const float d0 = __bfloat162float(sdh[(0 * SMALL_TILE + s) * H + o]);
+#pragma unroll
+      for (int i = 0; i < NIN; ++i) w0[i] = fmaf(d0, sxn[s * NIN + i], w0[i]);
+      b[0] += d0;
+      b[1] += __bfloat162float(sdh[(1 * SMALL_TILE + s) * H + o]);
+      b[2] += __bfloat162float(sdh[(2 * SMALL_TILE + s) * H + o]);
+      b[3] += __bfloat162float(sdh[(3 * SMALL_TILE + s) * H + o]);
+      const float a = gelu(sh3[s * H + o]);
+#pragma unroll
+      for (int m = 0; m < NOUT; ++m) w4[m] = fmaf(sdy[s * NOUT + m], a, w4[m]);
+      if (o < NOUT) b4 += sdy[s * NOUT + o];
+    }
+    __syncthreads();  // the buffer is refilled by the next-but-one stage
   }
+  float* p = part + (size_t)blockIdx.x * SMALL_N + o * SMALL_PER;
+#pragma unroll
+  for (int i = 0; i < NIN; ++i) p[i] = w0[i];
+#pragma unroll
+  for (int l = 0; l < 4; ++l) p[NIN + l] = b[l];
+#pragma unroll
+  for (int m = 0; m < NOUT; ++m) p[NIN + 4 + m] = w4[m];
+  if (o < NOUT) part[(size_t)blockIdx.x * SMALL_N + H * SMALL_PER + o] = b4;
 }
 
-// dW_l = sum over the split-K partials, in order
-__global__ void k_reduce_dw(const float* __restrict__ part, int z, float* grad) {
+// The gradient vector from the partials, each summed in order: dW_1..3 over
+// the z split-K partials of the hidden weight-gradient GEMMs, the thin
+// parameters over the zs sample chunks of k_small_part.
+__global__ void k_reduce_grads(const float* __restrict__ part, int z, const float* __restrict__ spart, int zs,
+                               float* grad) {
   const int q = blockIdx.x * blockDim.x + threadIdx.x;
-  if (q >= 3 * H * H) return;
-  const int l = q / (H * H), e = q % (H * H);
-  const float* p = part + (size_t)l * z * H * H;
+  if (q < 3 * H * H) {
+    const int l = q / (H * H), e = q % (H * H);
+    const float* p = part + (size_t)l * z * H * H;
+    float a = 0.f;
+#pragma unroll 8
+    for (int k = 0; k < z; ++k) a += p[(size_t)k * H * H + e];
+    grad[off_w(l + 1) + e] = a;
+    return;
+  }
+  const int r = q - 3 * H * H;
+  if (r >= SMALL_N) return;
   float a = 0.f;
-  for (int k = 0; k < z; ++k) a += p[(size_t)k * H * H + e];
-  grad[off_w(l + 1) + e] = a;
+#pragma unroll 8
+  for (int k = 0; k < zs; ++k) a += spart[(size_t)k * SMALL_N + r];
+  int dst;
+  if (r < H * SMALL_PER) {
+    const int o = r / SMALL_PER, k = r % SMALL_PER;
+    dst = k < NIN ? OFF_W0 + o * NIN + k : k < NIN + 4 ? (k == NIN ? OFF_B0 : off_b(k - NIN)) + o
+                                                       : OFF_W4 + (k - NIN - 4) * H + o;
+  } else {
+    dst = OFF_B4 + (r - H * SMALL_PER);
+  }
+  grad[dst] = a;
 }
 
+// the loss from k_head's partials: lane l sums partials l, l + 32, ... in
+// order, then a butterfly over the lanes (one warp)
 __global__ void k_loss_final(const float* part, int nb, int n, float* loss) {
-  if (threadIdx.x != 0 || blockIdx.x != 0) return;
+  if (blockIdx.x != 0 || threadIdx.x >= 32) return;
   float a = 0.f;
-  for (int b = 0; b < nb; ++b) a += part[b];
-  *loss = a / (4.f * (float)n);
+  for (int b = threadIdx.x; b < nb; b += 32) a += part[b];
+#pragma unroll
+  for (int w = 16; w > 0; w >>= 1) a += __shfl_xor_sync(0xffffffffu, a, w);
+  if (threadIdx.x == 0) *loss = a / (4.f * (float)n);
 }
 
+// Training batch number *it: `batch` pairs drawn with replacement from the n
+// pairs (x: n x NIN, t: n x NOUT, row-major), pair index = splitmix64 (Steele,
+// Lea and Flood, "Fast splittable pseudorandom number generators", 2014) of
+// seed + (it * batch + i + 1) * golden gamma, modulo n; gathered into xb, tb.
+__global__ void k_batch(const float* __restrict__ x, const float* __restrict__ t, long long n,
+                        unsigned long long seed, const int* it, int batch, float* xb, float* tb) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= batch) return;
+  unsigned long long z = seed + 0x9E3779B97F4A7C15ull * ((unsigned long long)*it * (unsigned long long)batch +
+                                                         (unsigned long long)i + 1ull);
+  z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+  z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+  z ^= z >> 31;
+  const long long j = (long long)(z % (unsigned long long)n);
+#pragma unroll
+  for (int k = 0; k < NIN; ++k) xb[(size_t)i * NIN + k] = x[(size_t)j * NIN + k];
+#pragma unroll
+  for (int k = 0; k < NOUT; ++k) tb[(size_t)i * NOUT + k] = t[(size_t)j * NOUT + k];
+}
+
+// End of training step k = *it of `steps`: the loss into hist[k] (if hist),
+// the next Adam update's learning rate (cosine decay from lr at k = 0 to
+// lr_end at k = steps - 1) and bias corrections 1 - beta^(t0 + k + 1) into
+// sched, then *it = k + 1.
+__global__ void k_train_tail(int* it, int steps, int t0, float lr, float lr_end, float b1, float b2,
+                             const float* loss, float* hist, float* sched) {
+  if (threadIdx.x != 0 || blockIdx.x != 0) return;
+  const int k = *it;
+  const double c = cos(3.141592653589793 * (double)k / (double)(steps > 1 ? steps - 1 : 1));
+  sched[0] = (float)((double)lr_end + 0.5 * ((double)lr - (double)lr_end) * (1.0 + c));
+  sched[1] = 1.f - powf(b1, (float)(t0 + k + 1));
+  sched[2] = 1.f - powf(b2, (float)(t0 + k + 1));
+  if (hist) hist[k] = *loss;
+  *it = k + 1;
+}
+
+// sched (may be null): lr, bc1, bc2 of this step in device memory (k_train_tail)
 __global__ void k_adam(float* p, float* m1, float* m2, const float* __restrict__ g, float lr, float b1, float b2,
-                       float eps, float bc1, float bc2) {
+                       float eps, float bc1, float bc2, const float* sched) {
   const int q = blockIdx.x * blockDim.x + threadIdx.x;
   if (q >= NPARAM) return;
+  if (sched) {
+    lr = sched[0];
+    bc1 = sched[1];
+    bc2 = sched[2];
+  }
   const float gq = g[q];
   const float a = b1 * m1[q] + (1.f - b1) * gq;
   const float b = b2 * m2[q] + (1.f - b2) * gq * gq;
@@ -742,6 +925,11 @@ struct rc_mlp {
   std::vector<void*> work;
   float *xn = nullptr, *Hs[4] = {}, *dy = nullptr, *loss_part = nullptr, *loss = nullptr, *part = nullptr,
         *grad = nullptr;
+  float* spart = nullptr;                                // k_small_part's partials
+  cudaStream_t side = nullptr;                           // the weight-gradient branch
+  cudaEvent_t ev_dh[4] = {}, ev_join = nullptr;          // dH_l ready / the branch done
+  float *xb = nullptr, *tb = nullptr, *sched = nullptr;  // rc_mlp_train: the batch, the step's schedule
+  int* it = nullptr;                                     // rc_mlp_train: the step counter
   __nv_bfloat16 *Arow[3] = {}, *Acol[3] = {}, *dHrow[4] = {}, *dHcol[4] = {};
   std::string err;
 };
@@ -775,6 +963,8 @@ int alloc_work(rc_mlp* m, size_t count, T** out) {
   return RC_OK;
 }
 
+// split-K slices of the hidden weight-gradient GEMMs, at most
+constexpr int ZSPLIT_MAX = 64;
 int ensure_work(rc_mlp* m, int n) {
   if (n <= m->cap) return RC_OK;
   for (void* p : m->work) cudaFree(p);
@@ -792,11 +982,16 @@ int ensure_work(rc_mlp* m, int n) {
     st |= alloc_work(m, N * Hh, &m->dHcol[l]);
   }
   st |= alloc_work(m, N * mlp::NOUT, &m->dy);
-  st |= alloc_work(m, (N + 127) / 128, &m->loss_part);
+  st |= alloc_work(m, (N + mlp::HEAD_SAMPLES - 1) / mlp::HEAD_SAMPLES, &m->loss_part);
   st |= alloc_work(m, (size_t)1, &m->loss);
+  st |= alloc_work(m, N * mlp::NIN, &m->xb);
+  st |= alloc_work(m, N * mlp::NOUT, &m->tb);
+  st |= alloc_work(m, (size_t)4, &m->sched);
+  st |= alloc_work(m, (size_t)1, &m->it);
   // split-K partials of the weight gradients, for up to n / 1024 splits
-  m->zsplit = std::max(1, n / 1024);
+  m->zsplit = std::max(1, std::min(ZSPLIT_MAX, n / 256));
   st |= alloc_work(m, (size_t)3 * m->zsplit * Hh * Hh, &m->part);
+  st |= alloc_work(m, (size_t)mlp::SMALL_ZMAX * mlp::SMALL_N, &m->spart);
   if (st) return st;
   m->cap = n;
   return RC_OK;
@@ -849,6 +1044,10 @@ int rc_mlp_create(int device, rc_mlp** out) {
   cudaMemset(m->m1, 0, P * sizeof(float));
   cudaMemset(m->m2, 0, P * sizeof(float));
   cudaMemset(m->derr, 0, sizeof(unsigned));
+  if (cudaStreamCreateWithFlags(&m->side, cudaStreamNonBlocking) != cudaSuccess) return bail(RC_ERR_CUDA);
+  for (auto& e : m->ev_dh)
+    if (cudaEventCreateWithFlags(&e, cudaEventDisableTiming) != cudaSuccess) return bail(RC_ERR_CUDA);
+  if (cudaEventCreateWithFlags(&m->ev_join, cudaEventDisableTiming) != cudaSuccess) return bail(RC_ERR_CUDA);
   // the fills run on the legacy stream; the network's kernels may run on
   // non-blocking streams, which are not ordered after it
   if (cudaDeviceSynchronize() != cudaSuccess) return bail(RC_ERR_CUDA);
@@ -857,11 +1056,13 @@ int rc_mlp_create(int device, rc_mlp** out) {
   for (int i = 0; i < 6; ++i) m->norm.dom[i] = dom[i];
   if (cudaFuncSetAttribute(mlp::k_mlp_fwd16<mlp::IoRaw>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                            mlp::F2_SMEM) != cudaSuccess ||
-      cudaFuncSetAttribute(mlp::k_gemm<mlp::EPI_FWD>, cudaFuncAttributeMaxDynamicSharedMemorySize, mlp::GEMM_SMEM) !=
+      cudaFuncSetAttribute(mlp::k_gemm<mlp::EPI_FWD, 64>, cudaFuncAttributeMaxDynamicSharedMemorySize, mlp::GEMM_SMEM) !=
           cudaSuccess ||
-      cudaFuncSetAttribute(mlp::k_gemm<mlp::EPI_BWD>, cudaFuncAttributeMaxDynamicSharedMemorySize, mlp::GEMM_SMEM) !=
+      cudaFuncSetAttribute(mlp::k_gemm<mlp::EPI_BWD, 64>, cudaFuncAttributeMaxDynamicSharedMemorySize, mlp::GEMM_SMEM) !=
           cudaSuccess ||
-      cudaFuncSetAttribute(mlp::k_gemm<mlp::EPI_F32>, cudaFuncAttributeMaxDynamicSharedMemorySize, mlp::GEMM_SMEM) !=
+      cudaFuncSetAttribute(mlp::k_gemm<mlp::EPI_F32, 128>, cudaFuncAttributeMaxDynamicSharedMemorySize, mlp::GEMM_SMEM) !=
+          cudaSuccess ||
+      cudaFuncSetAttribute(mlp::k_small_part, cudaFuncAttributeMaxDynamicSharedMemorySize, mlp::SMALL_SMEM) !=
           cudaSuccess)
     return bail(RC_ERR_CUDA);
   *out = m;
@@ -873,6 +1074,10 @@ int rc_mlp_destroy(rc_mlp* m) {
   for (void* p : m->work) cudaFree(p);
   cudaFree(m->params); cudaFree(m->m1); cudaFree(m->m2); cudaFree(m->grad);
   cudaFree(m->Wb); cudaFree(m->WbT); cudaFree(m->Wh); cudaFree(m->derr);
+  for (cudaEvent_t e : m->ev_dh)
+    if (e) cudaEventDestroy(e);
+  if (m->ev_join) cudaEventDestroy(m->ev_join);
+  if (m->side) cudaStreamDestroy(m->side);
   delete m;
   return RC_OK;
 }
@@ -921,17 +1126,22 @@ int rc_mlp_forward(rc_mlp* m, const float* d_x, int n, float* d_y, void* stream)
   return RC_OK;
 }
 
-int rc_mlp_gradient(rc_mlp* m, const float* d_x, const float* d_t, int n, float* d_grad, float* loss,
-                    void* stream) {
-  if (!m || !d_x || !d_t || !d_grad || n <= 0 || n % 128) return RC_ERR_ARG;
-  if (int st = ensure_work(m, n)) return st;
-  cudaStream_t s = static_cast<cudaStream_t>(stream);
+}  // extern "C"
+
+namespace {
+// the kernels of one loss-and-gradient evaluation on n samples (work buffers
+// sized for n), enqueued on s without synchronising
+int enqueue_gradient(rc_mlp* m, const float* d_x, const float* d_t, int n, float* d_grad, cudaStream_t s) {
   using namespace mlp;
-  // split-K of the weight gradients: about 8 chunks of 128 samples per CTA,
-  // an exact divisor of the n / 128 chunks (each split a whole number of chunks)
-  int z = std::max(1, std::min(m->zsplit, n / 1024));
+  // split-K of the weight gradients: about 2 chunks of 128 samples per CTA
+  // (at most ZSPLIT_MAX splits), an exact divisor of the n / 128 chunks (each
+  // split a whole number of chunks)
+  int z = std::max(1, std::min(m->zsplit, n / 256));
   while ((n / 128) % z) --z;
-  k_layer0<<<(n + 127) / 128, 128, 0, s>>>(d_x, m->norm, m->params, n, m->xn, m->Hs[0], m->Arow[0], m->Acol[0]);
+  // sample chunks of the thin parameters' gradients: 64 samples or more, at
+  // most SMALL_ZMAX chunks (n is a multiple of 128, so every chunk is whole tiles)
+  const int chunk = 64 * ((n + 64 * SMALL_ZMAX - 1) / (64 * SMALL_ZMAX)), zs = (n + chunk - 1) / chunk;
+  k_layer0<<<(n + 31) / 32, L0_THREADS, 0, s>>>(d_x, m->norm, m->params, n, m->xn, m->Hs[0], m->Arow[0], m->Acol[0]);
   // hidden layers 1..3 forward: H_l = A_{l-1} W_l^T + b_l
   for (int l = 1; l <= 3; ++l) {
     GemmArgs g{};
@@ -943,11 +1153,26 @@ int rc_mlp_gradient(rc_mlp* m, const float* d_x, const float* d_t, int n, float*
     g.Orow = l < 3 ? m->Arow[l] : m->dHrow[3];   // A3 row is not needed (the head recomputes it)
     g.Ocol = l < 3 ? m->Acol[l] : m->dHcol[3];   // scratch for l = 3, overwritten by the head
     g.err = m->derr;
-    k_gemm<EPI_FWD><<<dim3(1, n / 128, 1), 128, GEMM_SMEM, s>>>(g);
+    k_gemm<EPI_FWD, 64><<<dim3(H / 64, n / 128, 1), 128, GEMM_SMEM, s>>>(g);
   }
-  k_head<<<(n + HEAD_THREADS - 1) / HEAD_THREADS, HEAD_THREADS, 0, s>>>(m->Hs[3], d_t, m->params, n, m->dy,
+  k_head<<<(n + HEAD_SAMPLES - 1) / HEAD_SAMPLES, HEAD_THREADS, 0, s>>>(m->Hs[3], d_t, m->params, n, m->dy,
                                                                          m->dHrow[3], m->dHcol[3], m->loss_part);
-  // backward data: dH_{l-1} = (dH_l W_l) * gelu'(H_{l-1})
+  // backward data: dH_{l-1} = (dH_l W_l) * gelu'(H_{l-1}) on s; each weight
+  // gradient dW_l = dH_l^T A_{l-1} (split-K partials) on the side stream as
+  // soon as dH_l is ready, then the thin parameters' partials; s joins the
+  // side stream before the reduction
+  auto wgrad = [&](int l) {
+    GemmArgs g{};
+    g.A = m->dHcol[l]; g.lda = n;
+    g.B = m->Acol[l - 1]; g.ldb = n;
+    g.M = H; g.N = H; g.K = n;
+    g.C = m->part + (size_t)(l - 1) * z * H * H;
+    g.err = m->derr;
+    k_gemm<EPI_F32, 128><<<dim3(1, 1, z), 128, GEMM_SMEM, m->side>>>(g);
+  };
+  MLP_CU(cudaEventRecord(m->ev_dh[3], s));
+  MLP_CU(cudaStreamWaitEvent(m->side, m->ev_dh[3], 0));
+  wgrad(3);
   for (int l = 3; l >= 1; --l) {
     GemmArgs g{};
     g.A = m->dHrow[l]; g.lda = H;
@@ -957,24 +1182,30 @@ int rc_mlp_gradient(rc_mlp* m, const float* d_x, const float* d_t, int n, float*
     g.Orow = m->dHrow[l - 1];
     g.Ocol = m->dHcol[l - 1];
     g.err = m->derr;
-    k_gemm<EPI_BWD><<<dim3(1, n / 128, 1), 128, GEMM_SMEM, s>>>(g);
+    k_gemm<EPI_BWD, 64><<<dim3(H / 64, n / 128, 1), 128, GEMM_SMEM, s>>>(g);
+    MLP_CU(cudaEventRecord(m->ev_dh[l - 1], s));
+    MLP_CU(cudaStreamWaitEvent(m->side, m->ev_dh[l - 1], 0));
+    if (l > 1) wgrad(l - 1);
   }
-  // weight gradients of the hidden layers: dW_l = dH_l^T A_{l-1} (split-K partials)
-  for (int l = 1; l <= 3; ++l) {
-    GemmArgs g{};
-    g.A = m->dHcol[l]; g.lda = n;
-    g.B = m->Acol[l - 1]; g.ldb = n;
-    g.M = H; g.N = H; g.K = n;
-    g.C = m->part + (size_t)(l - 1) * z * H * H;
-    g.err = m->derr;
-    k_gemm<EPI_F32><<<dim3(1, 1, z), 128, GEMM_SMEM, s>>>(g);
-  }
-  k_reduce_dw<<<(3 * H * H + 255) / 256, 256, 0, s>>>(m->part, z, d_grad);
-  const int nsmall = H * NIN + 4 * H + NOUT * H + NOUT;
-  k_small_grads<<<(nsmall + 127) / 128, 128, 0, s>>>(m->xn, m->dHrow[0], m->dHrow[1], m->dHrow[2], m->dHrow[3],
-                                                     m->Hs[3], m->dy, n, d_grad);
-  k_loss_final<<<1, 32, 0, s>>>(m->loss_part, (n + HEAD_THREADS - 1) / HEAD_THREADS, n, m->loss);
+  k_small_part<<<zs, H, SMALL_SMEM, m->side>>>(m->xn, m->dHrow[0], m->dHrow[1], m->dHrow[2], m->dHrow[3], m->Hs[3],
+                                              m->dy, n, chunk, m->spart);
+  MLP_CU(cudaEventRecord(m->ev_join, m->side));
+  MLP_CU(cudaStreamWaitEvent(s, m->ev_join, 0));
+  k_reduce_grads<<<(3 * H * H + SMALL_N + 255) / 256, 256, 0, s>>>(m->part, z, m->spart, zs, d_grad);
+  k_loss_final<<<1, 32, 0, s>>>(m->loss_part, (n + HEAD_SAMPLES - 1) / HEAD_SAMPLES, n, m->loss);
   MLP_CU(cudaGetLastError());
+  return RC_OK;
+}
+}  // namespace
+
+extern "C" {
+
+int rc_mlp_gradient(rc_mlp* m, const float* d_x, const float* d_t, int n, float* d_grad, float* loss,
+                    void* stream) {
+  if (!m || !d_x || !d_t || !d_grad || n <= 0 || n % 128) return RC_ERR_ARG;
+  if (int st = ensure_work(m, n)) return st;
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  if (int st = enqueue_gradient(m, d_x, d_t, n, d_grad, s)) return st;
   if (loss) {
     MLP_CU(cudaMemcpyAsync(loss, m->loss, sizeof(float), cudaMemcpyDeviceToHost, s));
     unsigned e = 0;
@@ -994,10 +1225,59 @@ int rc_mlp_adam(rc_mlp* m, const float* d_grad, float lr, float beta1, float bet
   m->step += 1;
   const float bc1 = 1.f - std::pow(beta1, (float)m->step), bc2 = 1.f - std::pow(beta2, (float)m->step);
   mlp::k_adam<<<(mlp::NPARAM + 255) / 256, 256, 0, s>>>(m->params, m->m1, m->m2, d_grad, lr, beta1, beta2, eps, bc1,
-                                                       bc2);
+                                                       bc2, nullptr);
   mlp::k_pack<<<(3 * mlp::H * mlp::H + 255) / 256, 256, 0, s>>>(m->params, m->Wb, m->WbT);
   mlp::k_pack16<<<(mlp::PACK16_N + 255) / 256, 256, 0, s>>>(m->params, m->Wh);
   MLP_CU(cudaGetLastError());
+  return RC_OK;
+}
+
+// Adam on `steps` batches drawn on the device (k_batch), the learning rate
+// and bias corrections formed on the device (k_train_tail): one step (draw,
+// loss and gradient, Adam, the packed weights) is captured once as a CUDA
+// graph on a private stream and launched `steps` times on the caller's.
+int rc_mlp_train(rc_mlp* m, const float* d_x, const float* d_t, long long n, int steps, int batch, float lr,
+                 float lr_end, float beta1, float beta2, float eps, unsigned long long seed, float* d_loss,
+                 void* stream) {
+  if (!m || !d_x || !d_t || n <= 0 || steps < 0 || batch <= 0 || batch % 128) return RC_ERR_ARG;
+  if (steps == 0) return RC_OK;
+  if (int st = ensure_work(m, batch)) return st;
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  using namespace mlp;
+  MLP_CU(cudaMemsetAsync(m->it, 0, sizeof(int), s));
+  MLP_CU(cudaMemsetAsync(m->derr, 0, sizeof(unsigned), s));
+  cudaStream_t cs = nullptr;
+  MLP_CU(cudaStreamCreateWithFlags(&cs, cudaStreamNonBlocking));
+  cudaGraph_t g = nullptr;
+  cudaGraphExec_t ge = nullptr;
+  int st = RC_OK;
+  cudaError_t e = cudaStreamBeginCapture(cs, cudaStreamCaptureModeThreadLocal);
+  if (e == cudaSuccess) {
+    k_batch<<<(batch + 127) / 128, 128, 0, cs>>>(d_x, d_t, n, seed, m->it, batch, m->xb, m->tb);
+    st = enqueue_gradient(m, m->xb, m->tb, batch, m->grad, cs);
+    k_train_tail<<<1, 32, 0, cs>>>(m->it, steps, m->step, lr, lr_end, beta1, beta2, m->loss, d_loss, m->sched);
+    k_adam<<<(NPARAM + 255) / 256, 256, 0, cs>>>(m->params, m->m1, m->m2, m->grad, lr, beta1, beta2, eps, 1.f, 1.f,
+                                                m->sched);
+    k_pack<<<(3 * H * H + 255) / 256, 256, 0, cs>>>(m->params, m->Wb, m->WbT);
+    k_pack16<<<(PACK16_N + 255) / 256, 256, 0, cs>>>(m->params, m->Wh);
+    const cudaError_t e2 = cudaStreamEndCapture(cs, &g);
+    e = e2 != cudaSuccess ? e2 : cudaGetLastError();
+  }
+  if (e == cudaSuccess && st == RC_OK) e = cudaGraphInstantiate(&ge, g, 0);
+  for (int k = 0; e == cudaSuccess && st == RC_OK && k < steps; ++k) e = cudaGraphLaunch(ge, s);
+  unsigned derr = 0;
+  if (e == cudaSuccess && st == RC_OK) e = cudaMemcpyAsync(&derr, m->derr, sizeof(unsigned), cudaMemcpyDeviceToHost, s);
+  if (e == cudaSuccess && st == RC_OK) e = cudaStreamSynchronize(s);
+  if (ge) cudaGraphExecDestroy(ge);
+  if (g) cudaGraphDestroy(g);
+  cudaStreamDestroy(cs);
+  if (st) return st;
+  MLP_CU(e);
+  m->step += steps;
+  if (derr) {
+    m->err = "tensor-core wait gave up";
+    return (int)derr;
+  }
   return RC_OK;
 }
 

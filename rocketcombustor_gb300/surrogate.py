@@ -120,27 +120,25 @@ class MLP:
         self._check(load().rc_mlp_adam(self.handle, g.data_ptr(), lr, beta1, beta2, eps, ctypes.c_void_p(s)))
 
     def train(self, x, t, steps: int, batch: int = 8192, lr: float = 2e-3, lr_end: float = 1e-4, seed: int = 0,
-              log_every: int = 0):
-        """Adam on random batches (multiples of 128) with a cosine learning-rate
-        decay from lr to lr_end; returns the loss history (one per log point)."""
-        import math
-
+              log_every: int = 0, beta1: float = 0.9, beta2: float = 0.999, eps: float = 1e-8):
+        """Adam on random batches (multiples of 128, drawn on the device) with
+        a cosine learning-rate decay from lr to lr_end, all steps in one call
+        of rc_mlp_train (one CUDA graph launch per step); returns the loss
+        history (one (step, loss) per log point)."""
         import torch
+        if steps <= 0:
+            return []
+        x, t = x.contiguous(), t.contiguous()
         n = x.shape[0]
         batch = max(128, (min(batch, n) // 128) * 128)
-        gen = torch.Generator(device=x.device)
-        gen.manual_seed(seed)
-        hist = []
-        for it in range(steps):
-            idx = torch.randint(0, n, (batch,), generator=gen, device=x.device)
-            xb, tb = x[idx].contiguous(), t[idx].contiguous()
-            log = log_every and (it % log_every == 0 or it == steps - 1)
-            g, loss = self.gradient(xb, tb, sync_loss=bool(log))
-            a = lr_end + 0.5 * (lr - lr_end) * (1 + math.cos(math.pi * it / max(1, steps - 1)))
-            self.adam(g, a)
-            if log:
-                hist.append((it, loss))
-        return hist
+        loss = torch.empty(steps, dtype=torch.float32, device=x.device)
+        s = torch.cuda.current_stream(x.device).cuda_stream
+        self._check(load().rc_mlp_train(self.handle, x.data_ptr(), t.data_ptr(), n, steps, batch, lr, lr_end, beta1,
+                                        beta2, eps, seed, loss.data_ptr(), ctypes.c_void_p(s)))
+        if not log_every:
+            return []
+        h = loss.cpu().tolist()
+        return [(it, h[it]) for it in range(steps) if it % log_every == 0 or it == steps - 1]
 
     def close(self):
         if getattr(self, "handle", None):

@@ -90,3 +90,32 @@ def test_training_reduces_the_loss():
     t = torch.cat([torch.tanh(f), f * f, torch.sin(3 * f), 0 * f + 1], 1).contiguous()
     hist = m.train(x, t, steps=300, batch=2048, lr=3e-3, lr_end=3e-4, log_every=50)
     assert hist[-1][1] < 0.05 * hist[0][1], hist
+
+
+def test_training_is_reproducible_and_checks_its_arguments():
+    """rc_mlp_train twice from the same parameters and seed gives the same
+    parameters bit for bit (every gradient reduction has a fixed order, the
+    weight-gradient branch on its own stream included); a batch that is not a
+    multiple of 128 is refused."""
+    import ctypes
+
+    import torch
+    from rocketcombustor_gb300 import RcError, surrogate
+    from rocketcombustor_gb300 import load
+    x = torch.tensor(raw_samples(4096, 8), device="cuda")
+    t = torch.rand(4096, 4, device="cuda", generator=torch.Generator(device="cuda").manual_seed(2))
+    params = []
+    for _ in range(2):
+        m = surrogate.MLP(seed=5)
+        m.set_norm(MEAN, STD)
+        m.train(x, t, steps=40, batch=1024, lr=3e-3, lr_end=3e-4, seed=11)
+        params.append(m.get_params())
+        m.close()
+    assert np.array_equal(params[0], params[1])
+    m = surrogate.MLP(seed=5)
+    st = load().rc_mlp_train(m.handle, x.data_ptr(), t.data_ptr(), 4096, 10, 1000, 1e-3, 1e-4, 0.9, 0.999, 1e-8, 0,
+                             None, ctypes.c_void_p(0))
+    assert st != 0
+    with pytest.raises(RcError):
+        m._check(st)
+    m.close()
