@@ -913,8 +913,10 @@ __global__ void __launch_bounds__(FLOW32_THREADS, 1) k_lusgs_flow32(const Dev d,
 // about a quarter of a plain FP64 iteration's face flux: two warps per SM
 // (k_lusgs_flow32) fall behind the compact sweep on a large mesh and finish
 // long after its last pass, so there are enough update warps to keep each
-// sub-partition's FP64 unit busy.  Every wait is bounded (ERR_SYNC).
-constexpr int FLOWC32_NBUF = 4, FLOWC32_UPD = 6;
+// sub-partition's FP64 unit busy (on the 2,000,000-cell nozzle: 6 warps
+// 8.77 ms per mixed iteration, 8 warps 8.38, 10 warps 8.99, the registers
+// then capped at 136 a thread).  Every wait is bounded (ERR_SYNC).
+constexpr int FLOWC32_NBUF = 4, FLOWC32_UPD = 8;
 __host__ __device__ constexpr int flowc32_threads(int G) { return 32 * (2 * G + 3 + FLOWC32_UPD); }
 template <int NSP>
 struct PairPre32 {
@@ -1129,14 +1131,15 @@ __global__ void __launch_bounds__(flowc32_threads(G), 1) k_lusgs_flowc32(const D
       bar_arrive(4, T34);
     }
   } else {
-    // the Newton update warps (CW + 3 ..): update warp u takes the backward
-    // passes nf + u, nf + u + UPD, ... once finished, as many at a time as
-    // fill its 32 lanes with one cell each
+    // the Newton update warps (CW + 3 ..): update warp u takes the cells of
+    // the backward passes nf + u, nf + u + UPD, ... once finished, 32 at a
+    // time, one per lane: a batch runs on from pass to pass and may end inside
+    // one (off: the cells of pass k already taken)
     constexpr int UPD = FLOWC32_UPD;
     const int u = warp - CW - 3;
     int* cells = s_cells[u];
     unsigned err = 0;
-    for (int k = nf + u; k < n;) {
+    for (int k = nf + u, off = 0; k < n;) {
       for (unsigned spin = 0; s_done <= k && !s_bad; ++spin) {
         if (spin >= d.spin_limit) give_up();
         __nanosleep(256);
@@ -1150,6 +1153,10 @@ __global__ void __launch_bounds__(flowc32_threads(G), 1) k_lusgs_flowc32(const D
         const int pz = pass_of(kl);
         cnt = f.pcount[pz];
         t0 = f.pstart[pz];
+        if (lane == 0) {
+          cnt -= off;
+          t0 += off;
+        }
       }
       int incl = cnt;
 #pragma unroll
@@ -1157,24 +1164,24 @@ __global__ void __launch_bounds__(flowc32_threads(G), 1) k_lusgs_flowc32(const D
         const int x = __shfl_up_sync(0xffffffffu, incl, o);
         if (lane >= o) incl += x;
       }
-      const bool take = kl < avail && incl <= 32;
-      const int ntake = __popc(__ballot_sync(0xffffffffu, take));
-      if (ntake == 0) {
-        // pass k alone holds more than 32 cells: 32 of them at a time
-        const int pz = pass_of(k), ts = f.pstart[pz], nc = f.pcount[pz];
-        for (int c0 = 0; c0 < nc; c0 += 32)
-          if (c0 + lane < nc) update_cell<NSP>(d, th64, d.swi[1][ts + c0 + lane], err);
-        __syncwarp();
-        k += UPD;
-        continue;
-      }
-      if (take)
-        for (int c = 0; c < cnt; ++c) cells[incl - cnt + c] = t0 + c;
-      const int ncell = __shfl_sync(0xffffffffu, incl, ntake - 1);
+      const int excl = incl - cnt;
+      for (int c = 0; c < cnt && excl + c < 32; ++c) cells[excl + c] = t0 + c;
+      const int total = __shfl_sync(0xffffffffu, incl, 31);
+      const int ncell = total < 32 ? total : 32;
       __syncwarp();
       if (lane < ncell) update_cell<NSP>(d, th64, d.swi[1][cells[lane]], err);
       __syncwarp();
-      k += UPD * ntake;
+      if (total <= 32) {
+        // every finished pass of this warp taken whole
+        k += UPD * __popc(__ballot_sync(0xffffffffu, kl < avail));
+        off = 0;
+      } else {
+        // the batch ends inside candidate j (the first whose cells pass 32)
+        const int j = __ffs(__ballot_sync(0xffffffffu, incl > 32)) - 1;
+        const int ex = __shfl_sync(0xffffffffu, excl, j);
+        off = (j == 0 ? off : 0) + (32 - ex);
+        k += UPD * j;
+      }
     }
     flag(d, err);
   }
