@@ -352,16 +352,12 @@ def main():
             s.close()
             results[form] = r
         head = results[forms_req[0]]
-        t_max = head["t_local"]
-        if dist:
-            tt = torch.tensor([t_max], dtype=torch.float64)
-            dist.all_reduce(tt, op=dist.ReduceOp.MAX)
-            t_max = float(tt[0])
+        t_max = max_over_ranks(head["t_local"], dist)
         if rank != 0:
             dist.barrier()
             dist.destroy_process_group()
             return 0
-        value = world * NE * args.steps / t_max
+        value = job_throughput(world, NE, args.steps, t_max)
         peak, peak_kind = read_peaks()
         ab = algo_bytes_per_cell(V, NF / NE, cfg.viscous, cfg.combustion)
         sub_ms = head["subroutine_ms"]
@@ -441,6 +437,27 @@ def gpu_id(torch):
         return str(dev)
 
 
+def rank_barrier(dist):
+    """All ranks meet here (no-op on one rank)."""
+    if dist:
+        dist.barrier()
+
+
+def max_over_ranks(t_local: float, dist) -> float:
+    """The slowest rank's timed region, on every rank (gloo all-reduce MAX)."""
+    if not dist:
+        return t_local
+    import torch
+    tt = torch.tensor([t_local], dtype=torch.float64)
+    dist.all_reduce(tt, op=dist.ReduceOp.MAX)
+    return float(tt[0])
+
+
+def job_throughput(world: int, units_per_rank: int, steps: int, t_max: float) -> float:
+    """Whole-job units per second: every rank processed units_per_rank per step."""
+    return world * units_per_rank * steps / t_max
+
+
 def time_form(s, args, stream, flush, dist, torch, rc):
     """W warm-up iterations, then K device-timed iterations (L2 flushed between)."""
     with torch.cuda.stream(stream):
@@ -448,9 +465,8 @@ def time_form(s, args, stream, flush, dist, torch, rc):
             s.lu_sgs_stage(it + 1)
         s.sync()
         ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
-        if dist:
-            dist.barrier()
         torch.cuda.synchronize()
+        rank_barrier(dist)
         l0 = s.stats()["kernel_launches"]
         with ClockSampler(gpu_id(torch)) as clk:
             for it in range(args.steps):
@@ -460,6 +476,7 @@ def time_form(s, args, stream, flush, dist, torch, rc):
                 ev[it][1].record(stream)
             s.sync()
             torch.cuda.synchronize()
+        rank_barrier(dist)
         launches = s.stats()["kernel_launches"] - l0
         ms = [a.elapsed_time(b) for a, b in ev]
     return {"t_local": sum(ms) / 1e3, "launches": int(launches)}, clk.summary()
