@@ -676,20 +676,35 @@ __global__ void __launch_bounds__(32) k_bdf2_sweep(const Dev d, const ThermoDev<
 // 7 x 7 solves and up to five refinement passes, about 12 us of dependent
 // FP64) and uneven: with one launch per level every level lasts as long as
 // its slowest cell, here a slow cell holds up only the passes that read it.
-// Warps 0 and 1 take four cells of each pass each and load what the sweep
-// does not change (the neighbours' gas state, the cell's factorisation)
-// before the pass is handed over; warp 2 looks at the flags of the next pass,
-// hands it over (barrier 3) once the current one is done (barrier 4) and its
-// flags are set, and publishes the finished pass (flag = this launch's epoch),
-// before any blocking wait.  s_go[k % 2] = 0 after a bounded wait gave up
-// (ERR_SYNC): the compute warps then skip the pass.  The last block to finish
-// advances the epoch counter; the primitive update follows as its own launch.
-constexpr int BFLOW_THREADS = 96;
+// Warps 0 and 1 take four cells of each pass each.  Warps 3 and 4 stage one
+// pass ahead what the sweep does not change (the slot data, the cell's
+// factorised rows, its index and, forward, its right-hand side) in a double
+// buffer of shared memory, for warp 0 and warp 1 respectively, and arrive on
+// barrier 5.  Warp 2 looks at the flags of the next pass; once the current
+// pass is done (barrier 4) and the next one is staged (barrier 5) it hands
+// the next one over (barrier 3, which the staging warps also wait on before
+// they refill the other buffer), and it publishes the finished pass (flag =
+// this launch's epoch) before any blocking wait.  s_go[k % 2] = 0 after a
+// bounded wait gave up (ERR_SYNC): the compute warps then skip the pass.  The
+// last block to finish advances the epoch counter; the primitive update
+// follows as its own launch.
+template <int NSP>
+struct BStage {
+  BSlot<NSP> sp;
+  BRow<NSP> rw;
+  double hown;
+  int i, valid;
+};
+constexpr int BFLOW_THREADS = 160, BFLOW_NB = 96;  // all five warps; a role pair and the coordinator
+template <int NSP>
+constexpr int bflow_smem() { return (int)(2 * 2 * 32 * sizeof(BStage<NSP>)); }
 template <int NSP>
 __global__ void __launch_bounds__(BFLOW_THREADS, 1) k_bdf2_flow(const Dev d, const ThermoDev<NSP> th, const FlowDev f) {
   using namespace bdf2;
   constexpr int V = 3 + NSP;
   static_assert(V <= 7, "one lane per row and the flags in slot 7");
+  extern __shared__ __align__(16) uint8_t bflow_smem_raw[];
+  BStage<NSP>* s_st = reinterpret_cast<BStage<NSP>*>(bflow_smem_raw);  // [buffer][warp][lane]
   __shared__ double wsm[2][4 * V * 4];
   __shared__ unsigned s_epoch;
   __shared__ volatile int s_bad, s_go[2];
@@ -705,6 +720,7 @@ __global__ void __launch_bounds__(BFLOW_THREADS, 1) k_bdf2_flow(const Dev d, con
   const int f0 = f.boff[0][b], b0 = f.boff[1][b];
   const int nf = f.boff[0][b + 1] - f0, n = nf + (f.boff[1][b + 1] - b0);
   auto pass_of = [&](int k) { return k < nf ? f.blist[0][f0 + k] : f.blist[1][b0 + k - nf]; };
+  const int cell = lane >> 3, r = lane & 7, q = r & 3;
   if (warp == 2) {
     auto poll = [&](int k) {
       if (s_bad) return;
@@ -721,7 +737,9 @@ __global__ void __launch_bounds__(BFLOW_THREADS, 1) k_bdf2_flow(const Dev d, con
       for (int u = lane; u < nd; u += 32) ok = ok && ld_acquire(f.pflag + f.deps[d0 + u]) >= epoch;
       return __all_sync(FULL, ok) != 0;
     };
+    // pass k is staged (barrier 5), then handed over (barrier 3)
     auto hand_over = [&](int k) {
+      bar_named(5, BFLOW_NB);
       if (lane == 0) s_go[k & 1] = s_bad ? 0 : 1;
       __syncwarp();
       __threadfence_block();
@@ -734,7 +752,7 @@ __global__ void __launch_bounds__(BFLOW_THREADS, 1) k_bdf2_flow(const Dev d, con
     for (int k = 0; k < n; ++k) {
       const bool more = k + 1 < n;
       const bool go = more && ready(k + 1);
-      bar_named(4, BFLOW_THREADS);
+      bar_named(4, BFLOW_NB);
       if (go) hand_over(k + 1);
       if (lane == 0 && !s_bad) st_release(f.pflag + pass_of(k), epoch);
       if (more && !go) {
@@ -742,30 +760,50 @@ __global__ void __launch_bounds__(BFLOW_THREADS, 1) k_bdf2_flow(const Dev d, con
         hand_over(k + 1);
       }
     }
-  } else {
-    const int cell = lane >> 3, r = lane & 7, q = r & 3;
-    for (int k = 0; k < n; ++k) {
+  } else if (warp >= 3) {
+    const int w = warp - 3;  // stages for compute warp w
+    auto stage = [&](int k) {
       const bool fwd = k < nf;
       const int pz = pass_of(k), t0 = f.pstart[pz], t1 = t0 + f.pcount[pz];
-      const int t = t0 + 4 * warp + cell;
+      const int t = t0 + 4 * w + cell;
       const bool valid = t < t1;
       const int i = valid ? d.swi[fwd ? 0 : 1][t] : 0;
-      // what the sweep does not change: before the hand-over
-      const BSlot<NSP> sp = fwd ? bslot_load<NSP, true>(d, t, valid, q) : bslot_load<NSP, false>(d, t, valid, q);
-      const BRow<NSP> rw = brow_load<NSP>(d, i, valid, r);
-      // the cell's own increment: the set-up's right-hand side (forward), or
-      // what this block's forward pass of the cell wrote (backward; read after
-      // the hand-over, as the other warp may still be finishing the forward
-      // pass that holds the cell)
-      double hown = fwd && valid && r < V ? __ldcg(d.hWA + r * d.NE + i) : 0.0;
+      BStage<NSP>& e = s_st[((k & 1) * 2 + w) * 32 + lane];
+      e.sp = fwd ? bslot_load<NSP, true>(d, t, valid, q) : bslot_load<NSP, false>(d, t, valid, q);
+      e.rw = brow_load<NSP>(d, i, valid, r);
+      // forward: the set-up's right-hand side, which only this cell's own
+      // forward step changes
+      e.hown = fwd && valid && r < V ? __ldcg(d.hWA + r * d.NE + i) : 0.0;
+      e.i = i;
+      e.valid = valid ? 1 : 0;
+      __syncwarp();
+      __threadfence_block();
+      bar_arrive(5, BFLOW_NB);
+    };
+    if (n > 0) stage(0);
+    for (int k = 0; k < n; ++k) {
+      bar_named(3, BFLOW_THREADS);  // pass k handed over: the other buffer is free
+      if (k + 1 < n) stage(k + 1);
+    }
+  } else {
+    for (int k = 0; k < n; ++k) {
+      const bool fwd = k < nf;
       bar_named(3, BFLOW_THREADS);
-      if (!fwd && valid && r < V) hown = __ldcg(d.hWA + r * d.NE + i);
+      const BStage<NSP>& e = s_st[((k & 1) * 2 + warp) * 32 + lane];
+      const BSlot<NSP> sp = e.sp;
+      const BRow<NSP> rw = e.rw;
+      const int i = e.i;
+      const bool valid = e.valid != 0;
+      // backward: the cell's own increment, as this block's forward pass of
+      // the cell wrote it (read after the hand-over: the other warp may have
+      // been finishing the forward pass that holds the same cell)
+      const double hown = fwd ? e.hown : valid && r < V ? __ldcg(d.hWA + r * d.NE + i) : 0.0;
       if (s_go[k & 1]) {
         if (fwd) bdf2_cell_step<NSP, true, 4, true>(d, th, sp, rw, hown, i, valid, wsm[warp]);
         else bdf2_cell_step<NSP, false, 4, true>(d, th, sp, rw, hown, i, valid, wsm[warp]);
       }
       __syncwarp();
-      bar_arrive(4, BFLOW_THREADS);
+      bar_arrive(4, BFLOW_NB);
     }
   }
   __syncthreads();
@@ -843,6 +881,7 @@ cudaError_t bdf2_flow(const Dev& d, const void* th, const FlowDev& f, int grid, 
   cudaLaunchConfig_t cfg = {};
   cfg.gridDim = dim3((unsigned)grid);
   cfg.blockDim = dim3(BFLOW_THREADS);
+  cfg.dynamicSmemBytes = (size_t)bflow_smem<NSP>();
   cfg.stream = s;
   cudaLaunchAttribute attr[1];
   attr[0].id = cudaLaunchAttributeCooperative;
@@ -854,7 +893,10 @@ cudaError_t bdf2_flow(const Dev& d, const void* th, const FlowDev& f, int grid, 
 template <int NSP>
 int bdf2_flow_occupancy() {
   int nb = 0;
-  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_bdf2_flow<NSP>, BFLOW_THREADS, 0);
+  if (cudaFuncSetAttribute(k_bdf2_flow<NSP>, cudaFuncAttributeMaxDynamicSharedMemorySize, bflow_smem<NSP>()) !=
+      cudaSuccess)
+    return 0;
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_bdf2_flow<NSP>, BFLOW_THREADS, bflow_smem<NSP>());
   return nb;
 }
 template <int NSP>
