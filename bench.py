@@ -291,6 +291,9 @@ def main():
     ap.add_argument("--mlp-infer", type=int, default=0,
                     help="instead of the throughput line: the surrogate network's inference kernel alone on this "
                          "many synthetic samples (10 timed calls), with its error against the FP64 reference")
+    ap.add_argument("--mlp-train", type=int, default=0,
+                    help="instead of the throughput line: this many Adam steps of the surrogate network "
+                         "(rc_mlp_train, batches of 8,192 from 1,048,576 synthetic pairs), wall clock")
     ap.add_argument("--dc-window", type=int, default=20,
                     help="norm reads without a 1%% improvement before the mixed form switches to defect correction")
     args = ap.parse_args()
@@ -320,6 +323,8 @@ def main():
         return converge(args, rc, torch)
     if args.mlp_infer:
         return mlp_infer(args, torch)
+    if args.mlp_train:
+        return mlp_train(args, torch)
     torch.cuda.set_device(local)
     stream = torch.cuda.Stream(device=local)
     flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=f"cuda:{local}")
@@ -876,6 +881,36 @@ def mlp_infer(args, torch):
                       "tflops": flops * n / t / 1e12, "peak_bf16_tflops": read_peaks_tensor(),
                       "max_abs_err_vs_fp64": float(np.abs(y - yr).max()), "output_scale": float(np.abs(yr).max())}),
           flush=True)
+    net.close()
+    return 0
+
+
+def mlp_train(args, torch):
+    """`--mlp-train` Adam steps of the surrogate network (random weights, seed
+    7) on 1,048,576 synthetic pairs (the states of mlp_infer, smooth targets of
+    T), through rc_mlp_train (one CUDA graph per step): wall clock around the
+    call after a 20-step warm-up, TFLOP/s at 3 x the forward FLOP per sample."""
+    from rocketcombustor_gb300 import surrogate
+    rng = np.random.default_rng(9)
+    n = 1 << 20
+    x = np.stack([rng.uniform(300, 3800, n), 10 ** rng.uniform(4.7, 7, n), rng.uniform(0, .05, n),
+                  rng.uniform(0, .05, n), rng.uniform(.85, .95, n), rng.uniform(0, .02, n),
+                  10 ** rng.uniform(-9, -5, n)], 1).astype(np.float32)
+    f = (x[:, 0:1] - 2000) / 1000 * 0.5
+    t = np.concatenate([np.tanh(f), f * f, np.sin(3 * f), 0 * f + 1], 1).astype(np.float32)
+    xd, td = torch.tensor(x, device="cuda"), torch.tensor(t, device="cuda")
+    net = surrogate.MLP(seed=7)
+    net.fit_norm(xd)
+    net.train(xd, td, steps=20, batch=8192)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    hist = net.train(xd, td, steps=args.mlp_train, batch=8192, lr=2e-3, lr_end=3e-5, log_every=args.mlp_train)
+    torch.cuda.synchronize()
+    dt = time.perf_counter() - t0
+    flops = 3 * 2 * (7 * 128 + 3 * 128 * 128 + 128 * 4) * 8192
+    print(json.dumps({"mode": "mlp_train", "steps": args.mlp_train, "batch": 8192, "seconds": dt,
+                      "ms_per_step": 1e3 * dt / args.mlp_train, "tflops": flops * args.mlp_train / dt / 1e12,
+                      "loss_first_last": [hist[0][1], hist[-1][1]]}), flush=True)
     net.close()
     return 0
 
