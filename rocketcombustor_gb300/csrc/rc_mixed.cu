@@ -913,10 +913,13 @@ __global__ void __launch_bounds__(FLOW32_THREADS, 1) k_lusgs_flow32(const Dev d,
 // about a quarter of a plain FP64 iteration's face flux: two warps per SM
 // (k_lusgs_flow32) fall behind the compact sweep on a large mesh and finish
 // long after its last pass, so there are enough update warps to keep each
-// sub-partition's FP64 unit busy (on the 2,000,000-cell nozzle: 6 warps
-// 8.77 ms per mixed iteration, 8 warps 8.38, 10 warps 8.99, the registers
-// then capped at 136 a thread).  Every wait is bounded (ERR_SYNC).
-constexpr int FLOWC32_NBUF = 4, FLOWC32_UPD = 8;
+// sub-partition's FP64 unit busy.  Seven keep the block at 12 warps, three
+// per SM sub-partition, so a thread may hold the 149 registers the kernel
+// uses; a fourth warp on a sub-partition caps it at 128 (on the 2,000,000-cell
+// nozzle: 6 update warps 8.77 ms per mixed iteration, 7 warps 7.95, 8 warps
+// 8.38 with 168 bytes of spills, 10 warps 8.99).  Every wait is bounded
+// (ERR_SYNC).
+constexpr int FLOWC32_NBUF = 4, FLOWC32_UPD = 7;
 __host__ __device__ constexpr int flowc32_threads(int G) { return 32 * (2 * G + 3 + FLOWC32_UPD); }
 template <int NSP>
 struct PairPre32 {
