@@ -589,20 +589,32 @@ __device__ __forceinline__ long long berr_bits(double y, double wk, int r) {
 // through w (this warp's [cell][row][slot] scratch), then the cell's system
 // (rw: row r of its factorisation) solved with one lane per row and refined
 // as dgerfs does; hown is the cell's own increment (row r), i its index.
-template <int NSP, bool FWD, int CPW, bool L2>
+// PART 0: the whole step on this warp.  PART 1 and 2: two warps (warp 0 and
+// warp 1 of the block) on the same cells, PART 1 forming rows 1-3 of every
+// slot's terms, PART 2 rows 4..; they meet at named barrier 6 (64 threads),
+// after which PART 1 solves and PART 2 returns.  The terms, their places in w
+// and the sums are the same in every PART.
+template <int NSP, bool FWD, int CPW, bool L2, int PART = 0>
 __device__ __forceinline__ void bdf2_cell_step(const Dev& d, const ThermoDev<NSP>& th, const BSlot<NSP>& sp,
                                                const BRow<NSP>& rw, double hown, int i, bool valid, double* wsm) {
   using namespace bdf2;
   constexpr int V = 3 + NSP;
   const int lane = threadIdx.x & 31, cell = lane >> 3, r = lane & 7, base = cell * 8;
   const int q = r & 3;
-  const bool lo = r < 4;  // lanes 0-3 keep flux rows 1-3 of their slot, lanes 4-7 rows 4.. (energy, species)
+  // PART 0: lanes 0-3 keep flux rows 1-3 of their slot, lanes 4-7 rows 4..
+  // (energy, species); PART 1 / 2: all lanes the one half, lanes 0-3 store it
+  const bool lo = PART == 0 ? r < 4 : PART == 1;
   const int NE = d.NE;
   double c[V];
   bslot_terms<NSP, L2>(d, th, sp, lo, c);
   double* w = wsm + (cell < CPW ? cell : 0) * V * 4;  // [row][slot]
-  if (cell < CPW) bslot_put<NSP>(w, lo, q, c);
+  if (cell < CPW && (PART == 0 || r < 4)) bslot_put<NSP>(w, lo, q, c);
   __syncwarp();
+  if (PART == 2) {
+    bar_arrive(6, 64);
+    return;
+  }
+  if (PART == 1) bar_named(6, 64);
   double dflux = 0.0;
   if (r < V) {
 #pragma unroll
@@ -695,6 +707,8 @@ struct BStage {
   double hown;
   int i, valid;
 };
+// A pass of at most four cells runs on both compute warps split by rows
+// (bdf2_cell_step PART 1 and 2), otherwise four cells on each (PART 0).
 constexpr int BFLOW_THREADS = 160, BFLOW_NB = 96;  // all five warps; a role pair and the coordinator
 template <int NSP>
 constexpr int bflow_smem() { return (int)(2 * 2 * 32 * sizeof(BStage<NSP>)); }
@@ -707,7 +721,7 @@ __global__ void __launch_bounds__(BFLOW_THREADS, 1) k_bdf2_flow(const Dev d, con
   BStage<NSP>* s_st = reinterpret_cast<BStage<NSP>*>(bflow_smem_raw);  // [buffer][warp][lane]
   __shared__ double wsm[2][4 * V * 4];
   __shared__ unsigned s_epoch;
-  __shared__ volatile int s_bad, s_go[2];
+  __shared__ volatile int s_bad, s_go[2], s_split[2];
   if (threadIdx.x == 0) {
     s_epoch = ld_acquire(f.ctr) + 1u;
     s_bad = 0;
@@ -765,8 +779,10 @@ __global__ void __launch_bounds__(BFLOW_THREADS, 1) k_bdf2_flow(const Dev d, con
     auto stage = [&](int k) {
       const bool fwd = k < nf;
       const int pz = pass_of(k), t0 = f.pstart[pz], t1 = t0 + f.pcount[pz];
-      const int t = t0 + 4 * w + cell;
+      const bool split = t1 - t0 <= 4;  // both compute warps on cells t0 .. t0 + 3
+      const int t = t0 + (split ? 0 : 4 * w) + cell;
       const bool valid = t < t1;
+      if (w == 0 && lane == 0) s_split[k & 1] = split ? 1 : 0;
       const int i = valid ? d.swi[fwd ? 0 : 1][t] : 0;
       BStage<NSP>& e = s_st[((k & 1) * 2 + w) * 32 + lane];
       e.sp = fwd ? bslot_load<NSP, true>(d, t, valid, q) : bslot_load<NSP, false>(d, t, valid, q);
@@ -799,8 +815,18 @@ __global__ void __launch_bounds__(BFLOW_THREADS, 1) k_bdf2_flow(const Dev d, con
       // been finishing the forward pass that holds the same cell)
       const double hown = fwd ? e.hown : valid && r < V ? __ldcg(d.hWA + r * d.NE + i) : 0.0;
       if (s_go[k & 1]) {
-        if (fwd) bdf2_cell_step<NSP, true, 4, true>(d, th, sp, rw, hown, i, valid, wsm[warp]);
-        else bdf2_cell_step<NSP, false, 4, true>(d, th, sp, rw, hown, i, valid, wsm[warp]);
+        if (s_split[k & 1]) {
+          if (warp == 0) {
+            if (fwd) bdf2_cell_step<NSP, true, 4, true, 1>(d, th, sp, rw, hown, i, valid, wsm[0]);
+            else bdf2_cell_step<NSP, false, 4, true, 1>(d, th, sp, rw, hown, i, valid, wsm[0]);
+          } else {
+            if (fwd) bdf2_cell_step<NSP, true, 4, true, 2>(d, th, sp, rw, hown, i, valid, wsm[0]);
+            else bdf2_cell_step<NSP, false, 4, true, 2>(d, th, sp, rw, hown, i, valid, wsm[0]);
+          }
+        } else {
+          if (fwd) bdf2_cell_step<NSP, true, 4, true>(d, th, sp, rw, hown, i, valid, wsm[warp]);
+          else bdf2_cell_step<NSP, false, 4, true>(d, th, sp, rw, hown, i, valid, wsm[warp]);
+        }
       }
       __syncwarp();
       bar_arrive(4, BFLOW_NB);
